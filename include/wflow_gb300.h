@@ -1,0 +1,297 @@
+/*
+ * wflow_gb300.h -- C ABI of the GB300 (sm_103a) SBM + kinematic-wave step library.
+ *
+ * The library replaces the per-timestep hot path of Wflow.jl's `sbm` model:
+ *   update_model!(model)          Wflow/src/sbm_model.jl:60-92
+ *   compute_mass_balance!(model)  Wflow/src/mass_balance.jl:541-545
+ * which Wflow calls through the `update_func` seam of
+ *   run_timestep!(model; update_func = update_model!)  Wflow/src/Wflow.jl:311-322
+ * A Julia caller binds these entry points with `ccall`; every argument
+ * is a plain pointer, size or POD struct. All device memory, the CUDA stream and the
+ * captured CUDA graph of a step belong to the handle. Input arrays are copied at call time
+ * and never retained.
+ *
+ * Units are SI inside the path (m, s, K, m s-1, m3 s-1), as after Wflow's to_SI
+ * (Wflow/src/units.jl:271). Cell order in every array argument is the reference's land
+ * order (`domain.land.network.indices`), river order is `domain.river.network.indices`.
+ *
+ * Errors: every entry point returns WfStatus (0 = ok, negative = error class) and
+ * wf_last_error() gives a message; device-side problems (a bounded spin-wait that ran out,
+ * non-finite results) are raised through a device status word read after each step.
+ * Nothing traps or aborts.
+ */
+#ifndef WFLOW_GB300_H
+#define WFLOW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WF_ABI_VERSION 1
+#define WF_MAX_LAYERS 8
+
+typedef enum WfStatus {
+    WF_OK = 0,
+    WF_ERR_INVALID = -1,     /* bad argument or inconsistent sizes */
+    WF_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+    WF_ERR_CYCLE = -3,       /* the drainage graph has a cycle (routing/utils.jl:26-31) */
+    WF_ERR_NAN = -4,         /* non-finite input where the reference requires a value */
+    WF_ERR_SPIN = -5,        /* a routing wavefront wait ran out of its spin budget */
+    WF_ERR_UNSUPPORTED = -6, /* option outside the supported path */
+    WF_ERR_NOMEM = -7,       /* device allocation failed */
+    WF_ERR_STATE = -8        /* state blob of the wrong size or version */
+} WfStatus;
+
+/* Arithmetic form of the step. */
+typedef enum WfForm {
+    WF_FORM_FP64 = 0,  /* plain FP64 drop-in: every operation in FP64 */
+    WF_FORM_SPLIT = 1  /* FP32 bulk fluxes; FP64 Newton solves and storage/balance state */
+} WfForm;
+
+/* Vertical saturated hydraulic conductivity profile (Wflow/src/soil/soil.jl:213-244). */
+typedef enum WfKvProfile { WF_KV_EXPONENTIAL = 0, WF_KV_EXPONENTIAL_CONSTANT = 1 } WfKvProfile;
+
+/* Model settings, mirroring Wflow's [model] and [time] TOML sections
+ * (Wflow/src/config_structure.jl:62-100). */
+typedef struct WfConfig {
+    double dt;                                        /* time.timestepsecs [s] */
+    int32_t n_soil_layer_thickness;                   /* length of soil_layer__thickness */
+    int32_t snow;                                     /* snow__flag */
+    double soil_layer_thickness[WF_MAX_LAYERS - 1];   /* soil_layer__thickness [m] */
+    int32_t soil_infiltration_reduction;              /* soil_infiltration_reduction__flag */
+    int32_t water_mass_balance;                       /* water_mass_balance__flag */
+    int32_t adaptive_timestep;                        /* kinematic_wave__adaptive_time_step_flag */
+    int32_t kv_profile;                               /* WfKvProfile */
+    double land_dt_fixed;                             /* land_kinematic_wave__time_step [s] */
+    double river_dt_fixed;                            /* river_kinematic_wave__time_step [s] */
+    double subsurface_dt_fixed;                       /* subsurface_kinematic_wave__time_step [s] */
+    double subsurface_alpha;                          /* subsurface_kinematic_wave__alpha_coefficient */
+    int32_t form;                                     /* WfForm */
+    int32_t n_members;                                /* ensemble members sharing the domain (>= 1) */
+    int32_t per_member_soil;                          /* kv_0 and f given per member (n_land*n_members) */
+    int32_t reserved[7];
+} WfConfig;
+
+/* Drainage network and shared geometry (Wflow/src/domain.jl:1-45, network.jl:47-258).
+ * The graphs are given by one downstream index per node (Graphs.outneighbors of the D8
+ * flow graph, routing/utils.jl:6-33): -1 marks a pit. */
+typedef struct WfDomain {
+    int64_t n_land;
+    const int32_t* land_downstream;         /* [n_land] */
+    const double* area;                     /* [m2] */
+    const double* flow_width;               /* [m] */
+    const double* flow_length;              /* [m] */
+    const double* surface_flow_width;       /* [m] */
+    const double* slope;                    /* [-] (already clamped >= 1e-5) */
+    const double* flow_fraction_to_river;   /* [-] */
+    const double* river_fraction;           /* [-] */
+    const double* water_fraction;           /* [-] */
+    const double* elevation;                /* land_surface__elevation [m] */
+    const double* land_manning_n;           /* land_surface_water_flow__manning_n_parameter */
+    int64_t n_river;
+    const int32_t* river_land_index;        /* [n_river] land index of each river cell */
+    const int32_t* river_downstream;        /* [n_river], -1 for a pit */
+    const double* river_width;              /* river__width [m] */
+    const double* river_length;             /* river__length [m] */
+    const double* river_slope;              /* river__slope [-] (already clamped >= 1e-5) */
+    const double* river_manning_n;          /* river_water_flow__manning_n_parameter */
+    const double* river_bankfull_depth;     /* river_bank_water__depth [m] */
+    const double* river_external_inflow;    /* river_water__external_inflow_volume_flow_rate [m3 s-1] */
+} WfDomain;
+
+/* Static SBM parameters as Wflow reads them from the static maps, in SI units.
+ * Layered arrays are cell-major [i * n_layers + k] like Vector{SVector{N}} in the reference.
+ * Derived parameters (layer thickness, theta_fc, root fraction, soil water capacity,
+ * infiltration capacity of the soil, kh_0, specific yield, Manning alpha) are computed by
+ * the library exactly as the reference's initialisation does. */
+typedef struct WfParams {
+    /* vegetation (vegetation/parameters.jl:1-91, canopy.jl) */
+    const double* canopy_gap_fraction;
+    const double* maximum_canopy_storage;              /* [m] */
+    const double* crop_coefficient;
+    const double* rooting_depth;                       /* [m] */
+    const double* evaporation_to_precipitation_ratio;  /* Gash only (dt >= 23 h) */
+    /* snow (snow/snow.jl:175-224) */
+    const double* degree_day_factor;                   /* [m K-1 s-1] */
+    const double* temperature_threshold_snowfall;      /* [K] */
+    const double* temperature_interval_snowfall;       /* [K] */
+    const double* temperature_threshold_melt;          /* [K] */
+    const double* water_holding_capacity;              /* [-] */
+    /* soil (soil/soil.jl:319-617) */
+    const double* theta_s;
+    const double* theta_r;
+    const double* kv_0;                                /* [m s-1]; n_land*n_members if per_member_soil */
+    const double* f;                                   /* scale parameter [m-1]; idem */
+    const double* soil_thickness;                      /* [m] */
+    const double* air_entry_pressure;                  /* [m] */
+    const double* h1;
+    const double* h2;
+    const double* h3_high;
+    const double* h3_low;
+    const double* h4;                                  /* Feddes heads [m] */
+    const double* alpha_h1;
+    const double* infiltration_capacity_compacted_soil; /* [m s-1] */
+    const double* compacted_soil_area_fraction;
+    const double* wet_root_distribution_parameter;     /* [m-1] */
+    const double* cap_hmax;                            /* [m] */
+    const double* cap_n;
+    const double* maximum_leakage;                     /* [m s-1] */
+    const double* w_soil;
+    const double* cf_soil;
+    const double* z_exp;                               /* [m], exponential_constant profile only */
+    const double* brooks_corey_exponent;               /* [n_land * n_layers] */
+    const double* kv_factor;                           /* [n_land * n_layers] */
+    /* lateral subsurface (routing/subsurface/lateral_subsurface_flow.jl:87-132) */
+    const double* horizontal_to_vertical_ratio;        /* KsatHorFrac [-] */
+} WfParams;
+
+/* Per-cell and per-river-cell variables exposed through get/set (BMI get_value/set_value,
+ * Wflow/src/bmi.jl:208-248). Layered fields take a layer index. */
+typedef enum WfField {
+    /* land, states */
+    WF_F_CANOPY_STORAGE = 0,
+    WF_F_SNOW_STORAGE,
+    WF_F_SNOW_WATER,
+    WF_F_SOIL_SURFACE_TEMPERATURE,
+    WF_F_SATURATED_WATER_DEPTH,
+    WF_F_UNSATURATED_LAYER_DEPTH,   /* layered */
+    WF_F_SSF_Q,
+    WF_F_LAND_Q,
+    WF_F_LAND_H,
+    /* land, diagnostics of the last step */
+    WF_F_WATER_TABLE_DEPTH,
+    WF_F_UNSATURATED_STORE_DEPTH,
+    WF_F_TOTAL_SOIL_WATER_STORAGE,
+    WF_F_RECHARGE,
+    WF_F_NET_RUNOFF,
+    WF_F_RUNOFF,
+    WF_F_ACTUAL_EVAPOTRANSPIRATION,
+    WF_F_ACTUAL_LEAKAGE,
+    WF_F_TRANSPIRATION,
+    WF_F_SOIL_EVAPORATION,
+    WF_F_ACTUAL_INFILTRATION,
+    WF_F_EXFILTRATION_SATURATED_WATER,
+    WF_F_INTERCEPTION_RATE,
+    WF_F_SNOW_WATER_EQUIVALENT,
+    WF_F_NET_RUNOFF_RIVER,
+    WF_F_SSF_Q_AVERAGE,
+    WF_F_SSF_WATER_TABLE_DEPTH,
+    WF_F_SSF_STORAGE,
+    WF_F_SSF_TO_RIVER_AVERAGE,
+    WF_F_LAND_Q_AVERAGE,
+    WF_F_LAND_STORAGE,
+    WF_F_LAND_TO_RIVER_AVERAGE,
+    WF_F_LAND_INWATER,
+    WF_F_TOTAL_STORAGE,
+    WF_F_BALANCE_LAND_ERROR,
+    WF_F_BALANCE_LAND_RELATIVE_ERROR,
+    WF_F_BALANCE_OVERLAND_ERROR,
+    WF_F_BALANCE_OVERLAND_RELATIVE_ERROR,
+    WF_F_BALANCE_SUBSURFACE_ERROR,
+    WF_F_BALANCE_SUBSURFACE_RELATIVE_ERROR,
+    WF_F_VOLUMETRIC_WATER_CONTENT,  /* layered */
+    WF_F_LAND_END_,
+    /* river */
+    WF_F_RIVER_Q = 100,
+    WF_F_RIVER_H,
+    WF_F_RIVER_STORAGE,
+    WF_F_RIVER_Q_AVERAGE,
+    WF_F_RIVER_QIN_AVERAGE,
+    WF_F_RIVER_INWATER,
+    WF_F_BALANCE_RIVER_ERROR,
+    WF_F_BALANCE_RIVER_RELATIVE_ERROR,
+    WF_F_RIVER_END_
+} WfField;
+
+typedef struct WfHandle WfHandle;
+
+/* Per-handle counters since creation (reset with wf_reset_metrics). */
+typedef struct WfMetrics {
+    int64_t steps;                /* model steps taken */
+    int64_t cell_steps;           /* land cells x members x steps */
+    int64_t substeps_land;        /* overland sub-steps taken (sum over steps) */
+    int64_t substeps_river;
+    int64_t substeps_subsurface;
+    int64_t kernel_launches;      /* kernels launched by steps (graph nodes count once each) */
+    double step_ms_total;         /* CUDA-event time of all steps */
+    double max_abs_balance_error; /* of the last step with water_mass_balance, over all domains */
+    int32_t device_status;        /* last device status word (0 = ok) */
+    int32_t n_chains_land;        /* routing chains of the land graph */
+    int32_t n_chains_river;
+    int32_t max_chain_land;       /* longest chain (= graph height + 1) */
+    int32_t max_chain_river;
+    int32_t padding_slots_land;   /* padded slots of the land layout */
+} WfMetrics;
+
+/* Tuning knobs (filled by the autotuner; zero = library default). */
+typedef struct WfTuning {
+    int32_t vertical_block;   /* threads per block of the per-cell kernels */
+    int32_t routing_warps;    /* warps per block of the routing wavefront kernels */
+    int32_t routing_blocks_per_sm;
+    int32_t use_graph;        /* capture the step in a CUDA graph (1 = yes, default) */
+    int32_t reserved[4];
+} WfTuning;
+
+/* Library version / ABI check. */
+int32_t wf_abi_version(void);
+
+/* Model construction (replaces Model(config) for the hot-path state, Wflow/src/sbm_model.jl:7-57):
+ * copies inputs, derives parameters, builds the drainage-graph wavefront schedule, allocates
+ * device state in the cold-start values (soil.jl:164-178, utils.jl:916-937). */
+int32_t wf_create(const WfConfig* config, const WfDomain* domain, const WfParams* params,
+                  int32_t device, WfHandle** out);
+void wf_destroy(WfHandle* h);
+
+/* Message of the last error on this handle (or of the last failed wf_create when h is NULL). */
+const char* wf_last_error(const WfHandle* h);
+
+/* Forcing of the next step (AtmosphericForcing, Wflow/src/forcing.jl:2-10; io.jl:108-160):
+ * host arrays of n_land*n_members values, member-major, land order. */
+int32_t wf_set_forcing(WfHandle* h, const double* precipitation, const double* potential_evaporation,
+                       const double* temperature, int64_t count);
+/* Same from device pointers already in the library's slot order (see wf_get_slot_order). */
+int32_t wf_set_forcing_device_slots(WfHandle* h, const void* precipitation,
+                                    const void* potential_evaporation, const void* temperature);
+
+/* One model step: update_model! (sbm_model.jl:60-92) followed by compute_mass_balance!
+ * (mass_balance.jl:541-545) when water_mass_balance is set. Synchronous on return. */
+int32_t wf_step(WfHandle* h);
+/* Asynchronous variant: enqueue the step on the handle's stream without waiting. */
+int32_t wf_step_async(WfHandle* h);
+int32_t wf_synchronize(WfHandle* h);
+
+/* Copy a field to host (count values from element offset; member-major over land or river
+ * order). Layered fields take `layer`. BMI get_value / get_value_at_indices (bmi.jl:208-240). */
+int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* host_dst, int64_t offset,
+                     int64_t count);
+/* Overwrite a state field (BMI set_value, bmi.jl:246-248). */
+int32_t wf_set_field(WfHandle* h, int32_t field, int32_t layer, const double* host_src,
+                     int64_t offset, int64_t count);
+
+/* Outlet discharge: river q_average (or q) at each river pit, member-major [n_members * n_pits]. */
+int32_t wf_get_outlets(WfHandle* h, int32_t which /*0=q_average,1=q*/, double* host_dst,
+                       int64_t capacity, int64_t* n_written);
+
+/* Checkpoint of all step-carried state (states.jl; bmi.jl:357-371): query size with dst=NULL. */
+int32_t wf_get_state(WfHandle* h, void* dst, size_t* size);
+int32_t wf_set_state(WfHandle* h, const void* src, size_t size);
+
+int32_t wf_get_metrics(WfHandle* h, WfMetrics* out);
+int32_t wf_reset_metrics(WfHandle* h);
+int32_t wf_set_tuning(WfHandle* h, const WfTuning* t);
+
+/* Slot order of the land layout: ext_of_slot[s] = land index of slot s, -1 for padding. */
+int32_t wf_get_slot_order(WfHandle* h, int64_t* ext_of_slot, int64_t capacity, int64_t* n_slots);
+
+/* Number of land cells, river cells, river pits and layer count of a handle. */
+int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_outlets,
+                     int32_t* n_layers, int32_t* n_members);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WFLOW_GB300_H */

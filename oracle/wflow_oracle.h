@@ -1,0 +1,147 @@
+/*
+ * wflow_oracle.h -- C ABI of the CPU oracle (FP64 restatement of Wflow.jl's SBM +
+ * kinematic-wave step).
+ *
+ * TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / --impl reference leg as the checker. The product library never links it.
+ *
+ * The oracle consumes the same input description as the product (include/wflow_gb300.h)
+ * and follows the reference functions line by line; every function in wflow_oracle.cpp
+ * cites the Wflow.jl file:line it restates.
+ */
+#ifndef WFLOW_ORACLE_H
+#define WFLOW_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/wflow_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAXL WF_MAX_LAYERS
+
+/* One SBM soil column: parameters, boundary conditions and variables of SbmSoilModel
+ * (soil/soil.jl:3-211) for a single cell. Field names follow the reference. */
+typedef struct OrcSoil {
+    int32_t maximum_number_of_layers;
+    int32_t number_of_layers;
+    int32_t n_unsatlayers;
+    int32_t kv_profile; /* WfKvProfile */
+    /* parameters */
+    double theta_s, theta_r, theta_fc, soil_water_capacity;
+    double kv_0, f, z_exp, air_entry_pressure;
+    double h1, h2, h3_high, h3_low, h4, alpha_h1;
+    double soil_thickness;
+    double infiltration_capacity_soil, infiltration_capacity_compacted_soil;
+    double compacted_soil_area_fraction, wet_root_distribution_parameter;
+    double cap_hmax, cap_n, maximum_leakage, w_soil, cf_soil;
+    double rooting_depth, soil_fraction;
+    double actual_layer_thickness[ORC_MAXL];
+    double cumulative_layer_depth[ORC_MAXL + 1];
+    double brooks_corey_exponent[ORC_MAXL];
+    double kv_factor[ORC_MAXL];
+    double rootfraction[ORC_MAXL];
+    /* boundary conditions */
+    double water_flux_surface, potential_transpiration, potential_soilevaporation;
+    /* variables */
+    double unsaturated_layer_depth[ORC_MAXL];
+    double unsaturated_layer_thickness[ORC_MAXL];
+    double volumetric_water_content[ORC_MAXL];
+    double relative_volumetric_water_content[ORC_MAXL];
+    double h3, unsaturated_store_capacity, saturated_water_depth, drainable_water_depth;
+    double water_table_depth, transpiration, actual_evaporation_unsaturated_store;
+    double soil_evaporation, soil_evaporation_saturated_zone, actual_capillary_flux;
+    double actual_evaporation_saturated_zone, actual_evapotranspiration, actual_infiltration;
+    double actual_infiltration_soil, actual_infiltration_compacted_soil, infiltration;
+    double infiltration_excess, saturation_excess_water, exfiltration_saturated_water;
+    double excess_water_soil, excess_water_compacted_soil, runoff, net_runoff;
+    double root_zone_storage, volumetric_water_content_root_zone;
+    double relative_volumetric_water_content_root_zone, unsaturated_store_depth, transfer;
+    double recharge, actual_leakage, total_soil_water_storage, soil_surface_temperature;
+    double f_infiltration_reduction;
+} OrcSoil;
+
+/* layout of OrcSoil for the ctypes mirror: "name:offset:kind;..." (kind i=int32, d=double, aN=array) */
+const char* orc_soil_layout(void);
+int32_t orc_soil_sizeof(void);
+
+/* elementary functions (oracle_math.h) */
+double orc_exp(double x);
+double orc_log(double x);
+double orc_cbrt(double x);
+double orc_pow(double x, double y);
+double orc_cld(double x, double y);
+double orc_round_sigdigits(double x, int32_t d);
+
+/* process functions; out arrays receive the reference's return tuple in order */
+void orc_rainfall_interception_gash(double cmax, double e_r, double gap, double p, double cs,
+                                    double max_evap, double dt, double* out4);
+void orc_rainfall_interception_modrut(double p, double pet, double cs, double gap, double cmax,
+                                      double dt, double* out4);
+void orc_precipitation_hbv(double p, double t, double tti, double tt, double* out2);
+void orc_snowpack_hbv(double ss, double sw, double sp, double lp, double t, double ttm, double cfmax,
+                      double whc, double dt, double* out5);
+void orc_glacier_hbv(double gfrac, double gstore, double ss, double t, double g_ttm, double g_cfmax,
+                     double g_sifrac, double max_snow_to_glacier, double dt, double* out4);
+void orc_infiltration(double pot, double cfrac, double cap_soil, double cap_comp, double ucap,
+                      double fred, double dt, double* out2);
+void orc_unsatzone_flow_layer(double usd, double kv_z, double l_sat, double c, double dt, double* out2);
+double orc_head_brooks_corey(double vwc, double ts, double tr, double c, double psi);
+double orc_vwc_brooks_corey(double h, double psi, double ts, double tr, double c);
+double orc_feddes_h3(double h3h, double h3l, double tpot);
+double orc_rwu_reduction_feddes(double h, double h1, double h2, double h3, double h4, double a);
+double orc_soil_temperature(double tsoil_prev, double w_soil, double t);
+double orc_infiltration_reduction_factor(double tsoil, double cf, int32_t modelsnow, int32_t flag);
+double orc_soil_evaporation_unsaturated_store(double pot, double usld, double ulthick, int32_t nunsat,
+                                              double zi, double theta_e);
+double orc_soil_evaporation_saturated_store(double pot, int32_t nunsat, double lthick, double zi,
+                                            double theta_d, double dt);
+void orc_actual_infiltration_soil_path(double pot, double act, double cfrac, double cap_soil,
+                                       double cap_comp, double fred, double* out2);
+double orc_scurve(double x, double a, double b, double c);
+void orc_compute_mass_balance_error(double tin, double tout, double rate, double* out2);
+void orc_kinematic_wave(double qin, double qprev, double qlat, double alpha, double dt, double dx,
+                        double* out2);
+double orc_ssf_celerity(double zi, double slope, double sy, double kh0, double f, int32_t profile,
+                        double z_exp);
+double orc_kw_ssf_newton_raphson(double q, double c, double cel, double dt, double dx);
+/* soil-column functions (soil.jl, utils.jl) on one OrcSoil */
+void orc_update_bc_soil_model(OrcSoil* s, double canopy_potevap, double interception_rate,
+                              double pet, double wfs_runoff, double runoff_river, double runoff_land);
+void orc_unsaturated_zone_flow(OrcSoil* s, double dt);
+void orc_soil_evaporation(OrcSoil* s, double dt);
+void orc_transpiration(OrcSoil* s, double dt);
+void orc_capillary_flux(OrcSoil* s, double dt);
+void orc_update_soil_water_storage(OrcSoil* s, double exfilt_avg, double runoff_land, double ae_land,
+                                   double dt);
+void orc_water_table_change(const OrcSoil* s, double net_flux, double sy, double dt, double* out2);
+/* kinematic_wave_ssf (subsurface_process.jl:89-172); out4 = q, zi, exfilt, net_flux */
+void orc_kinematic_wave_ssf(double q_in, double q_prev, double zi_prev, double q_net, double slope,
+                            double sy, double d, double dt, double dx, double dw, double q_max,
+                            double kh0, double f, int32_t profile, double z_exp, OrcSoil* s,
+                            double* out4);
+/* stable_timestep of a kinematic-wave flow model (surface_kinwave.jl:674-704) */
+double orc_kinwave_stable_timestep(const double* q, const double* alpha, const double* flow_length,
+                                   int64_t n, double p);
+double orc_quantile(double* v, int64_t n, double p);
+
+/* full model */
+typedef struct OrcModel OrcModel;
+int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p, OrcModel** out);
+void orc_model_destroy(OrcModel* m);
+const char* orc_model_error(const OrcModel* m);
+int32_t orc_model_set_forcing(OrcModel* m, const double* P, const double* PET, const double* T);
+int32_t orc_model_step(OrcModel* m, int32_t n_threads);
+int32_t orc_model_get(OrcModel* m, int32_t field, int32_t layer, double* out);
+int32_t orc_model_set(OrcModel* m, int32_t field, int32_t layer, const double* in);
+int32_t orc_model_outlets(OrcModel* m, int32_t which, double* out, int64_t* n);
+/* sub-step counts of the last step */
+int32_t orc_model_substeps(OrcModel* m, int64_t* land, int64_t* river, int64_t* subsurface);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,270 @@
+"""Seeded synthetic SBM domains and forcing.
+
+Stands in for Wflow's staticmaps/forcing netCDF files (no such data ships with the reference
+test suite in this environment): a square raster catchment with a fractal DEM (Hurst 0.8,
+0-1000 m), a depression-free D8 drainage network draining to one corner outlet, a river
+network where more than 20 cells drain through a cell, and per-cell soil, vegetation and snow
+parameters drawn from the distributions of the benchmark configurations. Parameters that the
+reference gives defaults for use those defaults (Wflow/src/standard_name/standard_name_sbm.jl,
+standard_name_routing.jl). Units are SI, as after Wflow's `to_SI` (Wflow/src/units.jl:271).
+
+Derived geometry follows the reference initialisation:
+  flow length / width          Wflow/src/utils.jl:418-449
+  river fraction               Wflow/src/domain.jl:311-347
+  surface flow width           Wflow/src/utils.jl:458-466, domain.jl:231-233
+  flow fraction to river       Wflow/src/utils.jl:493-510
+  river graph (pit where the downstream cell is not a river cell)  Wflow/src/network.jl:214-258
+"""
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+MM = 1e-3
+MM_PER_DAY = (1.0 / 86400.0) * 1e-3   # Wflow's mm d-1 to m s-1 factor
+HURST = 0.8
+SCALE_RATIO_H08 = float.fromhex("0x1.2611186bae674p-1")  # 2**-0.8, passed to the generator (no pow on the host)
+
+
+@dataclass
+class Domain:
+    nx: int
+    ny: int
+    cell_size: float
+    ldd: np.ndarray
+    land: dict          # WfDomain land arrays + "land_downstream"
+    river: dict         # WfDomain river arrays + "river_land_index", "river_downstream"
+    params: dict        # WfParams arrays
+    upstream_cells: np.ndarray
+    catchment_of_cell: np.ndarray = None   # ragged batches: catchment id of each land cell
+    outlets: list = field(default_factory=list)
+
+    @property
+    def n_land(self):
+        return len(self.ldd)
+
+    @property
+    def n_river(self):
+        return len(self.river["river_land_index"])
+
+
+def _d8(nx, ny, seed, cell_size, min_slope=1e-4):
+    lib = abi.load_synth()
+    n = nx * ny
+    dem = np.zeros(n)
+    ldd = np.zeros(n, np.uint8)
+    ds = np.zeros(n, np.int32)
+    slope = np.zeros(n)
+    ups = np.zeros(n, np.int64)
+    fl = np.zeros(n)
+    fw = np.zeros(n)
+    import ctypes as C
+    st = lib.wf_synth_dem_d8(nx, ny, C.c_uint64(seed), SCALE_RATIO_H08, 1000.0, float(cell_size), min_slope,
+                             abi.as_ptr(dem), abi.as_ptr(ldd, C.c_uint8), abi.as_ptr(ds, C.c_int32),
+                             abi.as_ptr(slope), abi.as_ptr(ups, C.c_int64), abi.as_ptr(fl), abi.as_ptr(fw))
+    if st != 0:
+        raise RuntimeError(f"wf_synth_dem_d8 failed ({st})")
+    return dem, ldd, ds, slope, ups, fl, fw
+
+
+def make_domain(nx, cell_size, seed=1, ny=None, river_min_cells=20, n_layers_cfg=(100.0, 300.0, 800.0)):
+    """One square catchment of nx*ny cells (cells of `cell_size` metres)."""
+    ny = nx if ny is None else ny
+    dem, ldd, ds, slope, ups, fl, fw = _d8(nx, ny, seed, cell_size)
+    n = nx * ny
+    area = np.full(n, float(cell_size) * float(cell_size))
+    is_river = ups > river_min_cells
+    amax = float(ups.max())
+    river_width_all = np.where(is_river, 10.0 + 90.0 * np.sqrt(ups / amax), 0.0)
+    river_length_all = np.where(is_river, fl, 0.0)
+    river_fraction = np.where(is_river, np.minimum((river_length_all * river_width_all) / area, 1.0), 0.0)
+    water_fraction = np.maximum(np.zeros(n) - river_fraction, 0.0)
+    land_area = (1.0 - river_fraction) * area
+    sfw = np.where(is_river, land_area / fl, fw)
+    # flow fraction to river (utils.jl:493-510)
+    frac = np.zeros(n)
+    j = np.nonzero(ds >= 0)[0]
+    dsj = ds[j]
+    sel = is_river[dsj] & (ldd[j] != ldd[dsj])
+    jj, ii = j[sel], dsj[sel]
+    frac[jj] = slope[jj] / (slope[ii] + slope[jj])
+    land = dict(
+        land_downstream=ds.astype(np.int32), area=area, flow_width=fw, flow_length=fl, surface_flow_width=sfw,
+        slope=slope, flow_fraction_to_river=frac, river_fraction=river_fraction, water_fraction=water_fraction,
+        elevation=dem, land_manning_n=np.full(n, 0.072))
+    river_land = np.nonzero(is_river)[0].astype(np.int32)
+    rindex = np.full(n, -1, np.int64)
+    rindex[river_land] = np.arange(len(river_land))
+    rds_land = ds[river_land]
+    rds = np.where((rds_land >= 0) & is_river[np.maximum(rds_land, 0)], rindex[np.maximum(rds_land, 0)], -1)
+    nr = len(river_land)
+    river = dict(
+        river_land_index=river_land, river_downstream=rds.astype(np.int32),
+        river_width=river_width_all[river_land].copy(), river_length=river_length_all[river_land].copy(),
+        river_slope=slope[river_land].copy(), river_manning_n=np.full(nr, 0.036),
+        river_bankfull_depth=np.full(nr, 1.0), river_external_inflow=np.zeros(nr))
+    params = make_params(n, seed, n_layers=len(n_layers_cfg) + 1)
+    dom = Domain(nx=nx, ny=ny, cell_size=float(cell_size), ldd=ldd, land=land, river=river, params=params,
+                 upstream_cells=ups)
+    dom.outlets = [int(r) for r in np.nonzero(rds < 0)[0]]
+    return dom
+
+
+def make_params(n, seed, n_layers=4):
+    """Per-cell SBM parameters (SI). Distributions of the benchmark configurations; reference
+    defaults elsewhere (standard_name_sbm.jl line refs in the comments)."""
+    rng = np.random.default_rng([int(seed), 7])
+    p = {}
+    p["theta_s"] = rng.uniform(0.45, 0.6, n)
+    p["theta_r"] = rng.uniform(0.05, 0.1, n)
+    ksat_mm_d = np.clip(np.exp(np.log(200.0) + 0.8 * rng.standard_normal(n)), 50.0, 500.0)
+    p["kv_0"] = ksat_mm_d * MM_PER_DAY
+    p["f"] = rng.uniform(0.001, 0.01, n) * 1000.0              # mm-1 -> m-1
+    p["brooks_corey_exponent"] = rng.uniform(8.0, 12.0, n * n_layers)
+    p["soil_thickness"] = np.full(n, 2000.0 * MM)
+    p["air_entry_pressure"] = np.full(n, -0.1)                # -10 cm (:452-453)
+    p["h1"] = np.zeros(n)                                     # 0 cm (:668-669)
+    p["h2"] = np.full(n, -1.0)                                # -100 cm
+    p["h3_high"] = np.full(n, -4.0)                           # -400 cm
+    p["h3_low"] = np.full(n, -10.0)                           # -1000 cm
+    p["h4"] = np.full(n, -160.0)                              # -16000 cm
+    p["alpha_h1"] = np.ones(n)
+    p["infiltration_capacity_compacted_soil"] = np.full(n, 10.0 * MM_PER_DAY)  # 10 mm d-1 (:38-39)
+    p["compacted_soil_area_fraction"] = np.zeros(n)           # PathFrac 0
+    p["wet_root_distribution_parameter"] = np.full(n, -500.0 * 1000.0)  # -500 mm-1 (:497)
+    p["cap_hmax"] = np.full(n, 2000.0 * MM)                   # (:483)
+    p["cap_n"] = np.full(n, 2.0)
+    p["maximum_leakage"] = np.zeros(n)
+    p["w_soil"] = np.full(n, 0.1125)
+    p["cf_soil"] = np.full(n, 0.038)
+    p["z_exp"] = np.full(n, 0.0)
+    p["kv_factor"] = np.ones(n * n_layers)
+    p["horizontal_to_vertical_ratio"] = np.full(n, 100.0)     # no reference default: fixed here
+    # vegetation
+    p["canopy_gap_fraction"] = rng.uniform(0.1, 0.6, n)       # no reference default: fixed here
+    p["maximum_canopy_storage"] = np.full(n, 1.0 * MM)        # 1 mm (:711)
+    p["crop_coefficient"] = np.ones(n)
+    p["rooting_depth"] = rng.uniform(300.0, 800.0, n) * MM    # no reference default: fixed here
+    p["evaporation_to_precipitation_ratio"] = np.full(n, 0.1)  # (:651)
+    # snow (:8-19, :326-342)
+    p["degree_day_factor"] = np.full(n, 3.75 * MM_PER_DAY)
+    p["temperature_threshold_snowfall"] = np.full(n, 273.15)
+    p["temperature_interval_snowfall"] = np.full(n, 1.0)
+    p["temperature_threshold_melt"] = np.full(n, 273.15)
+    p["water_holding_capacity"] = np.full(n, 0.1)
+    return {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in p.items()}
+
+
+def perturb_members(params, n_members, seed):
+    """Ensemble members: KsatVer x 10^U(-0.5, 0.5) and f x U(0.5, 2) per member; returns
+    member-major kv_0/f arrays and the per-member precipitation factors lognormal(0, 0.3)."""
+    rng = np.random.default_rng([int(seed), 11])
+    kfac = 10.0 ** rng.uniform(-0.5, 0.5, n_members)
+    ffac = rng.uniform(0.5, 2.0, n_members)
+    pfac = np.exp(0.3 * rng.standard_normal(n_members))
+    kv0 = np.concatenate([params["kv_0"] * k for k in kfac])
+    f = np.concatenate([params["f"] * x for x in ffac])
+    return kv0, f, pfac
+
+
+def make_ragged(n_catchments, seed=3, cell_size=1000.0, log10_min=3.0, log10_max=6.0):
+    """Uneven batch: independent square catchments of log-uniform size packed into one domain."""
+    rng = np.random.default_rng([int(seed), 5])
+    sides = np.maximum(np.round(np.sqrt(10.0 ** rng.uniform(log10_min, log10_max, n_catchments))), 4).astype(int)
+    parts = [make_domain(int(s), cell_size, seed=int(seed) * 1000 + k) for k, s in enumerate(sides)]
+    return concat_domains(parts)
+
+
+def concat_domains(parts):
+    land, river, params = {}, {}, {}
+    off_l = off_r = 0
+    cat = []
+    outlets = []
+    for k, d in enumerate(parts):
+        for key, v in d.land.items():
+            if key == "land_downstream":
+                v = np.where(v >= 0, v + off_l, -1).astype(np.int32)
+            land.setdefault(key, []).append(v)
+        for key, v in d.river.items():
+            if key == "river_land_index":
+                v = (v + off_l).astype(np.int32)
+            elif key == "river_downstream":
+                v = np.where(v >= 0, v + off_r, -1).astype(np.int32)
+            river.setdefault(key, []).append(v)
+        for key, v in d.params.items():
+            params.setdefault(key, []).append(v)
+        cat.append(np.full(d.n_land, k, np.int32))
+        outlets += [o + off_r for o in d.outlets]
+        off_l += d.n_land
+        off_r += d.n_river
+    cat_arr = np.concatenate(cat)
+    out = Domain(nx=off_l, ny=1, cell_size=parts[0].cell_size,
+                 ldd=np.concatenate([d.ldd for d in parts]),
+                 land={k: np.ascontiguousarray(np.concatenate(v)) for k, v in land.items()},
+                 river={k: np.ascontiguousarray(np.concatenate(v)) for k, v in river.items()},
+                 params={k: np.ascontiguousarray(np.concatenate(v)) for k, v in params.items()},
+                 upstream_cells=np.concatenate([d.upstream_cells for d in parts]), catchment_of_cell=cat_arr)
+    out.outlets = outlets
+    return out
+
+
+def forcing(step, dt, n, seed=1, precip_scale=1.0):
+    """Forcing of model step `step` (0-based) in SI: precipitation and potential evaporation
+    [m s-1], temperature [K]. Daily rates are divided by the number of steps per day."""
+    rng = np.random.default_rng([int(seed), 1000003, int(step)])
+    steps_per_day = 86400.0 / dt
+    t_days = (step + 1) * dt / 86400.0
+    season = np.sin(2.0 * np.pi * t_days / 365.0)
+    dry = rng.random(n) < 0.4
+    p_mm_day = np.where(dry, 0.0, rng.gamma(0.4, 10.0, n)) * precip_scale
+    temp_c = 10.0 + 10.0 * season + 3.0 * rng.standard_normal(n)
+    pet_mm_day = np.full(n, 2.5 + 2.5 * season)
+    to_si = 1e-3 * (1.0 / dt)   # mm dt-1 -> m s-1
+    P = (p_mm_day / steps_per_day) * to_si
+    PET = (pet_mm_day / steps_per_day) * to_si
+    T = temp_c + 273.15
+    return np.ascontiguousarray(P), np.ascontiguousarray(PET), np.ascontiguousarray(T)
+
+
+def make_config(dt, n_members=1, form=abi.WF_FORM_FP64, snow=True, adaptive=False, mass_balance=True,
+                layers=(100.0, 300.0, 800.0), per_member_soil=False):
+    c = abi.WfConfig()
+    c.dt = float(dt)
+    c.n_soil_layer_thickness = len(layers)
+    for i, t in enumerate(layers):
+        c.soil_layer_thickness[i] = t * MM
+    c.snow = int(snow)
+    c.soil_infiltration_reduction = 0
+    c.water_mass_balance = int(mass_balance)
+    c.adaptive_timestep = int(adaptive)
+    c.kv_profile = abi.WF_KV_EXPONENTIAL
+    c.land_dt_fixed = 3600.0
+    c.river_dt_fixed = 900.0
+    c.subsurface_dt_fixed = 86400.0
+    c.subsurface_alpha = 1.0
+    c.form = int(form)
+    c.n_members = int(n_members)
+    c.per_member_soil = int(per_member_soil)
+    return c
+
+
+def c_structs(dom, params=None):
+    """WfDomain and WfParams structs pointing into the domain's arrays (keep `dom` alive)."""
+    import ctypes as C
+    params = dom.params if params is None else params
+    d = abi.WfDomain()
+    d.n_land = dom.n_land
+    d.land_downstream = abi.as_ptr(dom.land["land_downstream"], C.c_int32)
+    for k in abi.DOMAIN_LAND_ARRAYS:
+        setattr(d, k, abi.as_ptr(dom.land[k]))
+    d.n_river = dom.n_river
+    d.river_land_index = abi.as_ptr(dom.river["river_land_index"], C.c_int32)
+    d.river_downstream = abi.as_ptr(dom.river["river_downstream"], C.c_int32)
+    for k in abi.DOMAIN_RIVER_ARRAYS:
+        setattr(d, k, abi.as_ptr(dom.river[k]))
+    p = abi.WfParams()
+    for k in abi.PARAM_FIELDS:
+        setattr(p, k, abi.as_ptr(params.get(k)))
+    return d, p
