@@ -290,6 +290,16 @@ int32_t wf_get_slot_order(WfHandle* h, int64_t* ext_of_slot, int64_t capacity, i
 int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_outlets,
                      int32_t* n_layers, int32_t* n_members);
 
+/* ---- diagnostics (no counterpart in the reference) ---------------------------------------
+ * Size of the ABI structs for binding checks: 0 WfConfig, 1 WfDomain, 2 WfParams,
+ * 3 WfMetrics, 4 WfTuning; -1 otherwise. */
+int32_t wf_struct_size(int32_t which);
+/* Host-only planning of a drainage graph's wavefront schedule (no GPU needed):
+ * out_counts = {n_chains, n_chunks, n_slots, max_chain_len}; slot_of_node optional [n];
+ * ok = 1 when the schedule invariants hold; g_out = chains per chunk. */
+int32_t wf_plan_routing(int64_t n, const int32_t* downstream, int32_t members, int64_t* out_counts,
+                        int64_t* slot_of_node, int32_t* ok, int32_t* g_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,192 @@
+"""FP64 plain form on the GPU against the CPU oracle, through the C ABI.
+
+The FP64 form computes every operation in the same order as the oracle with the same
+elementary-function implementations, so results are expected to agree bit for bit; the
+acceptance bar asserted here is the drop-in tolerance, relative 1e-9 (absolute 1e-300 for
+exact zeros), and the exact-equality fraction is asserted separately.
+"""
+
+import numpy as np
+import pytest
+
+from wflow_gb300 import abi, synthetic
+from wflow_gb300.model import Model
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+
+LAND = ["CANOPY_STORAGE", "SNOW_STORAGE", "SNOW_WATER", "SOIL_SURFACE_TEMPERATURE", "SATURATED_WATER_DEPTH",
+        "SSF_Q", "LAND_Q", "LAND_H", "WATER_TABLE_DEPTH", "UNSATURATED_STORE_DEPTH", "TOTAL_SOIL_WATER_STORAGE",
+        "RECHARGE", "NET_RUNOFF", "RUNOFF", "ACTUAL_EVAPOTRANSPIRATION", "ACTUAL_LEAKAGE", "TRANSPIRATION",
+        "SOIL_EVAPORATION", "ACTUAL_INFILTRATION", "EXFILTRATION_SATURATED_WATER", "INTERCEPTION_RATE",
+        "NET_RUNOFF_RIVER", "SSF_Q_AVERAGE", "SSF_WATER_TABLE_DEPTH", "SSF_STORAGE", "SSF_TO_RIVER_AVERAGE",
+        "LAND_Q_AVERAGE", "LAND_STORAGE", "LAND_TO_RIVER_AVERAGE", "LAND_INWATER", "TOTAL_STORAGE",
+        "BALANCE_LAND_ERROR", "BALANCE_OVERLAND_ERROR", "BALANCE_SUBSURFACE_ERROR"]
+RIVER = ["RIVER_Q", "RIVER_H", "RIVER_STORAGE", "RIVER_Q_AVERAGE", "RIVER_QIN_AVERAGE", "RIVER_INWATER",
+         "BALANCE_RIVER_ERROR"]
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    both_nan = np.isnan(a) & np.isnan(b)
+    d = np.abs(a - b)
+    scale = np.maximum(np.abs(a), np.abs(b))
+    r = np.where(scale > 1e-300, d / np.maximum(scale, 1e-300), d)
+    r[both_nan] = 0.0
+    return r
+
+
+def compare(gpu, orc, fields, layers=0):
+    worst = {}
+    exact = 0
+    total = 0
+    for f in fields:
+        fid = abi.FIELD[f]
+        for k in (range(layers) if f in abi.LAYERED_FIELDS else [0]):
+            g = gpu.get_value(fid, layer=k)
+            o = orc.get(fid, layer=k)
+            r = rel_err(g, o)
+            worst[f if k == 0 else f"{f}[{k}]"] = float(r.max()) if r.size else 0.0
+            exact += int(np.sum((g == o) | (np.isnan(g) & np.isnan(o))))
+            total += g.size
+    return worst, exact / max(total, 1)
+
+
+def run_pair(dom, cfg, steps, seed=1, params=None, check_every=1, precip_scale=None):
+    gpu = Model(cfg, dom, params=params)
+    orc = O.OracleModel(cfg, dom, params=params)
+    M = max(1, cfg.n_members)
+    results = []
+    for s in range(steps):
+        P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=seed)
+        if M > 1:
+            scale = precip_scale if precip_scale is not None else np.ones(M)
+            P = np.concatenate([P * scale[m] for m in range(M)])
+            PET = np.tile(PET, M)
+            T = np.tile(T, M)
+        gpu.run_timestep(P, PET, T)
+        orc.set_forcing(P, PET, T)
+        orc.step()
+        if (s + 1) % check_every == 0 or s == steps - 1:
+            results.append(compare(gpu, orc, LAND + ["UNSATURATED_LAYER_DEPTH", "VOLUMETRIC_WATER_CONTENT"] +
+                                   (RIVER if dom.n_river else []), layers=gpu.N))
+    return gpu, orc, results
+
+
+def assert_parity(results, min_exact=0.999):
+    for worst, exact_frac in results:
+        bad = {k: v for k, v in worst.items() if v > RTOL}
+        assert not bad, bad
+        assert exact_frac >= min_exact, exact_frac
+
+
+def test_daily_gash_64(gpu_lib):
+    dom = synthetic.make_domain(64, 1000.0, seed=1)
+    cfg = synthetic.make_config(86400.0)
+    gpu, orc, res = run_pair(dom, cfg, 30, check_every=5)
+    assert_parity(res)
+    assert np.array_equal(gpu.outlets(0), orc.outlets(0))
+
+
+def test_hourly_rutter_48(gpu_lib):
+    dom = synthetic.make_domain(48, 250.0, seed=2)
+    cfg = synthetic.make_config(3600.0)
+    gpu, orc, res = run_pair(dom, cfg, 48, check_every=12)
+    assert_parity(res)
+
+
+def test_snow_off_and_kv_exponential_constant(gpu_lib):
+    dom = synthetic.make_domain(24, 1000.0, seed=4)
+    params = dict(dom.params)
+    params["z_exp"] = np.full(dom.n_land, 0.6)
+    cfg = synthetic.make_config(86400.0, snow=False)
+    cfg.kv_profile = abi.WF_KV_EXPONENTIAL_CONSTANT
+    gpu, orc, res = run_pair(dom, cfg, 10, params=params, check_every=5)
+    assert_parity(res)
+
+
+def test_single_cell_and_no_river(gpu_lib):
+    dom = synthetic.make_domain(2, 1000.0, seed=6, ny=1)
+    assert dom.n_river == 0
+    cfg = synthetic.make_config(86400.0)
+    gpu, orc, res = run_pair(dom, cfg, 5)
+    worst, _ = res[-1]
+    assert all(v <= RTOL for v in worst.values()), worst
+
+
+def test_ensemble_members_match_oracle(gpu_lib):
+    dom = synthetic.make_domain(32, 1000.0, seed=7)
+    M = 4
+    kv0, f, pfac = synthetic.perturb_members(dom.params, M, seed=7)
+    params = dict(dom.params, kv_0=kv0, f=f)
+    cfg = synthetic.make_config(86400.0, n_members=M, per_member_soil=True)
+    gpu, orc, res = run_pair(dom, cfg, 8, params=params, precip_scale=pfac, check_every=4)
+    assert_parity(res)
+    q = gpu.outlets(0)
+    assert q.size == M and len(set(np.round(q, 12))) > 1  # members differ
+
+
+def test_restart_equivalence(gpu_lib):
+    # test/run.jl: a cold run equals a run interrupted, checkpointed and resumed
+    dom = synthetic.make_domain(32, 1000.0, seed=8)
+    cfg = synthetic.make_config(86400.0)
+    a = Model(cfg, dom)
+    b = Model(cfg, dom)
+    for s in range(12):
+        P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=8)
+        a.run_timestep(P, PET, T)
+        if s < 5:
+            b.run_timestep(P, PET, T)
+        if s == 4:
+            blob = b.save_state()
+            b.close()
+            b = Model(cfg, dom)
+            b.load_state(blob)
+        if s > 4:
+            b.run_timestep(P, PET, T)
+    for f in ["SATURATED_WATER_DEPTH", "SSF_Q", "LAND_Q", "RIVER_Q", "RIVER_Q_AVERAGE", "SNOW_STORAGE"]:
+        assert np.array_equal(a.get_value(f), b.get_value(f)), f
+
+
+def test_graph_and_eager_paths_agree(gpu_lib):
+    dom = synthetic.make_domain(32, 1000.0, seed=9)
+    cfg = synthetic.make_config(86400.0)
+    a = Model(cfg, dom)
+    b = Model(cfg, dom)
+    b.set_tuning(use_graph=0, routing_warps=2)
+    for s in range(4):
+        P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=9)
+        a.run_timestep(P, PET, T)
+        b.run_timestep(P, PET, T)
+    for f in ["SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE"]:
+        assert np.array_equal(a.get_value(f), b.get_value(f)), f
+    assert a.metrics()["kernel_launches"] > 0
+
+
+def test_bounded_wait_reports_error_and_recovers(gpu_lib):
+    # a wait on an epoch nothing publishes must end within its budget with WF_ERR_SPIN
+    dom = synthetic.make_domain(16, 1000.0, seed=10)
+    cfg = synthetic.make_config(86400.0)
+    m = Model(cfg, dom)
+    m.set_tuning(use_graph=0, wait_budget_us=20000, wait_offset=1000)
+    P, PET, T = synthetic.forcing(0, cfg.dt, dom.n_land, seed=10)
+    with pytest.raises(RuntimeError, match="status -5"):
+        m.run_timestep(P, PET, T)
+    m.set_tuning(use_graph=1)
+    m.run_timestep(P, PET, T)  # the context stays usable
+    assert np.all(np.isfinite(m.get_value("SSF_Q")))
+
+
+def test_set_value_and_get_value_at_indices(gpu_lib):
+    dom = synthetic.make_domain(16, 1000.0, seed=11)
+    cfg = synthetic.make_config(86400.0)
+    m = Model(cfg, dom)
+    v = m.get_value("SATURATED_WATER_DEPTH")
+    m.set_value("SATURATED_WATER_DEPTH", v[10:20] * 0.5, offset=10)
+    w = m.get_value("SATURATED_WATER_DEPTH", offset=5, count=20)
+    assert np.array_equal(w[5:15], v[10:20] * 0.5)
+    assert np.array_equal(w[:5], v[5:10])
+    with pytest.raises(RuntimeError):
+        m.set_value("RECHARGE", v[:3])

@@ -1,0 +1,124 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports what the header
+declares, struct layouts agree with the ctypes mirror, the wavefront planner's invariants hold
+on drainage forests of every shape, and the synthetic domains are valid D8 forests."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from wflow_gb300 import abi, build, synthetic
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build_all()
+    return abi.load_library()
+
+
+def test_header_symbols_exported(lib):
+    names = abi.header_symbols()
+    assert "wf_create" in names and "wf_step" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_synth_header_symbols_exported():
+    s = abi.load_synth()
+    text = (abi.REPO_ROOT / "include" / "wflow_gb300_synth.h").read_text()
+    assert "wf_synth_dem_d8" in text
+    assert hasattr(s, "wf_synth_dem_d8")
+
+
+def test_struct_sizes_match(lib):
+    for i, cls in enumerate([abi.WfConfig, abi.WfDomain, abi.WfParams, abi.WfMetrics, abi.WfTuning]):
+        assert lib.wf_struct_size(i) == C.sizeof(cls), cls.__name__
+
+
+def _plan(lib, ds, members):
+    ds = np.ascontiguousarray(ds, np.int32)
+    counts = np.zeros(4, np.int64)
+    slot = np.zeros(max(1, len(ds)), np.int64)
+    ok = C.c_int32()
+    g = C.c_int32()
+    st = lib.wf_plan_routing(len(ds), ds.ctypes.data_as(C.POINTER(C.c_int32)), members,
+                             counts.ctypes.data_as(C.POINTER(C.c_int64)), slot.ctypes.data_as(C.POINTER(C.c_int64)),
+                             C.byref(ok), C.byref(g))
+    return st, counts, slot[: len(ds)], ok.value, g.value
+
+
+def _random_forest(n, rng, n_roots=1):
+    ds = np.full(n, -1, np.int32)
+    for i in range(n_roots, n):
+        ds[i] = rng.integers(0, i)
+    perm = rng.permutation(n)
+    inv = np.empty(n, np.int64)
+    inv[perm] = np.arange(n)
+    out = np.full(n, -1, np.int32)
+    out[inv] = np.where(ds >= 0, inv[np.maximum(ds, 0)], -1)
+    return out
+
+
+@pytest.mark.parametrize("members", [1, 2, 8, 32, 64])
+def test_plan_invariants(lib, members):
+    rng = np.random.default_rng(members)
+    cases = [np.array([-1]), np.array([1, 2, -1]), np.array([2, 2, -1]), np.array([-1, -1, -1]),
+             np.array([1, 2, 3, -1, 3, 4])]
+    cases += [_random_forest(n, rng, r) for n, r in [(50, 1), (500, 3), (3000, 1)]]
+    for ds in cases:
+        st, counts, slot, ok, G = _plan(lib, ds, members)
+        assert st == 0
+        assert ok == 1, ds
+        assert G == max(1, 32 // members)
+        n_chains, n_chunks, n_slots, max_len = counts
+        assert n_slots >= len(ds)
+        assert len(set(slot.tolist())) == len(ds)
+        assert n_chains % G == 0
+
+
+def test_plan_rejects_cycles(lib):
+    st, *_ = _plan(lib, np.array([1, 0], np.int32), 1)
+    assert st == abi.WF_ERR_CYCLE
+    st, *_ = _plan(lib, np.array([0], np.int32), 1)
+    assert st == abi.WF_ERR_CYCLE
+    st, *_ = _plan(lib, np.array([5], np.int32), 1)
+    assert st != 0
+
+
+def test_plan_real_domain_height(lib):
+    dom = synthetic.make_domain(64, 1000.0, seed=3)
+    st, counts, slot, ok, G = _plan(lib, dom.land["land_downstream"], 1)
+    assert st == 0 and ok == 1
+    # chain length of the longest chain = height of the outlet + 1
+    ds = dom.land["land_downstream"]
+    order = np.argsort(-dom.land["elevation"], kind="stable")
+    h = np.zeros(len(ds), np.int64)
+    for v in order:
+        if ds[v] >= 0:
+            h[ds[v]] = max(h[ds[v]], h[v] + 1)
+    assert counts[3] == h.max() + 1
+
+
+def test_synthetic_domain_is_valid_d8():
+    dom = synthetic.make_domain(48, 250.0, seed=5)
+    ds = dom.land["land_downstream"]
+    assert (ds == -1).sum() == 1 and ds[0] == -1  # one corner outlet
+    z = dom.land["elevation"]
+    assert np.all(z[ds[ds >= 0]] < z[ds >= 0] + 1e-9)
+    assert np.all(dom.land["slope"] >= 1e-4)
+    assert dom.n_river > 0
+    rds = dom.river["river_downstream"]
+    assert (rds == -1).sum() == 1
+    assert np.all(dom.land["river_fraction"] <= 1.0)
+    # identical on a second call (seeded)
+    dom2 = synthetic.make_domain(48, 250.0, seed=5)
+    assert np.array_equal(dom.land["elevation"], dom2.land["elevation"])
+
+
+def test_forcing_distribution():
+    P, PET, T = synthetic.forcing(10, 86400.0, 20000, seed=2)
+    dry = (P == 0).mean()
+    assert 0.37 < dry < 0.43
+    mm_day = P * 86400.0 * 1000.0
+    assert abs(mm_day[mm_day > 0].mean() - 4.0) < 0.3   # gamma(0.4, 10) mean
+    assert np.all(T > 250) and np.all(PET >= 0)

@@ -1,0 +1,1002 @@
+// wf_api.cu -- C ABI of the step library (include/wflow_gb300.h).
+//
+// wf_create restates the reference's model initialisation for the hot-path state:
+// derived soil parameters (Wflow/src/soil/soil.jl:319-617), vegetation clip
+// (sbm.jl:57-58), cold state (soil.jl:152-200), lateral subsurface initial q / q_max
+// (utils.jl:916-937) and storage (lateral_subsurface_flow.jl:134-141), Manning alpha of the
+// overland and river kinematic waves (surface_kinwave.jl:32-44, 67-86). It then plans the
+// wavefront schedule of both drainage graphs (wf_plan.cpp), permutes every array into the
+// slot layout and uploads it. wf_step runs one update_model! + compute_mass_balance! on the
+// handle's stream; the fixed-sub-step sequence is captured once in a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "wf_fields.cuh"
+#include "wf_kernels.h"
+#include "wf_math.cuh"
+#include "wf_plan.h"
+#include "wflow_gb300.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevGraphAlloc {
+    WfRoutingPlan plan;
+    int64_t *chunk_base = nullptr, *up_slot = nullptr, *node_of_slot = nullptr;
+    int32_t *chunk_len = nullptr, *chain_len = nullptr, *up_ptr = nullptr, *up_chain = nullptr;
+    uint8_t* is_chain_end = nullptr;
+    uint32_t* flags = nullptr;
+    double* end_q = nullptr;
+    unsigned long long* ticket = nullptr;
+    int32_t s_cap = 1;
+};
+
+}  // namespace
+
+struct WfHandle {
+    WfConfig cfg{};
+    std::string err;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    int64_t n = 0, nr = 0;
+    int M = 1, N = 4;
+    DevGraphAlloc land, river;
+    WfDevFields F{};
+    std::vector<void*> allocs;
+    int32_t* status = nullptr;  // device status word
+    double* staging = nullptr;  // [max(n, nr) * M] external-order staging
+    double* host_pinned = nullptr;
+    size_t host_pinned_bytes = 0;
+    double* dts_land = nullptr;
+    double* dts_river = nullptr;
+    double* dts_ssf = nullptr;
+    std::vector<double> h_dts_land, h_dts_river, h_dts_ssf;
+    std::vector<int64_t> outlet_slots;  // river slots of river pits
+    int64_t* d_land_node_of_slot = nullptr;
+    WfTuning tuning{};
+    WfMetrics metrics{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_valid = false;
+    uint64_t wait_ns = 2000000000ull;  // 2 s per wait
+    uint32_t wait_offset = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int64_t launches_per_step = 0;
+};
+
+namespace {
+
+int set_err(WfHandle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return set_err(h, WF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+    } while (0)
+
+template <class T>
+int dalloc(WfHandle* h, T** p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) return set_err(h, WF_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    h->allocs.push_back(*p);
+    return WF_OK;
+}
+
+template <class T>
+int upload(WfHandle* h, T** p, const std::vector<T>& v) {
+    int rc = dalloc(h, p, v.size());
+    if (rc) return rc;
+    if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return WF_OK;
+}
+
+// Upload an external-order array of n_ext*M (member-major) values into slot layout.
+int upload_slots(WfHandle* h, double** dst, const std::vector<double>& ext, const WfRoutingPlan& P, int M,
+                 int64_t n_ext, bool per_member) {
+    std::vector<double> v((size_t)P.n_slots * (per_member ? M : 1), 0.0);
+    for (int64_t s = 0; s < P.n_slots; ++s) {
+        int64_t node = P.node_of_slot[s];
+        if (node < 0) continue;
+        if (per_member) {
+            for (int m = 0; m < M; ++m) v[s * M + m] = ext[(size_t)m * n_ext + node];
+        } else {
+            v[s] = ext[node];
+        }
+    }
+    return upload(h, dst, v);
+}
+
+int plan_graph(WfHandle* h, DevGraphAlloc& G, int64_t n, const int32_t* ds, int M, int32_t s_cap) {
+    std::string err;
+    int rc = wf_build_plan(n, ds, M, G.plan, err);
+    if (rc) return set_err(h, rc == WF_ERR_CYCLE ? WF_ERR_CYCLE : WF_ERR_INVALID, err);
+    const WfRoutingPlan& P = G.plan;
+    if ((rc = upload(h, &G.chunk_base, P.chunk_base))) return rc;
+    if ((rc = upload(h, &G.chunk_len, P.chunk_len))) return rc;
+    if ((rc = upload(h, &G.chain_len, P.chain_len))) return rc;
+    if ((rc = upload(h, &G.up_ptr, P.up_ptr))) return rc;
+    if ((rc = upload(h, &G.up_slot, P.up_slot))) return rc;
+    if ((rc = upload(h, &G.up_chain, P.up_chain))) return rc;
+    if ((rc = upload(h, &G.is_chain_end, P.is_chain_end))) return rc;
+    if ((rc = upload(h, &G.node_of_slot, P.node_of_slot))) return rc;
+    G.s_cap = s_cap;
+    if ((rc = dalloc(h, &G.flags, (size_t)P.n_chains * M))) return rc;
+    if ((rc = dalloc(h, &G.end_q, (size_t)P.n_chains * M * s_cap))) return rc;
+    if ((rc = dalloc(h, &G.ticket, 1))) return rc;
+    return WF_OK;
+}
+
+WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
+    WfDevGraph g{};
+    g.n_slots = G.plan.n_slots;
+    g.n_chunks = G.plan.n_chunks;
+    g.n_chains = G.plan.n_chains;
+    g.G = G.plan.G;
+    g.M = M;
+    g.chunk_base = G.chunk_base;
+    g.chunk_len = G.chunk_len;
+    g.chain_len = G.chain_len;
+    g.up_ptr = G.up_ptr;
+    g.up_slot = G.up_slot;
+    g.up_chain = G.up_chain;
+    g.is_chain_end = G.is_chain_end;
+    g.flags = G.flags;
+    g.end_q = G.end_q;
+    g.ticket = G.ticket;
+    g.s_cap = G.s_cap;
+    return g;
+}
+
+// fixed sub-steps of a sweep (routing/timestepping.jl:11-16 with the while loop of the
+// update_*_flow_model! drivers)
+std::vector<double> fixed_substeps(double dt_fixed, double dt) {
+    std::vector<double> v;
+    double t = 0.0;
+    while (t < dt) {
+        double ts = dt_fixed;
+        if (t + ts > dt) ts = dt - t;
+        v.push_back(ts);
+        t += ts;
+        if (v.size() > 1000000) break;
+    }
+    return v;
+}
+
+WfLaunchCfg launch_cfg(const WfHandle* h) {
+    WfLaunchCfg c{};
+    c.stream = h->stream;
+    c.num_sms = h->num_sms;
+    c.vertical_block = h->tuning.vertical_block;
+    c.walk_warps = h->tuning.routing_warps;
+    c.walk_blocks = h->tuning.routing_blocks_per_sm > 0 ? h->tuning.routing_blocks_per_sm * h->num_sms : 0;
+    return c;
+}
+
+// ------------------------------------------------------------------ gather/scatter kernels
+__global__ void gather_kernel(const double* src, double* dst, const int64_t* node_of_slot, int64_t slots, int M,
+                              int64_t n_ext) {
+    const int64_t E = slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / M;
+        const int m = (int)(e - s * M);
+        const int64_t node = node_of_slot[s];
+        if (node >= 0) dst[e] = src[(int64_t)m * n_ext + node];
+    }
+}
+__global__ void scatter_kernel(const double* src, double* dst, const int64_t* node_of_slot, int64_t slots, int M,
+                               int64_t n_ext) {
+    const int64_t E = slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / M;
+        const int m = (int)(e - s * M);
+        const int64_t node = node_of_slot[s];
+        if (node >= 0) dst[(int64_t)m * n_ext + node] = src[e];
+    }
+}
+__global__ void broadcast_member_kernel(const double* src, double* dst, const int64_t* node_of_slot, int64_t slots,
+                                        int M, const double* scale) {
+    const int64_t E = slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / M;
+        const int64_t node = node_of_slot[s];
+        if (node >= 0) dst[e] = scale ? src[node] * scale[e - s * M] : src[node];
+    }
+}
+
+int grid_of(int64_t n, int block) {
+    int64_t b = (n + block - 1) / block;
+    if (b > 65535LL * 16) b = 65535LL * 16;
+    return (int)(b < 1 ? 1 : b);
+}
+
+// Field table: WfField -> device array
+struct FieldRef {
+    double* p = nullptr;
+    bool river = false;
+    bool member = true;
+    bool derived_vwc = false;
+    bool settable = false;
+};
+
+FieldRef field_ref(WfHandle* h, int field, int layer) {
+    FieldRef r;
+    auto& Mf = h->F.Mf;
+    auto& RM = h->F.RM;
+    switch (field) {
+        case WF_F_CANOPY_STORAGE: r.p = Mf[CANOPY]; r.settable = true; break;
+        case WF_F_SNOW_STORAGE: r.p = Mf[SNOW]; r.settable = true; break;
+        case WF_F_SNOW_WATER: r.p = Mf[SNOW_WATER]; r.settable = true; break;
+        case WF_F_SOIL_SURFACE_TEMPERATURE: r.p = Mf[TSOIL]; r.settable = true; break;
+        case WF_F_SATURATED_WATER_DEPTH: r.p = Mf[SAT]; r.settable = true; break;
+        case WF_F_UNSATURATED_LAYER_DEPTH:
+            r.p = (layer >= 0 && layer < h->N) ? h->F.LY[LY_USLD][layer] : nullptr;
+            r.settable = true;
+            break;
+        case WF_F_SSF_Q: r.p = Mf[SSF_Q]; r.settable = true; break;
+        case WF_F_LAND_Q: r.p = Mf[OL_Q]; r.settable = true; break;
+        case WF_F_LAND_H: r.p = Mf[OL_H]; r.settable = true; break;
+        case WF_F_WATER_TABLE_DEPTH: r.p = Mf[ZI]; break;
+        case WF_F_UNSATURATED_STORE_DEPTH: r.p = Mf[USTOREDEPTH]; break;
+        case WF_F_TOTAL_SOIL_WATER_STORAGE: r.p = Mf[TSWS]; r.settable = true; break;
+        case WF_F_RECHARGE: r.p = Mf[RECHARGE]; break;
+        case WF_F_NET_RUNOFF: r.p = Mf[NET_RUNOFF]; break;
+        case WF_F_RUNOFF: r.p = Mf[RUNOFF]; break;
+        case WF_F_ACTUAL_EVAPOTRANSPIRATION: r.p = Mf[AET]; break;
+        case WF_F_ACTUAL_LEAKAGE: r.p = Mf[LEAKAGE]; break;
+        case WF_F_TRANSPIRATION: r.p = Mf[TRANSPIRATION]; break;
+        case WF_F_SOIL_EVAPORATION: r.p = Mf[SOIL_EVAP]; break;
+        case WF_F_ACTUAL_INFILTRATION: r.p = Mf[ACT_INFILT]; break;
+        case WF_F_EXFILTRATION_SATURATED_WATER: r.p = Mf[EXFILT]; break;
+        case WF_F_INTERCEPTION_RATE: r.p = Mf[INTERCEPTION]; break;
+        case WF_F_SNOW_WATER_EQUIVALENT: r.p = Mf[SWE]; break;
+        case WF_F_NET_RUNOFF_RIVER: r.p = Mf[NET_RUNOFF_RIVER]; break;
+        case WF_F_SSF_Q_AVERAGE: r.p = Mf[SSF_Q_AVG]; break;
+        case WF_F_SSF_WATER_TABLE_DEPTH: r.p = Mf[SSF_ZI]; break;
+        case WF_F_SSF_STORAGE: r.p = Mf[SSF_STORAGE]; break;
+        case WF_F_SSF_TO_RIVER_AVERAGE: r.p = Mf[SSF_TR_AVG]; break;
+        case WF_F_LAND_Q_AVERAGE: r.p = Mf[OL_Q_AVG]; break;
+        case WF_F_LAND_STORAGE: r.p = Mf[OL_STORAGE]; r.settable = true; break;
+        case WF_F_LAND_TO_RIVER_AVERAGE: r.p = Mf[OL_TR_AVG]; break;
+        case WF_F_LAND_INWATER: r.p = Mf[OL_INWATER]; break;
+        case WF_F_TOTAL_STORAGE: r.p = Mf[TOTAL_STORAGE]; break;
+        case WF_F_BALANCE_LAND_ERROR: r.p = Mf[BL_ERR]; break;
+        case WF_F_BALANCE_LAND_RELATIVE_ERROR: r.p = Mf[BL_REL]; break;
+        case WF_F_BALANCE_OVERLAND_ERROR: r.p = Mf[BO_ERR]; break;
+        case WF_F_BALANCE_OVERLAND_RELATIVE_ERROR: r.p = Mf[BO_REL]; break;
+        case WF_F_BALANCE_SUBSURFACE_ERROR: r.p = Mf[BS_ERR]; break;
+        case WF_F_BALANCE_SUBSURFACE_RELATIVE_ERROR: r.p = Mf[BS_REL]; break;
+        case WF_F_VOLUMETRIC_WATER_CONTENT:
+            r.derived_vwc = (layer >= 0 && layer < h->N);
+            break;
+        case WF_F_RIVER_Q: r.p = RM[RV_Q]; r.river = true; r.settable = true; break;
+        case WF_F_RIVER_H: r.p = RM[RV_H]; r.river = true; r.settable = true; break;
+        case WF_F_RIVER_STORAGE: r.p = RM[RV_STORAGE]; r.river = true; r.settable = true; break;
+        case WF_F_RIVER_Q_AVERAGE: r.p = RM[RV_Q_AVG]; r.river = true; break;
+        case WF_F_RIVER_QIN_AVERAGE: r.p = RM[RV_QIN_AVG]; r.river = true; break;
+        case WF_F_RIVER_INWATER: r.p = RM[RV_INWATER]; r.river = true; break;
+        case WF_F_BALANCE_RIVER_ERROR: r.p = RM[BR_ERR]; r.river = true; break;
+        case WF_F_BALANCE_RIVER_RELATIVE_ERROR: r.p = RM[BR_REL]; r.river = true; break;
+        default: break;
+    }
+    return r;
+}
+
+// State carried from one step to the next (checkpoint content), in this order.
+struct StateItem {
+    int field;
+    int layer;
+};
+std::vector<StateItem> state_items(const WfHandle* h) {
+    std::vector<StateItem> v;
+    for (int f : {WF_F_CANOPY_STORAGE, WF_F_SNOW_STORAGE, WF_F_SNOW_WATER, WF_F_SOIL_SURFACE_TEMPERATURE,
+                  WF_F_SATURATED_WATER_DEPTH, WF_F_TOTAL_SOIL_WATER_STORAGE, WF_F_SSF_Q, WF_F_LAND_Q, WF_F_LAND_H,
+                  WF_F_LAND_STORAGE, WF_F_RIVER_Q, WF_F_RIVER_H, WF_F_RIVER_STORAGE})
+        v.push_back({f, 0});
+    for (int k = 0; k < h->N; ++k) v.push_back({WF_F_UNSATURATED_LAYER_DEPTH, k});
+    return v;
+}
+
+struct StateHeader {
+    char magic[8];
+    int32_t version;
+    int32_t n_members;
+    int64_t n_land;
+    int64_t n_river;
+    int32_t n_layers;
+    int32_t n_items;
+};
+
+int run_step(WfHandle* h);
+
+}  // namespace
+
+// ============================================================================ C ABI =======
+extern "C" {
+
+int32_t wf_abi_version(void) { return WF_ABI_VERSION; }
+
+int32_t wf_struct_size(int32_t which) {
+    switch (which) {
+        case 0: return (int32_t)sizeof(WfConfig);
+        case 1: return (int32_t)sizeof(WfDomain);
+        case 2: return (int32_t)sizeof(WfParams);
+        case 3: return (int32_t)sizeof(WfMetrics);
+        case 4: return (int32_t)sizeof(WfTuning);
+        default: return -1;
+    }
+}
+
+const char* wf_last_error(const WfHandle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32_t device, WfHandle** out) {
+    WfHandle* h = nullptr;
+    if (!out) return set_err(nullptr, WF_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (!c || !d || !p) return set_err(nullptr, WF_ERR_INVALID, "null argument");
+    const int N = c->n_soil_layer_thickness + 1;
+    if (N < 2 || N > WF_MAX_LAYERS) return set_err(nullptr, WF_ERR_INVALID, "soil_layer__thickness length out of range");
+    if (d->n_land <= 0 || d->n_river < 0) return set_err(nullptr, WF_ERR_INVALID, "empty domain");
+    if (c->dt <= 0.0) return set_err(nullptr, WF_ERR_INVALID, "dt must be positive");
+    if (c->form != WF_FORM_FP64 && c->form != WF_FORM_SPLIT) return set_err(nullptr, WF_ERR_INVALID, "unknown form");
+    if (c->form == WF_FORM_SPLIT) return set_err(nullptr, WF_ERR_UNSUPPORTED, "the split form is not built yet");
+    if (c->kv_profile != WF_KV_EXPONENTIAL && c->kv_profile != WF_KV_EXPONENTIAL_CONSTANT)
+        return set_err(nullptr, WF_ERR_UNSUPPORTED, "only the exponential and exponential_constant Kv profiles");
+    const int M = c->n_members > 0 ? c->n_members : 1;
+    if (!((M <= 32 && (M & (M - 1)) == 0) || (M > 32 && M % 32 == 0)))
+        return set_err(nullptr, WF_ERR_INVALID, "n_members must be a power of two up to 32 or a multiple of 32");
+    const double* req[] = {d->area, d->flow_width, d->flow_length, d->surface_flow_width, d->slope,
+                           d->flow_fraction_to_river, d->river_fraction, d->water_fraction, d->elevation,
+                           d->land_manning_n, p->canopy_gap_fraction, p->maximum_canopy_storage, p->crop_coefficient,
+                           p->rooting_depth, p->theta_s, p->theta_r, p->kv_0, p->f, p->soil_thickness,
+                           p->air_entry_pressure, p->h1, p->h2, p->h3_high, p->h3_low, p->h4, p->alpha_h1,
+                           p->infiltration_capacity_compacted_soil, p->compacted_soil_area_fraction,
+                           p->wet_root_distribution_parameter, p->cap_hmax, p->cap_n, p->maximum_leakage, p->w_soil,
+                           p->cf_soil, p->brooks_corey_exponent, p->kv_factor, p->horizontal_to_vertical_ratio};
+    for (const double* a : req)
+        if (!a) return set_err(nullptr, WF_ERR_INVALID, "missing required input array");
+    if (c->snow && (!p->degree_day_factor || !p->temperature_threshold_snowfall || !p->temperature_interval_snowfall ||
+                    !p->temperature_threshold_melt || !p->water_holding_capacity))
+        return set_err(nullptr, WF_ERR_INVALID, "snow parameters missing");
+    if (d->n_river > 0 && (!d->river_land_index || !d->river_downstream || !d->river_width || !d->river_length ||
+                           !d->river_slope || !d->river_manning_n || !d->river_bankfull_depth))
+        return set_err(nullptr, WF_ERR_INVALID, "river arrays missing");
+    if (!d->land_downstream) return set_err(nullptr, WF_ERR_INVALID, "land_downstream missing");
+
+    h = new WfHandle();
+    h->cfg = *c;
+    h->cfg.n_members = M;
+    h->n = d->n_land;
+    h->nr = d->n_river;
+    h->M = M;
+    h->N = N;
+    h->device = device;
+    auto fail = [&](int rc) {
+        g_create_error = h->err;
+        wf_destroy(h);
+        return rc;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) {
+        set_err(h, WF_ERR_CUDA, "cudaSetDevice failed");
+        return fail(WF_ERR_CUDA);
+    }
+    {
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+            set_err(h, WF_ERR_CUDA, "cudaGetDeviceProperties failed");
+            return fail(WF_ERR_CUDA);
+        }
+        h->num_sms = prop.multiProcessorCount;
+    }
+    int rc;
+#define CKR(expr)                  \
+    do {                           \
+        if ((rc = (expr))) return fail(rc); \
+    } while (0)
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_err(h, WF_ERR_CUDA, "cudaStreamCreate failed");
+        return fail(WF_ERR_CUDA);
+    }
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    const int64_t n = h->n, nr = h->nr;
+    // river indices
+    for (int64_t r = 0; r < nr; ++r) {
+        if (d->river_land_index[r] < 0 || d->river_land_index[r] >= n) {
+            set_err(h, WF_ERR_INVALID, "river_land_index out of range");
+            return fail(WF_ERR_INVALID);
+        }
+    }
+    // sub-steps (fixed mode)
+    if (c->adaptive_timestep) {
+        set_err(h, WF_ERR_UNSUPPORTED, "adaptive kinematic-wave time stepping is not supported by this build");
+        return fail(WF_ERR_UNSUPPORTED);
+    }
+    h->h_dts_land = fixed_substeps(c->land_dt_fixed, c->dt);
+    h->h_dts_river = fixed_substeps(c->river_dt_fixed, c->dt);
+    h->h_dts_ssf = fixed_substeps(c->subsurface_dt_fixed, c->dt);
+    if (h->h_dts_land.empty() || h->h_dts_river.empty() || h->h_dts_ssf.empty() || h->h_dts_land.size() > 100000 ||
+        h->h_dts_river.size() > 100000 || h->h_dts_ssf.size() > 100000) {
+        set_err(h, WF_ERR_INVALID, "invalid fixed kinematic-wave time steps");
+        return fail(WF_ERR_INVALID);
+    }
+    CKR(upload(h, &h->dts_land, h->h_dts_land));
+    CKR(upload(h, &h->dts_river, h->h_dts_river));
+    CKR(upload(h, &h->dts_ssf, h->h_dts_ssf));
+    // wavefront schedules
+    const int cap_land = (int)std::min<size_t>(std::max(h->h_dts_land.size(), h->h_dts_ssf.size()), 128);
+    const int cap_river = (int)std::min<size_t>(h->h_dts_river.size(), 128);
+    CKR(plan_graph(h, h->land, n, d->land_downstream, M, cap_land));
+    CKR(plan_graph(h, h->river, nr, d->river_downstream ? d->river_downstream : nullptr, M, cap_river));
+    const WfRoutingPlan& PL = h->land.plan;
+    const WfRoutingPlan& PR = h->river.plan;
+
+    // ---- derived parameters and cold state in external order (reference initialisation)
+    const int per_member = c->per_member_soil != 0;
+    std::vector<double> theta_fc(n), swc(n), rdclip(n), sy(n), ol_alpha(n);
+    std::vector<int8_t> nlayers(n);
+    std::vector<double> act((size_t)N * n), rootfrac((size_t)N * n);
+    double cfg_thick[WF_MAX_LAYERS], cfg_cum[WF_MAX_LAYERS + 1];
+    for (int k = 0; k < N - 1; ++k) cfg_thick[k] = c->soil_layer_thickness[k];
+    cfg_thick[N - 1] = wfm::from_bits(0x7ff8000000000000ULL);
+    cfg_cum[0] = 0.0;
+    for (int k = 0; k < N; ++k) cfg_cum[k + 1] = cfg_cum[k] + cfg_thick[k];
+    const double NaN = wfm::from_bits(0x7ff8000000000000ULL);
+    for (int64_t i = 0; i < n; ++i) {
+        const double dsoil = p->soil_thickness[i];
+        double a[WF_MAX_LAYERS], cum[WF_MAX_LAYERS + 1];
+        int nl = N;
+        for (int k = 0; k < N; ++k) {  // set_layerthickness (utils.jl:390-404)
+            double t = cfg_thick[k] * NaN;
+            if (dsoil > cfg_cum[k + 1]) t = cfg_thick[k];
+            else if (dsoil - cfg_cum[k] > 0.0) t = dsoil - cfg_cum[k];
+            a[k] = t;
+            if (t != t) nl -= 1;
+        }
+        cum[0] = 0.0;
+        for (int k = 0; k < N; ++k) cum[k + 1] = cum[k] + a[k];
+        nlayers[i] = (int8_t)nl;
+        const double ts = p->theta_s[i], tr = p->theta_r[i], psi = p->air_entry_pressure[i];
+        // field_capacity (soil_process.jl:137-159) at h = -1 m
+        double tfc = 0.0, tot = 0.0;
+        for (int k = 0; k < nl; ++k) {
+            const double cexp = p->brooks_corey_exponent[i * N + k];
+            double v = ts;
+            if (-1.0 < psi) {
+                const double lam = 2.0 / (cexp - 3.0);
+                v = (ts - tr) * wfm::pow(psi / -1.0, lam) + tr;
+            }
+            tfc += v * a[k];
+            tot += a[k];
+        }
+        theta_fc[i] = tfc / tot;
+        swc[i] = dsoil * (ts - tr);
+        rdclip[i] = wfm::jmin(dsoil * 0.99, p->rooting_depth[i]);
+        const double rd0 = p->rooting_depth[i];
+        for (int k = 0; k < N; ++k) {  // default root fraction (soil.jl:543-563)
+            double rf = 0.0;
+            if (rd0 > 0.0) {
+                if ((rd0 - cum[k]) >= a[k]) rf = a[k] / rd0;
+                else rf = wfm::jmax((rd0 - cum[k]) / rd0, 0.0);
+            }
+            rootfrac[(size_t)k * n + i] = rf;
+            act[(size_t)k * n + i] = a[k];
+        }
+        sy[i] = wfm::jmax(ts - theta_fc[i], 0.02);
+        ol_alpha[i] = wfm::pow(d->land_manning_n[i] / wfm::sqrt_(d->slope[i]), 0.6) *
+                      wfm::pow(d->surface_flow_width[i], (2.0 / 3.0) * 0.6);
+    }
+    // per-member parameters and cold state
+    std::vector<double> kv0((size_t)n * M), fsc((size_t)n * M), qmax((size_t)n * M), sat((size_t)n * M),
+        zi((size_t)n * M), ssf_q((size_t)n * M), ssf_st((size_t)n * M), tsoil((size_t)n * M, 10.0 + 273.15);
+    for (int m = 0; m < M; ++m) {
+        for (int64_t i = 0; i < n; ++i) {
+            const size_t j = (size_t)m * n + i;
+            const int64_t ip = per_member ? (int64_t)j : i;
+            kv0[j] = p->kv_0[ip];
+            fsc[j] = p->f[ip];
+            const double ts = p->theta_s[i], tr = p->theta_r[i], dsoil = p->soil_thickness[i];
+            sat[j] = 0.85 * swc[i];
+            zi[j] = wfm::jmax(0.0, dsoil - sat[j] / (ts - tr));
+            const double kh0 = p->horizontal_to_vertical_ratio[i] * kv0[j];
+            const double f = fsc[j], slope = d->slope[i];
+            if (c->kv_profile == WF_KV_EXPONENTIAL) {
+                qmax[j] = ((kh0 * slope) / f) * (1.0 - wfm::exp(-f * dsoil));
+                ssf_q[j] = ((kh0 * slope) / f) * (wfm::exp(-f * zi[j]) - wfm::exp(-f * dsoil)) * d->flow_width[i];
+            } else {
+                const double zx = p->z_exp ? p->z_exp[i] : 0.0;
+                const double qc = kh0 * wfm::exp(-f * zx) * slope * (dsoil - zx);
+                qmax[j] = ((kh0 * slope) / f) * (1.0 - wfm::exp(-f * zx)) + qc;
+                if (zi[j] < zx)
+                    ssf_q[j] = (((kh0 * slope) / f) * (wfm::exp(-f * zi[j]) - wfm::exp(-f * zx)) + qc) * d->flow_width[i];
+                else
+                    ssf_q[j] = kh0 * wfm::exp(-f * zi[j]) * slope * (dsoil - zi[j]) * d->flow_width[i];
+            }
+            ssf_st[j] = sy[i] * (dsoil - zi[j]) * d->area[i];
+        }
+    }
+    // ---- land static fields (slot layout)
+    WfDevFields& F = h->F;
+    auto ext_vec = [&](const double* src, double dflt) {
+        std::vector<double> v(n);
+        for (int64_t i = 0; i < n; ++i) v[i] = src ? src[i] : dflt;
+        return v;
+    };
+    struct LS {
+        int idx;
+        std::vector<double> v;
+    };
+    std::vector<LS> ls = {
+        {AREA, ext_vec(d->area, 0)}, {FLOW_WIDTH, ext_vec(d->flow_width, 0)}, {FLOW_LENGTH, ext_vec(d->flow_length, 0)},
+        {SFW, ext_vec(d->surface_flow_width, 0)}, {SLOPE, ext_vec(d->slope, 0)},
+        {FRAC_TO_RIVER, ext_vec(d->flow_fraction_to_river, 0)}, {RIVER_FRACTION, ext_vec(d->river_fraction, 0)},
+        {WATER_FRACTION, ext_vec(d->water_fraction, 0)}, {TOP, ext_vec(d->elevation, 0)}, {OL_ALPHA, ol_alpha},
+        {SY, sy}, {GAP, ext_vec(p->canopy_gap_fraction, 0)}, {CMAX, ext_vec(p->maximum_canopy_storage, 0)},
+        {KC, ext_vec(p->crop_coefficient, 0)}, {E_R, ext_vec(p->evaporation_to_precipitation_ratio, 0.1)},
+        {DDF, ext_vec(p->degree_day_factor, 0)}, {TT, ext_vec(p->temperature_threshold_snowfall, 273.15)},
+        {TTI, ext_vec(p->temperature_interval_snowfall, 1.0)}, {TTM, ext_vec(p->temperature_threshold_melt, 273.15)},
+        {WHC, ext_vec(p->water_holding_capacity, 0.1)}, {THETA_S, ext_vec(p->theta_s, 0)},
+        {THETA_R, ext_vec(p->theta_r, 0)}, {THETA_FC, theta_fc}, {SWC, swc},
+        {SOIL_THICKNESS, ext_vec(p->soil_thickness, 0)}, {PSI_B, ext_vec(p->air_entry_pressure, 0)},
+        {H1, ext_vec(p->h1, 0)}, {H2, ext_vec(p->h2, 0)}, {H3_HIGH, ext_vec(p->h3_high, 0)},
+        {H3_LOW, ext_vec(p->h3_low, 0)}, {H4, ext_vec(p->h4, 0)}, {ALPHA_H1, ext_vec(p->alpha_h1, 0)},
+        {CAP_COMP, ext_vec(p->infiltration_capacity_compacted_soil, 0)},
+        {COMPACT_FRAC, ext_vec(p->compacted_soil_area_fraction, 0)},
+        {ROOTDISTPAR, ext_vec(p->wet_root_distribution_parameter, 0)}, {CAP_HMAX, ext_vec(p->cap_hmax, 0)},
+        {CAP_N, ext_vec(p->cap_n, 0)}, {MAX_LEAKAGE, ext_vec(p->maximum_leakage, 0)}, {W_SOIL, ext_vec(p->w_soil, 0)},
+        {CF_SOIL, ext_vec(p->cf_soil, 0)}, {ROOTING_DEPTH, rdclip}, {Z_EXP, ext_vec(p->z_exp, 0)},
+        {KH_RATIO, ext_vec(p->horizontal_to_vertical_ratio, 0)}};
+    for (auto& x : ls) CKR(upload_slots(h, &F.L[x.idx], x.v, PL, M, n, false));
+    for (int k = 0; k < N; ++k) {
+        std::vector<double> va(act.begin() + (size_t)k * n, act.begin() + (size_t)(k + 1) * n);
+        std::vector<double> vr(rootfrac.begin() + (size_t)k * n, rootfrac.begin() + (size_t)(k + 1) * n);
+        std::vector<double> vc(n), vk(n);
+        for (int64_t i = 0; i < n; ++i) {
+            vc[i] = p->brooks_corey_exponent[i * N + k];
+            vk[i] = p->kv_factor[i * N + k];
+        }
+        CKR(upload_slots(h, &F.LY[LY_ACT_THICK][k], va, PL, M, n, false));
+        CKR(upload_slots(h, &F.LY[LY_ROOTFRAC][k], vr, PL, M, n, false));
+        CKR(upload_slots(h, &F.LY[LY_C][k], vc, PL, M, n, false));
+        CKR(upload_slots(h, &F.LY[LY_KVFRAC][k], vk, PL, M, n, false));
+        std::vector<double> zeros((size_t)n * M, 0.0);
+        CKR(upload_slots(h, &F.LY[LY_USLD][k], zeros, PL, M, n, true));
+    }
+    {
+        std::vector<int8_t> nl_slots(PL.n_slots, 0);
+        for (int64_t s = 0; s < PL.n_slots; ++s)
+            if (PL.node_of_slot[s] >= 0) nl_slots[s] = nlayers[PL.node_of_slot[s]];
+        int8_t* dnl;
+        CKR(upload(h, &dnl, nl_slots));
+        F.nlayers = dnl;
+    }
+    // ---- land member fields
+    std::vector<double> zeros_m((size_t)n * M, 0.0);
+    for (int f = 0; f < M_COUNT; ++f) {
+        const std::vector<double>* src = &zeros_m;
+        switch (f) {
+            case KV0: src = &kv0; break;
+            case FSCALE: src = &fsc; break;
+            case Q_MAX: src = &qmax; break;
+            case TSOIL: src = &tsoil; break;
+            case SAT: src = &sat; break;
+            case TSWS: src = &sat; break;
+            case ZI: src = &zi; break;
+            case SSF_ZI: src = &zi; break;
+            case SSF_Q: src = &ssf_q; break;
+            case SSF_STORAGE: src = &ssf_st; break;
+            default: break;
+        }
+        CKR(upload_slots(h, &F.Mf[f], *src, PL, M, n, true));
+    }
+    // ---- river fields
+    std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr);
+    for (int64_t r = 0; r < nr; ++r) {
+        r_width[r] = d->river_width[r];
+        r_length[r] = d->river_length[r];
+        r_ext[r] = d->river_external_inflow ? d->river_external_inflow[r] : 0.0;
+        r_area[r] = d->area[d->river_land_index[r]];
+        const double wp = d->river_width[r] + d->river_bankfull_depth[r];
+        r_alpha[r] = wfm::pow(d->river_manning_n[r] / wfm::sqrt_(d->river_slope[r]), 0.6) *
+                     wfm::pow(wp, (2.0 / 3.0) * 0.6);
+    }
+    CKR(upload_slots(h, &F.R[R_WIDTH], r_width, PR, M, nr, false));
+    CKR(upload_slots(h, &F.R[R_LENGTH], r_length, PR, M, nr, false));
+    CKR(upload_slots(h, &F.R[R_ALPHA], r_alpha, PR, M, nr, false));
+    CKR(upload_slots(h, &F.R[R_EXT_INFLOW], r_ext, PR, M, nr, false));
+    CKR(upload_slots(h, &F.R[R_AREA], r_area, PR, M, nr, false));
+    std::vector<double> zeros_r((size_t)std::max<int64_t>(nr, 1) * M, 0.0);
+    for (int f = 0; f < RM_COUNT; ++f) CKR(upload_slots(h, &F.RM[f], zeros_r, PR, M, nr, true));
+    // ---- maps
+    {
+        std::vector<int64_t> land_river_slot(PL.n_slots, -1), river_land_slot(std::max<int64_t>(PR.n_slots, 1), -1);
+        for (int64_t r = 0; r < nr; ++r) {
+            const int64_t ls_ = PL.slot_of_node[d->river_land_index[r]];
+            const int64_t rs_ = PR.slot_of_node[r];
+            land_river_slot[ls_] = rs_;
+            river_land_slot[rs_] = ls_;
+        }
+        int64_t *a, *b;
+        CKR(upload(h, &a, land_river_slot));
+        CKR(upload(h, &b, river_land_slot));
+        F.land_river_slot = a;
+        F.river_land_slot = b;
+        F.land_node_of_slot = h->land.node_of_slot;
+        F.river_node_of_slot = h->river.node_of_slot;
+        for (int64_t r = 0; r < nr; ++r)
+            if (d->river_downstream[r] < 0) h->outlet_slots.push_back(PR.slot_of_node[r]);
+    }
+    F.land_slots = PL.n_slots;
+    F.river_slots = PR.n_slots;
+    F.N = N;
+    F.M = M;
+    F.snow = c->snow;
+    F.infilt_reduction = c->soil_infiltration_reduction;
+    F.gash = c->dt >= 23.0 * 3600.0;
+    F.kv_profile = c->kv_profile;
+    F.mass_balance = c->water_mass_balance;
+    F.dt = c->dt;
+    CKR(dalloc(h, &h->status, 1));
+    CK(cudaMemset(h->status, 0, sizeof(int32_t)));
+    F.status = h->status;
+    CKR(dalloc(h, &h->staging, (size_t)std::max<int64_t>(std::max(n, nr), 1) * M * 3));
+    h->tuning.use_graph = 1;
+    h->metrics.n_chains_land = (int32_t)PL.n_chains;
+    h->metrics.n_chains_river = (int32_t)PR.n_chains;
+    h->metrics.max_chain_land = PL.max_len;
+    h->metrics.max_chain_river = PR.max_len;
+    h->metrics.padding_slots_land = (int32_t)(PL.n_slots - n);
+    CK(cudaDeviceSynchronize());
+#undef CKR
+    *out = h;
+    return WF_OK;
+}
+
+void wf_destroy(WfHandle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->host_pinned) cudaFreeHost(h->host_pinned);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const double* T, int64_t count) {
+    if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
+    const int64_t full = h->n * h->M;
+    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
+    const double* src[3] = {P, PET, T};
+    const int dst[3] = {PRECIP, POTEVAP, TEMP};
+    const int block = 256;
+    for (int k = 0; k < 3; ++k) {
+        double* stg = h->staging + (size_t)k * std::max(h->n, h->nr) * h->M;
+        CK(cudaMemcpyAsync(stg, src[k], count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        if (count == full) {
+            gather_kernel<<<grid_of(h->F.land_slots * h->M, block), block, 0, h->stream>>>(
+                stg, h->F.Mf[dst[k]], h->F.land_node_of_slot, h->F.land_slots, h->M, h->n);
+        } else {
+            broadcast_member_kernel<<<grid_of(h->F.land_slots * h->M, block), block, 0, h->stream>>>(
+                stg, h->F.Mf[dst[k]], h->F.land_node_of_slot, h->F.land_slots, h->M, nullptr);
+        }
+        CK(cudaGetLastError());
+    }
+    return WF_OK;
+}
+
+int32_t wf_set_forcing_device_slots(WfHandle* h, const void* P, const void* PET, const void* T) {
+    if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
+    const size_t bytes = (size_t)h->F.land_slots * h->M * sizeof(double);
+    CK(cudaMemcpyAsync(h->F.Mf[PRECIP], P, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->F.Mf[POTEVAP], PET, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->F.Mf[TEMP], T, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    return WF_OK;
+}
+
+int32_t wf_step_async(WfHandle* h) {
+    if (!h) return WF_ERR_INVALID;
+    return run_step(h);
+}
+
+int32_t wf_synchronize(WfHandle* h) {
+    if (!h) return WF_ERR_INVALID;
+    CK(cudaStreamSynchronize(h->stream));
+    int32_t st = 0;
+    CK(cudaMemcpy(&st, h->status, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    h->metrics.device_status = st;
+    if (st & WF_DEV_SPIN_TIMEOUT) {
+        cudaMemset(h->status, 0, sizeof(int32_t));
+        return set_err(h, WF_ERR_SPIN, "a routing wavefront wait ran out of its time budget");
+    }
+    return WF_OK;
+}
+
+int32_t wf_step(WfHandle* h) {
+    if (!h) return WF_ERR_INVALID;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    int rc = run_step(h);
+    if (rc) return rc;
+    CK(cudaEventRecord(h->ev1, h->stream));
+    rc = wf_synchronize(h);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->metrics.step_ms_total += ms;
+    return rc;
+}
+
+int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int64_t offset, int64_t count) {
+    if (!h || !dst) return set_err(h, WF_ERR_INVALID, "null argument");
+    FieldRef r = field_ref(h, field, layer);
+    if (!r.p && !r.derived_vwc) return set_err(h, WF_ERR_INVALID, "unknown field or layer");
+    const int64_t n_ext = r.river ? h->nr : h->n;
+    const int64_t total = n_ext * h->M;
+    if (offset < 0 || count < 0 || offset + count > total) return set_err(h, WF_ERR_INVALID, "range out of bounds");
+    WfLaunchCfg lc = launch_cfg(h);
+    double* src = r.p;
+    double* tmp = h->staging + (size_t)std::max(h->n, h->nr) * h->M;  // second staging third
+    if (r.derived_vwc) {
+        CK(wf_fp64_vwc(h->F, layer, tmp, lc));
+        src = tmp;
+    }
+    const int block = 256;
+    const int64_t slots = r.river ? h->F.river_slots : h->F.land_slots;
+    const int64_t* nos = r.river ? h->F.river_node_of_slot : h->F.land_node_of_slot;
+    scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(src, h->staging, nos, slots, h->M, n_ext);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst, h->staging + offset, count * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return WF_OK;
+}
+
+int32_t wf_set_field(WfHandle* h, int32_t field, int32_t layer, const double* src, int64_t offset, int64_t count) {
+    if (!h || !src) return set_err(h, WF_ERR_INVALID, "null argument");
+    FieldRef r = field_ref(h, field, layer);
+    if (!r.p || !r.settable) return set_err(h, WF_ERR_INVALID, "field is not settable");
+    const int64_t n_ext = r.river ? h->nr : h->n;
+    const int64_t total = n_ext * h->M;
+    if (offset < 0 || count < 0 || offset + count > total) return set_err(h, WF_ERR_INVALID, "range out of bounds");
+    const int block = 256;
+    const int64_t slots = r.river ? h->F.river_slots : h->F.land_slots;
+    const int64_t* nos = r.river ? h->F.river_node_of_slot : h->F.land_node_of_slot;
+    scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p, h->staging, nos, slots, h->M, n_ext);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->staging + offset, src, count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    gather_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(h->staging, r.p, nos, slots, h->M, n_ext);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return WF_OK;
+}
+
+int32_t wf_get_outlets(WfHandle* h, int32_t which, double* dst, int64_t capacity, int64_t* n_written) {
+    if (!h || !dst || !n_written) return set_err(h, WF_ERR_INVALID, "null argument");
+    const int64_t need = (int64_t)h->outlet_slots.size() * h->M;
+    *n_written = 0;
+    if (capacity < need) return set_err(h, WF_ERR_INVALID, "capacity too small");
+    double* src = which == 0 ? h->F.RM[RV_Q_AVG] : h->F.RM[RV_Q];
+    int64_t k = 0;
+    for (int m = 0; m < h->M; ++m)
+        for (int64_t s : h->outlet_slots) {
+            CK(cudaMemcpyAsync(dst + k, src + s * h->M + m, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            ++k;
+        }
+    CK(cudaStreamSynchronize(h->stream));
+    *n_written = k;
+    return WF_OK;
+}
+
+int32_t wf_get_state(WfHandle* h, void* dst, size_t* size) {
+    if (!h || !size) return set_err(h, WF_ERR_INVALID, "null argument");
+    auto items = state_items(h);
+    size_t bytes = sizeof(StateHeader);
+    for (auto& it : items) bytes += (size_t)((it.field >= WF_F_RIVER_Q) ? h->nr : h->n) * h->M * sizeof(double);
+    if (!dst) {
+        *size = bytes;
+        return WF_OK;
+    }
+    if (*size < bytes) return set_err(h, WF_ERR_STATE, "state buffer too small");
+    StateHeader hd{};
+    std::memcpy(hd.magic, "WFGB300S", 8);
+    hd.version = 1;
+    hd.n_members = h->M;
+    hd.n_land = h->n;
+    hd.n_river = h->nr;
+    hd.n_layers = h->N;
+    hd.n_items = (int32_t)items.size();
+    std::memcpy(dst, &hd, sizeof(hd));
+    char* p = (char*)dst + sizeof(hd);
+    for (auto& it : items) {
+        const int64_t cnt = ((it.field >= WF_F_RIVER_Q) ? h->nr : h->n) * h->M;
+        int rc = wf_get_field(h, it.field, it.layer, (double*)p, 0, cnt);
+        if (rc) return rc;
+        p += cnt * sizeof(double);
+    }
+    *size = bytes;
+    return WF_OK;
+}
+
+int32_t wf_set_state(WfHandle* h, const void* src, size_t size) {
+    if (!h || !src) return set_err(h, WF_ERR_INVALID, "null argument");
+    if (size < sizeof(StateHeader)) return set_err(h, WF_ERR_STATE, "state blob too small");
+    StateHeader hd;
+    std::memcpy(&hd, src, sizeof(hd));
+    auto items = state_items(h);
+    if (std::memcmp(hd.magic, "WFGB300S", 8) != 0 || hd.version != 1 || hd.n_members != h->M || hd.n_land != h->n ||
+        hd.n_river != h->nr || hd.n_layers != h->N || hd.n_items != (int32_t)items.size())
+        return set_err(h, WF_ERR_STATE, "state blob does not match this model");
+    const char* p = (const char*)src + sizeof(hd);
+    size_t used = sizeof(hd);
+    for (auto& it : items) {
+        const int64_t cnt = ((it.field >= WF_F_RIVER_Q) ? h->nr : h->n) * h->M;
+        used += cnt * sizeof(double);
+        if (used > size) return set_err(h, WF_ERR_STATE, "state blob truncated");
+        int rc = wf_set_field(h, it.field, it.layer, (const double*)p, 0, cnt);
+        if (rc) return rc;
+        p += cnt * sizeof(double);
+    }
+    return WF_OK;
+}
+
+int32_t wf_get_metrics(WfHandle* h, WfMetrics* out) {
+    if (!h || !out) return WF_ERR_INVALID;
+    *out = h->metrics;
+    return WF_OK;
+}
+
+int32_t wf_reset_metrics(WfHandle* h) {
+    if (!h) return WF_ERR_INVALID;
+    WfMetrics keep = h->metrics;
+    h->metrics = WfMetrics{};
+    h->metrics.n_chains_land = keep.n_chains_land;
+    h->metrics.n_chains_river = keep.n_chains_river;
+    h->metrics.max_chain_land = keep.max_chain_land;
+    h->metrics.max_chain_river = keep.max_chain_river;
+    h->metrics.padding_slots_land = keep.padding_slots_land;
+    return WF_OK;
+}
+
+int32_t wf_set_tuning(WfHandle* h, const WfTuning* t) {
+    if (!h || !t) return WF_ERR_INVALID;
+    if (t->vertical_block < 0 || t->vertical_block > 1024 || (t->vertical_block % 32) != 0 || t->routing_warps < 0 ||
+        t->routing_warps > 32 || t->routing_blocks_per_sm < 0 || t->routing_blocks_per_sm > 64)
+        return set_err(h, WF_ERR_INVALID, "tuning out of range");
+    h->tuning = *t;
+    h->graph_valid = false;
+    // test hooks in reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset
+    if (t->reserved[0] > 0) h->wait_ns = (uint64_t)t->reserved[0] * 1000ull;
+    h->wait_offset = (uint32_t)t->reserved[1];
+    return WF_OK;
+}
+
+int32_t wf_get_slot_order(WfHandle* h, int64_t* ext_of_slot, int64_t capacity, int64_t* n_slots) {
+    if (!h || !n_slots) return WF_ERR_INVALID;
+    *n_slots = h->land.plan.n_slots;
+    if (ext_of_slot) {
+        if (capacity < *n_slots) return set_err(h, WF_ERR_INVALID, "capacity too small");
+        for (int64_t s = 0; s < *n_slots; ++s) ext_of_slot[s] = h->land.plan.node_of_slot[s];
+    }
+    return WF_OK;
+}
+
+int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_outlets, int32_t* n_layers,
+                     int32_t* n_members) {
+    if (!h) return WF_ERR_INVALID;
+    if (n_land) *n_land = h->n;
+    if (n_river) *n_river = h->nr;
+    if (n_outlets) *n_outlets = (int64_t)h->outlet_slots.size();
+    if (n_layers) *n_layers = h->N;
+    if (n_members) *n_members = h->M;
+    return WF_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Enqueue one model step on the handle's stream.
+int enqueue_step(WfHandle* h, int64_t* launches) {
+    const WfLaunchCfg lc = launch_cfg(h);
+    const bool split = h->cfg.form == WF_FORM_SPLIT;
+    int64_t nl = 0;
+    WfDevGraph gl = dev_graph(h->land, h->M), gr = dev_graph(h->river, h->M);
+    CK(split ? wf_split_vertical(h->F, lc) : wf_fp64_vertical(h->F, lc));
+    ++nl;
+    auto sweep = [&](DevGraphAlloc& G, const WfDevGraph& g, const std::vector<double>& dts, double* d_dts,
+                     int which) -> int {
+        const int total = (int)dts.size();
+        for (int first = 0; first < total; first += G.s_cap) {
+            WfSweep sw{};
+            sw.S = std::min(G.s_cap, total - first);
+            sw.first = first;
+            sw.last_of_step = (first + sw.S == total);
+            sw.total = total;
+            sw.epoch0 = 1;
+            sw.dt = h->cfg.dt;
+            sw.dts = d_dts + first;
+            sw.wait_ns = h->wait_ns;
+            sw.wait_offset = h->wait_offset;
+            CK(cudaMemsetAsync(G.flags, 0, (size_t)G.plan.n_chains * h->M * sizeof(uint32_t), h->stream));
+            CK(cudaMemsetAsync(G.ticket, 0, sizeof(unsigned long long), h->stream));
+            cudaError_t e;
+            if (which == 0) e = split ? wf_split_ssf(h->F, g, sw, lc) : wf_fp64_ssf(h->F, g, sw, lc);
+            else if (which == 1) e = split ? wf_split_overland(h->F, g, sw, lc) : wf_fp64_overland(h->F, g, sw, lc);
+            else e = split ? wf_split_river(h->F, g, sw, lc) : wf_fp64_river(h->F, g, sw, lc);
+            CK(e);
+            ++nl;
+        }
+        return WF_OK;
+    };
+    int rc;
+    if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;
+    if ((rc = sweep(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
+    if (h->nr > 0 && (rc = sweep(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
+    CK(split ? wf_split_balance(h->F, lc) : wf_fp64_balance(h->F, lc));
+    ++nl;
+    if (launches) *launches = nl;
+    return WF_OK;
+}
+
+int run_step(WfHandle* h) {
+    int64_t launches = 0;
+    if (h->tuning.use_graph) {
+        if (!h->graph_valid) {
+            if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+            if (h->graph) cudaGraphDestroy(h->graph);
+            h->graph_exec = nullptr;
+            h->graph = nullptr;
+            CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_step(h, &launches);
+            cudaGraph_t g = nullptr;
+            cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            CK(ee);
+            h->graph = g;
+            CK(cudaGraphInstantiate(&h->graph_exec, h->graph, 0));
+            h->graph_valid = true;
+            h->launches_per_step = launches;
+        }
+        CK(cudaGraphLaunch(h->graph_exec, h->stream));
+        launches = h->launches_per_step;
+    } else {
+        int rc = enqueue_step(h, &launches);
+        if (rc) return rc;
+    }
+    h->metrics.steps += 1;
+    h->metrics.cell_steps += h->n * h->M;
+    h->metrics.kernel_launches += launches;
+    h->metrics.substeps_land += (int64_t)h->h_dts_land.size();
+    h->metrics.substeps_river += (int64_t)h->h_dts_river.size();
+    h->metrics.substeps_subsurface += (int64_t)h->h_dts_ssf.size();
+    return WF_OK;
+}
+
+}  // namespace
+
+cudaError_t wf_gather_ext(const double* src_ext, double* dst_slots, const int64_t* node_of_slot, int64_t slots, int M,
+                          int64_t n_ext, cudaStream_t s) {
+    gather_kernel<<<grid_of(slots * M, 256), 256, 0, s>>>(src_ext, dst_slots, node_of_slot, slots, M, n_ext);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_scatter_ext(const double* src_slots, double* dst_ext, const int64_t* node_of_slot, int64_t slots, int M,
+                           int64_t n_ext, cudaStream_t s) {
+    scatter_kernel<<<grid_of(slots * M, 256), 256, 0, s>>>(src_slots, dst_ext, node_of_slot, slots, M, n_ext);
+    return cudaGetLastError();
+}

@@ -1,0 +1,107 @@
+// wf_fields.cuh -- device field table of a model handle.
+//
+// Structure-of-arrays: one device array per field. Land fields are indexed in the wavefront
+// slot layout (see wf_plan.h): static per-cell parameters by slot, member-specific
+// parameters, forcing, states and outputs by element e = slot * M + m. River fields use the
+// river graph's own slot layout. Padding slots exist in both layouts and are skipped by every
+// kernel (node_of_slot < 0).
+#pragma once
+
+#include <cstdint>
+
+#include "wflow_gb300.h"
+
+#define WF_L_FIELDS(X)                                                                             \
+    X(AREA) X(FLOW_WIDTH) X(FLOW_LENGTH) X(SFW) X(SLOPE) X(FRAC_TO_RIVER) X(RIVER_FRACTION)          \
+    X(WATER_FRACTION) X(TOP) X(OL_ALPHA) X(SY) X(GAP) X(CMAX) X(KC) X(E_R) X(DDF) X(TT) X(TTI) X(TTM) \
+    X(WHC) X(THETA_S) X(THETA_R) X(THETA_FC) X(SWC) X(SOIL_THICKNESS) X(PSI_B) X(H1) X(H2) X(H3_HIGH) \
+    X(H3_LOW) X(H4) X(ALPHA_H1) X(CAP_COMP) X(COMPACT_FRAC) X(ROOTDISTPAR) X(CAP_HMAX) X(CAP_N)       \
+    X(MAX_LEAKAGE) X(W_SOIL) X(CF_SOIL) X(ROOTING_DEPTH) X(Z_EXP) X(KH_RATIO)
+
+#define WF_M_FIELDS(X)                                                                             \
+    X(KV0) X(FSCALE) X(Q_MAX) X(PRECIP) X(POTEVAP) X(TEMP) X(CANOPY) X(SNOW) X(SNOW_WATER) X(TSOIL) X(SAT) X(TSWS)    \
+    X(USTOREDEPTH) X(ZI) X(SSF_ZI) X(SSF_Q) X(SSF_Q_AVG) X(SSF_QIN_AVG) X(SSF_TR_AVG) X(SSF_EXF_AVG) \
+    X(SSF_QNET_AVG) X(RCH_FLUX_AVG) X(SSF_STORAGE) X(SSF_QIN_CUM) X(SSF_Q_CUM) X(SSF_TR_CUM)         \
+    X(SSF_EXF_CUM) X(SSF_QNET_CUM) X(RCH_FLUX_CUM) X(OL_Q) X(OL_H) X(OL_STORAGE) X(OL_Q_AVG)          \
+    X(OL_QIN_AVG) X(OL_TR_AVG) X(OL_INWATER) X(OL_QLAT) X(OL_Q_CUM) X(OL_QIN_CUM) X(OL_TR_CUM)       \
+    X(RECHARGE) X(NET_RUNOFF_RIVER) X(AET) X(LEAKAGE) X(SATEX) X(INFEX) X(RUNOFF_LAND) X(AE_LAND)     \
+    X(INTERCEPTION) X(TRANSPIRATION) X(SOIL_EVAP) X(ACT_INFILT) X(SWE) X(NET_RUNOFF) X(RUNOFF)        \
+    X(EXFILT) X(BL_PREV) X(BO_PREV) X(TOTAL_STORAGE) X(BL_ERR) X(BL_REL) X(BO_ERR) X(BO_REL)          \
+    X(BS_ERR) X(BS_REL)
+
+#define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA)
+
+#define WF_RM_FIELDS(X)                                                                            \
+    X(RV_Q) X(RV_H) X(RV_STORAGE) X(RV_Q_AVG) X(RV_QIN_AVG) X(RV_INWATER) X(RV_QLAT) X(RV_ABS_AVG)    \
+    X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL)
+
+#define WF_ENUM_ITEM(name) name,
+enum WfLandStatic { WF_L_FIELDS(WF_ENUM_ITEM) L_COUNT };
+enum WfLandMember { WF_M_FIELDS(WF_ENUM_ITEM) M_COUNT };
+enum WfRiverStatic { WF_R_FIELDS(WF_ENUM_ITEM) R_COUNT };
+enum WfRiverMember { WF_RM_FIELDS(WF_ENUM_ITEM) RM_COUNT };
+#undef WF_ENUM_ITEM
+
+// Layered fields: N arrays each.
+enum WfLayered { LY_ACT_THICK = 0, LY_C, LY_KVFRAC, LY_ROOTFRAC, LY_USLD, LY_COUNT };
+
+struct WfDevFields {
+    double* L[L_COUNT];
+    double* Mf[M_COUNT];
+    double* R[R_COUNT];
+    double* RM[RM_COUNT];
+    double* LY[LY_COUNT][WF_MAX_LAYERS];  // ACT_THICK/C/KVFRAC/ROOTFRAC by slot, USLD by element
+    const int8_t* nlayers;                // [land slots]
+    const int64_t* land_node_of_slot;     // [land slots], -1 padding
+    const int64_t* land_river_slot;       // [land slots], river slot or -1
+    const int64_t* river_node_of_slot;    // [river slots], -1 padding
+    const int64_t* river_land_slot;       // [river slots], land slot of the river cell
+    int64_t land_slots;
+    int64_t river_slots;
+    int32_t N;      // maximum_number_of_layers
+    int32_t M;      // members
+    int32_t snow;
+    int32_t infilt_reduction;
+    int32_t gash;
+    int32_t kv_profile;
+    int32_t mass_balance;
+    double dt;
+    int32_t* status;  // device status word (0 = ok)
+};
+
+// Routing graph on the device (one per land / river graph).
+struct WfDevGraph {
+    int64_t n_slots;
+    int64_t n_chunks;
+    int64_t n_chains;
+    int32_t G;
+    int32_t M;
+    const int64_t* chunk_base;
+    const int32_t* chunk_len;
+    const int32_t* chain_len;
+    const int32_t* up_ptr;
+    const int64_t* up_slot;
+    const int32_t* up_chain;
+    const uint8_t* is_chain_end;
+    uint32_t* flags;      // [n_chains * M] epoch of the last published sub-step
+    double* end_q;        // [n_chains * M * s_cap] q of each chain end per sub-step
+    unsigned long long* ticket;  // work counter of the current launch
+    int32_t s_cap;        // sub-steps per launch
+};
+
+// Sub-stepping of one routing sweep launch.
+struct WfSweep {
+    int32_t S;            // sub-steps in this launch
+    int32_t first;        // index of the first sub-step within the model step
+    int32_t last_of_step; // 1 when the launch ends the model step's sub-stepping
+    int32_t total;        // total sub-steps of the model step
+    uint32_t epoch0;      // epoch of sub-step 0 of this launch
+    double dt;            // model step
+    const double* dts;    // [S] sub-step sizes (device)
+    uint64_t wait_ns;     // spin-wait budget per wait [ns]
+    uint32_t wait_offset; // test hook: added to awaited epochs (0 in production)
+};
+
+// Device status codes (OR-ed bits)
+#define WF_DEV_SPIN_TIMEOUT 1
+#define WF_DEV_NONFINITE 2

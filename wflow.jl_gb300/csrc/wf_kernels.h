@@ -1,0 +1,38 @@
+// wf_kernels.h -- launchers of the step kernels (one set per arithmetic form).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "wf_fields.cuh"
+
+struct WfLaunchCfg {
+    cudaStream_t stream;
+    int num_sms;
+    int vertical_block;   // threads per block of per-cell kernels
+    int walk_warps;       // warps per block of wavefront kernels
+    int walk_blocks;      // blocks of the persistent wavefront grid (0 = occupancy)
+};
+
+// FP64 plain form (kernels_fp64.cu)
+cudaError_t wf_fp64_vertical(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_fp64_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_fp64_overland(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_fp64_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_fp64_balance(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_fp64_vwc(const WfDevFields& F, int layer, double* out, const WfLaunchCfg& c);
+// Courant sub-step of a kinematic-wave sweep (adaptive mode): writes dt to *dt_out.
+cudaError_t wf_fp64_stable_dt(const WfDevFields& F, int which /*0 land 1 river 2 ssf*/, double* scratch,
+                              int64_t* count, double* dt_out, const WfLaunchCfg& c);
+
+// FP32/FP64 split form (kernels_split.cu)
+cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_split_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_split_overland(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_split_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c);
+
+// gather/scatter between the external (land/river) order and the slot order
+cudaError_t wf_gather_ext(const double* src_ext, double* dst_slots, const int64_t* node_of_slot, int64_t slots,
+                          int M, int64_t n_ext, cudaStream_t s);
+cudaError_t wf_scatter_ext(const double* src_slots, double* dst_ext, const int64_t* node_of_slot, int64_t slots,
+                           int M, int64_t n_ext, cudaStream_t s);

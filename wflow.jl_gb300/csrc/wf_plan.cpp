@@ -1,0 +1,213 @@
+// wf_plan.cpp -- long-path chain decomposition and slot layout of a drainage forest.
+#include "wf_plan.h"
+
+#include <algorithm>
+#include <numeric>
+
+#include "wflow_gb300.h"
+
+int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& P, std::string& err) {
+    P = WfRoutingPlan();
+    P.n = n;
+    P.M = members < 1 ? 1 : members;
+    if (P.M <= 32) {
+        if ((P.M & (P.M - 1)) != 0) {
+            err = "members must be a power of two up to 32 or a multiple of 32";
+            return -1;
+        }
+        P.G = 32 / P.M;
+    } else {
+        if (P.M % 32 != 0) {
+            err = "members must be a power of two up to 32 or a multiple of 32";
+            return -1;
+        }
+        P.G = 1;
+    }
+    if (n == 0) {
+        P.chunk_base.assign(1, 0);
+        P.up_ptr.assign(1, 0);
+        return 0;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        if (ds[i] < -1 || ds[i] >= n || ds[i] == i) {
+            err = "downstream index out of range at node " + std::to_string(i);
+            return ds[i] == i ? WF_ERR_CYCLE : -1;
+        }
+    }
+    // children CSR (ascending node index)
+    std::vector<int32_t> indeg(n, 0);
+    for (int64_t i = 0; i < n; ++i)
+        if (ds[i] >= 0) indeg[ds[i]]++;
+    std::vector<int64_t> cptr(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) cptr[i + 1] = cptr[i] + indeg[i];
+    std::vector<int64_t> child(cptr[n]);
+    {
+        std::vector<int64_t> fill(cptr.begin(), cptr.end() - 1);
+        for (int64_t i = 0; i < n; ++i)
+            if (ds[i] >= 0) child[fill[ds[i]]++] = i;
+    }
+    // heights by Kahn order from the leaves
+    std::vector<int32_t> height(n, 0), left(indeg);
+    std::vector<int64_t> order;
+    order.reserve(n);
+    for (int64_t i = 0; i < n; ++i)
+        if (left[i] == 0) order.push_back(i);
+    for (size_t q = 0; q < order.size(); ++q) {
+        int64_t v = order[q];
+        int64_t d = ds[v];
+        if (d >= 0) {
+            if (height[v] + 1 > height[d]) height[d] = height[v] + 1;
+            if (--left[d] == 0) order.push_back(d);
+        }
+    }
+    if ((int64_t)order.size() != n) {
+        err = "cycle in drainage graph";
+        return WF_ERR_CYCLE;
+    }
+    // heavy child: highest child, ties to the lowest node index
+    std::vector<int64_t> heavy(n, -1);
+    for (int64_t v = 0; v < n; ++v) {
+        int64_t best = -1;
+        for (int64_t k = cptr[v]; k < cptr[v + 1]; ++k) {
+            int64_t u = child[k];
+            if (best < 0 || height[u] > height[best]) best = u;
+        }
+        heavy[v] = best;
+    }
+    // chains from every leaf
+    struct Chain {
+        int64_t start;
+        int32_t len;
+        int64_t end;
+    };
+    std::vector<Chain> chains;
+    for (int64_t v = 0; v < n; ++v) {
+        if (indeg[v] != 0) continue;
+        int64_t u = v;
+        int32_t len = 1;
+        while (ds[u] >= 0 && heavy[ds[u]] == u) {
+            u = ds[u];
+            ++len;
+        }
+        chains.push_back({v, len, u});
+    }
+    std::stable_sort(chains.begin(), chains.end(), [](const Chain& a, const Chain& b) {
+        return a.len != b.len ? a.len < b.len : a.end < b.end;
+    });
+    const int G = P.G;
+    const int64_t nc_real = (int64_t)chains.size();
+    P.n_chains = (nc_real + G - 1) / G * G;
+    P.n_chunks = P.n_chains / G;
+    P.chain_len.assign(P.n_chains, 0);
+    P.chunk_len.assign(P.n_chunks, 0);
+    P.chunk_base.assign(P.n_chunks + 1, 0);
+    for (int64_t c = 0; c < nc_real; ++c) P.chain_len[c] = chains[c].len;
+    for (int64_t k = 0; k < P.n_chunks; ++k) {
+        int32_t mx = 0;
+        for (int g = 0; g < G; ++g) mx = std::max(mx, P.chain_len[k * G + g]);
+        P.chunk_len[k] = mx;
+        P.chunk_base[k + 1] = P.chunk_base[k] + (int64_t)mx * G;
+        P.max_len = std::max(P.max_len, mx);
+    }
+    P.n_slots = P.chunk_base[P.n_chunks];
+    P.slot_of_node.assign(n, -1);
+    P.node_of_slot.assign(P.n_slots, -1);
+    P.chain_of_node.assign(n, -1);
+    P.is_chain_end.assign(P.n_slots, 0);
+    for (int64_t c = 0; c < nc_real; ++c) {
+        int64_t chunk = c / G, g = c % G;
+        int64_t u = chains[c].start;
+        for (int32_t k = 0; k < chains[c].len; ++k) {
+            int64_t s = P.chunk_base[chunk] + (int64_t)k * G + g;
+            P.slot_of_node[u] = s;
+            P.node_of_slot[s] = u;
+            P.chain_of_node[u] = (int32_t)c;
+            if (k == chains[c].len - 1) P.is_chain_end[s] = 1;
+            u = ds[u];
+        }
+    }
+    P.ds_slot.assign(P.n_slots, -1);
+    P.up_ptr.assign(P.n_slots + 1, 0);
+    for (int64_t s = 0; s < P.n_slots; ++s) {
+        int64_t v = P.node_of_slot[s];
+        P.up_ptr[s + 1] = P.up_ptr[s] + (v >= 0 ? (int32_t)(cptr[v + 1] - cptr[v]) : 0);
+        if (v >= 0 && ds[v] >= 0) P.ds_slot[s] = P.slot_of_node[ds[v]];
+    }
+    P.up_slot.resize(P.up_ptr[P.n_slots]);
+    P.up_chain.resize(P.up_ptr[P.n_slots]);
+    for (int64_t s = 0; s < P.n_slots; ++s) {
+        int64_t v = P.node_of_slot[s];
+        if (v < 0) continue;
+        int32_t o = P.up_ptr[s];
+        for (int64_t k = cptr[v]; k < cptr[v + 1]; ++k, ++o) {
+            int64_t u = child[k];
+            P.up_slot[o] = P.slot_of_node[u];
+            P.up_chain[o] = (u == heavy[v]) ? -1 : P.chain_of_node[u];
+        }
+    }
+    return 0;
+}
+
+bool wf_check_plan(const WfRoutingPlan& P, const int32_t* ds, std::string& err) {
+    const int G = P.G;
+    // position == height, chain lengths sorted
+    for (int64_t c = 1; c < P.n_chains; ++c) {
+        if (P.chain_len[c] != 0 && P.chain_len[c] < P.chain_len[c - 1]) {
+            err = "chains not sorted by length";
+            return false;
+        }
+    }
+    for (int64_t s = 0; s < P.n_slots; ++s) {
+        int64_t v = P.node_of_slot[s];
+        if (v < 0) continue;
+        int64_t chunk = 0;
+        while (P.chunk_base[chunk + 1] <= s) ++chunk;
+        int64_t k = (s - P.chunk_base[chunk]) / G;
+        int64_t my_chain = P.chain_of_node[v];
+        for (int32_t o = P.up_ptr[s]; o < P.up_ptr[s + 1]; ++o) {
+            int64_t us = P.up_slot[o];
+            int64_t u = P.node_of_slot[us];
+            if (u < 0 || ds[u] != v) {
+                err = "upstream list mismatch";
+                return false;
+            }
+            if (P.up_chain[o] < 0) {
+                if (us != s - G) {
+                    err = "heavy child is not the previous chain position";
+                    return false;
+                }
+            } else {
+                int64_t uc = P.up_chain[o];
+                if (!P.is_chain_end[us] || uc >= my_chain || P.chain_len[uc] > k) {
+                    err = "light child chain does not precede its consumer";
+                    return false;
+                }
+            }
+        }
+    }
+    return true;
+}
+
+extern "C" {
+
+// Host-only entry used by the tests: plan a graph and return its schedule summary.
+//   out_counts[0..3] = n_chains, n_chunks, n_slots, max_len
+//   slot_of_node[n] (may be null), ok = 1 when wf_check_plan passes.
+int32_t wf_plan_routing(int64_t n, const int32_t* downstream, int32_t members, int64_t* out_counts,
+                        int64_t* slot_of_node, int32_t* ok, int32_t* g_out) {
+    WfRoutingPlan P;
+    std::string err;
+    int rc = wf_build_plan(n, downstream, members, P, err);
+    if (rc != 0) return rc;
+    out_counts[0] = P.n_chains;
+    out_counts[1] = P.n_chunks;
+    out_counts[2] = P.n_slots;
+    out_counts[3] = P.max_len;
+    if (slot_of_node)
+        for (int64_t i = 0; i < n; ++i) slot_of_node[i] = P.slot_of_node[i];
+    *ok = wf_check_plan(P, downstream, err) ? 1 : 0;
+    *g_out = P.G;
+    return 0;
+}
+
+}  // extern "C"

@@ -209,11 +209,11 @@ def _declare(lib):
             f.argtypes = args
 
 
-def header_symbols():
-    """Entry points declared in include/*.h (names of functions starting with wf_)."""
+def header_symbols(header="wflow_gb300.h"):
+    """Entry points declared in an include/ header (names of functions starting with wf_)."""
     import re
     names = set()
-    for h in (REPO_ROOT / "include").glob("*.h"):
+    for h in [REPO_ROOT / "include" / header]:
         text = h.read_text()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         for m in re.finditer(r"\b(wf_[a-z0-9_]+)\s*\(", text):

@@ -87,7 +87,7 @@ def build_cuda(force=False, verbose=False):
     if verbose:
         for l in logs:
             print(l)
-    _run([nvcc, *ARCH, "-shared", "-o", str(LIB_PATH), *[str(o) for o in objs], "-lcudart"])
+    _run([nvcc, *ARCH, "-shared", "--cudart", "static", "-o", str(LIB_PATH), *[str(o) for o in objs]])
     return LIB_PATH
 
 

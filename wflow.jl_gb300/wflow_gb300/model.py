@@ -1,0 +1,127 @@
+"""Host mirror of Wflow.jl's model API on the hot path, over the C ABI.
+
+Names follow the reference so that a caller (and the tests) read like Wflow:
+  Model(config, domain)            Model(config) for the `sbm` hot-path state (sbm_model.jl:7-57)
+  model.update_model()             update_model! + compute_mass_balance! (sbm_model.jl:60-92,
+                                   mass_balance.jl:541-545) on the GPU
+  model.run_timestep(P, PET, T)    run_timestep! (Wflow.jl:311-322) with the forcing of the step
+  model.get_value / set_value      BMI get_value / set_value (bmi.jl:208-248)
+  model.save_state / load_state    BMI save_state / load_state (bmi.jl:357-371)
+Errors from the library raise RuntimeError with the library's message, like the reference's
+throw-and-log behaviour. There is no CPU fallback: without the CUDA library this module fails.
+"""
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi, synthetic
+
+
+class Model:
+    def __init__(self, config, domain, params=None, device=0):
+        self.lib = abi.load_library(required=True)
+        self.config = config
+        self.domain = domain
+        self._params = params if params is not None else domain.params
+        self._d, self._p = synthetic.c_structs(domain, self._params)
+        h = C.c_void_p()
+        st = self.lib.wf_create(C.byref(config), C.byref(self._d), C.byref(self._p), int(device), C.byref(h))
+        if st != abi.WF_OK:
+            msg = self.lib.wf_last_error(None)
+            raise RuntimeError(f"wf_create failed with status {st}: {msg.decode() if msg else ''}")
+        self.h = h
+        self.n = domain.n_land
+        self.nr = domain.n_river
+        self.M = max(1, config.n_members)
+        self.N = config.n_soil_layer_thickness + 1
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != abi.WF_OK:
+            msg = self.lib.wf_last_error(self.h)
+            raise RuntimeError(f"{what} failed with status {st}: {msg.decode() if msg else ''}")
+
+    # ---- stepping
+    def set_forcing(self, precipitation, potential_evaporation, temperature):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (precipitation, potential_evaporation, temperature)]
+        cnt = arrs[0].size
+        self._check(self.lib.wf_set_forcing(self.h, *[abi.as_ptr(a) for a in arrs], cnt), "wf_set_forcing")
+
+    def update_model(self):
+        self._check(self.lib.wf_step(self.h), "wf_step")
+
+    def run_timestep(self, precipitation, potential_evaporation, temperature):
+        self.set_forcing(precipitation, potential_evaporation, temperature)
+        self.update_model()
+
+    def step_async(self):
+        self._check(self.lib.wf_step_async(self.h), "wf_step_async")
+
+    def synchronize(self):
+        self._check(self.lib.wf_synchronize(self.h), "wf_synchronize")
+
+    # ---- BMI-like access
+    def get_value(self, field, layer=0, offset=0, count=None):
+        fid = abi.FIELD[field] if isinstance(field, str) else int(field)
+        total = (self.nr if abi.is_river_field(fid) else self.n) * self.M
+        count = total - offset if count is None else count
+        out = np.empty(count)
+        self._check(self.lib.wf_get_field(self.h, fid, layer, abi.as_ptr(out), offset, count), "wf_get_field")
+        return out
+
+    def set_value(self, field, values, layer=0, offset=0):
+        fid = abi.FIELD[field] if isinstance(field, str) else int(field)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self.lib.wf_set_field(self.h, fid, layer, abi.as_ptr(v), offset, v.size), "wf_set_field")
+
+    def outlets(self, which=0):
+        n_out = C.c_int64()
+        no = C.c_int64()
+        self.lib.wf_get_sizes(self.h, None, None, C.byref(no), None, None)
+        out = np.empty(max(1, no.value * self.M))
+        self._check(self.lib.wf_get_outlets(self.h, which, abi.as_ptr(out), out.size, C.byref(n_out)), "wf_get_outlets")
+        return out[: n_out.value].copy()
+
+    def save_state(self):
+        size = C.c_size_t(0)
+        self._check(self.lib.wf_get_state(self.h, None, C.byref(size)), "wf_get_state")
+        buf = (C.c_char * size.value)()
+        self._check(self.lib.wf_get_state(self.h, buf, C.byref(size)), "wf_get_state")
+        return bytes(buf)
+
+    def load_state(self, blob):
+        buf = C.create_string_buffer(blob, len(blob))
+        self._check(self.lib.wf_set_state(self.h, buf, len(blob)), "wf_set_state")
+
+    def metrics(self):
+        m = abi.WfMetrics()
+        self._check(self.lib.wf_get_metrics(self.h, C.byref(m)), "wf_get_metrics")
+        return {k: getattr(m, k) for k, _ in abi.WfMetrics._fields_}
+
+    def set_tuning(self, vertical_block=0, routing_warps=0, routing_blocks_per_sm=0, use_graph=1,
+                   wait_budget_us=0, wait_offset=0):
+        t = abi.WfTuning()
+        t.vertical_block, t.routing_warps, t.routing_blocks_per_sm, t.use_graph = (
+            vertical_block, routing_warps, routing_blocks_per_sm, use_graph)
+        t.reserved[0] = wait_budget_us
+        t.reserved[1] = wait_offset
+        self._check(self.lib.wf_set_tuning(self.h, C.byref(t)), "wf_set_tuning")
+
+    def slot_order(self):
+        ns = C.c_int64()
+        self.lib.wf_get_slot_order(self.h, None, 0, C.byref(ns))
+        out = np.empty(ns.value, np.int64)
+        self._check(self.lib.wf_get_slot_order(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)), out.size,
+                                               C.byref(ns)), "wf_get_slot_order")
+        return out
