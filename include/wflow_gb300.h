@@ -286,6 +286,14 @@ int32_t wf_set_tuning(WfHandle* h, const WfTuning* t);
 /* Slot order of the land layout: ext_of_slot[s] = land index of slot s, -1 for padding. */
 int32_t wf_get_slot_order(WfHandle* h, int64_t* ext_of_slot, int64_t capacity, int64_t* n_slots);
 
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or order their own work
+ * against the step. */
+int32_t wf_get_stream(WfHandle* h, void** stream);
+
+/* Per-kernel device time of the steps run with kernel timing on (WfTuning.reserved[2] = 1):
+ * ms[0..4] = vertical, subsurface, overland, river, balance (sums), calls = timed steps. */
+int32_t wf_get_kernel_times(WfHandle* h, double* ms5, int64_t* calls);
+
 /* Number of land cells, river cells, river pits and layer count of a handle. */
 int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_outlets,
                      int32_t* n_layers, int32_t* n_members);

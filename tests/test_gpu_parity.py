@@ -38,20 +38,35 @@ def rel_err(a, b):
     return r
 
 
+# Balance errors are differences of nearly equal totals: they are compared in absolute terms
+# against the scale of the fluxes that enter them.
+BALANCE_SCALE = {"BALANCE_LAND_ERROR": "ACTUAL_EVAPOTRANSPIRATION", "BALANCE_OVERLAND_ERROR": "LAND_Q_AVERAGE",
+                 "BALANCE_SUBSURFACE_ERROR": "SSF_Q_AVERAGE", "BALANCE_RIVER_ERROR": "RIVER_Q_AVERAGE"}
+
+
 def compare(gpu, orc, fields, layers=0):
     worst = {}
     exact = 0
     total = 0
+    inexact = {}
     for f in fields:
         fid = abi.FIELD[f]
         for k in (range(layers) if f in abi.LAYERED_FIELDS else [0]):
             g = gpu.get_value(fid, layer=k)
             o = orc.get(fid, layer=k)
-            r = rel_err(g, o)
-            worst[f if k == 0 else f"{f}[{k}]"] = float(r.max()) if r.size else 0.0
-            exact += int(np.sum((g == o) | (np.isnan(g) & np.isnan(o))))
+            name = f if k == 0 else f"{f}[{k}]"
+            if f in BALANCE_SCALE:
+                scale = np.max(np.abs(orc.get(abi.FIELD[BALANCE_SCALE[f]]))) + 1e-300
+                r = np.abs(g - o) / scale
+            else:
+                r = rel_err(g, o)
+            worst[name] = float(r.max()) if r.size else 0.0
+            eq = (g == o) | (np.isnan(g) & np.isnan(o))
+            exact += int(np.sum(eq))
             total += g.size
-    return worst, exact / max(total, 1)
+            if not eq.all():
+                inexact[name] = round(float(1.0 - eq.mean()), 5)
+    return worst, exact / max(total, 1), inexact
 
 
 def run_pair(dom, cfg, steps, seed=1, params=None, check_every=1, precip_scale=None):
@@ -76,10 +91,10 @@ def run_pair(dom, cfg, steps, seed=1, params=None, check_every=1, precip_scale=N
 
 
 def assert_parity(results, min_exact=0.999):
-    for worst, exact_frac in results:
+    for worst, exact_frac, inexact in results:
         bad = {k: v for k, v in worst.items() if v > RTOL}
-        assert not bad, bad
-        assert exact_frac >= min_exact, exact_frac
+        assert not bad, (bad, inexact)
+        assert exact_frac >= min_exact, (exact_frac, inexact)
 
 
 def test_daily_gash_64(gpu_lib):
@@ -112,7 +127,7 @@ def test_single_cell_and_no_river(gpu_lib):
     assert dom.n_river == 0
     cfg = synthetic.make_config(86400.0)
     gpu, orc, res = run_pair(dom, cfg, 5)
-    worst, _ = res[-1]
+    worst, _, _ = res[-1]
     assert all(v <= RTOL for v in worst.values()), worst
 
 

@@ -38,7 +38,7 @@ int32_t wf_synth_dem_d8(int32_t nx, int32_t ny, uint64_t seed, double scale_rati
                         double cell_size, double min_slope, double* dem, uint8_t* ldd,
                         int32_t* downstream, double* slope, int64_t* upstream_cells,
                         double* flow_length, double* flow_width) {
-    if (nx < 2 || ny < 2 || !(scale_ratio > 0.0) || !(cell_size > 0.0)) return -1;
+    if (nx < 1 || ny < 1 || !(scale_ratio > 0.0) || !(cell_size > 0.0)) return -1;
     // ---- diamond-square on a (2^k + 1) square grid
     int size = 2;
     while (size + 1 < nx || size + 1 < ny) size *= 2;

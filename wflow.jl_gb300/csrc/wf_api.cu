@@ -69,6 +69,10 @@ struct WfHandle {
     uint32_t wait_offset = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int64_t launches_per_step = 0;
+    bool kernel_timing = false;
+    cudaEvent_t kev[6] = {};
+    double kernel_ms[5] = {0, 0, 0, 0, 0};
+    int64_t kernel_calls = 0;
 };
 
 namespace {
@@ -411,6 +415,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     }
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
+    for (auto& e : h->kev) cudaEventCreate(&e);
     const int64_t n = h->n, nr = h->nr;
     // river indices
     for (int64_t r = 0; r < nr; ++r) {
@@ -673,6 +678,8 @@ void wf_destroy(WfHandle* h) {
     if (h->host_pinned) cudaFreeHost(h->host_pinned);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    for (auto& e : h->kev)
+        if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -879,6 +886,7 @@ int32_t wf_set_tuning(WfHandle* h, const WfTuning* t) {
     // test hooks in reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset
     if (t->reserved[0] > 0) h->wait_ns = (uint64_t)t->reserved[0] * 1000ull;
     h->wait_offset = (uint32_t)t->reserved[1];
+    h->kernel_timing = t->reserved[2] != 0;
     return WF_OK;
 }
 
@@ -889,6 +897,20 @@ int32_t wf_get_slot_order(WfHandle* h, int64_t* ext_of_slot, int64_t capacity, i
         if (capacity < *n_slots) return set_err(h, WF_ERR_INVALID, "capacity too small");
         for (int64_t s = 0; s < *n_slots; ++s) ext_of_slot[s] = h->land.plan.node_of_slot[s];
     }
+    return WF_OK;
+}
+
+int32_t wf_get_stream(WfHandle* h, void** stream) {
+    if (!h || !stream) return WF_ERR_INVALID;
+    *stream = (void*)h->stream;
+    return WF_OK;
+}
+
+int32_t wf_get_kernel_times(WfHandle* h, double* ms5, int64_t* calls) {
+    if (!h || !ms5) return WF_ERR_INVALID;
+    CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 5; ++k) ms5[k] = h->kernel_ms[k];
+    if (calls) *calls = h->kernel_calls;
     return WF_OK;
 }
 
@@ -913,8 +935,14 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
     const bool split = h->cfg.form == WF_FORM_SPLIT;
     int64_t nl = 0;
     WfDevGraph gl = dev_graph(h->land, h->M), gr = dev_graph(h->river, h->M);
+    const bool timing = h->kernel_timing && !h->tuning.use_graph;
+    auto mark = [&](int i) {
+        if (timing) cudaEventRecord(h->kev[i], h->stream);
+    };
+    mark(0);
     CK(split ? wf_split_vertical(h->F, lc) : wf_fp64_vertical(h->F, lc));
     ++nl;
+    mark(1);
     auto sweep = [&](DevGraphAlloc& G, const WfDevGraph& g, const std::vector<double>& dts, double* d_dts,
                      int which) -> int {
         const int total = (int)dts.size();
@@ -942,10 +970,23 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
     };
     int rc;
     if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;
+    mark(2);
     if ((rc = sweep(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
+    mark(3);
     if (h->nr > 0 && (rc = sweep(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
+    mark(4);
     CK(split ? wf_split_balance(h->F, lc) : wf_fp64_balance(h->F, lc));
     ++nl;
+    mark(5);
+    if (timing) {
+        CK(cudaEventSynchronize(h->kev[5]));
+        for (int k = 0; k < 5; ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, h->kev[k], h->kev[k + 1]);
+            h->kernel_ms[k] += ms;
+        }
+        h->kernel_calls += 1;
+    }
     if (launches) *launches = nl;
     return WF_OK;
 }

@@ -1,0 +1,228 @@
+"""
+    WflowGB300
+
+Julia side of the GB300 drop-in for Wflow.jl's `sbm` hot path. It binds the C ABI of
+`libwflow_gb300.so` (include/wflow_gb300.h) with `ccall` and plugs into the reference's own
+seam, `Wflow.run_timestep!(model; update_func = ...)` (Wflow/src/Wflow.jl:311-322):
+
+    using Wflow, WflowGB300
+    model = Wflow.Model(Wflow.Config("sbm_config.toml"))
+    gpu = WflowGB300.GpuStep(model)                 # uploads domain, parameters, state
+    Wflow.load_fixed_forcing!(model)
+    for t in 1:nsteps
+        Wflow.run_timestep!(model; update_func = m -> WflowGB300.gpu_update_model!(gpu, m))
+    end
+
+`gpu_update_model!` replaces `update_model!` (Wflow/src/sbm_model.jl:60-92) and
+`compute_mass_balance!` (Wflow/src/mass_balance.jl:541-545): it uploads the step's
+`AtmosphericForcing`, runs one step on the GPU and refreshes the host mirrors that BMI
+`get_value_ptr` hands out (Wflow/src/bmi.jl:208-228). Errors come back as a negative status
+and are rethrown as Julia exceptions with the library's message, like Wflow's own
+throw-and-log path (Wflow/src/Wflow.jl:285-299).
+"""
+module WflowGB300
+
+using Wflow
+
+const LIB = get(ENV, "WFLOW_GB300_LIB", joinpath(@__DIR__, "..", "_build", "libwflow_gb300.so"))
+const WF_MAX_LAYERS = 8
+
+# ---- C structs (layout of include/wflow_gb300.h) --------------------------------------------
+struct WfConfig
+    dt::Float64
+    n_soil_layer_thickness::Int32
+    snow::Int32
+    soil_layer_thickness::NTuple{7, Float64}
+    soil_infiltration_reduction::Int32
+    water_mass_balance::Int32
+    adaptive_timestep::Int32
+    kv_profile::Int32
+    land_dt_fixed::Float64
+    river_dt_fixed::Float64
+    subsurface_dt_fixed::Float64
+    subsurface_alpha::Float64
+    form::Int32
+    n_members::Int32
+    per_member_soil::Int32
+    reserved::NTuple{7, Int32}
+end
+
+struct WfDomain
+    n_land::Int64
+    land_downstream::Ptr{Int32}
+    area::Ptr{Float64}
+    flow_width::Ptr{Float64}
+    flow_length::Ptr{Float64}
+    surface_flow_width::Ptr{Float64}
+    slope::Ptr{Float64}
+    flow_fraction_to_river::Ptr{Float64}
+    river_fraction::Ptr{Float64}
+    water_fraction::Ptr{Float64}
+    elevation::Ptr{Float64}
+    land_manning_n::Ptr{Float64}
+    n_river::Int64
+    river_land_index::Ptr{Int32}
+    river_downstream::Ptr{Int32}
+    river_width::Ptr{Float64}
+    river_length::Ptr{Float64}
+    river_slope::Ptr{Float64}
+    river_manning_n::Ptr{Float64}
+    river_bankfull_depth::Ptr{Float64}
+    river_external_inflow::Ptr{Float64}
+end
+
+const PARAM_NAMES = (:canopy_gap_fraction, :maximum_canopy_storage, :crop_coefficient, :rooting_depth,
+    :evaporation_to_precipitation_ratio, :degree_day_factor, :temperature_threshold_snowfall,
+    :temperature_interval_snowfall, :temperature_threshold_melt, :water_holding_capacity, :theta_s,
+    :theta_r, :kv_0, :f, :soil_thickness, :air_entry_pressure, :h1, :h2, :h3_high, :h3_low, :h4,
+    :alpha_h1, :infiltration_capacity_compacted_soil, :compacted_soil_area_fraction,
+    :wet_root_distribution_parameter, :cap_hmax, :cap_n, :maximum_leakage, :w_soil, :cf_soil, :z_exp,
+    :brooks_corey_exponent, :kv_factor, :horizontal_to_vertical_ratio)
+
+struct WfParams
+    ptrs::NTuple{34, Ptr{Float64}}
+end
+
+# WfField ids (enum WfField)
+const F_LAND = (:canopy_storage, :snow_storage, :snow_water, :soil_surface_temperature,
+    :saturated_water_depth, :unsaturated_layer_depth, :ssf_q, :land_q, :land_h, :water_table_depth)
+const F_RIVER_Q = Int32(100)
+const F_RIVER_H = Int32(101)
+const F_RIVER_Q_AVERAGE = Int32(103)
+
+mutable struct GpuStep
+    handle::Ptr{Cvoid}
+    keep::Vector{Any}              # arrays whose pointers were handed to wf_create
+    n_land::Int
+    n_river::Int
+    forcing::NTuple{3, Vector{Float64}}
+end
+
+check(st, h, what) = st == 0 || error("$what failed ($st): " *
+                                      unsafe_string(ccall((:wf_last_error, LIB), Cstring, (Ptr{Cvoid},), h)))
+
+"Downstream index of every node of a Graphs.jl D8 flow graph (-1 for a pit), 0-based."
+function downstream_index(graph)
+    n = Wflow.Graphs.nv(graph)
+    ds = fill(Int32(-1), n)
+    for v in 1:n
+        out = Wflow.Graphs.outneighbors(graph, v)
+        isempty(out) || (ds[v] = Int32(only(out) - 1))
+    end
+    return ds
+end
+
+"""
+    GpuStep(model::Wflow.Model)
+
+Copy the model's domain, parameters (as read from the static maps, in SI) and current state
+to a new library handle (`wf_create`, then `wf_set_field` for a warm state).
+"""
+function GpuStep(model)
+    (; domain, land, routing, config) = model
+    lp = domain.land.parameters
+    rp = domain.river.parameters
+    soil = land.soil.parameters
+    veg = soil.vegetation_parameter_set
+    keep = Any[]
+    k(x) = (push!(keep, x); pointer(x))
+    ds_land = downstream_index(domain.land.network.graph)
+    ds_river = downstream_index(domain.river.network.graph)
+    nl = length(config.model.soil_layer__thickness)
+    thick = ntuple(i -> i <= nl ? config.model.soil_layer__thickness[i] / 1000.0 : 0.0, 7)
+    cfg = WfConfig(tosecond(model.clock.dt), Int32(nl), Int32(config.model.snow__flag), thick,
+        Int32(config.model.soil_infiltration_reduction__flag), Int32(config.model.water_mass_balance__flag),
+        Int32(config.model.kinematic_wave__adaptive_time_step_flag), Int32(0),
+        config.model.land_kinematic_wave__time_step, config.model.river_kinematic_wave__time_step,
+        config.model.subsurface_kinematic_wave__time_step,
+        config.model.subsurface_kinematic_wave__alpha_coefficient, Int32(0), Int32(1), Int32(0),
+        ntuple(_ -> Int32(0), 7))
+    land_n = routing.overland_flow.parameters.mannings_n
+    dom = WfDomain(length(ds_land), k(ds_land), k(lp.area), k(lp.flow_width), k(lp.flow_length),
+        k(lp.surface_flow_width), k(lp.slope), k(lp.flow_fraction_to_river), k(lp.river_fraction),
+        k(lp.water_fraction), k(routing.subsurface_flow.parameters.top), k(land_n), length(ds_river),
+        k(Int32.(domain.river.network.land_indices .- 1)), k(ds_river), k(rp.flow_width), k(rp.flow_length),
+        k(rp.slope), k(routing.river_flow.parameters.mannings_n),
+        k(routing.river_flow.parameters.bankfull_depth),
+        k(routing.river_flow.boundary_conditions.external_inflow))
+    layered(v) = collect(Iterators.flatten(v))
+    # static parameters as read (before derivation), see WfParams in the header
+    src = Dict{Symbol, Vector{Float64}}(
+        :canopy_gap_fraction => veg.canopy_gap_fraction, :maximum_canopy_storage => veg.maximum_canopy_storage,
+        :crop_coefficient => veg.crop_coefficient, :rooting_depth => veg.rooting_depth,
+        :theta_s => soil.theta_s, :theta_r => soil.theta_r, :kv_0 => soil.kv_profile.kv_0,
+        :f => soil.kv_profile.hydraulic_conductivity_scale_parameter, :soil_thickness => soil.soil_thickness,
+        :air_entry_pressure => soil.air_entry_pressure, :h1 => soil.h1, :h2 => soil.h2,
+        :h3_high => soil.h3_high, :h3_low => soil.h3_low, :h4 => soil.h4, :alpha_h1 => soil.alpha_h1,
+        :infiltration_capacity_compacted_soil => soil.infiltration_capacity_compacted_soil,
+        :compacted_soil_area_fraction => soil.compacted_soil_area_fraction,
+        :wet_root_distribution_parameter => soil.wet_root_distribution_parameter,
+        :cap_hmax => soil.cap_hmax, :cap_n => soil.cap_n, :maximum_leakage => soil.maximum_leakage,
+        :w_soil => soil.w_soil, :cf_soil => soil.cf_soil,
+        :brooks_corey_exponent => layered(soil.brooks_corey_exponent),
+        :kv_factor => layered(soil.vertical_hydraulic_conductivity_factor),
+        :horizontal_to_vertical_ratio =>
+            routing.subsurface_flow.parameters.horizontal_to_vertical_hydraulic_conductivity_ratio)
+    if config.model.snow__flag
+        sp = land.snow.parameters
+        src[:degree_day_factor] = sp.degree_day_factor
+        src[:temperature_threshold_snowfall] = sp.temperature_threshold_snowfall
+        src[:temperature_interval_snowfall] = sp.temperature_interval_snowfall
+        src[:temperature_threshold_melt] = sp.temperature_threshold_melt
+        src[:water_holding_capacity] = sp.water_holding_capacity
+    end
+    params = WfParams(ntuple(i -> haskey(src, PARAM_NAMES[i]) ? k(src[PARAM_NAMES[i]]) : Ptr{Float64}(0), 34))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:wf_create, LIB), Int32, (Ref{WfConfig}, Ref{WfDomain}, Ref{WfParams}, Int32, Ref{Ptr{Cvoid}}),
+        cfg, dom, params, Int32(0), h)
+    check(st, C_NULL, "wf_create")
+    n = length(ds_land)
+    gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)))
+    finalizer(g -> ccall((:wf_destroy, LIB), Cvoid, (Ptr{Cvoid},), g.handle), gpu)
+    return gpu
+end
+
+"""
+    gpu_update_model!(gpu::GpuStep, model)
+
+`update_func` for `Wflow.run_timestep!`: one update_model! + compute_mass_balance! on the GPU.
+"""
+function gpu_update_model!(gpu::GpuStep, model)
+    f = model.land.atmospheric_forcing
+    st = ccall((:wf_set_forcing, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+        gpu.handle, f.precipitation, f.potential_evaporation, f.temperature, gpu.n_land)
+    check(st, gpu.handle, "wf_set_forcing")
+    check(ccall((:wf_step, LIB), Int32, (Ptr{Cvoid},), gpu.handle), gpu.handle, "wf_step")
+    sync_mirrors!(gpu, model)
+    return nothing
+end
+
+"Copy a library field into a host vector (BMI get_value semantics)."
+function get_field!(dst::Vector{Float64}, gpu::GpuStep, field::Integer; layer::Integer = 0)
+    st = ccall((:wf_get_field, LIB), Int32, (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}, Int64, Int64),
+        gpu.handle, Int32(field), Int32(layer), dst, 0, length(dst))
+    check(st, gpu.handle, "wf_get_field")
+    return dst
+end
+
+"Write a host vector into a library state field (BMI set_value semantics)."
+function set_field!(gpu::GpuStep, field::Integer, src::Vector{Float64}; layer::Integer = 0)
+    st = ccall((:wf_set_field, LIB), Int32, (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}, Int64, Int64),
+        gpu.handle, Int32(field), Int32(layer), src, 0, length(src))
+    check(st, gpu.handle, "wf_set_field")
+end
+
+"Refresh the host vectors Wflow's BMI and writers read after a GPU step."
+function sync_mirrors!(gpu::GpuStep, model)
+    (; routing) = model
+    get_field!(routing.river_flow.variables.q, gpu, F_RIVER_Q)
+    get_field!(routing.river_flow.variables.h, gpu, F_RIVER_H)
+    get_field!(routing.river_flow.variables.q_average, gpu, F_RIVER_Q_AVERAGE)
+    get_field!(routing.overland_flow.variables.q, gpu, 7)
+    get_field!(routing.overland_flow.variables.h, gpu, 8)
+    get_field!(routing.subsurface_flow.variables.q, gpu, 6)
+    get_field!(model.land.soil.variables.saturated_water_depth, gpu, 4)
+    return nothing
+end
+
+end # module

@@ -199,6 +199,8 @@ def _declare(lib):
         f.restype = res
         f.argtypes = args
     extra = {
+        "wf_get_stream": (_i32, [H, C.POINTER(C.c_void_p)]),
+        "wf_get_kernel_times": (_i32, [H, _pd, C.POINTER(_i64)]),
         "wf_struct_size": (_i32, [_i32]),
         "wf_plan_routing": (_i32, [_i64, _pi32, _i32, C.POINTER(_i64), C.POINTER(_i64), _pi32, _pi32]),
     }

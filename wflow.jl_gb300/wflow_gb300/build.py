@@ -79,7 +79,7 @@ def build_cuda(force=False, verbose=False):
             cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-c", "-ffp-contract=off", *inc,
                    "-I", "/usr/local/cuda/include", "-o", str(obj), str(src)]
         else:
-            cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                    "-Xptxas", "-v" if verbose else "-O3", *extra, *inc, "-c", "-o", str(obj), str(src)]
         cmds.append(cmd)
     with ThreadPoolExecutor(max_workers=len(cmds)) as ex:

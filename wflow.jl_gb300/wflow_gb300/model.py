@@ -110,13 +110,29 @@ class Model:
         return {k: getattr(m, k) for k, _ in abi.WfMetrics._fields_}
 
     def set_tuning(self, vertical_block=0, routing_warps=0, routing_blocks_per_sm=0, use_graph=1,
-                   wait_budget_us=0, wait_offset=0):
+                   wait_budget_us=0, wait_offset=0, kernel_timing=0):
         t = abi.WfTuning()
         t.vertical_block, t.routing_warps, t.routing_blocks_per_sm, t.use_graph = (
             vertical_block, routing_warps, routing_blocks_per_sm, use_graph)
         t.reserved[0] = wait_budget_us
         t.reserved[1] = wait_offset
+        t.reserved[2] = kernel_timing
         self._check(self.lib.wf_set_tuning(self.h, C.byref(t)), "wf_set_tuning")
+
+    def stream(self):
+        s = C.c_void_p()
+        self._check(self.lib.wf_get_stream(self.h, C.byref(s)), "wf_get_stream")
+        return s.value
+
+    def kernel_times(self):
+        ms = np.zeros(5)
+        calls = C.c_int64()
+        self._check(self.lib.wf_get_kernel_times(self.h, abi.as_ptr(ms), C.byref(calls)), "wf_get_kernel_times")
+        return dict(zip(["vertical", "subsurface", "overland", "river", "balance"], ms.tolist())), calls.value
+
+    def set_forcing_device_slots(self, p_ptr, pet_ptr, t_ptr):
+        self._check(self.lib.wf_set_forcing_device_slots(self.h, C.c_void_p(p_ptr), C.c_void_p(pet_ptr),
+                                                         C.c_void_p(t_ptr)), "wf_set_forcing_device_slots")
 
     def slot_order(self):
         ns = C.c_int64()
