@@ -166,6 +166,12 @@ def run_gpu(args):
             bufs.append(torch.from_numpy(slot_arr.reshape(-1)).to(dev))
         resident.append(bufs)
     torch.cuda.synchronize()
+    tuning = None
+    if not args.no_autotune:
+        from wflow_gb300 import autotune
+        t0 = time.time()
+        tuning, _ = autotune.tune(model, lambda s: member_forcing(10_000 + s, dt, n, members, pfac, seed=args.seed))
+        log(f"[bench] autotune {tuning} in {time.time() - t0:.1f}s")
     stream = torch.cuda.ExternalStream(model.stream(), device=dev)
     m0 = model.metrics()
     for s in range(W):
@@ -231,7 +237,7 @@ def run_gpu(args):
         e2e_s = float(t.item())
     e2e_value = cells * K * ws / e2e_s
     # ---- per-kernel times (eager launches with events between kernels) for the roofline
-    model.set_tuning(use_graph=0, kernel_timing=1)
+    model.set_tuning(**(tuning or {}), use_graph=0, kernel_timing=1)
     for s in range(min(K, 5)):
         b = resident[W + s]
         model.set_forcing_device_slots(b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr())
@@ -258,7 +264,8 @@ def run_gpu(args):
                                                                "subsurface": 1},
                    "l2": "state 1.2 GB per 1M cells >> 129 MB L2, no flush needed",
                    "chains_land": mt["n_chains_land"], "max_chain_land": mt["max_chain_land"],
-                   "max_chain_river": mt["max_chain_river"], "parallelism": f"replicas{ws}"},
+                   "max_chain_river": mt["max_chain_river"], "parallelism": f"replicas{ws}",
+                   "tuning": tuning},
         "e2e": {"value": e2e_value, "unit": "cell-timesteps/s", "h2d_bytes_per_step": 3 * 8 * cells,
                 "d2h_bytes_per_step": 8 * n_out},
         "gpu_launches": int(launches),
@@ -370,6 +377,7 @@ def main():
     ap.add_argument("--workload", default="single_1024_hourly", choices=list(WORKLOADS))
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

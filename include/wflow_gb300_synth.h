@@ -15,13 +15,14 @@
 extern "C" {
 #endif
 
-/* Fractal DEM (diamond-square with amplitude ratio `scale_ratio` = 2^-H per level) rescaled to
- * [0, zmax], priority-flood pit filling with an epsilon gradient towards the single outlet at
+/* Fractal DEM (diamond-square with amplitude ratio `scale_ratio` = 2^-H per level) plus a plane
+ * dipping to the outlet corner with `tilt` times the fractal relief, rescaled to [0, zmax],
+ * priority-flood pit filling with an epsilon gradient towards the single outlet at
  * cell (0, 0), D8 steepest descent (PCRaster codes 1-9), downstream index (-1 at the outlet),
  * slope (>= min_slope), upstream cell counts (including the cell). Cell index = y * nx + x.
  * Returns 0 on success. */
 int32_t wf_synth_dem_d8(int32_t nx, int32_t ny, uint64_t seed, double scale_ratio, double zmax,
-                        double cell_size, double min_slope, double* dem, uint8_t* ldd,
+                        double cell_size, double min_slope, double tilt, double* dem, uint8_t* ldd,
                         int32_t* downstream, double* slope, int64_t* upstream_cells,
                         double* flow_length, double* flow_width);
 

@@ -205,3 +205,62 @@ def test_set_value_and_get_value_at_indices(gpu_lib):
     assert np.array_equal(w[:5], v[5:10])
     with pytest.raises(RuntimeError):
         m.set_value("RECHARGE", v[:3])
+
+
+# ---------------------------------------------------------------- split form ----------
+def split_errors(dom, cfg_split, steps, seed=1, params=None, precip_scale=None):
+    """Run the split form and the FP64 oracle side by side; return the worst relative errors
+    of outlet discharge, per-cell discharge and storages, and the split form's own worst
+    relative balance closure."""
+    import copy
+    cfg64 = copy.copy(cfg_split)
+    cfg64.form = abi.WF_FORM_FP64
+    gpu = Model(cfg_split, dom, params=params)
+    orc = O.OracleModel(cfg64, dom, params=params)
+    M = max(1, cfg_split.n_members)
+    worst = {"outlet_q": 0.0, "river_q": 0.0, "soil_storage": 0.0, "snow_storage": 0.0, "closure": 0.0}
+    for s in range(steps):
+        P, PET, T = synthetic.forcing(s, cfg_split.dt, dom.n_land, seed=seed)
+        if M > 1:
+            scale = precip_scale if precip_scale is not None else np.ones(M)
+            P = np.concatenate([P * scale[m] for m in range(M)])
+            PET, T = np.tile(PET, M), np.tile(T, M)
+        gpu.run_timestep(P, PET, T)
+        orc.set_forcing(P, PET, T)
+        orc.step()
+        qo, qg = orc.outlets(0), gpu.outlets(0)
+        worst["outlet_q"] = max(worst["outlet_q"], float(np.max(np.abs(qg - qo) / np.maximum(np.abs(qo), 1e-12))))
+        rq_o, rq_g = orc.get(abi.FIELD["RIVER_Q"]), gpu.get_value("RIVER_Q")
+        big = rq_o > 1e-3 * rq_o.max()
+        worst["river_q"] = max(worst["river_q"], float(np.max(np.abs(rq_g - rq_o)[big] / rq_o[big])))
+        so, sg = orc.get(abi.FIELD["TOTAL_SOIL_WATER_STORAGE"]), gpu.get_value("TOTAL_SOIL_WATER_STORAGE")
+        worst["soil_storage"] = max(worst["soil_storage"], float(np.max(np.abs(sg - so) / so)))
+        wo, wg = orc.get(abi.FIELD["SNOW_STORAGE"]), gpu.get_value("SNOW_STORAGE")
+        wbig = wo > 1e-4
+        if wbig.any():
+            worst["snow_storage"] = max(worst["snow_storage"], float(np.max(np.abs(wg - wo)[wbig] / wo[wbig])))
+        rel = np.abs(gpu.get_value("BALANCE_LAND_RELATIVE_ERROR"))
+        worst["closure"] = max(worst["closure"], float(rel.max()))
+    return worst
+
+
+def test_split_form_accuracy_daily(gpu_lib):
+    dom = synthetic.make_domain(48, 1000.0, seed=12)
+    cfg = synthetic.make_config(86400.0, form=abi.WF_FORM_SPLIT)
+    w = split_errors(dom, cfg, 40)
+    print("split daily errors", w)
+    assert w["outlet_q"] <= 1e-4, w
+    assert w["soil_storage"] <= 1e-4, w
+    assert w["closure"] <= 1e-7, w
+
+
+def test_split_form_accuracy_hourly_ensemble(gpu_lib):
+    dom = synthetic.make_domain(32, 250.0, seed=13)
+    M = 32
+    kv0, f, pfac = synthetic.perturb_members(dom.params, M, seed=13)
+    params = dict(dom.params, kv_0=kv0, f=f)
+    cfg = synthetic.make_config(3600.0, n_members=M, form=abi.WF_FORM_SPLIT, per_member_soil=True)
+    w = split_errors(dom, cfg, 48, params=params, precip_scale=pfac)
+    print("split hourly ensemble errors", w)
+    assert w["outlet_q"] <= 1e-4, w
+    assert w["closure"] <= 1e-7, w

@@ -185,8 +185,12 @@ __device__ void kinematic_wave(double q_in, double q_prev, double q_lat, double 
         const double fu = u3 * (dt_dx * u2 + alpha) - cterm;
         if (wfm::fabs_(fu) <= 1.0e-12) break;
         const double df = u2 * (c1 * u2 + c2);
+        const double u_old = u;
         u -= fu / df;
         if (wfm::isnan_(u) || u <= 0.0) u = KIN_WAVE_MIN_FLOW_QROOT;
+        // an iterate that no longer changes repeats itself until max_iters: stop here with the
+        // identical result (e.g. no positive root when the lateral inflow is negative)
+        if (u == u_old) break;
     }
     u = jmax(u, KIN_WAVE_MIN_FLOW_QROOT);
     const double u3 = u * u * u;
@@ -312,10 +316,12 @@ __device__ double kw_ssf_newton(double q, double cterm, double celerity, double 
     const double df = dt_dx + cinv;
     while (true) {
         const double fq = dt_dx * q + cinv * q - cterm;
+        const double q_old = q;
         q -= (fq / df);
         if (wfm::isnan_(q)) q = 0.0;
         q = jmax(q, KIN_WAVE_MIN_FLOW);
         if ((wfm::fabs_(fq) <= 1.0e-12) || (count >= 3000)) break;
+        if (q == q_old) break;  // fixed point: the remaining iterations repeat this one
         count += 1;
     }
     return q;
@@ -944,7 +950,8 @@ __global__ void __launch_bounds__(256) balance_kernel(WfDevFields F) {
         double err, rel;
         // land hydrology balance (mass_balance.jl:215-253)
         {
-            const double tin = Mf[SSF_QIN_AVG][e] / area + (Mf[PRECIP][e] + 0.0) + 0.0 + 0.0 / area;
+            const double Pv = F.split ? (double)F.Mh[PRECIP][e] : Mf[PRECIP][e];
+            const double tin = Mf[SSF_QIN_AVG][e] / area + (Pv + 0.0) + 0.0 + 0.0 / area;
             const double vout = Mf[NET_RUNOFF][e] + Mf[AET][e] + Mf[NET_RUNOFF_RIVER][e] + Mf[LEAKAGE][e] + 0.0;
             const double tout = Mf[SSF_Q_AVG][e] / area + vout + 0.0 + 0.0 / area;
             const double storage = Mf[TSWS][e] + canopy + (snow + sw) + 0.0 * 0.0 + 0.0;

@@ -35,7 +35,7 @@ extern "C" {
 // Returns 0 on success, -1 on bad arguments.
 //   hurst in (0, 1]; scale_ratio = 2^-hurst must be given by the caller (no pow here).
 int32_t wf_synth_dem_d8(int32_t nx, int32_t ny, uint64_t seed, double scale_ratio, double zmax,
-                        double cell_size, double min_slope, double* dem, uint8_t* ldd,
+                        double cell_size, double min_slope, double tilt, double* dem, uint8_t* ldd,
                         int32_t* downstream, double* slope, int64_t* upstream_cells,
                         double* flow_length, double* flow_width) {
     if (nx < 1 || ny < 1 || !(scale_ratio > 0.0) || !(cell_size > 0.0)) return -1;
@@ -72,18 +72,28 @@ int32_t wf_synth_dem_d8(int32_t nx, int32_t ny, uint64_t seed, double scale_rati
             }
         }
     }
-    // crop and rescale to [0, zmax]
+    // crop, add the regional plane dipping to the outlet corner (relative weight `tilt` of the
+    // fractal relief) and rescale to [0, zmax]
     const int64_t n = (int64_t)nx * ny;
-    double lo = 1e300, hi = -1e300;
+    double flo = 1e300, fhi = -1e300;
     for (int y = 0; y < ny; ++y)
         for (int x = 0; x < nx; ++x) {
             double v = H(x, y);
+            flo = v < flo ? v : flo;
+            fhi = v > fhi ? v : fhi;
+        }
+    const double relief = fhi - flo > 0.0 ? fhi - flo : 1.0;
+    const double diag_len = (double)(nx - 1) + (double)(ny - 1) > 0.0 ? (double)(nx - 1) + (double)(ny - 1) : 1.0;
+    double lo = 1e300, hi = -1e300;
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+            double v = H(x, y) + tilt * relief * ((double)x + (double)y) / diag_len;
+            dem[(int64_t)y * nx + x] = v;
             lo = v < lo ? v : lo;
             hi = v > hi ? v : hi;
         }
     double span = hi - lo > 0.0 ? hi - lo : 1.0;
-    for (int y = 0; y < ny; ++y)
-        for (int x = 0; x < nx; ++x) dem[(int64_t)y * nx + x] = (H(x, y) - lo) / span * zmax;
+    for (int64_t i = 0; i < n; ++i) dem[i] = (dem[i] - lo) / span * zmax;
     // ---- priority-flood + epsilon from the single outlet at (0, 0)
     const double eps = 1e-5;
     std::vector<uint8_t> seen(n, 0);

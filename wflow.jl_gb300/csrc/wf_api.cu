@@ -123,6 +123,22 @@ int upload_slots(WfHandle* h, double** dst, const std::vector<double>& ext, cons
     return upload(h, dst, v);
 }
 
+// FP32 copy of an external-order array in slot layout (split form).
+int upload_slots_f32(WfHandle* h, float** dst, const std::vector<double>& ext, const WfRoutingPlan& P, int M,
+                     int64_t n_ext, bool per_member) {
+    std::vector<float> v((size_t)P.n_slots * (per_member ? M : 1), 0.0f);
+    for (int64_t s = 0; s < P.n_slots; ++s) {
+        int64_t node = P.node_of_slot[s];
+        if (node < 0) continue;
+        if (per_member) {
+            for (int m = 0; m < M; ++m) v[s * M + m] = (float)ext[(size_t)m * n_ext + node];
+        } else {
+            v[s] = (float)ext[node];
+        }
+    }
+    return upload(h, dst, v);
+}
+
 int plan_graph(WfHandle* h, DevGraphAlloc& G, int64_t n, const int32_t* ds, int M, int32_t s_cap) {
     std::string err;
     int rc = wf_build_plan(n, ds, M, G.plan, err);
@@ -210,6 +226,39 @@ __global__ void scatter_kernel(const double* src, double* dst, const int64_t* no
         if (node >= 0) dst[(int64_t)m * n_ext + node] = src[e];
     }
 }
+__global__ void gather_f32_kernel(const double* src, float* dst, const int64_t* node_of_slot, int64_t slots, int M,
+                                  int64_t n_ext) {
+    const int64_t E = slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / M;
+        const int m = (int)(e - s * M);
+        const int64_t node = node_of_slot[s];
+        if (node >= 0) dst[e] = (float)src[(int64_t)m * n_ext + node];
+    }
+}
+__global__ void scatter_f32_kernel(const float* src, double* dst, const int64_t* node_of_slot, int64_t slots, int M,
+                                   int64_t n_ext) {
+    const int64_t E = slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / M;
+        const int m = (int)(e - s * M);
+        const int64_t node = node_of_slot[s];
+        if (node >= 0) dst[(int64_t)m * n_ext + node] = (double)src[e];
+    }
+}
+__global__ void to_f32_kernel(const double* src, float* dst, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+__global__ void broadcast_member_f32_kernel(const double* src, float* dst, const int64_t* node_of_slot, int64_t slots,
+                                            int M) {
+    const int64_t E = slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / M;
+        const int64_t node = node_of_slot[s];
+        if (node >= 0) dst[e] = (float)src[node];
+    }
+}
 __global__ void broadcast_member_kernel(const double* src, double* dst, const int64_t* node_of_slot, int64_t slots,
                                         int M, const double* scale) {
     const int64_t E = slots * M;
@@ -229,6 +278,7 @@ int grid_of(int64_t n, int block) {
 // Field table: WfField -> device array
 struct FieldRef {
     double* p = nullptr;
+    float* p32 = nullptr;
     bool river = false;
     bool member = true;
     bool derived_vwc = false;
@@ -295,6 +345,15 @@ FieldRef field_ref(WfHandle* h, int field, int layer) {
         case WF_F_BALANCE_RIVER_RELATIVE_ERROR: r.p = RM[BR_REL]; r.river = true; break;
         default: break;
     }
+    if (h->F.split && !r.river && r.p) {
+        for (int f = 0; f < M_COUNT; ++f) {
+            if (r.p == Mf[f] && wf_split_f32_member(f)) {
+                r.p32 = h->F.Mh[f];
+                r.p = nullptr;
+                break;
+            }
+        }
+    }
     return r;
 }
 
@@ -355,7 +414,6 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     if (d->n_land <= 0 || d->n_river < 0) return set_err(nullptr, WF_ERR_INVALID, "empty domain");
     if (c->dt <= 0.0) return set_err(nullptr, WF_ERR_INVALID, "dt must be positive");
     if (c->form != WF_FORM_FP64 && c->form != WF_FORM_SPLIT) return set_err(nullptr, WF_ERR_INVALID, "unknown form");
-    if (c->form == WF_FORM_SPLIT) return set_err(nullptr, WF_ERR_UNSUPPORTED, "the split form is not built yet");
     if (c->kv_profile != WF_KV_EXPONENTIAL && c->kv_profile != WF_KV_EXPONENTIAL_CONSTANT)
         return set_err(nullptr, WF_ERR_UNSUPPORTED, "only the exponential and exponential_constant Kv profiles");
     const int M = c->n_members > 0 ? c->n_members : 1;
@@ -624,6 +682,38 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     CKR(upload_slots(h, &F.R[R_AREA], r_area, PR, M, nr, false));
     std::vector<double> zeros_r((size_t)std::max<int64_t>(nr, 1) * M, 0.0);
     for (int f = 0; f < RM_COUNT; ++f) CKR(upload_slots(h, &F.RM[f], zeros_r, PR, M, nr, true));
+    // ---- split form: FP32 copies of the static fields and FP32 member fields
+    F.split = c->form == WF_FORM_SPLIT;
+    if (F.split) {
+        for (auto& x : ls) CKR(upload_slots_f32(h, &F.Lf[x.idx], x.v, PL, M, n, false));
+        for (int k = 0; k < N; ++k) {
+            std::vector<double> va(act.begin() + (size_t)k * n, act.begin() + (size_t)(k + 1) * n);
+            std::vector<double> vr(rootfrac.begin() + (size_t)k * n, rootfrac.begin() + (size_t)(k + 1) * n);
+            std::vector<double> vc(n), vk(n);
+            for (int64_t i = 0; i < n; ++i) {
+                vc[i] = p->brooks_corey_exponent[i * N + k];
+                vk[i] = p->kv_factor[i * N + k];
+            }
+            CKR(upload_slots_f32(h, &F.LYf[LY_ACT_THICK][k], va, PL, M, n, false));
+            CKR(upload_slots_f32(h, &F.LYf[LY_ROOTFRAC][k], vr, PL, M, n, false));
+            CKR(upload_slots_f32(h, &F.LYf[LY_C][k], vc, PL, M, n, false));
+            CKR(upload_slots_f32(h, &F.LYf[LY_KVFRAC][k], vk, PL, M, n, false));
+        }
+        for (int f = 0; f < M_COUNT; ++f) {
+            if (!wf_split_f32_member(f)) continue;
+            const std::vector<double>* src = &zeros_m;
+            if (f == KV0) src = &kv0;
+            if (f == FSCALE) src = &fsc;
+            if (f == Q_MAX) src = &qmax;
+            if (f == TSOIL) src = &tsoil;
+            CKR(upload_slots_f32(h, &F.Mh[f], *src, PL, M, n, true));
+        }
+        CKR(upload_slots_f32(h, &F.Rf[R_WIDTH], r_width, PR, M, nr, false));
+        CKR(upload_slots_f32(h, &F.Rf[R_LENGTH], r_length, PR, M, nr, false));
+        CKR(upload_slots_f32(h, &F.Rf[R_ALPHA], r_alpha, PR, M, nr, false));
+        CKR(upload_slots_f32(h, &F.Rf[R_EXT_INFLOW], r_ext, PR, M, nr, false));
+        CKR(upload_slots_f32(h, &F.Rf[R_AREA], r_area, PR, M, nr, false));
+    }
     // ---- maps
     {
         std::vector<int64_t> land_river_slot(PL.n_slots, -1), river_land_slot(std::max<int64_t>(PR.n_slots, 1), -1);
@@ -694,12 +784,20 @@ int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const do
     for (int k = 0; k < 3; ++k) {
         double* stg = h->staging + (size_t)k * std::max(h->n, h->nr) * h->M;
         CK(cudaMemcpyAsync(stg, src[k], count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        if (count == full) {
-            gather_kernel<<<grid_of(h->F.land_slots * h->M, block), block, 0, h->stream>>>(
-                stg, h->F.Mf[dst[k]], h->F.land_node_of_slot, h->F.land_slots, h->M, h->n);
+        const int g = grid_of(h->F.land_slots * h->M, block);
+        if (h->F.split) {
+            if (count == full)
+                gather_f32_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mh[dst[k]], h->F.land_node_of_slot,
+                                                              h->F.land_slots, h->M, h->n);
+            else
+                broadcast_member_f32_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mh[dst[k]], h->F.land_node_of_slot,
+                                                                        h->F.land_slots, h->M);
+        } else if (count == full) {
+            gather_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mf[dst[k]], h->F.land_node_of_slot, h->F.land_slots,
+                                                      h->M, h->n);
         } else {
-            broadcast_member_kernel<<<grid_of(h->F.land_slots * h->M, block), block, 0, h->stream>>>(
-                stg, h->F.Mf[dst[k]], h->F.land_node_of_slot, h->F.land_slots, h->M, nullptr);
+            broadcast_member_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mf[dst[k]], h->F.land_node_of_slot,
+                                                                h->F.land_slots, h->M, nullptr);
         }
         CK(cudaGetLastError());
     }
@@ -708,7 +806,16 @@ int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const do
 
 int32_t wf_set_forcing_device_slots(WfHandle* h, const void* P, const void* PET, const void* T) {
     if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
-    const size_t bytes = (size_t)h->F.land_slots * h->M * sizeof(double);
+    const int64_t cnt = h->F.land_slots * h->M;
+    if (h->F.split) {
+        const int g = grid_of(cnt, 256);
+        to_f32_kernel<<<g, 256, 0, h->stream>>>((const double*)P, h->F.Mh[PRECIP], cnt);
+        to_f32_kernel<<<g, 256, 0, h->stream>>>((const double*)PET, h->F.Mh[POTEVAP], cnt);
+        to_f32_kernel<<<g, 256, 0, h->stream>>>((const double*)T, h->F.Mh[TEMP], cnt);
+        CK(cudaGetLastError());
+        return WF_OK;
+    }
+    const size_t bytes = (size_t)cnt * sizeof(double);
     CK(cudaMemcpyAsync(h->F.Mf[PRECIP], P, bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->F.Mf[POTEVAP], PET, bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->F.Mf[TEMP], T, bytes, cudaMemcpyDeviceToDevice, h->stream));
@@ -749,7 +856,7 @@ int32_t wf_step(WfHandle* h) {
 int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int64_t offset, int64_t count) {
     if (!h || !dst) return set_err(h, WF_ERR_INVALID, "null argument");
     FieldRef r = field_ref(h, field, layer);
-    if (!r.p && !r.derived_vwc) return set_err(h, WF_ERR_INVALID, "unknown field or layer");
+    if (!r.p && !r.p32 && !r.derived_vwc) return set_err(h, WF_ERR_INVALID, "unknown field or layer");
     const int64_t n_ext = r.river ? h->nr : h->n;
     const int64_t total = n_ext * h->M;
     if (offset < 0 || count < 0 || offset + count > total) return set_err(h, WF_ERR_INVALID, "range out of bounds");
@@ -763,7 +870,11 @@ int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int
     const int block = 256;
     const int64_t slots = r.river ? h->F.river_slots : h->F.land_slots;
     const int64_t* nos = r.river ? h->F.river_node_of_slot : h->F.land_node_of_slot;
-    scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(src, h->staging, nos, slots, h->M, n_ext);
+    if (r.p32)
+        scatter_f32_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p32, h->staging, nos, slots, h->M,
+                                                                                  n_ext);
+    else
+        scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(src, h->staging, nos, slots, h->M, n_ext);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(dst, h->staging + offset, count * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -773,17 +884,27 @@ int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int
 int32_t wf_set_field(WfHandle* h, int32_t field, int32_t layer, const double* src, int64_t offset, int64_t count) {
     if (!h || !src) return set_err(h, WF_ERR_INVALID, "null argument");
     FieldRef r = field_ref(h, field, layer);
-    if (!r.p || !r.settable) return set_err(h, WF_ERR_INVALID, "field is not settable");
+    if ((!r.p && !r.p32) || !r.settable) return set_err(h, WF_ERR_INVALID, "field is not settable");
     const int64_t n_ext = r.river ? h->nr : h->n;
     const int64_t total = n_ext * h->M;
     if (offset < 0 || count < 0 || offset + count > total) return set_err(h, WF_ERR_INVALID, "range out of bounds");
     const int block = 256;
     const int64_t slots = r.river ? h->F.river_slots : h->F.land_slots;
     const int64_t* nos = r.river ? h->F.river_node_of_slot : h->F.land_node_of_slot;
-    scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p, h->staging, nos, slots, h->M, n_ext);
+    if (r.p32)
+        scatter_f32_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p32, h->staging, nos, slots, h->M,
+                                                                                  n_ext);
+    else
+        scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p, h->staging, nos, slots, h->M,
+                                                                              n_ext);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->staging + offset, src, count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    gather_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(h->staging, r.p, nos, slots, h->M, n_ext);
+    if (r.p32)
+        gather_f32_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(h->staging, r.p32, nos, slots, h->M,
+                                                                                 n_ext);
+    else
+        gather_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(h->staging, r.p, nos, slots, h->M,
+                                                                             n_ext);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return WF_OK;

@@ -45,12 +45,25 @@ enum WfRiverMember { WF_RM_FIELDS(WF_ENUM_ITEM) RM_COUNT };
 // Layered fields: N arrays each.
 enum WfLayered { LY_ACT_THICK = 0, LY_C, LY_KVFRAC, LY_ROOTFRAC, LY_USLD, LY_COUNT };
 
+// Member fields kept in FP32 by the split form (pure diagnostics, forcing, parameters);
+// every other member field (storages, balance terms, routing state) stays FP64.
+__host__ __device__ inline bool wf_split_f32_member(int f) {
+    return f == KV0 || f == FSCALE || f == Q_MAX || f == PRECIP || f == POTEVAP || f == TEMP || f == TSOIL ||
+           f == INTERCEPTION || f == TRANSPIRATION || f == SOIL_EVAP || f == ACT_INFILT || f == SWE;
+}
+
 struct WfDevFields {
     double* L[L_COUNT];
     double* Mf[M_COUNT];
     double* R[R_COUNT];
     double* RM[RM_COUNT];
     double* LY[LY_COUNT][WF_MAX_LAYERS];  // ACT_THICK/C/KVFRAC/ROOTFRAC by slot, USLD by element
+    // split form only: FP32 copies of the static fields and the FP32 member fields
+    float* Lf[L_COUNT];
+    float* LYf[LY_COUNT][WF_MAX_LAYERS];
+    float* Mh[M_COUNT];
+    float* Rf[R_COUNT];
+    int32_t split;
     const int8_t* nlayers;                // [land slots]
     const int64_t* land_node_of_slot;     // [land slots], -1 padding
     const int64_t* land_river_slot;       // [land slots], river slot or -1

@@ -164,7 +164,7 @@ def load_synth():
             build.build_synth()
         lib = C.CDLL(str(SYNTH_LIB_PATH))
         lib.wf_synth_dem_d8.restype = _i32
-        lib.wf_synth_dem_d8.argtypes = [_i32, _i32, C.c_uint64, _dbl, _dbl, _dbl, _dbl, _pd,
+        lib.wf_synth_dem_d8.argtypes = [_i32, _i32, C.c_uint64, _dbl, _dbl, _dbl, _dbl, _dbl, _pd,
                                         C.POINTER(C.c_uint8), _pi32, _pd, C.POINTER(C.c_int64), _pd, _pd]
         _synth = lib
     return _synth

@@ -1,0 +1,56 @@
+"""Launch-shape autotuner for a model handle.
+
+The wavefront kernels are bound by the latency of the longest chain and by how many warps
+share an SM's FP64 pipe while the short chains drain, so the best number of resident warps
+depends on the graph (chain-length distribution) and the form; the per-cell kernels depend on
+the block size. The tuner times a few steps of each candidate with per-kernel CUDA events
+and keeps the fastest for each kernel family. Candidates only change the schedule, never
+the result: the wavefront produces the same values for any dispatch order.
+"""
+
+import itertools
+
+from .model import Model
+
+
+def _time_steps(model: Model, forcing, steps):
+    model.set_tuning(**model._tune_state, use_graph=0, kernel_timing=1)
+    before, calls0 = model.kernel_times()
+    for s in range(steps):
+        P, PET, T = forcing(s)
+        model.run_timestep(P, PET, T)
+    after, calls1 = model.kernel_times()
+    n = max(calls1 - calls0, 1)
+    return {k: (after[k] - before[k]) / n for k in after}
+
+
+def tune(model: Model, forcing, steps=1, verbose=False):
+    """Pick routing warps/blocks per SM and the per-cell block size; returns the choice and the
+    measured milliseconds per step of each candidate."""
+    model._tune_state = dict(vertical_block=0, routing_warps=0, routing_blocks_per_sm=0)
+    _time_steps(model, forcing, 1)  # warm-up
+    results = []
+    best_route, best_route_t = None, float("inf")
+    for warps, bps in itertools.product([2, 4], [1, 2, 4, 0]):
+        model._tune_state = dict(vertical_block=0, routing_warps=warps, routing_blocks_per_sm=bps)
+        t = _time_steps(model, forcing, steps)
+        route = t["subsurface"] + t["overland"] + t["river"]
+        results.append(("routing", warps, bps, route))
+        if verbose:
+            print(f"routing warps={warps} blocks/SM={bps}: {route:.3f} ms")
+        if route < best_route_t:
+            best_route, best_route_t = (warps, bps), route
+    best_block, best_block_t = 0, float("inf")
+    for block in [128, 256]:
+        model._tune_state = dict(vertical_block=block, routing_warps=best_route[0],
+                                 routing_blocks_per_sm=best_route[1])
+        t = _time_steps(model, forcing, steps)
+        results.append(("vertical", block, 0, t["vertical"]))
+        if verbose:
+            print(f"vertical block={block}: {t['vertical']:.3f} ms")
+        if t["vertical"] < best_block_t:
+            best_block, best_block_t = block, t["vertical"]
+    choice = dict(vertical_block=best_block, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1])
+    model._tune_state = choice
+    model.set_tuning(**choice, use_graph=1)
+    return choice, results

@@ -35,6 +35,7 @@ class Model:
         self.nr = domain.n_river
         self.M = max(1, config.n_members)
         self.N = config.n_soil_layer_thickness + 1
+        self._tune_state = dict(vertical_block=0, routing_warps=0, routing_blocks_per_sm=0)
 
     def close(self):
         if getattr(self, "h", None):

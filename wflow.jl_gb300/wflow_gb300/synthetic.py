@@ -50,7 +50,11 @@ class Domain:
         return len(self.river["river_land_index"])
 
 
-def _d8(nx, ny, seed, cell_size, min_slope=1e-4):
+DEM_TILT = float(__import__("os").environ.get("WF_SYNTH_TILT", "1.0"))
+
+
+def _d8(nx, ny, seed, cell_size, min_slope=1e-4, tilt=None):
+    tilt = DEM_TILT if tilt is None else tilt
     lib = abi.load_synth()
     n = nx * ny
     dem = np.zeros(n)
@@ -61,7 +65,7 @@ def _d8(nx, ny, seed, cell_size, min_slope=1e-4):
     fl = np.zeros(n)
     fw = np.zeros(n)
     import ctypes as C
-    st = lib.wf_synth_dem_d8(nx, ny, C.c_uint64(seed), SCALE_RATIO_H08, 1000.0, float(cell_size), min_slope,
+    st = lib.wf_synth_dem_d8(nx, ny, C.c_uint64(seed), SCALE_RATIO_H08, 1000.0, float(cell_size), min_slope, tilt,
                              abi.as_ptr(dem), abi.as_ptr(ldd, C.c_uint8), abi.as_ptr(ds, C.c_int32),
                              abi.as_ptr(slope), abi.as_ptr(ups, C.c_int64), abi.as_ptr(fl), abi.as_ptr(fw))
     if st != 0:
