@@ -394,7 +394,7 @@ __device__ void kinematic_wave_ssf(double q_in, double q_prev, double zi_prev, d
 // ----------------------------------------------------------------- vertical kernel ------
 
 template <int MAXN>
-__global__ void __launch_bounds__(128) vertical_kernel(WfDevFields F) {
+__global__ void __launch_bounds__(256) vertical_kernel(WfDevFields F) {
     const int M = F.M;
     const int64_t E = F.land_slots * M;
     const double dt = F.dt;
