@@ -21,6 +21,7 @@
 #include "wf_kernels.h"
 #include "wf_math.cuh"
 #include "wf_walker.cuh"
+#include "wf_wave.cuh"
 
 using wfm::jclamp;
 using wfm::jmax;
@@ -217,13 +218,131 @@ struct ColumnS {
 };
 
 // ----------------------------------------------------------------- vertical kernel ------
+//
+// GB300 issues FP64 instructions (arithmetic, compares and FP32<->FP64 conversions alike) at
+// about 1/70 of its FP32 FMA rate, so this kernel keeps FP64 instructions to the few that the
+// water balance needs:
+//   * every store (canopy, snow, liquid snow water, unsaturated layers) is its FP64 content at
+//     the start of the step plus the exact sum of the step's FP32 increments, accumulated with
+//     error-free transformations (TwoSum/TwoProd) in an FP32 pair and added once at the end;
+//   * every partition of a flux that crosses the cell boundary (throughfall/interception/
+//     stemflow, rain/snow, river/land/soil runoff, infiltration/infiltration excess/saturation
+//     excess) is an FP64 residual, so the parts always sum to the whole;
+//   * the outputs that enter the balance are FP64 sums of the same FP32 values the stores saw.
+// Rates, limiters, layer geometry and all transcendental functions are FP32.
+
+// FP64 reciprocal from an FP32 seed and two Newton steps (about 4 FP64 FMAs instead of a
+// division); relative error near 1 ulp for normal inputs, inf/0/NaN handled by the seed check.
+__device__ __forceinline__ double wfm_rcp(double x) {
+    const float xf = (float)x;
+    double r = (double)(1.0f / xf);
+    if (!(fabsf(xf) < 3.0e38f && xf != 0.0f)) return 1.0 / x;
+    r = r * fma(-x, r, 2.0);
+    r = r * fma(-x, r, 2.0);
+    return r;
+}
+
+// FP64 store updated by FP32 increments without rounding loss.
+struct Store {
+    double base;
+    float bf;      // base rounded to FP32 (for FP32 decisions)
+    float hi, lo;  // increments of this step: exactly hi + lo
+    bool mod;      // content differs from what was loaded
+    __device__ __forceinline__ void init(double b) {
+        base = b;
+        bf = (float)b;
+        hi = 0.0f;
+        lo = 0.0f;
+        mod = false;
+    }
+    __device__ __forceinline__ float val() const { return bf + hi; }
+    __device__ __forceinline__ void add(float x) {  // TwoSum
+        const float s = hi + x;
+        const float bp = s - hi;
+        const float e = (hi - (s - bp)) + (x - bp);
+        hi = s;
+        lo += e;
+        mod = true;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {  // TwoProd
+        const float p = a * b;
+        const float e = fmaf(a, b, -p);
+        add(p);
+        lo += e;
+    }
+    __device__ __forceinline__ void add_d(double x) {
+        const float xh = (float)x;
+        add(xh);
+        lo += (float)(x - (double)xh);
+    }
+    __device__ __forceinline__ bool changed() const { return mod; }
+    __device__ __forceinline__ double value() const { return base + ((double)hi + (double)lo); }
+    __device__ __forceinline__ void zero() {
+        base = 0.0;
+        bf = 0.0f;
+        hi = 0.0f;
+        lo = 0.0f;
+        mod = true;
+    }
+    __device__ __forceinline__ void set(double v) {
+        init(v);
+        mod = true;
+    }
+    __device__ __forceinline__ double take_all() {  // empties the store, returns its content
+        const double v = value();
+        zero();
+        return v;
+    }
+};
+
+// Layer geometry at water-table depth zi (utils.jl set_layerthickness): which layers are
+// unsaturated is decided in FP64 against the static cumulative depths, thicknesses are FP32.
+template <int MAXN>
+struct ColG {
+    int N, nl, nu;
+    float act[MAXN], cum[MAXN + 1], thick[MAXN];
+    double thick_last;  // FP64 thickness of the deepest unsaturated layer (0 when none)
+    __device__ __forceinline__ void set(const WfDevFields& F, int64_t slot, double zi) {
+        N = F.N;
+        nl = F.nlayers[slot];
+        nu = N;
+        cum[0] = 0.0f;
+        thick_last = 0.0;
+        double c0 = 0.0;
+#pragma unroll
+        for (int k = 0; k < MAXN; ++k) {
+            float t = __int_as_float(0x7fc00000);
+            if (k < N) {
+                act[k] = F.LYf[LY_ACT_THICK][k][slot];
+                cum[k + 1] = F.LYf[LY_CUM][k][slot];
+                const double c1 = F.LY[LY_CUM][k][slot];
+                if (zi > c1) {
+                    t = act[k];
+                    thick_last = F.LY[LY_ACT_THICK][k][slot];
+                } else {
+                    const double r = zi - c0;
+                    if (r > 0.0) {
+                        t = (float)r;
+                        thick_last = r;
+                    }
+                }
+                c0 = c1;
+            } else {
+                act[k] = t;
+                cum[k + 1] = t;
+            }
+            thick[k] = t;
+            if (k < N && t != t) nu -= 1;
+        }
+    }
+};
 
 template <int MAXN>
 __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
     const int M = F.M;
     const int64_t E = F.land_slots * M;
-    const double dt = F.dt;
-    const float dtf = (float)dt;
+    const double dt = F.dt, inv_dt = F.inv_dt;
+    const float dtf = (float)F.dt, inv_dtf = (float)F.inv_dt;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
@@ -232,145 +351,180 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         float* const* Mh = F.Mh;
         float* const* Lf = F.Lf;
         const float Pf = Mh[PRECIP][e], PETf = Mh[POTEVAP][e], Tf = Mh[TEMP][e];
-        const double Pd = (double)Pf, PET = (double)PETf;
-        double canopy = Mf[CANOPY][e];
-        double snow = Mf[SNOW][e], snow_water = Mf[SNOW_WATER][e];
-        if (F.mass_balance) Mf[BL_PREV][e] = Mf[TSWS][e] + canopy + (snow + snow_water);
-        // ---- interception
+        const double Pd = (double)Pf;
+        const double canopy0 = Mf[CANOPY][e], snow0 = F.snow ? Mf[SNOW][e] : 0.0,
+                     sw0 = F.snow ? Mf[SNOW_WATER][e] : 0.0;
+        if (F.mass_balance) Mf[BL_PREV][e] = Mf[TSWS][e] + canopy0 + (snow0 + sw0);
+        // ---- interception (canopy.jl:213-226 Gash, :259-271 Rutter)
         const float gapf = Lf[GAP][slot], cmaxf = Lf[CMAX][slot];
-        const double gap = gapf, cmax = cmaxf;
-        const double potevap = (double)(Lf[KC][slot] * PETf * (1.0f - gapf));
-        double tf, ic, sf;
+        const float potevap_f = Lf[KC][slot] * PETf * (1.0f - gapf);
+        double tf_d, ic_d;
+        float icf, sff;
+        Store canopy;
+        canopy.base = canopy0;
+        canopy.hi = canopy.lo = 0.0f;
+        canopy.mod = false;
         if (F.gash) {
-            const float e_rf = Lf[E_R][slot];
-            const double e_r = e_rf;
-            if (cmax > 0.0) {
-                double fs, fi, psat;
-                if (gap < 1.0 / 1.1) {
-                    fs = 0.1 * gap;
-                    fi = 1.0 - 1.1 * gap;
-                    psat = e_r > fi ? 0.0
-                                    : (double)(-cmaxf / (e_rf * dtf) * logf(1.0f - e_rf / (float)fi));
+            if (cmaxf > 0.0f) {
+                const float e_r = Lf[E_R][slot];
+                float fs, fi, psat;
+                if (gapf < 1.0f / 1.1f) {
+                    fs = 0.1f * gapf;
+                    fi = 1.0f - 1.1f * gapf;
+                    psat = e_r > fi ? 0.0f : -cmaxf / (e_r * dtf) * logf(1.0f - e_r / fi);
                 } else {
-                    fs = 1.0 - gap;
-                    fi = 0.0;
-                    psat = 0.0;
+                    fs = 1.0f - gapf;
+                    fi = 0.0f;
+                    psat = 0.0f;
                 }
-                ic = Pd > psat ? (fi * psat - cmax / dt) + e_r * (Pd - psat) + cmax / dt : fi * Pd;
-                sf = fs * Pd;
-                tf = Pd - ic - sf;
-                if (ic > potevap) {
-                    tf += ic - potevap;
-                    ic = potevap;
-                }
+                const float ic = Pf > psat ? (fi * psat - cmaxf * inv_dtf) + e_r * (Pf - psat) + cmaxf * inv_dtf
+                                           : fi * Pf;
+                sff = fs * Pf;
+                icf = fminf(ic, potevap_f);
+                ic_d = (double)icf;
+                tf_d = Pd - ic_d - (double)sff;
             } else {
-                tf = Pd;
-                ic = 0.0;
-                sf = 0.0;
+                tf_d = Pd;
+                icf = 0.0f;
+                ic_d = 0.0;
+                sff = 0.0f;
             }
         } else {
-            double fs, pc;
-            if (gap < 1.0 / 1.1) {
-                fs = 0.1 * gap;
-                pc = (1.0 - gap - fs) * Pd;
+            float fs, pcf;
+            if (gapf < 1.0f / 1.1f) {
+                fs = 0.1f * gapf;
+                pcf = (1.0f - gapf - fs) * Pf;
             } else {
-                fs = 1.0 - gap;
-                pc = 0.0;
+                fs = 1.0f - gapf;
+                pcf = 0.0f;
             }
-            sf = fs * Pd;
-            tf = gap * Pd;
-            if (canopy > cmax) {
-                tf += (canopy - cmax) / dt;
-                canopy = cmax;
+            sff = fs * Pf;
+            tf_d = Pd - (double)sff - (double)pcf;
+            const double cmax_d = F.L[CMAX][slot];
+            canopy.bf = (float)canopy0;
+            if (canopy0 > cmax_d) {
+                tf_d += (canopy0 - cmax_d) * inv_dt;
+                canopy.set(cmax_d);
             }
-            canopy += pc * dt;
-            const double max_evap = canopy / dt;
-            if (potevap > max_evap) {
-                ic = max_evap;
-                canopy = 0.0;
+            canopy.add_prod(pcf, dtf);
+            if (potevap_f * dtf >= canopy.val() && potevap_f > 0.0f) {
+                ic_d = canopy.take_all() * inv_dt;
+                icf = (float)ic_d;
             } else {
-                ic = potevap;
-                canopy -= ic * dt;
+                icf = potevap_f;
+                ic_d = (double)icf;
+                canopy.add_prod(-icf, dtf);
             }
-            if (canopy > cmax) {
-                tf += (canopy - cmax) / dt;
-                canopy = cmax;
+            if (canopy.val() > cmaxf) {
+                const double c = canopy.value();
+                if (c > cmax_d) {
+                    tf_d += (c - cmax_d) * inv_dt;
+                    canopy.set(cmax_d);
+                }
             }
         }
-        // ---- snow
-        double wfs;
+        // ---- snow (snow.jl:238-293, snow_process.jl:26-116)
+        double wfs_d;
         float swe_out = 0.0f;
+        Store snow, sw;
         if (F.snow) {
-            const double eff = tf + sf;
+            snow.init(snow0);
+            sw.init(sw0);
+            const double eff_d = tf_d + (double)sff;
             const float tti = Lf[TTI][slot], tt = Lf[TT][slot];
             const float rainfrac = tti == 0.0f ? (Tf > tt ? 1.0f : 0.0f)
-                                               : fminj(fmaxj((Tf - (tt - tti / 2.0f)) / tti, 0.0f), 1.0f);
-            const double lp = (double)rainfrac * eff;
-            const double sp = eff - lp;
+                                               : fminf(fmaxf((Tf - (tt - tti / 2.0f)) / tti, 0.0f), 1.0f);
+            const double lp_d = (double)rainfrac * eff_d;
+            const double sp_d = eff_d - lp_d;
             const float ttm = Lf[TTM][slot], ddf = Lf[DDF][slot];
             if (Tf > ttm) {
-                const double melt = jmin((double)(ddf * (Tf - ttm)), snow / dt);
-                snow -= melt * dt;
-                snow_water += melt * dt;
+                const float melt = ddf * (Tf - ttm);
+                if (melt * dtf >= snow.val()) {
+                    if (snow.val() > 0.0f) sw.add_d(snow.take_all());
+                } else {
+                    snow.add_prod(-melt, dtf);
+                    sw.add_prod(melt, dtf);
+                }
             } else {
-                const double refr = jmin((double)(ddf * 0.05f * (ttm - Tf) * dtf), snow_water);
-                snow += refr;
-                snow_water -= refr;
+                const float refr = ddf * 0.05f * (ttm - Tf) * dtf;
+                if (refr >= sw.val()) {
+                    if (sw.val() > 0.0f) snow.add_d(sw.take_all());
+                } else {
+                    snow.add(refr);
+                    sw.add(-refr);
+                }
             }
-            snow = jmax(snow, 0.0);
-            snow_water = jmax(snow_water, 0.0);
-            snow += sp * dt;
-            snow_water += lp * dt;
-            const double maxsw = snow * (double)Lf[WHC][slot];
-            double srunoff = 0.0;
-            if (snow_water > maxsw) {
-                srunoff = (snow_water - maxsw) / dt;
-                snow_water = maxsw;
+            snow.add_d(sp_d * dt);
+            sw.add_d(lp_d * dt);
+            const float whc = Lf[WHC][slot];
+            double srunoff_d = 0.0;
+            if (sw.val() > snow.val() * whc) {
+                const double maxsw = snow.value() * (double)whc;
+                const double s = sw.value();
+                if (s > maxsw) {
+                    srunoff_d = (s - maxsw) * inv_dt;
+                    sw.set(maxsw);
+                }
             }
-            swe_out = (float)(snow_water + snow);
-            wfs = srunoff;
+            swe_out = sw.val() + snow.val();
+            wfs_d = srunoff_d;
         } else {
-            wfs = tf + sf;
+            wfs_d = tf_d + (double)sff;
         }
-        // ---- open water
+        // ---- open water (runoff.jl open-water runoff and evaporation)
         const double rfrac = F.L[RIVER_FRACTION][slot], wfrac = F.L[WATER_FRACTION][slot];
-        const double wd_land = Mf[OL_H][e];
+        const float rfrac_f = Lf[RIVER_FRACTION][slot], wfrac_f = Lf[WATER_FRACTION][slot];
+        const float wd_land = (float)Mf[OL_H][e];
         const int64_t rs = F.land_river_slot[slot];
-        const double wd_river = rs >= 0 ? F.RM[RV_H][rs * M + m] : 0.0;
-        const double runoff_river = jmin(1.0, rfrac) * wfs;
-        const double runoff_land = jmin(1.0, wfrac) * wfs;
-        const double ae_river = rfrac * jmin(wd_river / dt, PET);
-        const double ae_land = wfrac * jmin(wd_land / dt, PET);
-        // ---- soil
-        const double soil_fraction = jmax(gap - wfrac - rfrac, 0.0);
-        const double pot_trans = jmax(0.0, potevap - ic);
-        const double pot_soilevap = soil_fraction * PET;
-        const double wfs_soil = jmax(wfs - runoff_river - runoff_land, 0.0);
-        ColumnS<MAXN> col;
-        col.load_static(F, slot);
-        col.kv0 = Mh[KV0][e];
-        col.f = Mh[FSCALE][e];
-        const double ts = col.ts, tr = col.tr, te = ts - tr;
-        const float tef = (float)te;
-        const double swc = F.L[SWC][slot];
+        const float wd_river = rs >= 0 ? (float)F.RM[RV_H][rs * M + m] : 0.0f;
+        const double runoff_river_d = fmin(1.0, rfrac) * wfs_d;
+        const double runoff_land_d = fmin(1.0, wfrac) * wfs_d;
+        const float ae_river_f = rfrac_f * fminf(wd_river * inv_dtf, PETf);
+        const float ae_land_f = wfrac_f * fminf(wd_land * inv_dtf, PETf);
+        const double ae_river_d = (double)ae_river_f, ae_land_d = (double)ae_land_f;
+        // ---- soil (soil.jl update! of SbmSoilModel)
+        const double wfs_soil_d = fmax(wfs_d - runoff_river_d - runoff_land_d, 0.0);
+        const float soil_fraction = fmaxf(gapf - wfrac_f - rfrac_f, 0.0f);
+        const float pot_trans = fmaxf(0.0f, potevap_f - icf);
+        const float pot_soilevap = soil_fraction * PETf;
+        const double d_soil = F.L[SOIL_THICKNESS][slot];
         const double sat = Mf[SAT][e];
-#pragma unroll
-        for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? F.LY[LY_USLD][k][e] : 0.0;
+        const double zi = fmax(0.0, d_soil - sat * F.L[INV_TE][slot]);
+        ColG<MAXN> g;
+        g.set(F, slot, zi);
+        const float zif = (float)zi, df = Lf[SOIL_THICKNESS][slot];
+        const float ts = Lf[THETA_S][slot], tr = Lf[THETA_R][slot], tfc = Lf[THETA_FC][slot];
+        const float te = ts - tr;
+        const float kv0 = Mh[KV0][e], fsc = Mh[FSCALE][e], zexp = Lf[Z_EXP][slot];
+        const bool kv_const = F.kv_profile == WF_KV_EXPONENTIAL_CONSTANT;
+        // Kv at depth z of layer n (1-based); the layer's factor is selected without dynamic
+        // indexing so that the per-layer arrays stay in registers
+#define WF_KV_AT(z_, n_)                                           \
+    ([&]() {                                                       \
+        float zz_ = (z_);                                          \
+        if (kv_const && !(zz_ < zexp)) zz_ = zexp;                 \
+        float kf_ = 0.0f;                                          \
+        _Pragma("unroll") for (int j_ = 0; j_ < MAXN; ++j_) if (j_ == (n_) - 1) kf_ = kvf[j_]; \
+        return kf_ * kv0 * expf(-fsc * zz_);                       \
+    }())
+        Store us[MAXN];
         float kvf[MAXN], cexp[MAXN], rfr[MAXN];
+        float usd = 0.0f;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k) {
-            kvf[k] = k < col.N ? F.LYf[LY_KVFRAC][k][slot] : 0.0f;
-            cexp[k] = k < col.N ? F.LYf[LY_C][k][slot] : 0.0f;
-            rfr[k] = k < col.N ? F.LYf[LY_ROOTFRAC][k][slot] : 0.0f;
+            if (k < g.N) {
+                us[k].init(F.LY[LY_USLD][k][e]);
+                kvf[k] = F.LYf[LY_KVFRAC][k][slot];
+                cexp[k] = F.LYf[LY_C][k][slot];
+                rfr[k] = F.LYf[LY_ROOTFRAC][k][slot];
+            } else {
+                us[k].zero();
+                kvf[k] = cexp[k] = rfr[k] = 0.0f;
+            }
+            if (k < g.nl) usd += us[k].val();
         }
-        double usd = 0.0;
-#pragma unroll
-        for (int k = 0; k < MAXN; ++k)
-            if (k < col.nl) usd += col.usld[k];
-        const double zi = jmax(0.0, col.d - sat / te);
-        double drain = (col.d - zi) * jmax(ts - col.tfc, 0.02);
-        double ucap = swc - sat - usd;
-        col.set_thickness(zi);
+        float drain = (df - zif) * fmaxf(ts - tfc, 0.02f);
+        float ucap = Lf[SWC][slot] - (float)sat - usd;
         float tsoil = Mh[TSOIL][e];
         if (F.snow) tsoil = tsoil + Lf[W_SOIL][slot] * (Tf - tsoil);
         float fred = 1.0f;
@@ -378,167 +532,226 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             const float cf = Lf[CF_SOIL][slot];
             fred = 1.0f / (1.0f / (1.0f - cf) + expf(-8.0f * (tsoil - 273.15f))) + cf;
         }
-        // infiltration
-        const double cfrac = F.L[COMPACT_FRAC][slot];
-        const double cap_soil = (double)(col.kv0 * kvf[0]);
-        const double cap_comp = F.L[CAP_COMP][slot];
-        const double soilinf = wfs_soil * (1.0 - cfrac);
-        const double pathinf = wfs_soil * cfrac;
-        const double mis = jmin(cap_soil * fred, soilinf);
-        const double mip = jmin(cap_comp * fred, pathinf);
-        const double infiltration = jmin(mip + mis, jmax(0.0, ucap / dt));
-        const double infex = (soilinf - mis) + (pathinf - mip);
-        // unsaturated zone flow: FP32 rates, FP64 layer stores
-        double transfer = 0.0;
-        if (col.nu > 0) {
-            double z = 0.0, flow = 0.0;
+        // infiltration (soil_process.jl infiltration): FP64 partition of the water reaching the soil
+        const double soilinf_d = wfs_soil_d * (1.0 - F.L[COMPACT_FRAC][slot]);
+        const double pathinf_d = wfs_soil_d - soilinf_d;
+        const float cap_soil = kv0 * kvf[0] * fred, cap_comp = Lf[CAP_COMP][slot] * fred;
+        const float soilinf_f = (float)soilinf_d, pathinf_f = (float)pathinf_d;
+        const double mis_d = cap_soil < soilinf_f ? (double)cap_soil : soilinf_d;
+        const double mip_d = cap_comp < pathinf_f ? (double)cap_comp : pathinf_d;
+        const double infex_d = (soilinf_d - mis_d) + (pathinf_d - mip_d);
+        const float capmax = fmaxf(0.0f, ucap * inv_dtf);
+        const float infil_f = fminf(__double2float_rz(mis_d + mip_d), capmax);
+        // unsaturated zone flow (soil_process.jl:51-92): FP32 rates, exact transfers
+        double transfer_d = 0.0;
+        if (g.nu > 0) {
+            float z = 0.0f, flow_f = infil_f;
+            double flow_amt = 0.0;
+            bool amt = false;
 #pragma unroll
             for (int k = 0; k < MAXN; ++k) {
-                if (k >= col.nu) break;
-                z = z + col.thick[k];
-                const double l_sat = col.thick[k] * te;
-                const float kv_z = col.kv_at(kvf, z, k + 1);
-                const double u = col.usld[k] + (k == 0 ? infiltration : flow) * dt;
-                if (u <= 0.0) {
-                    col.usld[k] = 0.0;
-                    flow = 0.0;
+                if (k >= g.nu) continue;
+                z += g.thick[k];
+                const float l_sat = g.thick[k] * te;
+                const float kv_z = WF_KV_AT(z, k + 1);
+                if (amt) us[k].add_d(flow_amt);
+                else us[k].add_prod(flow_f, dtf);
+                const float u = us[k].val();
+                if (u <= 0.0f) {
+                    us[k].zero();
+                    flow_f = 0.0f;
+                    amt = false;
                     continue;
                 }
                 bool drained;
-                double rate = (double)unsat_rate((float)u, kv_z, (float)l_sat, cexp[k], dtf, drained);
-                double un = u - rate * dt;
-                if (drained || un < 0.0) {
-                    rate = u / dt;
-                    un = 0.0;
+                const float rate = unsat_rate(u, kv_z, l_sat, cexp[k], dtf, drained);
+                if (drained || u - rate * dtf < 0.0f) {
+                    flow_amt = us[k].take_all();
+                    amt = true;
+                } else {
+                    us[k].add_prod(-rate, dtf);
+                    flow_f = rate;
+                    amt = false;
                 }
-                col.usld[k] = un;
-                flow = rate;
             }
-            transfer = flow;
+            transfer_d = amt ? flow_amt * inv_dt : (double)flow_f;
         }
-        // soil evaporation
-        double soilevap, esat;
+        // soil evaporation (soil.jl soil_evaporation!)
+        double se_d;
+        float se_f, esat_f = 0.0f;
         {
-            double pot = pot_soilevap;
-            double se;
-            if (col.nu == 0) {
-                se = 0.0;
-            } else if (col.nu == 1) {
-                se = pot * jmin(1.0, col.usld[0] / (zi * te));
+            float se = 0.0f;
+            const float u0 = us[0].val();
+            if (g.nu == 1) se = pot_soilevap * fminf(1.0f, u0 / (zif * te));
+            else if (g.nu > 1) se = pot_soilevap * fminf(1.0f, u0 / (g.thick[0] * te));
+            if (se > 0.0f && se * dtf >= u0) {
+                se_d = us[0].take_all() * inv_dt;
+                se_f = (float)se_d;
             } else {
-                se = pot * jmin(1.0, col.usld[0] / (col.thick[0] * te));
+                se_f = se;
+                se_d = (double)se;
+                us[0].add_prod(-se, dtf);
             }
-            se = jmin(se, col.usld[0] / dt);
-            pot -= se;
-            col.usld[0] -= se * dt;
-            if (col.nu == 0 || col.nu == 1) {
-                esat = pot * jmin(1.0, (col.act[0] - zi) / col.act[0]);
-                esat = jmin(esat, (col.act[0] - zi) * jmax(ts - col.tfc, 0.02) / dt);
-            } else {
-                esat = 0.0;
+            const float pot = pot_soilevap - se_f;
+            if (g.nu <= 1) {
+                const float a0 = g.act[0];
+                esat_f = fminf(pot * fminf(1.0f, (a0 - zif) / a0), (a0 - zif) * fmaxf(ts - tfc, 0.02f) * inv_dtf);
             }
-            soilevap = se + esat;
-            drain -= esat * dt;
+            drain -= esat_f * dtf;
         }
-        // transpiration: FP32 heads and reduction factors, FP64 extraction
-        double actevapustore = 0.0, act_sat;
+        // transpiration (soil.jl transpiration!): FP32 heads, Feddes reduction and root water uptake
+        double actevap_d = 0.0;
+        float actevap_f = 0.0f, act_sat_f;
         {
-            const double rd = F.L[ROOTING_DEPTH][slot];
+            const float rd = Lf[ROOTING_DEPTH][slot];
             const float h1 = Lf[H1][slot], h2 = Lf[H2][slot], h4 = Lf[H4][slot], a1 = Lf[ALPHA_H1][slot];
             const float psi = Lf[PSI_B][slot];
-            const float tpd = (float)pot_trans / MM_PER_DAY_F;
+            const float tpd = pot_trans / MM_PER_DAY_F;
             const float h3l = Lf[H3_LOW][slot], h3h = Lf[H3_HIGH][slot];
             const float h3 = tpd <= 1.0f ? h3l : (tpd < 5.0f ? h3l + (h3h - h3l) * (tpd - 1.0f) / 4.0f : h3h);
-            double sum_rf = 0.0, rf_low = 0.0;
+            float sum_rf = 0.0f, rf_low = 0.0f;
 #pragma unroll
             for (int k = 1; k <= MAXN; ++k) {
-                if (k > col.nu) break;
-                double r = rfr[k - 1];
-                if (k == col.nu && zi < rd) r = r * (col.thick[k - 1] / jmin(col.act[k - 1], rd - col.cum[k - 1]));
-                sum_rf += r;
-                rf_low = r;
+                if (k <= g.nu) {
+                    float r = rfr[k - 1];
+                    if (k == g.nu && zif < rd) r = r * (g.thick[k - 1] / fminf(g.act[k - 1], rd - g.cum[k - 1]));
+                    sum_rf += r;
+                    rf_low = r;
+                }
             }
 #pragma unroll
             for (int k = 1; k <= MAXN; ++k) {
-                if (k > col.nu) break;
-                const double r = k < col.nu ? (double)rfr[k - 1] : rf_low;
-                const double rs_ = rd > 0.0 ? jmax(1.0 / sum_rf, 1.0) * r : 0.0;
-                const float vwc = fmaxj((float)(col.usld[k - 1] / col.thick[k - 1]), 1e-7f);
+                if (k > g.nu) continue;
+                const float r = k < g.nu ? rfr[k - 1] : rf_low;
+                const float rs_ = rd > 0.0f ? fmaxf(1.0f / sum_rf, 1.0f) * r : 0.0f;
+                const float uk = us[k - 1].val();
+                const float vwc = fmaxf(uk / g.thick[k - 1], 1e-7f);
                 const float lam = 2.0f / (cexp[k - 1] - 3.0f);
-                const float head = lam > 0.0f ? psi / powj(vwc / tef, 1.0f / lam) : psi;
+                const float head = lam > 0.0f ? psi / powj(vwc / te, 1.0f / lam) : psi;
                 const float alpha = rwu_feddes_f(head, h1, h2, h3, h4, a1);
-                const double availcap = jmin(1.0, jmax(0.0, (rd - col.cum[k - 1]) / col.thick[k - 1]));
-                const double a = jmin((double)alpha * rs_ * pot_trans, col.usld[k - 1] * availcap / dt);
-                col.usld[k - 1] -= a * dt;
-                actevapustore += a;
+                const float availcap = fminf(1.0f, fmaxf(0.0f, (rd - g.cum[k - 1]) / g.thick[k - 1]));
+                const float want = alpha * rs_ * pot_trans;
+                const float avail = uk * availcap * inv_dtf;
+                if (want > 0.0f && want >= avail && availcap >= 1.0f) {
+                    const double a = us[k - 1].take_all() * inv_dt;
+                    actevap_d += a;
+                    actevap_f += (float)a;
+                } else {
+                    const float a = fminf(want, avail);
+                    us[k - 1].add_prod(-a, dtf);
+                    actevap_d += (double)a;
+                    actevap_f += a;
+                }
             }
-            const float wetroots = 1.0f / (1.0f + expf(-Lf[ROOTDISTPAR][slot] * (float)(zi - rd)));
+            const float wetroots = 1.0f / (1.0f + expf(-Lf[ROOTDISTPAR][slot] * (zif - rd)));
             const float alpha0 = rwu_feddes_f(0.0f, h1, h2, h3, h4, a1);
-            act_sat = jmin((pot_trans - actevapustore) * (double)(wetroots * alpha0), drain / dt);
-            drain -= act_sat * dt;
+            act_sat_f = fminf((pot_trans - actevap_f) * (wetroots * alpha0), drain * inv_dtf);
+            drain -= act_sat_f * dtf;
         }
-        const double transpiration = actevapustore + act_sat;
-        // actual infiltration
-        double excess = 0.0;
+        // actual infiltration: water above the capacity of a layer moves up, the top layer's
+        // excess leaves the soil (soil.jl)
+        float excess = 0.0f;
 #pragma unroll
         for (int k = MAXN; k >= 1; --k) {
-            if (k > col.nu) continue;
-            excess = jmax(0.0, col.usld[k - 1] - col.thick[k - 1] * te);
-            col.usld[k - 1] -= excess;
-            if (k > 1) col.usld[k - 2] += excess;
+            if (k > g.nu) continue;
+            excess = fmaxf(0.0f, us[k - 1].val() - g.thick[k - 1] * te);
+            us[k - 1].add(-excess);
+            if (k > 1) us[k - 2].add(excess);
         }
-        const double act_infilt = infiltration - excess / dt;
-        const double satex = (wfs_soil - act_infilt) - infex;
-        usd = 0.0;
+        const double act_infilt_d = (double)infil_f - (double)excess * inv_dt;
+        const double satex_d = (wfs_soil_d - act_infilt_d) - infex_d;
+        usd = 0.0f;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k)
-            if (k < col.nl) usd += col.usld[k];
-        ucap = swc - sat - usd;
-        // capillary flux
-        double capflux_act = 0.0;
-        if (col.nu > 0) {
-            const double ksat = (double)col.kv_at(kvf, zi, col.nu);
-            const double maxcap = jmax(0.0, jmin(jmin(jmin(ksat, actevapustore), ucap / dt), drain / dt));
-            const double rd = F.L[ROOTING_DEPTH][slot];
+            if (k < g.nl) usd += us[k].val();
+        ucap = Lf[SWC][slot] - (float)sat - usd;
+        // capillary rise (soil.jl capillary_flux!)
+        Store capacc;
+        capacc.zero();
+        if (g.nu > 0) {
+            const float ksat = WF_KV_AT(zif, g.nu);
+            const float maxcap = fmaxf(0.0f, fminf(fminf(fminf(ksat, actevap_f), ucap * inv_dtf), drain * inv_dtf));
+            const float rd = Lf[ROOTING_DEPTH][slot];
             const float chmax = Lf[CAP_HMAX][slot];
-            double capflux =
-                zi > rd ? maxcap * (double)powj(1.0f - fminj((float)zi, chmax) / chmax, Lf[CAP_N][slot]) : 0.0;
+            float capflux = zif > rd ? maxcap * powj(1.0f - fminf(zif, chmax) / chmax, Lf[CAP_N][slot]) : 0.0f;
 #pragma unroll
             for (int k = MAXN; k >= 1; --k) {
-                if (k > col.nu) continue;
-                const double toadd = jmin(capflux, jmax((col.thick[k - 1] * te - col.usld[k - 1]) / dt, 0.0));
-                col.usld[k - 1] += toadd * dt;
+                if (k > g.nu) continue;
+                const float toadd =
+                    fminf(capflux, fmaxf((g.thick[k - 1] * te - us[k - 1].val()) * inv_dtf, 0.0f));
+                us[k - 1].add_prod(toadd, dtf);
                 capflux -= toadd;
-                capflux_act += toadd;
+                capacc.add(toadd);
             }
         }
-        const double deepksat = (double)col.kv_at(kvf, col.d, col.nl);
-        const double leak = jmax(0.0, jmin(F.L[MAX_LEAKAGE][slot], jmin(drain / dt, deepksat)));
-        const double recharge = transfer - capflux_act - leak - act_sat - esat;
-        const double aet = soilevap + transpiration + ae_river + ae_land + ic;
+        const double capflux_d = (double)capacc.hi + (double)capacc.lo;
+        const float deepksat = WF_KV_AT(df, g.nl);
+        const float leak_f = fmaxf(0.0f, fminf(Lf[MAX_LEAKAGE][slot], fminf(drain * inv_dtf, deepksat)));
+        const double leak_d = (double)leak_f;
+        const double recharge = transfer_d - capflux_d - leak_d - (double)act_sat_f - (double)esat_f;
+        const double soilevap_d = se_d + (double)esat_f;
+        const double transpiration_d = actevap_d + (double)act_sat_f;
+        const double aet = soilevap_d + transpiration_d + ae_river_d + ae_land_d + ic_d;
         // ---- write back
-        Mf[CANOPY][e] = canopy;
-        Mf[SNOW][e] = snow;
-        Mf[SNOW_WATER][e] = snow_water;
+        if (!F.gash) Mf[CANOPY][e] = canopy.value();
+        if (F.snow) {
+            Mf[SNOW][e] = snow.value();
+            Mf[SNOW_WATER][e] = sw.value();
+            Mh[SWE][e] = swe_out;
+        }
         Mh[TSOIL][e] = tsoil;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k)
-            if (k < col.N) F.LY[LY_USLD][k][e] = col.usld[k];
+            if (k < g.N && us[k].changed()) F.LY[LY_USLD][k][e] = us[k].value();
         Mf[ZI][e] = zi;
         Mf[SSF_ZI][e] = zi;
         Mf[RECHARGE][e] = recharge;
-        Mf[NET_RUNOFF_RIVER][e] = runoff_river - ae_river;
+        Mf[NET_RUNOFF_RIVER][e] = runoff_river_d - ae_river_d;
         Mf[AET][e] = aet;
-        Mf[LEAKAGE][e] = leak;
-        Mf[SATEX][e] = satex;
-        Mf[INFEX][e] = infex;
-        Mf[RUNOFF_LAND][e] = runoff_land;
-        Mf[AE_LAND][e] = ae_land;
-        Mh[INTERCEPTION][e] = (float)ic;
-        Mh[TRANSPIRATION][e] = (float)transpiration;
-        Mh[SOIL_EVAP][e] = (float)soilevap;
-        Mh[ACT_INFILT][e] = (float)act_infilt;
-        if (F.snow) Mh[SWE][e] = swe_out;
+        Mf[LEAKAGE][e] = leak_d;
+        Mf[SATEX][e] = satex_d;
+        Mf[INFEX][e] = infex_d;
+        Mf[RUNOFF_LAND][e] = runoff_land_d;
+        Mf[AE_LAND][e] = ae_land_d;
+        Mh[INTERCEPTION][e] = icf;
+        Mh[TRANSPIRATION][e] = actevap_f + act_sat_f;
+        Mh[SOIL_EVAP][e] = se_f + esat_f;
+        Mh[ACT_INFILT][e] = infil_f - excess * inv_dtf;
+        // storages at the start of the routing (overland and river balances)
+        if (F.mass_balance) {
+            Mf[BO_PREV][e] = Mf[OL_STORAGE][e];
+            if (rs >= 0) F.RM[BR_PREV][rs * M + m] = F.RM[RV_STORAGE][rs * M + m];
+        }
+        // terms of the subsurface solve that do not depend on the upstream discharge
+        if (F.ssf_single) {
+            double flux = recharge * F.L[AREA][slot];  // recharge flux of the subsurface model
+            if (zi >= d_soil) flux = fmax(0.0, flux);
+            Mf[SSF_QNET][e] = flux;
+            float z = zif;
+            if (kv_const && !(z < zexp)) z = zexp;
+            const float cel = Lf[KH_RATIO][slot] * kv0 * expf(-fsc * z) * Lf[SLOPE][slot] / Lf[SY][slot];
+            const float cinv = 1.0f / cel;
+            Mf[SSF_T2][e] = Mf[SSF_Q][e] * (double)cinv;
+            Mf[SSF_RDF][e] = (double)(1.0f / (Lf[SSF_DTDX][slot] + cinv));
+            // deepest unsaturated layer: what a rising water table fills first. The rise it
+            // allows, dt * rate / (theta_e - usld / thickness), moves water between the layer and
+            // the saturated store, so it is FP64 (with the layer's FP64 thickness and content).
+            double rth = 0.0, rcap = 0.0, rrho = 0.0;
+            if (g.nu > 0) {
+                const double dts = F.dt_ssf;
+                const double te_d = F.L[THETA_S][slot] - F.L[THETA_R][slot];
+                double uk = 0.0;
+#pragma unroll
+                for (int k = 0; k < MAXN; ++k)
+                    if (k + 1 == g.nu) uk = us[k].changed() ? us[k].value() : us[k].base;
+                rth = g.thick_last;
+                rcap = fmax(rth * te_d - uk, 0.0) * F.inv_dt_ssf;
+                rrho = dts * rth * wfm_rcp(te_d * rth - uk);
+            }
+            Mf[SSF_RTH][e] = rth;
+            Mf[SSF_RCAP][e] = rcap;
+            Mf[SSF_RRHO][e] = rrho;
+        }
     }
 }
 
@@ -837,6 +1050,507 @@ struct RiverSplitPhys {
     }
 };
 
+// ====================================================================== slim wavefronts ====
+//
+// The sweeps below keep only the discharge solve on the critical path (wf_wave.cuh); the
+// per-cell kernels before (vertical epilogue) and after (post kernels) each sweep do the rest.
+
+// Root of dt_dx u^5 + alpha u^3 = cterm for the kinematic wave in u = Q^0.2 (the reference's
+// Newton-Raphson on Q, surface_process.jl:24-70, written for u): Newton iterations in FP32
+// from the upper bound min((cterm/alpha)^(1/3), (cterm/dt_dx)^(1/5)) (or the previous u when it
+// lies below that bound) until |du| <= 1e-6 u, then one FP64 Newton correction of the FP32
+// root, which leaves |f(u)| at the FP64 rounding level of cterm. Results below the reference's
+// floor (Q = 1e-30, u = QROOT) are raised to it, as the reference does.
+__device__ __forceinline__ void kw_solve_u(double qin, double q_prev, double qlat, double dt_s, double alpha,
+                                           double dt_dx, double u_prev, double& u_out, double& q_out) {
+    if (qin + q_prev + qlat == 0.0) {
+        u_out = 0.0;
+        q_out = 0.0;
+        return;
+    }
+    const double cterm = dt_dx * qin + (alpha * (u_prev * u_prev * u_prev) + dt_s * qlat);
+    const double QR = KIN_WAVE_MIN_FLOW_QROOT;
+    const double floor_c = alpha * (QR * QR * QR) + dt_dx * KIN_WAVE_MIN_FLOW;
+    double u;
+    if (!(cterm > floor_c)) {
+        u = QR;
+    } else {
+        const float a = (float)dt_dx, b = (float)alpha, c = (float)cterm;
+        const float ub = fminf(cbrtf(c / b), powf(c / a, 0.2f));
+        const float up = (float)u_prev;
+        float v = (up > 0.0f && up < ub) ? up : ub;
+        const float a5 = 5.0f * a, b3 = 3.0f * b;
+        float dg = 1.0f;
+#pragma unroll 1
+        for (int it = 0; it < 12; ++it) {
+            const float v2 = v * v;
+            const float g = v2 * v * fmaf(a, v2, b) - c;
+            dg = v2 * fmaf(a5, v2, b3);
+            const float dv = __fdividef(g, dg);
+            v = fminf(v - dv, ub);
+            if (!(fabsf(dv) > 1e-6f * v)) break;
+        }
+        const float v2 = v * v;
+        dg = v2 * fmaf(a5, v2, b3);
+        u = (double)v;
+        const double u2 = u * u;
+        const double f = u2 * u * fma(dt_dx, u2, alpha) - cterm;
+        u = fma(-f, (double)(1.0f / dg), u);
+        if (!(u > QR)) u = QR;
+    }
+    const double u2 = u * u;
+    u_out = u;
+    q_out = u2 * u2 * u;
+}
+
+// q^0.2 for a discharge set from outside the step (BMI set_value, restart).
+__device__ __forceinline__ double u_of_q(double q) {
+    if (!(q > 0.0)) return 0.0;
+    const float u0 = powf((float)q, 0.2f);
+    double u = (double)u0;
+    const double u2 = u * u;
+    return u - (u2 * u2 * u - q) * (double)(1.0f / (5.0f * u0 * u0 * u0 * u0));
+}
+
+// Subsurface node when the fast path cannot decide: the full column computation of the fused
+// form (water-table change over every unsaturated layer, the reference's sub-iterations when
+// the water table moves by more than 0.1 per step, subsurface_process.jl:100-196), which also
+// writes the updated unsaturated layers and water table.
+template <int MAXN>
+__device__ __noinline__ void ssf_full_split(const WfDevFields& F, int64_t slot, int64_t e, double qin, double q_net, double dt_s,
+                               double& q_out, double& zi_out, double& exf_out, double& nf_out) {
+    double* const* Mf = F.Mf;
+    double* const* L = F.L;
+    const double d = L[SOIL_THICKNESS][slot];
+    const double zi_ssf = Mf[SSF_ZI][e];
+    ColumnS<MAXN> col;
+    col.load_static(F, slot);
+    col.kv0 = F.Mh[KV0][e];
+    col.f = F.Mh[FSCALE][e];
+#pragma unroll
+    for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? F.LY[LY_USLD][k][e] : 0.0;
+    col.set_thickness(Mf[ZI][e]);
+    const double q_prev = Mf[SSF_Q][e];
+    const double sy = L[SY][slot], dx = L[FLOW_LENGTH][slot], dw = L[FLOW_WIDTH][slot];
+    const double slope = L[SLOPE][slot];
+    const float kh0 = F.Lf[KH_RATIO][slot] * col.kv0;
+    const double q_max = (double)F.Mh[Q_MAX][e];
+    auto celerity = [&](double zi) {
+        float z = (float)zi;
+        if (col.profile == WF_KV_EXPONENTIAL_CONSTANT && !(z < col.zexp)) z = col.zexp;
+        return (double)(kh0 * expf(-col.f * z) * (float)slope) / sy;
+    };
+    double cel = celerity(zi_ssf);
+    double cterm = (dt_s / dx) * (qin + q_net) + q_prev / cel;
+    double q = kw_ssf_newton_s((q_prev + qin) / 2.0, cterm, cel, dt_s, dx);
+    q = jmin(q, q_max * dw);
+    double netflux = (qin + q_net - q) / (dw * dx);
+    double dh, exfilt;
+    col.water_table_change(netflux, sy, dt_s, dh, exfilt);
+    double zi = zi_ssf - dh;
+    if (zi > d) q = jmax(q - (dw * dx) * sy * (zi - d) / dt_s, KIN_WAVE_MIN_FLOW);
+    zi = jclamp(zi, 0.0, d);
+    const long its = (long)wfm::ceil_(wfm::round_sigdigits(wfm::fabs_(zi - zi_ssf) / 0.1, 12));
+    if (its > 1) {
+        const double dts2 = dt_s / (double)its;
+        double q_sum = 0.0, ex_sum = 0.0, nf_sum = 0.0, qp = q_prev, zp = zi_ssf;
+        for (long i = 0; i < its; ++i) {
+            cel = celerity(zp);
+            cterm = (dts2 / dx) * qin + qp / cel + q_net * (dts2 / dx);
+            q = kw_ssf_newton_s(qp, cterm, cel, dts2, dx);
+            q = jmin(q, q_max * dw);
+            netflux = (qin + q_net - q) / (dw * dx);
+            col.water_table_change(netflux, sy, dts2, dh, exfilt);
+            zi = zp - dh;
+            if (zi > d) q = jmax(q - (dw * dx) * sy * (zi - d) / dts2, KIN_WAVE_MIN_FLOW);
+            zi = jclamp(zi, 0.0, d);
+            col.update_ustorelayerdepth(zp, zi);
+            ex_sum += exfilt;
+            nf_sum += netflux;
+            q_sum += q;
+            qp = q;
+            zp = zi;
+        }
+        q = q_sum / (double)its;
+        exfilt = ex_sum / (double)its;
+        netflux = nf_sum / (double)its;
+    } else {
+        col.update_ustorelayerdepth(zi_ssf, zi);
+    }
+#pragma unroll
+    for (int k = 0; k < MAXN; ++k)
+        if (k < col.N) F.LY[LY_USLD][k][e] = col.usld[k];
+    Mf[ZI][e] = zi;
+    q_out = q;
+    zi_out = zi;
+    exf_out = exfilt;
+    nf_out = netflux;
+}
+
+// Lateral subsurface flow, one sub-step per model step (subsurface_process.jl:100-196 per
+// node). The solve of the linear kinematic wave is q = cterm / (dt/dx + 1/c); the water-table
+// change is decided from the deepest unsaturated layer prepared by the vertical kernel, and
+// anything else (several layers filled, a water table moving by more than 0.1, non-finite
+// values) goes through ssf_full_split.
+template <int MAXN>
+struct SsfWave {
+    WfDevFields F;
+    WfDevGraph g;
+    WfSweep sw;
+    struct In {
+        double q_prev, q_net, t2, rdf, zi, d, dtdx, idwdx, dtsy, k2, qmaxdw, rth, rcap, rrho;
+        wfv::UpList up;
+    };
+    __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
+        double* const* Mf = F.Mf;
+        double* const* L = F.L;
+        x.q_prev = Mf[SSF_Q][e];
+        x.q_net = Mf[SSF_QNET][e];
+        x.t2 = Mf[SSF_T2][e];
+        x.rdf = Mf[SSF_RDF][e];
+        x.zi = Mf[SSF_ZI][e];
+        x.rth = Mf[SSF_RTH][e];
+        x.rcap = Mf[SSF_RCAP][e];
+        x.rrho = Mf[SSF_RRHO][e];
+        x.d = L[SOIL_THICKNESS][slot];
+        x.dtdx = L[SSF_DTDX][slot];
+        x.idwdx = L[SSF_IDWDX][slot];
+        x.dtsy = L[SSF_DTSY][slot];
+        x.k2 = L[SSF_K2][slot];
+        x.qmaxdw = (double)F.Mh[Q_MAX][e] * L[FLOW_WIDTH][slot];
+        wfv::load_up(g, slot, m, x.up);
+    }
+    __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
+                                         double* qh) {
+        double qin;
+        if (!wfv::gather<true>(g, sw, x.up, m, 0, qh[0], F.status, qin)) return false;
+        double q, zi_new, exf, nf;
+        double flag;
+        if (qin + x.q_prev == 0.0 && x.q_net <= 0.0) {
+            q = 0.0;
+            zi_new = x.d;
+            exf = 0.0;
+            nf = 0.0;
+            flag = 1.0;
+        } else {
+            const double cterm = x.dtdx * (qin + x.q_net) + x.t2;
+            q = cterm * x.rdf;
+            if (q != q) q = 0.0;
+            q = jmax(q, KIN_WAVE_MIN_FLOW);
+            q = jmin(q, x.qmaxdw);
+            nf = (qin + x.q_net - q) * x.idwdx;
+            bool full = false;
+            double dh = 0.0;
+            exf = 0.0;
+            if (nf <= 0.0) {
+                dh = nf * x.dtsy;
+            } else if (!(nf > 0.0) || (x.rth != 0.0 && x.rcap <= nf)) {
+                full = true;
+            } else if (x.rth == 0.0) {
+                exf = nf;
+            } else {
+                dh = nf * x.rrho;
+            }
+            double zi = x.zi - dh;
+            if (!full) {
+                if (zi > x.d) q = jmax(q - x.k2 * (zi - x.d), KIN_WAVE_MIN_FLOW);
+                zi = jclamp(zi, 0.0, x.d);
+                if (!(wfm::fabs_(zi - x.zi) * 10.0 <= 1.0)) full = true;
+            }
+            if (full) {
+                ssf_full_split<MAXN>(F, slot, e, qin, x.q_net, sw.dts[0], q, zi, exf, nf);
+                flag = 2.0;
+            } else {
+                flag = 0.0;
+            }
+            zi_new = zi;
+        }
+        double* const* Mf = F.Mf;
+        qh[0] = q;
+        if (is_end) wfv::publish(g, chain, m, 0, q);
+        Mf[SSF_Q][e] = q;
+        Mf[SSF_ZI][e] = zi_new;
+        Mf[SSF_TEXF][e] = exf;
+        Mf[SSF_TNF][e] = nf;
+        Mf[SSF_TQIN][e] = qin;
+        Mf[SSF_FLAG][e] = flag;
+        return true;
+    }
+};
+
+// Overland flow (surface_process.jl:24-70 per node, routing/surface_kinwave.jl sub-steps).
+struct OlWave {
+    WfDevFields F;
+    WfDevGraph g;
+    WfSweep sw;
+    struct In {
+        double u, q, qlat, alpha, inv_dx;
+        bool sfw_pos;
+        wfv::UpList up;
+    };
+    __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
+        x.u = F.Mf[OL_U][e];
+        x.q = F.Mf[OL_Q][e];
+        x.qlat = F.Mf[OL_QLAT][e];
+        x.alpha = F.L[OL_ALPHA][slot];
+        x.inv_dx = F.L[INV_FLOW_LENGTH][slot];
+        x.sfw_pos = F.L[SFW][slot] > 0.0;
+        wfv::load_up(g, slot, m, x.up);
+    }
+    __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
+                                         double* qh) {
+        const int stride = blockDim.x;
+        double u = x.u, qp = x.q, qsum = 0.0;
+        for (int s = 0; s < sw.S; ++s) {
+            const double dt_s = sw.dts[s];
+            double qin;
+            if (!wfv::gather<true>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
+            if (!x.sfw_pos) qin = 0.0;
+            double un, qn;
+            kw_solve_u(qin, qp, x.qlat, dt_s, x.alpha, dt_s * x.inv_dx, u, un, qn);
+            u = un;
+            qp = qn;
+            qh[s * stride] = qn;
+            if (is_end) wfv::publish(g, chain, m, s, qn);
+            qsum = fma(qn, dt_s, qsum);
+        }
+        double* const* Mf = F.Mf;
+        Mf[OL_U][e] = u;
+        Mf[OL_Q][e] = qp;
+        Mf[OL_QSUM][e] = sw.first == 0 ? qsum : Mf[OL_QSUM][e] + qsum;
+        return true;
+    }
+};
+
+// River flow (surface_process.jl:24-70 per node, routing/river_kinwave.jl sub-steps), with the
+// abstraction of a negative external inflow limited to 80 % of the storage.
+struct RvWave {
+    WfDevFields F;
+    WfDevGraph g;
+    WfSweep sw;
+    struct In {
+        double u, q, qlat, qlatt, alpha, inv_len, len, ext;
+        wfv::UpList up;
+    };
+    __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
+        x.u = F.RM[RV_U][e];
+        x.q = F.RM[RV_Q][e];
+        x.qlat = F.RM[RV_QLAT][e];
+        x.qlatt = F.RM[RV_QLATT][e];
+        x.alpha = F.R[R_ALPHA][slot];
+        x.inv_len = F.R[R_INV_LENGTH][slot];
+        x.len = F.R[R_LENGTH][slot];
+        x.ext = F.R[R_EXT_INFLOW][slot];
+        wfv::load_up(g, slot, m, x.up);
+    }
+    __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
+                                         double* qh) {
+        const int stride = blockDim.x;
+        double u = x.u, qp = x.q, qsum = 0.0, asum = 0.0;
+        for (int s = 0; s < sw.S; ++s) {
+            const double dt_s = sw.dts[s];
+            double qin;
+            if (!wfv::gather<false>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
+            double ql = x.qlatt, absd = 0.0;
+            if (x.ext < 0.0) {
+                const double storage = x.len * (x.alpha * (u * u * u));
+                absd = jmin(-x.ext, (storage / dt_s) * 0.80);
+                ql = x.qlat + (-absd / x.len);
+            }
+            double un, qn;
+            kw_solve_u(qin, qp, ql, dt_s, x.alpha, dt_s * x.inv_len, u, un, qn);
+            u = un;
+            qp = qn;
+            qh[s * stride] = qn;
+            if (is_end) wfv::publish(g, chain, m, s, qn);
+            qsum = fma(qn, dt_s, qsum);
+            asum = fma(absd, dt_s, asum);
+        }
+        double* const* RM = F.RM;
+        RM[RV_U][e] = u;
+        RM[RV_Q][e] = qp;
+        RM[RV_QSUM][e] = sw.first == 0 ? qsum : RM[RV_QSUM][e] + qsum;
+        RM[RV_ABSSUM][e] = sw.first == 0 ? asum : RM[RV_ABSSUM][e] + asum;
+        return true;
+    }
+};
+
+template <class Phys>
+__global__ void __launch_bounds__(128) wave_kernel(Phys phys) {
+    wfv::walk(phys.g, phys.sw, phys, phys.F.status);
+}
+
+template <class Phys>
+cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
+    const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
+    const size_t smem = (size_t)threads * phys.sw.S * sizeof(double);
+    int blocks = c.walk_blocks;
+    if (blocks <= 0) {
+        int per_sm = 0;
+        cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wave_kernel<Phys>, threads, smem);
+        if (err != cudaSuccess) return err;
+        blocks = c.num_sms * (per_sm > 0 ? per_sm : 1);
+    }
+    const int64_t items = phys.g.n_chunks * (phys.g.M > 32 ? phys.g.M / 32 : 1);
+    const int64_t need = (items + threads / 32 - 1) / (threads / 32);
+    if (blocks > need) blocks = (int)(need < 1 ? 1 : need);
+    wave_kernel<Phys><<<blocks, threads, smem, c.stream>>>(phys);
+    return cudaGetLastError();
+}
+
+// --------------------------------------------------------------- post-sweep kernels ------
+
+// After the subsurface sweep: unsaturated-layer adjustment to the new water table
+// (soil.jl update_ustorelayerdepth!), averages of the sweep, subsurface storage, the soil
+// water storage update (sbm.jl update_soil_water_storage!) and the overland lateral inflow.
+template <int MAXN>
+__global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph g) {
+    const int M = F.M;
+    const int64_t E = F.land_slots * M;
+    const double dt = F.dt, dt_s = F.dt_ssf;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t slot = e / M;
+        if (F.land_node_of_slot[slot] < 0) continue;
+        const int m = (int)(e - slot * M);
+        double* const* Mf = F.Mf;
+        double* const* L = F.L;
+        const int flag = (int)Mf[SSF_FLAG][e];
+        const double zi_soil = Mf[ZI][e];
+        const double zi_new = Mf[SSF_ZI][e];
+        ColumnS<MAXN> col;
+        col.load_static(F, slot);
+#pragma unroll
+        for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? F.LY[LY_USLD][k][e] : 0.0;
+        double zi_s;
+        if (flag == 0) {
+            col.set_thickness(zi_soil);
+            col.update_ustorelayerdepth(zi_soil, zi_new);
+#pragma unroll
+            for (int k = 0; k < MAXN; ++k)
+                if (k < col.N) F.LY[LY_USLD][k][e] = col.usld[k];
+            Mf[ZI][e] = zi_new;
+            zi_s = zi_new;
+        } else if (flag == 1) {
+            col.set_thickness(zi_soil);
+            zi_s = zi_soil;
+        } else {
+            col.set_thickness(zi_new);
+            zi_s = zi_new;
+        }
+        double tr = 0.0;
+        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o)
+            tr += Mf[SSF_Q][g.up_slot[o] * M + m] * g.up_fr[o];
+        const double area = L[AREA][slot], d = col.d;
+        const double q = Mf[SSF_Q][e], qin = Mf[SSF_TQIN][e], exf = Mf[SSF_TEXF][e], nf = Mf[SSF_TNF][e];
+        const double flux = Mf[SSF_QNET][e];
+        Mf[SSF_STORAGE][e] = L[SY][slot] * (d - zi_new) * area;
+        const double exf_avg = (exf * dt_s) / dt;
+        Mf[RCH_FLUX_AVG][e] = (flux * dt_s) / dt;
+        Mf[SSF_QIN_AVG][e] = (qin * dt_s) / dt;
+        Mf[SSF_Q_AVG][e] = (q * dt_s) / dt;
+        Mf[SSF_QNET_AVG][e] = (nf * area * dt_s) / dt;
+        Mf[SSF_EXF_AVG][e] = exf_avg;
+        Mf[SSF_TR_AVG][e] = (tr * dt_s) / dt;
+        double usd = 0.0;
+#pragma unroll
+        for (int k = 0; k < MAXN; ++k)
+            if (k < col.nu) usd += col.usld[k];
+        const double runoff = jmax(0.0, exf_avg + Mf[SATEX][e] + Mf[RUNOFF_LAND][e] + Mf[INFEX][e]);
+        const double sat = (d - zi_s) * (col.ts - col.tr);
+        Mf[SAT][e] = sat;
+        Mf[USTOREDEPTH][e] = usd;
+        Mf[TSWS][e] = sat + usd;
+        Mf[EXFILT][e] = exf_avg;
+        Mf[RUNOFF][e] = runoff;
+        const double net_runoff = runoff - Mf[AE_LAND][e];
+        Mf[NET_RUNOFF][e] = net_runoff;
+        const double inwater = net_runoff * area;
+        Mf[OL_INWATER][e] = inwater;
+        Mf[OL_QLAT][e] = inwater / L[FLOW_LENGTH][slot];
+    }
+}
+
+// After the overland sweep: water depth and storage, averages, and the lateral inflow of the
+// river cell of each land cell (routing/river_kinwave.jl update_lateral_inflow!).
+__global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph g) {
+    const int M = F.M;
+    const int64_t E = F.land_slots * M;
+    const double dt = F.dt;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t slot = e / M;
+        if (F.land_node_of_slot[slot] < 0) continue;
+        const int m = (int)(e - slot * M);
+        double* const* Mf = F.Mf;
+        double* const* L = F.L;
+        const double sfw = L[SFW][slot], fl = L[FLOW_LENGTH][slot];
+        const double u = Mf[OL_U][e];
+        const double a = L[OL_ALPHA][slot] * (u * u * u);
+        double h = Mf[OL_H][e];
+        if (sfw > 0.0) h = a / sfw;
+        Mf[OL_H][e] = h;
+        Mf[OL_STORAGE][e] = fl * sfw * h;
+        double qin = 0.0, tr = 0.0;
+        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
+            const double qs = Mf[OL_QSUM][g.up_slot[o] * M + m];
+            qin += qs * g.up_w[o];
+            tr += qs * g.up_fr[o];
+        }
+        if (!(sfw > 0.0)) qin = 0.0;
+        Mf[OL_Q_AVG][e] = Mf[OL_QSUM][e] / dt;
+        const double tr_avg = tr / dt;
+        Mf[OL_TR_AVG][e] = tr_avg;
+        Mf[OL_QIN_AVG][e] = qin / dt;
+        const int64_t rs = F.land_river_slot[slot];
+        if (rs >= 0) {
+            const int64_t re = rs * M + m;
+            const double len = F.R[R_LENGTH][rs];
+            const double inw = Mf[SSF_TR_AVG][e] + tr_avg + Mf[NET_RUNOFF_RIVER][e] * F.R[R_AREA][rs];
+            F.RM[RV_INWATER][re] = inw;
+            const double qlat = inw / len;
+            F.RM[RV_QLAT][re] = qlat;
+            const double ext = F.R[R_EXT_INFLOW][rs];
+            F.RM[RV_QLATT][re] = ext < 0.0 ? qlat : qlat + ext / len;
+        }
+    }
+}
+
+// After the river sweep: water depth, storage and averages.
+__global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph g) {
+    const int M = F.M;
+    const int64_t E = F.river_slots * M;
+    const double dt = F.dt;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t slot = e / M;
+        if (F.river_node_of_slot[slot] < 0) continue;
+        const int m = (int)(e - slot * M);
+        double* const* RM = F.RM;
+        double* const* R = F.R;
+        const double u = RM[RV_U][e];
+        const double a = R[R_ALPHA][slot] * (u * u * u);
+        RM[RV_H][e] = a / R[R_WIDTH][slot];
+        RM[RV_STORAGE][e] = R[R_LENGTH][slot] * a;
+        double qin = 0.0;
+        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) qin += RM[RV_QSUM][g.up_slot[o] * M + m];
+        RM[RV_Q_AVG][e] = RM[RV_QSUM][e] / dt;
+        RM[RV_QIN_AVG][e] = qin / dt;
+        RM[RV_ABS_AVG][e] = RM[RV_ABSSUM][e] / dt;
+    }
+}
+
+// u = Q^0.2 of the overland and river discharges (after a discharge was set from outside).
+__global__ void __launch_bounds__(256) sync_u_kernel(WfDevFields F) {
+    const int M = F.M;
+    const int64_t EL = F.land_slots * M, ER = F.river_slots * M;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < EL + ER; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < EL) {
+            F.Mf[OL_U][i] = u_of_q(F.Mf[OL_Q][i]);
+        } else {
+            const int64_t e = i - EL;
+            F.RM[RV_U][e] = u_of_q(F.RM[RV_Q][e]);
+        }
+    }
+}
+
 template <class Phys>
 __global__ void __launch_bounds__(128) walk_split_kernel(Phys phys) {
     wfw::walk(phys.g, phys.sw, phys, phys.F.status);
@@ -892,3 +1606,42 @@ cudaError_t wf_split_river(const WfDevFields& F, const WfDevGraph& g, const WfSw
 }
 
 cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c) { return wf_fp64_balance(F, c); }
+
+cudaError_t wf_split_ssf_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
+    if (F.N <= 4) return launch_wave(SsfWave<4>{F, g, sw}, c);
+    return launch_wave(SsfWave<WF_MAX_LAYERS>{F, g, sw}, c);
+}
+
+cudaError_t wf_split_overland_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw,
+                                   const WfLaunchCfg& c) {
+    return launch_wave(OlWave{F, g, sw}, c);
+}
+
+cudaError_t wf_split_river_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
+    return launch_wave(RvWave{F, g, sw}, c);
+}
+
+cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {
+    const int block = 256;
+    const int grid = grid_for(F.land_slots * F.M, block, c.num_sms);
+    if (F.N <= 4)
+        ssf_post_kernel<4><<<grid, block, 0, c.stream>>>(F, g);
+    else
+        ssf_post_kernel<WF_MAX_LAYERS><<<grid, block, 0, c.stream>>>(F, g);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_split_overland_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {
+    ol_post_kernel<<<grid_for(F.land_slots * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F, g);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_split_river_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {
+    rv_post_kernel<<<grid_for(F.river_slots * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F, g);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_split_sync_u(const WfDevFields& F, const WfLaunchCfg& c) {
+    sync_u_kernel<<<grid_for((F.land_slots + F.river_slots) * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F);
+    return cudaGetLastError();
+}

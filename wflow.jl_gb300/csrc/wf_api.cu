@@ -18,6 +18,7 @@
 
 #include "wf_fields.cuh"
 #include "wf_kernels.h"
+#include "wf_wave.cuh"
 #include "wf_math.cuh"
 #include "wf_plan.h"
 #include "wflow_gb300.h"
@@ -31,6 +32,7 @@ struct DevGraphAlloc {
     int64_t *chunk_base = nullptr, *up_slot = nullptr, *node_of_slot = nullptr;
     int32_t *chunk_len = nullptr, *chain_len = nullptr, *up_ptr = nullptr, *up_chain = nullptr;
     uint8_t* is_chain_end = nullptr;
+    double *up_w = nullptr, *up_fr = nullptr;
     uint32_t* flags = nullptr;
     double* end_q = nullptr;
     unsigned long long* ticket = nullptr;
@@ -65,6 +67,7 @@ struct WfHandle {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
+    bool u_dirty = false;  // split form: discharges were set from outside, u = Q^0.2 is stale
     uint64_t wait_ns = 2000000000ull;  // 2 s per wait
     uint32_t wait_offset = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -173,6 +176,8 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.up_slot = G.up_slot;
     g.up_chain = G.up_chain;
     g.is_chain_end = G.is_chain_end;
+    g.up_w = G.up_w;
+    g.up_fr = G.up_fr;
     g.flags = G.flags;
     g.end_q = G.end_q;
     g.ticket = G.ticket;
@@ -621,6 +626,27 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         {CAP_N, ext_vec(p->cap_n, 0)}, {MAX_LEAKAGE, ext_vec(p->maximum_leakage, 0)}, {W_SOIL, ext_vec(p->w_soil, 0)},
         {CF_SOIL, ext_vec(p->cf_soil, 0)}, {ROOTING_DEPTH, rdclip}, {Z_EXP, ext_vec(p->z_exp, 0)},
         {KH_RATIO, ext_vec(p->horizontal_to_vertical_ratio, 0)}};
+    {
+        // per-cell constants of the slim wavefronts (split form): 1/dx and the subsurface terms
+        // of a single sub-step dt_s
+        const double dts = h->h_dts_ssf[0];
+        std::vector<double> inv_dx(n), dtdx(n), idwdx(n), dtsy(n), k2(n), inv_te(n);
+        for (int64_t i = 0; i < n; ++i) {
+            const double dx = d->flow_length[i], dw = d->flow_width[i];
+            inv_te[i] = 1.0 / (p->theta_s[i] - p->theta_r[i]);
+            inv_dx[i] = 1.0 / dx;
+            dtdx[i] = dts / dx;
+            idwdx[i] = 1.0 / (dw * dx);
+            dtsy[i] = dts / sy[i];
+            k2[i] = (dw * dx) * sy[i] / dts;
+        }
+        ls.push_back({INV_FLOW_LENGTH, inv_dx});
+        ls.push_back({SSF_DTDX, dtdx});
+        ls.push_back({SSF_IDWDX, idwdx});
+        ls.push_back({SSF_DTSY, dtsy});
+        ls.push_back({SSF_K2, k2});
+        ls.push_back({INV_TE, inv_te});
+    }
     for (auto& x : ls) CKR(upload_slots(h, &F.L[x.idx], x.v, PL, M, n, false));
     for (int k = 0; k < N; ++k) {
         std::vector<double> va(act.begin() + (size_t)k * n, act.begin() + (size_t)(k + 1) * n);
@@ -634,6 +660,13 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         CKR(upload_slots(h, &F.LY[LY_ROOTFRAC][k], vr, PL, M, n, false));
         CKR(upload_slots(h, &F.LY[LY_C][k], vc, PL, M, n, false));
         CKR(upload_slots(h, &F.LY[LY_KVFRAC][k], vk, PL, M, n, false));
+        std::vector<double> vcum(n);
+        for (int64_t i = 0; i < n; ++i) {
+            double c = 0.0;
+            for (int j = 0; j <= k; ++j) c += act[(size_t)j * n + i];
+            vcum[i] = c;
+        }
+        CKR(upload_slots(h, &F.LY[LY_CUM][k], vcum, PL, M, n, false));
         std::vector<double> zeros((size_t)n * M, 0.0);
         CKR(upload_slots(h, &F.LY[LY_USLD][k], zeros, PL, M, n, true));
     }
@@ -646,8 +679,10 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         F.nlayers = dnl;
     }
     // ---- land member fields
+    F.split = c->form == WF_FORM_SPLIT;
     std::vector<double> zeros_m((size_t)n * M, 0.0);
     for (int f = 0; f < M_COUNT; ++f) {
+        if (!F.split && wf_split_only_member(f)) continue;
         const std::vector<double>* src = &zeros_m;
         switch (f) {
             case KV0: src = &kv0; break;
@@ -665,10 +700,11 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         CKR(upload_slots(h, &F.Mf[f], *src, PL, M, n, true));
     }
     // ---- river fields
-    std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr);
+    std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr), r_inv_len(nr);
     for (int64_t r = 0; r < nr; ++r) {
         r_width[r] = d->river_width[r];
         r_length[r] = d->river_length[r];
+        r_inv_len[r] = 1.0 / d->river_length[r];
         r_ext[r] = d->river_external_inflow ? d->river_external_inflow[r] : 0.0;
         r_area[r] = d->area[d->river_land_index[r]];
         const double wp = d->river_width[r] + d->river_bankfull_depth[r];
@@ -680,10 +716,30 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     CKR(upload_slots(h, &F.R[R_ALPHA], r_alpha, PR, M, nr, false));
     CKR(upload_slots(h, &F.R[R_EXT_INFLOW], r_ext, PR, M, nr, false));
     CKR(upload_slots(h, &F.R[R_AREA], r_area, PR, M, nr, false));
+    CKR(upload_slots(h, &F.R[R_INV_LENGTH], r_inv_len, PR, M, nr, false));
     std::vector<double> zeros_r((size_t)std::max<int64_t>(nr, 1) * M, 0.0);
-    for (int f = 0; f < RM_COUNT; ++f) CKR(upload_slots(h, &F.RM[f], zeros_r, PR, M, nr, true));
+    for (int f = 0; f < RM_COUNT; ++f) {
+        if (!F.split && wf_split_only_river_member(f)) continue;
+        CKR(upload_slots(h, &F.RM[f], zeros_r, PR, M, nr, true));
+    }
+    // ---- upstream weights of the wavefront gathers: land discharge splits into the part that
+    // goes to the river (flow_fraction_to_river) and the rest that flows downstream
+    for (int g = 0; g < 2; ++g) {
+        DevGraphAlloc& G = g == 0 ? h->land : h->river;
+        const WfRoutingPlan& P = G.plan;
+        const size_t ne = P.up_slot.size();
+        std::vector<double> w(std::max<size_t>(ne, 1), 1.0), fr(std::max<size_t>(ne, 1), 0.0);
+        for (size_t o = 0; o < ne; ++o) {
+            if (g != 0) continue;
+            const int64_t node = P.node_of_slot[P.up_slot[o]];
+            const double f = d->flow_fraction_to_river ? d->flow_fraction_to_river[node] : 0.0;
+            w[o] = 1.0 - f;
+            fr[o] = f;
+        }
+        CKR(upload(h, &G.up_w, w));
+        CKR(upload(h, &G.up_fr, fr));
+    }
     // ---- split form: FP32 copies of the static fields and FP32 member fields
-    F.split = c->form == WF_FORM_SPLIT;
     if (F.split) {
         for (auto& x : ls) CKR(upload_slots_f32(h, &F.Lf[x.idx], x.v, PL, M, n, false));
         for (int k = 0; k < N; ++k) {
@@ -698,6 +754,13 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
             CKR(upload_slots_f32(h, &F.LYf[LY_ROOTFRAC][k], vr, PL, M, n, false));
             CKR(upload_slots_f32(h, &F.LYf[LY_C][k], vc, PL, M, n, false));
             CKR(upload_slots_f32(h, &F.LYf[LY_KVFRAC][k], vk, PL, M, n, false));
+            std::vector<double> vcum(n);
+            for (int64_t i = 0; i < n; ++i) {
+                double cc = 0.0;
+                for (int j = 0; j <= k; ++j) cc += act[(size_t)j * n + i];
+                vcum[i] = cc;
+            }
+            CKR(upload_slots_f32(h, &F.LYf[LY_CUM][k], vcum, PL, M, n, false));
         }
         for (int f = 0; f < M_COUNT; ++f) {
             if (!wf_split_f32_member(f)) continue;
@@ -743,6 +806,10 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     F.kv_profile = c->kv_profile;
     F.mass_balance = c->water_mass_balance;
     F.dt = c->dt;
+    F.inv_dt = 1.0 / c->dt;
+    F.ssf_single = F.split && h->h_dts_ssf.size() == 1;
+    F.dt_ssf = h->h_dts_ssf[0];
+    F.inv_dt_ssf = 1.0 / h->h_dts_ssf[0];
     CKR(dalloc(h, &h->status, 1));
     CK(cudaMemset(h->status, 0, sizeof(int32_t)));
     F.status = h->status;
@@ -907,6 +974,7 @@ int32_t wf_set_field(WfHandle* h, int32_t field, int32_t layer, const double* sr
                                                                              n_ext);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
+    if (field == WF_F_LAND_Q || field == WF_F_RIVER_Q) h->u_dirty = true;
     return WF_OK;
 }
 
@@ -1089,13 +1157,56 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         }
         return WF_OK;
     };
+    // split form: slim wavefronts (end_q sentinel hand-off, node-major sub-step groups)
+    // followed by their per-cell completion kernels
+    auto wave = [&](DevGraphAlloc& G, const WfDevGraph& g, const std::vector<double>& dts, double* d_dts,
+                    int which) -> int {
+        const int total = (int)dts.size();
+        const int group = std::min<int>(G.s_cap, wfv::MAX_GROUP);
+        for (int first = 0; first < total; first += group) {
+            WfSweep sw{};
+            sw.S = std::min(group, total - first);
+            sw.first = first;
+            sw.last_of_step = (first + sw.S == total);
+            sw.total = total;
+            sw.epoch0 = 1;
+            sw.dt = h->cfg.dt;
+            sw.dts = d_dts + first;
+            sw.wait_ns = h->wait_ns;
+            sw.wait_offset = h->wait_offset;
+            CK(cudaMemsetAsync(G.end_q, 0xFF, (size_t)G.plan.n_chains * h->M * G.s_cap * sizeof(double), h->stream));
+            CK(cudaMemsetAsync(G.ticket, 0, sizeof(unsigned long long), h->stream));
+            cudaError_t e;
+            if (which == 0) e = wf_split_ssf_wave(h->F, g, sw, lc);
+            else if (which == 1) e = wf_split_overland_wave(h->F, g, sw, lc);
+            else e = wf_split_river_wave(h->F, g, sw, lc);
+            CK(e);
+            ++nl;
+        }
+        if (which == 0) CK(wf_split_ssf_post(h->F, g, lc));
+        else if (which == 1) CK(wf_split_overland_post(h->F, g, lc));
+        else CK(wf_split_river_post(h->F, g, lc));
+        ++nl;
+        return WF_OK;
+    };
     int rc;
-    if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;
-    mark(2);
-    if ((rc = sweep(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
-    mark(3);
-    if (h->nr > 0 && (rc = sweep(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
-    mark(4);
+    if (split) {
+        if (h->F.ssf_single) rc = wave(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0);
+        else rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0);
+        if (rc) return rc;
+        mark(2);
+        if ((rc = wave(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
+        mark(3);
+        if (h->nr > 0 && (rc = wave(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
+        mark(4);
+    } else {
+        if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;
+        mark(2);
+        if ((rc = sweep(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
+        mark(3);
+        if (h->nr > 0 && (rc = sweep(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
+        mark(4);
+    }
     CK(split ? wf_split_balance(h->F, lc) : wf_fp64_balance(h->F, lc));
     ++nl;
     mark(5);
@@ -1114,6 +1225,10 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
 
 int run_step(WfHandle* h) {
     int64_t launches = 0;
+    if (h->u_dirty) {
+        if (h->cfg.form == WF_FORM_SPLIT) CK(wf_split_sync_u(h->F, launch_cfg(h)));
+        h->u_dirty = false;
+    }
     if (h->tuning.use_graph) {
         if (!h->graph_valid) {
             if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);

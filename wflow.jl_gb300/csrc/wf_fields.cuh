@@ -16,7 +16,8 @@
     X(WATER_FRACTION) X(TOP) X(OL_ALPHA) X(SY) X(GAP) X(CMAX) X(KC) X(E_R) X(DDF) X(TT) X(TTI) X(TTM) \
     X(WHC) X(THETA_S) X(THETA_R) X(THETA_FC) X(SWC) X(SOIL_THICKNESS) X(PSI_B) X(H1) X(H2) X(H3_HIGH) \
     X(H3_LOW) X(H4) X(ALPHA_H1) X(CAP_COMP) X(COMPACT_FRAC) X(ROOTDISTPAR) X(CAP_HMAX) X(CAP_N)       \
-    X(MAX_LEAKAGE) X(W_SOIL) X(CF_SOIL) X(ROOTING_DEPTH) X(Z_EXP) X(KH_RATIO)
+    X(MAX_LEAKAGE) X(W_SOIL) X(CF_SOIL) X(ROOTING_DEPTH) X(Z_EXP) X(KH_RATIO) X(INV_FLOW_LENGTH)  \
+    X(SSF_DTDX) X(SSF_IDWDX) X(SSF_DTSY) X(SSF_K2) X(INV_TE)
 
 #define WF_M_FIELDS(X)                                                                             \
     X(KV0) X(FSCALE) X(Q_MAX) X(PRECIP) X(POTEVAP) X(TEMP) X(CANOPY) X(SNOW) X(SNOW_WATER) X(TSOIL) X(SAT) X(TSWS)    \
@@ -27,13 +28,16 @@
     X(RECHARGE) X(NET_RUNOFF_RIVER) X(AET) X(LEAKAGE) X(SATEX) X(INFEX) X(RUNOFF_LAND) X(AE_LAND)     \
     X(INTERCEPTION) X(TRANSPIRATION) X(SOIL_EVAP) X(ACT_INFILT) X(SWE) X(NET_RUNOFF) X(RUNOFF)        \
     X(EXFILT) X(BL_PREV) X(BO_PREV) X(TOTAL_STORAGE) X(BL_ERR) X(BL_REL) X(BO_ERR) X(BO_REL)          \
-    X(BS_ERR) X(BS_REL)
+    X(BS_ERR) X(BS_REL)                                                                            \
+    X(SSF_QNET) X(SSF_T2) X(SSF_RDF) X(SSF_RTH) X(SSF_RCAP) X(SSF_RRHO) X(SSF_TQIN) X(SSF_TEXF)     \
+    X(SSF_TNF) X(SSF_FLAG) X(OL_U) X(OL_QSUM)
 
-#define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA)
+#define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA) X(R_INV_LENGTH)
 
 #define WF_RM_FIELDS(X)                                                                            \
     X(RV_Q) X(RV_H) X(RV_STORAGE) X(RV_Q_AVG) X(RV_QIN_AVG) X(RV_INWATER) X(RV_QLAT) X(RV_ABS_AVG)    \
-    X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL)
+    X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL) X(RV_U) X(RV_QSUM) X(RV_ABSSUM) \
+    X(RV_QLATT)
 
 #define WF_ENUM_ITEM(name) name,
 enum WfLandStatic { WF_L_FIELDS(WF_ENUM_ITEM) L_COUNT };
@@ -43,7 +47,8 @@ enum WfRiverMember { WF_RM_FIELDS(WF_ENUM_ITEM) RM_COUNT };
 #undef WF_ENUM_ITEM
 
 // Layered fields: N arrays each.
-enum WfLayered { LY_ACT_THICK = 0, LY_C, LY_KVFRAC, LY_ROOTFRAC, LY_USLD, LY_COUNT };
+// LY_CUM: depth of the bottom of each layer (cumulative thickness, static).
+enum WfLayered { LY_ACT_THICK = 0, LY_C, LY_KVFRAC, LY_ROOTFRAC, LY_USLD, LY_CUM, LY_COUNT };
 
 // Member fields kept in FP32 by the split form (pure diagnostics, forcing, parameters);
 // every other member field (storages, balance terms, routing state) stays FP64.
@@ -51,6 +56,10 @@ __host__ __device__ inline bool wf_split_f32_member(int f) {
     return f == KV0 || f == FSCALE || f == Q_MAX || f == PRECIP || f == POTEVAP || f == TEMP || f == TSOIL ||
            f == INTERCEPTION || f == TRANSPIRATION || f == SOIL_EVAP || f == ACT_INFILT || f == SWE;
 }
+
+// Member fields only the split form's slim wavefront uses (not allocated by the FP64 form).
+__host__ __device__ inline bool wf_split_only_member(int f) { return f >= SSF_QNET; }
+__host__ __device__ inline bool wf_split_only_river_member(int f) { return f >= RV_U; }
 
 struct WfDevFields {
     double* L[L_COUNT];
@@ -78,7 +87,11 @@ struct WfDevFields {
     int32_t gash;
     int32_t kv_profile;
     int32_t mass_balance;
+    int32_t ssf_single;   // split form: one subsurface sub-step per step (slim subsurface wavefront)
     double dt;
+    double inv_dt;        // 1 / dt
+    double dt_ssf;        // subsurface sub-step when ssf_single
+    double inv_dt_ssf;    // 1 / dt_ssf
     int32_t* status;  // device status word (0 = ok)
 };
 
@@ -96,6 +109,8 @@ struct WfDevGraph {
     const int64_t* up_slot;
     const int32_t* up_chain;
     const uint8_t* is_chain_end;
+    const double* up_w;   // [up entries] weight of the upstream discharge (land: 1 - fraction to river)
+    const double* up_fr;  // [up entries] fraction of the upstream discharge to the river (land only)
     uint32_t* flags;      // [n_chains * M] epoch of the last published sub-step
     double* end_q;        // [n_chains * M * s_cap] q of each chain end per sub-step
     unsigned long long* ticket;  // work counter of the current launch

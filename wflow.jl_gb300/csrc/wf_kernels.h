@@ -30,6 +30,15 @@ cudaError_t wf_split_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSwee
 cudaError_t wf_split_overland(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
 cudaError_t wf_split_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
 cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c);
+// slim wavefronts of the split form (wf_wave.cuh) and their per-cell completion kernels
+cudaError_t wf_split_ssf_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_split_overland_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw,
+                                   const WfLaunchCfg& c);
+cudaError_t wf_split_river_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
+cudaError_t wf_split_overland_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
+cudaError_t wf_split_river_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
+cudaError_t wf_split_sync_u(const WfDevFields& F, const WfLaunchCfg& c);
 
 // gather/scatter between the external (land/river) order and the slot order
 cudaError_t wf_gather_ext(const double* src_ext, double* dst_slots, const int64_t* node_of_slot, int64_t slots,

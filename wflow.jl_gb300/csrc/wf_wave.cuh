@@ -1,0 +1,184 @@
+// wf_wave.cuh -- slim persistent wavefront walker (node-major sub-steps, sentinel hand-off).
+//
+// Only the discharge propagates downstream in a kinematic-wave sweep, so the walker carries
+// nothing but the solve: per-node terms that do not depend on the upstream discharge are
+// prepared by the per-cell kernels before the sweep, and every output that nothing downstream
+// reads (water depths, storages, averages, soil-column updates) is finished by per-cell
+// kernels after it. What remains on the critical path of a chain position is the gather of
+// the upstream discharges and the solve.
+//
+// A warp owns one chunk (G chains x M members, or one chain x 32 members) taken from a global
+// ticket counter in chain-length order, and walks it leaf -> chain end. Each node is advanced
+// through all sub-steps of the launch before the walker moves downstream (node-major order):
+// the node's own state stays in registers across sub-steps and the heavy child's discharge
+// of every sub-step is handed over in a per-thread shared-memory row. Chain ends publish the
+// discharge of each sub-step into end_q, which is filled with a sentinel bit pattern before
+// the launch; a consumer reads the slot with a relaxed 64-bit load until the sentinel is gone
+// (one round trip instead of flag-then-value). No value other than the published discharge
+// itself crosses warps, so no acquire/release pairing is needed: 64-bit aligned stores and
+// loads are single-copy atomic.
+//
+// Every wait is bounded by a wall-clock budget (globaltimer); a wait that runs out sets
+// WF_DEV_SPIN_TIMEOUT in the device status word and all lanes abort.
+#pragma once
+
+#include <cstdint>
+
+#include "wf_fields.cuh"
+
+namespace wfv {
+
+constexpr unsigned long long SENTINEL = 0xFFFFFFFFFFFFFFFFULL;   // end_q fill (a NaN no arithmetic yields here)
+constexpr unsigned long long QUIET_NAN = 0x7FF8000000000000ULL;  // published in place of the sentinel pattern
+constexpr int MAX_GROUP = 16;                                    // sub-steps per launch of the slim walker
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const double* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(double* p, double x) {
+    unsigned long long v = (unsigned long long)__double_as_longlong(x);
+    if (v == SENTINEL) v = QUIET_NAN;
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t now_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ int32_t status_ld(const int32_t* s) {
+    return *reinterpret_cast<const volatile int32_t*>(s);
+}
+
+// end_q index of chain `chain`, member m, sub-step s of the launch (members innermost, so a
+// warp of 32 members reads 256 contiguous bytes).
+__device__ __forceinline__ int64_t end_index(const WfDevGraph& g, int64_t chain, int m, int s) {
+    return (chain * g.s_cap + s) * g.M + m;
+}
+
+// Discharge published at end_q[idx]; `first` is a value already loaded from that slot (or the
+// sentinel). False when the budget ran out or another lane aborted. `hold` (test hook, 0 in
+// production) makes every wait run out.
+__device__ __forceinline__ bool await_end(const WfDevGraph& g, const WfSweep& sw, int64_t idx,
+                                          unsigned long long first, int32_t* status, double& out) {
+    unsigned long long b = first;
+    if (b != SENTINEL && sw.wait_offset == 0) {
+        out = __longlong_as_double((long long)b);
+        return true;
+    }
+    const uint64_t t0 = now_ns();
+    while (true) {
+        __nanosleep(32);
+        b = ld_relaxed(&g.end_q[idx]);
+        if (b != SENTINEL && sw.wait_offset == 0) {
+            out = __longlong_as_double((long long)b);
+            return true;
+        }
+        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return false;
+        if (now_ns() - t0 > sw.wait_ns) {
+            atomicOr(status, WF_DEV_SPIN_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void publish(const WfDevGraph& g, int64_t chain, int m, int s, double q) {
+    st_relaxed(&g.end_q[end_index(g, chain, m, s)], q);
+}
+
+// Upstream list of one node with its first light entry prefetched for sub-step 0.
+struct UpList {
+    int32_t o0, o1;
+    int32_t lo;                // up entry of the prefetched light child (-1: none)
+    unsigned long long lq;     // its end_q content at prefetch time (may be the sentinel)
+};
+
+__device__ __forceinline__ void load_up(const WfDevGraph& g, int64_t slot, int m, UpList& u) {
+    u.o0 = g.up_ptr[slot];
+    u.o1 = g.up_ptr[slot + 1];
+    u.lo = -1;
+    u.lq = SENTINEL;
+    for (int32_t o = u.o0; o < u.o1; ++o) {
+        const int32_t uc = g.up_chain[o];
+        if (uc >= 0) {
+            u.lo = o;
+            u.lq = ld_relaxed(&g.end_q[end_index(g, uc, m, 0)]);
+            break;
+        }
+    }
+}
+
+// Weighted upstream sums at sub-step s in up-list order: qin = sum w*q (w = 1 - fraction to
+// river on land, 1 on rivers). `qh` is the heavy child's discharge of this sub-step.
+template <bool WEIGHTED>
+__device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, const UpList& u, int m, int s,
+                                       double qh, int32_t* status, double& qin) {
+    double acc = 0.0;
+    for (int32_t o = u.o0; o < u.o1; ++o) {
+        const int32_t uc = g.up_chain[o];
+        double q;
+        if (uc < 0) {
+            q = qh;
+        } else {
+            const int64_t idx = end_index(g, uc, m, s);
+            const unsigned long long first = (o == u.lo && s == 0) ? u.lq : ld_relaxed(&g.end_q[idx]);
+            if (!await_end(g, sw, idx, first, status, q)) return false;
+        }
+        acc = WEIGHTED ? acc + q * g.up_w[o] : acc + q;
+    }
+    qin = acc;
+    return true;
+}
+
+// Phys interface:
+//   struct In;                                               per-node inputs (prefetched)
+//   void load(int64_t slot, int64_t e, int m, In&)           independent of upstream discharge
+//   bool node(const In&, int64_t slot, int64_t e, int m, int64_t chain, bool is_end, double* qh)
+//     advances the node through sw.S sub-steps; qh[s * stride] holds the heavy child's discharge
+//     of sub-step s on entry and this node's discharge on exit. Returns false to abort.
+template <class Phys>
+__device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
+    extern __shared__ double wave_smem[];
+    const unsigned lane = threadIdx.x & 31u;
+    double* qh = wave_smem + threadIdx.x;  // row of this thread: qh[s * blockDim.x]
+    const int M = g.M, G = g.G;
+    const int gpc = M > 32 ? M / 32 : 1;
+    const uint64_t n_items = (uint64_t)g.n_chunks * gpc;
+    while (true) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(g.ticket, 1ULL);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= n_items) return;
+        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
+        const int64_t chunk = (int64_t)(item / gpc);
+        int gi, m;
+        if (M <= 32) {
+            gi = (int)lane / M;
+            m = (int)lane % M;
+        } else {
+            gi = 0;
+            m = (int)(item % gpc) * 32 + (int)lane;
+        }
+        const int64_t chain = chunk * G + gi;
+        const int len = g.chain_len[chain];
+        const int L = g.chunk_len[chunk];
+        const int64_t base = g.chunk_base[chunk];
+        typename Phys::In cur, nxt;
+        if (len > 0) phys.load(base + gi, (base + gi) * M + m, m, cur);
+        for (int k = 0; k < L; ++k) {
+            const int64_t slot = base + (int64_t)k * G + gi;
+            if (k + 1 < len) {
+                const int64_t ns = slot + G;
+                phys.load(ns, ns * M + m, m, nxt);
+            }
+            bool ok = true;
+            if (k < len) ok = phys.node(cur, slot, slot * M + m, m, chain, k == len - 1, qh);
+            if (__any_sync(0xffffffffu, !ok)) return;
+            __syncwarp();
+            cur = nxt;
+        }
+    }
+}
+
+}  // namespace wfv
