@@ -261,6 +261,28 @@ int32_t wf_set_forcing_device_slots(WfHandle* h, const void* precipitation,
 int32_t wf_step(WfHandle* h);
 /* Asynchronous variant: enqueue the step on the handle's stream without waiting. */
 int32_t wf_step_async(WfHandle* h);
+
+/* Size of the static scratch of wf_step_static (bytes). */
+#define WF_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
+/* One model step like wf_step (same kernels, same results), allocating nothing: no cudaMalloc,
+ * cudaFree, CUDA graph instantiation or other allocating call. It has no counterpart in the
+ * reference (Wflow.jl has no allocation-free step); it is for hosts that cannot allocate
+ * device memory once the model exists, such as frameworks that reserve the whole device for
+ * their own memory pool after set-up and coupling loops that cannot afford the device-wide
+ * synchronisation of an allocation.
+ *   - The routing wavefronts take their scratch (work ticket, chain-end flags, published
+ *     chain-end discharges) from one file-scope device array of WF_STATIC_SCRATCH_BYTES.
+ *     Models whose scratch need exceeds it, (256 + 4 * chains * members rounded up to 256 +
+ *     8 * chains * members * sub-steps per launch) bytes for the larger of the land and river
+ *     graphs, are rejected with WF_ERR_UNSUPPORTED and a message giving the need.
+ *   - The first call on a device looks the array's address up (cudaGetSymbolAddress, with that
+ *     device current); make that first call before any stream capture.
+ *   - Every call on a device shares the array, which keeps the last call's contents; each sweep
+ *     clears what must start at zero before it runs. Calls that overlap on the GPU (handles
+ *     stepped concurrently from different streams or threads) race on the array and must be
+ *     serialised by the caller.
+ * Synchronous on return, like wf_step. */
+int32_t wf_step_static(WfHandle* h);
 int32_t wf_synchronize(WfHandle* h);
 
 /* Copy a field to host (count values from element offset; member-major over land or river

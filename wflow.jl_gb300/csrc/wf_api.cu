@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1276,4 +1277,158 @@ cudaError_t wf_scatter_ext(const double* src_slots, double* dst_ext, const int64
                            int64_t n_ext, cudaStream_t s) {
     scatter_kernel<<<grid_of(slots * M, 256), 256, 0, s>>>(src_slots, dst_ext, node_of_slot, slots, M, n_ext);
     return cudaGetLastError();
+}
+
+// ===================================================================== static scratch ====
+//
+// wf_step_static: the model step without any allocation. The routing wavefronts take their
+// scratch (work ticket, chain-end flags, published chain-end discharges) from one file-scope
+// device array instead of the handle's buffers, and the step's launches are issued directly
+// (no CUDA graph is built or instantiated). The array is shared by every handle and every call
+// on a device and keeps the last call's contents; each sweep launch clears what must start at
+// zero (ticket, flags) or at the sentinel (published discharges) before it runs.
+
+static __device__ __align__(256) unsigned char wf_static_scratch[WF_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+unsigned char* g_static_ptr[kStaticMaxDevices] = {};
+
+// Device address of the static scratch on the handle's device, looked up once per device with
+// that device current (the first wf_step_static call on a device does this).
+int static_scratch(WfHandle* h, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (h->device < 0 || h->device >= kStaticMaxDevices)
+        return set_err(h, WF_ERR_INVALID, "wf_step_static: device index out of range");
+    if (!g_static_ptr[h->device]) {
+        int prev = -1;
+        CK(cudaGetDevice(&prev));
+        CK(cudaSetDevice(h->device));
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, wf_static_scratch);
+        const cudaError_t e2 = cudaSetDevice(prev);
+        if (e != cudaSuccess)
+            return set_err(h, WF_ERR_CUDA,
+                           std::string("wf_step_static: cudaGetSymbolAddress of the static scratch failed: ") +
+                               cudaGetErrorString(e));
+        if (e2 != cudaSuccess) return set_err(h, WF_ERR_CUDA, "wf_step_static: restoring the current device failed");
+        g_static_ptr[h->device] = (unsigned char*)p;
+    }
+    *out = g_static_ptr[h->device];
+    return WF_OK;
+}
+
+// Scratch bytes one sweep launch of graph G needs: ticket, flags, published discharges.
+size_t static_need(const DevGraphAlloc& G, int M) {
+    const size_t slots = (size_t)G.plan.n_chains * M;
+    const size_t flags = (slots * sizeof(uint32_t) + 255) / 256 * 256;
+    return 256 + flags + slots * G.s_cap * sizeof(double);
+}
+
+// Graph view whose scratch points into the static array.
+WfDevGraph static_graph(const DevGraphAlloc& G, int M, unsigned char* base) {
+    WfDevGraph g = dev_graph(G, M);
+    const size_t slots = (size_t)G.plan.n_chains * M;
+    g.ticket = (unsigned long long*)base;
+    g.flags = (uint32_t*)(base + 256);
+    g.end_q = (double*)(base + 256 + (slots * sizeof(uint32_t) + 255) / 256 * 256);
+    return g;
+}
+
+// The launches of enqueue_step with the wavefront scratch of the static array.
+int enqueue_step_static(WfHandle* h, unsigned char* base, int64_t* launches) {
+    const WfLaunchCfg lc = launch_cfg(h);
+    const bool split = h->cfg.form == WF_FORM_SPLIT;
+    int64_t nl = 0;
+    const WfDevGraph gl = static_graph(h->land, h->M, base), gr = static_graph(h->river, h->M, base);
+    CK(split ? wf_split_vertical(h->F, lc) : wf_fp64_vertical(h->F, lc));
+    ++nl;
+    auto clear = [&](const DevGraphAlloc& G, const WfDevGraph& g, bool sentinel) -> int {
+        const size_t slots = (size_t)G.plan.n_chains * h->M;
+        CK(cudaMemsetAsync(g.ticket, 0, sizeof(unsigned long long), h->stream));
+        if (sentinel) CK(cudaMemsetAsync(g.end_q, 0xFF, slots * G.s_cap * sizeof(double), h->stream));
+        else CK(cudaMemsetAsync(g.flags, 0, slots * sizeof(uint32_t), h->stream));
+        return WF_OK;
+    };
+    auto sweep = [&](const DevGraphAlloc& G, const WfDevGraph& g, const std::vector<double>& dts, double* d_dts,
+                     int which, bool wave) -> int {
+        const int total = (int)dts.size();
+        const int group = wave ? std::min<int>(G.s_cap, wfv::MAX_GROUP) : G.s_cap;
+        for (int first = 0; first < total; first += group) {
+            WfSweep sw{};
+            sw.S = std::min(group, total - first);
+            sw.first = first;
+            sw.last_of_step = (first + sw.S == total);
+            sw.total = total;
+            sw.epoch0 = 1;
+            sw.dt = h->cfg.dt;
+            sw.dts = d_dts + first;
+            sw.wait_ns = h->wait_ns;
+            sw.wait_offset = h->wait_offset;
+            int rc = clear(G, g, wave);
+            if (rc) return rc;
+            cudaError_t e;
+            if (wave) {
+                if (which == 0) e = wf_split_ssf_wave(h->F, g, sw, lc);
+                else if (which == 1) e = wf_split_overland_wave(h->F, g, sw, lc);
+                else e = wf_split_river_wave(h->F, g, sw, lc);
+            } else if (which == 0) {
+                e = split ? wf_split_ssf(h->F, g, sw, lc) : wf_fp64_ssf(h->F, g, sw, lc);
+            } else if (which == 1) {
+                e = wf_fp64_overland(h->F, g, sw, lc);
+            } else {
+                e = wf_fp64_river(h->F, g, sw, lc);
+            }
+            CK(e);
+            ++nl;
+        }
+        if (wave) {
+            if (which == 0) CK(wf_split_ssf_post(h->F, g, lc));
+            else if (which == 1) CK(wf_split_overland_post(h->F, g, lc));
+            else CK(wf_split_river_post(h->F, g, lc));
+            ++nl;
+        }
+        return WF_OK;
+    };
+    int rc;
+    if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0, split && h->F.ssf_single))) return rc;
+    if ((rc = sweep(h->land, gl, h->h_dts_land, h->dts_land, 1, split))) return rc;
+    if (h->nr > 0 && (rc = sweep(h->river, gr, h->h_dts_river, h->dts_river, 2, split))) return rc;
+    CK(split ? wf_split_balance(h->F, lc) : wf_fp64_balance(h->F, lc));
+    ++nl;
+    if (launches) *launches = nl;
+    return WF_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t wf_step_static(WfHandle* h) {
+    if (!h) return WF_ERR_INVALID;
+    const size_t need = std::max(static_need(h->land, h->M), h->nr > 0 ? static_need(h->river, h->M) : (size_t)0);
+    if (need > (size_t)WF_STATIC_SCRATCH_BYTES) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg),
+                      "wf_step_static: the routing wavefronts of this model need %zu bytes of scratch, more than "
+                      "the %zu-byte static scratch; use wf_step",
+                      need, (size_t)WF_STATIC_SCRATCH_BYTES);
+        return set_err(h, WF_ERR_UNSUPPORTED, msg);
+    }
+    unsigned char* base = nullptr;
+    int rc = static_scratch(h, &base);
+    if (rc) return rc;
+    if (h->u_dirty) {
+        if (h->cfg.form == WF_FORM_SPLIT) CK(wf_split_sync_u(h->F, launch_cfg(h)));
+        h->u_dirty = false;
+    }
+    int64_t launches = 0;
+    if ((rc = enqueue_step_static(h, base, &launches))) return rc;
+    h->metrics.steps += 1;
+    h->metrics.cell_steps += h->n * h->M;
+    h->metrics.kernel_launches += launches;
+    h->metrics.substeps_land += (int64_t)h->h_dts_land.size();
+    h->metrics.substeps_river += (int64_t)h->h_dts_river.size();
+    h->metrics.substeps_subsurface += (int64_t)h->h_dts_ssf.size();
+    return wf_synchronize(h);
 }

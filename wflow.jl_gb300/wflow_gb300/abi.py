@@ -20,6 +20,7 @@ WF_MAX_LAYERS = 8
 
 # WfStatus
 WF_OK = 0
+WF_STATIC_SCRATCH_BYTES = 16 * 1024 * 1024  # static scratch of wf_step_static
 WF_ERR_INVALID = -1
 WF_ERR_CUDA = -2
 WF_ERR_CYCLE = -3
@@ -182,6 +183,7 @@ def _declare(lib):
         "wf_set_forcing_device_slots": (_i32, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
         "wf_step": (_i32, [H]),
         "wf_step_async": (_i32, [H]),
+        "wf_step_static": (_i32, [H]),
         "wf_synchronize": (_i32, [H]),
         "wf_get_field": (_i32, [H, _i32, _i32, _pd, _i64, _i64]),
         "wf_set_field": (_i32, [H, _i32, _i32, _pd, _i64, _i64]),

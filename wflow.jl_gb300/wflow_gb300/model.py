@@ -66,6 +66,11 @@ class Model:
         self.set_forcing(precipitation, potential_evaporation, temperature)
         self.update_model()
 
+    def update_model_static(self):
+        """The step without any allocation (wf_step_static): scratch from a fixed 16 MiB device
+        array shared by all models on the device; calls must not overlap on the GPU."""
+        self._check(self.lib.wf_step_static(self.h), "wf_step_static")
+
     def step_async(self):
         self._check(self.lib.wf_step_async(self.h), "wf_step_async")
 
