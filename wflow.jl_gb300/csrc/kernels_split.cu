@@ -1403,11 +1403,13 @@ cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
 // After the subsurface sweep: unsaturated-layer adjustment to the new water table
 // (soil.jl update_ustorelayerdepth!), averages of the sweep, subsurface storage, the soil
 // water storage update (sbm.jl update_soil_water_storage!) and the overland lateral inflow.
+// FP64 for the stores; divisions replaced by static reciprocals.
 template <int MAXN>
 __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph g) {
     const int M = F.M;
+    const int N = F.N;
     const int64_t E = F.land_slots * M;
-    const double dt = F.dt, dt_s = F.dt_ssf;
+    const double r_s = F.dt_ssf * F.inv_dt;  // sub-step / step (1 when they are equal)
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
@@ -1417,46 +1419,74 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
         const int flag = (int)Mf[SSF_FLAG][e];
         const double zi_soil = Mf[ZI][e];
         const double zi_new = Mf[SSF_ZI][e];
-        ColumnS<MAXN> col;
-        col.load_static(F, slot);
+        double usld[MAXN], act[MAXN], cum[MAXN + 1];  // cum[k]: depth of the top of layer k
+        cum[0] = 0.0;
 #pragma unroll
-        for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? F.LY[LY_USLD][k][e] : 0.0;
-        double zi_s;
-        if (flag == 0) {
-            col.set_thickness(zi_soil);
-            col.update_ustorelayerdepth(zi_soil, zi_new);
+        for (int k = 0; k < MAXN; ++k) {
+            usld[k] = k < N ? F.LY[LY_USLD][k][e] : 0.0;
+            act[k] = k < N ? F.LY[LY_ACT_THICK][k][slot] : 0.0;
+            cum[k + 1] = k < N ? F.LY[LY_CUM][k][slot] : __longlong_as_double(0x7ff8000000000000LL);
+        }
+        // layer k is unsaturated iff the water table lies below its top (utils.jl set_layerthickness)
+        auto nu_at = [&](double ref) {
+            int c = 0;
 #pragma unroll
             for (int k = 0; k < MAXN; ++k)
-                if (k < col.N) F.LY[LY_USLD][k][e] = col.usld[k];
-            Mf[ZI][e] = zi_new;
-            zi_s = zi_new;
+                if (k < N && ref > cum[k]) ++c;
+            return c;
+        };
+        auto thick_at = [&](double ref, int k) {
+            return ref > cum[k + 1] ? act[k] : (ref > cum[k] ? ref - cum[k] : __longlong_as_double(0x7ff8000000000000LL));
+        };
+        double zi_s = zi_new;
+        if (flag == 0) {
+            if (zi_new != zi_soil) {
+                const int n_prev = nu_at(zi_soil), n_new = nu_at(zi_new);
+                if (zi_new < zi_soil) {
+#pragma unroll
+                    for (int k = 1; k <= MAXN; ++k) {
+                        if (k < n_new || k > n_prev) continue;
+                        const double t = thick_at(zi_new, k - 1);
+                        usld[k - 1] = t != t ? 0.0 : t * wfm_rcp(thick_at(zi_soil, k - 1)) * usld[k - 1];
+                        F.LY[LY_USLD][k - 1][e] = usld[k - 1];
+                    }
+                } else {
+                    const double tfc_tr = L[THETA_FC][slot] - L[THETA_R][slot];
+#pragma unroll
+                    for (int k = 1; k <= MAXN; ++k) {
+                        if (k < n_prev || k > n_new) continue;
+                        double tp = thick_at(zi_soil, k - 1);
+                        tp = tp != tp ? 0.0 : tp;
+                        usld[k - 1] = usld[k - 1] + (thick_at(zi_new, k - 1) - tp) * tfc_tr;
+                        F.LY[LY_USLD][k - 1][e] = usld[k - 1];
+                    }
+                }
+                Mf[ZI][e] = zi_new;
+            }
         } else if (flag == 1) {
-            col.set_thickness(zi_soil);
             zi_s = zi_soil;
-        } else {
-            col.set_thickness(zi_new);
-            zi_s = zi_new;
         }
+        const int nu = nu_at(zi_s);
         double tr = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o)
             tr += Mf[SSF_Q][g.up_slot[o] * M + m] * g.up_fr[o];
-        const double area = L[AREA][slot], d = col.d;
+        const double area = L[AREA][slot], d = L[SOIL_THICKNESS][slot];
         const double q = Mf[SSF_Q][e], qin = Mf[SSF_TQIN][e], exf = Mf[SSF_TEXF][e], nf = Mf[SSF_TNF][e];
         const double flux = Mf[SSF_QNET][e];
         Mf[SSF_STORAGE][e] = L[SY][slot] * (d - zi_new) * area;
-        const double exf_avg = (exf * dt_s) / dt;
-        Mf[RCH_FLUX_AVG][e] = (flux * dt_s) / dt;
-        Mf[SSF_QIN_AVG][e] = (qin * dt_s) / dt;
-        Mf[SSF_Q_AVG][e] = (q * dt_s) / dt;
-        Mf[SSF_QNET_AVG][e] = (nf * area * dt_s) / dt;
+        const double exf_avg = exf * r_s;
+        Mf[RCH_FLUX_AVG][e] = flux * r_s;
+        Mf[SSF_QIN_AVG][e] = qin * r_s;
+        Mf[SSF_Q_AVG][e] = q * r_s;
+        Mf[SSF_QNET_AVG][e] = nf * area * r_s;
         Mf[SSF_EXF_AVG][e] = exf_avg;
-        Mf[SSF_TR_AVG][e] = (tr * dt_s) / dt;
+        Mf[SSF_TR_AVG][e] = tr * r_s;
         double usd = 0.0;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k)
-            if (k < col.nu) usd += col.usld[k];
-        const double runoff = jmax(0.0, exf_avg + Mf[SATEX][e] + Mf[RUNOFF_LAND][e] + Mf[INFEX][e]);
-        const double sat = (d - zi_s) * (col.ts - col.tr);
+            if (k < nu) usd += usld[k];
+        const double runoff = fmax(0.0, exf_avg + Mf[SATEX][e] + Mf[RUNOFF_LAND][e] + Mf[INFEX][e]);
+        const double sat = (d - zi_s) * (L[THETA_S][slot] - L[THETA_R][slot]);
         Mf[SAT][e] = sat;
         Mf[USTOREDEPTH][e] = usd;
         Mf[TSWS][e] = sat + usd;
@@ -1466,7 +1496,7 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
         Mf[NET_RUNOFF][e] = net_runoff;
         const double inwater = net_runoff * area;
         Mf[OL_INWATER][e] = inwater;
-        Mf[OL_QLAT][e] = inwater / L[FLOW_LENGTH][slot];
+        Mf[OL_QLAT][e] = inwater * L[INV_FLOW_LENGTH][slot];
     }
 }
 
@@ -1475,41 +1505,41 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
 __global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph g) {
     const int M = F.M;
     const int64_t E = F.land_slots * M;
-    const double dt = F.dt;
+    const double inv_dt = F.inv_dt;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
         double* const* Mf = F.Mf;
         double* const* L = F.L;
-        const double sfw = L[SFW][slot], fl = L[FLOW_LENGTH][slot];
-        const double u = Mf[OL_U][e];
-        const double a = L[OL_ALPHA][slot] * (u * u * u);
-        double h = Mf[OL_H][e];
-        if (sfw > 0.0) h = a / sfw;
-        Mf[OL_H][e] = h;
-        Mf[OL_STORAGE][e] = fl * sfw * h;
+        const double inv_sfw = L[INV_SFW][slot];
+        if (inv_sfw > 0.0) {
+            const double u = Mf[OL_U][e];
+            const double h = L[OL_ALPHA][slot] * (u * u * u) * inv_sfw;
+            Mf[OL_H][e] = h;
+            Mf[OL_STORAGE][e] = L[FLOW_LENGTH][slot] * L[SFW][slot] * h;
+        }
         double qin = 0.0, tr = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             const double qs = Mf[OL_QSUM][g.up_slot[o] * M + m];
             qin += qs * g.up_w[o];
             tr += qs * g.up_fr[o];
         }
-        if (!(sfw > 0.0)) qin = 0.0;
-        Mf[OL_Q_AVG][e] = Mf[OL_QSUM][e] / dt;
-        const double tr_avg = tr / dt;
+        if (!(inv_sfw > 0.0)) qin = 0.0;
+        Mf[OL_Q_AVG][e] = Mf[OL_QSUM][e] * inv_dt;
+        const double tr_avg = tr * inv_dt;
         Mf[OL_TR_AVG][e] = tr_avg;
-        Mf[OL_QIN_AVG][e] = qin / dt;
+        Mf[OL_QIN_AVG][e] = qin * inv_dt;
         const int64_t rs = F.land_river_slot[slot];
         if (rs >= 0) {
             const int64_t re = rs * M + m;
-            const double len = F.R[R_LENGTH][rs];
+            const double inv_len = F.R[R_INV_LENGTH][rs];
             const double inw = Mf[SSF_TR_AVG][e] + tr_avg + Mf[NET_RUNOFF_RIVER][e] * F.R[R_AREA][rs];
             F.RM[RV_INWATER][re] = inw;
-            const double qlat = inw / len;
+            const double qlat = inw * inv_len;
             F.RM[RV_QLAT][re] = qlat;
             const double ext = F.R[R_EXT_INFLOW][rs];
-            F.RM[RV_QLATT][re] = ext < 0.0 ? qlat : qlat + ext / len;
+            F.RM[RV_QLATT][re] = ext < 0.0 ? qlat : qlat + ext * inv_len;
         }
     }
 }
@@ -1518,7 +1548,7 @@ __global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph 
 __global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph g) {
     const int M = F.M;
     const int64_t E = F.river_slots * M;
-    const double dt = F.dt;
+    const double inv_dt = F.inv_dt;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.river_node_of_slot[slot] < 0) continue;
@@ -1527,13 +1557,80 @@ __global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph 
         double* const* R = F.R;
         const double u = RM[RV_U][e];
         const double a = R[R_ALPHA][slot] * (u * u * u);
-        RM[RV_H][e] = a / R[R_WIDTH][slot];
+        RM[RV_H][e] = a * R[R_INV_WIDTH][slot];
         RM[RV_STORAGE][e] = R[R_LENGTH][slot] * a;
         double qin = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) qin += RM[RV_QSUM][g.up_slot[o] * M + m];
-        RM[RV_Q_AVG][e] = RM[RV_QSUM][e] / dt;
-        RM[RV_QIN_AVG][e] = qin / dt;
-        RM[RV_ABS_AVG][e] = RM[RV_ABSSUM][e] / dt;
+        RM[RV_Q_AVG][e] = RM[RV_QSUM][e] * inv_dt;
+        RM[RV_QIN_AVG][e] = qin * inv_dt;
+        RM[RV_ABS_AVG][e] = RM[RV_ABSSUM][e] * inv_dt;
+    }
+}
+
+// Water balance of the split form (mass_balance.jl:215-253 land, :382-399 overland,
+// :470-490 subsurface, :290-313 river) and update_total_water_storage! (sbm.jl:143-182):
+// the error terms are FP64 differences of the FP64 totals, the relative errors are FP32
+// quotients, and every division by dt or area is a multiplication by a static reciprocal.
+__device__ __forceinline__ void mb_error_s(double tin, double tout, double rate, double& err, double& rel) {
+    err = tin - tout - rate;
+    const float avg = (float)((tin + tout) * 0.5);
+    rel = avg == 0.0f ? 0.0 : (double)((float)err / avg);
+}
+
+__global__ void __launch_bounds__(256) balance_split_kernel(WfDevFields F) {
+    const int M = F.M;
+    const int64_t EL = F.land_slots * M, ER = F.river_slots * M;
+    const double inv_dt = F.inv_dt;
+    double* const* Mf = F.Mf;
+    double* const* L = F.L;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < EL + ER; e += (int64_t)gridDim.x * blockDim.x) {
+        if (e >= EL) {
+            if (!F.mass_balance) continue;
+            const int64_t re = e - EL;
+            const int64_t rs = re / M;
+            if (F.river_node_of_slot[rs] < 0) continue;
+            double* const* RM = F.RM;
+            const double tin = RM[RV_INWATER][re] + RM[RV_QIN_AVG][re] + fmax(0.0, F.R[R_EXT_INFLOW][rs]);
+            const double tout = RM[RV_Q_AVG][re] + RM[RV_ABS_AVG][re];
+            double err, rel;
+            mb_error_s(tin, tout, (RM[RV_STORAGE][re] - RM[BR_PREV][re]) * inv_dt, err, rel);
+            RM[BR_ERR][re] = err;
+            RM[BR_REL][re] = rel;
+            continue;
+        }
+        const int64_t slot = e / M;
+        if (F.land_node_of_slot[slot] < 0) continue;
+        const int m = (int)(e - slot * M);
+        const int64_t rs = F.land_river_slot[slot];
+        const double inv_area = L[INV_AREA][slot];
+        double ts = 0.0;
+        if (rs >= 0) ts = F.RM[RV_H][rs * M + m] * F.R[R_WIDTH][rs] * F.R[R_LENGTH][rs] * inv_area;
+        const double snow = Mf[SNOW][e], sw = Mf[SNOW_WATER][e], canopy = Mf[CANOPY][e];
+        const double tsws = Mf[TSWS][e];
+        ts += snow + sw + canopy + tsws + Mf[OL_H][e] * (1.0 - L[RIVER_FRACTION][slot]);
+        Mf[TOTAL_STORAGE][e] = ts;
+        if (!F.mass_balance) continue;
+        double err, rel;
+        {
+            const double tin = Mf[SSF_QIN_AVG][e] * inv_area + (double)F.Mh[PRECIP][e];
+            const double vout = Mf[NET_RUNOFF][e] + Mf[AET][e] + Mf[NET_RUNOFF_RIVER][e] + Mf[LEAKAGE][e];
+            const double tout = Mf[SSF_Q_AVG][e] * inv_area + vout;
+            const double storage = tsws + canopy + (snow + sw);
+            mb_error_s(tin, tout, (storage - Mf[BL_PREV][e]) * inv_dt, err, rel);
+            Mf[BL_ERR][e] = err;
+            Mf[BL_REL][e] = rel;
+        }
+        mb_error_s(Mf[OL_INWATER][e] + Mf[OL_QIN_AVG][e], Mf[OL_Q_AVG][e], (Mf[OL_STORAGE][e] - Mf[BO_PREV][e]) * inv_dt,
+                   err, rel);
+        Mf[BO_ERR][e] = err;
+        Mf[BO_REL][e] = rel;
+        {
+            const double flux = Mf[RCH_FLUX_AVG][e];
+            const double fin = fmax(flux, 0.0), fout = fmax(-flux, 0.0);
+            mb_error_s(Mf[SSF_QIN_AVG][e] + fin, Mf[SSF_Q_AVG][e] + fout, Mf[SSF_QNET_AVG][e], err, rel);
+            Mf[BS_ERR][e] = err;
+            Mf[BS_REL][e] = rel;
+        }
     }
 }
 
@@ -1605,7 +1702,11 @@ cudaError_t wf_split_river(const WfDevFields& F, const WfDevGraph& g, const WfSw
     return launch_walk_split(RiverSplitPhys{F, g, sw}, c);
 }
 
-cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c) { return wf_fp64_balance(F, c); }
+cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c) {
+    const int block = 256;
+    balance_split_kernel<<<grid_for((F.land_slots + F.river_slots) * F.M, block, c.num_sms), block, 0, c.stream>>>(F);
+    return cudaGetLastError();
+}
 
 cudaError_t wf_split_ssf_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
     if (F.N <= 4) return launch_wave(SsfWave<4>{F, g, sw}, c);

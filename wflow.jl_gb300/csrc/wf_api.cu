@@ -631,9 +631,11 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         // per-cell constants of the slim wavefronts (split form): 1/dx and the subsurface terms
         // of a single sub-step dt_s
         const double dts = h->h_dts_ssf[0];
-        std::vector<double> inv_dx(n), dtdx(n), idwdx(n), dtsy(n), k2(n), inv_te(n);
+        std::vector<double> inv_dx(n), dtdx(n), idwdx(n), dtsy(n), k2(n), inv_te(n), inv_area(n), inv_sfw(n);
         for (int64_t i = 0; i < n; ++i) {
             const double dx = d->flow_length[i], dw = d->flow_width[i];
+            inv_area[i] = 1.0 / d->area[i];
+            inv_sfw[i] = d->surface_flow_width[i] > 0.0 ? 1.0 / d->surface_flow_width[i] : 0.0;
             inv_te[i] = 1.0 / (p->theta_s[i] - p->theta_r[i]);
             inv_dx[i] = 1.0 / dx;
             dtdx[i] = dts / dx;
@@ -647,6 +649,8 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         ls.push_back({SSF_DTSY, dtsy});
         ls.push_back({SSF_K2, k2});
         ls.push_back({INV_TE, inv_te});
+        ls.push_back({INV_AREA, inv_area});
+        ls.push_back({INV_SFW, inv_sfw});
     }
     for (auto& x : ls) CKR(upload_slots(h, &F.L[x.idx], x.v, PL, M, n, false));
     for (int k = 0; k < N; ++k) {
@@ -701,11 +705,12 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         CKR(upload_slots(h, &F.Mf[f], *src, PL, M, n, true));
     }
     // ---- river fields
-    std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr), r_inv_len(nr);
+    std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr), r_inv_len(nr), r_inv_w(nr);
     for (int64_t r = 0; r < nr; ++r) {
         r_width[r] = d->river_width[r];
         r_length[r] = d->river_length[r];
         r_inv_len[r] = 1.0 / d->river_length[r];
+        r_inv_w[r] = 1.0 / d->river_width[r];
         r_ext[r] = d->river_external_inflow ? d->river_external_inflow[r] : 0.0;
         r_area[r] = d->area[d->river_land_index[r]];
         const double wp = d->river_width[r] + d->river_bankfull_depth[r];
@@ -718,6 +723,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     CKR(upload_slots(h, &F.R[R_EXT_INFLOW], r_ext, PR, M, nr, false));
     CKR(upload_slots(h, &F.R[R_AREA], r_area, PR, M, nr, false));
     CKR(upload_slots(h, &F.R[R_INV_LENGTH], r_inv_len, PR, M, nr, false));
+    CKR(upload_slots(h, &F.R[R_INV_WIDTH], r_inv_w, PR, M, nr, false));
     std::vector<double> zeros_r((size_t)std::max<int64_t>(nr, 1) * M, 0.0);
     for (int f = 0; f < RM_COUNT; ++f) {
         if (!F.split && wf_split_only_river_member(f)) continue;

@@ -17,7 +17,7 @@
     X(WHC) X(THETA_S) X(THETA_R) X(THETA_FC) X(SWC) X(SOIL_THICKNESS) X(PSI_B) X(H1) X(H2) X(H3_HIGH) \
     X(H3_LOW) X(H4) X(ALPHA_H1) X(CAP_COMP) X(COMPACT_FRAC) X(ROOTDISTPAR) X(CAP_HMAX) X(CAP_N)       \
     X(MAX_LEAKAGE) X(W_SOIL) X(CF_SOIL) X(ROOTING_DEPTH) X(Z_EXP) X(KH_RATIO) X(INV_FLOW_LENGTH)  \
-    X(SSF_DTDX) X(SSF_IDWDX) X(SSF_DTSY) X(SSF_K2) X(INV_TE)
+    X(SSF_DTDX) X(SSF_IDWDX) X(SSF_DTSY) X(SSF_K2) X(INV_TE) X(INV_AREA) X(INV_SFW)
 
 #define WF_M_FIELDS(X)                                                                             \
     X(KV0) X(FSCALE) X(Q_MAX) X(PRECIP) X(POTEVAP) X(TEMP) X(CANOPY) X(SNOW) X(SNOW_WATER) X(TSOIL) X(SAT) X(TSWS)    \
@@ -32,7 +32,7 @@
     X(SSF_QNET) X(SSF_T2) X(SSF_RDF) X(SSF_RTH) X(SSF_RCAP) X(SSF_RRHO) X(SSF_TQIN) X(SSF_TEXF)     \
     X(SSF_TNF) X(SSF_FLAG) X(OL_U) X(OL_QSUM)
 
-#define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA) X(R_INV_LENGTH)
+#define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA) X(R_INV_LENGTH) X(R_INV_WIDTH)
 
 #define WF_RM_FIELDS(X)                                                                            \
     X(RV_Q) X(RV_H) X(RV_STORAGE) X(RV_Q_AVG) X(RV_QIN_AVG) X(RV_INWATER) X(RV_QLAT) X(RV_ABS_AVG)    \
