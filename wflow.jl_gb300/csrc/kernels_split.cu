@@ -21,6 +21,7 @@
 #include "wf_kernels.h"
 #include "wf_math.cuh"
 #include "wf_walker.cuh"
+#include "wf_ff.cuh"
 #include "wf_wave.cuh"
 
 using wfm::jclamp;
@@ -78,47 +79,6 @@ __device__ __forceinline__ float rwu_feddes_f(float h, float h1, float h2, float
         return 0.0f;
     }
     return 1.0f;
-}
-
-// kinematic wave for surface flow with an FP64 Newton solve
-__device__ void kinematic_wave_split(double q_in, double q_prev, double q_lat, double alpha, double dt, double dx,
-                                     double& q, double& area) {
-    if (q_in + q_prev + q_lat == 0.0) {
-        q = 0.0;
-        area = 0.0;
-        return;
-    }
-    const double dt_dx = dt / dx;
-    double u_prev = 0.0;
-    if (q_prev > 0.0) {
-        const float u0 = powj((float)q_prev, 0.2f);
-        double u = (double)u0;
-        if (u0 > 0.0f) {  // one FP64 Newton step on u^5 = q_prev
-            const double u2 = u * u;
-            const double inv = (double)(1.0f / (5.0f * u0 * u0 * u0 * u0));
-            u = u - (u2 * u2 * u - q_prev) * inv;
-        }
-        u_prev = u;
-    }
-    const double cterm = dt_dx * q_in + alpha * u_prev * u_prev * u_prev + dt * q_lat;
-    double u = u_prev > 0.0 ? u_prev : (double)cbrtf((float)(cterm / alpha));
-    const double c1 = 5.0 * dt_dx, c2 = 3.0 * alpha;
-    for (int it = 0; it < 3000; ++it) {
-        const double u2 = u * u;
-        const double u3 = u2 * u;
-        const double fu = u3 * (dt_dx * u2 + alpha) - cterm;
-        if (wfm::fabs_(fu) <= 1.0e-12) break;
-        const double df = u2 * (c1 * u2 + c2);
-        const float rdf = 1.0f / (float)df;
-        const double u_old = u;
-        u -= (rdf == rdf && rdf != 0.0f && wfm::fabs_((double)rdf) < 3.0e38) ? fu * (double)rdf : fu / df;
-        if (wfm::isnan_(u) || u <= 0.0) u = KIN_WAVE_MIN_FLOW_QROOT;
-        if (u == u_old) break;
-    }
-    u = jmax(u, KIN_WAVE_MIN_FLOW_QROOT);
-    const double u3 = u * u * u;
-    area = alpha * u3;
-    q = u3 * u * u;
 }
 
 // ----------------------------------------------------------------- soil column ----------
@@ -301,13 +261,11 @@ template <int MAXN>
 struct ColG {
     int N, nl, nu;
     float act[MAXN], cum[MAXN + 1], thick[MAXN];
-    double thick_last;  // FP64 thickness of the deepest unsaturated layer (0 when none)
     __device__ __forceinline__ void set(const WfDevFields& F, int64_t slot, double zi) {
         N = F.N;
         nl = F.nlayers[slot];
         nu = N;
         cum[0] = 0.0f;
-        thick_last = 0.0;
         double c0 = 0.0;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k) {
@@ -318,13 +276,9 @@ struct ColG {
                 const double c1 = F.LY[LY_CUM][k][slot];
                 if (zi > c1) {
                     t = act[k];
-                    thick_last = F.LY[LY_ACT_THICK][k][slot];
                 } else {
                     const double r = zi - c0;
-                    if (r > 0.0) {
-                        t = (float)r;
-                        thick_last = r;
-                    }
+                    if (r > 0.0) t = (float)r;
                 }
                 c0 = c1;
             } else {
@@ -722,35 +676,34 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             Mf[BO_PREV][e] = Mf[OL_STORAGE][e];
             if (rs >= 0) F.RM[BR_PREV][rs * M + m] = F.RM[RV_STORAGE][rs * M + m];
         }
-        // terms of the subsurface solve that do not depend on the upstream discharge
+        // terms of the subsurface solve that do not depend on the upstream discharge: the FP64
+        // recharge flux for the exact bookkeeping, FP32 inputs of the walker
         if (F.ssf_single) {
             double flux = recharge * F.L[AREA][slot];  // recharge flux of the subsurface model
             if (zi >= d_soil) flux = fmax(0.0, flux);
             Mf[SSF_QNET][e] = flux;
+            Mh[SSF_QNETF][e] = (float)flux;
+            Mh[SSF_ZIF][e] = zif;
             float z = zif;
             if (kv_const && !(z < zexp)) z = zexp;
             const float cel = Lf[KH_RATIO][slot] * kv0 * expf(-fsc * z) * Lf[SLOPE][slot] / Lf[SY][slot];
             const float cinv = 1.0f / cel;
-            Mf[SSF_T2][e] = Mf[SSF_Q][e] * (double)cinv;
-            Mf[SSF_RDF][e] = (double)(1.0f / (Lf[SSF_DTDX][slot] + cinv));
-            // deepest unsaturated layer: what a rising water table fills first. The rise it
-            // allows, dt * rate / (theta_e - usld / thickness), moves water between the layer and
-            // the saturated store, so it is FP64 (with the layer's FP64 thickness and content).
-            double rth = 0.0, rcap = 0.0, rrho = 0.0;
-            if (g.nu > 0) {
-                const double dts = F.dt_ssf;
-                const double te_d = F.L[THETA_S][slot] - F.L[THETA_R][slot];
-                double uk = 0.0;
+            Mh[SSF_T2][e] = (float)Mf[SSF_Q][e] * cinv;
+            Mh[SSF_RDF][e] = 1.0f / (Lf[SSF_DTDX][slot] + cinv);
+            // deepest unsaturated layer: what a rising water table fills first
+            float rth = 0.0f, rcap = 0.0f, rrho = 0.0f;
+            const float dts = (float)F.dt_ssf;
 #pragma unroll
-                for (int k = 0; k < MAXN; ++k)
-                    if (k + 1 == g.nu) uk = us[k].changed() ? us[k].value() : us[k].base;
-                rth = g.thick_last;
-                rcap = fmax(rth * te_d - uk, 0.0) * F.inv_dt_ssf;
-                rrho = dts * rth * wfm_rcp(te_d * rth - uk);
+            for (int k = 0; k < MAXN; ++k) {
+                if (k + 1 != g.nu) continue;
+                rth = g.thick[k];
+                const float uk = us[k].val();
+                rcap = fmaxf(rth * te - uk, 0.0f) / dts;
+                rrho = dts / (te - uk / rth);
             }
-            Mf[SSF_RTH][e] = rth;
-            Mf[SSF_RCAP][e] = rcap;
-            Mf[SSF_RRHO][e] = rrho;
+            Mh[SSF_RTH][e] = rth;
+            Mh[SSF_RCAP][e] = rcap;
+            Mh[SSF_RRHO][e] = rrho;
         }
     }
 }
@@ -926,126 +879,11 @@ struct SsfSplitPhys {
         Mf[NET_RUNOFF][e] = net_runoff;
         const double inwater = net_runoff * area;
         Mf[OL_INWATER][e] = inwater;
-        Mf[OL_QLAT][e] = inwater / L[FLOW_LENGTH][slot];
-        return true;
-    }
-};
-
-// --------------------------------------------------------------- overland wavefront -----
-
-struct OverlandSplitPhys {
-    WfDevFields F;
-    WfDevGraph g;
-    WfSweep sw;
-
-    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
-        double* const* Mf = F.Mf;
-        double* const* L = F.L;
-        const double dt_s = sw.dts[s];
-        const bool first = (sw.first + s == 0);
-        const bool last = sw.last_of_step && (s == sw.S - 1);
-        if (first && F.mass_balance) Mf[BO_PREV][e] = Mf[OL_STORAGE][e];
-        const double sfw = L[SFW][slot];
-        double tr = 0.0, qin = 0.0;
-        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
-            double qu;
-            if (!wfw::upstream_q(g, sw, Mf[OL_Q], o, m, s, ep, F.status, qu)) return false;
-            const double fr = L[FRAC_TO_RIVER][g.up_slot[o]];
-            tr += qu * fr;
-            qin += qu * (1.0 - fr);
-        }
-        if (!(sfw > 0.0)) qin = 0.0;
-        const double fl = L[FLOW_LENGTH][slot];
-        double q, a;
-        kinematic_wave_split(qin, Mf[OL_Q][e], Mf[OL_QLAT][e], L[OL_ALPHA][slot], dt_s, fl, q, a);
-        double h = Mf[OL_H][e];
-        if (sfw > 0.0) h = a / sfw;
-        Mf[OL_Q][e] = q;
-        Mf[OL_H][e] = h;
-        Mf[OL_STORAGE][e] = fl * sfw * h;
-        if (is_end) wfw::publish(g, chain, m, s, ep, q);
-        double c_tr = tr * dt_s, c_q = q * dt_s, c_qin = qin * dt_s;
-        if (!first) {
-            c_tr += Mf[OL_TR_CUM][e];
-            c_q += Mf[OL_Q_CUM][e];
-            c_qin += Mf[OL_QIN_CUM][e];
-        }
-        if (!last) {
-            Mf[OL_TR_CUM][e] = c_tr;
-            Mf[OL_Q_CUM][e] = c_q;
-            Mf[OL_QIN_CUM][e] = c_qin;
-            return true;
-        }
-        const double dt = sw.dt;
-        Mf[OL_Q_AVG][e] = c_q / dt;
-        Mf[OL_TR_AVG][e] = c_tr / dt;
-        Mf[OL_QIN_AVG][e] = c_qin / dt;
-        return true;
-    }
-};
-
-// ------------------------------------------------------------------ river wavefront ------
-
-struct RiverSplitPhys {
-    WfDevFields F;
-    WfDevGraph g;
-    WfSweep sw;
-
-    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
-        double* const* RM = F.RM;
-        double* const* R = F.R;
-        const int M = F.M;
-        const double dt_s = sw.dts[s];
-        const bool first = (sw.first + s == 0);
-        const bool last = sw.last_of_step && (s == sw.S - 1);
-        const double len = R[R_LENGTH][slot];
-        double qlat;
-        if (first) {
-            if (F.mass_balance) RM[BR_PREV][e] = RM[RV_STORAGE][e];
-            const int64_t le = F.river_land_slot[slot] * M + m;
-            const double inw = F.Mf[SSF_TR_AVG][le] + F.Mf[OL_TR_AVG][le] + F.Mf[NET_RUNOFF_RIVER][le] * R[R_AREA][slot];
-            RM[RV_INWATER][e] = inw;
-            qlat = inw / len;
-            RM[RV_QLAT][e] = qlat;
-        } else {
-            qlat = RM[RV_QLAT][e];
-        }
-        double qin = 0.0;
-        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
-            double qu;
-            if (!wfw::upstream_q(g, sw, RM[RV_Q], o, m, s, ep, F.status, qu)) return false;
-            qin += qu;
-        }
-        const double ext = R[R_EXT_INFLOW][slot];
-        double inflow, absd = 0.0;
-        if (ext < 0.0) {
-            absd = jmin(-ext, (RM[RV_STORAGE][e] / dt_s) * 0.80);
-            inflow = -absd / len;
-        } else {
-            inflow = ext / len;
-        }
-        double q, a;
-        kinematic_wave_split(qin, RM[RV_Q][e], qlat + inflow, R[R_ALPHA][slot], dt_s, len, q, a);
-        RM[RV_Q][e] = q;
-        RM[RV_H][e] = a / R[R_WIDTH][slot];
-        RM[RV_STORAGE][e] = len * a;
-        if (is_end) wfw::publish(g, chain, m, s, ep, q);
-        double c_q = q * dt_s, c_qin = qin * dt_s, c_ab = absd * dt_s;
-        if (!first) {
-            c_q += RM[RV_Q_CUM][e];
-            c_qin += RM[RV_QIN_CUM][e];
-            c_ab += RM[RV_ABS_CUM][e];
-        }
-        if (!last) {
-            RM[RV_Q_CUM][e] = c_q;
-            RM[RV_QIN_CUM][e] = c_qin;
-            RM[RV_ABS_CUM][e] = c_ab;
-            return true;
-        }
-        const double dt = sw.dt;
-        RM[RV_Q_AVG][e] = c_q / dt;
-        RM[RV_ABS_AVG][e] = c_ab / dt;
-        RM[RV_QIN_AVG][e] = c_qin / dt;
+        const double qlat = inwater / L[FLOW_LENGTH][slot];
+        Mf[OL_QLAT][e] = qlat;
+        const wff::ff qlf = wff::from_d(qlat);
+        F.Mh[OL_QLATH][e] = qlf.hi;
+        F.Mh[OL_QLATL][e] = qlf.lo;
         return true;
     }
 };
@@ -1056,51 +894,48 @@ struct RiverSplitPhys {
 // per-cell kernels before (vertical epilogue) and after (post kernels) each sweep do the rest.
 
 // Root of dt_dx u^5 + alpha u^3 = cterm for the kinematic wave in u = Q^0.2 (the reference's
-// Newton-Raphson on Q, surface_process.jl:24-70, written for u): Newton iterations in FP32
-// from the upper bound min((cterm/alpha)^(1/3), (cterm/dt_dx)^(1/5)) (or the previous u when it
-// lies below that bound) until |du| <= 1e-6 u, then one FP64 Newton correction of the FP32
-// root, which leaves |f(u)| at the FP64 rounding level of cterm. Results below the reference's
-// floor (Q = 1e-30, u = QROOT) are raised to it, as the reference does.
-__device__ __forceinline__ void kw_solve_u(double qin, double q_prev, double qlat, double dt_s, double alpha,
-                                           double dt_dx, double u_prev, double& u_out, double& q_out) {
-    if (qin + q_prev + qlat == 0.0) {
-        u_out = 0.0;
-        q_out = 0.0;
+// Newton-Raphson on Q, surface_process.jl:24-70, written for u), in double-FP32: Newton
+// iterations in FP32 from the upper bound min((cterm/alpha)^(1/3), (cterm/dt_dx)^(1/5)) (or
+// from the previous u when it lies below that bound) until |du| <= 3e-7 u, then one Newton
+// correction with the residual evaluated in double-FP32, which leaves |f(u)| at about 1e-13 of
+// cterm. Q = u^5 is formed from the correction du as v^5 - 5 v^4 du (the dropped terms are of
+// relative size (du/v)^2). Results below the reference's floor (Q = 1e-30, u = QROOT) are
+// raised to it, as the reference does.
+__device__ __forceinline__ void kw_solve_ff(wff::ff cterm, wff::ff dt_dx, float alpha, float u_prev, wff::ff& u_out,
+                                            wff::ff& q_out) {
+    const float QR = (float)KIN_WAVE_MIN_FLOW_QROOT;
+    const float floor_c = alpha * (QR * QR * QR);
+    if (!(cterm.hi > floor_c)) {
+        u_out = {QR, 0.0f};
+        q_out = {(float)KIN_WAVE_MIN_FLOW, 0.0f};
         return;
     }
-    const double cterm = dt_dx * qin + (alpha * (u_prev * u_prev * u_prev) + dt_s * qlat);
-    const double QR = KIN_WAVE_MIN_FLOW_QROOT;
-    const double floor_c = alpha * (QR * QR * QR) + dt_dx * KIN_WAVE_MIN_FLOW;
-    double u;
-    if (!(cterm > floor_c)) {
-        u = QR;
-    } else {
-        const float a = (float)dt_dx, b = (float)alpha, c = (float)cterm;
-        const float ub = fminf(cbrtf(c / b), powf(c / a, 0.2f));
-        const float up = (float)u_prev;
-        float v = (up > 0.0f && up < ub) ? up : ub;
-        const float a5 = 5.0f * a, b3 = 3.0f * b;
-        float dg = 1.0f;
+    const float a = dt_dx.hi, b = alpha, c = cterm.hi;
+    const float ub = 1.00001f * fminf(__powf(__fdividef(c, b), 1.0f / 3.0f), __powf(__fdividef(c, a), 0.2f));
+    float v = (u_prev > 0.0f && u_prev < ub) ? u_prev : ub;
+    const float a5 = 5.0f * a, b3 = 3.0f * b;
 #pragma unroll 1
-        for (int it = 0; it < 12; ++it) {
-            const float v2 = v * v;
-            const float g = v2 * v * fmaf(a, v2, b) - c;
-            dg = v2 * fmaf(a5, v2, b3);
-            const float dv = __fdividef(g, dg);
-            v = fminf(v - dv, ub);
-            if (!(fabsf(dv) > 1e-6f * v)) break;
-        }
+    for (int it = 0; it < 12; ++it) {
         const float v2 = v * v;
-        dg = v2 * fmaf(a5, v2, b3);
-        u = (double)v;
-        const double u2 = u * u;
-        const double f = u2 * u * fma(dt_dx, u2, alpha) - cterm;
-        u = fma(-f, (double)(1.0f / dg), u);
-        if (!(u > QR)) u = QR;
+        const float g = v2 * v * fmaf(a, v2, b) - c;
+        const float dg = v2 * fmaf(a5, v2, b3);
+        const float dv = __fdividef(g, dg);
+        v = fminf(v - dv, ub);
+        if (!(fabsf(dv) > 3e-7f * v)) break;
     }
-    const double u2 = u * u;
+    const wff::ff v2 = wff::two_prod(v, v);
+    const wff::ff v3 = wff::mul(v2, v);
+    const wff::ff v5 = wff::mul(v3, v2);
+    const wff::ff f = wff::add(wff::add(wff::mul(dt_dx, v5), wff::mul(v3, b)), wff::neg(cterm));
+    const float dv = __fdividef(f.hi, v2.hi * fmaf(a5, v2.hi, b3));
+    wff::ff u = wff::two_sum(v, -dv);
+    wff::ff q = wff::add(v5, wff::mul(wff::mul(v2, v2), -5.0f * dv));
+    if (!(u.hi > QR)) {
+        u = {QR, 0.0f};
+        q = {(float)KIN_WAVE_MIN_FLOW, 0.0f};
+    }
     u_out = u;
-    q_out = u2 * u2 * u;
+    q_out = q;
 }
 
 // q^0.2 for a discharge set from outside the step (BMI set_value, restart).
@@ -1188,189 +1023,236 @@ __device__ __noinline__ void ssf_full_split(const WfDevFields& F, int64_t slot, 
 }
 
 // Lateral subsurface flow, one sub-step per model step (subsurface_process.jl:100-196 per
-// node). The solve of the linear kinematic wave is q = cterm / (dt/dx + 1/c); the water-table
-// change is decided from the deepest unsaturated layer prepared by the vertical kernel, and
-// anything else (several layers filled, a water table moving by more than 0.1, non-finite
-// values) goes through ssf_full_split.
+// node), FP32 on the critical path. The linear kinematic wave gives q = cterm / (dt/dx + 1/c);
+// what q depends on beyond that -- the cut of q when the water table would fall below the soil
+// (zi > d) and the reference's sub-iterations when the water table moves by more than 0.1 --
+// is decided in FP32 with margins, and every case too close to call in FP32 (or a water table
+// rising through more than one layer, or non-finite values) goes through the exact FP64
+// computation of ssf_full_split. The FP64 bookkeeping of the fast cases (net flux, water-table
+// change, exfiltration) is redone exactly by ssf_post_kernel from the same q.
+enum SsfFlag { SSF_FAST = 0, SSF_EARLY = 1, SSF_FULL = 2, SSF_CUT = 3 };
+
 template <int MAXN>
 struct SsfWave {
     WfDevFields F;
     WfDevGraph g;
     WfSweep sw;
     struct In {
-        double q_prev, q_net, t2, rdf, zi, d, dtdx, idwdx, dtsy, k2, qmaxdw, rth, rcap, rrho;
+        float qnet, t2, rdf, zi, rth, rcap, rrho, qmaxdw, d, dtdx, idwdx, dtsy, k2;
+        bool qprev_zero;
         wfv::UpList up;
     };
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
-        double* const* Mf = F.Mf;
-        double* const* L = F.L;
-        x.q_prev = Mf[SSF_Q][e];
-        x.q_net = Mf[SSF_QNET][e];
-        x.t2 = Mf[SSF_T2][e];
-        x.rdf = Mf[SSF_RDF][e];
-        x.zi = Mf[SSF_ZI][e];
-        x.rth = Mf[SSF_RTH][e];
-        x.rcap = Mf[SSF_RCAP][e];
-        x.rrho = Mf[SSF_RRHO][e];
-        x.d = L[SOIL_THICKNESS][slot];
-        x.dtdx = L[SSF_DTDX][slot];
-        x.idwdx = L[SSF_IDWDX][slot];
-        x.dtsy = L[SSF_DTSY][slot];
-        x.k2 = L[SSF_K2][slot];
-        x.qmaxdw = (double)F.Mh[Q_MAX][e] * L[FLOW_WIDTH][slot];
-        wfv::load_up(g, slot, m, x.up);
+        float* const* Mh = F.Mh;
+        float* const* Lf = F.Lf;
+        x.qnet = Mh[SSF_QNETF][e];
+        x.t2 = Mh[SSF_T2][e];
+        x.rdf = Mh[SSF_RDF][e];
+        x.zi = Mh[SSF_ZIF][e];
+        x.rth = Mh[SSF_RTH][e];
+        x.rcap = Mh[SSF_RCAP][e];
+        x.rrho = Mh[SSF_RRHO][e];
+        x.qmaxdw = Mh[Q_MAX][e] * Lf[FLOW_WIDTH][slot];
+        x.d = Lf[SOIL_THICKNESS][slot];
+        x.dtdx = Lf[SSF_DTDX][slot];
+        x.idwdx = Lf[SSF_IDWDX][slot];
+        x.dtsy = Lf[SSF_DTSY][slot];
+        x.k2 = Lf[SSF_K2][slot];
+        x.qprev_zero = (__double_as_longlong(F.Mf[SSF_Q][e]) << 1) == 0;
+        wfv::load_up(g, sw, slot, m, x.up);
     }
     __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
-                                         double* qh) {
-        double qin;
-        if (!wfv::gather<true>(g, sw, x.up, m, 0, qh[0], F.status, qin)) return false;
-        double q, zi_new, exf, nf;
-        double flag;
-        if (qin + x.q_prev == 0.0 && x.q_net <= 0.0) {
-            q = 0.0;
-            zi_new = x.d;
-            exf = 0.0;
-            nf = 0.0;
-            flag = 1.0;
+                                         unsigned long long* qh) {
+        wff::ff qinff;
+        if (!wfv::gather<true>(g, sw, x.up, m, 0, qh[0], F.status, qinff)) return false;
+        const float qin = qinff.hi + qinff.lo;
+        float q = 0.0f, qu = 0.0f;
+        int flag;
+        if (qinff.hi == 0.0f && x.qprev_zero && x.qnet <= 0.0f) {
+            flag = SSF_EARLY;
         } else {
-            const double cterm = x.dtdx * (qin + x.q_net) + x.t2;
+            const float cterm = x.dtdx * (qin + x.qnet) + x.t2;
             q = cterm * x.rdf;
-            if (q != q) q = 0.0;
-            q = jmax(q, KIN_WAVE_MIN_FLOW);
-            q = jmin(q, x.qmaxdw);
-            nf = (qin + x.q_net - q) * x.idwdx;
+            if (q != q) q = 0.0f;
+            q = fminf(fmaxf(q, 1e-30f), x.qmaxdw);
+            qu = q;
+            const float nf = (qin + x.qnet - q) * x.idwdx;
             bool full = false;
-            double dh = 0.0;
-            exf = 0.0;
-            if (nf <= 0.0) {
+            float dh = 0.0f;
+            if (nf <= 0.0f) {
                 dh = nf * x.dtsy;
-            } else if (!(nf > 0.0) || (x.rth != 0.0 && x.rcap <= nf)) {
+            } else if (!(nf > 0.0f) || (x.rth != 0.0f && x.rcap <= nf * 1.0001f)) {
                 full = true;
-            } else if (x.rth == 0.0) {
-                exf = nf;
-            } else {
+            } else if (x.rth != 0.0f) {
                 dh = nf * x.rrho;
             }
-            double zi = x.zi - dh;
+            flag = SSF_FAST;
             if (!full) {
-                if (zi > x.d) q = jmax(q - x.k2 * (zi - x.d), KIN_WAVE_MIN_FLOW);
-                zi = jclamp(zi, 0.0, x.d);
-                if (!(wfm::fabs_(zi - x.zi) * 10.0 <= 1.0)) full = true;
+                float zi = x.zi - dh;
+                if (fabsf(zi - x.d) <= 1e-5f * x.d) {
+                    full = true;
+                } else if (zi > x.d) {
+                    q = fmaxf(q - x.k2 * (zi - x.d), 1e-30f);
+                    zi = x.d;
+                    flag = SSF_CUT;
+                }
+                zi = fminf(fmaxf(zi, 0.0f), x.d);
+                if (!(fabsf(zi - x.zi) * 10.0f <= 0.999f)) full = true;
             }
             if (full) {
-                ssf_full_split<MAXN>(F, slot, e, qin, x.q_net, sw.dts[0], q, zi, exf, nf);
-                flag = 2.0;
-            } else {
-                flag = 0.0;
+                double qd, zid, exfd, nfd;
+                const double qind = (double)qin;
+                ssf_full_split<MAXN>(F, slot, e, qind, F.Mf[SSF_QNET][e], sw.dts[0], qd, zid, exfd, nfd);
+                double* const* Mf = F.Mf;
+                Mf[SSF_Q][e] = qd;
+                Mf[SSF_ZI][e] = zid;
+                Mf[SSF_TEXF][e] = exfd;
+                Mf[SSF_TNF][e] = nfd;
+                Mf[SSF_TQIN][e] = qind;
+                q = (float)qd;
+                flag = SSF_FULL;
             }
-            zi_new = zi;
         }
-        double* const* Mf = F.Mf;
-        qh[0] = q;
-        if (is_end) wfv::publish(g, chain, m, 0, q);
-        Mf[SSF_Q][e] = q;
-        Mf[SSF_ZI][e] = zi_new;
-        Mf[SSF_TEXF][e] = exf;
-        Mf[SSF_TNF][e] = nf;
-        Mf[SSF_TQIN][e] = qin;
-        Mf[SSF_FLAG][e] = flag;
+        float* const* Mh = F.Mh;
+        const wff::ff qf = {q, 0.0f};
+        qh[0] = wff::pack(qf);
+        if (is_end) wfv::publish(g, chain, m, 0, qf);
+        Mh[SSF_QF][e] = q;
+        Mh[SSF_QUF][e] = qu;
+        Mh[SSF_QINF][e] = qin;
+        Mh[SSF_FLAG][e] = (float)flag;
         return true;
     }
 };
 
-// Overland flow (surface_process.jl:24-70 per node, routing/surface_kinwave.jl sub-steps).
+// Overland flow (surface_process.jl:24-70 per node, routing/surface_kinwave.jl sub-steps) in
+// double-FP32: discharge, u = Q^0.2 and the lateral inflow are pairs of FP32 arrays.
 struct OlWave {
     WfDevFields F;
     WfDevGraph g;
     WfSweep sw;
     struct In {
-        double u, q, qlat, alpha, inv_dx;
+        wff::ff u, q, qlat, invdx;
+        float alpha;
         bool sfw_pos;
         wfv::UpList up;
     };
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
-        x.u = F.Mf[OL_U][e];
-        x.q = F.Mf[OL_Q][e];
-        x.qlat = F.Mf[OL_QLAT][e];
-        x.alpha = F.L[OL_ALPHA][slot];
-        x.inv_dx = F.L[INV_FLOW_LENGTH][slot];
-        x.sfw_pos = F.L[SFW][slot] > 0.0;
-        wfv::load_up(g, slot, m, x.up);
+        float* const* Mh = F.Mh;
+        x.u = {Mh[OL_UH][e], Mh[OL_UL][e]};
+        x.q = {Mh[OL_QH][e], Mh[OL_QL][e]};
+        x.qlat = {Mh[OL_QLATH][e], Mh[OL_QLATL][e]};
+        x.invdx = {F.Lf[INV_FLOW_LENGTH][slot], F.Lf[INV_DX_LO][slot]};
+        x.alpha = F.Lf[OL_ALPHA][slot];
+        x.sfw_pos = F.Lf[SFW][slot] > 0.0f;
+        wfv::load_up(g, sw, slot, m, x.up);
     }
     __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
-                                         double* qh) {
+                                         unsigned long long* qh) {
         const int stride = blockDim.x;
-        double u = x.u, qp = x.q, qsum = 0.0;
+        wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f};
         for (int s = 0; s < sw.S; ++s) {
-            const double dt_s = sw.dts[s];
-            double qin;
+            const float dt_s = sw.dts_f[s];
+            wff::ff qin;
             if (!wfv::gather<true>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
-            if (!x.sfw_pos) qin = 0.0;
-            double un, qn;
-            kw_solve_u(qin, qp, x.qlat, dt_s, x.alpha, dt_s * x.inv_dx, u, un, qn);
+            if (!x.sfw_pos) qin = {0.0f, 0.0f};
+            wff::ff un, qn;
+            if (qin.hi == 0.0f && qp.hi == 0.0f && x.qlat.hi == 0.0f) {
+                un = {0.0f, 0.0f};
+                qn = {0.0f, 0.0f};
+            } else {
+                const wff::ff dt_dx = wff::mul(x.invdx, dt_s);
+                const wff::ff u3 = wff::mul(wff::mul(u, u), u);
+                const wff::ff cterm =
+                    wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, x.alpha), wff::mul(x.qlat, dt_s)));
+                kw_solve_ff(cterm, dt_dx, x.alpha, u.hi, un, qn);
+            }
             u = un;
             qp = qn;
-            qh[s * stride] = qn;
+            qh[s * stride] = wff::pack(qn);
             if (is_end) wfv::publish(g, chain, m, s, qn);
-            qsum = fma(qn, dt_s, qsum);
+            qsum = wff::add(qsum, wff::mul(qn, dt_s));
         }
-        double* const* Mf = F.Mf;
-        Mf[OL_U][e] = u;
-        Mf[OL_Q][e] = qp;
-        Mf[OL_QSUM][e] = sw.first == 0 ? qsum : Mf[OL_QSUM][e] + qsum;
+        float* const* Mh = F.Mh;
+        Mh[OL_UH][e] = u.hi;
+        Mh[OL_UL][e] = u.lo;
+        Mh[OL_QH][e] = qp.hi;
+        Mh[OL_QL][e] = qp.lo;
+        if (sw.first != 0) qsum = wff::add(qsum, wff::ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]});
+        Mh[OL_QSUMH][e] = qsum.hi;
+        Mh[OL_QSUML][e] = qsum.lo;
         return true;
     }
 };
 
-// River flow (surface_process.jl:24-70 per node, routing/river_kinwave.jl sub-steps), with the
-// abstraction of a negative external inflow limited to 80 % of the storage.
+// River flow (surface_process.jl:24-70 per node, routing/river_kinwave.jl sub-steps) in
+// double-FP32, with the abstraction of a negative external inflow limited to 80 % of the
+// storage.
 struct RvWave {
     WfDevFields F;
     WfDevGraph g;
     WfSweep sw;
     struct In {
-        double u, q, qlat, qlatt, alpha, inv_len, len, ext;
+        wff::ff u, q, qlatt, invlen;
+        float alpha, len, ext;
         wfv::UpList up;
     };
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
-        x.u = F.RM[RV_U][e];
-        x.q = F.RM[RV_Q][e];
-        x.qlat = F.RM[RV_QLAT][e];
-        x.qlatt = F.RM[RV_QLATT][e];
-        x.alpha = F.R[R_ALPHA][slot];
-        x.inv_len = F.R[R_INV_LENGTH][slot];
-        x.len = F.R[R_LENGTH][slot];
-        x.ext = F.R[R_EXT_INFLOW][slot];
-        wfv::load_up(g, slot, m, x.up);
+        float* const* RMh = F.RMh;
+        x.u = {RMh[RV_UH][e], RMh[RV_UL][e]};
+        x.q = {RMh[RV_QH][e], RMh[RV_QL][e]};
+        x.qlatt = {RMh[RV_QLATTH][e], RMh[RV_QLATTL][e]};
+        x.invlen = {F.Rf[R_INV_LENGTH][slot], F.Rf[R_INV_LEN_LO][slot]};
+        x.alpha = F.Rf[R_ALPHA][slot];
+        x.len = F.Rf[R_LENGTH][slot];
+        x.ext = F.Rf[R_EXT_INFLOW][slot];
+        wfv::load_up(g, sw, slot, m, x.up);
     }
     __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
-                                         double* qh) {
+                                         unsigned long long* qh) {
         const int stride = blockDim.x;
-        double u = x.u, qp = x.q, qsum = 0.0, asum = 0.0;
+        wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f}, asum = {0.0f, 0.0f};
         for (int s = 0; s < sw.S; ++s) {
-            const double dt_s = sw.dts[s];
-            double qin;
+            const float dt_s = sw.dts_f[s];
+            wff::ff qin;
             if (!wfv::gather<false>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
-            double ql = x.qlatt, absd = 0.0;
-            if (x.ext < 0.0) {
-                const double storage = x.len * (x.alpha * (u * u * u));
-                absd = jmin(-x.ext, (storage / dt_s) * 0.80);
-                ql = x.qlat + (-absd / x.len);
+            wff::ff ql = x.qlatt;
+            if (x.ext < 0.0f) {  // abstraction: qlatt holds the lateral inflow alone
+                const float storage = x.len * (x.alpha * (u.hi * u.hi * u.hi));
+                const float absd = fminf(-x.ext, (storage / dt_s) * 0.80f);
+                ql = wff::add(ql, wff::mul(x.invlen, -absd));
+                asum = wff::add(asum, wff::two_prod(absd, dt_s));
             }
-            double un, qn;
-            kw_solve_u(qin, qp, ql, dt_s, x.alpha, dt_s * x.inv_len, u, un, qn);
+            wff::ff un, qn;
+            if (qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
+                un = {0.0f, 0.0f};
+                qn = {0.0f, 0.0f};
+            } else {
+                const wff::ff dt_dx = wff::mul(x.invlen, dt_s);
+                const wff::ff u3 = wff::mul(wff::mul(u, u), u);
+                const wff::ff cterm =
+                    wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, x.alpha), wff::mul(ql, dt_s)));
+                kw_solve_ff(cterm, dt_dx, x.alpha, u.hi, un, qn);
+            }
             u = un;
             qp = qn;
-            qh[s * stride] = qn;
+            qh[s * stride] = wff::pack(qn);
             if (is_end) wfv::publish(g, chain, m, s, qn);
-            qsum = fma(qn, dt_s, qsum);
-            asum = fma(absd, dt_s, asum);
+            qsum = wff::add(qsum, wff::mul(qn, dt_s));
         }
-        double* const* RM = F.RM;
-        RM[RV_U][e] = u;
-        RM[RV_Q][e] = qp;
-        RM[RV_QSUM][e] = sw.first == 0 ? qsum : RM[RV_QSUM][e] + qsum;
-        RM[RV_ABSSUM][e] = sw.first == 0 ? asum : RM[RV_ABSSUM][e] + asum;
+        float* const* RMh = F.RMh;
+        RMh[RV_UH][e] = u.hi;
+        RMh[RV_UL][e] = u.lo;
+        RMh[RV_QH][e] = qp.hi;
+        RMh[RV_QL][e] = qp.lo;
+        if (sw.first != 0) {
+            qsum = wff::add(qsum, wff::ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]});
+            asum = wff::add(asum, wff::ff{RMh[RV_ABSH][e], RMh[RV_ABSL][e]});
+        }
+        RMh[RV_QSUMH][e] = qsum.hi;
+        RMh[RV_QSUML][e] = qsum.lo;
+        RMh[RV_ABSH][e] = asum.hi;
+        RMh[RV_ABSL][e] = asum.lo;
         return true;
     }
 };
@@ -1400,10 +1282,10 @@ cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
 
 // --------------------------------------------------------------- post-sweep kernels ------
 
-// After the subsurface sweep: unsaturated-layer adjustment to the new water table
-// (soil.jl update_ustorelayerdepth!), averages of the sweep, subsurface storage, the soil
+// After the subsurface sweep: the exact FP64 bookkeeping of the fast cases (net flux and
+// water-table change from the walker's q, exfiltration), the unsaturated-layer adjustment to
+// the new water table (soil.jl update_ustorelayerdepth!), averages, subsurface storage, the soil
 // water storage update (sbm.jl update_soil_water_storage!) and the overland lateral inflow.
-// FP64 for the stores; divisions replaced by static reciprocals.
 template <int MAXN>
 __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph g) {
     const int M = F.M;
@@ -1415,10 +1297,12 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
         double* const* Mf = F.Mf;
+        float* const* Mh = F.Mh;
         double* const* L = F.L;
-        const int flag = (int)Mf[SSF_FLAG][e];
+        const int flag = (int)Mh[SSF_FLAG][e];
         const double zi_soil = Mf[ZI][e];
-        const double zi_new = Mf[SSF_ZI][e];
+        const double d = L[SOIL_THICKNESS][slot];
+        const double te = L[THETA_S][slot] - L[THETA_R][slot];
         double usld[MAXN], act[MAXN], cum[MAXN + 1];  // cum[k]: depth of the top of layer k
         cum[0] = 0.0;
 #pragma unroll
@@ -1438,8 +1322,48 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
         auto thick_at = [&](double ref, int k) {
             return ref > cum[k + 1] ? act[k] : (ref > cum[k] ? ref - cum[k] : __longlong_as_double(0x7ff8000000000000LL));
         };
-        double zi_s = zi_new;
-        if (flag == 0) {
+        double q, qin, exf, nf, zi_new, zi_s;
+        if (flag == SSF_EARLY) {
+            q = qin = exf = nf = 0.0;
+            zi_new = d;
+            zi_s = zi_soil;
+            Mf[SSF_Q][e] = 0.0;
+            Mf[SSF_ZI][e] = d;
+        } else if (flag == SSF_FULL) {
+            q = Mf[SSF_Q][e];
+            qin = Mf[SSF_TQIN][e];
+            exf = Mf[SSF_TEXF][e];
+            nf = Mf[SSF_TNF][e];
+            zi_new = zi_s = Mf[SSF_ZI][e];
+#pragma unroll
+            for (int k = 0; k < MAXN; ++k) usld[k] = k < N ? F.LY[LY_USLD][k][e] : 0.0;
+        } else {
+            q = (double)Mh[SSF_QF][e];
+            qin = (double)Mh[SSF_QINF][e];
+            const double qu = (double)Mh[SSF_QUF][e];
+            nf = (qin + Mf[SSF_QNET][e] - qu) * L[SSF_IDWDX][slot];
+            // water_table_change (subsurface_process.jl): falling by net flux / specific yield,
+            // rising through the unsaturated layers from the deepest up
+            double dh = 0.0, rem = nf;
+            if (nf <= 0.0) {
+                dh = nf * L[SSF_DTSY][slot];
+            } else {
+                const double dts = F.dt_ssf;
+                const int nu0 = nu_at(zi_soil);
+#pragma unroll
+                for (int k = MAXN; k >= 1; --k) {
+                    if (k > nu0 || rem == 0.0) continue;
+                    const double t = thick_at(zi_soil, k - 1);
+                    const double cap = fmax(t * te - usld[k - 1], 0.0) * F.inv_dt_ssf;
+                    const double fl = fmin(rem, cap);
+                    dh += cap <= rem ? t : fl * dts * wfm_rcp(te - usld[k - 1] * wfm_rcp(t));
+                    rem -= fl;
+                }
+            }
+            exf = fmax(rem, 0.0);
+            double zi = zi_soil - dh;
+            if (flag == SSF_CUT || zi > d) zi = d;
+            zi_new = zi_s = fmin(fmax(zi, 0.0), d);
             if (zi_new != zi_soil) {
                 const int n_prev = nu_at(zi_soil), n_new = nu_at(zi_new);
                 if (zi_new < zi_soil) {
@@ -1463,15 +1387,14 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
                 }
                 Mf[ZI][e] = zi_new;
             }
-        } else if (flag == 1) {
-            zi_s = zi_soil;
+            Mf[SSF_Q][e] = q;
+            Mf[SSF_ZI][e] = zi_new;
         }
         const int nu = nu_at(zi_s);
         double tr = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o)
-            tr += Mf[SSF_Q][g.up_slot[o] * M + m] * g.up_fr[o];
-        const double area = L[AREA][slot], d = L[SOIL_THICKNESS][slot];
-        const double q = Mf[SSF_Q][e], qin = Mf[SSF_TQIN][e], exf = Mf[SSF_TEXF][e], nf = Mf[SSF_TNF][e];
+            tr += (double)Mh[SSF_QF][g.up_slot[o] * M + m] * g.up_fr[o];
+        const double area = L[AREA][slot];
         const double flux = Mf[SSF_QNET][e];
         Mf[SSF_STORAGE][e] = L[SY][slot] * (d - zi_new) * area;
         const double exf_avg = exf * r_s;
@@ -1486,7 +1409,7 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
         for (int k = 0; k < MAXN; ++k)
             if (k < nu) usd += usld[k];
         const double runoff = fmax(0.0, exf_avg + Mf[SATEX][e] + Mf[RUNOFF_LAND][e] + Mf[INFEX][e]);
-        const double sat = (d - zi_s) * (L[THETA_S][slot] - L[THETA_R][slot]);
+        const double sat = (d - zi_s) * te;
         Mf[SAT][e] = sat;
         Mf[USTOREDEPTH][e] = usd;
         Mf[TSWS][e] = sat + usd;
@@ -1496,12 +1419,17 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
         Mf[NET_RUNOFF][e] = net_runoff;
         const double inwater = net_runoff * area;
         Mf[OL_INWATER][e] = inwater;
-        Mf[OL_QLAT][e] = inwater * L[INV_FLOW_LENGTH][slot];
+        const double qlat = inwater * L[INV_FLOW_LENGTH][slot];
+        Mf[OL_QLAT][e] = qlat;
+        const wff::ff qlf = wff::from_d(qlat);
+        Mh[OL_QLATH][e] = qlf.hi;
+        Mh[OL_QLATL][e] = qlf.lo;
     }
 }
 
-// After the overland sweep: water depth and storage, averages, and the lateral inflow of the
-// river cell of each land cell (routing/river_kinwave.jl update_lateral_inflow!).
+// After the overland sweep: discharge, water depth and storage in FP64 from the double-FP32
+// state, averages, and the lateral inflow of the river cell of each land cell
+// (routing/river_kinwave.jl update_lateral_inflow!).
 __global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph g) {
     const int M = F.M;
     const int64_t E = F.land_slots * M;
@@ -1511,22 +1439,25 @@ __global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph 
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
         double* const* Mf = F.Mf;
+        float* const* Mh = F.Mh;
         double* const* L = F.L;
+        Mf[OL_Q][e] = wff::to_d({Mh[OL_QH][e], Mh[OL_QL][e]});
         const double inv_sfw = L[INV_SFW][slot];
         if (inv_sfw > 0.0) {
-            const double u = Mf[OL_U][e];
-            const double h = L[OL_ALPHA][slot] * (u * u * u) * inv_sfw;
-            Mf[OL_H][e] = h;
-            Mf[OL_STORAGE][e] = L[FLOW_LENGTH][slot] * L[SFW][slot] * h;
+            const double u = wff::to_d({Mh[OL_UH][e], Mh[OL_UL][e]});
+            const double a = (double)F.Lf[OL_ALPHA][slot] * (u * u * u);
+            Mf[OL_H][e] = a * inv_sfw;
+            Mf[OL_STORAGE][e] = L[FLOW_LENGTH][slot] * a;
         }
         double qin = 0.0, tr = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
-            const double qs = Mf[OL_QSUM][g.up_slot[o] * M + m];
-            qin += qs * g.up_w[o];
+            const int64_t ue = g.up_slot[o] * M + m;
+            const double qs = wff::to_d({Mh[OL_QSUMH][ue], Mh[OL_QSUML][ue]});
+            qin += qs * (double)g.up_wf[o];
             tr += qs * g.up_fr[o];
         }
         if (!(inv_sfw > 0.0)) qin = 0.0;
-        Mf[OL_Q_AVG][e] = Mf[OL_QSUM][e] * inv_dt;
+        Mf[OL_Q_AVG][e] = wff::to_d({Mh[OL_QSUMH][e], Mh[OL_QSUML][e]}) * inv_dt;
         const double tr_avg = tr * inv_dt;
         Mf[OL_TR_AVG][e] = tr_avg;
         Mf[OL_QIN_AVG][e] = qin * inv_dt;
@@ -1539,12 +1470,14 @@ __global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph 
             const double qlat = inw * inv_len;
             F.RM[RV_QLAT][re] = qlat;
             const double ext = F.R[R_EXT_INFLOW][rs];
-            F.RM[RV_QLATT][re] = ext < 0.0 ? qlat : qlat + ext * inv_len;
+            const wff::ff qlt = wff::from_d(ext < 0.0 ? qlat : qlat + ext * inv_len);
+            F.RMh[RV_QLATTH][re] = qlt.hi;
+            F.RMh[RV_QLATTL][re] = qlt.lo;
         }
     }
 }
 
-// After the river sweep: water depth, storage and averages.
+// After the river sweep: discharge, water depth, storage and averages in FP64.
 __global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph g) {
     const int M = F.M;
     const int64_t E = F.river_slots * M;
@@ -1554,16 +1487,21 @@ __global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph 
         if (F.river_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
         double* const* RM = F.RM;
+        float* const* RMh = F.RMh;
         double* const* R = F.R;
-        const double u = RM[RV_U][e];
-        const double a = R[R_ALPHA][slot] * (u * u * u);
+        RM[RV_Q][e] = wff::to_d({RMh[RV_QH][e], RMh[RV_QL][e]});
+        const double u = wff::to_d({RMh[RV_UH][e], RMh[RV_UL][e]});
+        const double a = (double)F.Rf[R_ALPHA][slot] * (u * u * u);
         RM[RV_H][e] = a * R[R_INV_WIDTH][slot];
         RM[RV_STORAGE][e] = R[R_LENGTH][slot] * a;
         double qin = 0.0;
-        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) qin += RM[RV_QSUM][g.up_slot[o] * M + m];
-        RM[RV_Q_AVG][e] = RM[RV_QSUM][e] * inv_dt;
+        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
+            const int64_t ue = g.up_slot[o] * M + m;
+            qin += wff::to_d({RMh[RV_QSUMH][ue], RMh[RV_QSUML][ue]});
+        }
+        RM[RV_Q_AVG][e] = wff::to_d({RMh[RV_QSUMH][e], RMh[RV_QSUML][e]}) * inv_dt;
         RM[RV_QIN_AVG][e] = qin * inv_dt;
-        RM[RV_ABS_AVG][e] = RM[RV_ABSSUM][e] * inv_dt;
+        RM[RV_ABS_AVG][e] = wff::to_d({RMh[RV_ABSH][e], RMh[RV_ABSL][e]}) * inv_dt;
     }
 }
 
@@ -1634,16 +1572,27 @@ __global__ void __launch_bounds__(256) balance_split_kernel(WfDevFields F) {
     }
 }
 
-// u = Q^0.2 of the overland and river discharges (after a discharge was set from outside).
+// Double-FP32 discharge and u = Q^0.2 of the overland and river state from the FP64 fields
+// (after a discharge was set from outside, and at creation).
 __global__ void __launch_bounds__(256) sync_u_kernel(WfDevFields F) {
     const int M = F.M;
     const int64_t EL = F.land_slots * M, ER = F.river_slots * M;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < EL + ER; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < EL) {
-            F.Mf[OL_U][i] = u_of_q(F.Mf[OL_Q][i]);
+            const double q = F.Mf[OL_Q][i];
+            const wff::ff qf = wff::from_d(q), uf = wff::from_d(u_of_q(q));
+            F.Mh[OL_QH][i] = qf.hi;
+            F.Mh[OL_QL][i] = qf.lo;
+            F.Mh[OL_UH][i] = uf.hi;
+            F.Mh[OL_UL][i] = uf.lo;
         } else {
             const int64_t e = i - EL;
-            F.RM[RV_U][e] = u_of_q(F.RM[RV_Q][e]);
+            const double q = F.RM[RV_Q][e];
+            const wff::ff qf = wff::from_d(q), uf = wff::from_d(u_of_q(q));
+            F.RMh[RV_QH][e] = qf.hi;
+            F.RMh[RV_QL][e] = qf.lo;
+            F.RMh[RV_UH][e] = uf.hi;
+            F.RMh[RV_UL][e] = uf.lo;
         }
     }
 }
@@ -1694,13 +1643,7 @@ cudaError_t wf_split_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSwee
     return launch_walk_split(SsfSplitPhys<WF_MAX_LAYERS>{F, g, sw}, c);
 }
 
-cudaError_t wf_split_overland(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
-    return launch_walk_split(OverlandSplitPhys{F, g, sw}, c);
-}
 
-cudaError_t wf_split_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
-    return launch_walk_split(RiverSplitPhys{F, g, sw}, c);
-}
 
 cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c) {
     const int block = 256;

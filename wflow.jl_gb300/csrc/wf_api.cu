@@ -34,6 +34,7 @@ struct DevGraphAlloc {
     int32_t *chunk_len = nullptr, *chain_len = nullptr, *up_ptr = nullptr, *up_chain = nullptr;
     uint8_t* is_chain_end = nullptr;
     double *up_w = nullptr, *up_fr = nullptr;
+    float *up_wf = nullptr, *up_frf = nullptr;
     uint32_t* flags = nullptr;
     double* end_q = nullptr;
     unsigned long long* ticket = nullptr;
@@ -179,6 +180,8 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.is_chain_end = G.is_chain_end;
     g.up_w = G.up_w;
     g.up_fr = G.up_fr;
+    g.up_wf = G.up_wf;
+    g.up_frf = G.up_frf;
     g.flags = G.flags;
     g.end_q = G.end_q;
     g.ticket = G.ticket;
@@ -631,13 +634,14 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         // per-cell constants of the slim wavefronts (split form): 1/dx and the subsurface terms
         // of a single sub-step dt_s
         const double dts = h->h_dts_ssf[0];
-        std::vector<double> inv_dx(n), dtdx(n), idwdx(n), dtsy(n), k2(n), inv_te(n), inv_area(n), inv_sfw(n);
+        std::vector<double> inv_dx(n), dtdx(n), idwdx(n), dtsy(n), k2(n), inv_te(n), inv_area(n), inv_sfw(n), inv_dx_lo(n);
         for (int64_t i = 0; i < n; ++i) {
             const double dx = d->flow_length[i], dw = d->flow_width[i];
             inv_area[i] = 1.0 / d->area[i];
             inv_sfw[i] = d->surface_flow_width[i] > 0.0 ? 1.0 / d->surface_flow_width[i] : 0.0;
             inv_te[i] = 1.0 / (p->theta_s[i] - p->theta_r[i]);
             inv_dx[i] = 1.0 / dx;
+            inv_dx_lo[i] = inv_dx[i] - (double)(float)inv_dx[i];
             dtdx[i] = dts / dx;
             idwdx[i] = 1.0 / (dw * dx);
             dtsy[i] = dts / sy[i];
@@ -651,6 +655,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         ls.push_back({INV_TE, inv_te});
         ls.push_back({INV_AREA, inv_area});
         ls.push_back({INV_SFW, inv_sfw});
+        ls.push_back({INV_DX_LO, inv_dx_lo});
     }
     for (auto& x : ls) CKR(upload_slots(h, &F.L[x.idx], x.v, PL, M, n, false));
     for (int k = 0; k < N; ++k) {
@@ -688,6 +693,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     std::vector<double> zeros_m((size_t)n * M, 0.0);
     for (int f = 0; f < M_COUNT; ++f) {
         if (!F.split && wf_split_only_member(f)) continue;
+        if (wf_split_f32_only(f)) continue;  // FP32 arrays only (below)
         const std::vector<double>* src = &zeros_m;
         switch (f) {
             case KV0: src = &kv0; break;
@@ -705,12 +711,13 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         CKR(upload_slots(h, &F.Mf[f], *src, PL, M, n, true));
     }
     // ---- river fields
-    std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr), r_inv_len(nr), r_inv_w(nr);
+    std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr), r_inv_len(nr), r_inv_w(nr), r_inv_len_lo(nr);
     for (int64_t r = 0; r < nr; ++r) {
         r_width[r] = d->river_width[r];
         r_length[r] = d->river_length[r];
         r_inv_len[r] = 1.0 / d->river_length[r];
         r_inv_w[r] = 1.0 / d->river_width[r];
+        r_inv_len_lo[r] = r_inv_len[r] - (double)(float)r_inv_len[r];
         r_ext[r] = d->river_external_inflow ? d->river_external_inflow[r] : 0.0;
         r_area[r] = d->area[d->river_land_index[r]];
         const double wp = d->river_width[r] + d->river_bankfull_depth[r];
@@ -724,9 +731,13 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     CKR(upload_slots(h, &F.R[R_AREA], r_area, PR, M, nr, false));
     CKR(upload_slots(h, &F.R[R_INV_LENGTH], r_inv_len, PR, M, nr, false));
     CKR(upload_slots(h, &F.R[R_INV_WIDTH], r_inv_w, PR, M, nr, false));
+    CKR(upload_slots(h, &F.R[R_INV_LEN_LO], r_inv_len_lo, PR, M, nr, false));
     std::vector<double> zeros_r((size_t)std::max<int64_t>(nr, 1) * M, 0.0);
     for (int f = 0; f < RM_COUNT; ++f) {
-        if (!F.split && wf_split_only_river_member(f)) continue;
+        if (wf_split_only_river_member(f)) {
+            if (F.split) CKR(upload_slots_f32(h, &F.RMh[f], zeros_r, PR, M, nr, true));
+            continue;
+        }
         CKR(upload_slots(h, &F.RM[f], zeros_r, PR, M, nr, true));
     }
     // ---- upstream weights of the wavefront gathers: land discharge splits into the part that
@@ -745,6 +756,9 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         }
         CKR(upload(h, &G.up_w, w));
         CKR(upload(h, &G.up_fr, fr));
+        std::vector<float> wf(w.begin(), w.end()), frf(fr.begin(), fr.end());
+        CKR(upload(h, &G.up_wf, wf));
+        CKR(upload(h, &G.up_frf, frf));
     }
     // ---- split form: FP32 copies of the static fields and FP32 member fields
     if (F.split) {
@@ -770,7 +784,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
             CKR(upload_slots_f32(h, &F.LYf[LY_CUM][k], vcum, PL, M, n, false));
         }
         for (int f = 0; f < M_COUNT; ++f) {
-            if (!wf_split_f32_member(f)) continue;
+            if (!wf_split_f32_member(f) && !wf_split_f32_only(f)) continue;
             const std::vector<double>* src = &zeros_m;
             if (f == KV0) src = &kv0;
             if (f == FSCALE) src = &fsc;
@@ -783,6 +797,8 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         CKR(upload_slots_f32(h, &F.Rf[R_ALPHA], r_alpha, PR, M, nr, false));
         CKR(upload_slots_f32(h, &F.Rf[R_EXT_INFLOW], r_ext, PR, M, nr, false));
         CKR(upload_slots_f32(h, &F.Rf[R_AREA], r_area, PR, M, nr, false));
+        CKR(upload_slots_f32(h, &F.Rf[R_INV_LENGTH], r_inv_len, PR, M, nr, false));
+        CKR(upload_slots_f32(h, &F.Rf[R_INV_LEN_LO], r_inv_len_lo, PR, M, nr, false));
     }
     // ---- maps
     {
@@ -822,6 +838,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     F.status = h->status;
     CKR(dalloc(h, &h->staging, (size_t)std::max<int64_t>(std::max(n, nr), 1) * M * 3));
     h->tuning.use_graph = 1;
+    h->u_dirty = F.split != 0;  // double-FP32 routing state from the FP64 discharges on the first step
     h->metrics.n_chains_land = (int32_t)PL.n_chains;
     h->metrics.n_chains_river = (int32_t)PR.n_chains;
     h->metrics.max_chain_land = PL.max_len;
@@ -1157,8 +1174,8 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
             CK(cudaMemsetAsync(G.ticket, 0, sizeof(unsigned long long), h->stream));
             cudaError_t e;
             if (which == 0) e = split ? wf_split_ssf(h->F, g, sw, lc) : wf_fp64_ssf(h->F, g, sw, lc);
-            else if (which == 1) e = split ? wf_split_overland(h->F, g, sw, lc) : wf_fp64_overland(h->F, g, sw, lc);
-            else e = split ? wf_split_river(h->F, g, sw, lc) : wf_fp64_river(h->F, g, sw, lc);
+            else if (which == 1) e = wf_fp64_overland(h->F, g, sw, lc);
+            else e = wf_fp64_river(h->F, g, sw, lc);
             CK(e);
             ++nl;
         }
@@ -1179,6 +1196,7 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
             sw.epoch0 = 1;
             sw.dt = h->cfg.dt;
             sw.dts = d_dts + first;
+            for (int j = 0; j < sw.S && j < 16; ++j) sw.dts_f[j] = (float)dts[first + j];
             sw.wait_ns = h->wait_ns;
             sw.wait_offset = h->wait_offset;
             CK(cudaMemsetAsync(G.end_q, 0xFF, (size_t)G.plan.n_chains * h->M * G.s_cap * sizeof(double), h->stream));
@@ -1371,6 +1389,7 @@ int enqueue_step_static(WfHandle* h, unsigned char* base, int64_t* launches) {
             sw.epoch0 = 1;
             sw.dt = h->cfg.dt;
             sw.dts = d_dts + first;
+            for (int j = 0; j < sw.S && j < 16; ++j) sw.dts_f[j] = (float)dts[first + j];
             sw.wait_ns = h->wait_ns;
             sw.wait_offset = h->wait_offset;
             int rc = clear(G, g, wave);

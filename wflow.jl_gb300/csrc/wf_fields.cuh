@@ -17,7 +17,7 @@
     X(WHC) X(THETA_S) X(THETA_R) X(THETA_FC) X(SWC) X(SOIL_THICKNESS) X(PSI_B) X(H1) X(H2) X(H3_HIGH) \
     X(H3_LOW) X(H4) X(ALPHA_H1) X(CAP_COMP) X(COMPACT_FRAC) X(ROOTDISTPAR) X(CAP_HMAX) X(CAP_N)       \
     X(MAX_LEAKAGE) X(W_SOIL) X(CF_SOIL) X(ROOTING_DEPTH) X(Z_EXP) X(KH_RATIO) X(INV_FLOW_LENGTH)  \
-    X(SSF_DTDX) X(SSF_IDWDX) X(SSF_DTSY) X(SSF_K2) X(INV_TE) X(INV_AREA) X(INV_SFW)
+    X(SSF_DTDX) X(SSF_IDWDX) X(SSF_DTSY) X(SSF_K2) X(INV_TE) X(INV_AREA) X(INV_SFW) X(INV_DX_LO)
 
 #define WF_M_FIELDS(X)                                                                             \
     X(KV0) X(FSCALE) X(Q_MAX) X(PRECIP) X(POTEVAP) X(TEMP) X(CANOPY) X(SNOW) X(SNOW_WATER) X(TSOIL) X(SAT) X(TSWS)    \
@@ -29,15 +29,18 @@
     X(INTERCEPTION) X(TRANSPIRATION) X(SOIL_EVAP) X(ACT_INFILT) X(SWE) X(NET_RUNOFF) X(RUNOFF)        \
     X(EXFILT) X(BL_PREV) X(BO_PREV) X(TOTAL_STORAGE) X(BL_ERR) X(BL_REL) X(BO_ERR) X(BO_REL)          \
     X(BS_ERR) X(BS_REL)                                                                            \
-    X(SSF_QNET) X(SSF_T2) X(SSF_RDF) X(SSF_RTH) X(SSF_RCAP) X(SSF_RRHO) X(SSF_TQIN) X(SSF_TEXF)     \
-    X(SSF_TNF) X(SSF_FLAG) X(OL_U) X(OL_QSUM)
+    X(SSF_QNET) X(SSF_TQIN) X(SSF_TEXF) X(SSF_TNF)                                                 \
+    X(SSF_T2) X(SSF_RDF) X(SSF_RTH) X(SSF_RCAP) X(SSF_RRHO) X(SSF_FLAG) X(SSF_QNETF) X(SSF_ZIF)      \
+    X(SSF_QF) X(SSF_QUF) X(SSF_QINF) X(OL_UH) X(OL_UL) X(OL_QH) X(OL_QL) X(OL_QSUMH) X(OL_QSUML)     \
+    X(OL_QLATH) X(OL_QLATL)
 
-#define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA) X(R_INV_LENGTH) X(R_INV_WIDTH)
+#define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA) X(R_INV_LENGTH) X(R_INV_WIDTH) X(R_INV_LEN_LO)
 
 #define WF_RM_FIELDS(X)                                                                            \
     X(RV_Q) X(RV_H) X(RV_STORAGE) X(RV_Q_AVG) X(RV_QIN_AVG) X(RV_INWATER) X(RV_QLAT) X(RV_ABS_AVG)    \
-    X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL) X(RV_U) X(RV_QSUM) X(RV_ABSSUM) \
-    X(RV_QLATT)
+    X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL)                         \
+    X(RV_UH) X(RV_UL) X(RV_QH) X(RV_QL) X(RV_QSUMH) X(RV_QSUML) X(RV_ABSH) X(RV_ABSL) X(RV_QLATTH)   \
+    X(RV_QLATTL)
 
 #define WF_ENUM_ITEM(name) name,
 enum WfLandStatic { WF_L_FIELDS(WF_ENUM_ITEM) L_COUNT };
@@ -57,9 +60,13 @@ __host__ __device__ inline bool wf_split_f32_member(int f) {
            f == INTERCEPTION || f == TRANSPIRATION || f == SOIL_EVAP || f == ACT_INFILT || f == SWE;
 }
 
-// Member fields only the split form's slim wavefront uses (not allocated by the FP64 form).
+// Member fields only the split form's slim wavefronts use (not allocated by the FP64 form).
 __host__ __device__ inline bool wf_split_only_member(int f) { return f >= SSF_QNET; }
-__host__ __device__ inline bool wf_split_only_river_member(int f) { return f >= RV_U; }
+__host__ __device__ inline bool wf_split_only_river_member(int f) { return f >= RV_UH; }
+// Of those, the ones held only in FP32 (Mh / RMh): walker inputs and the double-FP32 routing
+// state (pairs *H + *L).
+__host__ __device__ inline bool wf_split_f32_only(int f) { return f >= SSF_T2; }
+__host__ __device__ inline bool wf_split_f32_only_river(int f) { return f >= RV_UH; }
 
 struct WfDevFields {
     double* L[L_COUNT];
@@ -72,6 +79,7 @@ struct WfDevFields {
     float* LYf[LY_COUNT][WF_MAX_LAYERS];
     float* Mh[M_COUNT];
     float* Rf[R_COUNT];
+    float* RMh[RM_COUNT];
     int32_t split;
     const int8_t* nlayers;                // [land slots]
     const int64_t* land_node_of_slot;     // [land slots], -1 padding
@@ -111,6 +119,8 @@ struct WfDevGraph {
     const uint8_t* is_chain_end;
     const double* up_w;   // [up entries] weight of the upstream discharge (land: 1 - fraction to river)
     const double* up_fr;  // [up entries] fraction of the upstream discharge to the river (land only)
+    const float* up_wf;   // FP32 copies of up_w / up_fr (split form)
+    const float* up_frf;
     uint32_t* flags;      // [n_chains * M] epoch of the last published sub-step
     double* end_q;        // [n_chains * M * s_cap] q of each chain end per sub-step
     unsigned long long* ticket;  // work counter of the current launch
@@ -126,6 +136,7 @@ struct WfSweep {
     uint32_t epoch0;      // epoch of sub-step 0 of this launch
     double dt;            // model step
     const double* dts;    // [S] sub-step sizes (device)
+    float dts_f[16];      // FP32 copy of the first 16 sub-step sizes (split form's slim walkers)
     uint64_t wait_ns;     // spin-wait budget per wait [ns]
     uint32_t wait_offset; // test hook: added to awaited epochs (0 in production)
 };

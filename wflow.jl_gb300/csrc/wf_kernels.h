@@ -27,8 +27,6 @@ cudaError_t wf_fp64_stable_dt(const WfDevFields& F, int which /*0 land 1 river 2
 // FP32/FP64 split form (kernels_split.cu)
 cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c);
 cudaError_t wf_split_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
-cudaError_t wf_split_overland(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
-cudaError_t wf_split_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
 cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c);
 // slim wavefronts of the split form (wf_wave.cuh) and their per-cell completion kernels
 cudaError_t wf_split_ssf_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);

@@ -24,21 +24,22 @@
 
 #include <cstdint>
 
+#include "wf_ff.cuh"
 #include "wf_fields.cuh"
 
 namespace wfv {
 
-constexpr unsigned long long SENTINEL = 0xFFFFFFFFFFFFFFFFULL;   // end_q fill (a NaN no arithmetic yields here)
-constexpr unsigned long long QUIET_NAN = 0x7FF8000000000000ULL;  // published in place of the sentinel pattern
+constexpr unsigned long long SENTINEL = 0xFFFFFFFFFFFFFFFFULL;   // end_q fill (a NaN pair no arithmetic yields here)
+constexpr unsigned long long QUIET_NAN = 0x7FC000007FC00000ULL;  // published in place of the sentinel pattern
 constexpr int MAX_GROUP = 16;                                    // sub-steps per launch of the slim walker
+constexpr int PREFETCH_SUBSTEPS = 4;                             // light-child values prefetched per node
 
-__device__ __forceinline__ unsigned long long ld_relaxed(const double* p) {
+__device__ __forceinline__ unsigned long long ld_relaxed(const void* p) {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_relaxed(double* p, double x) {
-    unsigned long long v = (unsigned long long)__double_as_longlong(x);
+__device__ __forceinline__ void st_relaxed(void* p, unsigned long long v) {
     if (v == SENTINEL) v = QUIET_NAN;
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -52,19 +53,20 @@ __device__ __forceinline__ int32_t status_ld(const int32_t* s) {
 }
 
 // end_q index of chain `chain`, member m, sub-step s of the launch (members innermost, so a
-// warp of 32 members reads 256 contiguous bytes).
+// warp of 32 members reads 256 contiguous bytes). Each slot holds one packed double-FP32
+// discharge (wf_ff.cuh).
 __device__ __forceinline__ int64_t end_index(const WfDevGraph& g, int64_t chain, int m, int s) {
     return (chain * g.s_cap + s) * g.M + m;
 }
 
-// Discharge published at end_q[idx]; `first` is a value already loaded from that slot (or the
-// sentinel). False when the budget ran out or another lane aborted. `hold` (test hook, 0 in
-// production) makes every wait run out.
+// Discharge word published at end_q[idx]; `first` is a value already loaded from that slot (or
+// the sentinel). False when the budget ran out or another lane aborted. A non-zero
+// sw.wait_offset (test hook, 0 in production) makes every wait run out.
 __device__ __forceinline__ bool await_end(const WfDevGraph& g, const WfSweep& sw, int64_t idx,
-                                          unsigned long long first, int32_t* status, double& out) {
+                                          unsigned long long first, int32_t* status, unsigned long long& out) {
     unsigned long long b = first;
     if (b != SENTINEL && sw.wait_offset == 0) {
-        out = __longlong_as_double((long long)b);
+        out = b;
         return true;
     }
     const uint64_t t0 = now_ns();
@@ -72,7 +74,7 @@ __device__ __forceinline__ bool await_end(const WfDevGraph& g, const WfSweep& sw
         __nanosleep(32);
         b = ld_relaxed(&g.end_q[idx]);
         if (b != SENTINEL && sw.wait_offset == 0) {
-            out = __longlong_as_double((long long)b);
+            out = b;
             return true;
         }
         if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return false;
@@ -83,49 +85,63 @@ __device__ __forceinline__ bool await_end(const WfDevGraph& g, const WfSweep& sw
     }
 }
 
-__device__ __forceinline__ void publish(const WfDevGraph& g, int64_t chain, int m, int s, double q) {
-    st_relaxed(&g.end_q[end_index(g, chain, m, s)], q);
+__device__ __forceinline__ void publish(const WfDevGraph& g, int64_t chain, int m, int s, wff::ff q) {
+    st_relaxed(&g.end_q[end_index(g, chain, m, s)], wff::pack(q));
 }
 
-// Upstream list of one node with its first light entry prefetched for sub-step 0.
+// Upstream list of one node with the first light entry's words of the first sub-steps
+// prefetched (loaded together, so they cost one round trip).
 struct UpList {
     int32_t o0, o1;
-    int32_t lo;                // up entry of the prefetched light child (-1: none)
-    unsigned long long lq;     // its end_q content at prefetch time (may be the sentinel)
+    int32_t lo;                                  // up entry of the prefetched light child (-1: none)
+    int64_t lbase;                               // its end_q index at sub-step 0
+    unsigned long long lq[PREFETCH_SUBSTEPS];    // its end_q words at prefetch time (may be sentinels)
 };
 
-__device__ __forceinline__ void load_up(const WfDevGraph& g, int64_t slot, int m, UpList& u) {
+__device__ __forceinline__ void load_up(const WfDevGraph& g, const WfSweep& sw, int64_t slot, int m, UpList& u) {
     u.o0 = g.up_ptr[slot];
     u.o1 = g.up_ptr[slot + 1];
     u.lo = -1;
-    u.lq = SENTINEL;
+    u.lbase = 0;
+#pragma unroll
+    for (int s = 0; s < PREFETCH_SUBSTEPS; ++s) u.lq[s] = SENTINEL;
     for (int32_t o = u.o0; o < u.o1; ++o) {
         const int32_t uc = g.up_chain[o];
         if (uc >= 0) {
             u.lo = o;
-            u.lq = ld_relaxed(&g.end_q[end_index(g, uc, m, 0)]);
+            u.lbase = end_index(g, uc, m, 0);
+#pragma unroll
+            for (int s = 0; s < PREFETCH_SUBSTEPS; ++s)
+                if (s < sw.S) u.lq[s] = ld_relaxed(&g.end_q[u.lbase + (int64_t)s * g.M]);
             break;
         }
     }
 }
 
-// Weighted upstream sums at sub-step s in up-list order: qin = sum w*q (w = 1 - fraction to
-// river on land, 1 on rivers). `qh` is the heavy child's discharge of this sub-step.
+// Weighted upstream sum at sub-step s in up-list order: qin = sum w*q (w = 1 - fraction to
+// river on land, 1 on rivers), in double-FP32. `qh` is the heavy child's word of this sub-step.
 template <bool WEIGHTED>
 __device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, const UpList& u, int m, int s,
-                                       double qh, int32_t* status, double& qin) {
-    double acc = 0.0;
+                                       unsigned long long qh, int32_t* status, wff::ff& qin) {
+    wff::ff acc = {0.0f, 0.0f};
     for (int32_t o = u.o0; o < u.o1; ++o) {
         const int32_t uc = g.up_chain[o];
-        double q;
+        unsigned long long w;
         if (uc < 0) {
-            q = qh;
+            w = qh;
         } else {
             const int64_t idx = end_index(g, uc, m, s);
-            const unsigned long long first = (o == u.lo && s == 0) ? u.lq : ld_relaxed(&g.end_q[idx]);
-            if (!await_end(g, sw, idx, first, status, q)) return false;
+            unsigned long long first = SENTINEL;
+            if (o == u.lo) {
+#pragma unroll
+                for (int j = 0; j < PREFETCH_SUBSTEPS; ++j)
+                    if (j == s) first = u.lq[j];
+            }
+            if (first == SENTINEL) first = ld_relaxed(&g.end_q[idx]);
+            if (!await_end(g, sw, idx, first, status, w)) return false;
         }
-        acc = WEIGHTED ? acc + q * g.up_w[o] : acc + q;
+        const wff::ff q = wff::unpack(w);
+        acc = WEIGHTED ? wff::add(acc, wff::mul(q, g.up_wf[o])) : wff::add(acc, q);
     }
     qin = acc;
     return true;
@@ -134,14 +150,15 @@ __device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, c
 // Phys interface:
 //   struct In;                                               per-node inputs (prefetched)
 //   void load(int64_t slot, int64_t e, int m, In&)           independent of upstream discharge
-//   bool node(const In&, int64_t slot, int64_t e, int m, int64_t chain, bool is_end, double* qh)
-//     advances the node through sw.S sub-steps; qh[s * stride] holds the heavy child's discharge
-//     of sub-step s on entry and this node's discharge on exit. Returns false to abort.
+//   bool node(const In&, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
+//             unsigned long long* qh)
+//     advances the node through sw.S sub-steps; qh[s * stride] holds the heavy child's packed
+//     discharge of sub-step s on entry and this node's on exit. Returns false to abort.
 template <class Phys>
 __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
-    extern __shared__ double wave_smem[];
+    extern __shared__ unsigned long long wave_smem[];
     const unsigned lane = threadIdx.x & 31u;
-    double* qh = wave_smem + threadIdx.x;  // row of this thread: qh[s * blockDim.x]
+    unsigned long long* qh = wave_smem + threadIdx.x;  // row of this thread: qh[s * blockDim.x]
     const int M = g.M, G = g.G;
     const int gpc = M > 32 ? M / 32 : 1;
     const uint64_t n_items = (uint64_t)g.n_chunks * gpc;
