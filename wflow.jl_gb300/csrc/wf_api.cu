@@ -31,7 +31,8 @@ thread_local std::string g_create_error;
 struct DevGraphAlloc {
     WfRoutingPlan plan;
     int64_t *chunk_base = nullptr, *up_slot = nullptr, *node_of_slot = nullptr;
-    int32_t *chunk_len = nullptr, *chain_len = nullptr, *up_ptr = nullptr, *up_chain = nullptr;
+    int32_t *chunk_len = nullptr, *chain_len = nullptr, *up_ptr = nullptr, *up_chain = nullptr, *chunk_g = nullptr;
+    int64_t* chunk_chain0 = nullptr;
     uint8_t* is_chain_end = nullptr;
     double *up_w = nullptr, *up_fr = nullptr;
     float *up_wf = nullptr, *up_frf = nullptr;
@@ -151,6 +152,8 @@ int plan_graph(WfHandle* h, DevGraphAlloc& G, int64_t n, const int32_t* ds, int 
     const WfRoutingPlan& P = G.plan;
     if ((rc = upload(h, &G.chunk_base, P.chunk_base))) return rc;
     if ((rc = upload(h, &G.chunk_len, P.chunk_len))) return rc;
+    if ((rc = upload(h, &G.chunk_g, P.chunk_g))) return rc;
+    if ((rc = upload(h, &G.chunk_chain0, P.chunk_chain0))) return rc;
     if ((rc = upload(h, &G.chain_len, P.chain_len))) return rc;
     if ((rc = upload(h, &G.up_ptr, P.up_ptr))) return rc;
     if ((rc = upload(h, &G.up_slot, P.up_slot))) return rc;
@@ -173,6 +176,8 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.M = M;
     g.chunk_base = G.chunk_base;
     g.chunk_len = G.chunk_len;
+    g.chunk_g = G.chunk_g;
+    g.chunk_chain0 = G.chunk_chain0;
     g.chain_len = G.chain_len;
     g.up_ptr = G.up_ptr;
     g.up_slot = G.up_slot;

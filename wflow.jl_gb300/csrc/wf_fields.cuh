@@ -112,6 +112,8 @@ struct WfDevGraph {
     int32_t M;
     const int64_t* chunk_base;
     const int32_t* chunk_len;
+    const int32_t* chunk_g;        // chains in each chunk (G, or 1 for a long chain)
+    const int64_t* chunk_chain0;   // first chain of each chunk
     const int32_t* chain_len;
     const int32_t* up_ptr;
     const int64_t* up_slot;

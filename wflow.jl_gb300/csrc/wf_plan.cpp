@@ -96,17 +96,40 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
     });
     const int G = P.G;
     const int64_t nc_real = (int64_t)chains.size();
-    P.n_chains = (nc_real + G - 1) / G * G;
-    P.n_chunks = P.n_chains / G;
+    // The longest chains carry the critical path of every sweep; packing them G to a warp would
+    // make each of their steps pay for the divergent paths of G chains, so (when G > 1) they get
+    // a chunk of their own: chains of at least max(64, longest / 8) nodes, the 4096 longest at
+    // most. The remaining chains are packed G per chunk (padded to a multiple of G).
+    int64_t n_solo = 0;
+    if (G > 1 && nc_real > 0) {
+        const int32_t longest = chains.back().len;
+        const int32_t thr = std::max<int32_t>(64, longest / 8);
+        while (n_solo < nc_real && n_solo < 4096 && chains[nc_real - 1 - n_solo].len >= thr) ++n_solo;
+    }
+    const int64_t n_packed = nc_real - n_solo;
+    const int64_t packed_chains = (n_packed + G - 1) / G * G;
+    const int64_t packed_chunks = packed_chains / G;
+    P.n_chains = packed_chains + n_solo;
+    P.n_chunks = packed_chunks + n_solo;
     P.chain_len.assign(P.n_chains, 0);
     P.chunk_len.assign(P.n_chunks, 0);
+    P.chunk_g.assign(P.n_chunks, G);
+    P.chunk_chain0.assign(P.n_chunks, 0);
     P.chunk_base.assign(P.n_chunks + 1, 0);
-    for (int64_t c = 0; c < nc_real; ++c) P.chain_len[c] = chains[c].len;
+    std::vector<int64_t> chain_id(nc_real);  // sorted chain -> chain index (padding skipped)
+    for (int64_t c = 0; c < nc_real; ++c) {
+        chain_id[c] = c < n_packed ? c : packed_chains + (c - n_packed);
+        P.chain_len[chain_id[c]] = chains[c].len;
+    }
     for (int64_t k = 0; k < P.n_chunks; ++k) {
+        const int gk = k < packed_chunks ? G : 1;
+        const int64_t c0 = k < packed_chunks ? k * G : packed_chains + (k - packed_chunks);
+        P.chunk_g[k] = gk;
+        P.chunk_chain0[k] = c0;
         int32_t mx = 0;
-        for (int g = 0; g < G; ++g) mx = std::max(mx, P.chain_len[k * G + g]);
+        for (int g = 0; g < gk; ++g) mx = std::max(mx, P.chain_len[c0 + g]);
         P.chunk_len[k] = mx;
-        P.chunk_base[k + 1] = P.chunk_base[k] + (int64_t)mx * G;
+        P.chunk_base[k + 1] = P.chunk_base[k] + (int64_t)mx * gk;
         P.max_len = std::max(P.max_len, mx);
     }
     P.n_slots = P.chunk_base[P.n_chunks];
@@ -115,13 +138,16 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
     P.chain_of_node.assign(n, -1);
     P.is_chain_end.assign(P.n_slots, 0);
     for (int64_t c = 0; c < nc_real; ++c) {
-        int64_t chunk = c / G, g = c % G;
+        const int64_t id = chain_id[c];
+        const int64_t chunk = id < packed_chains ? id / G : packed_chunks + (id - packed_chains);
+        const int64_t g = id < packed_chains ? id % G : 0;
+        const int gk = P.chunk_g[chunk];
         int64_t u = chains[c].start;
         for (int32_t k = 0; k < chains[c].len; ++k) {
-            int64_t s = P.chunk_base[chunk] + (int64_t)k * G + g;
+            int64_t s = P.chunk_base[chunk] + (int64_t)k * gk + g;
             P.slot_of_node[u] = s;
             P.node_of_slot[s] = u;
-            P.chain_of_node[u] = (int32_t)c;
+            P.chain_of_node[u] = (int32_t)id;
             if (k == chains[c].len - 1) P.is_chain_end[s] = 1;
             u = ds[u];
         }
@@ -149,19 +175,22 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
 }
 
 bool wf_check_plan(const WfRoutingPlan& P, const int32_t* ds, std::string& err) {
-    const int G = P.G;
-    // position == height, chain lengths sorted
-    for (int64_t c = 1; c < P.n_chains; ++c) {
-        if (P.chain_len[c] != 0 && P.chain_len[c] < P.chain_len[c - 1]) {
+    // chain lengths sorted (padding chains have length 0)
+    int32_t prev = 0;
+    for (int64_t c = 0; c < P.n_chains; ++c) {
+        if (P.chain_len[c] == 0) continue;
+        if (P.chain_len[c] < prev) {
             err = "chains not sorted by length";
             return false;
         }
+        prev = P.chain_len[c];
     }
     for (int64_t s = 0; s < P.n_slots; ++s) {
         int64_t v = P.node_of_slot[s];
         if (v < 0) continue;
         int64_t chunk = 0;
         while (P.chunk_base[chunk + 1] <= s) ++chunk;
+        const int G = P.chunk_g[chunk];
         int64_t k = (s - P.chunk_base[chunk]) / G;
         int64_t my_chain = P.chain_of_node[v];
         for (int32_t o = P.up_ptr[s]; o < P.up_ptr[s + 1]; ++o) {

@@ -10,8 +10,9 @@
 // sorted by length form a valid dependency order: a lane only ever waits for chains dispatched
 // before its own, which guarantees forward progress of the persistent kernels.
 //
-// Chains are packed G per chunk (G = 32 / members for <= 32 members, else 1) and chunks are
-// laid out node-position-major: slot(c, k, g) = chunk_base[c] + k * G + g. With M members per
+// Chains are packed G per chunk (G = 32 / members for <= 32 members, else 1; the longest chains,
+// which carry the critical path, get a chunk each) and chunks are laid out
+// node-position-major: slot(c, k, g) = chunk_base[c] + k * G_c + g. With M members per
 // node the element index is slot * M + m, so one warp touches 32 consecutive elements at
 // every step of the walk. Every kernel of the step uses this slot layout.
 #pragma once
@@ -30,6 +31,8 @@ struct WfRoutingPlan {
     int32_t max_len = 0;    // longest chain = graph height + 1
     std::vector<int64_t> chunk_base;    // [n_chunks + 1]
     std::vector<int32_t> chunk_len;     // [n_chunks]
+    std::vector<int32_t> chunk_g;       // [n_chunks] chains in the chunk (G, or 1 for a long chain)
+    std::vector<int64_t> chunk_chain0;  // [n_chunks] index of the chunk's first chain
     std::vector<int32_t> chain_len;     // [n_chains] (0 for padding chains)
     std::vector<int64_t> slot_of_node;  // [n]
     std::vector<int64_t> node_of_slot;  // [n_slots], -1 for padding

@@ -77,7 +77,7 @@ __device__ __forceinline__ void publish(const WfDevGraph& g, int64_t chain, int 
 template <class Phys>
 __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
     const unsigned lane = threadIdx.x & 31u;
-    const int M = g.M, G = g.G;
+    const int M = g.M;
     const int gpc = M > 32 ? M / 32 : 1;
     const uint64_t n_items = (uint64_t)g.n_chunks * gpc;
     while (true) {
@@ -95,8 +95,9 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
             gi = 0;
             m = (int)(item % gpc) * 32 + (int)lane;
         }
-        const int64_t chain = chunk * G + gi;
-        const int len = g.chain_len[chain];
+        const int Gc = g.chunk_g[chunk];
+        const int64_t chain = g.chunk_chain0[chunk] + (gi < Gc ? gi : 0);
+        const int len = gi < Gc ? g.chain_len[chain] : 0;
         const int L = g.chunk_len[chunk];
         const int64_t base = g.chunk_base[chunk];
         for (int s = 0; s < sw.S; ++s) {
@@ -104,7 +105,7 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
             for (int k = 0; k < L; ++k) {
                 bool ok = true;
                 if (k < len) {
-                    const int64_t slot = base + (int64_t)k * G + gi;
+                    const int64_t slot = base + (int64_t)k * Gc + gi;
                     ok = phys.node(slot, slot * M + m, m, s, ep, chain, k == len - 1);
                 }
                 if (__any_sync(0xffffffffu, !ok)) return;

@@ -159,7 +159,7 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
     extern __shared__ unsigned long long wave_smem[];
     const unsigned lane = threadIdx.x & 31u;
     unsigned long long* qh = wave_smem + threadIdx.x;  // row of this thread: qh[s * blockDim.x]
-    const int M = g.M, G = g.G;
+    const int M = g.M;
     const int gpc = M > 32 ? M / 32 : 1;
     const uint64_t n_items = (uint64_t)g.n_chunks * gpc;
     while (true) {
@@ -177,16 +177,17 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
             gi = 0;
             m = (int)(item % gpc) * 32 + (int)lane;
         }
-        const int64_t chain = chunk * G + gi;
-        const int len = g.chain_len[chain];
+        const int Gc = g.chunk_g[chunk];
+        const int64_t chain = g.chunk_chain0[chunk] + (gi < Gc ? gi : 0);
+        const int len = gi < Gc ? g.chain_len[chain] : 0;
         const int L = g.chunk_len[chunk];
         const int64_t base = g.chunk_base[chunk];
         typename Phys::In cur, nxt;
         if (len > 0) phys.load(base + gi, (base + gi) * M + m, m, cur);
         for (int k = 0; k < L; ++k) {
-            const int64_t slot = base + (int64_t)k * G + gi;
+            const int64_t slot = base + (int64_t)k * Gc + gi;
             if (k + 1 < len) {
-                const int64_t ns = slot + G;
+                const int64_t ns = slot + Gc;
                 phys.load(ns, ns * M + m, m, nxt);
             }
             bool ok = true;
