@@ -15,6 +15,7 @@
 
 #include "wf_fields.cuh"
 #include "wf_kernels.h"
+#include "wf_launch.cuh"
 #include "wf_math.cuh"
 #include "wf_walker.cuh"
 
@@ -1011,17 +1012,11 @@ int grid_for(int64_t n, int block, int num_sms) {
 template <class Phys>
 cudaError_t launch_walk(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
-    int blocks = c.walk_blocks;
-    if (blocks <= 0) {
-        int per_sm = 0;
-        cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, walk_kernel<Phys>, threads, 0);
-        if (err != cudaSuccess) return err;
-        blocks = c.num_sms * (per_sm > 0 ? per_sm : 1);
-    }
-    const int64_t items = phys.g.n_chunks * (phys.g.M > 32 ? phys.g.M / 32 : 1);
-    const int64_t need = (items + threads / 32 - 1) / (threads / 32);
-    if (blocks > need) blocks = (int)(need < 1 ? 1 : need);
-    walk_kernel<Phys><<<blocks, threads, 0, c.stream>>>(phys);
+    int blocks;
+    Phys p = phys;
+    cudaError_t err = wave_grid(walk_kernel<Phys>, threads, 0, c, p.g, blocks, p.sw.prio_items);
+    if (err != cudaSuccess) return err;
+    walk_kernel<Phys><<<blocks, threads, 0, c.stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -19,6 +19,7 @@
 
 #include "wf_fields.cuh"
 #include "wf_kernels.h"
+#include "wf_launch.cuh"
 #include "wf_math.cuh"
 #include "wf_walker.cuh"
 #include "wf_ff.cuh"
@@ -1265,18 +1266,12 @@ __global__ void __launch_bounds__(128) wave_kernel(Phys phys) {
 template <class Phys>
 cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
-    const size_t smem = (size_t)threads * phys.sw.S * sizeof(double);
-    int blocks = c.walk_blocks;
-    if (blocks <= 0) {
-        int per_sm = 0;
-        cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wave_kernel<Phys>, threads, smem);
-        if (err != cudaSuccess) return err;
-        blocks = c.num_sms * (per_sm > 0 ? per_sm : 1);
-    }
-    const int64_t items = phys.g.n_chunks * (phys.g.M > 32 ? phys.g.M / 32 : 1);
-    const int64_t need = (items + threads / 32 - 1) / (threads / 32);
-    if (blocks > need) blocks = (int)(need < 1 ? 1 : need);
-    wave_kernel<Phys><<<blocks, threads, smem, c.stream>>>(phys);
+    const size_t smem = (size_t)threads * phys.sw.S * sizeof(unsigned long long);
+    int blocks;
+    Phys p = phys;
+    cudaError_t err = wave_grid(wave_kernel<Phys>, threads, smem, c, p.g, blocks, p.sw.prio_items);
+    if (err != cudaSuccess) return err;
+    wave_kernel<Phys><<<blocks, threads, smem, c.stream>>>(p);
     return cudaGetLastError();
 }
 
@@ -1605,17 +1600,11 @@ __global__ void __launch_bounds__(128) walk_split_kernel(Phys phys) {
 template <class Phys>
 cudaError_t launch_walk_split(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
-    int blocks = c.walk_blocks;
-    if (blocks <= 0) {
-        int per_sm = 0;
-        cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, walk_split_kernel<Phys>, threads, 0);
-        if (err != cudaSuccess) return err;
-        blocks = c.num_sms * (per_sm > 0 ? per_sm : 1);
-    }
-    const int64_t items = phys.g.n_chunks * (phys.g.M > 32 ? phys.g.M / 32 : 1);
-    const int64_t need = (items + threads / 32 - 1) / (threads / 32);
-    if (blocks > need) blocks = (int)(need < 1 ? 1 : need);
-    walk_split_kernel<Phys><<<blocks, threads, 0, c.stream>>>(phys);
+    int blocks;
+    Phys p = phys;
+    cudaError_t err = wave_grid(walk_split_kernel<Phys>, threads, 0, c, p.g, blocks, p.sw.prio_items);
+    if (err != cudaSuccess) return err;
+    walk_split_kernel<Phys><<<blocks, threads, 0, c.stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -172,6 +172,7 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.n_slots = G.plan.n_slots;
     g.n_chunks = G.plan.n_chunks;
     g.n_chains = G.plan.n_chains;
+    g.n_long_chunks = G.plan.n_long_chunks;
     g.G = G.plan.G;
     g.M = M;
     g.chunk_base = G.chunk_base;

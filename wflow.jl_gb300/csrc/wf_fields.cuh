@@ -108,6 +108,7 @@ struct WfDevGraph {
     int64_t n_slots;
     int64_t n_chunks;
     int64_t n_chains;
+    int64_t n_long_chunks;  // trailing chunks of the longest chains (dispatched first)
     int32_t G;
     int32_t M;
     const int64_t* chunk_base;
@@ -138,6 +139,7 @@ struct WfSweep {
     uint32_t epoch0;      // epoch of sub-step 0 of this launch
     double dt;            // model step
     const double* dts;    // [S] sub-step sizes (device)
+    int64_t prio_items;   // work items dispatched first (the longest chains), set at launch
     float dts_f[16];      // FP32 copy of the first 16 sub-step sizes (split form's slim walkers)
     uint64_t wait_ns;     // spin-wait budget per wait [ns]
     uint32_t wait_offset; // test hook: added to awaited epochs (0 in production)

@@ -133,6 +133,12 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
         P.max_len = std::max(P.max_len, mx);
     }
     P.n_slots = P.chunk_base[P.n_chunks];
+    {
+        const int32_t thr = std::max<int32_t>(64, P.max_len / 8);
+        P.n_long_chunks = 0;
+        while (P.n_long_chunks < P.n_chunks && P.chunk_len[P.n_chunks - 1 - P.n_long_chunks] >= thr)
+            ++P.n_long_chunks;
+    }
     P.slot_of_node.assign(n, -1);
     P.node_of_slot.assign(P.n_slots, -1);
     P.chain_of_node.assign(n, -1);

@@ -2,9 +2,11 @@
 //
 // One warp owns one chunk (G chains x M members, or one chain x 32 members) at a time and
 // walks it in lockstep from the leaves to the chain ends, sub-step by sub-step. Chunks are
-// taken from a global ticket counter in chain-length order, so a lane only waits for chain
-// ends of chunks dispatched earlier (or of shorter chains of its own chunk, which the lockstep
-// walk has already finished). Chain ends publish their discharge of every sub-step into a
+// taken from a global ticket counter: a bounded number of the longest chains first (see
+// wave_grid in wf_launch.cuh for why that keeps progress guaranteed), then the others in
+// chain-length order, so an ordinary chunk only waits for chain ends of chunks dispatched
+// earlier (or of shorter chains of its own chunk, which the lockstep walk has already
+// finished). Chain ends publish their discharge of every sub-step into a
 // per-sub-step buffer and then release an epoch flag; consumers acquire the flag and read the
 // buffer, so no producer can overwrite a value a consumer still needs.
 //
@@ -80,11 +82,15 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
     const int M = g.M;
     const int gpc = M > 32 ? M / 32 : 1;
     const uint64_t n_items = (uint64_t)g.n_chunks * gpc;
+    const uint64_t prio = (uint64_t)sw.prio_items;
     while (true) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(g.ticket, 1ULL);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= n_items) return;
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(g.ticket, 1ULL);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n_items) return;
+        // the first prio_items tickets take the longest chains, longest first; the rest take
+        // the other items in dependency (chain length) order
+        const unsigned long long item = t < prio ? n_items - 1 - t : t - prio;
         if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
         const int64_t chunk = (int64_t)(item / gpc);
         int gi, m;

@@ -8,7 +8,8 @@
 // the upstream discharges and the solve.
 //
 // A warp owns one chunk (G chains x M members, or one chain x 32 members) taken from a global
-// ticket counter in chain-length order, and walks it leaf -> chain end. Each node is advanced
+// ticket counter (a bounded number of the longest chains first, then the others in chain-length
+// order; wave_grid in wf_launch.cuh) and walks it leaf -> chain end. Each node is advanced
 // through all sub-steps of the launch before the walker moves downstream (node-major order):
 // the node's own state stays in registers across sub-steps and the heavy child's discharge
 // of every sub-step is handed over in a per-thread shared-memory row. Chain ends publish the
@@ -162,11 +163,15 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
     const int M = g.M;
     const int gpc = M > 32 ? M / 32 : 1;
     const uint64_t n_items = (uint64_t)g.n_chunks * gpc;
+    const uint64_t prio = (uint64_t)sw.prio_items;
     while (true) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(g.ticket, 1ULL);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= n_items) return;
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(g.ticket, 1ULL);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n_items) return;
+        // the first prio_items tickets take the longest chains, longest first; the rest take
+        // the other items in dependency (chain length) order
+        const unsigned long long item = t < prio ? n_items - 1 - t : t - prio;
         if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
         const int64_t chunk = (int64_t)(item / gpc);
         int gi, m;
