@@ -1,17 +1,20 @@
 """Throughput of the SBM + kinematic-wave step on a GB300 (cell-timesteps per second).
 
-Default workload: one 1024 x 1024 synthetic catchment (250 m cells), hourly steps, SBM with
-snow, kinematic-wave subsurface/overland/river routing with the reference's fixed sub-steps
-(land 3600 s, river 900 s, subsurface 86400 s clamped to dt) and the water balance on.
+Default workload: a 64-member ensemble on one 1024 x 1024 synthetic catchment (250 m cells,
+67M cell-instances), hourly steps, SBM with snow, kinematic-wave subsurface/overland/river
+routing with the reference's fixed sub-steps (land 3600 s, river 900 s, subsurface 86400 s
+clamped to dt) and the water balance on, in the FP32/FP64 split form. The same line carries the
+FP64 plain form on the same workload (`fp64_plain`, `split_over_fp64`) and the split form's
+outlet-discharge and closure errors against it (`accuracy`).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp64|split] [--workload NAME]
   python bench.py --impl reference ...   # the CPU restatement of the reference (the oracle)
 
 `value` times K steps with the step's forcing already resident in HBM (CUDA events on the
 library's stream). `e2e` times the same K steps through the public C ABI with host forcing
-from pinned memory copied in and the outlet discharge copied out every step. The state of a
-1024^2 model (about 1.2 GB in FP64) is far larger than the 129 MB L2, so no L2 flush is
-needed between steps.
+from pinned memory copied in and the outlet discharge copied out every step. The model state
+(tens of GB for the ensemble, over 1 GB for one 1024^2 domain) is far larger than the 129 MB
+L2, so no L2 flush is needed between steps.
 """
 
 import argparse
@@ -35,9 +38,13 @@ WORKLOADS = {
     "single_64_daily": (64, 1000.0, 86400.0, 1, 365),
 }
 
-# Algorithmic bytes per cell and launch of each kernel (FP64 form), from the fields each
-# kernel reads and writes once per cell.
+# Algorithmic bytes per cell (and member) of one launch of each kernel: the fields each kernel
+# reads and writes once per cell. FP64 form: FP64 fields throughout. Split form (vertical): FP32
+# forcing and member parameters (28 B), 11 FP64 states read (88 B), 20 FP64 states and fluxes
+# written (160 B), 13 FP32 diagnostics and subsurface inputs written (52 B), static fields shared
+# by the members of a cell (~8 B per member at 64 members).
 ALGO_BYTES_FP64 = {"vertical": 729, "subsurface": 400, "overland": 136, "river": 160, "balance": 240}
+ALGO_BYTES_SPLIT = {"vertical": 336, "subsurface": 200, "overland": 80, "river": 80, "balance": 200}
 
 
 def log(*a):
@@ -148,7 +155,9 @@ def run_gpu(args):
     dom, params, cfg, pfac = build_workload(args.workload, form, seed=args.seed)
     side, cell, dt, members, _ = WORKLOADS[args.workload]
     n = dom.n_land
+    free0 = torch.cuda.mem_get_info(local)[0]
     model = Model(cfg, dom, params=params, device=local)
+    state_gb = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
     lib = model.lib
     # ---- forcing resident in HBM, in the library's slot order, for W + K steps
     slots = model.slot_order()
@@ -262,7 +271,7 @@ def run_gpu(args):
                    "dt_s": dt, "form": args.form, "substeps": {"land": int(round(dt / min(dt, 3600.0))),
                                                                "river": int(np.ceil(dt / 900.0)),
                                                                "subsurface": 1},
-                   "l2": "state 1.2 GB per 1M cells >> 129 MB L2, no flush needed",
+                   "l2": f"model state {state_gb:.1f} GB on the device >> 129 MB L2, no flush needed",
                    "chains_land": mt["n_chains_land"], "max_chain_land": mt["max_chain_land"],
                    "max_chain_river": mt["max_chain_river"], "parallelism": f"replicas{ws}",
                    "tuning": tuning},
@@ -280,19 +289,92 @@ def run_gpu(args):
     except Exception:
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    bytes_launch = ALGO_BYTES_FP64[dom_k] * cells
+    algo = ALGO_BYTES_SPLIT if form == abi.WF_FORM_SPLIT else ALGO_BYTES_FP64
+    bytes_launch = algo[dom_k] * cells
     if dom_k == "river":
-        bytes_launch = ALGO_BYTES_FP64[dom_k] * dom.n_river * members * int(np.ceil(dt / 900.0))
+        bytes_launch = algo[dom_k] * dom.n_river * members * int(np.ceil(dt / 900.0))
     achieved = bytes_launch / (kt[dom_k] / 1e3) / 1e9 if kt[dom_k] > 0 else 0.0
     result["roofline"] = {"kernel": dom_k, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": traffic_from_profiles(dom_k, args.workload),
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
+    # ---- the FP64 plain form on the same workload and forcing: throughput ratio and the split
+    # form's error against it (the FP64 form reproduces the FP64 oracle bit for bit)
+    if form == abi.WF_FORM_SPLIT and not args.no_fp64_leg:
+        result.update(fp64_leg(args, model, dom, params, resident, W, K, dt, members, n, dev))
+        result["split_over_fp64"] = value / result["fp64_plain"]["value"]
     model.close()
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(args) if not args.no_cpu_baseline else None
         print(json.dumps(result), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def fp64_leg(args, split_model, dom, params, resident, W, K, dt, members, n, dev):
+    """Time the FP64 plain form on the same resident forcing (fewer steps: it is slower), then
+    replay both forms over the same steps from the same cold state and compare outlet discharge
+    and the split form's land-balance closure."""
+    import torch
+
+    from wflow_gb300 import abi, synthetic
+    from wflow_gb300.model import Model
+
+    cfg64 = synthetic.make_config(dt, n_members=members, form=abi.WF_FORM_FP64, per_member_soil=members > 1)
+    m64 = Model(cfg64, dom, params=params, device=dev.index or 0)
+    stream = torch.cuda.ExternalStream(m64.stream(), device=dev)
+    k64 = max(2, min(K, 5))
+    for s in range(W):
+        b = resident[s]
+        m64.set_forcing_device_slots(b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr())
+        m64.update_model()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for s in range(W, W + k64):
+        b = resident[s]
+        m64.set_forcing_device_slots(b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr())
+        m64.step_async()
+    ev1.record(stream)
+    ev1.synchronize()
+    m64.synchronize()
+    ms64 = ev0.elapsed_time(ev1)
+    m64.close()
+    # accuracy: both forms from the cold state over the same steps
+    cfg_s = synthetic.make_config(dt, n_members=members, form=abi.WF_FORM_SPLIT, per_member_soil=members > 1)
+    a = Model(cfg64, dom, params=params, device=dev.index or 0)
+    b_ = Model(cfg_s, dom, params=params, device=dev.index or 0)
+    worst_q = 0.0
+    closure = {"split": [0.0, 0.0], "fp64": [0.0, 0.0]}  # [max relative error, max |error| / median flux]
+    for s in range(min(W + K, 8)):
+        r = resident[s]
+        for mdl in (a, b_):
+            mdl.set_forcing_device_slots(r[0].data_ptr(), r[1].data_ptr(), r[2].data_ptr())
+            mdl.update_model()
+        qa, qb = a.outlets(1), b_.outlets(1)
+        worst_q = max(worst_q, float(np.max(np.abs(qb - qa) / np.maximum(np.abs(qa), 1e-12))))
+        for name, mdl in (("fp64", a), ("split", b_)):
+            err = mdl.get_value("BALANCE_LAND_ERROR")
+            rel = mdl.get_value("BALANCE_LAND_RELATIVE_ERROR")
+            nz = rel != 0.0
+            flux = np.median(np.abs(err[nz] / rel[nz])) if nz.any() else 1.0
+            closure[name][0] = max(closure[name][0], float(np.max(np.abs(rel))))
+            closure[name][1] = max(closure[name][1], float(np.max(np.abs(err)) / flux))
+    a.close()
+    b_.close()
+    cells = n * members
+    return {"fp64_plain": {"value": cells * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
+                           "unit": "cell-timesteps/s"},
+            "accuracy": {"outlet_q_rel_err_max": worst_q,
+                         "land_balance_closure_rel_max": {"split": closure["split"][0], "fp64": closure["fp64"][0]},
+                         "land_balance_closure_over_median_flux": {"split": closure["split"][1],
+                                                                   "fp64": closure["fp64"][1]},
+                         "closure_note": "relative error as the reference defines it (error / mean of in- and "
+                                         "outflow) peaks in cells whose fluxes are ~1e-12 m/s, for the FP64 "
+                                         "form as well; the flux-normalised figure divides by the median flux",
+                         "steps": min(W + K, 8),
+                         "against": "FP64 plain form on the GPU (bit-identical to the FP64 oracle in the parity "
+                                    "tests)"}}
 
 
 def traffic_from_profiles(kernel, workload):
@@ -316,6 +398,12 @@ def cpu_baseline(args, steps=None):
 
     dom, params, cfg, pfac = build_workload(args.workload, abi.WF_FORM_FP64, seed=args.seed)
     side, cell, dt, members, _ = WORKLOADS[args.workload]
+    if members > 1:  # bounded sample: the first member of the ensemble (cost is linear in members)
+        from wflow_gb300 import synthetic
+        cfg = synthetic.make_config(dt, n_members=1, form=abi.WF_FORM_FP64)
+        params = dom.params
+        pfac = pfac[:1]
+        members = 1
     threads = os.cpu_count() or 1
     orc = oracle_py.OracleModel(cfg, dom, params=params)
     n = dom.n_land
@@ -335,15 +423,16 @@ def cpu_baseline(args, steps=None):
             break
     el = time.perf_counter() - t0
     return {"value": n * members * done / el, "unit": "cell-timesteps/s", "cores": threads, "kind": "port",
-            "sample": f"{done} steps of the {args.workload} workload ({n * members} cells) after 1 warm-up step, "
-                      f"{el:.1f} s"}
+            "sample": f"{done} steps of {n * members} cells of the {args.workload} workload "
+                      f"({'first member of the ensemble, ' if WORKLOADS[args.workload][3] > 1 else ''}"
+                      f"after 1 warm-up step), {el:.1f} s"}
 
 
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
-    cb = cpu_baseline(args, steps=args.steps)
+    cb = cpu_baseline(args, steps=min(args.steps, 10))
     side, cell, dt, members, _ = WORKLOADS[args.workload]
     result = {
         "impl": "reference",
@@ -358,7 +447,8 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded), same workload as the GPU arm",
-        "config": {"workload": args.workload, "cells": side * side, "members": members, "dt_s": dt},
+        "config": {"workload": args.workload, "cells": side * side, "members": members, "dt_s": dt,
+                   "form": "fp64 (the reference's arithmetic)"},
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": "cell-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "Julia (the reference's own runtime) is not installed on this host; the reference arm is the "
@@ -370,14 +460,15 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "split"])
-    ap.add_argument("--workload", default="single_1024_hourly", choices=list(WORKLOADS))
+    ap.add_argument("--form", default="split", choices=["fp64", "split"])
+    ap.add_argument("--workload", default="ensemble64_1024_hourly", choices=list(WORKLOADS))
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64 plain comparison leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
