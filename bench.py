@@ -36,6 +36,8 @@ WORKLOADS = {
     "single_1024_hourly": (1024, 250.0, 3600.0, 1, 720),
     "ensemble64_1024_hourly": (1024, 250.0, 3600.0, 64, 240),
     "single_64_daily": (64, 1000.0, 86400.0, 1, 365),
+    # small case of the ensemble workload for multi-pass profiler captures (1/16 of the cells)
+    "ensemble64_256_hourly": (256, 250.0, 3600.0, 64, 10),
 }
 
 # Algorithmic bytes per cell (and member) of one launch of each kernel: the fields each kernel
@@ -457,6 +459,29 @@ def run_reference(args):
     print(json.dumps(result), flush=True)
 
 
+def run_profile(args):
+    """Profiler driver: build the workload, run --steps eager steps (one launch per kernel, no
+    CUDA graph), print the per-kernel milliseconds to stderr and exit."""
+    import torch
+
+    from wflow_gb300 import abi, build
+    from wflow_gb300.model import Model
+
+    torch.cuda.set_device(0)
+    build.build_all()
+    form = abi.WF_FORM_SPLIT if args.form == "split" else abi.WF_FORM_FP64
+    dom, params, cfg, pfac = build_workload(args.workload, form, seed=args.seed)
+    side, cell, dt, members, _ = WORKLOADS[args.workload]
+    model = Model(cfg, dom, params=params)
+    model.set_tuning(vertical_block=128, routing_warps=2, routing_blocks_per_sm=0, use_graph=0, kernel_timing=1)
+    for s in range(args.steps):
+        P, PET, T = member_forcing(s, dt, dom.n_land, members, pfac, seed=args.seed)
+        model.run_timestep(P, PET, T)
+    kt, calls = model.kernel_times()
+    log(f"[profile] {args.workload} {args.form}: ms per step {({k: round(v / max(calls, 1), 3) for k, v in kt.items()})}")
+    model.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -469,10 +494,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64 plain comparison leg")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiler driver: run --steps eager steps of the workload and exit (no JSON line)")
     args = ap.parse_args()
-    if args.warmup < 3:
+    if args.warmup < 3 and not args.profile:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
