@@ -31,6 +31,44 @@ using wfm::jmin;
 
 namespace {
 
+// FP64 view of the split form's double-FP32 member fields, for the rare paths that keep the
+// reference's FP64 arithmetic (the full subsurface column computation, sub-stepped subsurface
+// flow): Mf[field][e] reads and writes a (high, low) pair as one double.
+struct FFRef {
+    float* h;
+    float* l;
+    double* d;  // the field is FP64 (a large store)
+    __device__ __forceinline__ operator double() const { return d ? *d : (double)*h + (double)*l; }
+    __device__ __forceinline__ FFRef& operator=(double v) {
+        if (d) {
+            *d = v;
+            return *this;
+        }
+        const float a = (float)v;
+        *h = a;
+        *l = (float)(v - (double)a);
+        return *this;
+    }
+};
+struct FFRow {
+    float* h;
+    float* l;
+    double* d;
+    __device__ __forceinline__ FFRef operator[](int64_t e) const {
+        return d ? FFRef{nullptr, nullptr, d + e} : FFRef{h + e, l + e, nullptr};
+    }
+};
+struct FFMem {  // member fields
+    const WfDevFields& F;
+    __device__ __forceinline__ FFRow operator[](int f) const {
+        return wf_split_fp64_member(f) ? FFRow{nullptr, nullptr, F.Mf[f]} : FFRow{F.Mh[f], F.Ml[f], nullptr};
+    }
+};
+struct FFUsld {  // unsaturated layer stores
+    const WfDevFields& F;
+    __device__ __forceinline__ FFRow operator[](int k) const { return {F.LYf[LY_USLD][k], F.LYl[k], nullptr}; }
+};
+
 constexpr double KIN_WAVE_MIN_FLOW = 1e-30;
 constexpr double KIN_WAVE_MIN_FLOW_QROOT = 0x1.0c6f7a0b5ed8ap-20;
 constexpr float MM_PER_DAY_F = (float)((1.0 / 86400.0) * 1e-3);
@@ -203,20 +241,19 @@ __device__ __forceinline__ double wfm_rcp(double x) {
     return r;
 }
 
-// FP64 store updated by FP32 increments without rounding loss.
+// Store of the split form: its content at the start of the step (a double-FP32 pair) plus
+// the exact sum of the step's FP32 increments (TwoSum / TwoProd), added once at the end.
 struct Store {
-    double base;
-    float bf;      // base rounded to FP32 (for FP32 decisions)
+    wff::ff base;
     float hi, lo;  // increments of this step: exactly hi + lo
     bool mod;      // content differs from what was loaded
-    __device__ __forceinline__ void init(double b) {
+    __device__ __forceinline__ void init(wff::ff b) {
         base = b;
-        bf = (float)b;
         hi = 0.0f;
         lo = 0.0f;
         mod = false;
     }
-    __device__ __forceinline__ float val() const { return bf + hi; }
+    __device__ __forceinline__ float val() const { return base.hi + hi; }
     __device__ __forceinline__ void add(float x) {  // TwoSum
         const float s = hi + x;
         const float bp = s - hi;
@@ -231,26 +268,24 @@ struct Store {
         add(p);
         lo += e;
     }
-    __device__ __forceinline__ void add_d(double x) {
-        const float xh = (float)x;
-        add(xh);
-        lo += (float)(x - (double)xh);
+    __device__ __forceinline__ void add(wff::ff x) {
+        add(x.hi);
+        lo += x.lo;
     }
     __device__ __forceinline__ bool changed() const { return mod; }
-    __device__ __forceinline__ double value() const { return base + ((double)hi + (double)lo); }
+    __device__ __forceinline__ wff::ff value() const { return wff::add(base, wff::ff{hi, lo}); }
     __device__ __forceinline__ void zero() {
-        base = 0.0;
-        bf = 0.0f;
+        base = {0.0f, 0.0f};
         hi = 0.0f;
         lo = 0.0f;
         mod = true;
     }
-    __device__ __forceinline__ void set(double v) {
+    __device__ __forceinline__ void set(wff::ff v) {
         init(v);
         mod = true;
     }
-    __device__ __forceinline__ double take_all() {  // empties the store, returns its content
-        const double v = value();
+    __device__ __forceinline__ wff::ff take_all() {  // empties the store, returns its content
+        const wff::ff v = value();
         zero();
         return v;
     }
@@ -273,13 +308,12 @@ struct ColG {
             float t = __int_as_float(0x7fc00000);
             if (k < N) {
                 act[k] = F.LYf[LY_ACT_THICK][k][slot];
-                cum[k + 1] = F.LYf[LY_CUM][k][slot];
                 const double c1 = F.LY[LY_CUM][k][slot];
+                cum[k + 1] = F.LYf[LY_CUM][k][slot];
                 if (zi > c1) {
                     t = act[k];
-                } else {
-                    const double r = zi - c0;
-                    if (r > 0.0) t = (float)r;
+                } else if (zi > c0) {
+                    t = (float)(zi - c0);
                 }
                 c0 = c1;
             } else {
@@ -292,33 +326,55 @@ struct ColG {
     }
 };
 
+__device__ __forceinline__ wff::ff ldm(const WfDevFields& F, int f, int64_t e) { return {F.Mh[f][e], F.Ml[f][e]}; }
+__device__ __forceinline__ void stm(const WfDevFields& F, int f, int64_t e, wff::ff v) {
+    F.Mh[f][e] = v.hi;
+    F.Ml[f][e] = v.lo;
+}
+__device__ __forceinline__ wff::ff lds(const WfDevFields& F, int f, int64_t slot) { return {F.Lf[f][slot], F.Ll[f][slot]}; }
+__device__ __forceinline__ wff::ff ldr(const WfDevFields& F, int f, int64_t e) { return {F.RMh[f][e], F.RMl[f][e]}; }
+__device__ __forceinline__ void str(const WfDevFields& F, int f, int64_t e, wff::ff v) {
+    F.RMh[f][e] = v.hi;
+    F.RMl[f][e] = v.lo;
+}
+__device__ __forceinline__ wff::ff ldrs(const WfDevFields& F, int f, int64_t slot) {
+    return {F.Rf[f][slot], F.Rl[f][slot]};
+}
+
+// ----------------------------------------------------------------- vertical kernel ------
+//
+// GB300 issues FP64 instructions (arithmetic, compares and FP32<->FP64 conversions alike) at
+// about 1/70 of its FP32 FMA rate, so the split form executes none here: rates, limiters and
+// transcendental functions are FP32; every store (canopy, snow, liquid snow water,
+// unsaturated layers) and every flux that enters the water balance is a double-FP32 pair
+// (wf_ff.cuh); stores take the step's FP32 increments exactly (TwoSum/TwoProd); partitions of
+// a flux are exact residuals, so the parts always sum to the whole.
 template <int MAXN>
 __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
+    using wff::ff;
     const int M = F.M;
     const int64_t E = F.land_slots * M;
-    const double dt = F.dt, inv_dt = F.inv_dt;
-    const float dtf = (float)F.dt, inv_dtf = (float)F.inv_dt;
+    const float dtf = (float)F.dt;
+    const ff inv_dt = {F.inv_dt_hi, F.inv_dt_lo};
+    const float inv_dtf = F.inv_dt_hi;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
-        double* const* Mf = F.Mf;
         float* const* Mh = F.Mh;
         float* const* Lf = F.Lf;
         const float Pf = Mh[PRECIP][e], PETf = Mh[POTEVAP][e], Tf = Mh[TEMP][e];
-        const double Pd = (double)Pf;
-        const double canopy0 = Mf[CANOPY][e], snow0 = F.snow ? Mf[SNOW][e] : 0.0,
-                     sw0 = F.snow ? Mf[SNOW_WATER][e] : 0.0;
-        if (F.mass_balance) Mf[BL_PREV][e] = Mf[TSWS][e] + canopy0 + (snow0 + sw0);
+        const ff canopy0 = ldm(F, CANOPY, e);
+        const ff snow0 = F.snow ? ldm(F, SNOW, e) : ff{0.0f, 0.0f};
+        const ff sw0 = F.snow ? ldm(F, SNOW_WATER, e) : ff{0.0f, 0.0f};
+        if (F.mass_balance) F.Mf[BL_PREV][e] = F.Mf[TSWS][e] + wff::to_d(wff::add(canopy0, wff::add(snow0, sw0)));
         // ---- interception (canopy.jl:213-226 Gash, :259-271 Rutter)
         const float gapf = Lf[GAP][slot], cmaxf = Lf[CMAX][slot];
         const float potevap_f = Lf[KC][slot] * PETf * (1.0f - gapf);
-        double tf_d, ic_d;
+        ff tf, ic;
         float icf, sff;
         Store canopy;
-        canopy.base = canopy0;
-        canopy.hi = canopy.lo = 0.0f;
-        canopy.mod = false;
+        canopy.init(canopy0);
         if (F.gash) {
             if (cmaxf > 0.0f) {
                 const float e_r = Lf[E_R][slot];
@@ -332,16 +388,16 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
                     fi = 0.0f;
                     psat = 0.0f;
                 }
-                const float ic = Pf > psat ? (fi * psat - cmaxf * inv_dtf) + e_r * (Pf - psat) + cmaxf * inv_dtf
-                                           : fi * Pf;
+                const float icr = Pf > psat ? (fi * psat - cmaxf * inv_dtf) + e_r * (Pf - psat) + cmaxf * inv_dtf
+                                            : fi * Pf;
                 sff = fs * Pf;
-                icf = fminf(ic, potevap_f);
-                ic_d = (double)icf;
-                tf_d = Pd - ic_d - (double)sff;
+                icf = fminf(icr, potevap_f);
+                ic = wff::from_f(icf);
+                tf = wff::sub(wff::two_sum(Pf, -icf), sff);
             } else {
-                tf_d = Pd;
+                tf = wff::from_f(Pf);
                 icf = 0.0f;
-                ic_d = 0.0;
+                ic = {0.0f, 0.0f};
                 sff = 0.0f;
             }
         } else {
@@ -354,48 +410,47 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
                 pcf = 0.0f;
             }
             sff = fs * Pf;
-            tf_d = Pd - (double)sff - (double)pcf;
-            const double cmax_d = F.L[CMAX][slot];
-            canopy.bf = (float)canopy0;
-            if (canopy0 > cmax_d) {
-                tf_d += (canopy0 - cmax_d) * inv_dt;
-                canopy.set(cmax_d);
+            tf = wff::sub(wff::two_sum(Pf, -sff), pcf);
+            const ff cmax = lds(F, CMAX, slot);
+            if (wff::gt(canopy0, cmax)) {
+                tf = wff::add(tf, wff::mul(wff::sub(canopy0, cmax), inv_dt));
+                canopy.set(cmax);
             }
             canopy.add_prod(pcf, dtf);
             if (potevap_f * dtf >= canopy.val() && potevap_f > 0.0f) {
-                ic_d = canopy.take_all() * inv_dt;
-                icf = (float)ic_d;
+                ic = wff::mul(canopy.take_all(), inv_dt);
+                icf = wff::to_f(ic);
             } else {
                 icf = potevap_f;
-                ic_d = (double)icf;
+                ic = wff::from_f(icf);
                 canopy.add_prod(-icf, dtf);
             }
             if (canopy.val() > cmaxf) {
-                const double c = canopy.value();
-                if (c > cmax_d) {
-                    tf_d += (c - cmax_d) * inv_dt;
-                    canopy.set(cmax_d);
+                const ff c = canopy.value();
+                if (wff::gt(c, cmax)) {
+                    tf = wff::add(tf, wff::mul(wff::sub(c, cmax), inv_dt));
+                    canopy.set(cmax);
                 }
             }
         }
         // ---- snow (snow.jl:238-293, snow_process.jl:26-116)
-        double wfs_d;
+        ff wfs;
         float swe_out = 0.0f;
         Store snow, sw;
         if (F.snow) {
             snow.init(snow0);
             sw.init(sw0);
-            const double eff_d = tf_d + (double)sff;
+            const ff eff = wff::add(tf, sff);
             const float tti = Lf[TTI][slot], tt = Lf[TT][slot];
             const float rainfrac = tti == 0.0f ? (Tf > tt ? 1.0f : 0.0f)
                                                : fminf(fmaxf((Tf - (tt - tti / 2.0f)) / tti, 0.0f), 1.0f);
-            const double lp_d = (double)rainfrac * eff_d;
-            const double sp_d = eff_d - lp_d;
+            const ff lp = wff::mul(eff, rainfrac);
+            const ff sp = wff::sub(eff, lp);
             const float ttm = Lf[TTM][slot], ddf = Lf[DDF][slot];
             if (Tf > ttm) {
                 const float melt = ddf * (Tf - ttm);
                 if (melt * dtf >= snow.val()) {
-                    if (snow.val() > 0.0f) sw.add_d(snow.take_all());
+                    if (snow.val() > 0.0f) sw.add(snow.take_all());
                 } else {
                     snow.add_prod(-melt, dtf);
                     sw.add_prod(melt, dtf);
@@ -403,55 +458,68 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             } else {
                 const float refr = ddf * 0.05f * (ttm - Tf) * dtf;
                 if (refr >= sw.val()) {
-                    if (sw.val() > 0.0f) snow.add_d(sw.take_all());
+                    if (sw.val() > 0.0f) snow.add(sw.take_all());
                 } else {
                     snow.add(refr);
                     sw.add(-refr);
                 }
             }
-            snow.add_d(sp_d * dt);
-            sw.add_d(lp_d * dt);
+            snow.add(wff::mul(sp, dtf));
+            sw.add(wff::mul(lp, dtf));
             const float whc = Lf[WHC][slot];
-            double srunoff_d = 0.0;
+            wfs = {0.0f, 0.0f};
             if (sw.val() > snow.val() * whc) {
-                const double maxsw = snow.value() * (double)whc;
-                const double s = sw.value();
-                if (s > maxsw) {
-                    srunoff_d = (s - maxsw) * inv_dt;
+                const ff maxsw = wff::mul(snow.value(), whc);
+                const ff s = sw.value();
+                if (wff::gt(s, maxsw)) {
+                    wfs = wff::mul(wff::sub(s, maxsw), inv_dt);
                     sw.set(maxsw);
                 }
             }
             swe_out = sw.val() + snow.val();
-            wfs_d = srunoff_d;
         } else {
-            wfs_d = tf_d + (double)sff;
+            wfs = wff::add(tf, sff);
         }
         // ---- open water (runoff.jl open-water runoff and evaporation)
-        const double rfrac = F.L[RIVER_FRACTION][slot], wfrac = F.L[WATER_FRACTION][slot];
         const float rfrac_f = Lf[RIVER_FRACTION][slot], wfrac_f = Lf[WATER_FRACTION][slot];
-        const float wd_land = (float)Mf[OL_H][e];
+        const float wd_land = Mh[OL_H][e];
         const int64_t rs = F.land_river_slot[slot];
-        const float wd_river = rs >= 0 ? (float)F.RM[RV_H][rs * M + m] : 0.0f;
-        const double runoff_river_d = fmin(1.0, rfrac) * wfs_d;
-        const double runoff_land_d = fmin(1.0, wfrac) * wfs_d;
+        const float wd_river = rs >= 0 ? F.RMh[RV_H][rs * M + m] : 0.0f;
+        const ff runoff_river = wff::mul(wfs, fminf(1.0f, rfrac_f));
+        const ff runoff_land = wff::mul(wfs, fminf(1.0f, wfrac_f));
         const float ae_river_f = rfrac_f * fminf(wd_river * inv_dtf, PETf);
         const float ae_land_f = wfrac_f * fminf(wd_land * inv_dtf, PETf);
-        const double ae_river_d = (double)ae_river_f, ae_land_d = (double)ae_land_f;
         // ---- soil (soil.jl update! of SbmSoilModel)
-        const double wfs_soil_d = fmax(wfs_d - runoff_river_d - runoff_land_d, 0.0);
+        const ff wfs_soil = wff::fmax0(wff::sub(wff::sub(wfs, runoff_river), runoff_land));
         const float soil_fraction = fmaxf(gapf - wfrac_f - rfrac_f, 0.0f);
         const float pot_trans = fmaxf(0.0f, potevap_f - icf);
         const float pot_soilevap = soil_fraction * PETf;
         const double d_soil = F.L[SOIL_THICKNESS][slot];
-        const double sat = Mf[SAT][e];
-        const double zi = fmax(0.0, d_soil - sat * F.L[INV_TE][slot]);
+        const double sat = F.Mf[SAT][e];
+        const double zi = fmax(0.0, fma(-sat, F.L[INV_TE][slot], d_soil));
         ColG<MAXN> g;
         g.set(F, slot, zi);
-        const float zif = (float)zi, df = Lf[SOIL_THICKNESS][slot];
+        const float zif = (float)zi, df = Lf[SOIL_THICKNESS][slot], satf = (float)sat;
         const float ts = Lf[THETA_S][slot], tr = Lf[THETA_R][slot], tfc = Lf[THETA_FC][slot];
         const float te = ts - tr;
         const float kv0 = Mh[KV0][e], fsc = Mh[FSCALE][e], zexp = Lf[Z_EXP][slot];
         const bool kv_const = F.kv_profile == WF_KV_EXPONENTIAL_CONSTANT;
+        Store us[MAXN];
+        float kvf[MAXN], cexp[MAXN], rfr[MAXN];
+        float usd = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXN; ++k) {
+            if (k < g.N) {
+                us[k].init({F.LYf[LY_USLD][k][e], F.LYl[k][e]});
+                kvf[k] = F.LYf[LY_KVFRAC][k][slot];
+                cexp[k] = F.LYf[LY_C][k][slot];
+                rfr[k] = F.LYf[LY_ROOTFRAC][k][slot];
+            } else {
+                us[k].init({0.0f, 0.0f});
+                kvf[k] = cexp[k] = rfr[k] = 0.0f;
+            }
+            if (k < g.nl) usd += us[k].val();
+        }
         // Kv at depth z of layer n (1-based); the layer's factor is selected without dynamic
         // indexing so that the per-layer arrays stay in registers
 #define WF_KV_AT(z_, n_)                                           \
@@ -462,24 +530,8 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         _Pragma("unroll") for (int j_ = 0; j_ < MAXN; ++j_) if (j_ == (n_) - 1) kf_ = kvf[j_]; \
         return kf_ * kv0 * expf(-fsc * zz_);                       \
     }())
-        Store us[MAXN];
-        float kvf[MAXN], cexp[MAXN], rfr[MAXN];
-        float usd = 0.0f;
-#pragma unroll
-        for (int k = 0; k < MAXN; ++k) {
-            if (k < g.N) {
-                us[k].init(F.LY[LY_USLD][k][e]);
-                kvf[k] = F.LYf[LY_KVFRAC][k][slot];
-                cexp[k] = F.LYf[LY_C][k][slot];
-                rfr[k] = F.LYf[LY_ROOTFRAC][k][slot];
-            } else {
-                us[k].zero();
-                kvf[k] = cexp[k] = rfr[k] = 0.0f;
-            }
-            if (k < g.nl) usd += us[k].val();
-        }
         float drain = (df - zif) * fmaxf(ts - tfc, 0.02f);
-        float ucap = Lf[SWC][slot] - (float)sat - usd;
+        float ucap = Lf[SWC][slot] - satf - usd;
         float tsoil = Mh[TSOIL][e];
         if (F.snow) tsoil = tsoil + Lf[W_SOIL][slot] * (Tf - tsoil);
         float fred = 1.0f;
@@ -487,64 +539,60 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             const float cf = Lf[CF_SOIL][slot];
             fred = 1.0f / (1.0f / (1.0f - cf) + expf(-8.0f * (tsoil - 273.15f))) + cf;
         }
-        // infiltration (soil_process.jl infiltration): FP64 partition of the water reaching the soil
-        const double soilinf_d = wfs_soil_d * (1.0 - F.L[COMPACT_FRAC][slot]);
-        const double pathinf_d = wfs_soil_d - soilinf_d;
+        // infiltration (soil_process.jl infiltration): exact partition of the water reaching the soil
+        const ff soilinf = wff::mul(wfs_soil, 1.0f - Lf[COMPACT_FRAC][slot]);
+        const ff pathinf = wff::sub(wfs_soil, soilinf);
         const float cap_soil = kv0 * kvf[0] * fred, cap_comp = Lf[CAP_COMP][slot] * fred;
-        const float soilinf_f = (float)soilinf_d, pathinf_f = (float)pathinf_d;
-        const double mis_d = cap_soil < soilinf_f ? (double)cap_soil : soilinf_d;
-        const double mip_d = cap_comp < pathinf_f ? (double)cap_comp : pathinf_d;
-        const double infex_d = (soilinf_d - mis_d) + (pathinf_d - mip_d);
+        const ff mis = cap_soil < soilinf.hi ? wff::from_f(cap_soil) : soilinf;
+        const ff mip = cap_comp < pathinf.hi ? wff::from_f(cap_comp) : pathinf;
+        const ff infex = wff::add(wff::sub(soilinf, mis), wff::sub(pathinf, mip));
         const float capmax = fmaxf(0.0f, ucap * inv_dtf);
-        const float infil_f = fminf(__double2float_rz(mis_d + mip_d), capmax);
+        const ff infil_sum = wff::add(mis, mip);
+        const ff infil = infil_sum.hi > capmax ? wff::from_f(capmax) : infil_sum;
         // unsaturated zone flow (soil_process.jl:51-92): FP32 rates, exact transfers
-        double transfer_d = 0.0;
+        ff transfer = {0.0f, 0.0f};
         if (g.nu > 0) {
-            float z = 0.0f, flow_f = infil_f;
-            double flow_amt = 0.0;
-            bool amt = false;
+            float z = 0.0f;
+            ff flow = infil;  // inflow of the layer as a rate
 #pragma unroll
             for (int k = 0; k < MAXN; ++k) {
                 if (k >= g.nu) continue;
                 z += g.thick[k];
                 const float l_sat = g.thick[k] * te;
                 const float kv_z = WF_KV_AT(z, k + 1);
-                if (amt) us[k].add_d(flow_amt);
-                else us[k].add_prod(flow_f, dtf);
+                us[k].add(wff::mul(flow, dtf));
                 const float u = us[k].val();
                 if (u <= 0.0f) {
                     us[k].zero();
-                    flow_f = 0.0f;
-                    amt = false;
+                    flow = {0.0f, 0.0f};
                     continue;
                 }
                 bool drained;
                 const float rate = unsat_rate(u, kv_z, l_sat, cexp[k], dtf, drained);
                 if (drained || u - rate * dtf < 0.0f) {
-                    flow_amt = us[k].take_all();
-                    amt = true;
+                    flow = wff::mul(us[k].take_all(), inv_dt);
                 } else {
                     us[k].add_prod(-rate, dtf);
-                    flow_f = rate;
-                    amt = false;
+                    flow = wff::from_f(rate);
                 }
             }
-            transfer_d = amt ? flow_amt * inv_dt : (double)flow_f;
+            transfer = flow;
         }
         // soil evaporation (soil.jl soil_evaporation!)
-        double se_d;
+        ff soilevap;
         float se_f, esat_f = 0.0f;
         {
             float se = 0.0f;
             const float u0 = us[0].val();
             if (g.nu == 1) se = pot_soilevap * fminf(1.0f, u0 / (zif * te));
             else if (g.nu > 1) se = pot_soilevap * fminf(1.0f, u0 / (g.thick[0] * te));
+            ff se_ff;
             if (se > 0.0f && se * dtf >= u0) {
-                se_d = us[0].take_all() * inv_dt;
-                se_f = (float)se_d;
+                se_ff = wff::mul(us[0].take_all(), inv_dt);
+                se_f = wff::to_f(se_ff);
             } else {
                 se_f = se;
-                se_d = (double)se;
+                se_ff = wff::from_f(se);
                 us[0].add_prod(-se, dtf);
             }
             const float pot = pot_soilevap - se_f;
@@ -553,9 +601,10 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
                 esat_f = fminf(pot * fminf(1.0f, (a0 - zif) / a0), (a0 - zif) * fmaxf(ts - tfc, 0.02f) * inv_dtf);
             }
             drain -= esat_f * dtf;
+            soilevap = wff::add(se_ff, esat_f);
         }
         // transpiration (soil.jl transpiration!): FP32 heads, Feddes reduction and root water uptake
-        double actevap_d = 0.0;
+        ff actevap = {0.0f, 0.0f};
         float actevap_f = 0.0f, act_sat_f;
         {
             const float rd = Lf[ROOTING_DEPTH][slot];
@@ -588,13 +637,13 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
                 const float want = alpha * rs_ * pot_trans;
                 const float avail = uk * availcap * inv_dtf;
                 if (want > 0.0f && want >= avail && availcap >= 1.0f) {
-                    const double a = us[k - 1].take_all() * inv_dt;
-                    actevap_d += a;
-                    actevap_f += (float)a;
+                    const ff a = wff::mul(us[k - 1].take_all(), inv_dt);
+                    actevap = wff::add(actevap, a);
+                    actevap_f += wff::to_f(a);
                 } else {
                     const float a = fminf(want, avail);
                     us[k - 1].add_prod(-a, dtf);
-                    actevap_d += (double)a;
+                    actevap = wff::add(actevap, a);
                     actevap_f += a;
                 }
             }
@@ -613,16 +662,16 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             us[k - 1].add(-excess);
             if (k > 1) us[k - 2].add(excess);
         }
-        const double act_infilt_d = (double)infil_f - (double)excess * inv_dt;
-        const double satex_d = (wfs_soil_d - act_infilt_d) - infex_d;
+        const ff act_infilt = wff::sub(infil, wff::mul(inv_dt, excess));
+        const ff satex = wff::sub(wff::sub(wfs_soil, act_infilt), infex);
         usd = 0.0f;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k)
             if (k < g.nl) usd += us[k].val();
-        ucap = Lf[SWC][slot] - (float)sat - usd;
+        ucap = Lf[SWC][slot] - satf - usd;
         // capillary rise (soil.jl capillary_flux!)
         Store capacc;
-        capacc.zero();
+        capacc.init({0.0f, 0.0f});
         if (g.nu > 0) {
             const float ksat = WF_KV_AT(zif, g.nu);
             const float maxcap = fmaxf(0.0f, fminf(fminf(fminf(ksat, actevap_f), ucap * inv_dtf), drain * inv_dtf));
@@ -639,57 +688,60 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
                 capacc.add(toadd);
             }
         }
-        const double capflux_d = (double)capacc.hi + (double)capacc.lo;
+        const ff capflux = wff::fast_two_sum(capacc.hi, capacc.lo);
         const float deepksat = WF_KV_AT(df, g.nl);
+#undef WF_KV_AT
         const float leak_f = fmaxf(0.0f, fminf(Lf[MAX_LEAKAGE][slot], fminf(drain * inv_dtf, deepksat)));
-        const double leak_d = (double)leak_f;
-        const double recharge = transfer_d - capflux_d - leak_d - (double)act_sat_f - (double)esat_f;
-        const double soilevap_d = se_d + (double)esat_f;
-        const double transpiration_d = actevap_d + (double)act_sat_f;
-        const double aet = soilevap_d + transpiration_d + ae_river_d + ae_land_d + ic_d;
+        const ff recharge = wff::sub(wff::sub(wff::sub(wff::sub(transfer, capflux), leak_f), act_sat_f), esat_f);
+        const ff transpiration = wff::add(actevap, act_sat_f);
+        const ff aet = wff::add(wff::add(wff::add(wff::add(soilevap, transpiration), ae_river_f), ae_land_f), ic);
         // ---- write back
-        if (!F.gash) Mf[CANOPY][e] = canopy.value();
+        if (!F.gash && canopy.changed()) stm(F, CANOPY, e, canopy.value());
         if (F.snow) {
-            Mf[SNOW][e] = snow.value();
-            Mf[SNOW_WATER][e] = sw.value();
+            stm(F, SNOW, e, snow.value());
+            stm(F, SNOW_WATER, e, sw.value());
             Mh[SWE][e] = swe_out;
         }
         Mh[TSOIL][e] = tsoil;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k)
-            if (k < g.N && us[k].changed()) F.LY[LY_USLD][k][e] = us[k].value();
-        Mf[ZI][e] = zi;
-        Mf[SSF_ZI][e] = zi;
-        Mf[RECHARGE][e] = recharge;
-        Mf[NET_RUNOFF_RIVER][e] = runoff_river_d - ae_river_d;
-        Mf[AET][e] = aet;
-        Mf[LEAKAGE][e] = leak_d;
-        Mf[SATEX][e] = satex_d;
-        Mf[INFEX][e] = infex_d;
-        Mf[RUNOFF_LAND][e] = runoff_land_d;
-        Mf[AE_LAND][e] = ae_land_d;
+            if (k < g.N && us[k].changed()) {
+                const ff v = us[k].value();
+                F.LYf[LY_USLD][k][e] = v.hi;
+                F.LYl[k][e] = v.lo;
+            }
+        F.Mf[ZI][e] = zi;
+        F.Mf[SSF_ZI][e] = zi;
+        stm(F, RECHARGE, e, recharge);
+        stm(F, NET_RUNOFF_RIVER, e, wff::sub(runoff_river, ae_river_f));
+        stm(F, AET, e, aet);
+        stm(F, LEAKAGE, e, wff::from_f(leak_f));
+        stm(F, SATEX, e, satex);
+        stm(F, INFEX, e, infex);
+        stm(F, RUNOFF_LAND, e, runoff_land);
+        stm(F, AE_LAND, e, wff::from_f(ae_land_f));
         Mh[INTERCEPTION][e] = icf;
-        Mh[TRANSPIRATION][e] = actevap_f + act_sat_f;
-        Mh[SOIL_EVAP][e] = se_f + esat_f;
-        Mh[ACT_INFILT][e] = infil_f - excess * inv_dtf;
+        Mh[TRANSPIRATION][e] = wff::to_f(transpiration);
+        Mh[SOIL_EVAP][e] = wff::to_f(soilevap);
+        Mh[ACT_INFILT][e] = wff::to_f(act_infilt);
         // storages at the start of the routing (overland and river balances)
         if (F.mass_balance) {
-            Mf[BO_PREV][e] = Mf[OL_STORAGE][e];
-            if (rs >= 0) F.RM[BR_PREV][rs * M + m] = F.RM[RV_STORAGE][rs * M + m];
+            stm(F, BO_PREV, e, ldm(F, OL_STORAGE, e));
+            if (rs >= 0) str(F, BR_PREV, rs * M + m, ldr(F, RV_STORAGE, rs * M + m));
         }
-        // terms of the subsurface solve that do not depend on the upstream discharge: the FP64
-        // recharge flux for the exact bookkeeping, FP32 inputs of the walker
+        // terms of the subsurface solve that do not depend on the upstream discharge: the
+        // double-FP32 recharge flux for the exact bookkeeping, FP32 inputs of the walker
         if (F.ssf_single) {
-            double flux = recharge * F.L[AREA][slot];  // recharge flux of the subsurface model
-            if (zi >= d_soil) flux = fmax(0.0, flux);
-            Mf[SSF_QNET][e] = flux;
-            Mh[SSF_QNETF][e] = (float)flux;
+            ff flux = wff::mul(recharge, lds(F, AREA, slot));  // recharge flux of the subsurface model
+            if (zi >= d_soil) flux = wff::fmax0(flux);
+            stm(F, SSF_QNET, e, flux);
+            Mh[SSF_QNETF][e] = wff::to_f(flux);
             Mh[SSF_ZIF][e] = zif;
             float z = zif;
             if (kv_const && !(z < zexp)) z = zexp;
             const float cel = Lf[KH_RATIO][slot] * kv0 * expf(-fsc * z) * Lf[SLOPE][slot] / Lf[SY][slot];
             const float cinv = 1.0f / cel;
-            Mh[SSF_T2][e] = (float)Mf[SSF_Q][e] * cinv;
+            Mh[SSF_T2][e] = wff::to_f(ldm(F, SSF_Q, e)) * cinv;
             Mh[SSF_RDF][e] = 1.0f / (Lf[SSF_DTDX][slot] + cinv);
             // deepest unsaturated layer: what a rising water table fills first
             float rth = 0.0f, rcap = 0.0f, rrho = 0.0f;
@@ -730,6 +782,21 @@ __device__ __forceinline__ double kw_ssf_newton_s(double q, double cterm, double
     return q;
 }
 
+// q of upstream entry o (sub-stepped subsurface flow): the heavy child from the double-FP32
+// discharge field, a light child from the published chain ends.
+__device__ __forceinline__ bool upstream_q_ff(const WfDevGraph& g, const WfSweep& sw, FFRow q, int32_t o, int m, int s,
+                                              uint32_t ep, int32_t* status, double& out) {
+    const int32_t uc = g.up_chain[o];
+    if (uc < 0) {
+        out = (double)q[g.up_slot[o] * g.M + m];
+        return true;
+    }
+    const int64_t fe = (int64_t)uc * g.M + m;
+    if (!wfw::wait_epoch(&g.flags[fe], ep + sw.wait_offset, sw, status)) return false;
+    out = __ldcg(&g.end_q[fe * g.s_cap + s]);
+    return true;
+}
+
 template <int MAXN>
 struct SsfSplitPhys {
     WfDevFields F;
@@ -737,7 +804,7 @@ struct SsfSplitPhys {
     WfSweep sw;
 
     __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
-        double* const* Mf = F.Mf;
+        const FFMem Mf{F};
         double* const* L = F.L;
         const double dt_s = sw.dts[s];
         const double area = L[AREA][slot];
@@ -749,7 +816,7 @@ struct SsfSplitPhys {
         double qin = 0.0, tr = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             double qu;
-            if (!wfw::upstream_q(g, sw, Mf[SSF_Q], o, m, s, ep, F.status, qu)) return false;
+            if (!upstream_q_ff(g, sw, Mf[SSF_Q], o, m, s, ep, F.status, qu)) return false;
             const double fr = L[FRAC_TO_RIVER][g.up_slot[o]];
             qin += qu * (1.0 - fr);
             tr += qu * fr;
@@ -759,7 +826,7 @@ struct SsfSplitPhys {
         col.kv0 = F.Mh[KV0][e];
         col.f = F.Mh[FSCALE][e];
 #pragma unroll
-        for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? F.LY[LY_USLD][k][e] : 0.0;
+        for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? FFUsld{F}[k][e] : 0.0;
         const double zi_soil = Mf[ZI][e];
         col.set_thickness(zi_soil);
         const double q_prev = Mf[SSF_Q][e];
@@ -838,7 +905,7 @@ struct SsfSplitPhys {
         if (!early) {
 #pragma unroll
             for (int k = 0; k < MAXN; ++k)
-                if (k < col.N) F.LY[LY_USLD][k][e] = col.usld[k];
+                if (k < col.N) FFUsld{F}[k][e] = col.usld[k];
             Mf[ZI][e] = zi_new;
         }
         if (is_end) wfw::publish(g, chain, m, s, ep, q);
@@ -861,7 +928,7 @@ struct SsfSplitPhys {
         Mf[SSF_TR_AVG][e] = c_tr / dt;
         if (early) {
 #pragma unroll
-            for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? F.LY[LY_USLD][k][e] : 0.0;
+            for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? FFUsld{F}[k][e] : 0.0;
             col.set_thickness(zi_soil);
         }
         const double zi_s = early ? zi_soil : zi_new;
@@ -882,9 +949,6 @@ struct SsfSplitPhys {
         Mf[OL_INWATER][e] = inwater;
         const double qlat = inwater / L[FLOW_LENGTH][slot];
         Mf[OL_QLAT][e] = qlat;
-        const wff::ff qlf = wff::from_d(qlat);
-        F.Mh[OL_QLATH][e] = qlf.hi;
-        F.Mh[OL_QLATL][e] = qlf.lo;
         return true;
     }
 };
@@ -955,7 +1019,7 @@ __device__ __forceinline__ double u_of_q(double q) {
 template <int MAXN>
 __device__ __noinline__ void ssf_full_split(const WfDevFields& F, int64_t slot, int64_t e, double qin, double q_net, double dt_s,
                                double& q_out, double& zi_out, double& exf_out, double& nf_out) {
-    double* const* Mf = F.Mf;
+    const FFMem Mf{F};
     double* const* L = F.L;
     const double d = L[SOIL_THICKNESS][slot];
     const double zi_ssf = Mf[SSF_ZI][e];
@@ -964,7 +1028,7 @@ __device__ __noinline__ void ssf_full_split(const WfDevFields& F, int64_t slot, 
     col.kv0 = F.Mh[KV0][e];
     col.f = F.Mh[FSCALE][e];
 #pragma unroll
-    for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? F.LY[LY_USLD][k][e] : 0.0;
+    for (int k = 0; k < MAXN; ++k) col.usld[k] = k < col.N ? FFUsld{F}[k][e] : 0.0;
     col.set_thickness(Mf[ZI][e]);
     const double q_prev = Mf[SSF_Q][e];
     const double sy = L[SY][slot], dx = L[FLOW_LENGTH][slot], dw = L[FLOW_WIDTH][slot];
@@ -1015,7 +1079,7 @@ __device__ __noinline__ void ssf_full_split(const WfDevFields& F, int64_t slot, 
     }
 #pragma unroll
     for (int k = 0; k < MAXN; ++k)
-        if (k < col.N) F.LY[LY_USLD][k][e] = col.usld[k];
+        if (k < col.N) FFUsld{F}[k][e] = col.usld[k];
     Mf[ZI][e] = zi;
     q_out = q;
     zi_out = zi;
@@ -1059,7 +1123,7 @@ struct SsfWave {
         x.idwdx = Lf[SSF_IDWDX][slot];
         x.dtsy = Lf[SSF_DTSY][slot];
         x.k2 = Lf[SSF_K2][slot];
-        x.qprev_zero = (__double_as_longlong(F.Mf[SSF_Q][e]) << 1) == 0;
+        x.qprev_zero = F.Mh[SSF_Q][e] == 0.0f;
         wfv::load_up(g, sw, slot, m, x.up);
     }
     __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
@@ -1103,8 +1167,8 @@ struct SsfWave {
             if (full) {
                 double qd, zid, exfd, nfd;
                 const double qind = (double)qin;
-                ssf_full_split<MAXN>(F, slot, e, qind, F.Mf[SSF_QNET][e], sw.dts[0], qd, zid, exfd, nfd);
-                double* const* Mf = F.Mf;
+                const FFMem Mf{F};
+                ssf_full_split<MAXN>(F, slot, e, qind, (double)Mf[SSF_QNET][e], sw.dts[0], qd, zid, exfd, nfd);
                 Mf[SSF_Q][e] = qd;
                 Mf[SSF_ZI][e] = zid;
                 Mf[SSF_TEXF][e] = exfd;
@@ -1141,8 +1205,8 @@ struct OlWave {
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
         float* const* Mh = F.Mh;
         x.u = {Mh[OL_UH][e], Mh[OL_UL][e]};
-        x.q = {Mh[OL_QH][e], Mh[OL_QL][e]};
-        x.qlat = {Mh[OL_QLATH][e], Mh[OL_QLATL][e]};
+        x.q = ldm(F, OL_Q, e);
+        x.qlat = ldm(F, OL_QLAT, e);
         x.invdx = {F.Lf[INV_FLOW_LENGTH][slot], F.Lf[INV_DX_LO][slot]};
         x.alpha = F.Lf[OL_ALPHA][slot];
         x.sfw_pos = F.Lf[SFW][slot] > 0.0f;
@@ -1177,8 +1241,7 @@ struct OlWave {
         float* const* Mh = F.Mh;
         Mh[OL_UH][e] = u.hi;
         Mh[OL_UL][e] = u.lo;
-        Mh[OL_QH][e] = qp.hi;
-        Mh[OL_QL][e] = qp.lo;
+        stm(F, OL_Q, e, qp);
         if (sw.first != 0) qsum = wff::add(qsum, wff::ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]});
         Mh[OL_QSUMH][e] = qsum.hi;
         Mh[OL_QSUML][e] = qsum.lo;
@@ -1201,7 +1264,7 @@ struct RvWave {
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
         float* const* RMh = F.RMh;
         x.u = {RMh[RV_UH][e], RMh[RV_UL][e]};
-        x.q = {RMh[RV_QH][e], RMh[RV_QL][e]};
+        x.q = ldr(F, RV_Q, e);
         x.qlatt = {RMh[RV_QLATTH][e], RMh[RV_QLATTL][e]};
         x.invlen = {F.Rf[R_INV_LENGTH][slot], F.Rf[R_INV_LEN_LO][slot]};
         x.alpha = F.Rf[R_ALPHA][slot];
@@ -1244,8 +1307,7 @@ struct RvWave {
         float* const* RMh = F.RMh;
         RMh[RV_UH][e] = u.hi;
         RMh[RV_UL][e] = u.lo;
-        RMh[RV_QH][e] = qp.hi;
-        RMh[RV_QL][e] = qp.lo;
+        str(F, RV_Q, e, qp);
         if (sw.first != 0) {
             qsum = wff::add(qsum, wff::ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]});
             asum = wff::add(asum, wff::ff{RMh[RV_ABSH][e], RMh[RV_ABSL][e]});
@@ -1277,34 +1339,41 @@ cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
 
 // --------------------------------------------------------------- post-sweep kernels ------
 
-// After the subsurface sweep: the exact FP64 bookkeeping of the fast cases (net flux and
+// After the subsurface sweep: the exact bookkeeping of the fast cases (net flux and
 // water-table change from the walker's q, exfiltration), the unsaturated-layer adjustment to
 // the new water table (soil.jl update_ustorelayerdepth!), averages, subsurface storage, the soil
 // water storage update (sbm.jl update_soil_water_storage!) and the overland lateral inflow.
+// Fluxes and the unsaturated stores are double-FP32; the water table and the saturated store
+// are FP64 (large stores, see wf_split_fp64_member).
 template <int MAXN>
 __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph g) {
+    using wff::ff;
     const int M = F.M;
     const int N = F.N;
     const int64_t E = F.land_slots * M;
-    const double r_s = F.dt_ssf * F.inv_dt;  // sub-step / step (1 when they are equal)
+    const float r_s = (float)(F.dt_ssf * F.inv_dt);  // sub-step / step (1 when they are equal)
+    const ff dts = wff::from_f((float)F.dt_ssf);
+    const ff inv_dts = {F.inv_dts_hi, F.inv_dts_lo};
+    const double NANV = __longlong_as_double(0x7ff8000000000000LL);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
-        double* const* Mf = F.Mf;
         float* const* Mh = F.Mh;
         double* const* L = F.L;
         const int flag = (int)Mh[SSF_FLAG][e];
-        const double zi_soil = Mf[ZI][e];
+        const double zi_soil = F.Mf[ZI][e];
         const double d = L[SOIL_THICKNESS][slot];
-        const double te = L[THETA_S][slot] - L[THETA_R][slot];
-        double usld[MAXN], act[MAXN], cum[MAXN + 1];  // cum[k]: depth of the top of layer k
+        const double te_d = L[THETA_S][slot] - L[THETA_R][slot];
+        const ff te = wff::from_d(te_d);
+        ff usld[MAXN];
+        double act[MAXN], cum[MAXN + 1];  // cum[k]: depth of the top of layer k
         cum[0] = 0.0;
 #pragma unroll
         for (int k = 0; k < MAXN; ++k) {
-            usld[k] = k < N ? F.LY[LY_USLD][k][e] : 0.0;
-            act[k] = k < N ? F.LY[LY_ACT_THICK][k][slot] : 0.0;
-            cum[k + 1] = k < N ? F.LY[LY_CUM][k][slot] : __longlong_as_double(0x7ff8000000000000LL);
+            usld[k] = k < N ? ff{F.LYf[LY_USLD][k][e], F.LYl[k][e]} : ff{0.0f, 0.0f};
+            act[k] = k < N ? F.LY[LY_ACT_THICK][k][slot] : NANV;
+            cum[k + 1] = k < N ? F.LY[LY_CUM][k][slot] : NANV;
         }
         // layer k is unsaturated iff the water table lies below its top (utils.jl set_layerthickness)
         auto nu_at = [&](double ref) {
@@ -1315,50 +1384,52 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
             return c;
         };
         auto thick_at = [&](double ref, int k) {
-            return ref > cum[k + 1] ? act[k] : (ref > cum[k] ? ref - cum[k] : __longlong_as_double(0x7ff8000000000000LL));
+            return ref > cum[k + 1] ? act[k] : (ref > cum[k] ? ref - cum[k] : NANV);
         };
-        double q, qin, exf, nf, zi_new, zi_s;
+        ff q, qin, exf, nf;
+        double zi_new, zi_s;
         if (flag == SSF_EARLY) {
-            q = qin = exf = nf = 0.0;
+            q = qin = exf = nf = {0.0f, 0.0f};
             zi_new = d;
             zi_s = zi_soil;
-            Mf[SSF_Q][e] = 0.0;
-            Mf[SSF_ZI][e] = d;
+            stm(F, SSF_Q, e, q);
+            F.Mf[SSF_ZI][e] = d;
         } else if (flag == SSF_FULL) {
-            q = Mf[SSF_Q][e];
-            qin = Mf[SSF_TQIN][e];
-            exf = Mf[SSF_TEXF][e];
-            nf = Mf[SSF_TNF][e];
-            zi_new = zi_s = Mf[SSF_ZI][e];
+            q = ldm(F, SSF_Q, e);
+            qin = ldm(F, SSF_TQIN, e);
+            exf = ldm(F, SSF_TEXF, e);
+            nf = ldm(F, SSF_TNF, e);
+            zi_new = zi_s = F.Mf[SSF_ZI][e];
 #pragma unroll
-            for (int k = 0; k < MAXN; ++k) usld[k] = k < N ? F.LY[LY_USLD][k][e] : 0.0;
+            for (int k = 0; k < MAXN; ++k) usld[k] = k < N ? ff{F.LYf[LY_USLD][k][e], F.LYl[k][e]} : ff{0.0f, 0.0f};
         } else {
-            q = (double)Mh[SSF_QF][e];
-            qin = (double)Mh[SSF_QINF][e];
-            const double qu = (double)Mh[SSF_QUF][e];
-            nf = (qin + Mf[SSF_QNET][e] - qu) * L[SSF_IDWDX][slot];
+            q = wff::from_f(Mh[SSF_QF][e]);
+            qin = wff::from_f(Mh[SSF_QINF][e]);
+            const float qu = Mh[SSF_QUF][e];
+            nf = wff::mul(wff::sub(wff::add(ldm(F, SSF_QNET, e), qin), qu), lds(F, SSF_IDWDX, slot));
             // water_table_change (subsurface_process.jl): falling by net flux / specific yield,
             // rising through the unsaturated layers from the deepest up
-            double dh = 0.0, rem = nf;
-            if (nf <= 0.0) {
-                dh = nf * L[SSF_DTSY][slot];
+            ff dh = {0.0f, 0.0f}, rem = nf;
+            if (nf.hi <= 0.0f) {
+                dh = wff::mul(nf, lds(F, SSF_DTSY, slot));
             } else {
-                const double dts = F.dt_ssf;
                 const int nu0 = nu_at(zi_soil);
 #pragma unroll
                 for (int k = MAXN; k >= 1; --k) {
-                    if (k > nu0 || rem == 0.0) continue;
-                    const double t = thick_at(zi_soil, k - 1);
-                    const double cap = fmax(t * te - usld[k - 1], 0.0) * F.inv_dt_ssf;
-                    const double fl = fmin(rem, cap);
-                    dh += cap <= rem ? t : fl * dts * wfm_rcp(te - usld[k - 1] * wfm_rcp(t));
-                    rem -= fl;
+                    if (k > nu0 || rem.hi == 0.0f) continue;
+                    const ff t = wff::from_d(thick_at(zi_soil, k - 1));
+                    const ff cap = wff::mul(wff::fmax0(wff::sub(wff::mul(t, te), usld[k - 1])), inv_dts);
+                    const ff fl = wff::fmin(rem, cap);
+                    if (wff::le(cap, rem)) dh = wff::add(dh, t);
+                    else dh = wff::add(dh, wff::div(wff::mul(fl, dts), wff::sub(te, wff::div(usld[k - 1], t))));
+                    rem = wff::sub(rem, fl);
                 }
             }
-            exf = fmax(rem, 0.0);
-            double zi = zi_soil - dh;
+            exf = wff::fmax0(rem);
+            double zi = zi_soil - wff::to_d(dh);
             if (flag == SSF_CUT || zi > d) zi = d;
-            zi_new = zi_s = fmin(fmax(zi, 0.0), d);
+            zi = fmax(zi, 0.0);
+            zi_new = zi_s = zi;
             if (zi_new != zi_soil) {
                 const int n_prev = nu_at(zi_soil), n_new = nu_at(zi_new);
                 if (zi_new < zi_soil) {
@@ -1366,8 +1437,10 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
                     for (int k = 1; k <= MAXN; ++k) {
                         if (k < n_new || k > n_prev) continue;
                         const double t = thick_at(zi_new, k - 1);
-                        usld[k - 1] = t != t ? 0.0 : t * wfm_rcp(thick_at(zi_soil, k - 1)) * usld[k - 1];
-                        F.LY[LY_USLD][k - 1][e] = usld[k - 1];
+                        usld[k - 1] = t != t ? ff{0.0f, 0.0f}
+                                             : wff::mul(wff::from_d(t * wfm_rcp(thick_at(zi_soil, k - 1))), usld[k - 1]);
+                        F.LYf[LY_USLD][k - 1][e] = usld[k - 1].hi;
+                        F.LYl[k - 1][e] = usld[k - 1].lo;
                     }
                 } else {
                     const double tfc_tr = L[THETA_FC][slot] - L[THETA_R][slot];
@@ -1376,219 +1449,237 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
                         if (k < n_prev || k > n_new) continue;
                         double tp = thick_at(zi_soil, k - 1);
                         tp = tp != tp ? 0.0 : tp;
-                        usld[k - 1] = usld[k - 1] + (thick_at(zi_new, k - 1) - tp) * tfc_tr;
-                        F.LY[LY_USLD][k - 1][e] = usld[k - 1];
+                        usld[k - 1] = wff::add(usld[k - 1], wff::from_d((thick_at(zi_new, k - 1) - tp) * tfc_tr));
+                        F.LYf[LY_USLD][k - 1][e] = usld[k - 1].hi;
+                        F.LYl[k - 1][e] = usld[k - 1].lo;
                     }
                 }
-                Mf[ZI][e] = zi_new;
+                F.Mf[ZI][e] = zi_new;
             }
-            Mf[SSF_Q][e] = q;
-            Mf[SSF_ZI][e] = zi_new;
+            stm(F, SSF_Q, e, q);
+            F.Mf[SSF_ZI][e] = zi_new;
         }
         const int nu = nu_at(zi_s);
-        double tr = 0.0;
+        ff tr = {0.0f, 0.0f};
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o)
-            tr += (double)Mh[SSF_QF][g.up_slot[o] * M + m] * g.up_fr[o];
-        const double area = L[AREA][slot];
-        const double flux = Mf[SSF_QNET][e];
-        Mf[SSF_STORAGE][e] = L[SY][slot] * (d - zi_new) * area;
-        const double exf_avg = exf * r_s;
-        Mf[RCH_FLUX_AVG][e] = flux * r_s;
-        Mf[SSF_QIN_AVG][e] = qin * r_s;
-        Mf[SSF_Q_AVG][e] = q * r_s;
-        Mf[SSF_QNET_AVG][e] = nf * area * r_s;
-        Mf[SSF_EXF_AVG][e] = exf_avg;
-        Mf[SSF_TR_AVG][e] = tr * r_s;
-        double usd = 0.0;
+            tr = wff::add(tr, wff::two_prod(Mh[SSF_QF][g.up_slot[o] * M + m], g.up_frf[o]));
+        const ff area = lds(F, AREA, slot);
+        const ff flux = ldm(F, SSF_QNET, e);
+        stm(F, SSF_STORAGE, e, wff::mul(wff::from_d(L[SY][slot] * (d - zi_new)), area));
+        const ff exf_avg = wff::mul(exf, r_s);
+        stm(F, RCH_FLUX_AVG, e, wff::mul(flux, r_s));
+        stm(F, SSF_QIN_AVG, e, wff::mul(qin, r_s));
+        stm(F, SSF_Q_AVG, e, wff::mul(q, r_s));
+        stm(F, SSF_QNET_AVG, e, wff::mul(wff::mul(nf, area), r_s));
+        stm(F, SSF_EXF_AVG, e, exf_avg);
+        stm(F, SSF_TR_AVG, e, wff::mul(tr, r_s));
+        ff usd = {0.0f, 0.0f};
 #pragma unroll
         for (int k = 0; k < MAXN; ++k)
-            if (k < nu) usd += usld[k];
-        const double runoff = fmax(0.0, exf_avg + Mf[SATEX][e] + Mf[RUNOFF_LAND][e] + Mf[INFEX][e]);
-        const double sat = (d - zi_s) * te;
-        Mf[SAT][e] = sat;
-        Mf[USTOREDEPTH][e] = usd;
-        Mf[TSWS][e] = sat + usd;
-        Mf[EXFILT][e] = exf_avg;
-        Mf[RUNOFF][e] = runoff;
-        const double net_runoff = runoff - Mf[AE_LAND][e];
-        Mf[NET_RUNOFF][e] = net_runoff;
-        const double inwater = net_runoff * area;
-        Mf[OL_INWATER][e] = inwater;
-        const double qlat = inwater * L[INV_FLOW_LENGTH][slot];
-        Mf[OL_QLAT][e] = qlat;
-        const wff::ff qlf = wff::from_d(qlat);
-        Mh[OL_QLATH][e] = qlf.hi;
-        Mh[OL_QLATL][e] = qlf.lo;
+            if (k < nu) usd = wff::add(usd, usld[k]);
+        const ff runoff = wff::fmax0(
+            wff::add(wff::add(wff::add(exf_avg, ldm(F, SATEX, e)), ldm(F, RUNOFF_LAND, e)), ldm(F, INFEX, e)));
+        const double sat = (d - zi_s) * te_d;
+        F.Mf[SAT][e] = sat;
+        stm(F, USTOREDEPTH, e, usd);
+        F.Mf[TSWS][e] = sat + wff::to_d(usd);
+        stm(F, EXFILT, e, exf_avg);
+        stm(F, RUNOFF, e, runoff);
+        const ff net_runoff = wff::sub(runoff, ldm(F, AE_LAND, e));
+        stm(F, NET_RUNOFF, e, net_runoff);
+        const ff inwater = wff::mul(net_runoff, area);
+        stm(F, OL_INWATER, e, inwater);
+        stm(F, OL_QLAT, e, wff::mul(inwater, lds(F, INV_FLOW_LENGTH, slot)));
     }
 }
 
-// After the overland sweep: discharge, water depth and storage in FP64 from the double-FP32
-// state, averages, and the lateral inflow of the river cell of each land cell
-// (routing/river_kinwave.jl update_lateral_inflow!).
+// After the overland sweep: water depth and storage from the double-FP32 state, averages, and
+// the lateral inflow of the river cell of each land cell (routing/river_kinwave.jl
+// update_lateral_inflow!).
 __global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph g) {
+    using wff::ff;
     const int M = F.M;
     const int64_t E = F.land_slots * M;
-    const double inv_dt = F.inv_dt;
+    const ff inv_dt = {F.inv_dt_hi, F.inv_dt_lo};
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
-        double* const* Mf = F.Mf;
         float* const* Mh = F.Mh;
-        double* const* L = F.L;
-        Mf[OL_Q][e] = wff::to_d({Mh[OL_QH][e], Mh[OL_QL][e]});
-        const double inv_sfw = L[INV_SFW][slot];
-        if (inv_sfw > 0.0) {
-            const double u = wff::to_d({Mh[OL_UH][e], Mh[OL_UL][e]});
-            const double a = (double)F.Lf[OL_ALPHA][slot] * (u * u * u);
-            Mf[OL_H][e] = a * inv_sfw;
-            Mf[OL_STORAGE][e] = L[FLOW_LENGTH][slot] * a;
+        const ff inv_sfw = lds(F, INV_SFW, slot);
+        if (inv_sfw.hi > 0.0f) {
+            const ff u = {Mh[OL_UH][e], Mh[OL_UL][e]};
+            const ff a = wff::mul(wff::mul(wff::mul(u, u), u), F.Lf[OL_ALPHA][slot]);
+            stm(F, OL_H, e, wff::mul(a, inv_sfw));
+            stm(F, OL_STORAGE, e, wff::mul(a, lds(F, FLOW_LENGTH, slot)));
         }
-        double qin = 0.0, tr = 0.0;
+        ff qin = {0.0f, 0.0f}, tr = {0.0f, 0.0f};
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             const int64_t ue = g.up_slot[o] * M + m;
-            const double qs = wff::to_d({Mh[OL_QSUMH][ue], Mh[OL_QSUML][ue]});
-            qin += qs * (double)g.up_wf[o];
-            tr += qs * g.up_fr[o];
+            const ff qs = {Mh[OL_QSUMH][ue], Mh[OL_QSUML][ue]};
+            qin = wff::add(qin, wff::mul(qs, g.up_wf[o]));
+            tr = wff::add(tr, wff::mul(qs, g.up_frf[o]));
         }
-        if (!(inv_sfw > 0.0)) qin = 0.0;
-        Mf[OL_Q_AVG][e] = wff::to_d({Mh[OL_QSUMH][e], Mh[OL_QSUML][e]}) * inv_dt;
-        const double tr_avg = tr * inv_dt;
-        Mf[OL_TR_AVG][e] = tr_avg;
-        Mf[OL_QIN_AVG][e] = qin * inv_dt;
+        if (!(inv_sfw.hi > 0.0f)) qin = {0.0f, 0.0f};
+        stm(F, OL_Q_AVG, e, wff::mul(ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]}, inv_dt));
+        const ff tr_avg = wff::mul(tr, inv_dt);
+        stm(F, OL_TR_AVG, e, tr_avg);
+        stm(F, OL_QIN_AVG, e, wff::mul(qin, inv_dt));
         const int64_t rs = F.land_river_slot[slot];
         if (rs >= 0) {
             const int64_t re = rs * M + m;
-            const double inv_len = F.R[R_INV_LENGTH][rs];
-            const double inw = Mf[SSF_TR_AVG][e] + tr_avg + Mf[NET_RUNOFF_RIVER][e] * F.R[R_AREA][rs];
-            F.RM[RV_INWATER][re] = inw;
-            const double qlat = inw * inv_len;
-            F.RM[RV_QLAT][re] = qlat;
-            const double ext = F.R[R_EXT_INFLOW][rs];
-            const wff::ff qlt = wff::from_d(ext < 0.0 ? qlat : qlat + ext * inv_len);
+            const ff inv_len = ldrs(F, R_INV_LENGTH, rs);
+            const ff inw = wff::add(wff::add(ldm(F, SSF_TR_AVG, e), tr_avg),
+                                    wff::mul(ldm(F, NET_RUNOFF_RIVER, e), ldrs(F, R_AREA, rs)));
+            str(F, RV_INWATER, re, inw);
+            const ff qlat = wff::mul(inw, inv_len);
+            str(F, RV_QLAT, re, qlat);
+            const float ext = F.Rf[R_EXT_INFLOW][rs];
+            const ff qlt = ext < 0.0f ? qlat : wff::add(qlat, wff::mul(inv_len, ext));
             F.RMh[RV_QLATTH][re] = qlt.hi;
             F.RMh[RV_QLATTL][re] = qlt.lo;
         }
     }
 }
 
-// After the river sweep: discharge, water depth, storage and averages in FP64.
+// After the river sweep: water depth, storage and averages.
 __global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph g) {
+    using wff::ff;
     const int M = F.M;
     const int64_t E = F.river_slots * M;
-    const double inv_dt = F.inv_dt;
+    const ff inv_dt = {F.inv_dt_hi, F.inv_dt_lo};
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.river_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
-        double* const* RM = F.RM;
         float* const* RMh = F.RMh;
-        double* const* R = F.R;
-        RM[RV_Q][e] = wff::to_d({RMh[RV_QH][e], RMh[RV_QL][e]});
-        const double u = wff::to_d({RMh[RV_UH][e], RMh[RV_UL][e]});
-        const double a = (double)F.Rf[R_ALPHA][slot] * (u * u * u);
-        RM[RV_H][e] = a * R[R_INV_WIDTH][slot];
-        RM[RV_STORAGE][e] = R[R_LENGTH][slot] * a;
-        double qin = 0.0;
+        const ff u = {RMh[RV_UH][e], RMh[RV_UL][e]};
+        const ff a = wff::mul(wff::mul(wff::mul(u, u), u), F.Rf[R_ALPHA][slot]);
+        str(F, RV_H, e, wff::mul(a, ldrs(F, R_INV_WIDTH, slot)));
+        str(F, RV_STORAGE, e, wff::mul(a, ldrs(F, R_LENGTH, slot)));
+        ff qin = {0.0f, 0.0f};
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             const int64_t ue = g.up_slot[o] * M + m;
-            qin += wff::to_d({RMh[RV_QSUMH][ue], RMh[RV_QSUML][ue]});
+            qin = wff::add(qin, ff{RMh[RV_QSUMH][ue], RMh[RV_QSUML][ue]});
         }
-        RM[RV_Q_AVG][e] = wff::to_d({RMh[RV_QSUMH][e], RMh[RV_QSUML][e]}) * inv_dt;
-        RM[RV_QIN_AVG][e] = qin * inv_dt;
-        RM[RV_ABS_AVG][e] = wff::to_d({RMh[RV_ABSH][e], RMh[RV_ABSL][e]}) * inv_dt;
+        str(F, RV_Q_AVG, e, wff::mul(ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]}, inv_dt));
+        str(F, RV_QIN_AVG, e, wff::mul(qin, inv_dt));
+        str(F, RV_ABS_AVG, e, wff::mul(ff{RMh[RV_ABSH][e], RMh[RV_ABSL][e]}, inv_dt));
     }
 }
 
 // Water balance of the split form (mass_balance.jl:215-253 land, :382-399 overland,
-// :470-490 subsurface, :290-313 river) and update_total_water_storage! (sbm.jl:143-182):
-// the error terms are FP64 differences of the FP64 totals, the relative errors are FP32
-// quotients, and every division by dt or area is a multiplication by a static reciprocal.
-__device__ __forceinline__ void mb_error_s(double tin, double tout, double rate, double& err, double& rel) {
-    err = tin - tout - rate;
-    const float avg = (float)((tin + tout) * 0.5);
-    rel = avg == 0.0f ? 0.0 : (double)((float)err / avg);
+// :470-490 subsurface, :290-313 river) and update_total_water_storage! (sbm.jl:143-182), in
+// double-FP32; relative errors are FP32 quotients.
+__device__ __forceinline__ void mb_error_ff(wff::ff tin, wff::ff tout, wff::ff rate, wff::ff& err, wff::ff& rel) {
+    err = wff::sub(wff::sub(tin, tout), rate);
+    const float avg = (wff::to_f(tin) + wff::to_f(tout)) * 0.5f;
+    rel = {avg == 0.0f ? 0.0f : __fdividef(wff::to_f(err), avg), 0.0f};
 }
 
 __global__ void __launch_bounds__(256) balance_split_kernel(WfDevFields F) {
+    using wff::ff;
     const int M = F.M;
     const int64_t EL = F.land_slots * M, ER = F.river_slots * M;
-    const double inv_dt = F.inv_dt;
-    double* const* Mf = F.Mf;
-    double* const* L = F.L;
+    const ff inv_dt = {F.inv_dt_hi, F.inv_dt_lo};
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < EL + ER; e += (int64_t)gridDim.x * blockDim.x) {
+        ff err, rel;
         if (e >= EL) {
             if (!F.mass_balance) continue;
             const int64_t re = e - EL;
             const int64_t rs = re / M;
             if (F.river_node_of_slot[rs] < 0) continue;
-            double* const* RM = F.RM;
-            const double tin = RM[RV_INWATER][re] + RM[RV_QIN_AVG][re] + fmax(0.0, F.R[R_EXT_INFLOW][rs]);
-            const double tout = RM[RV_Q_AVG][re] + RM[RV_ABS_AVG][re];
-            double err, rel;
-            mb_error_s(tin, tout, (RM[RV_STORAGE][re] - RM[BR_PREV][re]) * inv_dt, err, rel);
-            RM[BR_ERR][re] = err;
-            RM[BR_REL][re] = rel;
+            const ff tin = wff::add(wff::add(ldr(F, RV_INWATER, re), ldr(F, RV_QIN_AVG, re)),
+                                    wff::fmax0(ldrs(F, R_EXT_INFLOW, rs)));
+            const ff tout = wff::add(ldr(F, RV_Q_AVG, re), ldr(F, RV_ABS_AVG, re));
+            mb_error_ff(tin, tout, wff::mul(wff::sub(ldr(F, RV_STORAGE, re), ldr(F, BR_PREV, re)), inv_dt), err, rel);
+            str(F, BR_ERR, re, err);
+            str(F, BR_REL, re, rel);
             continue;
         }
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
         const int64_t rs = F.land_river_slot[slot];
-        const double inv_area = L[INV_AREA][slot];
-        double ts = 0.0;
-        if (rs >= 0) ts = F.RM[RV_H][rs * M + m] * F.R[R_WIDTH][rs] * F.R[R_LENGTH][rs] * inv_area;
-        const double snow = Mf[SNOW][e], sw = Mf[SNOW_WATER][e], canopy = Mf[CANOPY][e];
-        const double tsws = Mf[TSWS][e];
-        ts += snow + sw + canopy + tsws + Mf[OL_H][e] * (1.0 - L[RIVER_FRACTION][slot]);
-        Mf[TOTAL_STORAGE][e] = ts;
+        const ff inv_area = lds(F, INV_AREA, slot);
+        const ff snow = ldm(F, SNOW, e), sw = ldm(F, SNOW_WATER, e), canopy = ldm(F, CANOPY, e);
+        const double tsws = F.Mf[TSWS][e];
+        ff ts = wff::add(wff::add(wff::add(snow, sw), canopy), wff::from_d(tsws));
+        ts = wff::add(ts, wff::mul(ldm(F, OL_H, e), 1.0f - F.Lf[RIVER_FRACTION][slot]));
+        if (rs >= 0)
+            ts = wff::add(ts, wff::mul(wff::mul(wff::mul(ldr(F, RV_H, rs * M + m), ldrs(F, R_WIDTH, rs)),
+                                                ldrs(F, R_LENGTH, rs)),
+                                       inv_area));
+        stm(F, TOTAL_STORAGE, e, ts);
         if (!F.mass_balance) continue;
-        double err, rel;
         {
-            const double tin = Mf[SSF_QIN_AVG][e] * inv_area + (double)F.Mh[PRECIP][e];
-            const double vout = Mf[NET_RUNOFF][e] + Mf[AET][e] + Mf[NET_RUNOFF_RIVER][e] + Mf[LEAKAGE][e];
-            const double tout = Mf[SSF_Q_AVG][e] * inv_area + vout;
-            const double storage = tsws + canopy + (snow + sw);
-            mb_error_s(tin, tout, (storage - Mf[BL_PREV][e]) * inv_dt, err, rel);
-            Mf[BL_ERR][e] = err;
-            Mf[BL_REL][e] = rel;
+            const ff tin = wff::add(wff::mul(ldm(F, SSF_QIN_AVG, e), inv_area), F.Mh[PRECIP][e]);
+            const ff vout = wff::add(wff::add(wff::add(ldm(F, NET_RUNOFF, e), ldm(F, AET, e)),
+                                              ldm(F, NET_RUNOFF_RIVER, e)),
+                                     ldm(F, LEAKAGE, e));
+            const ff tout = wff::add(wff::mul(ldm(F, SSF_Q_AVG, e), inv_area), vout);
+            const double ds = (tsws - F.Mf[BL_PREV][e]) + wff::to_d(wff::add(canopy, wff::add(snow, sw)));
+            mb_error_ff(tin, tout, wff::mul(wff::from_d(ds), inv_dt), err, rel);
+            stm(F, BL_ERR, e, err);
+            stm(F, BL_REL, e, rel);
         }
-        mb_error_s(Mf[OL_INWATER][e] + Mf[OL_QIN_AVG][e], Mf[OL_Q_AVG][e], (Mf[OL_STORAGE][e] - Mf[BO_PREV][e]) * inv_dt,
-                   err, rel);
-        Mf[BO_ERR][e] = err;
-        Mf[BO_REL][e] = rel;
+        mb_error_ff(wff::add(ldm(F, OL_INWATER, e), ldm(F, OL_QIN_AVG, e)), ldm(F, OL_Q_AVG, e),
+                    wff::mul(wff::sub(ldm(F, OL_STORAGE, e), ldm(F, BO_PREV, e)), inv_dt), err, rel);
+        stm(F, BO_ERR, e, err);
+        stm(F, BO_REL, e, rel);
         {
-            const double flux = Mf[RCH_FLUX_AVG][e];
-            const double fin = fmax(flux, 0.0), fout = fmax(-flux, 0.0);
-            mb_error_s(Mf[SSF_QIN_AVG][e] + fin, Mf[SSF_Q_AVG][e] + fout, Mf[SSF_QNET_AVG][e], err, rel);
-            Mf[BS_ERR][e] = err;
-            Mf[BS_REL][e] = rel;
+            const ff flux = ldm(F, RCH_FLUX_AVG, e);
+            const ff fin = wff::fmax0(flux), fout = wff::fmax0(wff::neg(flux));
+            mb_error_ff(wff::add(ldm(F, SSF_QIN_AVG, e), fin), wff::add(ldm(F, SSF_Q_AVG, e), fout),
+                        ldm(F, SSF_QNET_AVG, e), err, rel);
+            stm(F, BS_ERR, e, err);
+            stm(F, BS_REL, e, rel);
         }
     }
 }
 
-// Double-FP32 discharge and u = Q^0.2 of the overland and river state from the FP64 fields
-// (after a discharge was set from outside, and at creation).
+// u = Q^0.2 of the overland and river discharges (after a discharge was set from outside,
+// and at creation), in double-FP32 from an FP64 root.
 __global__ void __launch_bounds__(256) sync_u_kernel(WfDevFields F) {
     const int M = F.M;
     const int64_t EL = F.land_slots * M, ER = F.river_slots * M;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < EL + ER; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < EL) {
-            const double q = F.Mf[OL_Q][i];
-            const wff::ff qf = wff::from_d(q), uf = wff::from_d(u_of_q(q));
-            F.Mh[OL_QH][i] = qf.hi;
-            F.Mh[OL_QL][i] = qf.lo;
+            const wff::ff uf = wff::from_d(u_of_q(wff::to_d(ldm(F, OL_Q, i))));
             F.Mh[OL_UH][i] = uf.hi;
             F.Mh[OL_UL][i] = uf.lo;
         } else {
             const int64_t e = i - EL;
-            const double q = F.RM[RV_Q][e];
-            const wff::ff qf = wff::from_d(q), uf = wff::from_d(u_of_q(q));
-            F.RMh[RV_QH][e] = qf.hi;
-            F.RMh[RV_QL][e] = qf.lo;
+            const wff::ff uf = wff::from_d(u_of_q(wff::to_d(ldr(F, RV_Q, e))));
             F.RMh[RV_UH][e] = uf.hi;
             F.RMh[RV_UL][e] = uf.lo;
         }
+    }
+}
+
+// Volumetric water content of one layer after a step (soil.jl:1320-1342), split form.
+__global__ void __launch_bounds__(256) vwc_split_kernel(WfDevFields F, int layer, double* out) {
+    const int M = F.M;
+    const int64_t E = F.land_slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t slot = e / M;
+        if (F.land_node_of_slot[slot] < 0) continue;
+        const double zi = F.Mf[ZI][e];
+        const double top = layer == 0 ? 0.0 : F.LY[LY_CUM][layer - 1][slot];
+        const double bot = F.LY[LY_CUM][layer][slot];
+        const double act = F.LY[LY_ACT_THICK][layer][slot];
+        const double ts = F.L[THETA_S][slot], tr = F.L[THETA_R][slot];
+        double v = __longlong_as_double(0x7ff8000000000000LL);
+        if (layer < F.nlayers[slot]) {
+            if (zi > top) {
+                const double thick = zi > bot ? act : zi - top;
+                const double usld = (double)F.LYf[LY_USLD][layer][e] + (double)F.LYl[layer][e];
+                v = (usld + (act - thick) * (ts - tr)) / act + tr;
+            } else {
+                v = ts;
+            }
+        }
+        out[e] = v;
     }
 }
 
@@ -1671,6 +1762,11 @@ cudaError_t wf_split_overland_post(const WfDevFields& F, const WfDevGraph& g, co
 
 cudaError_t wf_split_river_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {
     rv_post_kernel<<<grid_for(F.river_slots * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F, g);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_split_vwc(const WfDevFields& F, int layer, double* out, const WfLaunchCfg& c) {
+    vwc_split_kernel<<<grid_for(F.land_slots * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F, layer, out);
     return cudaGetLastError();
 }
 

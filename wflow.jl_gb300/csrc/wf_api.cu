@@ -63,7 +63,8 @@ struct WfHandle {
     double* dts_river = nullptr;
     double* dts_ssf = nullptr;
     std::vector<double> h_dts_land, h_dts_river, h_dts_ssf;
-    std::vector<int64_t> outlet_slots;  // river slots of river pits
+    std::vector<int64_t> outlet_slots;
+    int64_t* d_outlet_slots = nullptr;  // river slots of river pits
     int64_t* d_land_node_of_slot = nullptr;
     WfTuning tuning{};
     WfMetrics metrics{};
@@ -143,6 +144,28 @@ int upload_slots_f32(WfHandle* h, float** dst, const std::vector<double>& ext, c
         }
     }
     return upload(h, dst, v);
+}
+
+// Double-FP32 pair (high part, low part) of an external-order array in slot layout (split form).
+int upload_slots_ff(WfHandle* h, float** hi, float** lo, const std::vector<double>& ext, const WfRoutingPlan& P,
+                    int M, int64_t n_ext, bool per_member) {
+    std::vector<float> vh((size_t)P.n_slots * (per_member ? M : 1), 0.0f), vl(vh.size(), 0.0f);
+    auto put = [&](size_t i, double x) {
+        const float a = (float)x;
+        vh[i] = a;
+        vl[i] = (float)(x - (double)a);
+    };
+    for (int64_t s = 0; s < P.n_slots; ++s) {
+        int64_t node = P.node_of_slot[s];
+        if (node < 0) continue;
+        if (per_member) {
+            for (int m = 0; m < M; ++m) put(s * M + m, ext[(size_t)m * n_ext + node]);
+        } else {
+            put(s, ext[node]);
+        }
+    }
+    int rc = upload(h, hi, vh);
+    return rc ? rc : upload(h, lo, vl);
 }
 
 int plan_graph(WfHandle* h, DevGraphAlloc& G, int64_t n, const int32_t* ds, int M, int32_t s_cap) {
@@ -241,25 +264,40 @@ __global__ void scatter_kernel(const double* src, double* dst, const int64_t* no
         if (node >= 0) dst[(int64_t)m * n_ext + node] = src[e];
     }
 }
+// FP64 external order -> FP32 (or a double-FP32 pair when lo is given) in slot order
 __global__ void gather_f32_kernel(const double* src, float* dst, const int64_t* node_of_slot, int64_t slots, int M,
-                                  int64_t n_ext) {
+                                  int64_t n_ext, float* lo = nullptr) {
     const int64_t E = slots * M;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t s = e / M;
         const int m = (int)(e - s * M);
         const int64_t node = node_of_slot[s];
-        if (node >= 0) dst[e] = (float)src[(int64_t)m * n_ext + node];
+        if (node < 0) continue;
+        const double x = src[(int64_t)m * n_ext + node];
+        const float a = (float)x;
+        dst[e] = a;
+        if (lo) lo[e] = (float)(x - (double)a);
     }
 }
+// FP32 (or double-FP32 pair) in slot order -> FP64 external order
 __global__ void scatter_f32_kernel(const float* src, double* dst, const int64_t* node_of_slot, int64_t slots, int M,
-                                   int64_t n_ext) {
+                                   int64_t n_ext, const float* lo = nullptr) {
     const int64_t E = slots * M;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t s = e / M;
         const int m = (int)(e - s * M);
         const int64_t node = node_of_slot[s];
-        if (node >= 0) dst[(int64_t)m * n_ext + node] = (double)src[e];
+        if (node >= 0) dst[(int64_t)m * n_ext + node] = (double)src[e] + (lo ? (double)lo[e] : 0.0);
     }
+}
+// Discharge at the outlets from double-FP32 pairs, member-major (split form).
+__global__ void outlets_ff_kernel(const float* hi, const float* lo, const int64_t* slots, int64_t n_out, int M,
+                                  double* dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n_out * M) return;
+    const int m = (int)(i / n_out);
+    const int64_t e = slots[i - (int64_t)m * n_out] * M + m;
+    dst[i] = (double)hi[e] + (double)lo[e];
 }
 __global__ void to_f32_kernel(const double* src, float* dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -292,8 +330,11 @@ int grid_of(int64_t n, int block) {
 
 // Field table: WfField -> device array
 struct FieldRef {
-    double* p = nullptr;
-    float* p32 = nullptr;
+    double* p = nullptr;      // FP64 array (FP64 form)
+    float* p32 = nullptr;     // FP32 array, or the high part of a double-FP32 pair (split form)
+    float* p32lo = nullptr;   // low part of a double-FP32 pair (split form)
+    int idx = -1;             // member / river-member field index
+    bool usld = false;        // unsaturated layer store of layer `layer`
     bool river = false;
     bool member = true;
     bool derived_vwc = false;
@@ -305,68 +346,80 @@ FieldRef field_ref(WfHandle* h, int field, int layer) {
     auto& Mf = h->F.Mf;
     auto& RM = h->F.RM;
     switch (field) {
-        case WF_F_CANOPY_STORAGE: r.p = Mf[CANOPY]; r.settable = true; break;
-        case WF_F_SNOW_STORAGE: r.p = Mf[SNOW]; r.settable = true; break;
-        case WF_F_SNOW_WATER: r.p = Mf[SNOW_WATER]; r.settable = true; break;
-        case WF_F_SOIL_SURFACE_TEMPERATURE: r.p = Mf[TSOIL]; r.settable = true; break;
-        case WF_F_SATURATED_WATER_DEPTH: r.p = Mf[SAT]; r.settable = true; break;
+        case WF_F_CANOPY_STORAGE: r.idx = CANOPY; r.settable = true; break;
+        case WF_F_SNOW_STORAGE: r.idx = SNOW; r.settable = true; break;
+        case WF_F_SNOW_WATER: r.idx = SNOW_WATER; r.settable = true; break;
+        case WF_F_SOIL_SURFACE_TEMPERATURE: r.idx = TSOIL; r.settable = true; break;
+        case WF_F_SATURATED_WATER_DEPTH: r.idx = SAT; r.settable = true; break;
         case WF_F_UNSATURATED_LAYER_DEPTH:
-            r.p = (layer >= 0 && layer < h->N) ? h->F.LY[LY_USLD][layer] : nullptr;
+            r.usld = layer >= 0 && layer < h->N;
             r.settable = true;
             break;
-        case WF_F_SSF_Q: r.p = Mf[SSF_Q]; r.settable = true; break;
-        case WF_F_LAND_Q: r.p = Mf[OL_Q]; r.settable = true; break;
-        case WF_F_LAND_H: r.p = Mf[OL_H]; r.settable = true; break;
-        case WF_F_WATER_TABLE_DEPTH: r.p = Mf[ZI]; break;
-        case WF_F_UNSATURATED_STORE_DEPTH: r.p = Mf[USTOREDEPTH]; break;
-        case WF_F_TOTAL_SOIL_WATER_STORAGE: r.p = Mf[TSWS]; r.settable = true; break;
-        case WF_F_RECHARGE: r.p = Mf[RECHARGE]; break;
-        case WF_F_NET_RUNOFF: r.p = Mf[NET_RUNOFF]; break;
-        case WF_F_RUNOFF: r.p = Mf[RUNOFF]; break;
-        case WF_F_ACTUAL_EVAPOTRANSPIRATION: r.p = Mf[AET]; break;
-        case WF_F_ACTUAL_LEAKAGE: r.p = Mf[LEAKAGE]; break;
-        case WF_F_TRANSPIRATION: r.p = Mf[TRANSPIRATION]; break;
-        case WF_F_SOIL_EVAPORATION: r.p = Mf[SOIL_EVAP]; break;
-        case WF_F_ACTUAL_INFILTRATION: r.p = Mf[ACT_INFILT]; break;
-        case WF_F_EXFILTRATION_SATURATED_WATER: r.p = Mf[EXFILT]; break;
-        case WF_F_INTERCEPTION_RATE: r.p = Mf[INTERCEPTION]; break;
-        case WF_F_SNOW_WATER_EQUIVALENT: r.p = Mf[SWE]; break;
-        case WF_F_NET_RUNOFF_RIVER: r.p = Mf[NET_RUNOFF_RIVER]; break;
-        case WF_F_SSF_Q_AVERAGE: r.p = Mf[SSF_Q_AVG]; break;
-        case WF_F_SSF_WATER_TABLE_DEPTH: r.p = Mf[SSF_ZI]; break;
-        case WF_F_SSF_STORAGE: r.p = Mf[SSF_STORAGE]; break;
-        case WF_F_SSF_TO_RIVER_AVERAGE: r.p = Mf[SSF_TR_AVG]; break;
-        case WF_F_LAND_Q_AVERAGE: r.p = Mf[OL_Q_AVG]; break;
-        case WF_F_LAND_STORAGE: r.p = Mf[OL_STORAGE]; r.settable = true; break;
-        case WF_F_LAND_TO_RIVER_AVERAGE: r.p = Mf[OL_TR_AVG]; break;
-        case WF_F_LAND_INWATER: r.p = Mf[OL_INWATER]; break;
-        case WF_F_TOTAL_STORAGE: r.p = Mf[TOTAL_STORAGE]; break;
-        case WF_F_BALANCE_LAND_ERROR: r.p = Mf[BL_ERR]; break;
-        case WF_F_BALANCE_LAND_RELATIVE_ERROR: r.p = Mf[BL_REL]; break;
-        case WF_F_BALANCE_OVERLAND_ERROR: r.p = Mf[BO_ERR]; break;
-        case WF_F_BALANCE_OVERLAND_RELATIVE_ERROR: r.p = Mf[BO_REL]; break;
-        case WF_F_BALANCE_SUBSURFACE_ERROR: r.p = Mf[BS_ERR]; break;
-        case WF_F_BALANCE_SUBSURFACE_RELATIVE_ERROR: r.p = Mf[BS_REL]; break;
+        case WF_F_SSF_Q: r.idx = SSF_Q; r.settable = true; break;
+        case WF_F_LAND_Q: r.idx = OL_Q; r.settable = true; break;
+        case WF_F_LAND_H: r.idx = OL_H; r.settable = true; break;
+        case WF_F_WATER_TABLE_DEPTH: r.idx = ZI; break;
+        case WF_F_UNSATURATED_STORE_DEPTH: r.idx = USTOREDEPTH; break;
+        case WF_F_TOTAL_SOIL_WATER_STORAGE: r.idx = TSWS; r.settable = true; break;
+        case WF_F_RECHARGE: r.idx = RECHARGE; break;
+        case WF_F_NET_RUNOFF: r.idx = NET_RUNOFF; break;
+        case WF_F_RUNOFF: r.idx = RUNOFF; break;
+        case WF_F_ACTUAL_EVAPOTRANSPIRATION: r.idx = AET; break;
+        case WF_F_ACTUAL_LEAKAGE: r.idx = LEAKAGE; break;
+        case WF_F_TRANSPIRATION: r.idx = TRANSPIRATION; break;
+        case WF_F_SOIL_EVAPORATION: r.idx = SOIL_EVAP; break;
+        case WF_F_ACTUAL_INFILTRATION: r.idx = ACT_INFILT; break;
+        case WF_F_EXFILTRATION_SATURATED_WATER: r.idx = EXFILT; break;
+        case WF_F_INTERCEPTION_RATE: r.idx = INTERCEPTION; break;
+        case WF_F_SNOW_WATER_EQUIVALENT: r.idx = SWE; break;
+        case WF_F_NET_RUNOFF_RIVER: r.idx = NET_RUNOFF_RIVER; break;
+        case WF_F_SSF_Q_AVERAGE: r.idx = SSF_Q_AVG; break;
+        case WF_F_SSF_WATER_TABLE_DEPTH: r.idx = SSF_ZI; break;
+        case WF_F_SSF_STORAGE: r.idx = SSF_STORAGE; break;
+        case WF_F_SSF_TO_RIVER_AVERAGE: r.idx = SSF_TR_AVG; break;
+        case WF_F_LAND_Q_AVERAGE: r.idx = OL_Q_AVG; break;
+        case WF_F_LAND_STORAGE: r.idx = OL_STORAGE; r.settable = true; break;
+        case WF_F_LAND_TO_RIVER_AVERAGE: r.idx = OL_TR_AVG; break;
+        case WF_F_LAND_INWATER: r.idx = OL_INWATER; break;
+        case WF_F_TOTAL_STORAGE: r.idx = TOTAL_STORAGE; break;
+        case WF_F_BALANCE_LAND_ERROR: r.idx = BL_ERR; break;
+        case WF_F_BALANCE_LAND_RELATIVE_ERROR: r.idx = BL_REL; break;
+        case WF_F_BALANCE_OVERLAND_ERROR: r.idx = BO_ERR; break;
+        case WF_F_BALANCE_OVERLAND_RELATIVE_ERROR: r.idx = BO_REL; break;
+        case WF_F_BALANCE_SUBSURFACE_ERROR: r.idx = BS_ERR; break;
+        case WF_F_BALANCE_SUBSURFACE_RELATIVE_ERROR: r.idx = BS_REL; break;
         case WF_F_VOLUMETRIC_WATER_CONTENT:
             r.derived_vwc = (layer >= 0 && layer < h->N);
             break;
-        case WF_F_RIVER_Q: r.p = RM[RV_Q]; r.river = true; r.settable = true; break;
-        case WF_F_RIVER_H: r.p = RM[RV_H]; r.river = true; r.settable = true; break;
-        case WF_F_RIVER_STORAGE: r.p = RM[RV_STORAGE]; r.river = true; r.settable = true; break;
-        case WF_F_RIVER_Q_AVERAGE: r.p = RM[RV_Q_AVG]; r.river = true; break;
-        case WF_F_RIVER_QIN_AVERAGE: r.p = RM[RV_QIN_AVG]; r.river = true; break;
-        case WF_F_RIVER_INWATER: r.p = RM[RV_INWATER]; r.river = true; break;
-        case WF_F_BALANCE_RIVER_ERROR: r.p = RM[BR_ERR]; r.river = true; break;
-        case WF_F_BALANCE_RIVER_RELATIVE_ERROR: r.p = RM[BR_REL]; r.river = true; break;
+        case WF_F_RIVER_Q: r.idx = RV_Q; r.river = true; r.settable = true; break;
+        case WF_F_RIVER_H: r.idx = RV_H; r.river = true; r.settable = true; break;
+        case WF_F_RIVER_STORAGE: r.idx = RV_STORAGE; r.river = true; r.settable = true; break;
+        case WF_F_RIVER_Q_AVERAGE: r.idx = RV_Q_AVG; r.river = true; break;
+        case WF_F_RIVER_QIN_AVERAGE: r.idx = RV_QIN_AVG; r.river = true; break;
+        case WF_F_RIVER_INWATER: r.idx = RV_INWATER; r.river = true; break;
+        case WF_F_BALANCE_RIVER_ERROR: r.idx = BR_ERR; r.river = true; break;
+        case WF_F_BALANCE_RIVER_RELATIVE_ERROR: r.idx = BR_REL; r.river = true; break;
         default: break;
     }
-    if (h->F.split && !r.river && r.p) {
-        for (int f = 0; f < M_COUNT; ++f) {
-            if (r.p == Mf[f] && wf_split_f32_member(f)) {
-                r.p32 = h->F.Mh[f];
-                r.p = nullptr;
-                break;
-            }
+    const WfDevFields& F = h->F;
+    if (r.usld) {
+        if (!F.split) {
+            r.p = F.LY[LY_USLD][layer];
+        } else {
+            r.p32 = F.LYf[LY_USLD][layer];
+            r.p32lo = F.LYl[layer];
+        }
+    } else if (r.idx >= 0) {
+        if (!F.split) {
+            r.p = r.river ? RM[r.idx] : Mf[r.idx];
+        } else if (r.river) {
+            r.p32 = F.RMh[r.idx];
+            r.p32lo = F.RMl[r.idx];
+        } else if (wf_split_fp64_member(r.idx)) {
+            r.p = Mf[r.idx];
+        } else {
+            r.p32 = F.Mh[r.idx];
+            if (!wf_split_f32_member(r.idx)) r.p32lo = F.Ml[r.idx];
         }
     }
     return r;
@@ -607,6 +660,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     }
     // ---- land static fields (slot layout)
     WfDevFields& F = h->F;
+    F.split = c->form == WF_FORM_SPLIT;
     auto ext_vec = [&](const double* src, double dflt) {
         std::vector<double> v(n);
         for (int64_t i = 0; i < n; ++i) v[i] = src ? src[i] : dflt;
@@ -684,7 +738,8 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         }
         CKR(upload_slots(h, &F.LY[LY_CUM][k], vcum, PL, M, n, false));
         std::vector<double> zeros((size_t)n * M, 0.0);
-        CKR(upload_slots(h, &F.LY[LY_USLD][k], zeros, PL, M, n, true));
+        if (F.split) CKR(upload_slots_ff(h, &F.LYf[LY_USLD][k], &F.LYl[k], zeros, PL, M, n, true));
+        else CKR(upload_slots(h, &F.LY[LY_USLD][k], zeros, PL, M, n, true));
     }
     {
         std::vector<int8_t> nl_slots(PL.n_slots, 0);
@@ -695,11 +750,10 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         F.nlayers = dnl;
     }
     // ---- land member fields
-    F.split = c->form == WF_FORM_SPLIT;
     std::vector<double> zeros_m((size_t)n * M, 0.0);
     for (int f = 0; f < M_COUNT; ++f) {
         if (!F.split && wf_split_only_member(f)) continue;
-        if (wf_split_f32_only(f)) continue;  // FP32 arrays only (below)
+        if (F.split && !wf_split_ff_member(f) && !wf_split_fp64_member(f)) continue;  // FP32 arrays only (below)
         const std::vector<double>* src = &zeros_m;
         switch (f) {
             case KV0: src = &kv0; break;
@@ -714,7 +768,8 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
             case SSF_STORAGE: src = &ssf_st; break;
             default: break;
         }
-        CKR(upload_slots(h, &F.Mf[f], *src, PL, M, n, true));
+        if (F.split && wf_split_ff_member(f)) CKR(upload_slots_ff(h, &F.Mh[f], &F.Ml[f], *src, PL, M, n, true));
+        else CKR(upload_slots(h, &F.Mf[f], *src, PL, M, n, true));
     }
     // ---- river fields
     std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr), r_inv_len(nr), r_inv_w(nr), r_inv_len_lo(nr);
@@ -744,7 +799,8 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
             if (F.split) CKR(upload_slots_f32(h, &F.RMh[f], zeros_r, PR, M, nr, true));
             continue;
         }
-        CKR(upload_slots(h, &F.RM[f], zeros_r, PR, M, nr, true));
+        if (F.split) CKR(upload_slots_ff(h, &F.RMh[f], &F.RMl[f], zeros_r, PR, M, nr, true));
+        else CKR(upload_slots(h, &F.RM[f], zeros_r, PR, M, nr, true));
     }
     // ---- upstream weights of the wavefront gathers: land discharge splits into the part that
     // goes to the river (flow_fraction_to_river) and the rest that flows downstream
@@ -768,7 +824,11 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     }
     // ---- split form: FP32 copies of the static fields and FP32 member fields
     if (F.split) {
-        for (auto& x : ls) CKR(upload_slots_f32(h, &F.Lf[x.idx], x.v, PL, M, n, false));
+        for (auto& x : ls) {
+            float* dummy = nullptr;
+            CKR(upload_slots_ff(h, &dummy, &F.Ll[x.idx], x.v, PL, M, n, false));
+            F.Lf[x.idx] = dummy;
+        }
         for (int k = 0; k < N; ++k) {
             std::vector<double> va(act.begin() + (size_t)k * n, act.begin() + (size_t)(k + 1) * n);
             std::vector<double> vr(rootfrac.begin() + (size_t)k * n, rootfrac.begin() + (size_t)(k + 1) * n);
@@ -777,7 +837,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
                 vc[i] = p->brooks_corey_exponent[i * N + k];
                 vk[i] = p->kv_factor[i * N + k];
             }
-            CKR(upload_slots_f32(h, &F.LYf[LY_ACT_THICK][k], va, PL, M, n, false));
+            CKR(upload_slots_ff(h, &F.LYf[LY_ACT_THICK][k], &F.LYsl[LY_ACT_THICK][k], va, PL, M, n, false));
             CKR(upload_slots_f32(h, &F.LYf[LY_ROOTFRAC][k], vr, PL, M, n, false));
             CKR(upload_slots_f32(h, &F.LYf[LY_C][k], vc, PL, M, n, false));
             CKR(upload_slots_f32(h, &F.LYf[LY_KVFRAC][k], vk, PL, M, n, false));
@@ -787,7 +847,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
                 for (int j = 0; j <= k; ++j) cc += act[(size_t)j * n + i];
                 vcum[i] = cc;
             }
-            CKR(upload_slots_f32(h, &F.LYf[LY_CUM][k], vcum, PL, M, n, false));
+            CKR(upload_slots_ff(h, &F.LYf[LY_CUM][k], &F.LYsl[LY_CUM][k], vcum, PL, M, n, false));
         }
         for (int f = 0; f < M_COUNT; ++f) {
             if (!wf_split_f32_member(f) && !wf_split_f32_only(f)) continue;
@@ -798,13 +858,14 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
             if (f == TSOIL) src = &tsoil;
             CKR(upload_slots_f32(h, &F.Mh[f], *src, PL, M, n, true));
         }
-        CKR(upload_slots_f32(h, &F.Rf[R_WIDTH], r_width, PR, M, nr, false));
-        CKR(upload_slots_f32(h, &F.Rf[R_LENGTH], r_length, PR, M, nr, false));
-        CKR(upload_slots_f32(h, &F.Rf[R_ALPHA], r_alpha, PR, M, nr, false));
-        CKR(upload_slots_f32(h, &F.Rf[R_EXT_INFLOW], r_ext, PR, M, nr, false));
-        CKR(upload_slots_f32(h, &F.Rf[R_AREA], r_area, PR, M, nr, false));
-        CKR(upload_slots_f32(h, &F.Rf[R_INV_LENGTH], r_inv_len, PR, M, nr, false));
-        CKR(upload_slots_f32(h, &F.Rf[R_INV_LEN_LO], r_inv_len_lo, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_WIDTH], &F.Rl[R_WIDTH], r_width, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_LENGTH], &F.Rl[R_LENGTH], r_length, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_ALPHA], &F.Rl[R_ALPHA], r_alpha, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_EXT_INFLOW], &F.Rl[R_EXT_INFLOW], r_ext, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_AREA], &F.Rl[R_AREA], r_area, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_INV_LENGTH], &F.Rl[R_INV_LENGTH], r_inv_len, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_INV_LEN_LO], &F.Rl[R_INV_LEN_LO], r_inv_len_lo, PR, M, nr, false));
+        CKR(upload_slots_ff(h, &F.Rf[R_INV_WIDTH], &F.Rl[R_INV_WIDTH], r_inv_w, PR, M, nr, false));
     }
     // ---- maps
     {
@@ -824,6 +885,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         F.river_node_of_slot = h->river.node_of_slot;
         for (int64_t r = 0; r < nr; ++r)
             if (d->river_downstream[r] < 0) h->outlet_slots.push_back(PR.slot_of_node[r]);
+        if (!h->outlet_slots.empty()) CKR(upload(h, &h->d_outlet_slots, h->outlet_slots));
     }
     F.land_slots = PL.n_slots;
     F.river_slots = PR.n_slots;
@@ -839,6 +901,10 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     F.ssf_single = F.split && h->h_dts_ssf.size() == 1;
     F.dt_ssf = h->h_dts_ssf[0];
     F.inv_dt_ssf = 1.0 / h->h_dts_ssf[0];
+    F.inv_dt_hi = (float)F.inv_dt;
+    F.inv_dt_lo = (float)(F.inv_dt - (double)F.inv_dt_hi);
+    F.inv_dts_hi = (float)F.inv_dt_ssf;
+    F.inv_dts_lo = (float)(F.inv_dt_ssf - (double)F.inv_dts_hi);
     CKR(dalloc(h, &h->status, 1));
     CK(cudaMemset(h->status, 0, sizeof(int32_t)));
     F.status = h->status;
@@ -961,7 +1027,7 @@ int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int
     double* src = r.p;
     double* tmp = h->staging + (size_t)std::max(h->n, h->nr) * h->M;  // second staging third
     if (r.derived_vwc) {
-        CK(wf_fp64_vwc(h->F, layer, tmp, lc));
+        CK(h->F.split ? wf_split_vwc(h->F, layer, tmp, lc) : wf_fp64_vwc(h->F, layer, tmp, lc));
         src = tmp;
     }
     const int block = 256;
@@ -969,7 +1035,7 @@ int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int
     const int64_t* nos = r.river ? h->F.river_node_of_slot : h->F.land_node_of_slot;
     if (r.p32)
         scatter_f32_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p32, h->staging, nos, slots, h->M,
-                                                                                  n_ext);
+                                                                                  n_ext, r.p32lo);
     else
         scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(src, h->staging, nos, slots, h->M, n_ext);
     CK(cudaGetLastError());
@@ -990,7 +1056,7 @@ int32_t wf_set_field(WfHandle* h, int32_t field, int32_t layer, const double* sr
     const int64_t* nos = r.river ? h->F.river_node_of_slot : h->F.land_node_of_slot;
     if (r.p32)
         scatter_f32_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p32, h->staging, nos, slots, h->M,
-                                                                                  n_ext);
+                                                                                  n_ext, r.p32lo);
     else
         scatter_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(r.p, h->staging, nos, slots, h->M,
                                                                               n_ext);
@@ -998,7 +1064,7 @@ int32_t wf_set_field(WfHandle* h, int32_t field, int32_t layer, const double* sr
     CK(cudaMemcpyAsync(h->staging + offset, src, count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (r.p32)
         gather_f32_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(h->staging, r.p32, nos, slots, h->M,
-                                                                                 n_ext);
+                                                                                 n_ext, r.p32lo);
     else
         gather_kernel<<<grid_of(slots * h->M, block), block, 0, h->stream>>>(h->staging, r.p, nos, slots, h->M,
                                                                              n_ext);
@@ -1013,6 +1079,18 @@ int32_t wf_get_outlets(WfHandle* h, int32_t which, double* dst, int64_t capacity
     const int64_t need = (int64_t)h->outlet_slots.size() * h->M;
     *n_written = 0;
     if (capacity < need) return set_err(h, WF_ERR_INVALID, "capacity too small");
+    if (h->F.split) {  // double-FP32 pairs: convert on the device, one copy out
+        if (need > 0) {
+            const int f = which == 0 ? RV_Q_AVG : RV_Q;
+            outlets_ff_kernel<<<(unsigned)((need + 255) / 256), 256, 0, h->stream>>>(
+                h->F.RMh[f], h->F.RMl[f], h->d_outlet_slots, (int64_t)h->outlet_slots.size(), h->M, h->staging);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(dst, h->staging, need * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        }
+        CK(cudaStreamSynchronize(h->stream));
+        *n_written = need;
+        return WF_OK;
+    }
     double* src = which == 0 ? h->F.RM[RV_Q_AVG] : h->F.RM[RV_Q];
     int64_t k = 0;
     for (int m = 0; m < h->M; ++m)

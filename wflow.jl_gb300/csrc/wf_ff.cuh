@@ -52,7 +52,29 @@ __device__ __forceinline__ ff mul(ff a, float b) {
     p.lo = fmaf(a.lo, b, p.lo);
     return fast_two_sum(p.hi, p.lo);
 }
+__device__ __forceinline__ ff sub(ff a, ff b) { return add(a, neg(b)); }
+__device__ __forceinline__ ff sub(ff a, float b) { return add(a, -b); }
+// a / b with one Newton correction of the FP32 quotient (about 44 bits)
+__device__ __forceinline__ ff div(ff a, ff b) {
+    const float q1 = __fdividef(a.hi, b.hi);
+    const ff r = sub(a, mul(b, q1));
+    const float q2 = __fdividef(r.hi, b.hi);
+    return fast_two_sum(q1, q2);
+}
+__device__ __forceinline__ ff div(ff a, float b) { return div(a, ff{b, 0.0f}); }
+__device__ __forceinline__ bool lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool gt(ff a, ff b) { return lt(b, a); }
+__device__ __forceinline__ bool le(ff a, ff b) { return !lt(b, a); }
+__device__ __forceinline__ ff fmin(ff a, ff b) { return lt(b, a) ? b : a; }
+__device__ __forceinline__ ff fmax(ff a, ff b) { return lt(a, b) ? b : a; }
+__device__ __forceinline__ ff fmax0(ff a) { return a.hi > 0.0f ? a : ff{0.0f, 0.0f}; }
+__device__ __forceinline__ float to_f(ff a) { return a.hi + a.lo; }
 __device__ __forceinline__ ff from_f(float x) { return {x, 0.0f}; }
+__device__ __forceinline__ ff ld(const float* h, const float* l, int64_t i) { return {h[i], l[i]}; }
+__device__ __forceinline__ void st(float* h, float* l, int64_t i, ff v) {
+    h[i] = v.hi;
+    l[i] = v.lo;
+}
 __host__ __device__ __forceinline__ double to_d(ff a) { return (double)a.hi + (double)a.lo; }
 __host__ __device__ __forceinline__ ff from_d(double x) {
     const float h = (float)x;

@@ -31,16 +31,14 @@
     X(BS_ERR) X(BS_REL)                                                                            \
     X(SSF_QNET) X(SSF_TQIN) X(SSF_TEXF) X(SSF_TNF)                                                 \
     X(SSF_T2) X(SSF_RDF) X(SSF_RTH) X(SSF_RCAP) X(SSF_RRHO) X(SSF_FLAG) X(SSF_QNETF) X(SSF_ZIF)      \
-    X(SSF_QF) X(SSF_QUF) X(SSF_QINF) X(OL_UH) X(OL_UL) X(OL_QH) X(OL_QL) X(OL_QSUMH) X(OL_QSUML)     \
-    X(OL_QLATH) X(OL_QLATL)
+    X(SSF_QF) X(SSF_QUF) X(SSF_QINF) X(OL_UH) X(OL_UL) X(OL_QSUMH) X(OL_QSUML)
 
 #define WF_R_FIELDS(X) X(R_WIDTH) X(R_LENGTH) X(R_ALPHA) X(R_EXT_INFLOW) X(R_AREA) X(R_INV_LENGTH) X(R_INV_WIDTH) X(R_INV_LEN_LO)
 
 #define WF_RM_FIELDS(X)                                                                            \
     X(RV_Q) X(RV_H) X(RV_STORAGE) X(RV_Q_AVG) X(RV_QIN_AVG) X(RV_INWATER) X(RV_QLAT) X(RV_ABS_AVG)    \
     X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL)                         \
-    X(RV_UH) X(RV_UL) X(RV_QH) X(RV_QL) X(RV_QSUMH) X(RV_QSUML) X(RV_ABSH) X(RV_ABSL) X(RV_QLATTH)   \
-    X(RV_QLATTL)
+    X(RV_UH) X(RV_UL) X(RV_QSUMH) X(RV_QSUML) X(RV_ABSH) X(RV_ABSL) X(RV_QLATTH) X(RV_QLATTL)
 
 #define WF_ENUM_ITEM(name) name,
 enum WfLandStatic { WF_L_FIELDS(WF_ENUM_ITEM) L_COUNT };
@@ -67,6 +65,18 @@ __host__ __device__ inline bool wf_split_only_river_member(int f) { return f >= 
 // state (pairs *H + *L).
 __host__ __device__ inline bool wf_split_f32_only(int f) { return f >= SSF_T2; }
 __host__ __device__ inline bool wf_split_f32_only_river(int f) { return f >= RV_UH; }
+// Split form: the large stores stay FP64 (saturated depth, water-table depths, total soil
+// water and the land balance's previous storage): a step changes them by as little as
+// 1e-15 of their size in dry cells, below the double-FP32 resolution.
+__host__ __device__ inline bool wf_split_fp64_member(int f) {
+    return f == SAT || f == ZI || f == SSF_ZI || f == TSWS || f == BL_PREV;
+}
+// Split form: member fields held as double-FP32 pairs (every other field that is FP64 in the
+// FP64 form and not one of the FP32 fields above).
+__host__ __device__ inline bool wf_split_ff_member(int f) {
+    return !wf_split_f32_member(f) && !wf_split_f32_only(f) && !wf_split_fp64_member(f);
+}
+__host__ __device__ inline bool wf_split_ff_river(int f) { return !wf_split_f32_only_river(f); }
 
 struct WfDevFields {
     double* L[L_COUNT];
@@ -80,6 +90,16 @@ struct WfDevFields {
     float* Mh[M_COUNT];
     float* Rf[R_COUNT];
     float* RMh[RM_COUNT];
+    // split form: the member fields that are FP64 in the FP64 form are double-FP32 pairs
+    // (high part in Mh / RMh / LYf[LY_USLD], low part here); low parts of the static fields
+    float* Ml[M_COUNT];
+    float* RMl[RM_COUNT];
+    float* LYl[WF_MAX_LAYERS];
+    float* Ll[L_COUNT];
+    float* Rl[R_COUNT];
+    float* LYsl[LY_COUNT][WF_MAX_LAYERS];  // low parts of LY_ACT_THICK and LY_CUM
+    float inv_dt_hi, inv_dt_lo;            // 1/dt as a double-FP32 pair
+    float inv_dts_hi, inv_dts_lo;          // 1/dt_ssf as a double-FP32 pair
     int32_t split;
     const int8_t* nlayers;                // [land slots]
     const int64_t* land_node_of_slot;     // [land slots], -1 padding

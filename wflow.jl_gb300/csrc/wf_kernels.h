@@ -37,6 +37,7 @@ cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const W
 cudaError_t wf_split_overland_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
 cudaError_t wf_split_river_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
 cudaError_t wf_split_sync_u(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_split_vwc(const WfDevFields& F, int layer, double* out, const WfLaunchCfg& c);
 
 // gather/scatter between the external (land/river) order and the slot order
 cudaError_t wf_gather_ext(const double* src_ext, double* dst_slots, const int64_t* node_of_slot, int64_t slots,
