@@ -363,21 +363,59 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         const int m = (int)(e - slot * M);
         float* const* Mh = F.Mh;
         float* const* Lf = F.Lf;
+        // per-cell parameters, loaded up front so that the loads are in flight together
+        const float p_alpha_h1 = Lf[ALPHA_H1][slot];
+        const float p_cap_comp = Lf[CAP_COMP][slot];
+        const float p_cap_hmax = Lf[CAP_HMAX][slot];
+        const float p_cap_n = Lf[CAP_N][slot];
+        const float p_cf_soil = Lf[CF_SOIL][slot];
+        const float p_cmax = Lf[CMAX][slot];
+        const float p_compact_frac = Lf[COMPACT_FRAC][slot];
+        const float p_ddf = Lf[DDF][slot];
+        const float p_e_r = Lf[E_R][slot];
+        const float p_gap = Lf[GAP][slot];
+        const float p_h1 = Lf[H1][slot];
+        const float p_h2 = Lf[H2][slot];
+        const float p_h3_high = Lf[H3_HIGH][slot];
+        const float p_h3_low = Lf[H3_LOW][slot];
+        const float p_h4 = Lf[H4][slot];
+        const float p_kc = Lf[KC][slot];
+        const float p_kh_ratio = Lf[KH_RATIO][slot];
+        const float p_max_leakage = Lf[MAX_LEAKAGE][slot];
+        const float p_psi_b = Lf[PSI_B][slot];
+        const float p_river_fraction = Lf[RIVER_FRACTION][slot];
+        const float p_rootdistpar = Lf[ROOTDISTPAR][slot];
+        const float p_rooting_depth = Lf[ROOTING_DEPTH][slot];
+        const float p_slope = Lf[SLOPE][slot];
+        const float p_soil_thickness = Lf[SOIL_THICKNESS][slot];
+        const float p_ssf_dtdx = Lf[SSF_DTDX][slot];
+        const float p_swc = Lf[SWC][slot];
+        const float p_sy = Lf[SY][slot];
+        const float p_theta_fc = Lf[THETA_FC][slot];
+        const float p_theta_r = Lf[THETA_R][slot];
+        const float p_theta_s = Lf[THETA_S][slot];
+        const float p_tt = Lf[TT][slot];
+        const float p_tti = Lf[TTI][slot];
+        const float p_ttm = Lf[TTM][slot];
+        const float p_water_fraction = Lf[WATER_FRACTION][slot];
+        const float p_whc = Lf[WHC][slot];
+        const float p_w_soil = Lf[W_SOIL][slot];
+        const float p_z_exp = Lf[Z_EXP][slot];
         const float Pf = Mh[PRECIP][e], PETf = Mh[POTEVAP][e], Tf = Mh[TEMP][e];
         const ff canopy0 = ldm(F, CANOPY, e);
         const ff snow0 = F.snow ? ldm(F, SNOW, e) : ff{0.0f, 0.0f};
         const ff sw0 = F.snow ? ldm(F, SNOW_WATER, e) : ff{0.0f, 0.0f};
         if (F.mass_balance) F.Mf[BL_PREV][e] = F.Mf[TSWS][e] + wff::to_d(wff::add(canopy0, wff::add(snow0, sw0)));
         // ---- interception (canopy.jl:213-226 Gash, :259-271 Rutter)
-        const float gapf = Lf[GAP][slot], cmaxf = Lf[CMAX][slot];
-        const float potevap_f = Lf[KC][slot] * PETf * (1.0f - gapf);
+        const float gapf = p_gap, cmaxf = p_cmax;
+        const float potevap_f = p_kc * PETf * (1.0f - gapf);
         ff tf, ic;
         float icf, sff;
         Store canopy;
         canopy.init(canopy0);
         if (F.gash) {
             if (cmaxf > 0.0f) {
-                const float e_r = Lf[E_R][slot];
+                const float e_r = p_e_r;
                 float fs, fi, psat;
                 if (gapf < 1.0f / 1.1f) {
                     fs = 0.1f * gapf;
@@ -441,12 +479,12 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             snow.init(snow0);
             sw.init(sw0);
             const ff eff = wff::add(tf, sff);
-            const float tti = Lf[TTI][slot], tt = Lf[TT][slot];
+            const float tti = p_tti, tt = p_tt;
             const float rainfrac = tti == 0.0f ? (Tf > tt ? 1.0f : 0.0f)
                                                : fminf(fmaxf((Tf - (tt - tti / 2.0f)) / tti, 0.0f), 1.0f);
             const ff lp = wff::mul(eff, rainfrac);
             const ff sp = wff::sub(eff, lp);
-            const float ttm = Lf[TTM][slot], ddf = Lf[DDF][slot];
+            const float ttm = p_ttm, ddf = p_ddf;
             if (Tf > ttm) {
                 const float melt = ddf * (Tf - ttm);
                 if (melt * dtf >= snow.val()) {
@@ -466,7 +504,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             }
             snow.add(wff::mul(sp, dtf));
             sw.add(wff::mul(lp, dtf));
-            const float whc = Lf[WHC][slot];
+            const float whc = p_whc;
             wfs = {0.0f, 0.0f};
             if (sw.val() > snow.val() * whc) {
                 const ff maxsw = wff::mul(snow.value(), whc);
@@ -481,7 +519,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             wfs = wff::add(tf, sff);
         }
         // ---- open water (runoff.jl open-water runoff and evaporation)
-        const float rfrac_f = Lf[RIVER_FRACTION][slot], wfrac_f = Lf[WATER_FRACTION][slot];
+        const float rfrac_f = p_river_fraction, wfrac_f = p_water_fraction;
         const float wd_land = Mh[OL_H][e];
         const int64_t rs = F.land_river_slot[slot];
         const float wd_river = rs >= 0 ? F.RMh[RV_H][rs * M + m] : 0.0f;
@@ -499,10 +537,10 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         const double zi = fmax(0.0, fma(-sat, F.L[INV_TE][slot], d_soil));
         ColG<MAXN> g;
         g.set(F, slot, zi);
-        const float zif = (float)zi, df = Lf[SOIL_THICKNESS][slot], satf = (float)sat;
-        const float ts = Lf[THETA_S][slot], tr = Lf[THETA_R][slot], tfc = Lf[THETA_FC][slot];
+        const float zif = (float)zi, df = p_soil_thickness, satf = (float)sat;
+        const float ts = p_theta_s, tr = p_theta_r, tfc = p_theta_fc;
         const float te = ts - tr;
-        const float kv0 = Mh[KV0][e], fsc = Mh[FSCALE][e], zexp = Lf[Z_EXP][slot];
+        const float kv0 = Mh[KV0][e], fsc = Mh[FSCALE][e], zexp = p_z_exp;
         const bool kv_const = F.kv_profile == WF_KV_EXPONENTIAL_CONSTANT;
         Store us[MAXN];
         float kvf[MAXN], cexp[MAXN], rfr[MAXN];
@@ -531,18 +569,18 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         return kf_ * kv0 * expf(-fsc * zz_);                       \
     }())
         float drain = (df - zif) * fmaxf(ts - tfc, 0.02f);
-        float ucap = Lf[SWC][slot] - satf - usd;
+        float ucap = p_swc - satf - usd;
         float tsoil = Mh[TSOIL][e];
-        if (F.snow) tsoil = tsoil + Lf[W_SOIL][slot] * (Tf - tsoil);
+        if (F.snow) tsoil = tsoil + p_w_soil * (Tf - tsoil);
         float fred = 1.0f;
         if (F.snow && F.infilt_reduction) {
-            const float cf = Lf[CF_SOIL][slot];
+            const float cf = p_cf_soil;
             fred = 1.0f / (1.0f / (1.0f - cf) + expf(-8.0f * (tsoil - 273.15f))) + cf;
         }
         // infiltration (soil_process.jl infiltration): exact partition of the water reaching the soil
-        const ff soilinf = wff::mul(wfs_soil, 1.0f - Lf[COMPACT_FRAC][slot]);
+        const ff soilinf = wff::mul(wfs_soil, 1.0f - p_compact_frac);
         const ff pathinf = wff::sub(wfs_soil, soilinf);
-        const float cap_soil = kv0 * kvf[0] * fred, cap_comp = Lf[CAP_COMP][slot] * fred;
+        const float cap_soil = kv0 * kvf[0] * fred, cap_comp = p_cap_comp * fred;
         const ff mis = cap_soil < soilinf.hi ? wff::from_f(cap_soil) : soilinf;
         const ff mip = cap_comp < pathinf.hi ? wff::from_f(cap_comp) : pathinf;
         const ff infex = wff::add(wff::sub(soilinf, mis), wff::sub(pathinf, mip));
@@ -607,11 +645,11 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         ff actevap = {0.0f, 0.0f};
         float actevap_f = 0.0f, act_sat_f;
         {
-            const float rd = Lf[ROOTING_DEPTH][slot];
-            const float h1 = Lf[H1][slot], h2 = Lf[H2][slot], h4 = Lf[H4][slot], a1 = Lf[ALPHA_H1][slot];
-            const float psi = Lf[PSI_B][slot];
+            const float rd = p_rooting_depth;
+            const float h1 = p_h1, h2 = p_h2, h4 = p_h4, a1 = p_alpha_h1;
+            const float psi = p_psi_b;
             const float tpd = pot_trans / MM_PER_DAY_F;
-            const float h3l = Lf[H3_LOW][slot], h3h = Lf[H3_HIGH][slot];
+            const float h3l = p_h3_low, h3h = p_h3_high;
             const float h3 = tpd <= 1.0f ? h3l : (tpd < 5.0f ? h3l + (h3h - h3l) * (tpd - 1.0f) / 4.0f : h3h);
             float sum_rf = 0.0f, rf_low = 0.0f;
 #pragma unroll
@@ -647,7 +685,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
                     actevap_f += a;
                 }
             }
-            const float wetroots = 1.0f / (1.0f + expf(-Lf[ROOTDISTPAR][slot] * (zif - rd)));
+            const float wetroots = 1.0f / (1.0f + expf(-p_rootdistpar * (zif - rd)));
             const float alpha0 = rwu_feddes_f(0.0f, h1, h2, h3, h4, a1);
             act_sat_f = fminf((pot_trans - actevap_f) * (wetroots * alpha0), drain * inv_dtf);
             drain -= act_sat_f * dtf;
@@ -668,16 +706,16 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
 #pragma unroll
         for (int k = 0; k < MAXN; ++k)
             if (k < g.nl) usd += us[k].val();
-        ucap = Lf[SWC][slot] - satf - usd;
+        ucap = p_swc - satf - usd;
         // capillary rise (soil.jl capillary_flux!)
         Store capacc;
         capacc.init({0.0f, 0.0f});
         if (g.nu > 0) {
             const float ksat = WF_KV_AT(zif, g.nu);
             const float maxcap = fmaxf(0.0f, fminf(fminf(fminf(ksat, actevap_f), ucap * inv_dtf), drain * inv_dtf));
-            const float rd = Lf[ROOTING_DEPTH][slot];
-            const float chmax = Lf[CAP_HMAX][slot];
-            float capflux = zif > rd ? maxcap * powj(1.0f - fminf(zif, chmax) / chmax, Lf[CAP_N][slot]) : 0.0f;
+            const float rd = p_rooting_depth;
+            const float chmax = p_cap_hmax;
+            float capflux = zif > rd ? maxcap * powj(1.0f - fminf(zif, chmax) / chmax, p_cap_n) : 0.0f;
 #pragma unroll
             for (int k = MAXN; k >= 1; --k) {
                 if (k > g.nu) continue;
@@ -691,7 +729,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         const ff capflux = wff::fast_two_sum(capacc.hi, capacc.lo);
         const float deepksat = WF_KV_AT(df, g.nl);
 #undef WF_KV_AT
-        const float leak_f = fmaxf(0.0f, fminf(Lf[MAX_LEAKAGE][slot], fminf(drain * inv_dtf, deepksat)));
+        const float leak_f = fmaxf(0.0f, fminf(p_max_leakage, fminf(drain * inv_dtf, deepksat)));
         const ff recharge = wff::sub(wff::sub(wff::sub(wff::sub(transfer, capflux), leak_f), act_sat_f), esat_f);
         const ff transpiration = wff::add(actevap, act_sat_f);
         const ff aet = wff::add(wff::add(wff::add(wff::add(soilevap, transpiration), ae_river_f), ae_land_f), ic);
@@ -739,10 +777,10 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             Mh[SSF_ZIF][e] = zif;
             float z = zif;
             if (kv_const && !(z < zexp)) z = zexp;
-            const float cel = Lf[KH_RATIO][slot] * kv0 * expf(-fsc * z) * Lf[SLOPE][slot] / Lf[SY][slot];
+            const float cel = p_kh_ratio * kv0 * expf(-fsc * z) * p_slope / p_sy;
             const float cinv = 1.0f / cel;
             Mh[SSF_T2][e] = wff::to_f(ldm(F, SSF_Q, e)) * cinv;
-            Mh[SSF_RDF][e] = 1.0f / (Lf[SSF_DTDX][slot] + cinv);
+            Mh[SSF_RDF][e] = 1.0f / (p_ssf_dtdx + cinv);
             // deepest unsaturated layer: what a rising water table fills first
             float rth = 0.0f, rcap = 0.0f, rrho = 0.0f;
             const float dts = (float)F.dt_ssf;
@@ -1351,55 +1389,58 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
     const int M = F.M;
     const int N = F.N;
     const int64_t E = F.land_slots * M;
-    const float r_s = (float)(F.dt_ssf * F.inv_dt);  // sub-step / step (1 when they are equal)
+    const float r_s = F.r_s;  // sub-step / step (1 when they are equal)
     const ff dts = wff::from_f((float)F.dt_ssf);
     const ff inv_dts = {F.inv_dts_hi, F.inv_dts_lo};
-    const double NANV = __longlong_as_double(0x7ff8000000000000LL);
+    const ff NANF = {__int_as_float(0x7fc00000), 0.0f};
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
         float* const* Mh = F.Mh;
-        double* const* L = F.L;
         const int flag = (int)Mh[SSF_FLAG][e];
         const double zi_soil = F.Mf[ZI][e];
-        const double d = L[SOIL_THICKNESS][slot];
-        const double te_d = L[THETA_S][slot] - L[THETA_R][slot];
-        const ff te = wff::from_d(te_d);
-        ff usld[MAXN];
-        double act[MAXN], cum[MAXN + 1];  // cum[k]: depth of the top of layer k
-        cum[0] = 0.0;
+        const ff zis = wff::from_d(zi_soil);
+        const ff d = lds(F, SOIL_THICKNESS, slot);
+        const ff te = wff::sub(lds(F, THETA_S, slot), lds(F, THETA_R, slot));
+        ff usld[MAXN], act[MAXN], cum[MAXN + 1];  // cum[k]: depth of the top of layer k
+        cum[0] = {0.0f, 0.0f};
 #pragma unroll
         for (int k = 0; k < MAXN; ++k) {
             usld[k] = k < N ? ff{F.LYf[LY_USLD][k][e], F.LYl[k][e]} : ff{0.0f, 0.0f};
-            act[k] = k < N ? F.LY[LY_ACT_THICK][k][slot] : NANV;
-            cum[k + 1] = k < N ? F.LY[LY_CUM][k][slot] : NANV;
+            act[k] = k < N ? ff{F.LYf[LY_ACT_THICK][k][slot], F.LYsl[LY_ACT_THICK][k][slot]} : NANF;
+            cum[k + 1] = k < N ? ff{F.LYf[LY_CUM][k][slot], F.LYsl[LY_CUM][k][slot]} : NANF;
         }
-        // layer k is unsaturated iff the water table lies below its top (utils.jl set_layerthickness)
-        auto nu_at = [&](double ref) {
+        // layer geometry (utils.jl set_layerthickness) on the double-FP32 pairs of the depths:
+        // layer k is unsaturated iff the water table lies below its top
+        auto nu_at = [&](ff ref) {
             int c = 0;
 #pragma unroll
             for (int k = 0; k < MAXN; ++k)
-                if (k < N && ref > cum[k]) ++c;
+                if (k < N && wff::gt(ref, cum[k])) ++c;
             return c;
         };
-        auto thick_at = [&](double ref, int k) {
-            return ref > cum[k + 1] ? act[k] : (ref > cum[k] ? ref - cum[k] : NANV);
+        auto thick_at = [&](ff ref, int k) {
+            return wff::gt(ref, cum[k + 1]) ? act[k] : (wff::gt(ref, cum[k]) ? wff::sub(ref, cum[k]) : NANF);
         };
         ff q, qin, exf, nf;
         double zi_new, zi_s;
+        ff zin, zss;  // double-FP32 copies of zi_new and zi_s
         if (flag == SSF_EARLY) {
             q = qin = exf = nf = {0.0f, 0.0f};
-            zi_new = d;
+            zi_new = F.L[SOIL_THICKNESS][slot];
+            zin = d;
             zi_s = zi_soil;
+            zss = zis;
             stm(F, SSF_Q, e, q);
-            F.Mf[SSF_ZI][e] = d;
+            F.Mf[SSF_ZI][e] = zi_new;
         } else if (flag == SSF_FULL) {
             q = ldm(F, SSF_Q, e);
             qin = ldm(F, SSF_TQIN, e);
             exf = ldm(F, SSF_TEXF, e);
             nf = ldm(F, SSF_TNF, e);
             zi_new = zi_s = F.Mf[SSF_ZI][e];
+            zin = zss = wff::from_d(zi_new);
 #pragma unroll
             for (int k = 0; k < MAXN; ++k) usld[k] = k < N ? ff{F.LYf[LY_USLD][k][e], F.LYl[k][e]} : ff{0.0f, 0.0f};
         } else {
@@ -1413,11 +1454,11 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
             if (nf.hi <= 0.0f) {
                 dh = wff::mul(nf, lds(F, SSF_DTSY, slot));
             } else {
-                const int nu0 = nu_at(zi_soil);
+                const int nu0 = nu_at(zis);
 #pragma unroll
                 for (int k = MAXN; k >= 1; --k) {
                     if (k > nu0 || rem.hi == 0.0f) continue;
-                    const ff t = wff::from_d(thick_at(zi_soil, k - 1));
+                    const ff t = thick_at(zis, k - 1);
                     const ff cap = wff::mul(wff::fmax0(wff::sub(wff::mul(t, te), usld[k - 1])), inv_dts);
                     const ff fl = wff::fmin(rem, cap);
                     if (wff::le(cap, rem)) dh = wff::add(dh, t);
@@ -1426,30 +1467,32 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
                 }
             }
             exf = wff::fmax0(rem);
+            // the water table itself is an FP64 store
+            const double dmax = F.L[SOIL_THICKNESS][slot];
             double zi = zi_soil - wff::to_d(dh);
-            if (flag == SSF_CUT || zi > d) zi = d;
+            if (flag == SSF_CUT || zi > dmax) zi = dmax;
             zi = fmax(zi, 0.0);
             zi_new = zi_s = zi;
+            zin = zss = wff::from_d(zi);
             if (zi_new != zi_soil) {
-                const int n_prev = nu_at(zi_soil), n_new = nu_at(zi_new);
+                const int n_prev = nu_at(zis), n_new = nu_at(zin);
                 if (zi_new < zi_soil) {
 #pragma unroll
                     for (int k = 1; k <= MAXN; ++k) {
                         if (k < n_new || k > n_prev) continue;
-                        const double t = thick_at(zi_new, k - 1);
-                        usld[k - 1] = t != t ? ff{0.0f, 0.0f}
-                                             : wff::mul(wff::from_d(t * wfm_rcp(thick_at(zi_soil, k - 1))), usld[k - 1]);
+                        const ff t = thick_at(zin, k - 1);
+                        usld[k - 1] = t.hi != t.hi ? ff{0.0f, 0.0f} : wff::mul(wff::div(t, thick_at(zis, k - 1)), usld[k - 1]);
                         F.LYf[LY_USLD][k - 1][e] = usld[k - 1].hi;
                         F.LYl[k - 1][e] = usld[k - 1].lo;
                     }
                 } else {
-                    const double tfc_tr = L[THETA_FC][slot] - L[THETA_R][slot];
+                    const ff tfc_tr = wff::sub(lds(F, THETA_FC, slot), lds(F, THETA_R, slot));
 #pragma unroll
                     for (int k = 1; k <= MAXN; ++k) {
                         if (k < n_prev || k > n_new) continue;
-                        double tp = thick_at(zi_soil, k - 1);
-                        tp = tp != tp ? 0.0 : tp;
-                        usld[k - 1] = wff::add(usld[k - 1], wff::from_d((thick_at(zi_new, k - 1) - tp) * tfc_tr));
+                        ff tp = thick_at(zis, k - 1);
+                        if (tp.hi != tp.hi) tp = {0.0f, 0.0f};
+                        usld[k - 1] = wff::add(usld[k - 1], wff::mul(wff::sub(thick_at(zin, k - 1), tp), tfc_tr));
                         F.LYf[LY_USLD][k - 1][e] = usld[k - 1].hi;
                         F.LYl[k - 1][e] = usld[k - 1].lo;
                     }
@@ -1459,13 +1502,13 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
             stm(F, SSF_Q, e, q);
             F.Mf[SSF_ZI][e] = zi_new;
         }
-        const int nu = nu_at(zi_s);
+        const int nu = nu_at(zss);
         ff tr = {0.0f, 0.0f};
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o)
             tr = wff::add(tr, wff::two_prod(Mh[SSF_QF][g.up_slot[o] * M + m], g.up_frf[o]));
         const ff area = lds(F, AREA, slot);
         const ff flux = ldm(F, SSF_QNET, e);
-        stm(F, SSF_STORAGE, e, wff::mul(wff::from_d(L[SY][slot] * (d - zi_new)), area));
+        stm(F, SSF_STORAGE, e, wff::mul(wff::mul(wff::sub(d, zin), F.Lf[SY][slot]), area));
         const ff exf_avg = wff::mul(exf, r_s);
         stm(F, RCH_FLUX_AVG, e, wff::mul(flux, r_s));
         stm(F, SSF_QIN_AVG, e, wff::mul(qin, r_s));
@@ -1479,7 +1522,8 @@ __global__ void __launch_bounds__(256) ssf_post_kernel(WfDevFields F, WfDevGraph
             if (k < nu) usd = wff::add(usd, usld[k]);
         const ff runoff = wff::fmax0(
             wff::add(wff::add(wff::add(exf_avg, ldm(F, SATEX, e)), ldm(F, RUNOFF_LAND, e)), ldm(F, INFEX, e)));
-        const double sat = (d - zi_s) * te_d;
+        // saturated store and total soil water: FP64 stores
+        const double sat = (F.L[SOIL_THICKNESS][slot] - zi_s) * (F.L[THETA_S][slot] - F.L[THETA_R][slot]);
         F.Mf[SAT][e] = sat;
         stm(F, USTOREDEPTH, e, usd);
         F.Mf[TSWS][e] = sat + wff::to_d(usd);

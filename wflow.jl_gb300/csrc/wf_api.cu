@@ -905,6 +905,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     F.inv_dt_lo = (float)(F.inv_dt - (double)F.inv_dt_hi);
     F.inv_dts_hi = (float)F.inv_dt_ssf;
     F.inv_dts_lo = (float)(F.inv_dt_ssf - (double)F.inv_dts_hi);
+    F.r_s = (float)(F.dt_ssf / F.dt);
     CKR(dalloc(h, &h->status, 1));
     CK(cudaMemset(h->status, 0, sizeof(int32_t)));
     F.status = h->status;

@@ -100,6 +100,7 @@ struct WfDevFields {
     float* LYsl[LY_COUNT][WF_MAX_LAYERS];  // low parts of LY_ACT_THICK and LY_CUM
     float inv_dt_hi, inv_dt_lo;            // 1/dt as a double-FP32 pair
     float inv_dts_hi, inv_dts_lo;          // 1/dt_ssf as a double-FP32 pair
+    float r_s;                             // dt_ssf / dt
     int32_t split;
     const int8_t* nlayers;                // [land slots]
     const int64_t* land_node_of_slot;     // [land slots], -1 padding
