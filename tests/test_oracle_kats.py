@@ -212,3 +212,38 @@ def test_julia_cld_and_round_semantics():
     assert math.ceil(L.orc_round_sigdigits(1.0000000000000002, 12)) == 1
     assert L.orc_round_sigdigits(123.456789012345678, 12) == 123.456789012
     assert L.orc_round_sigdigits(0.0, 12) == 0.0
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 7, 50, 1001])
+@pytest.mark.parametrize("p", [0.02, 0.05, 0.5])
+def test_quantile_is_type7(n, p):
+    # the quantile that sets adaptive sub-steps (Statistics.jl quantile!, type 7) equals numpy's
+    # default ('linear') definition
+    import ctypes as C
+    rng = np.random.default_rng([n, int(p * 100)])
+    v = np.exp(rng.normal(5.0, 2.0, n))
+    ref = float(np.quantile(v, p))
+    w = v.copy()
+    got = O.lib().orc_quantile(w.ctypes.data_as(C.POINTER(C.c_double)), C.c_int64(n), C.c_double(p))
+    assert got == pytest.approx(ref, rel=1e-14, abs=0.0)
+
+
+def test_stable_timestep_counts_only_flowing_cells():
+    # surface_kinwave.jl:674-704: cells with Q <= 1e-30 do not count; one flowing cell gives its
+    # own Courant time; none gives 600 s
+    import ctypes as C
+    pd = C.POINTER(C.c_double)
+    alpha = np.array([2.0, 3.0, 4.0])
+    fl = np.array([1000.0, 1200.0, 800.0])
+
+    def dt_of(q, p=0.05):
+        q = np.asarray(q, float)
+        return O.lib().orc_kinwave_stable_timestep(q.ctypes.data_as(pd), alpha.ctypes.data_as(pd),
+                                                   fl.ctypes.data_as(pd), C.c_int64(3), C.c_double(p))
+
+    assert dt_of([0.0, 1e-31, 0.0]) == 600.0
+    one = dt_of([0.0, 5.0, 0.0])
+    assert one == pytest.approx(fl[1] * alpha[1] * 0.6 * 5.0 ** -0.4, rel=1e-14)
+    q = np.array([1.0, 5.0, 2.0])
+    times = fl * alpha * 0.6 * q ** -0.4
+    assert dt_of(q, 0.5) == pytest.approx(float(np.quantile(times, 0.5)), rel=1e-14)

@@ -681,7 +681,9 @@ struct SsfPhys {
     __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
         double* const* Mf = F.Mf;
         double* const* L = F.L;
-        const double dt_s = sw.dts[s];
+        double dt_s;
+        bool first, last;
+        if (!wf_substep(sw, m, s, dt_s, first, last)) return true;
         const double area = L[AREA][slot];
         const double d = L[SOIL_THICKNESS][slot];
         double zi_ssf = Mf[SSF_ZI][e];
@@ -716,8 +718,6 @@ struct SsfPhys {
         Mf[SSF_ZI][e] = zi_new;
         Mf[SSF_STORAGE][e] = L[SY][slot] * (d - zi_new) * area;
         // cumulative fluxes (set_flux_vars! zeroes them at the start of the model step)
-        const bool first = (sw.first + s == 0);
-        const bool last = sw.last_of_step && (s == sw.S - 1);
         double c_tr = (first ? 0.0 : Mf[SSF_TR_CUM][e]) + tr * dt_s;
         double c_rf = (first ? 0.0 : Mf[RCH_FLUX_CUM][e]) + flux * dt_s;
         double c_qin = (first ? 0.0 : Mf[SSF_QIN_CUM][e]) + qin * dt_s;
@@ -790,9 +790,9 @@ struct OverlandPhys {
     __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
         double* const* Mf = F.Mf;
         double* const* L = F.L;
-        const double dt_s = sw.dts[s];
-        const bool first = (sw.first + s == 0);
-        const bool last = sw.last_of_step && (s == sw.S - 1);
+        double dt_s;
+        bool first, last;
+        if (!wf_substep(sw, m, s, dt_s, first, last)) return true;
         if (first && F.mass_balance) Mf[BO_PREV][e] = Mf[OL_STORAGE][e];
         const double sfw = L[SFW][slot];
         double tr = 0.0, qin = 0.0;
@@ -841,9 +841,9 @@ struct RiverPhys {
         double* const* RM = F.RM;
         double* const* R = F.R;
         const int M = F.M;
-        const double dt_s = sw.dts[s];
-        const bool first = (sw.first + s == 0);
-        const bool last = sw.last_of_step && (s == sw.S - 1);
+        double dt_s;
+        bool first, last;
+        if (!wf_substep(sw, m, s, dt_s, first, last)) return true;
         const double len = R[R_LENGTH][slot];
         double qlat;
         if (first) {

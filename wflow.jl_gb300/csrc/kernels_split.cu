@@ -844,7 +844,9 @@ struct SsfSplitPhys {
     __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
         const FFMem Mf{F};
         double* const* L = F.L;
-        const double dt_s = sw.dts[s];
+        double dt_s;
+        bool first, last;
+        if (!wf_substep(sw, m, s, dt_s, first, last)) return true;
         const double area = L[AREA][slot];
         const double d = L[SOIL_THICKNESS][slot];
         double zi_ssf = Mf[SSF_ZI][e];
@@ -927,8 +929,6 @@ struct SsfSplitPhys {
         Mf[SSF_Q][e] = q;
         Mf[SSF_ZI][e] = zi_new;
         Mf[SSF_STORAGE][e] = sy * (d - zi_new) * area;
-        const bool first = (sw.first + s == 0);
-        const bool last = sw.last_of_step && (s == sw.S - 1);
         // cumulative sub-step fluxes: a single sub-step needs no accumulator
         double c_tr = tr * dt_s, c_rf = flux * dt_s, c_qin = qin * dt_s, c_q = q * dt_s, c_ex = exfilt * dt_s,
                c_nf = netflux * area * dt_s;
@@ -1253,9 +1253,15 @@ struct OlWave {
     __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
                                          unsigned long long* qh) {
         const int stride = blockDim.x;
+        bool first = sw.first == 0;
+        if (sw.aflag) {  // adaptive: one sub-step of this member's own size
+            const uint8_t f = sw.aflag[m];
+            if (!(f & WF_SUB_ACTIVE)) return true;
+            first = (f & WF_SUB_FIRST) != 0;
+        }
         wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f};
         for (int s = 0; s < sw.S; ++s) {
-            const float dt_s = sw.dts_f[s];
+            const wff::ff dt_s = sw.aflag ? wff::ff{sw.adt_hi[m], sw.adt_lo[m]} : wff::ff{sw.dts_f[s], 0.0f};
             wff::ff qin;
             if (!wfv::gather<true>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
             if (!x.sfw_pos) qin = {0.0f, 0.0f};
@@ -1280,7 +1286,7 @@ struct OlWave {
         Mh[OL_UH][e] = u.hi;
         Mh[OL_UL][e] = u.lo;
         stm(F, OL_Q, e, qp);
-        if (sw.first != 0) qsum = wff::add(qsum, wff::ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]});
+        if (!first) qsum = wff::add(qsum, wff::ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]});
         Mh[OL_QSUMH][e] = qsum.hi;
         Mh[OL_QSUML][e] = qsum.lo;
         return true;
@@ -1313,17 +1319,23 @@ struct RvWave {
     __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
                                          unsigned long long* qh) {
         const int stride = blockDim.x;
+        bool first = sw.first == 0;
+        if (sw.aflag) {  // adaptive: one sub-step of this member's own size
+            const uint8_t f = sw.aflag[m];
+            if (!(f & WF_SUB_ACTIVE)) return true;
+            first = (f & WF_SUB_FIRST) != 0;
+        }
         wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f}, asum = {0.0f, 0.0f};
         for (int s = 0; s < sw.S; ++s) {
-            const float dt_s = sw.dts_f[s];
+            const wff::ff dt_s = sw.aflag ? wff::ff{sw.adt_hi[m], sw.adt_lo[m]} : wff::ff{sw.dts_f[s], 0.0f};
             wff::ff qin;
             if (!wfv::gather<false>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
             wff::ff ql = x.qlatt;
             if (x.ext < 0.0f) {  // abstraction: qlatt holds the lateral inflow alone
                 const float storage = x.len * (x.alpha * (u.hi * u.hi * u.hi));
-                const float absd = fminf(-x.ext, (storage / dt_s) * 0.80f);
+                const float absd = fminf(-x.ext, (storage / dt_s.hi) * 0.80f);
                 ql = wff::add(ql, wff::mul(x.invlen, -absd));
-                asum = wff::add(asum, wff::two_prod(absd, dt_s));
+                asum = wff::add(asum, wff::mul(dt_s, absd));
             }
             wff::ff un, qn;
             if (qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
@@ -1346,7 +1358,7 @@ struct RvWave {
         RMh[RV_UH][e] = u.hi;
         RMh[RV_UL][e] = u.lo;
         str(F, RV_Q, e, qp);
-        if (sw.first != 0) {
+        if (!first) {
             qsum = wff::add(qsum, wff::ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]});
             asum = wff::add(asum, wff::ff{RMh[RV_ABSH][e], RMh[RV_ABSL][e]});
         }

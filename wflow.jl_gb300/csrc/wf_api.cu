@@ -80,6 +80,11 @@ struct WfHandle {
     cudaEvent_t kev[6] = {};
     double kernel_ms[5] = {0, 0, 0, 0, 0};
     int64_t kernel_calls = 0;
+    // adaptive (Courant) sub-stepping
+    bool adaptive = false;
+    WfAdaptive ad[3] = {};        // WF_ADAPT_SSF, WF_ADAPT_LAND, WF_ADAPT_RIVER
+    int32_t* h_more = nullptr;    // pinned host copy of WfAdaptive::more
+    int64_t last_substeps[3] = {0, 0, 0};
 };
 
 namespace {
@@ -231,6 +236,48 @@ std::vector<double> fixed_substeps(double dt_fixed, double dt) {
         if (v.size() > 1000000) break;
     }
     return v;
+}
+
+// Device state of the adaptive sub-step selection (one per sweep kind); the Courant-time keys
+// are shared, the sweeps run one after the other.
+int alloc_adaptive(WfHandle* h) {
+    const WfRoutingPlan& PL = h->land.plan;
+    const WfRoutingPlan& PR = h->river.plan;
+    const int M = h->M;
+    int rc;
+    unsigned long long* keys = nullptr;
+    if ((rc = dalloc(h, &keys, (size_t)std::max(PL.n_slots, PR.n_slots) * M))) return rc;
+    for (int k = 0; k < 3; ++k) {
+        WfAdaptive& A = h->ad[k];
+        A.kind = k;
+        A.M = M;
+        A.fp32_keys = h->F.split;
+        A.kv_profile = h->cfg.kv_profile;
+        A.p = k == WF_ADAPT_LAND ? 0.02 : 0.05;  // surface_kinwave.jl:374 (land), :638 (river)
+        A.dt = h->cfg.dt;
+        A.alpha = h->cfg.subsurface_alpha;
+        A.n_slots = k == WF_ADAPT_RIVER ? PR.n_slots : PL.n_slots;
+        A.keys = keys;
+        if ((rc = dalloc(h, &A.hist, (size_t)2 * M * 256))) return rc;
+        if ((rc = dalloc(h, &A.prefix, (size_t)2 * M))) return rc;
+        if ((rc = dalloc(h, &A.rank, (size_t)2 * M))) return rc;
+        if ((rc = dalloc(h, &A.count, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.minkey, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.done, 1))) return rc;
+        if ((rc = dalloc(h, &A.t, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.dt_s, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.dt_hi, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.dt_lo, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.flags, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.nsub, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.more, 1))) return rc;
+        CK(cudaMemset(A.hist, 0, (size_t)2 * M * 256 * sizeof(uint32_t)));
+        CK(cudaMemset(A.count, 0, (size_t)M * sizeof(long long)));
+        CK(cudaMemset(A.minkey, 0xFF, (size_t)M * sizeof(unsigned long long)));
+        CK(cudaMemset(A.done, 0, sizeof(uint32_t)));
+    }
+    CK(cudaHostAlloc((void**)&h->h_more, sizeof(int32_t), cudaHostAllocDefault));
+    return WF_OK;
 }
 
 WfLaunchCfg launch_cfg(const WfHandle* h) {
@@ -550,14 +597,20 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
             return fail(WF_ERR_INVALID);
         }
     }
-    // sub-steps (fixed mode)
-    if (c->adaptive_timestep) {
-        set_err(h, WF_ERR_UNSUPPORTED, "adaptive kinematic-wave time stepping is not supported by this build");
-        return fail(WF_ERR_UNSUPPORTED);
+    // sub-steps: fixed sizes, or adaptive (sizes chosen on the device every sub-step; one
+    // sub-step per sweep launch)
+    h->adaptive = c->adaptive_timestep != 0;
+    if (h->adaptive) {
+        if (!(c->subsurface_alpha > 0.0) || !(c->dt > 0.0)) {
+            set_err(h, WF_ERR_INVALID, "adaptive time stepping needs a positive subsurface alpha coefficient and dt");
+            return fail(WF_ERR_INVALID);
+        }
+        h->h_dts_land = h->h_dts_river = h->h_dts_ssf = std::vector<double>{c->dt};
+    } else {
+        h->h_dts_land = fixed_substeps(c->land_dt_fixed, c->dt);
+        h->h_dts_river = fixed_substeps(c->river_dt_fixed, c->dt);
+        h->h_dts_ssf = fixed_substeps(c->subsurface_dt_fixed, c->dt);
     }
-    h->h_dts_land = fixed_substeps(c->land_dt_fixed, c->dt);
-    h->h_dts_river = fixed_substeps(c->river_dt_fixed, c->dt);
-    h->h_dts_ssf = fixed_substeps(c->subsurface_dt_fixed, c->dt);
     if (h->h_dts_land.empty() || h->h_dts_river.empty() || h->h_dts_ssf.empty() || h->h_dts_land.size() > 100000 ||
         h->h_dts_river.size() > 100000 || h->h_dts_ssf.size() > 100000) {
         set_err(h, WF_ERR_INVALID, "invalid fixed kinematic-wave time steps");
@@ -898,7 +951,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     F.mass_balance = c->water_mass_balance;
     F.dt = c->dt;
     F.inv_dt = 1.0 / c->dt;
-    F.ssf_single = F.split && h->h_dts_ssf.size() == 1;
+    F.ssf_single = F.split && !h->adaptive && h->h_dts_ssf.size() == 1;
     F.dt_ssf = h->h_dts_ssf[0];
     F.inv_dt_ssf = 1.0 / h->h_dts_ssf[0];
     F.inv_dt_hi = (float)F.inv_dt;
@@ -917,6 +970,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     h->metrics.max_chain_land = PL.max_len;
     h->metrics.max_chain_river = PR.max_len;
     h->metrics.padding_slots_land = (int32_t)(PL.n_slots - n);
+    if (h->adaptive) CKR(alloc_adaptive(h));
     CK(cudaDeviceSynchronize());
 #undef CKR
     *out = h;
@@ -930,6 +984,7 @@ void wf_destroy(WfHandle* h) {
     if (h->graph) cudaGraphDestroy(h->graph);
     for (void* p : h->allocs) cudaFree(p);
     if (h->host_pinned) cudaFreeHost(h->host_pinned);
+    if (h->h_more) cudaFreeHost(h->h_more);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (auto& e : h->kev)
@@ -1227,7 +1282,10 @@ int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_
 
 namespace {
 
-// Enqueue one model step on the handle's stream.
+constexpr int64_t kMaxAdaptiveSubsteps = 100000;
+
+// Enqueue one model step on the handle's stream (with adaptive sub-steps the host waits for
+// the device after every sub-step, see below).
 int enqueue_step(WfHandle* h, int64_t* launches) {
     const WfLaunchCfg lc = launch_cfg(h);
     const bool split = h->cfg.form == WF_FORM_SPLIT;
@@ -1299,8 +1357,66 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         ++nl;
         return WF_OK;
     };
+    // adaptive sub-steps: the size of a sub-step follows from the state the previous one left
+    // (a quantile or minimum over the whole graph), so every sub-step is its own launch, preceded
+    // by the selection kernels and followed by a host read of whether a member needs another
+    auto adaptive = [&](DevGraphAlloc& G, const WfDevGraph& g, int kind) -> int {
+        WfAdaptive& A = h->ad[kind];
+        CK(cudaMemsetAsync(A.t, 0, (size_t)h->M * sizeof(double), h->stream));
+        CK(cudaMemsetAsync(A.nsub, 0, (size_t)h->M * sizeof(int32_t), h->stream));
+        const bool slim = split && kind != WF_ADAPT_SSF;
+        int64_t it = 0;
+        while (true) {
+            if (it >= kMaxAdaptiveSubsteps)
+                return set_err(h, WF_ERR_INVALID, "adaptive sub-stepping needed more than 100000 sub-steps in one step");
+            CK(wf_adaptive_substep(h->F, A, lc));
+            nl += (kind == WF_ADAPT_SSF ? 1 : (A.fp32_keys ? 4 : 8)) + 1;
+            WfSweep sw{};
+            sw.S = 1;
+            sw.epoch0 = 1;
+            sw.dt = h->cfg.dt;
+            sw.dts = A.dt_s;
+            sw.adt = A.dt_s;
+            sw.adt_hi = A.dt_hi;
+            sw.adt_lo = A.dt_lo;
+            sw.aflag = A.flags;
+            sw.wait_ns = h->wait_ns;
+            sw.wait_offset = h->wait_offset;
+            CK(cudaMemsetAsync(G.ticket, 0, sizeof(unsigned long long), h->stream));
+            cudaError_t e;
+            if (slim) {
+                CK(cudaMemsetAsync(G.end_q, 0xFF, (size_t)G.plan.n_chains * h->M * G.s_cap * sizeof(double),
+                                   h->stream));
+                e = kind == WF_ADAPT_LAND ? wf_split_overland_wave(h->F, g, sw, lc) : wf_split_river_wave(h->F, g, sw, lc);
+            } else {
+                CK(cudaMemsetAsync(G.flags, 0, (size_t)G.plan.n_chains * h->M * sizeof(uint32_t), h->stream));
+                if (kind == WF_ADAPT_SSF) e = split ? wf_split_ssf(h->F, g, sw, lc) : wf_fp64_ssf(h->F, g, sw, lc);
+                else if (kind == WF_ADAPT_LAND) e = wf_fp64_overland(h->F, g, sw, lc);
+                else e = wf_fp64_river(h->F, g, sw, lc);
+            }
+            CK(e);
+            ++nl;
+            ++it;
+            CK(cudaMemcpyAsync(h->h_more, A.more, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (!*h->h_more) break;
+        }
+        h->last_substeps[kind] = it;
+        if (slim) {
+            CK(kind == WF_ADAPT_LAND ? wf_split_overland_post(h->F, g, lc) : wf_split_river_post(h->F, g, lc));
+            ++nl;
+        }
+        return WF_OK;
+    };
     int rc;
-    if (split) {
+    if (h->adaptive) {
+        if ((rc = adaptive(h->land, gl, WF_ADAPT_SSF))) return rc;
+        mark(2);
+        if ((rc = adaptive(h->land, gl, WF_ADAPT_LAND))) return rc;
+        mark(3);
+        if (h->nr > 0 && (rc = adaptive(h->river, gr, WF_ADAPT_RIVER))) return rc;
+        mark(4);
+    } else if (split) {
         if (h->F.ssf_single) rc = wave(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0);
         else rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0);
         if (rc) return rc;
@@ -1339,7 +1455,7 @@ int run_step(WfHandle* h) {
         if (h->cfg.form == WF_FORM_SPLIT) CK(wf_split_sync_u(h->F, launch_cfg(h)));
         h->u_dirty = false;
     }
-    if (h->tuning.use_graph) {
+    if (h->tuning.use_graph && !h->adaptive) {
         if (!h->graph_valid) {
             if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
             if (h->graph) cudaGraphDestroy(h->graph);
@@ -1368,6 +1484,12 @@ int run_step(WfHandle* h) {
     h->metrics.steps += 1;
     h->metrics.cell_steps += h->n * h->M;
     h->metrics.kernel_launches += launches;
+    if (h->adaptive) {
+        h->metrics.substeps_subsurface += h->last_substeps[WF_ADAPT_SSF];
+        h->metrics.substeps_land += h->last_substeps[WF_ADAPT_LAND];
+        h->metrics.substeps_river += h->nr > 0 ? h->last_substeps[WF_ADAPT_RIVER] : 0;
+        return WF_OK;
+    }
     h->metrics.substeps_land += (int64_t)h->h_dts_land.size();
     h->metrics.substeps_river += (int64_t)h->h_dts_river.size();
     h->metrics.substeps_subsurface += (int64_t)h->h_dts_ssf.size();
@@ -1516,6 +1638,9 @@ int enqueue_step_static(WfHandle* h, unsigned char* base, int64_t* launches) {
 
 extern "C" int32_t wf_step_static(WfHandle* h) {
     if (!h) return WF_ERR_INVALID;
+    if (h->adaptive)
+        return set_err(h, WF_ERR_UNSUPPORTED,
+                       "wf_step_static: adaptive sub-stepping synchronises with the host every sub-step; use wf_step");
     const size_t need = std::max(static_need(h->land, h->M), h->nr > 0 ? static_need(h->river, h->M) : (size_t)0);
     if (need > (size_t)WF_STATIC_SCRATCH_BYTES) {
         char msg[256];

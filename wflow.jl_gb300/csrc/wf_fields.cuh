@@ -164,7 +164,68 @@ struct WfSweep {
     float dts_f[16];      // FP32 copy of the first 16 sub-step sizes (split form's slim walkers)
     uint64_t wait_ns;     // spin-wait budget per wait [ns]
     uint32_t wait_offset; // test hook: added to awaited epochs (0 in production)
+    // adaptive sub-stepping (one sub-step per launch, sizes per member); null for fixed steps
+    const double* adt;    // [M] sub-step of each member
+    const float* adt_hi;  // [M] the same as a double-FP32 pair (split form)
+    const float* adt_lo;
+    const uint8_t* aflag; // [M] WF_SUB_* bits
 };
+
+// Per-member flags of an adaptive sub-step
+#define WF_SUB_ACTIVE 1  // the member takes this sub-step (it has not reached the end of the step)
+#define WF_SUB_FIRST 2   // first sub-step of the model step
+#define WF_SUB_LAST 4    // last sub-step of the model step
+
+#ifdef __CUDACC__
+// Sub-step s of a sweep launch for member m: its size and whether it is the first or the last of
+// the model step. False when the member has already reached the end of the step (adaptive
+// sub-steps end at different times for different members).
+__device__ __forceinline__ bool wf_substep(const WfSweep& sw, int m, int s, double& dt_s, bool& first, bool& last) {
+    if (sw.aflag) {
+        const uint8_t f = sw.aflag[m];
+        dt_s = sw.adt[m];
+        first = (f & WF_SUB_FIRST) != 0;
+        last = (f & WF_SUB_LAST) != 0;
+        return (f & WF_SUB_ACTIVE) != 0;
+    }
+    dt_s = sw.dts[s];
+    first = (sw.first + s == 0);
+    last = sw.last_of_step && (s == sw.S - 1);
+    return true;
+}
+#endif
+
+// Adaptive (Courant) sub-step selection of one sweep kind: the Courant time of every cell, the
+// order statistics of the quantile (or the minimum for the subsurface) per member, and each
+// member's progress through the model step.
+struct WfAdaptive {
+    int32_t kind;           // WF_ADAPT_SSF, WF_ADAPT_LAND or WF_ADAPT_RIVER
+    int32_t M;
+    int32_t fp32_keys;      // keys are FP32 bit patterns (split form), else FP64
+    int32_t kv_profile;
+    double p;               // quantile probability (land 0.02, river 0.05)
+    double dt;              // model step
+    double alpha;           // subsurface stability coefficient
+    int64_t n_slots;        // slots of the swept graph
+    unsigned long long* keys;    // [n_slots * M] Courant time bit patterns, all ones for no value
+    uint32_t* hist;         // [2][M][256] digit histogram of the current pass
+    unsigned long long* prefix;  // [2][M] digits selected so far (then the two order statistics)
+    long long* rank;        // [2][M] rank left to select within the prefix
+    long long* count;       // [M] cells with a Courant time
+    unsigned long long* minkey;  // [M] minimum (subsurface)
+    uint32_t* done;         // blocks finished in the current pass
+    double* t;              // [M] time reached within the model step
+    double* dt_s;           // [M] current sub-step
+    float* dt_hi;           // [M] double-FP32 copy
+    float* dt_lo;
+    uint8_t* flags;         // [M] WF_SUB_* bits of the current sub-step
+    int32_t* nsub;          // [M] sub-steps taken in this model step
+    int32_t* more;          // 1 when some member has not reached the end of the step
+};
+
+#define WF_ADAPT_SSF 0
+#define WF_ADAPT_LAND 1
+#define WF_ADAPT_RIVER 2
 
 // Device status codes (OR-ed bits)
 #define WF_DEV_SPIN_TIMEOUT 1

@@ -20,9 +20,6 @@ cudaError_t wf_fp64_overland(const WfDevFields& F, const WfDevGraph& g, const Wf
 cudaError_t wf_fp64_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
 cudaError_t wf_fp64_balance(const WfDevFields& F, const WfLaunchCfg& c);
 cudaError_t wf_fp64_vwc(const WfDevFields& F, int layer, double* out, const WfLaunchCfg& c);
-// Courant sub-step of a kinematic-wave sweep (adaptive mode): writes dt to *dt_out.
-cudaError_t wf_fp64_stable_dt(const WfDevFields& F, int which /*0 land 1 river 2 ssf*/, double* scratch,
-                              int64_t* count, double* dt_out, const WfLaunchCfg& c);
 
 // FP32/FP64 split form (kernels_split.cu)
 cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c);
@@ -38,6 +35,10 @@ cudaError_t wf_split_overland_post(const WfDevFields& F, const WfDevGraph& g, co
 cudaError_t wf_split_river_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
 cudaError_t wf_split_sync_u(const WfDevFields& F, const WfLaunchCfg& c);
 cudaError_t wf_split_vwc(const WfDevFields& F, int layer, double* out, const WfLaunchCfg& c);
+
+// Adaptive sub-stepping (kernels_adaptive.cu): size and flags of every member's next sub-step
+// of the sweep A.kind, from the current state; sets *A.more when a further sub-step follows.
+cudaError_t wf_adaptive_substep(const WfDevFields& F, const WfAdaptive& A, const WfLaunchCfg& c);
 
 // gather/scatter between the external (land/river) order and the slot order
 cudaError_t wf_gather_ext(const double* src_ext, double* dst_slots, const int64_t* node_of_slot, int64_t slots,

@@ -20,11 +20,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units of the step library and their floating-point contraction policy:
 # FP64 plain-form kernels are compiled without implicit FMA contraction so that every
 # operation rounds like the reference's scalar Float64 code; the split form contracts freely.
+# The adaptive sub-step selection serves both forms and follows the FP64 policy.
 CUDA_UNITS = [
     ("wf_api.cu", []),
     ("wf_plan.cpp", None),
     ("kernels_fp64.cu", ["--fmad=false"]),
     ("kernels_split.cu", []),
+    ("kernels_adaptive.cu", ["--fmad=false"]),
 ]
 
 
