@@ -46,8 +46,10 @@ __device__ __forceinline__ unsigned long long courant_key(const WfDevFields& F, 
     const int64_t node = river ? F.river_node_of_slot[slot] : F.land_node_of_slot[slot];
     if (node < 0) return NO_KEY;
     if (A.fp32_keys) {
+        // the flow test on the double-FP32 discharge, which holds the floor values exactly
         const float q = river ? F.RMh[RV_Q][e] : F.Mh[OL_Q][e];
-        if (!(q > (float)KIN_WAVE_MIN_FLOW)) return NO_KEY;
+        const float q_lo = river ? F.RMl[RV_Q][e] : F.Ml[OL_Q][e];
+        if (!((double)q + (double)q_lo > KIN_WAVE_MIN_FLOW)) return NO_KEY;
         const float alpha = river ? F.Rf[R_ALPHA][slot] : F.Lf[OL_ALPHA][slot];
         const float dx = river ? F.Rf[R_LENGTH][slot] : F.Lf[FLOW_LENGTH][slot];
         const float c = 1.0f / (alpha * (float)BETA * powf(q, (float)BETA - 1.0f));

@@ -1002,15 +1002,24 @@ struct SsfSplitPhys {
 // from the previous u when it lies below that bound) until |du| <= 3e-7 u, then one Newton
 // correction with the residual evaluated in double-FP32, which leaves |f(u)| at about 1e-13 of
 // cterm. Q = u^5 is formed from the correction du as v^5 - 5 v^4 du (the dropped terms are of
-// relative size (du/v)^2). Results below the reference's floor (Q = 1e-30, u = QROOT) are
-// raised to it, as the reference does.
+// relative size (du/v)^2). Results below the reference's floor (u = QROOT) are raised to it, as
+// the reference does.
+//
+// The floor discharge QROOT^5 is 9.999999999999968e-31, just below KIN_WAVE_MIN_FLOW, so a cell
+// whose solve ended at the floor does not count as flowing in the Courant quantile of adaptive
+// sub-stepping; a floored cell whose next solve stops at once (kw_node_ff) keeps
+// pow(q, 0.2)^5 = 1.000000000000002e-30, just above it, and counts from then on. Both values
+// are held exactly as double-FP32 pairs (the low parts are FP32 subnormals).
+__device__ __forceinline__ wff::ff q_floor() { return {__uint_as_float(0x0da24260u), __uint_as_float(0x802287aeu)}; }
+__device__ __forceinline__ wff::ff q_rest() { return {__uint_as_float(0x0da24260u), __uint_as_float(0x802287abu)}; }
+
 __device__ __forceinline__ void kw_solve_ff(wff::ff cterm, wff::ff dt_dx, float alpha, float u_prev, wff::ff& u_out,
                                             wff::ff& q_out) {
     const float QR = (float)KIN_WAVE_MIN_FLOW_QROOT;
     const float floor_c = alpha * (QR * QR * QR);
     if (!(cterm.hi > floor_c)) {
         u_out = {QR, 0.0f};
-        q_out = {(float)KIN_WAVE_MIN_FLOW, 0.0f};
+        q_out = q_floor();
         return;
     }
     const float a = dt_dx.hi, b = alpha, c = cterm.hi;
@@ -1035,10 +1044,36 @@ __device__ __forceinline__ void kw_solve_ff(wff::ff cterm, wff::ff dt_dx, float 
     wff::ff q = wff::add(v5, wff::mul(wff::mul(v2, v2), -5.0f * dv));
     if (!(u.hi > QR)) {
         u = {QR, 0.0f};
-        q = {(float)KIN_WAVE_MIN_FLOW, 0.0f};
+        q = q_floor();
     }
     u_out = u;
     q_out = q;
+}
+
+// One kinematic-wave node update (surface_process.jl:24-70) from the upstream inflow qin, the
+// previous discharge qp (u = qp^0.2) and the lateral inflow ql. As in the reference: no flow at
+// all gives Q = 0; a cell with flow whose residual at the previous u is already within the
+// reference's absolute tolerance (|f| <= 1e-12) keeps its discharge (its Newton loop stops
+// before the first update); otherwise the root of the solve.
+__device__ __forceinline__ void kw_node_ff(wff::ff qin, wff::ff qp, wff::ff ql, wff::ff u, wff::ff dt_dx,
+                                           wff::ff dt_s, float alpha, wff::ff& un, wff::ff& qn) {
+    if (qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
+        un = {0.0f, 0.0f};
+        qn = {0.0f, 0.0f};
+        return;
+    }
+    if (qp.hi > 0.0f) {
+        const wff::ff f0 = wff::sub(wff::mul(dt_dx, wff::sub(qp, qin)), wff::mul(ql, dt_s));
+        if (fabsf(f0.hi) <= 1.0e-12f) {
+            const wff::ff fl = q_floor();
+            un = u;
+            qn = (qp.hi == fl.hi && qp.lo == fl.lo) ? q_rest() : qp;
+            return;
+        }
+    }
+    const wff::ff u3 = wff::mul(wff::mul(u, u), u);
+    const wff::ff cterm = wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, alpha), wff::mul(ql, dt_s)));
+    kw_solve_ff(cterm, dt_dx, alpha, u.hi, un, qn);
 }
 
 // q^0.2 for a discharge set from outside the step (BMI set_value, restart).
@@ -1266,16 +1301,7 @@ struct OlWave {
             if (!wfv::gather<true>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
             if (!x.sfw_pos) qin = {0.0f, 0.0f};
             wff::ff un, qn;
-            if (qin.hi == 0.0f && qp.hi == 0.0f && x.qlat.hi == 0.0f) {
-                un = {0.0f, 0.0f};
-                qn = {0.0f, 0.0f};
-            } else {
-                const wff::ff dt_dx = wff::mul(x.invdx, dt_s);
-                const wff::ff u3 = wff::mul(wff::mul(u, u), u);
-                const wff::ff cterm =
-                    wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, x.alpha), wff::mul(x.qlat, dt_s)));
-                kw_solve_ff(cterm, dt_dx, x.alpha, u.hi, un, qn);
-            }
+            kw_node_ff(qin, qp, x.qlat, u, wff::mul(x.invdx, dt_s), dt_s, x.alpha, un, qn);
             u = un;
             qp = qn;
             qh[s * stride] = wff::pack(qn);
@@ -1338,16 +1364,7 @@ struct RvWave {
                 asum = wff::add(asum, wff::mul(dt_s, absd));
             }
             wff::ff un, qn;
-            if (qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
-                un = {0.0f, 0.0f};
-                qn = {0.0f, 0.0f};
-            } else {
-                const wff::ff dt_dx = wff::mul(x.invlen, dt_s);
-                const wff::ff u3 = wff::mul(wff::mul(u, u), u);
-                const wff::ff cterm =
-                    wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, x.alpha), wff::mul(ql, dt_s)));
-                kw_solve_ff(cterm, dt_dx, x.alpha, u.hi, un, qn);
-            }
+            kw_node_ff(qin, qp, ql, u, wff::mul(x.invlen, dt_s), dt_s, x.alpha, un, qn);
             u = un;
             qp = qn;
             qh[s * stride] = wff::pack(qn);
