@@ -38,6 +38,14 @@ WORKLOADS = {
     "single_64_daily": (64, 1000.0, 86400.0, 1, 365),
     # small case of the ensemble workload for multi-pass profiler captures (1/16 of the cells)
     "ensemble64_256_hourly": (256, 250.0, 3600.0, 64, 10),
+    # one 4096 x 4096 domain at 100 m, hourly, adaptive (Courant) sub-steps, precipitation x3
+    "large_4096_adaptive_hourly": (4096, 100.0, 3600.0, 1, 240),
+    # uneven batch: 200 independent catchments of 10^3 - 10^6 cells (log-uniform), daily
+    "ragged200_daily": (0, 1000.0, 86400.0, 1, 365),
+}
+WORKLOAD_OPTIONS = {
+    "large_4096_adaptive_hourly": {"adaptive": True, "precip_scale": 3.0},
+    "ragged200_daily": {"ragged": 200},
 }
 
 # Algorithmic bytes per cell (and member) of one launch of each kernel: the fields each kernel
@@ -118,14 +126,20 @@ def build_workload(name, form, seed=1):
     from wflow_gb300 import abi, synthetic
 
     side, cell, dt, members, _ = WORKLOADS[name]
+    opts = WORKLOAD_OPTIONS.get(name, {})
     t0 = time.time()
-    dom = synthetic.make_domain(side, cell, seed=seed)
+    if opts.get("ragged"):
+        dom = synthetic.make_ragged(opts["ragged"], seed=seed, cell_size=cell, log10_min=3.0, log10_max=6.0)
+    else:
+        dom = synthetic.make_domain(side, cell, seed=seed)
     params = dom.params
-    cfg = synthetic.make_config(dt, n_members=members, form=form, per_member_soil=members > 1)
+    cfg = synthetic.make_config(dt, n_members=members, form=form, per_member_soil=members > 1,
+                                adaptive=opts.get("adaptive", False))
     pfac = np.ones(members)
     if members > 1:
         kv0, f, pfac = synthetic.perturb_members(dom.params, members, seed=seed)
         params = dict(dom.params, kv_0=kv0, f=f)
+    pfac = pfac * opts.get("precip_scale", 1.0)
     log(f"[bench] domain {name}: {dom.n_land} land cells, {dom.n_river} river cells, members {members}, "
         f"built in {time.time() - t0:.1f}s")
     return dom, params, cfg, pfac
@@ -136,7 +150,7 @@ def member_forcing(step, dt, n, members, pfac, seed=1):
 
     P, PET, T = synthetic.forcing(step, dt, n, seed=seed)
     if members == 1:
-        return P, PET, T
+        return (P * pfac[0] if pfac[0] != 1.0 else P), PET, T
     return (np.concatenate([P * pfac[m] for m in range(members)]), np.tile(PET, members), np.tile(T, members))
 
 
@@ -194,7 +208,8 @@ def run_gpu(args):
         torch.distributed.barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    launches0 = model.metrics()["kernel_launches"]
+    mt0 = model.metrics()
+    launches0 = mt0["kernel_launches"]
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -208,7 +223,9 @@ def run_gpu(args):
     model.synchronize()
     torch.cuda.synchronize()
     elapsed_ms = ev0.elapsed_time(ev1)
-    launches = model.metrics()["kernel_launches"] - launches0
+    mt1 = model.metrics()
+    launches = mt1["kernel_launches"] - launches0
+    substeps = {k: (mt1["substeps_" + k] - mt0["substeps_" + k]) / K for k in ("land", "river", "subsurface")}
     clk = clocks.stop()
     if ws > 1:
         t = torch.tensor([elapsed_ms], device=dev)
@@ -270,9 +287,10 @@ def run_gpu(args):
         "dtype": "f64" if form == abi.WF_FORM_FP64 else "f32+f64",
         "data": "synthetic (seeded fractal DEM, D8, SBM parameters and forcing of the benchmark configuration)",
         "config": {"workload": args.workload, "cells": n, "members": members, "river_cells": dom.n_river,
-                   "dt_s": dt, "form": args.form, "substeps": {"land": int(round(dt / min(dt, 3600.0))),
-                                                               "river": int(np.ceil(dt / 900.0)),
-                                                               "subsurface": 1},
+                   "dt_s": dt, "form": args.form,
+                   "substeps_per_step": substeps,
+                   "adaptive_substeps": bool(cfg.adaptive_timestep),
+                   "catchments": len(dom.outlets),
                    "l2": f"model state {state_gb:.1f} GB on the device >> 129 MB L2, no flush needed",
                    "chains_land": mt["n_chains_land"], "max_chain_land": mt["max_chain_land"],
                    "max_chain_river": mt["max_chain_river"], "parallelism": f"replicas{ws}",
@@ -294,7 +312,7 @@ def run_gpu(args):
     algo = ALGO_BYTES_SPLIT if form == abi.WF_FORM_SPLIT else ALGO_BYTES_FP64
     bytes_launch = algo[dom_k] * cells
     if dom_k == "river":
-        bytes_launch = algo[dom_k] * dom.n_river * members * int(np.ceil(dt / 900.0))
+        bytes_launch = algo[dom_k] * dom.n_river * members * substeps["river"]
     achieved = bytes_launch / (kt[dom_k] / 1e3) / 1e9 if kt[dom_k] > 0 else 0.0
     result["roofline"] = {"kernel": dom_k, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": traffic_from_profiles(dom_k, args.workload),
@@ -302,7 +320,7 @@ def run_gpu(args):
     # ---- the FP64 plain form on the same workload and forcing: throughput ratio and the split
     # form's error against it (the FP64 form reproduces the FP64 oracle bit for bit)
     if form == abi.WF_FORM_SPLIT and not args.no_fp64_leg:
-        result.update(fp64_leg(args, model, dom, params, resident, W, K, dt, members, n, dev))
+        result.update(fp64_leg(args, cfg, dom, params, resident, W, K, dt, members, n, dev))
         result["split_over_fp64"] = value / result["fp64_plain"]["value"]
     model.close()
     if rank == 0:
@@ -312,16 +330,19 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-def fp64_leg(args, split_model, dom, params, resident, W, K, dt, members, n, dev):
+def fp64_leg(args, cfg, dom, params, resident, W, K, dt, members, n, dev):
     """Time the FP64 plain form on the same resident forcing (fewer steps: it is slower), then
     replay both forms over the same steps from the same cold state and compare outlet discharge
     and the split form's land-balance closure."""
+    import copy
+
     import torch
 
-    from wflow_gb300 import abi, synthetic
+    from wflow_gb300 import abi
     from wflow_gb300.model import Model
 
-    cfg64 = synthetic.make_config(dt, n_members=members, form=abi.WF_FORM_FP64, per_member_soil=members > 1)
+    cfg64 = copy.copy(cfg)
+    cfg64.form = abi.WF_FORM_FP64
     m64 = Model(cfg64, dom, params=params, device=dev.index or 0)
     stream = torch.cuda.ExternalStream(m64.stream(), device=dev)
     k64 = max(2, min(K, 5))
@@ -343,7 +364,8 @@ def fp64_leg(args, split_model, dom, params, resident, W, K, dt, members, n, dev
     ms64 = ev0.elapsed_time(ev1)
     m64.close()
     # accuracy: both forms from the cold state over the same steps
-    cfg_s = synthetic.make_config(dt, n_members=members, form=abi.WF_FORM_SPLIT, per_member_soil=members > 1)
+    cfg_s = copy.copy(cfg)
+    cfg_s.form = abi.WF_FORM_SPLIT
     a = Model(cfg64, dom, params=params, device=dev.index or 0)
     b_ = Model(cfg_s, dom, params=params, device=dev.index or 0)
     worst_q = 0.0
@@ -402,7 +424,7 @@ def cpu_baseline(args, steps=None):
     side, cell, dt, members, _ = WORKLOADS[args.workload]
     if members > 1:  # bounded sample: the first member of the ensemble (cost is linear in members)
         from wflow_gb300 import synthetic
-        cfg = synthetic.make_config(dt, n_members=1, form=abi.WF_FORM_FP64)
+        cfg = synthetic.make_config(dt, n_members=1, form=abi.WF_FORM_FP64, adaptive=bool(cfg.adaptive_timestep))
         params = dom.params
         pfac = pfac[:1]
         members = 1
@@ -425,6 +447,7 @@ def cpu_baseline(args, steps=None):
             break
     el = time.perf_counter() - t0
     return {"value": n * members * done / el, "unit": "cell-timesteps/s", "cores": threads, "kind": "port",
+            "cells": n * members,
             "sample": f"{done} steps of {n * members} cells of the {args.workload} workload "
                       f"({'first member of the ensemble, ' if WORKLOADS[args.workload][3] > 1 else ''}"
                       f"after 1 warm-up step), {el:.1f} s"}
@@ -449,7 +472,7 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded), same workload as the GPU arm",
-        "config": {"workload": args.workload, "cells": side * side, "members": members, "dt_s": dt,
+        "config": {"workload": args.workload, "cells": cb["cells"], "members": members, "dt_s": dt,
                    "form": "fp64 (the reference's arithmetic)"},
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": "cell-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -51,7 +51,7 @@ def test_static_step_matches_step(gpu_lib, form, dt):
 
 
 def test_static_step_rejects_models_beyond_the_scratch(gpu_lib):
-    # daily steps with 900 s river sub-steps: 96 published discharges per river chain end and
+    # daily steps with 3600 s overland sub-steps: 24 published discharges per land chain end and
     # member in one launch
     dom = synthetic.make_domain(96, 1000.0, seed=6)
     members = 32
@@ -63,8 +63,9 @@ def test_static_step_rejects_models_beyond_the_scratch(gpu_lib):
         slots = chains * members
         return 256 + (slots * 4 + 255) // 256 * 256 + slots * substeps * 8
 
-    # land launches carry up to 24 overland sub-steps (3600 s), river launches 96 (900 s)
-    need_max = max(need(m["n_chains_land"], 24), need(m["n_chains_river"], 96))
+    # land launches carry 24 overland sub-steps (3600 s), river launches 32 of the 96 (900 s):
+    # the FP64 walker takes at most 32 sub-steps per launch
+    need_max = max(need(m["n_chains_land"], 24), need(m["n_chains_river"], 32))
     assert need_max > abi.WF_STATIC_SCRATCH_BYTES, need_max
     rc = model.lib.wf_step_static(model.h)
     assert rc == abi.WF_ERR_UNSUPPORTED

@@ -17,6 +17,8 @@
 // kernels_fp64.cu for the reference line citations of each function).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "wf_fields.cuh"
 #include "wf_kernels.h"
 #include "wf_launch.cuh"
@@ -1054,26 +1056,42 @@ __device__ __forceinline__ void kw_solve_ff(wff::ff cterm, wff::ff dt_dx, float 
 // previous discharge qp (u = qp^0.2) and the lateral inflow ql. As in the reference: no flow at
 // all gives Q = 0; a cell with flow whose residual at the previous u is already within the
 // reference's absolute tolerance (|f| <= 1e-12) keeps its discharge (its Newton loop stops
-// before the first update); otherwise the root of the solve.
-__device__ __forceinline__ void kw_node_ff(wff::ff qin, wff::ff qp, wff::ff ql, wff::ff u, wff::ff dt_dx,
-                                           wff::ff dt_s, float alpha, wff::ff& un, wff::ff& qn) {
-    if (qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
+// before the first update); otherwise the root of the solve. The solve is evaluated in every
+// case and the early-stop test beside it, so that the test does not lengthen the chain's
+// critical path.
+//
+// The early stop matters where a cell's discharge sits at or near the 1e-30 floor: it decides
+// whether the cell counts in the Courant quantile of adaptive sub-stepping, so the adaptive
+// sweeps apply it (ADAPT); with fixed sub-steps it changes discharges of about 1e-13 m3/s and
+// below only, and the fixed sweeps skip it (as well as the per-member sub-step sizes) to keep
+// their registers, and so their resident warps, at the fixed path's need. `DT` is float (fixed
+// sub-step, exact in FP32) or wff::ff (adaptive sub-step).
+__device__ __forceinline__ wff::ff mul_dt(wff::ff a, float dt) { return wff::mul(a, dt); }
+__device__ __forceinline__ wff::ff mul_dt(wff::ff a, wff::ff dt) { return wff::mul(a, dt); }
+
+template <bool ADAPT, class DT>
+__device__ __forceinline__ void kw_node_ff(wff::ff qin, wff::ff qp, wff::ff ql, wff::ff u, wff::ff dt_dx, DT dt_s,
+                                           float alpha, wff::ff& un, wff::ff& qn) {
+    if (!ADAPT && qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
         un = {0.0f, 0.0f};
         qn = {0.0f, 0.0f};
         return;
     }
-    if (qp.hi > 0.0f) {
-        const wff::ff f0 = wff::sub(wff::mul(dt_dx, wff::sub(qp, qin)), wff::mul(ql, dt_s));
-        if (fabsf(f0.hi) <= 1.0e-12f) {
+    const wff::ff u3 = wff::mul(wff::mul(u, u), u);
+    const wff::ff cterm = wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, alpha), mul_dt(ql, dt_s)));
+    kw_solve_ff(cterm, dt_dx, alpha, u.hi, un, qn);
+    if (ADAPT) {
+        const wff::ff f0 = wff::sub(wff::mul(dt_dx, wff::sub(qp, qin)), mul_dt(ql, dt_s));
+        if (qp.hi > 0.0f && fabsf(f0.hi) <= 1.0e-12f) {
             const wff::ff fl = q_floor();
             un = u;
             qn = (qp.hi == fl.hi && qp.lo == fl.lo) ? q_rest() : qp;
-            return;
+        }
+        if (qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
+            un = {0.0f, 0.0f};
+            qn = {0.0f, 0.0f};
         }
     }
-    const wff::ff u3 = wff::mul(wff::mul(u, u), u);
-    const wff::ff cterm = wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, alpha), wff::mul(ql, dt_s)));
-    kw_solve_ff(cterm, dt_dx, alpha, u.hi, un, qn);
 }
 
 // q^0.2 for a discharge set from outside the step (BMI set_value, restart).
@@ -1264,7 +1282,9 @@ struct SsfWave {
 };
 
 // Overland flow (surface_process.jl:24-70 per node, routing/surface_kinwave.jl sub-steps) in
-// double-FP32: discharge, u = Q^0.2 and the lateral inflow are pairs of FP32 arrays.
+// double-FP32: discharge, u = Q^0.2 and the lateral inflow are pairs of FP32 arrays. ADAPT: one
+// sub-step per launch of each member's own (adaptive) size.
+template <bool ADAPT>
 struct OlWave {
     WfDevFields F;
     WfDevGraph g;
@@ -1289,24 +1309,27 @@ struct OlWave {
                                          unsigned long long* qh) {
         const int stride = blockDim.x;
         bool first = sw.first == 0;
-        if (sw.aflag) {  // adaptive: one sub-step of this member's own size
+        if (ADAPT) {
             const uint8_t f = sw.aflag[m];
             if (!(f & WF_SUB_ACTIVE)) return true;
             first = (f & WF_SUB_FIRST) != 0;
         }
         wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f};
         for (int s = 0; s < sw.S; ++s) {
-            const wff::ff dt_s = sw.aflag ? wff::ff{sw.adt_hi[m], sw.adt_lo[m]} : wff::ff{sw.dts_f[s], 0.0f};
+            using DT = typename std::conditional<ADAPT, wff::ff, float>::type;
+            DT dt_s;
+            if constexpr (ADAPT) dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
+            else dt_s = sw.dts_f[s];
             wff::ff qin;
             if (!wfv::gather<true>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
             if (!x.sfw_pos) qin = {0.0f, 0.0f};
             wff::ff un, qn;
-            kw_node_ff(qin, qp, x.qlat, u, wff::mul(x.invdx, dt_s), dt_s, x.alpha, un, qn);
+            kw_node_ff<ADAPT>(qin, qp, x.qlat, u, mul_dt(x.invdx, dt_s), dt_s, x.alpha, un, qn);
             u = un;
             qp = qn;
             qh[s * stride] = wff::pack(qn);
             if (is_end) wfv::publish(g, chain, m, s, qn);
-            qsum = wff::add(qsum, wff::mul(qn, dt_s));
+            qsum = wff::add(qsum, mul_dt(qn, dt_s));
         }
         float* const* Mh = F.Mh;
         Mh[OL_UH][e] = u.hi;
@@ -1321,7 +1344,8 @@ struct OlWave {
 
 // River flow (surface_process.jl:24-70 per node, routing/river_kinwave.jl sub-steps) in
 // double-FP32, with the abstraction of a negative external inflow limited to 80 % of the
-// storage.
+// storage. ADAPT as for OlWave.
+template <bool ADAPT>
 struct RvWave {
     WfDevFields F;
     WfDevGraph g;
@@ -1346,30 +1370,39 @@ struct RvWave {
                                          unsigned long long* qh) {
         const int stride = blockDim.x;
         bool first = sw.first == 0;
-        if (sw.aflag) {  // adaptive: one sub-step of this member's own size
+        if (ADAPT) {
             const uint8_t f = sw.aflag[m];
             if (!(f & WF_SUB_ACTIVE)) return true;
             first = (f & WF_SUB_FIRST) != 0;
         }
         wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f}, asum = {0.0f, 0.0f};
         for (int s = 0; s < sw.S; ++s) {
-            const wff::ff dt_s = sw.aflag ? wff::ff{sw.adt_hi[m], sw.adt_lo[m]} : wff::ff{sw.dts_f[s], 0.0f};
+            using DT = typename std::conditional<ADAPT, wff::ff, float>::type;
+            DT dt_s;
+            float dt_f;
+            if constexpr (ADAPT) {
+                dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
+                dt_f = dt_s.hi;
+            } else {
+                dt_s = sw.dts_f[s];
+                dt_f = dt_s;
+            }
             wff::ff qin;
             if (!wfv::gather<false>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
             wff::ff ql = x.qlatt;
             if (x.ext < 0.0f) {  // abstraction: qlatt holds the lateral inflow alone
                 const float storage = x.len * (x.alpha * (u.hi * u.hi * u.hi));
-                const float absd = fminf(-x.ext, (storage / dt_s.hi) * 0.80f);
+                const float absd = fminf(-x.ext, (storage / dt_f) * 0.80f);
                 ql = wff::add(ql, wff::mul(x.invlen, -absd));
-                asum = wff::add(asum, wff::mul(dt_s, absd));
+                asum = wff::add(asum, mul_dt(wff::ff{absd, 0.0f}, dt_s));
             }
             wff::ff un, qn;
-            kw_node_ff(qin, qp, ql, u, wff::mul(x.invlen, dt_s), dt_s, x.alpha, un, qn);
+            kw_node_ff<ADAPT>(qin, qp, ql, u, mul_dt(x.invlen, dt_s), dt_s, x.alpha, un, qn);
             u = un;
             qp = qn;
             qh[s * stride] = wff::pack(qn);
             if (is_end) wfv::publish(g, chain, m, s, qn);
-            qsum = wff::add(qsum, wff::mul(qn, dt_s));
+            qsum = wff::add(qsum, mul_dt(qn, dt_s));
         }
         float* const* RMh = F.RMh;
         RMh[RV_UH][e] = u.hi;
@@ -1811,11 +1844,13 @@ cudaError_t wf_split_ssf_wave(const WfDevFields& F, const WfDevGraph& g, const W
 
 cudaError_t wf_split_overland_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw,
                                    const WfLaunchCfg& c) {
-    return launch_wave(OlWave{F, g, sw}, c);
+    if (sw.aflag) return launch_wave(OlWave<true>{F, g, sw}, c);
+    return launch_wave(OlWave<false>{F, g, sw}, c);
 }
 
 cudaError_t wf_split_river_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
-    return launch_wave(RvWave{F, g, sw}, c);
+    if (sw.aflag) return launch_wave(RvWave<true>{F, g, sw}, c);
+    return launch_wave(RvWave<false>{F, g, sw}, c);
 }
 
 cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {

@@ -72,7 +72,10 @@ struct WfHandle {
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
     bool u_dirty = false;  // split form: discharges were set from outside, u = Q^0.2 is stale
-    uint64_t wait_ns = 2000000000ull;  // 2 s per wait
+    // per-wait budget of the wavefront spin waits: a safety net against a wait that cannot end
+    // (a legitimate wait lasts at most about one sweep launch, seconds for the largest FP64
+    // sweeps); a wait that runs out ends the launch with WF_ERR_SPIN
+    uint64_t wait_ns = 30000000000ull;
     uint32_t wait_offset = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int64_t launches_per_step = 0;
@@ -620,8 +623,12 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     CKR(upload(h, &h->dts_river, h->h_dts_river));
     CKR(upload(h, &h->dts_ssf, h->h_dts_ssf));
     // wavefront schedules
-    const int cap_land = (int)std::min<size_t>(std::max(h->h_dts_land.size(), h->h_dts_ssf.size()), 128);
-    const int cap_river = (int)std::min<size_t>(h->h_dts_river.size(), 128);
+    // sub-steps per sweep launch: the split form's slim wavefronts take at most 16 (a shared-
+    // memory row per sub-step), the FP64 walker 32 (which bounds a launch to about a second on
+    // the largest domains)
+    const size_t cap = c->form == WF_FORM_SPLIT ? (size_t)wfv::MAX_GROUP : (size_t)32;
+    const int cap_land = (int)std::min<size_t>(std::max(h->h_dts_land.size(), h->h_dts_ssf.size()), cap);
+    const int cap_river = (int)std::min<size_t>(h->h_dts_river.size(), cap);
     CKR(plan_graph(h, h->land, n, d->land_downstream, M, cap_land));
     CKR(plan_graph(h, h->river, nr, d->river_downstream ? d->river_downstream : nullptr, M, cap_river));
     const WfRoutingPlan& PL = h->land.plan;
@@ -951,7 +958,10 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     F.mass_balance = c->water_mass_balance;
     F.dt = c->dt;
     F.inv_dt = 1.0 / c->dt;
-    F.ssf_single = F.split && !h->adaptive && h->h_dts_ssf.size() == 1;
+    // split form: the vertical kernel prepares the terms of a single subsurface sub-step; with
+    // adaptive sub-steps that sub-step is the whole model step (used when every member's first
+    // Courant sub-step reaches the end of the step, the usual case)
+    F.ssf_single = F.split && h->h_dts_ssf.size() == 1;
     F.dt_ssf = h->h_dts_ssf[0];
     F.inv_dt_ssf = 1.0 / h->h_dts_ssf[0];
     F.inv_dt_hi = (float)F.inv_dt;
@@ -1371,6 +1381,16 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
                 return set_err(h, WF_ERR_INVALID, "adaptive sub-stepping needed more than 100000 sub-steps in one step");
             CK(wf_adaptive_substep(h->F, A, lc));
             nl += (kind == WF_ADAPT_SSF ? 1 : (A.fp32_keys ? 4 : 8)) + 1;
+            if (split && kind == WF_ADAPT_SSF && it == 0) {
+                // every member's first sub-step spans the model step: the slim subsurface
+                // wavefront with the terms the vertical kernel prepared for a sub-step of dt
+                CK(cudaMemcpyAsync(h->h_more, A.more, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+                CK(cudaStreamSynchronize(h->stream));
+                if (!*h->h_more) {
+                    h->last_substeps[kind] = 1;
+                    return wave(G, g, h->h_dts_ssf, h->dts_ssf, 0);
+                }
+            }
             WfSweep sw{};
             sw.S = 1;
             sw.epoch0 = 1;
