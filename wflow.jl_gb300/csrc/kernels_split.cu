@@ -1070,13 +1070,14 @@ __device__ __forceinline__ wff::ff mul_dt(wff::ff a, float dt) { return wff::mul
 __device__ __forceinline__ wff::ff mul_dt(wff::ff a, wff::ff dt) { return wff::mul(a, dt); }
 
 template <bool ADAPT, class DT>
-__device__ __forceinline__ void kw_node_ff(wff::ff qin, wff::ff qp, wff::ff ql, wff::ff u, wff::ff dt_dx, DT dt_s,
+__device__ __forceinline__ void kw_node_ff(wff::ff qin, wff::ff qp, wff::ff ql, wff::ff u, wff::ff inv_dx, DT dt_s,
                                            float alpha, wff::ff& un, wff::ff& qn) {
     if (!ADAPT && qin.hi == 0.0f && qp.hi == 0.0f && ql.hi == 0.0f) {
         un = {0.0f, 0.0f};
         qn = {0.0f, 0.0f};
         return;
     }
+    const wff::ff dt_dx = mul_dt(inv_dx, dt_s);
     const wff::ff u3 = wff::mul(wff::mul(u, u), u);
     const wff::ff cterm = wff::add(wff::mul(dt_dx, qin), wff::add(wff::mul(u3, alpha), mul_dt(ql, dt_s)));
     kw_solve_ff(cterm, dt_dx, alpha, u.hi, un, qn);
@@ -1324,7 +1325,7 @@ struct OlWave {
             if (!wfv::gather<true>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
             if (!x.sfw_pos) qin = {0.0f, 0.0f};
             wff::ff un, qn;
-            kw_node_ff<ADAPT>(qin, qp, x.qlat, u, mul_dt(x.invdx, dt_s), dt_s, x.alpha, un, qn);
+            kw_node_ff<ADAPT>(qin, qp, x.qlat, u, x.invdx, dt_s, x.alpha, un, qn);
             u = un;
             qp = qn;
             qh[s * stride] = wff::pack(qn);
@@ -1397,7 +1398,7 @@ struct RvWave {
                 asum = wff::add(asum, mul_dt(wff::ff{absd, 0.0f}, dt_s));
             }
             wff::ff un, qn;
-            kw_node_ff<ADAPT>(qin, qp, ql, u, mul_dt(x.invlen, dt_s), dt_s, x.alpha, un, qn);
+            kw_node_ff<ADAPT>(qin, qp, ql, u, x.invlen, dt_s, x.alpha, un, qn);
             u = un;
             qp = qn;
             qh[s * stride] = wff::pack(qn);
