@@ -1191,13 +1191,14 @@ enum SsfFlag { SSF_FAST = 0, SSF_EARLY = 1, SSF_FULL = 2, SSF_CUT = 3 };
 
 template <int MAXN>
 struct SsfWave {
+    static constexpr int kDepth = 1;  // the per-node inputs are many: one position ahead
     WfDevFields F;
     WfDevGraph g;
     WfSweep sw;
     struct In {
         float qnet, t2, rdf, zi, rth, rcap, rrho, qmaxdw, d, dtdx, idwdx, dtsy, k2;
         bool qprev_zero;
-        wfv::UpList up;
+        wfv::UpRec up;
     };
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
         float* const* Mh = F.Mh;
@@ -1216,12 +1217,12 @@ struct SsfWave {
         x.dtsy = Lf[SSF_DTSY][slot];
         x.k2 = Lf[SSF_K2][slot];
         x.qprev_zero = F.Mh[SSF_Q][e] == 0.0f;
-        wfv::load_up(g, sw, slot, m, x.up);
+        wfv::load_rec<true>(g, slot, x.up);
     }
-    __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
-                                         unsigned long long* qh) {
+    __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
+                                         int64_t chain, bool is_end, bool heavy, unsigned long long* qh) {
         wff::ff qinff;
-        if (!wfv::gather<true>(g, sw, x.up, m, 0, qh[0], F.status, qinff)) return false;
+        if (!wfv::gather<true>(g, sw, x.up, ends, slot, m, 0, heavy, qh[0], F.status, qinff)) return false;
         const float qin = qinff.hi + qinff.lo;
         float q = 0.0f, qu = 0.0f;
         int flag;
@@ -1287,6 +1288,7 @@ struct SsfWave {
 // sub-step per launch of each member's own (adaptive) size.
 template <bool ADAPT>
 struct OlWave {
+    static constexpr int kDepth = 2;
     WfDevFields F;
     WfDevGraph g;
     WfSweep sw;
@@ -1294,7 +1296,7 @@ struct OlWave {
         wff::ff u, q, qlat, invdx;
         float alpha;
         bool sfw_pos;
-        wfv::UpList up;
+        wfv::UpRec up;
     };
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
         float* const* Mh = F.Mh;
@@ -1304,10 +1306,10 @@ struct OlWave {
         x.invdx = {F.Lf[INV_FLOW_LENGTH][slot], F.Lf[INV_DX_LO][slot]};
         x.alpha = F.Lf[OL_ALPHA][slot];
         x.sfw_pos = F.Lf[SFW][slot] > 0.0f;
-        wfv::load_up(g, sw, slot, m, x.up);
+        wfv::load_rec<true>(g, slot, x.up);
     }
-    __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
-                                         unsigned long long* qh) {
+    __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
+                                         int64_t chain, bool is_end, bool heavy, unsigned long long* qh) {
         const int stride = blockDim.x;
         bool first = sw.first == 0;
         if (ADAPT) {
@@ -1322,7 +1324,7 @@ struct OlWave {
             if constexpr (ADAPT) dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
             else dt_s = sw.dts_f[s];
             wff::ff qin;
-            if (!wfv::gather<true>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
+            if (!wfv::gather<true>(g, sw, x.up, ends, slot, m, s, heavy, qh[s * stride], F.status, qin)) return false;
             if (!x.sfw_pos) qin = {0.0f, 0.0f};
             wff::ff un, qn;
             kw_node_ff<ADAPT>(qin, qp, x.qlat, u, x.invdx, dt_s, x.alpha, un, qn);
@@ -1348,13 +1350,14 @@ struct OlWave {
 // storage. ADAPT as for OlWave.
 template <bool ADAPT>
 struct RvWave {
+    static constexpr int kDepth = 2;
     WfDevFields F;
     WfDevGraph g;
     WfSweep sw;
     struct In {
         wff::ff u, q, qlatt, invlen;
         float alpha, len, ext;
-        wfv::UpList up;
+        wfv::UpRec up;
     };
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
         float* const* RMh = F.RMh;
@@ -1365,10 +1368,10 @@ struct RvWave {
         x.alpha = F.Rf[R_ALPHA][slot];
         x.len = F.Rf[R_LENGTH][slot];
         x.ext = F.Rf[R_EXT_INFLOW][slot];
-        wfv::load_up(g, sw, slot, m, x.up);
+        wfv::load_rec<false>(g, slot, x.up);
     }
-    __device__ __forceinline__ bool node(const In& x, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
-                                         unsigned long long* qh) {
+    __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
+                                         int64_t chain, bool is_end, bool heavy, unsigned long long* qh) {
         const int stride = blockDim.x;
         bool first = sw.first == 0;
         if (ADAPT) {
@@ -1389,7 +1392,7 @@ struct RvWave {
                 dt_f = dt_s;
             }
             wff::ff qin;
-            if (!wfv::gather<false>(g, sw, x.up, m, s, qh[s * stride], F.status, qin)) return false;
+            if (!wfv::gather<false>(g, sw, x.up, ends, slot, m, s, heavy, qh[s * stride], F.status, qin)) return false;
             wff::ff ql = x.qlatt;
             if (x.ext < 0.0f) {  // abstraction: qlatt holds the lateral inflow alone
                 const float storage = x.len * (x.alpha * (u.hi * u.hi * u.hi));
@@ -1429,7 +1432,7 @@ __global__ void __launch_bounds__(128) wave_kernel(Phys phys) {
 template <class Phys>
 cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
-    const size_t smem = (size_t)threads * phys.sw.S * sizeof(unsigned long long);
+    const size_t smem = wfv::walk_smem(threads, phys.sw.S);
     int blocks;
     Phys p = phys;
     cudaError_t err = wave_grid(wave_kernel<Phys>, threads, smem, c, p.g, blocks, p.sw.prio_items);

@@ -36,6 +36,9 @@ struct DevGraphAlloc {
     uint8_t* is_chain_end = nullptr;
     double *up_w = nullptr, *up_fr = nullptr;
     float *up_wf = nullptr, *up_frf = nullptr;
+    int4* up_rec = nullptr;
+    float* up_whv = nullptr;
+    uint8_t* up_nlt = nullptr;
     uint32_t* flags = nullptr;
     double* end_q = nullptr;
     unsigned long long* ticket = nullptr;
@@ -204,6 +207,11 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.n_chunks = G.plan.n_chunks;
     g.n_chains = G.plan.n_chains;
     g.n_long_chunks = G.plan.n_long_chunks;
+    {
+        int64_t ns = 0;
+        while (ns < G.plan.n_chunks && G.plan.chunk_len[ns] <= wfv::SHORT_LEN) ++ns;
+        g.n_short_chunks = ns;
+    }
     g.G = G.plan.G;
     g.M = M;
     g.chunk_base = G.chunk_base;
@@ -219,6 +227,9 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.up_fr = G.up_fr;
     g.up_wf = G.up_wf;
     g.up_frf = G.up_frf;
+    g.up_rec = G.up_rec;
+    g.up_whv = G.up_whv;
+    g.up_nlt = G.up_nlt;
     g.flags = G.flags;
     g.end_q = G.end_q;
     g.ticket = G.ticket;
@@ -881,6 +892,34 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
         std::vector<float> wf(w.begin(), w.end()), frf(fr.begin(), fr.end());
         CKR(upload(h, &G.up_wf, wf));
         CKR(upload(h, &G.up_frf, frf));
+        // per-slot records of the slim wavefronts: the first two light children and the weights
+        std::vector<int4> rec(std::max<int64_t>(P.n_slots, 1), int4{-1, -1, 0, 0});
+        std::vector<float> whv(rec.size(), 0.0f);
+        std::vector<uint8_t> nlt(rec.size(), 0);
+        for (int64_t sl = 0; sl < P.n_slots; ++sl) {
+            int lights = 0;
+            for (int32_t o = P.up_ptr[sl]; o < P.up_ptr[sl + 1]; ++o) {
+                if (P.up_chain[o] < 0) {
+                    whv[sl] = wf[o];
+                    continue;
+                }
+                float wo = wf[o];
+                int32_t bits;
+                std::memcpy(&bits, &wo, sizeof(bits));
+                if (lights == 0) {
+                    rec[sl].x = P.up_chain[o];
+                    rec[sl].z = bits;
+                } else if (lights == 1) {
+                    rec[sl].y = P.up_chain[o];
+                    rec[sl].w = bits;
+                }
+                ++lights;
+            }
+            nlt[sl] = (uint8_t)std::min(lights, 255);
+        }
+        CKR(upload(h, &G.up_rec, rec));
+        CKR(upload(h, &G.up_whv, whv));
+        CKR(upload(h, &G.up_nlt, nlt));
     }
     // ---- split form: FP32 copies of the static fields and FP32 member fields
     if (F.split) {

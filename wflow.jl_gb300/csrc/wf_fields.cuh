@@ -9,6 +9,8 @@
 
 #include <cstdint>
 
+#include <vector_types.h>
+
 #include "wflow_gb300.h"
 
 #define WF_L_FIELDS(X)                                                                             \
@@ -130,6 +132,7 @@ struct WfDevGraph {
     int64_t n_chunks;
     int64_t n_chains;
     int64_t n_long_chunks;  // trailing chunks of the longest chains (dispatched first)
+    int64_t n_short_chunks; // leading chunks of at most 8 positions (batched per work ticket)
     int32_t G;
     int32_t M;
     const int64_t* chunk_base;
@@ -145,6 +148,12 @@ struct WfDevGraph {
     const double* up_fr;  // [up entries] fraction of the upstream discharge to the river (land only)
     const float* up_wf;   // FP32 copies of up_w / up_fr (split form)
     const float* up_frf;
+    // per-slot upstream records of the split form's slim wavefronts (wf_wave.cuh UpRec):
+    // {chain of light child 0, chain of light child 1, their weights as float bits}, the heavy
+    // child's weight and the number of light children
+    const int4* up_rec;
+    const float* up_whv;
+    const uint8_t* up_nlt;
     uint32_t* flags;      // [n_chains * M] epoch of the last published sub-step
     double* end_q;        // [n_chains * M * s_cap] q of each chain end per sub-step
     unsigned long long* ticket;  // work counter of the current launch

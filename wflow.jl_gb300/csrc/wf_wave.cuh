@@ -90,117 +90,248 @@ __device__ __forceinline__ void publish(const WfDevGraph& g, int64_t chain, int 
     st_relaxed(&g.end_q[end_index(g, chain, m, s)], wff::pack(q));
 }
 
-// Upstream list of one node with the first light entry's words of the first sub-steps
-// prefetched (loaded together, so they cost one round trip).
-struct UpList {
-    int32_t o0, o1;
-    int32_t lo;                                  // up entry of the prefetched light child (-1: none)
-    int64_t lbase;                               // its end_q index at sub-step 0
-    unsigned long long lq[PREFETCH_SUBSTEPS];    // its end_q words at prefetch time (may be sentinels)
+// Upstream inflow record of one node. A node at chain position k > 0 has its heavy child at
+// position k - 1 (its discharge is handed over in shared memory); its light children are chain
+// ends of shorter chains. The first two light children come from the per-slot record (one
+// 16-byte load, no dependent index loads), the rare further ones from the CSR list; the
+// end_q words of light child 0 for the first sub-steps and of light child 1 for sub-step 0 are
+// prefetched (load_ends), so a producer that finished earlier costs no round trip in gather.
+struct UpRec {
+    int32_t lt0, lt1;     // chains of light children 0 and 1 (-1: none)
+    float w_lt0, w_lt1;   // their weights
+    float w_hv;           // weight of the heavy child
+    int32_t n_lt;         // light children in all
+};
+// The prefetched end_q words of one node (kept apart from UpRec so that only the positions
+// whose words are in flight hold them).
+struct Ends {
+    unsigned long long lq0[PREFETCH_SUBSTEPS];  // light child 0, first sub-steps (may be sentinels)
+    unsigned long long lq1;                     // light child 1, sub-step 0
 };
 
-__device__ __forceinline__ void load_up(const WfDevGraph& g, const WfSweep& sw, int64_t slot, int m, UpList& u) {
-    u.o0 = g.up_ptr[slot];
-    u.o1 = g.up_ptr[slot + 1];
-    u.lo = -1;
-    u.lbase = 0;
-#pragma unroll
-    for (int s = 0; s < PREFETCH_SUBSTEPS; ++s) u.lq[s] = SENTINEL;
-    for (int32_t o = u.o0; o < u.o1; ++o) {
-        const int32_t uc = g.up_chain[o];
-        if (uc >= 0) {
-            u.lo = o;
-            u.lbase = end_index(g, uc, m, 0);
-#pragma unroll
-            for (int s = 0; s < PREFETCH_SUBSTEPS; ++s)
-                if (s < sw.S) u.lq[s] = ld_relaxed(&g.end_q[u.lbase + (int64_t)s * g.M]);
-            break;
-        }
-    }
+// Level-1 loads of the record (WEIGHTED: the land graph's weights, else all weights are 1).
+template <bool WEIGHTED>
+__device__ __forceinline__ void load_rec(const WfDevGraph& g, int64_t slot, UpRec& r) {
+    const int4 v = g.up_rec[slot];
+    r.lt0 = v.x;
+    r.lt1 = v.y;
+    r.w_lt0 = WEIGHTED ? __int_as_float(v.z) : 1.0f;
+    r.w_lt1 = WEIGHTED ? __int_as_float(v.w) : 1.0f;
+    r.w_hv = WEIGHTED ? g.up_whv[slot] : 1.0f;
+    r.n_lt = g.up_nlt[slot];
 }
 
-// Weighted upstream sum at sub-step s in up-list order: qin = sum w*q (w = 1 - fraction to
-// river on land, 1 on rivers), in double-FP32. `qh` is the heavy child's word of this sub-step.
-template <bool WEIGHTED>
-__device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, const UpList& u, int m, int s,
-                                       unsigned long long qh, int32_t* status, wff::ff& qin) {
-    wff::ff acc = {0.0f, 0.0f};
-    for (int32_t o = u.o0; o < u.o1; ++o) {
-        const int32_t uc = g.up_chain[o];
-        unsigned long long w;
-        if (uc < 0) {
-            w = qh;
-        } else {
-            const int64_t idx = end_index(g, uc, m, s);
-            unsigned long long first = SENTINEL;
-            if (o == u.lo) {
+// Level-2 loads: the light children's end_q words of the first sub-steps.
+__device__ __forceinline__ void load_ends(const WfDevGraph& g, const WfSweep& sw, int m, const UpRec& r, Ends& x) {
 #pragma unroll
-                for (int j = 0; j < PREFETCH_SUBSTEPS; ++j)
-                    if (j == s) first = u.lq[j];
-            }
-            if (first == SENTINEL) first = ld_relaxed(&g.end_q[idx]);
-            if (!await_end(g, sw, idx, first, status, w)) return false;
-        }
+    for (int s = 0; s < PREFETCH_SUBSTEPS; ++s) x.lq0[s] = SENTINEL;
+    x.lq1 = SENTINEL;
+    if (r.lt0 >= 0) {
+        const int64_t b = end_index(g, r.lt0, m, 0);
+#pragma unroll
+        for (int s = 0; s < PREFETCH_SUBSTEPS; ++s)
+            if (s < sw.S) x.lq0[s] = ld_relaxed(&g.end_q[b + (int64_t)s * g.M]);
+    }
+    if (r.lt1 >= 0) x.lq1 = ld_relaxed(&g.end_q[end_index(g, r.lt1, m, 0)]);
+}
+
+// Weighted upstream sum at sub-step s: qin = sum w*q (w = 1 - fraction to river on land, 1 on
+// rivers) in double-FP32, heavy child first, then the light children. `qh` is the heavy child's
+// word of this sub-step, `heavy` whether the node has one (chain position > 0).
+template <bool WEIGHTED>
+__device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, const UpRec& r, const Ends& x,
+                                       int64_t slot, int m, int s, bool heavy, unsigned long long qh, int32_t* status,
+                                       wff::ff& qin) {
+    wff::ff acc = {0.0f, 0.0f};
+    if (heavy) {
+        const wff::ff q = wff::unpack(qh);
+        acc = WEIGHTED ? wff::mul(q, r.w_hv) : q;
+    }
+    if (r.lt0 >= 0) {
+        unsigned long long first = SENTINEL;
+#pragma unroll
+        for (int j = 0; j < PREFETCH_SUBSTEPS; ++j)
+            if (j == s) first = x.lq0[j];
+        const int64_t idx = end_index(g, r.lt0, m, s);
+        if (first == SENTINEL) first = ld_relaxed(&g.end_q[idx]);
+        unsigned long long w;
+        if (!await_end(g, sw, idx, first, status, w)) return false;
         const wff::ff q = wff::unpack(w);
-        acc = WEIGHTED ? wff::add(acc, wff::mul(q, g.up_wf[o])) : wff::add(acc, q);
+        acc = WEIGHTED ? wff::add(acc, wff::mul(q, r.w_lt0)) : wff::add(acc, q);
+    }
+    if (r.lt1 >= 0) {
+        const int64_t idx = end_index(g, r.lt1, m, s);
+        unsigned long long first = s == 0 ? x.lq1 : SENTINEL;
+        if (first == SENTINEL) first = ld_relaxed(&g.end_q[idx]);
+        unsigned long long w;
+        if (!await_end(g, sw, idx, first, status, w)) return false;
+        const wff::ff q = wff::unpack(w);
+        acc = WEIGHTED ? wff::add(acc, wff::mul(q, r.w_lt1)) : wff::add(acc, q);
+    }
+    if (r.n_lt > 2) {  // further light children, in up-list order after the first two
+        int seen = 0;
+        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
+            const int32_t uc = g.up_chain[o];
+            if (uc < 0 || ++seen <= 2) continue;
+            const int64_t idx = end_index(g, uc, m, s);
+            unsigned long long w;
+            if (!await_end(g, sw, idx, ld_relaxed(&g.end_q[idx]), status, w)) return false;
+            const wff::ff q = wff::unpack(w);
+            acc = WEIGHTED ? wff::add(acc, wff::mul(q, g.up_wf[o])) : wff::add(acc, q);
+        }
     }
     qin = acc;
     return true;
 }
 
+// Work items are (chunk, member group) pairs in dependency (chain length) order. One ticket takes
+// a batch of up to BATCH consecutive short items (chunk length <= SHORT_LEN: the bulk of a
+// drainage forest is short tributary chains, and a ticket per chain would pay the ticket, the
+// descriptor loads and the prefetch start-up per chain), or a single longer item. The items of
+// a batch are walked as one sequence of positions, so the prefetch runs on across item
+// boundaries. Order and progress are unchanged: a batch holds consecutive items and a chain
+// waits only for strictly shorter chains, which come earlier in the batch or in the order.
+constexpr int BATCH = 8;
+constexpr int SHORT_LEN = 8;
+
+struct WarpBatch {  // per-warp shared descriptors of the items of the current ticket
+    long long base[BATCH];
+    long long chain0[BATCH];
+    int L[BATCH];
+    int Gc[BATCH];
+    int mbase[BATCH];     // first member of the item (more than 32 members)
+    int len[BATCH][32];   // length of each lane's chain (0: the lane idles in that item)
+};
+
+__host__ __device__ constexpr size_t walk_smem(int threads, int substeps) {
+    return (size_t)threads * substeps * sizeof(unsigned long long) + (size_t)(threads / 32) * sizeof(WarpBatch);
+}
+
 // Phys interface:
-//   struct In;                                               per-node inputs (prefetched)
-//   void load(int64_t slot, int64_t e, int m, In&)           independent of upstream discharge
-//   bool node(const In&, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
-//             unsigned long long* qh)
+//   struct In;                                   per-node inputs, including an UpRec `up`
+//   static constexpr int kDepth;                 1: prefetch one position ahead; 2: two (the
+//                                                inputs two ahead, their end_q words one ahead)
+//   void load(int64_t slot, int64_t e, int m, In&)   level-1 loads (state, statics, load_rec)
+//   bool node(const In&, const Ends&, int64_t slot, int64_t e, int m, int64_t chain, bool is_end,
+//             bool heavy, unsigned long long* qh)
 //     advances the node through sw.S sub-steps; qh[s * stride] holds the heavy child's packed
 //     discharge of sub-step s on entry and this node's on exit. Returns false to abort.
 template <class Phys>
 __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
     extern __shared__ unsigned long long wave_smem[];
+    constexpr int DEPTH = Phys::kDepth;
     const unsigned lane = threadIdx.x & 31u;
     unsigned long long* qh = wave_smem + threadIdx.x;  // row of this thread: qh[s * blockDim.x]
+    WarpBatch* wb = reinterpret_cast<WarpBatch*>(wave_smem + (size_t)blockDim.x * sw.S) + (threadIdx.x >> 5);
     const int M = g.M;
     const int gpc = M > 32 ? M / 32 : 1;
-    const uint64_t n_items = (uint64_t)g.n_chunks * gpc;
-    const uint64_t prio = (uint64_t)sw.prio_items;
+    const int gi = M <= 32 ? (int)lane / M : 0;
+    const int64_t n_items = g.n_chunks * gpc;
+    const int64_t prio = sw.prio_items;
+    const int64_t n_norm = n_items - prio;
+    const int64_t n_short = min(g.n_short_chunks * gpc, n_norm);
+    const int64_t n_sb = (n_short + BATCH - 1) / BATCH;
+    const uint64_t n_tickets = (uint64_t)(prio + n_sb + (n_norm - n_short));
     while (true) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(g.ticket, 1ULL);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= n_items) return;
-        // the first prio_items tickets take the longest chains, longest first; the rest take
-        // the other items in dependency (chain length) order
-        const unsigned long long item = t < prio ? n_items - 1 - t : t - prio;
-        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
-        const int64_t chunk = (int64_t)(item / gpc);
-        int gi, m;
-        if (M <= 32) {
-            gi = (int)lane / M;
-            m = (int)lane % M;
+        if (t >= n_tickets) return;
+        // the first prio_items tickets take the longest items, longest first; the rest take the
+        // others in dependency order, short ones in batches
+        int64_t first;
+        int count = 1;
+        if ((int64_t)t < prio) {
+            first = n_items - 1 - (int64_t)t;
         } else {
-            gi = 0;
-            m = (int)(item % gpc) * 32 + (int)lane;
+            const int64_t u = (int64_t)t - prio;
+            if (u < n_sb) {
+                first = u * BATCH;
+                count = (int)min((int64_t)BATCH, n_short - first);
+            } else {
+                first = n_short + (u - n_sb);
+            }
         }
-        const int Gc = g.chunk_g[chunk];
-        const int64_t chain = g.chunk_chain0[chunk] + (gi < Gc ? gi : 0);
-        const int len = gi < Gc ? g.chain_len[chain] : 0;
-        const int L = g.chunk_len[chunk];
-        const int64_t base = g.chunk_base[chunk];
+        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
+        if ((int)lane < count) {
+            const int64_t item = first + lane;
+            const int64_t chunk = item / gpc;
+            wb->base[lane] = g.chunk_base[chunk];
+            wb->chain0[lane] = g.chunk_chain0[chunk];
+            wb->L[lane] = g.chunk_len[chunk];
+            wb->Gc[lane] = g.chunk_g[chunk];
+            wb->mbase[lane] = (int)(item % gpc) * 32;
+        }
+        __syncwarp();
+        for (int j = 0; j < count; ++j) {
+            const int Gc = wb->Gc[j];
+            wb->len[j][lane] = gi < Gc ? g.chain_len[wb->chain0[j] + gi] : 0;
+        }
+        __syncwarp();
+        const int m_fixed = (int)lane % (M <= 32 ? M : 32);
+        // the walk over the positions (item it, chain position k) of the batch
+        auto valid = [&](int it, int k) { return it < count && k < wb->len[it][lane]; };
+        auto slot_of = [&](int it, int k) { return wb->base[it] + (int64_t)k * wb->Gc[it] + gi; };
+        auto member = [&](int it) { return M > 32 ? wb->mbase[it] + (int)lane : m_fixed; };
+        auto advance = [&](int& it, int& k) {
+            if (k + 1 < wb->L[it]) {
+                ++k;
+            } else {
+                ++it;
+                k = 0;
+            }
+        };
         typename Phys::In cur, nxt;
-        if (len > 0) phys.load(base + gi, (base + gi) * M + m, m, cur);
-        for (int k = 0; k < L; ++k) {
-            const int64_t slot = base + (int64_t)k * Gc + gi;
-            if (k + 1 < len) {
-                const int64_t ns = slot + Gc;
-                phys.load(ns, ns * M + m, m, nxt);
+        Ends ecur, enxt;
+        int cit = 0, ck = 0;
+        if (valid(cit, ck)) {
+            const int64_t sl = slot_of(cit, ck);
+            const int mm = member(cit);
+            phys.load(sl, sl * M + mm, mm, cur);
+            load_ends(g, sw, mm, cur.up, ecur);
+        }
+        int nit = cit, nk = ck;
+        advance(nit, nk);
+        if (DEPTH > 1 && valid(nit, nk)) {
+            const int64_t sl = slot_of(nit, nk);
+            const int mm = member(nit);
+            phys.load(sl, sl * M + mm, mm, nxt);
+        }
+        while (cit < count) {
+            int nnit = nit, nnk = nk;
+            if (nnit < count) advance(nnit, nnk);
+            typename Phys::In nn;
+            if (DEPTH > 1) {
+                if (valid(nit, nk)) load_ends(g, sw, member(nit), nxt.up, enxt);
+                if (valid(nnit, nnk)) {
+                    const int64_t sl = slot_of(nnit, nnk);
+                    const int mm = member(nnit);
+                    phys.load(sl, sl * M + mm, mm, nn);
+                }
+            } else if (valid(nit, nk)) {
+                const int64_t sl = slot_of(nit, nk);
+                const int mm = member(nit);
+                phys.load(sl, sl * M + mm, mm, nxt);
+                load_ends(g, sw, mm, nxt.up, enxt);
             }
             bool ok = true;
-            if (k < len) ok = phys.node(cur, slot, slot * M + m, m, chain, k == len - 1, qh);
+            if (valid(cit, ck)) {
+                const int64_t sl = slot_of(cit, ck);
+                const int mm = member(cit);
+                ok = phys.node(cur, ecur, sl, sl * M + mm, mm, wb->chain0[cit] + gi, ck == wb->len[cit][lane] - 1,
+                               ck > 0, qh);
+            }
             if (__any_sync(0xffffffffu, !ok)) return;
             __syncwarp();
             cur = nxt;
+            ecur = enxt;
+            if (DEPTH > 1) nxt = nn;
+            cit = nit;
+            ck = nk;
+            nit = nnit;
+            nk = nnk;
         }
+        __syncwarp();
     }
 }
 
