@@ -239,6 +239,15 @@ def run_gpu(args):
         P, PET, T = member_forcing(s, dt, n, members, pfac, seed=args.seed)
         pin = [torch.from_numpy(x).pin_memory() for x in (P, PET, T)]
         host.append(pin)
+    # The first device access to a freshly pinned host buffer maps its pages (about 30 GB/s
+    # instead of 200 GB/s on this host); a model run reads its forcing into the same buffers
+    # every step, so each buffer is touched once before the timed region.
+    scratch = torch.empty(n * members, dtype=torch.float64, device=dev)
+    for pin in host:
+        for x in pin:
+            scratch[: x.numel()].copy_(x, non_blocking=True)
+    torch.cuda.synchronize()
+    del scratch
     n_out = max(1, len(dom.outlets) * members)
     out = torch.empty(n_out, dtype=torch.float64).pin_memory()
     import ctypes as C
