@@ -1687,7 +1687,7 @@ __device__ __forceinline__ void mb_error_ff(wff::ff tin, wff::ff tout, wff::ff r
     rel = {avg == 0.0f ? 0.0f : __fdividef(wff::to_f(err), avg), 0.0f};
 }
 
-__global__ void __launch_bounds__(256) balance_split_kernel(WfDevFields F) {
+__global__ void __launch_bounds__(256, 4) balance_split_kernel(WfDevFields F) {
     using wff::ff;
     const int M = F.M;
     const int64_t EL = F.land_slots * M, ER = F.river_slots * M;
