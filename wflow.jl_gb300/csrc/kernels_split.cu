@@ -343,6 +343,76 @@ __device__ __forceinline__ wff::ff ldrs(const WfDevFields& F, int f, int64_t slo
     return {F.Rf[f][slot], F.Rl[f][slot]};
 }
 
+// ----------------------------------------------------------------- member-field staging --
+//
+// The vertical kernel reads some 27 member fields per element, each from its own array, and is
+// bound by the latency of those loads at the occupancy its registers allow. Each thread
+// therefore copies the member fields of the element it will compute next into its own
+// shared-memory slots with asynchronous copies (cp.async, 4 and 8 bytes) while it computes the
+// current one, and waits for them (cp.async.wait_group) only when it gets there: a per-thread
+// double buffer, so no barrier is involved (a thread reads back only what it copied itself).
+// The per-cell parameters stay ordinary loads: they are shared by the members of a cell and
+// come from L1/L2.
+enum VStage32 {
+    VS_PRECIP, VS_POTEVAP, VS_TEMP, VS_KV0, VS_FSCALE, VS_TSOIL, VS_OL_H, VS_CANOPY_H, VS_CANOPY_L, VS_SNOW_H,
+    VS_SNOW_L, VS_SW_H, VS_SW_L, VS_SSFQ_H, VS_SSFQ_L, VS_OLST_H, VS_OLST_L, VS_USLD_H
+};
+enum VStage64 { VD_SAT, VD_TSWS, VD_COUNT };
+template <int MAXN>
+struct VStage {
+    static constexpr int N32 = VS_USLD_H + 2 * MAXN;  // USLD high parts, then low parts
+    static constexpr size_t bytes_per_thread = N32 * sizeof(float) + VD_COUNT * sizeof(double);
+};
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Stage the member fields of element e into buffer (f32, f64) of this thread (stride = block
+// size between fields).
+template <int MAXN>
+__device__ __forceinline__ void stage_vertical(const WfDevFields& F, int64_t e, float* f32, double* f64, int st) {
+    auto c4 = [&](int i, const float* src) { cp_async4(f32 + i * st, src + e); };
+    c4(VS_PRECIP, F.Mh[PRECIP]);
+    c4(VS_POTEVAP, F.Mh[POTEVAP]);
+    c4(VS_TEMP, F.Mh[TEMP]);
+    c4(VS_KV0, F.Mh[KV0]);
+    c4(VS_FSCALE, F.Mh[FSCALE]);
+    c4(VS_TSOIL, F.Mh[TSOIL]);
+    c4(VS_OL_H, F.Mh[OL_H]);
+    c4(VS_CANOPY_H, F.Mh[CANOPY]);
+    c4(VS_CANOPY_L, F.Ml[CANOPY]);
+    if (F.snow) {
+        c4(VS_SNOW_H, F.Mh[SNOW]);
+        c4(VS_SNOW_L, F.Ml[SNOW]);
+        c4(VS_SW_H, F.Mh[SNOW_WATER]);
+        c4(VS_SW_L, F.Ml[SNOW_WATER]);
+    }
+    if (F.ssf_single) {
+        c4(VS_SSFQ_H, F.Mh[SSF_Q]);
+        c4(VS_SSFQ_L, F.Ml[SSF_Q]);
+    }
+    if (F.mass_balance) {
+        c4(VS_OLST_H, F.Mh[OL_STORAGE]);
+        c4(VS_OLST_L, F.Ml[OL_STORAGE]);
+    }
+#pragma unroll
+    for (int k = 0; k < MAXN; ++k)
+        if (k < F.N) {
+            c4(VS_USLD_H + k, F.LYf[LY_USLD][k]);
+            c4(VS_USLD_H + MAXN + k, F.LYl[k]);
+        }
+    cp_async8(f64 + VD_SAT * st, F.Mf[SAT] + e);
+    cp_async8(f64 + VD_TSWS * st, F.Mf[TSWS] + e);
+}
+
 // ----------------------------------------------------------------- vertical kernel ------
 //
 // GB300 issues FP64 instructions (arithmetic, compares and FP32<->FP64 conversions alike) at
@@ -352,14 +422,33 @@ __device__ __forceinline__ wff::ff ldrs(const WfDevFields& F, int f, int64_t slo
 // (wf_ff.cuh); stores take the step's FP32 increments exactly (TwoSum/TwoProd); partitions of
 // a flux are exact residuals, so the parts always sum to the whole.
 template <int MAXN>
-__global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
+__global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
     using wff::ff;
     const int M = F.M;
     const int64_t E = F.land_slots * M;
     const float dtf = (float)F.dt;
     const ff inv_dt = {F.inv_dt_hi, F.inv_dt_lo};
     const float inv_dtf = F.inv_dt_hi;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    // per-thread double buffer of staged member fields (layout: field-major, stride blockDim)
+    extern __shared__ double vstage_smem[];
+    const int bd = blockDim.x;
+    constexpr int N32 = VStage<MAXN>::N32;
+    double* const my64 = vstage_smem + threadIdx.x;  // buffer b: my64 + b * VD_COUNT * bd
+    float* const my32 = reinterpret_cast<float*>(vstage_smem + (size_t)2 * VD_COUNT * bd) + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * bd;
+    int64_t e = blockIdx.x * (int64_t)bd + threadIdx.x;
+    if (e < E) stage_vertical<MAXN>(F, e, my32, my64, bd);
+    cp_async_commit();
+    for (int buf = 0; e < E; e += stride, buf ^= 1) {
+        // stage the next element while this one computes
+        if (e + stride < E)
+            stage_vertical<MAXN>(F, e + stride, my32 + (buf ^ 1) * N32 * bd, my64 + (buf ^ 1) * VD_COUNT * bd, bd);
+        cp_async_commit();
+        cp_async_wait_prev();
+        const float* const vs = my32 + buf * N32 * bd;
+        const double* const vd = my64 + buf * VD_COUNT * bd;
+        auto V = [&](int i) { return vs[i * bd]; };
+        auto VF = [&](int ih, int il) { return ff{vs[ih * bd], vs[il * bd]}; };
         const int64_t slot = e / M;
         if (F.land_node_of_slot[slot] < 0) continue;
         const int m = (int)(e - slot * M);
@@ -403,11 +492,11 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         const float p_whc = Lf[WHC][slot];
         const float p_w_soil = Lf[W_SOIL][slot];
         const float p_z_exp = Lf[Z_EXP][slot];
-        const float Pf = Mh[PRECIP][e], PETf = Mh[POTEVAP][e], Tf = Mh[TEMP][e];
-        const ff canopy0 = ldm(F, CANOPY, e);
-        const ff snow0 = F.snow ? ldm(F, SNOW, e) : ff{0.0f, 0.0f};
-        const ff sw0 = F.snow ? ldm(F, SNOW_WATER, e) : ff{0.0f, 0.0f};
-        if (F.mass_balance) F.Mf[BL_PREV][e] = F.Mf[TSWS][e] + wff::to_d(wff::add(canopy0, wff::add(snow0, sw0)));
+        const float Pf = V(VS_PRECIP), PETf = V(VS_POTEVAP), Tf = V(VS_TEMP);
+        const ff canopy0 = VF(VS_CANOPY_H, VS_CANOPY_L);
+        const ff snow0 = F.snow ? VF(VS_SNOW_H, VS_SNOW_L) : ff{0.0f, 0.0f};
+        const ff sw0 = F.snow ? VF(VS_SW_H, VS_SW_L) : ff{0.0f, 0.0f};
+        if (F.mass_balance) F.Mf[BL_PREV][e] = vd[VD_TSWS * bd] + wff::to_d(wff::add(canopy0, wff::add(snow0, sw0)));
         // ---- interception (canopy.jl:213-226 Gash, :259-271 Rutter)
         const float gapf = p_gap, cmaxf = p_cmax;
         const float potevap_f = p_kc * PETf * (1.0f - gapf);
@@ -522,7 +611,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         }
         // ---- open water (runoff.jl open-water runoff and evaporation)
         const float rfrac_f = p_river_fraction, wfrac_f = p_water_fraction;
-        const float wd_land = Mh[OL_H][e];
+        const float wd_land = V(VS_OL_H);
         const int64_t rs = F.land_river_slot[slot];
         const float wd_river = rs >= 0 ? F.RMh[RV_H][rs * M + m] : 0.0f;
         const ff runoff_river = wff::mul(wfs, fminf(1.0f, rfrac_f));
@@ -535,14 +624,14 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         const float pot_trans = fmaxf(0.0f, potevap_f - icf);
         const float pot_soilevap = soil_fraction * PETf;
         const double d_soil = F.L[SOIL_THICKNESS][slot];
-        const double sat = F.Mf[SAT][e];
+        const double sat = vd[VD_SAT * bd];
         const double zi = fmax(0.0, fma(-sat, F.L[INV_TE][slot], d_soil));
         ColG<MAXN> g;
         g.set(F, slot, zi);
         const float zif = (float)zi, df = p_soil_thickness, satf = (float)sat;
         const float ts = p_theta_s, tr = p_theta_r, tfc = p_theta_fc;
         const float te = ts - tr;
-        const float kv0 = Mh[KV0][e], fsc = Mh[FSCALE][e], zexp = p_z_exp;
+        const float kv0 = V(VS_KV0), fsc = V(VS_FSCALE), zexp = p_z_exp;
         const bool kv_const = F.kv_profile == WF_KV_EXPONENTIAL_CONSTANT;
         Store us[MAXN];
         float kvf[MAXN], cexp[MAXN], rfr[MAXN];
@@ -550,7 +639,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
 #pragma unroll
         for (int k = 0; k < MAXN; ++k) {
             if (k < g.N) {
-                us[k].init({F.LYf[LY_USLD][k][e], F.LYl[k][e]});
+                us[k].init(VF(VS_USLD_H + k, VS_USLD_H + MAXN + k));
                 kvf[k] = F.LYf[LY_KVFRAC][k][slot];
                 cexp[k] = F.LYf[LY_C][k][slot];
                 rfr[k] = F.LYf[LY_ROOTFRAC][k][slot];
@@ -572,7 +661,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
     }())
         float drain = (df - zif) * fmaxf(ts - tfc, 0.02f);
         float ucap = p_swc - satf - usd;
-        float tsoil = Mh[TSOIL][e];
+        float tsoil = V(VS_TSOIL);
         if (F.snow) tsoil = tsoil + p_w_soil * (Tf - tsoil);
         float fred = 1.0f;
         if (F.snow && F.infilt_reduction) {
@@ -766,7 +855,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
         Mh[ACT_INFILT][e] = wff::to_f(act_infilt);
         // storages at the start of the routing (overland and river balances)
         if (F.mass_balance) {
-            stm(F, BO_PREV, e, ldm(F, OL_STORAGE, e));
+            stm(F, BO_PREV, e, VF(VS_OLST_H, VS_OLST_L));
             if (rs >= 0) str(F, BR_PREV, rs * M + m, ldr(F, RV_STORAGE, rs * M + m));
         }
         // terms of the subsurface solve that do not depend on the upstream discharge: the
@@ -781,7 +870,7 @@ __global__ void __launch_bounds__(256) vertical_split_kernel(WfDevFields F) {
             if (kv_const && !(z < zexp)) z = zexp;
             const float cel = p_kh_ratio * kv0 * expf(-fsc * z) * p_slope / p_sy;
             const float cinv = 1.0f / cel;
-            Mh[SSF_T2][e] = wff::to_f(ldm(F, SSF_Q, e)) * cinv;
+            Mh[SSF_T2][e] = wff::to_f(VF(VS_SSFQ_H, VS_SSFQ_L)) * cinv;
             Mh[SSF_RDF][e] = 1.0f / (p_ssf_dtdx + cinv);
             // deepest unsaturated layer: what a rising water table fills first
             float rth = 0.0f, rcap = 0.0f, rrho = 0.0f;
@@ -1821,10 +1910,19 @@ int grid_for(int64_t n, int block, int num_sms) {
 cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c) {
     const int block = c.vertical_block > 0 ? c.vertical_block : 256;
     const int grid = grid_for(F.land_slots * F.M, block, c.num_sms);
-    if (F.N <= 4)
-        vertical_split_kernel<4><<<grid, block, 0, c.stream>>>(F);
-    else
-        vertical_split_kernel<WF_MAX_LAYERS><<<grid, block, 0, c.stream>>>(F);
+    if (F.N <= 4) {
+        const size_t smem = 2 * VStage<4>::bytes_per_thread * block;
+        cudaError_t e = cudaFuncSetAttribute(vertical_split_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        vertical_split_kernel<4><<<grid, block, smem, c.stream>>>(F);
+    } else {
+        const size_t smem = 2 * VStage<WF_MAX_LAYERS>::bytes_per_thread * block;
+        cudaError_t e = cudaFuncSetAttribute(vertical_split_kernel<WF_MAX_LAYERS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        vertical_split_kernel<WF_MAX_LAYERS><<<grid, block, smem, c.stream>>>(F);
+    }
     return cudaGetLastError();
 }
 
