@@ -19,13 +19,15 @@ CSRC = PKG_ROOT / "csrc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units of the step library and their floating-point contraction policy:
 # FP64 plain-form kernels are compiled without implicit FMA contraction so that every
-# operation rounds like the reference's scalar Float64 code; the split form contracts freely.
-# The adaptive sub-step selection serves both forms and follows the FP64 policy.
+# operation rounds like the reference's scalar Float64 code; the split form contracts freely and
+# divides in FP32 with the full-range approximate division (2 ulp; its FP32 rates carry 1e-7
+# relative error anyway, and every balance quantity is an exact double-FP32 partition). The
+# adaptive sub-step selection serves both forms and follows the FP64 policy.
 CUDA_UNITS = [
     ("wf_api.cu", []),
     ("wf_plan.cpp", None),
     ("kernels_fp64.cu", ["--fmad=false"]),
-    ("kernels_split.cu", []),
+    ("kernels_split.cu", ["-prec-div=false"]),
     ("kernels_adaptive.cu", ["--fmad=false"]),
 ]
 
