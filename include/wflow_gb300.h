@@ -249,9 +249,19 @@ void wf_destroy(WfHandle* h);
 const char* wf_last_error(const WfHandle* h);
 
 /* Forcing of the next step (AtmosphericForcing, Wflow/src/forcing.jl:2-10; io.jl:108-160):
- * host arrays of n_land*n_members values, member-major, land order. */
+ * host arrays of n_land*n_members values, member-major, land order (or n_land values, the
+ * same for every member). From pinned host memory the copy is asynchronous: the arrays must
+ * stay unchanged until the next wf_step (or wf_synchronize after wf_step_async) returns. */
 int32_t wf_set_forcing(WfHandle* h, const double* precipitation, const double* potential_evaporation,
                        const double* temperature, int64_t count);
+/* The same with the host-to-device copies on a stream of the handle's own, so that they overlap
+ * a step still running (call it after wf_step_async of the previous step); the conversion into
+ * the model's layout waits for that step. The arrays must stay unchanged until the step that
+ * consumes them has returned from wf_step / wf_synchronize. No counterpart in the reference
+ * (Wflow reads the forcing between steps); it is the same boundary as wf_set_forcing,
+ * pipelined. */
+int32_t wf_set_forcing_async(WfHandle* h, const double* precipitation, const double* potential_evaporation,
+                             const double* temperature, int64_t count);
 /* Same from device pointers already in the library's slot order (see wf_get_slot_order). */
 int32_t wf_set_forcing_device_slots(WfHandle* h, const void* precipitation,
                                     const void* potential_evaporation, const void* temperature);

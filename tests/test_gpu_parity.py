@@ -264,3 +264,25 @@ def test_split_form_accuracy_hourly_ensemble(gpu_lib):
     print("split hourly ensemble errors", w)
     assert w["outlet_q"] <= 1e-4, w
     assert w["closure"] <= 1e-7, w
+
+
+def test_async_forcing_pipeline_matches_synchronous_steps(gpu_lib):
+    # wf_set_forcing_async of step k+1 issued while step k runs (wf_step_async) gives the same
+    # state as wf_set_forcing + wf_step, for both forms
+    import torch
+    dom = synthetic.make_domain(32, 1000.0, seed=21)
+    for form in (abi.WF_FORM_FP64, abi.WF_FORM_SPLIT):
+        cfg = synthetic.make_config(86400.0, form=form)
+        a, b = Model(cfg, dom), Model(cfg, dom)
+        forc = [[torch.from_numpy(x).pin_memory() for x in synthetic.forcing(s, cfg.dt, dom.n_land, seed=21)]
+                for s in range(5)]
+        b.set_forcing_async(*[x.numpy() for x in forc[0]])
+        for s in range(5):
+            a.run_timestep(*[x.numpy() for x in forc[s]])
+            b.step_async()
+            if s + 1 < 5:
+                b.set_forcing_async(*[x.numpy() for x in forc[s + 1]])
+            b.synchronize()
+        for f in ["SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE", "SATURATED_WATER_DEPTH"]:
+            assert np.array_equal(a.get_value(f), b.get_value(f)), (form, f)
+        assert np.array_equal(a.outlets(0), b.outlets(0))

@@ -91,6 +91,11 @@ struct WfHandle {
     WfAdaptive ad[3] = {};        // WF_ADAPT_SSF, WF_ADAPT_LAND, WF_ADAPT_RIVER
     int32_t* h_more = nullptr;    // pinned host copy of WfAdaptive::more
     int64_t last_substeps[3] = {0, 0, 0};
+    // wf_set_forcing_async: host-to-device copies on a stream of their own
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_fcopied = nullptr, ev_fconsumed = nullptr;
+    double* fstage = nullptr;     // [3][n_land * M] staged forcing in external order
+    double* outlets_buf = nullptr;  // [outlets * M] outlet discharge for wf_get_outlets
 };
 
 namespace {
@@ -1034,6 +1039,12 @@ void wf_destroy(WfHandle* h) {
     for (void* p : h->allocs) cudaFree(p);
     if (h->host_pinned) cudaFreeHost(h->host_pinned);
     if (h->h_more) cudaFreeHost(h->h_more);
+    if (h->copy_stream) {
+        cudaStreamSynchronize(h->copy_stream);
+        cudaStreamDestroy(h->copy_stream);
+    }
+    if (h->ev_fcopied) cudaEventDestroy(h->ev_fcopied);
+    if (h->ev_fconsumed) cudaEventDestroy(h->ev_fconsumed);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (auto& e : h->kev)
@@ -1042,16 +1053,18 @@ void wf_destroy(WfHandle* h) {
     delete h;
 }
 
-int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const double* T, int64_t count) {
-    if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
+}  // extern "C"
+
+namespace {
+
+// Forcing arrays staged on the device in external order (stg[k], k = P, PET, T) into the slot
+// order (and FP32 for the split form), on the handle's stream.
+int enqueue_forcing_gathers(WfHandle* h, double* const stg_of[3], int64_t count) {
     const int64_t full = h->n * h->M;
-    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
-    const double* src[3] = {P, PET, T};
     const int dst[3] = {PRECIP, POTEVAP, TEMP};
     const int block = 256;
     for (int k = 0; k < 3; ++k) {
-        double* stg = h->staging + (size_t)k * std::max(h->n, h->nr) * h->M;
-        CK(cudaMemcpyAsync(stg, src[k], count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        double* stg = stg_of[k];
         const int g = grid_of(h->F.land_slots * h->M, block);
         if (h->F.split) {
             if (count == full)
@@ -1069,6 +1082,50 @@ int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const do
         }
         CK(cudaGetLastError());
     }
+    return WF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const double* T, int64_t count) {
+    if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
+    const int64_t full = h->n * h->M;
+    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
+    const double* src[3] = {P, PET, T};
+    double* stg[3];
+    for (int k = 0; k < 3; ++k) {
+        stg[k] = h->staging + (size_t)k * std::max(h->n, h->nr) * h->M;
+        CK(cudaMemcpyAsync(stg[k], src[k], count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
+    return enqueue_forcing_gathers(h, stg, count);
+}
+
+int32_t wf_set_forcing_async(WfHandle* h, const double* P, const double* PET, const double* T, int64_t count) {
+    if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
+    const int64_t full = h->n * h->M;
+    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
+    if (!h->copy_stream) {  // first call: copy stream, events and a staging buffer of its own
+        CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_fcopied, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_fconsumed, cudaEventDisableTiming));
+        int rc = dalloc(h, &h->fstage, (size_t)3 * full);
+        if (rc) return rc;
+    }
+    // the staging buffer is free once the gathers of the previous call ran
+    CK(cudaStreamWaitEvent(h->copy_stream, h->ev_fconsumed, 0));
+    const double* src[3] = {P, PET, T};
+    double* stg[3];
+    for (int k = 0; k < 3; ++k) {
+        stg[k] = h->fstage + (size_t)k * full;
+        CK(cudaMemcpyAsync(stg[k], src[k], count * sizeof(double), cudaMemcpyHostToDevice, h->copy_stream));
+    }
+    CK(cudaEventRecord(h->ev_fcopied, h->copy_stream));
+    CK(cudaStreamWaitEvent(h->stream, h->ev_fcopied, 0));
+    int rc = enqueue_forcing_gathers(h, stg, count);
+    if (rc) return rc;
+    CK(cudaEventRecord(h->ev_fconsumed, h->stream));
     return WF_OK;
 }
 
@@ -1187,10 +1244,14 @@ int32_t wf_get_outlets(WfHandle* h, int32_t which, double* dst, int64_t capacity
     if (h->F.split) {  // double-FP32 pairs: convert on the device, one copy out
         if (need > 0) {
             const int f = which == 0 ? RV_Q_AVG : RV_Q;
+            if (!h->outlets_buf) {
+                int rc = dalloc(h, &h->outlets_buf, (size_t)need);
+                if (rc) return rc;
+            }
             outlets_ff_kernel<<<(unsigned)((need + 255) / 256), 256, 0, h->stream>>>(
-                h->F.RMh[f], h->F.RMl[f], h->d_outlet_slots, (int64_t)h->outlet_slots.size(), h->M, h->staging);
+                h->F.RMh[f], h->F.RMl[f], h->d_outlet_slots, (int64_t)h->outlet_slots.size(), h->M, h->outlets_buf);
             CK(cudaGetLastError());
-            CK(cudaMemcpyAsync(dst, h->staging, need * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(dst, h->outlets_buf, need * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         }
         CK(cudaStreamSynchronize(h->stream));
         *n_written = need;

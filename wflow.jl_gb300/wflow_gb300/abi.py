@@ -180,6 +180,7 @@ def _declare(lib):
         "wf_destroy": (None, [H]),
         "wf_last_error": (C.c_char_p, [H]),
         "wf_set_forcing": (_i32, [H, _pd, _pd, _pd, _i64]),
+        "wf_set_forcing_async": (_i32, [H, _pd, _pd, _pd, _i64]),
         "wf_set_forcing_device_slots": (_i32, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
         "wf_step": (_i32, [H]),
         "wf_step_async": (_i32, [H]),

@@ -59,6 +59,14 @@ class Model:
         cnt = arrs[0].size
         self._check(self.lib.wf_set_forcing(self.h, *[abi.as_ptr(a) for a in arrs], cnt), "wf_set_forcing")
 
+    def set_forcing_async(self, precipitation, potential_evaporation, temperature):
+        """wf_set_forcing_async: the copies overlap a step still running. The arrays (pinned
+        host memory for a real overlap) are kept referenced until the next step returns."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (precipitation, potential_evaporation, temperature)]
+        self._pending_forcing = arrs
+        self._check(self.lib.wf_set_forcing_async(self.h, *[abi.as_ptr(a) for a in arrs], arrs[0].size),
+                    "wf_set_forcing_async")
+
     def update_model(self):
         self._check(self.lib.wf_step(self.h), "wf_step")
 
