@@ -286,3 +286,24 @@ def test_async_forcing_pipeline_matches_synchronous_steps(gpu_lib):
         for f in ["SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE", "SATURATED_WATER_DEPTH"]:
             assert np.array_equal(a.get_value(f), b.get_value(f)), (form, f)
         assert np.array_equal(a.outlets(0), b.outlets(0))
+
+
+def test_six_soil_layers_and_constant_kv_both_forms(gpu_lib):
+    # more than four soil layers (the kernels' 8-layer instantiation) with the
+    # exponential_constant conductivity profile
+    layers = (50.0, 100.0, 200.0, 400.0, 600.0)
+    dom = synthetic.make_domain(24, 1000.0, seed=22, n_layers_cfg=layers)
+    params = dict(dom.params)
+    params["z_exp"] = np.full(dom.n_land, 0.8)
+    cfg = synthetic.make_config(86400.0, layers=layers)
+    cfg.kv_profile = abi.WF_KV_EXPONENTIAL_CONSTANT
+    gpu, orc, res = run_pair(dom, cfg, 10, params=params, check_every=5)
+    assert gpu.N == 6
+    assert_parity(res)
+    cfgs = synthetic.make_config(86400.0, form=abi.WF_FORM_SPLIT, layers=layers)
+    cfgs.kv_profile = abi.WF_KV_EXPONENTIAL_CONSTANT
+    w = split_errors(dom, cfgs, 20, params=params)
+    print("split six layers errors", w)
+    assert w["outlet_q"] <= 1e-4, w
+    assert w["soil_storage"] <= 1e-4, w
+    assert w["closure"] <= 1e-7, w
