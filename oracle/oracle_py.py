@@ -102,6 +102,30 @@ class Soil:
         return np.array((C.c_double * n).from_buffer(self.buf, off)[:])
 
 
+class Reservoir(C.Structure):
+    """OrcReservoir (wflow_oracle.cpp): one reservoir's parameters, boundary conditions of the
+    step and state."""
+    _fields_ = [("outflow_type", C.c_int32)] + [(n, C.c_double) for n in (
+        "area", "maximum_storage", "threshold", "rating_curve_coefficient", "rating_curve_exponent",
+        "maximum_release", "demand", "target_minimum_fraction", "target_full_fraction",
+        "external_inflow", "precipitation", "evaporation", "inflow_overland", "inflow_subsurface", "outflow_obs",
+        "storage", "waterlevel", "outflow",
+        "inflow_cumulative", "outflow_cumulative", "actevap_cumulative", "abstraction_cumulative")]
+
+    def __init__(self, **kw):
+        super().__init__()
+        nan = float("nan")
+        for n in ("maximum_storage", "threshold", "rating_curve_coefficient", "rating_curve_exponent",
+                  "maximum_release", "demand", "target_minimum_fraction", "target_full_fraction", "outflow_obs"):
+            setattr(self, n, nan)
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+def reservoir_update(r, q, dt):
+    lib().orc_reservoir_update(C.byref(r), C.c_double(q), C.c_double(dt))
+
+
 def call_out(fname, *args, nout):
     out = (C.c_double * nout)()
     fn = getattr(lib(), fname)

@@ -1503,6 +1503,128 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
 
 }  // namespace
 
+// ====================================================================== reservoirs ======
+//
+// Reservoir update at a river node (routing/surface/reservoir.jl:583-628), with the outflow
+// functions of types 2 (free weir, without a linked lower reservoir), 3 (modified Puls) and 4
+// (simple), the observed-outflow override (reservoir.jl:524-545) and the linear storage
+// profile (S = A H). The river-side wrapper (surface_kinwave.jl:441-489) limits a negative
+// external inflow (abstraction) to 98 % of the storage per step and forms the net inflow.
+struct OrcReservoir {
+    int32_t outflow_type;  // 2 free weir, 3 modified Puls, 4 simple
+    double area, maximum_storage, threshold, rating_curve_coefficient, rating_curve_exponent;
+    double maximum_release, demand, target_minimum_fraction, target_full_fraction;
+    // boundary conditions of the step
+    double external_inflow, precipitation, evaporation, inflow_overland, inflow_subsurface, outflow_obs;
+    // state
+    double storage, waterlevel, outflow;
+    double inflow_cumulative, outflow_cumulative, actevap_cumulative, abstraction_cumulative;
+};
+
+namespace {
+
+// reservoir.jl:389-418
+void reservoir_simple(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
+                      double& outflow, double& storage) {
+    storage = r.storage + (inflow + precipitation - evaporation) * dt;
+    storage = jmax(storage, 0.0);
+    double fill_fraction = storage / r.maximum_storage;
+    double fac = scurve(fill_fraction, r.target_minimum_fraction, 1.0, 30.0);
+    double demand_release = jmin(fac * r.demand, storage / dt);
+    storage -= demand_release * dt;
+    double release_wanted = jmax(0.0, (storage - r.maximum_storage * r.target_full_fraction) / dt);
+    double overflow_q = jmax(0.0, (storage - r.maximum_storage) / dt);
+    double release_realized = jmin(release_wanted, overflow_q + r.maximum_release - demand_release);
+    storage -= release_realized * dt;
+    outflow = release_realized + demand_release;
+}
+
+// reservoir.jl:424-452
+void reservoir_modified_puls(const OrcReservoir& r, double precipitation, double evaporation, double inflow,
+                             double dt, double& outflow, double& storage) {
+    double res_factor = r.area / (dt * std::sqrt(r.rating_curve_coefficient));
+    double si_factor = r.storage / dt + precipitation - evaporation + inflow;
+    double si_factor_adj = si_factor - r.area * r.threshold / dt;
+    if (si_factor_adj > 0.0) {
+        double quadratic_sol_term = -res_factor + std::sqrt((res_factor * res_factor + 4 * si_factor_adj));
+        outflow = quadratic_sol_term > 0.0 ? 0.25 * quadratic_sol_term * quadratic_sol_term : 0.0;
+    } else {
+        outflow = 0.0;
+    }
+    outflow = jmin(outflow, si_factor);
+    storage = (si_factor - outflow) * dt;
+}
+
+// reservoir.jl:482-521 without a linked lower reservoir
+void reservoir_free_weir(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
+                         double& outflow, double& storage) {
+    double storage_input = jmax(r.storage / dt + precipitation - evaporation + inflow, 0.0);
+    if (r.waterlevel > r.threshold) {
+        double dh = r.waterlevel - r.threshold;
+        outflow = r.rating_curve_coefficient * jpow(dh, r.rating_curve_exponent);
+        double maxflow = dh * r.area / dt;
+        outflow = jmin(outflow, maxflow);
+    } else {
+        outflow = 0.0;
+    }
+    storage = (storage_input - outflow) * dt;
+}
+
+// reservoir.jl:524-545
+void reservoir_outflow_obs(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
+                           double& outflow, double& storage) {
+    double storage_input = jmax(r.storage / dt + precipitation - evaporation + inflow, 0.0);
+    outflow = jmin(r.outflow_obs, storage_input);
+    storage = (storage_input - outflow) * dt;
+    if (!std::isnan(r.maximum_storage)) {
+        double overflow = jmax(0.0, (storage - r.maximum_storage) / dt);
+        storage -= overflow * dt;
+        outflow += overflow;
+    }
+}
+
+// reservoir.jl:583-628
+void update_reservoir(OrcReservoir& r, double inflow, double dt) {
+    double precipitation = r.precipitation * r.area;
+    double available_storage = r.storage + (inflow + precipitation) * dt;
+    double potential_evaporation = r.evaporation * r.area;
+    double evaporation = jmin(available_storage / dt, potential_evaporation);
+    double outflow = 0.0, storage = r.storage;
+    if (!std::isnan(r.outflow_obs)) reservoir_outflow_obs(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else if (r.outflow_type == 2) reservoir_free_weir(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else if (r.outflow_type == 3) reservoir_modified_puls(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else reservoir_simple(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    double waterlevel = r.waterlevel + (storage - r.storage) / r.area;  // linear profile
+    r.storage = storage;
+    r.waterlevel = waterlevel;
+    r.outflow = outflow;
+    r.inflow_cumulative += inflow * dt;
+    r.outflow_cumulative += outflow * dt;
+    r.actevap_cumulative += evaporation / r.area * dt;
+}
+
+// surface_kinwave.jl:441-489: net inflow of the reservoir at a river node whose discharge is q
+void update_reservoir_at_node(OrcReservoir& r, double q, double dt) {
+    double inflow;
+    if (r.external_inflow < 0.0) {
+        double abstraction = jmin(-r.external_inflow, (r.storage / dt) * 0.98);
+        r.abstraction_cumulative += abstraction * dt;
+        inflow = -abstraction;
+    } else {
+        inflow = r.external_inflow;
+    }
+    double net_inflow = q + r.inflow_overland + r.inflow_subsurface + inflow;
+    update_reservoir(r, net_inflow, dt);
+}
+
+}  // namespace
+
+extern "C" {
+// Reservoir at a river node with discharge q after the node's kinematic-wave update.
+void orc_reservoir_update(OrcReservoir* r, double q, double dt) { update_reservoir_at_node(*r, q, dt); }
+int32_t orc_reservoir_size() { return (int32_t)sizeof(OrcReservoir); }
+}  // extern "C"
+
 extern "C" {
 
 int32_t orc_model_step(OrcModel* m, int32_t n_threads) {

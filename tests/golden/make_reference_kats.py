@@ -291,12 +291,20 @@ def build():
                        q_max=num(R, 228), profile=1, z_exp=num(R, 229), soil=soil_b),
                   dict(q=num(R, 249), water_table_depth=num(R, 250), exfilt=num(R, 251), net_flux=num(R, 252))))
     riv = dict(flow_width=nums(R, 300)[:2], flow_length=nums(R, 301)[:2], alpha=nums(R, 343)[:2],
-               q=nums(R, 350)[:2], p=0.05)
-    K.append(case("river_stable_timestep_and_update", "kinwave_river_update", f"{R}:290-376", riv,
+               q=nums(R, 350)[:2], p=0.05,
+               reservoir=dict(external_inflow=num(R, 313), precipitation=num(R, 314), evaporation=num(R, 315),
+                              inflow_overland=num(R, 316), inflow_subsurface=num(R, 317), area=num(R, 323),
+                              maximum_release=num(R, 324), demand=num(R, 325),
+                              target_minimum_fraction=num(R, 326), target_full_fraction=num(R, 327),
+                              maximum_storage=num(R, 328), waterlevel=num(R, 331), storage=num(R, 332),
+                              outflow_type=4))
+    K.append(case("river_stable_timestep_and_update", "kinwave_river_update", f"{R}:290-383", riv,
                   dict(dt=num(R, 372), q=nums(R, 373)[:2], h=nums(R, 374)[:2], storage=nums(R, 375)[:2],
-                       q_cumulative=nums(R, 376)[:2], reservoir_outflow=num(R, 381)),
-                  note="node 2 receives the upstream reservoir outflow; its asserted value (line 381) is used "
-                       "as that input, so node 2 is a derived pin at rtol 1e-7"))
+                       q_cumulative=nums(R, 376)[:2], reservoir_waterlevel=num(R, 379),
+                       reservoir_storage=num(R, 380), reservoir_outflow=num(R, 381),
+                       reservoir_actevap_cumulative=num(R, 382)),
+                  note="node 1 carries a simple reservoir (outflow type 4, linear storage profile) with an "
+                       "abstraction; node 2 receives its outflow (the test's upstream list also keeps node 1)"))
     # ------------------------------------------------------------------------ utils.jl
     K.append(case("scurve", "scurve", f"{U}:66-77",
                   dict(x=num(U, 71), a=num(U, 67), b=num(U, 68), c=num(U, 69)), dict(s=num(U, 73))))

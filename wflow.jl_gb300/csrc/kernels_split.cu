@@ -218,30 +218,6 @@ struct ColumnS {
     }
 };
 
-// ----------------------------------------------------------------- vertical kernel ------
-//
-// GB300 issues FP64 instructions (arithmetic, compares and FP32<->FP64 conversions alike) at
-// about 1/70 of its FP32 FMA rate, so this kernel keeps FP64 instructions to the few that the
-// water balance needs:
-//   * every store (canopy, snow, liquid snow water, unsaturated layers) is its FP64 content at
-//     the start of the step plus the exact sum of the step's FP32 increments, accumulated with
-//     error-free transformations (TwoSum/TwoProd) in an FP32 pair and added once at the end;
-//   * every partition of a flux that crosses the cell boundary (throughfall/interception/
-//     stemflow, rain/snow, river/land/soil runoff, infiltration/infiltration excess/saturation
-//     excess) is an FP64 residual, so the parts always sum to the whole;
-//   * the outputs that enter the balance are FP64 sums of the same FP32 values the stores saw.
-// Rates, limiters, layer geometry and all transcendental functions are FP32.
-
-// FP64 reciprocal from an FP32 seed and two Newton steps (about 4 FP64 FMAs instead of a
-// division); relative error near 1 ulp for normal inputs, inf/0/NaN handled by the seed check.
-__device__ __forceinline__ double wfm_rcp(double x) {
-    const float xf = (float)x;
-    double r = (double)(1.0f / xf);
-    if (!(fabsf(xf) < 3.0e38f && xf != 0.0f)) return 1.0 / x;
-    r = r * fma(-x, r, 2.0);
-    r = r * fma(-x, r, 2.0);
-    return r;
-}
 
 // Store of the split form: its content at the start of the step (a double-FP32 pair) plus
 // the exact sum of the step's FP32 increments (TwoSum / TwoProd), added once at the end.
