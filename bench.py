@@ -125,6 +125,22 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def whole_job_rate(local_seconds, cells_per_rank, steps, device=None):
+    """Replicas: every rank steps its own copy of the workload (members and catchments are
+    independent, so the path has no exchange step); the job's time is the slowest rank's and its
+    work the sum over ranks. Returns (cell-timesteps/s of the whole job, job seconds)."""
+    import torch
+    import torch.distributed as dist
+
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    t = float(local_seconds)
+    if ws > 1:
+        x = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return cells_per_rank * steps * ws / t, t
+
+
 def build_workload(name, form, seed=1):
     from wflow_gb300 import abi, synthetic
 
@@ -230,12 +246,9 @@ def run_gpu(args):
     launches = mt1["kernel_launches"] - launches0
     substeps = {k: (mt1["substeps_" + k] - mt0["substeps_" + k]) / K for k in ("land", "river", "subsurface")}
     clk = clocks.stop()
-    if ws > 1:
-        t = torch.tensor([elapsed_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
     cells = n * members
-    value = cells * K * ws / (elapsed_ms / 1e3)
+    value, job_s = whole_job_rate(elapsed_ms / 1e3, cells, K, device=dev)
+    elapsed_ms = job_s * 1e3
     # ---- end to end through the public API: pinned host forcing in, outlet discharge out
     host = []
     for s in range(W, W + K):
@@ -279,11 +292,7 @@ def run_gpu(args):
     model.synchronize()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = cells * K * ws / e2e_s
+    e2e_value, e2e_s = whole_job_rate(e2e_s, cells, K, device=dev)
     # ---- per-kernel times (eager launches with events between kernels) for the roofline
     model.set_tuning(**(tuning or {}), use_graph=0, kernel_timing=1)
     for s in range(min(K, 5)):
