@@ -193,6 +193,7 @@ typedef enum WfField {
     WF_F_BALANCE_SUBSURFACE_ERROR,
     WF_F_BALANCE_SUBSURFACE_RELATIVE_ERROR,
     WF_F_VOLUMETRIC_WATER_CONTENT,  /* layered */
+    WF_F_LAND_QIN_AVERAGE,          /* overland inflow from upstream cells, step average [m3 s-1] */
     WF_F_LAND_END_,
     /* river */
     WF_F_RIVER_Q = 100,
@@ -203,8 +204,58 @@ typedef enum WfField {
     WF_F_RIVER_INWATER,
     WF_F_BALANCE_RIVER_ERROR,
     WF_F_BALANCE_RIVER_RELATIVE_ERROR,
-    WF_F_RIVER_END_
+    WF_F_RIVER_END_,
+    /* reservoirs (models created with wf_create_with_reservoirs), member-major over the
+     * reservoir order of WfReservoirs; ReservoirVariables / ReservoirBC of reservoir.jl:202-297 */
+    WF_F_RESERVOIR_STORAGE = 200,       /* state [m3] */
+    WF_F_RESERVOIR_WATERLEVEL,          /* state [m] */
+    WF_F_RESERVOIR_OUTFLOW,             /* [m3 s-1], last sub-step */
+    WF_F_RESERVOIR_OUTFLOW_AVERAGE,     /* [m3 s-1] */
+    WF_F_RESERVOIR_INFLOW_AVERAGE,      /* net inflow [m3 s-1] */
+    WF_F_RESERVOIR_ACTEVAP_AVERAGE,     /* [m s-1], set by the water balance (mass_balance.jl:274) */
+    WF_F_RESERVOIR_ABSTRACTION_AVERAGE, /* actual external abstraction [m3 s-1] */
+    WF_F_RESERVOIR_INFLOW_OVERLAND,     /* [m3 s-1] */
+    WF_F_RESERVOIR_INFLOW_SUBSURFACE,   /* [m3 s-1] */
+    WF_F_RESERVOIR_PRECIPITATION,       /* input: mean over the reservoir area [m s-1] */
+    WF_F_RESERVOIR_EVAPORATION,         /* input: mean potential evaporation [m s-1] */
+    WF_F_RESERVOIR_EXTERNAL_INFLOW,     /* input [m3 s-1]; negative = abstraction */
+    WF_F_RESERVOIR_OUTFLOW_OBS,         /* input [m3 s-1]; NaN = no observation */
+    WF_F_BALANCE_RESERVOIR_ERROR,
+    WF_F_BALANCE_RESERVOIR_RELATIVE_ERROR,
+    WF_F_RESERVOIR_END_
 } WfField;
+
+/* Outflow functions of a reservoir (ReservoirOutflowType, Wflow/src/routing/surface/reservoir.jl). */
+typedef enum WfReservoirOutflow {
+    WF_RES_FREE_WEIR = 2,     /* Q = b (H - H0)^e, no linked lower reservoir (reservoir.jl:482-521) */
+    WF_RES_MODIFIED_PULS = 3, /* Q = b (H - H0)^2 by the modified Puls approach (reservoir.jl:424-452) */
+    WF_RES_SIMPLE = 4         /* simple reservoir (reservoir.jl:389-418) */
+} WfReservoirOutflow;
+
+/* Reservoirs at river cells (reservoir__flag; reservoir.jl:1-300, network.jl:296-357), with the
+ * linear storage profile S = A H (storage_curve_type 1). The reservoir's outlet cell becomes a pit
+ * of the land and river upstream lists (domain.jl:95-121): the outlet cell's overland and
+ * subsurface discharge feed the reservoir (surface_kinwave.jl:771-802), its river discharge
+ * enters the reservoir within the river sweep and the reservoir outflow is the inflow of the
+ * downstream river cell (surface_kinwave.jl:441-489). Per-step inputs (precipitation and
+ * evaporation over the reservoir area, external inflow, observed outflow) are set with
+ * wf_set_field; the caller averages the forcing over the reservoir area and zeroes the land
+ * forcing there, as Wflow's forcing reader does (io.jl:128-137). */
+typedef struct WfReservoirs {
+    int64_t n;                              /* number of reservoirs */
+    const int32_t* river_index;             /* [n] river cell of each reservoir outlet */
+    const int32_t* outflow_curve_type;      /* [n] WfReservoirOutflow */
+    const double* area;                     /* reservoir_surface__area [m2] */
+    const double* waterlevel;               /* initial reservoir_water_surface__elevation [m] */
+    const double* maximum_storage;          /* reservoir_water__max_volume [m3] (NaN where unused) */
+    const double* threshold;                /* reservoir_water_flow_threshold_level__elevation [m] */
+    const double* rating_curve_coefficient; /* reservoir_water__rating_curve_coefficient */
+    const double* rating_curve_exponent;    /* reservoir_water__rating_curve_exponent */
+    const double* maximum_release;          /* reservoir_water_release_below_spillway__max_volume_flow_rate */
+    const double* demand;                   /* reservoir_water_demand__required_downstream_volume_flow_rate */
+    const double* target_minimum_fraction;  /* reservoir_water__target_min_volume_fraction */
+    const double* target_full_fraction;     /* reservoir_water__target_full_volume_fraction */
+} WfReservoirs;
 
 typedef struct WfHandle WfHandle;
 
@@ -217,7 +268,8 @@ typedef struct WfMetrics {
     int64_t substeps_subsurface;
     int64_t kernel_launches;      /* kernels launched by steps (graph nodes count once each) */
     double step_ms_total;         /* CUDA-event time of all steps */
-    double max_abs_balance_error; /* of the last step with water_mass_balance, over all domains */
+    double max_abs_balance_error; /* reserved, always 0: the balance errors are fields
+                                     (WF_F_BALANCE_*), read them with wf_get_field */
     int32_t device_status;        /* last device status word (0 = ok) */
     int32_t n_chains_land;        /* routing chains of the land graph */
     int32_t n_chains_river;
@@ -243,6 +295,13 @@ int32_t wf_abi_version(void);
  * device state in the cold-start values (soil.jl:164-178, utils.jl:916-937). */
 int32_t wf_create(const WfConfig* config, const WfDomain* domain, const WfParams* params,
                   int32_t device, WfHandle** out);
+/* The same with reservoirs (reservoir__flag = true; ReservoirModel, reservoir.jl:290-300);
+ * reservoirs may be NULL or hold n = 0. Rejected: a reservoir at a river pit (the reference
+ * raises the same error, surface_kinwave.jl:479-483), two reservoirs draining into one river
+ * cell (the reference then keeps the outflow of whichever it updates last), an unknown outflow
+ * type, a non-positive area. */
+int32_t wf_create_with_reservoirs(const WfConfig* config, const WfDomain* domain, const WfParams* params,
+                                  const WfReservoirs* reservoirs, int32_t device, WfHandle** out);
 void wf_destroy(WfHandle* h);
 
 /* Message of the last error on this handle (or of the last failed wf_create when h is NULL). */
@@ -329,10 +388,12 @@ int32_t wf_get_kernel_times(WfHandle* h, double* ms5, int64_t* calls);
 /* Number of land cells, river cells, river pits and layer count of a handle. */
 int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_outlets,
                      int32_t* n_layers, int32_t* n_members);
+/* Number of reservoirs of a handle. */
+int32_t wf_get_reservoir_count(WfHandle* h, int64_t* n_reservoirs);
 
 /* ---- diagnostics (no counterpart in the reference) ---------------------------------------
  * Size of the ABI structs for binding checks: 0 WfConfig, 1 WfDomain, 2 WfParams,
- * 3 WfMetrics, 4 WfTuning; -1 otherwise. */
+ * 3 WfMetrics, 4 WfTuning, 5 WfReservoirs; -1 otherwise. */
 int32_t wf_struct_size(int32_t which);
 /* Host-only planning of a drainage graph's wavefront schedule (no GPU needed):
  * out_counts = {n_chains, n_chunks, n_slots, max_chain_len}; slot_of_node optional [n];

@@ -146,7 +146,7 @@ def fcall(fname, *args, types=None):
 class OracleModel:
     """The oracle's full model on one synthetic domain (the CPU reference of a wf_create handle)."""
 
-    def __init__(self, cfg, dom, params=None):
+    def __init__(self, cfg, dom, params=None, reservoirs=None):
         import sys
         sys.path.insert(0, str(ORACLE_DIR.parent / "wflow.jl_gb300"))
         from wflow_gb300 import synthetic
@@ -155,7 +155,13 @@ class OracleModel:
         self._params = params if params is not None else dom.params
         self._d, self._p = synthetic.c_structs(dom, self._params)
         h = C.c_void_p()
-        st = lib().orc_model_create(C.byref(cfg), C.byref(self._d), C.byref(self._p), C.byref(h))
+        self._reservoirs = reservoirs
+        if reservoirs is not None:
+            self._r = synthetic.c_reservoirs(reservoirs)
+            st = lib().orc_model_create_with_reservoirs(C.byref(cfg), C.byref(self._d), C.byref(self._p),
+                                                        C.byref(self._r), C.byref(h))
+        else:
+            st = lib().orc_model_create(C.byref(cfg), C.byref(self._d), C.byref(self._p), C.byref(h))
         self.h = h
         if st != 0:
             msg = lib().orc_model_error(h)
@@ -163,6 +169,7 @@ class OracleModel:
         self.n = dom.n_land
         self.nr = dom.n_river
         self.M = max(1, cfg.n_members)
+        self.nres = 0 if reservoirs is None else int(reservoirs["river_index"].size)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -177,7 +184,7 @@ class OracleModel:
         lib().orc_model_step(self.h, threads)
 
     def get(self, field, layer=0):
-        nn = (self.nr if field >= 100 else self.n) * self.M
+        nn = (self.nres if field >= 200 else self.nr if field >= 100 else self.n) * self.M
         out = np.empty(nn)
         st = lib().orc_model_get(self.h, field, layer, out.ctypes.data_as(_pd))
         if st != 0:

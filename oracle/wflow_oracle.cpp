@@ -23,6 +23,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <vector>
 
@@ -861,6 +862,122 @@ inline double check_timestepsize(double ts, double t, double end) { return t + t
 
 }  // namespace
 
+// ====================================================================== reservoirs ======
+//
+// Reservoir update at a river node (routing/surface/reservoir.jl:583-628), with the outflow
+// functions of types 2 (free weir, without a linked lower reservoir), 3 (modified Puls) and 4
+// (simple), the observed-outflow override (reservoir.jl:524-545) and the linear storage
+// profile (S = A H). The river-side wrapper (surface_kinwave.jl:441-489) limits a negative
+// external inflow (abstraction) to 98 % of the storage per step and forms the net inflow.
+struct OrcReservoir {
+    int32_t outflow_type;  // 2 free weir, 3 modified Puls, 4 simple
+    double area, maximum_storage, threshold, rating_curve_coefficient, rating_curve_exponent;
+    double maximum_release, demand, target_minimum_fraction, target_full_fraction;
+    // boundary conditions of the step
+    double external_inflow, precipitation, evaporation, inflow_overland, inflow_subsurface, outflow_obs;
+    // state
+    double storage, waterlevel, outflow;
+    double inflow_cumulative, outflow_cumulative, actevap_cumulative, abstraction_cumulative;
+};
+
+namespace {
+
+// reservoir.jl:389-418
+void reservoir_simple(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
+                      double& outflow, double& storage) {
+    storage = r.storage + (inflow + precipitation - evaporation) * dt;
+    storage = jmax(storage, 0.0);
+    double fill_fraction = storage / r.maximum_storage;
+    double fac = scurve(fill_fraction, r.target_minimum_fraction, 1.0, 30.0);
+    double demand_release = jmin(fac * r.demand, storage / dt);
+    storage -= demand_release * dt;
+    double release_wanted = jmax(0.0, (storage - r.maximum_storage * r.target_full_fraction) / dt);
+    double overflow_q = jmax(0.0, (storage - r.maximum_storage) / dt);
+    double release_realized = jmin(release_wanted, overflow_q + r.maximum_release - demand_release);
+    storage -= release_realized * dt;
+    outflow = release_realized + demand_release;
+}
+
+// reservoir.jl:424-452
+void reservoir_modified_puls(const OrcReservoir& r, double precipitation, double evaporation, double inflow,
+                             double dt, double& outflow, double& storage) {
+    double res_factor = r.area / (dt * std::sqrt(r.rating_curve_coefficient));
+    double si_factor = r.storage / dt + precipitation - evaporation + inflow;
+    double si_factor_adj = si_factor - r.area * r.threshold / dt;
+    if (si_factor_adj > 0.0) {
+        double quadratic_sol_term = -res_factor + std::sqrt((res_factor * res_factor + 4 * si_factor_adj));
+        outflow = quadratic_sol_term > 0.0 ? 0.25 * quadratic_sol_term * quadratic_sol_term : 0.0;
+    } else {
+        outflow = 0.0;
+    }
+    outflow = jmin(outflow, si_factor);
+    storage = (si_factor - outflow) * dt;
+}
+
+// reservoir.jl:482-521 without a linked lower reservoir
+void reservoir_free_weir(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
+                         double& outflow, double& storage) {
+    double storage_input = jmax(r.storage / dt + precipitation - evaporation + inflow, 0.0);
+    if (r.waterlevel > r.threshold) {
+        double dh = r.waterlevel - r.threshold;
+        outflow = r.rating_curve_coefficient * jpow(dh, r.rating_curve_exponent);
+        double maxflow = dh * r.area / dt;
+        outflow = jmin(outflow, maxflow);
+    } else {
+        outflow = 0.0;
+    }
+    storage = (storage_input - outflow) * dt;
+}
+
+// reservoir.jl:524-545
+void reservoir_outflow_obs(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
+                           double& outflow, double& storage) {
+    double storage_input = jmax(r.storage / dt + precipitation - evaporation + inflow, 0.0);
+    outflow = jmin(r.outflow_obs, storage_input);
+    storage = (storage_input - outflow) * dt;
+    if (!std::isnan(r.maximum_storage)) {
+        double overflow = jmax(0.0, (storage - r.maximum_storage) / dt);
+        storage -= overflow * dt;
+        outflow += overflow;
+    }
+}
+
+// reservoir.jl:583-628
+void update_reservoir(OrcReservoir& r, double inflow, double dt) {
+    double precipitation = r.precipitation * r.area;
+    double available_storage = r.storage + (inflow + precipitation) * dt;
+    double potential_evaporation = r.evaporation * r.area;
+    double evaporation = jmin(available_storage / dt, potential_evaporation);
+    double outflow = 0.0, storage = r.storage;
+    if (!std::isnan(r.outflow_obs)) reservoir_outflow_obs(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else if (r.outflow_type == 2) reservoir_free_weir(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else if (r.outflow_type == 3) reservoir_modified_puls(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else reservoir_simple(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    double waterlevel = r.waterlevel + (storage - r.storage) / r.area;  // linear profile
+    r.storage = storage;
+    r.waterlevel = waterlevel;
+    r.outflow = outflow;
+    r.inflow_cumulative += inflow * dt;
+    r.outflow_cumulative += outflow * dt;
+    r.actevap_cumulative += evaporation / r.area * dt;
+}
+
+// surface_kinwave.jl:441-489: net inflow of the reservoir at a river node whose discharge is q
+void update_reservoir_at_node(OrcReservoir& r, double q, double dt) {
+    double inflow;
+    if (r.external_inflow < 0.0) {
+        double abstraction = jmin(-r.external_inflow, (r.storage / dt) * 0.98);
+        r.abstraction_cumulative += abstraction * dt;
+        inflow = -abstraction;
+    } else {
+        inflow = r.external_inflow;
+    }
+    double net_inflow = q + r.inflow_overland + r.inflow_subsurface + inflow;
+    update_reservoir(r, net_inflow, dt);
+}
+
+}  // namespace
+
 // ======================================================================= full model =====
 
 struct OrcModel {
@@ -902,6 +1019,12 @@ struct OrcModel {
         rv_inwater, rv_abs_cum, rv_abs_avg;
     std::vector<double> total_storage;
     std::vector<double> bl_prev, bl_err, bl_rel, bo_prev, bo_err, bo_rel, bs_err, bs_rel, br_prev, br_err, br_rel;
+    // reservoirs (member-major [mbr * nres + k])
+    int64_t nres = 0;
+    std::vector<OrcReservoir> res;
+    std::vector<int32_t> res_of_river;  // [nr] reservoir at a river cell, or -1
+    std::vector<int32_t> res_land;      // [nres] land cell of the reservoir outlet
+    std::vector<double> res_out_avg, res_in_avg, res_evap_avg, res_abs_avg, res_prev, res_err, res_rel;
     int64_t last_sub_land = 0, last_sub_river = 0, last_sub_ssf = 0;
     std::vector<double> buf;
 };
@@ -1162,6 +1285,80 @@ int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p
 
 void orc_model_destroy(OrcModel* m) { delete m; }
 
+// The model with reservoirs (ReservoirModel, routing/surface/reservoir.jl:290-300). Reservoir
+// outlet cells are pits of the land and river upstream lists (domain.jl:95-121,
+// utils.jl:61-71); the topological orders stay those of the full graphs, which remain valid.
+int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p,
+                                         const WfReservoirs* rs, OrcModel** out) {
+    int32_t st = orc_model_create(c, d, p, out);
+    if (st != WF_OK || !rs || rs->n == 0) return st;
+    OrcModel* m = *out;
+    const int64_t nres = rs->n, nr = m->nr, n = m->n;
+    const int M = m->M;
+    auto fail = [&](const std::string& msg) {
+        m->err = msg;
+        return WF_ERR_INVALID;
+    };
+    if (nres < 0 || !rs->river_index || !rs->outflow_curve_type || !rs->area || !rs->waterlevel)
+        return fail("reservoir arrays missing");
+    m->nres = nres;
+    m->res_of_river.assign(nr, -1);
+    m->res_land.assign(nres, -1);
+    std::vector<int32_t> fed(nr, -1);
+    for (int64_t k = 0; k < nres; ++k) {
+        const int32_t v = rs->river_index[k];
+        if (v < 0 || v >= nr) return fail("reservoir river index out of range");
+        if (m->res_of_river[v] >= 0) return fail("two reservoirs at one river cell");
+        if (m->r_ds[v] < 0) return fail("a reservoir without a downstream river node is not supported");
+        if (fed[m->r_ds[v]] >= 0) return fail("two reservoirs drain into one river cell");
+        const int32_t t = rs->outflow_curve_type[k];
+        if (t != 2 && t != 3 && t != 4) return fail("unsupported reservoir outflow type");
+        if (!(rs->area[k] > 0.0)) return fail("reservoir area must be positive");
+        fed[m->r_ds[v]] = (int32_t)k;
+        m->res_of_river[v] = (int32_t)k;
+        m->res_land[k] = m->r_land[v];
+    }
+    // upstream lists without the reservoir outlets
+    std::vector<int32_t> ds_cut(m->ds), rds_cut(m->r_ds);
+    for (int64_t k = 0; k < nres; ++k) {
+        ds_cut[m->res_land[k]] = -1;
+        rds_cut[rs->river_index[k]] = -1;
+    }
+    build_ups(n, ds_cut.data(), m->ups);
+    build_ups(nr, rds_cut.data(), m->r_ups);
+    const double NaN = std::numeric_limits<double>::quiet_NaN();
+    auto par = [&](const double* a, int64_t k) { return a ? a[k] : NaN; };
+    m->res.resize((size_t)M * nres);
+    for (int mbr = 0; mbr < M; ++mbr)
+        for (int64_t k = 0; k < nres; ++k) {
+            OrcReservoir& r = m->res[(size_t)mbr * nres + k];
+            r = OrcReservoir{};
+            r.outflow_type = rs->outflow_curve_type[k];
+            r.area = rs->area[k];
+            r.maximum_storage = par(rs->maximum_storage, k);
+            r.threshold = par(rs->threshold, k);
+            r.rating_curve_coefficient = par(rs->rating_curve_coefficient, k);
+            r.rating_curve_exponent = par(rs->rating_curve_exponent, k);
+            r.maximum_release = par(rs->maximum_release, k);
+            r.demand = par(rs->demand, k);
+            r.target_minimum_fraction = par(rs->target_minimum_fraction, k);
+            r.target_full_fraction = par(rs->target_full_fraction, k);
+            r.external_inflow = 0.0;
+            r.precipitation = 0.0;
+            r.evaporation = 0.0;
+            r.inflow_overland = 0.0;
+            r.inflow_subsurface = 0.0;
+            r.outflow_obs = NaN;
+            r.waterlevel = rs->waterlevel[k];
+            r.storage = r.area * r.waterlevel;  // initialize_storage, linear profile (reservoir.jl:343-360)
+            r.outflow = NaN;
+        }
+    for (auto* v : {&m->res_out_avg, &m->res_in_avg, &m->res_evap_avg, &m->res_abs_avg, &m->res_prev, &m->res_err,
+                    &m->res_rel})
+        v->assign((size_t)M * nres, 0.0);
+    return WF_OK;
+}
+
 int32_t orc_model_set_forcing(OrcModel* m, const double* P, const double* PET, const double* T) {
     int64_t nm = m->n * m->M;
     std::memcpy(m->P.data(), P, nm * 8);
@@ -1190,6 +1387,7 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
             m->bo_prev[o + i] = m->ol_storage[o + i];
         }
         for (int64_t r = 0; r < nr; ++r) m->br_prev[orr + r] = m->rv_storage[orr + r];
+        for (int64_t k = 0; k < m->nres; ++k) m->res_prev[mbr * m->nres + k] = m->res[mbr * m->nres + k].storage;
     }
     // ---- update_land_hydrology_model! (sbm.jl:82-132), per cell
 #pragma omp parallel for num_threads(n_threads) schedule(dynamic, 256)
@@ -1392,6 +1590,19 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
         m->rv_abs_cum[orr + r] = 0.0;
         m->rv_qin_cum[orr + r] = 0.0;
     }
+    // reservoir inflow from the outlet cell's overland and subsurface flow (update_inflow!,
+    // surface_kinwave.jl:771-802) and the reset of the step's cumulatives (set_reservoir_vars!,
+    // :227-237)
+    OrcReservoir* res = m->nres ? m->res.data() + (size_t)mbr * m->nres : nullptr;
+    for (int64_t k = 0; k < m->nres; ++k) {
+        OrcReservoir& r = res[k];
+        r.inflow_overland = m->ol_q_avg[o + m->res_land[k]];
+        r.inflow_subsurface = m->ssf_q_avg[o + m->res_land[k]];
+        r.inflow_cumulative = 0.0;
+        r.abstraction_cumulative = 0.0;
+        r.outflow_cumulative = 0.0;
+        r.actevap_cumulative = 0.0;
+    }
     {
         double t = 0.0;
         int64_t nsub = 0;
@@ -1421,6 +1632,13 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
                 kinematic_wave(m->rv_qin[j], m->rv_q[j], m->rv_qlat[j] + inflow, m->r_alpha[v], dt_s, m->r_length[v],
                                kw);
                 m->rv_q[j] = kw[0];
+                if (m->nres && m->res_of_river[v] >= 0) {
+                    // update_reservoir_model! (surface_kinwave.jl:441-489): the reservoir outflow
+                    // is the inflow of the downstream river cell
+                    OrcReservoir& r = res[m->res_of_river[v]];
+                    update_reservoir_at_node(r, m->rv_q[j], dt_s);
+                    m->rv_qin[orr + m->r_ds[v]] = r.outflow;
+                }
                 m->rv_h[j] = kw[1] / m->r_width[v];
                 m->rv_storage[j] = m->r_length[v] * kw[1];
                 m->rv_q_cum[j] += m->rv_q[j] * dt_s;
@@ -1435,6 +1653,12 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
         m->rv_q_avg[orr + r] = m->rv_q_cum[orr + r] / dt;
         m->rv_abs_avg[orr + r] = m->rv_abs_cum[orr + r] / dt;
         m->rv_qin_avg[orr + r] = m->rv_qin_cum[orr + r] / dt;
+    }
+    for (int64_t k = 0; k < m->nres; ++k) {  // average_reservoir_vars! (surface_kinwave.jl:244-258)
+        const int64_t q = (int64_t)mbr * m->nres + k;
+        m->res_out_avg[q] = res[k].outflow_cumulative / dt;
+        m->res_in_avg[q] = res[k].inflow_cumulative / dt;
+        m->res_abs_avg[q] = res[k].abstraction_cumulative / dt;
     }
     // ---- update_total_water_storage! (sbm.jl:143-182)
     for (int64_t i = 0; i < n; ++i) m->total_storage[o + i] = 0.0;
@@ -1478,6 +1702,18 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
             m->br_err[j] = eo[0];
             m->br_rel[j] = eo[1];
         }
+        for (int64_t k = 0; k < m->nres; ++k) {  // reservoir :261-284
+            const int64_t q = (int64_t)mbr * m->nres + k;
+            const OrcReservoir& r = res[k];
+            m->res_in_avg[q] = r.inflow_cumulative / dt;
+            m->res_evap_avg[q] = r.actevap_cumulative / dt;
+            double total_in = m->res_in_avg[q] + r.precipitation * r.area;
+            double total_out = m->res_out_avg[q] + m->res_evap_avg[q] * r.area;
+            double storage_rate = (r.storage - m->res_prev[q]) / dt;
+            compute_mass_balance_error(total_in, total_out, storage_rate, eo);
+            m->res_err[q] = eo[0];
+            m->res_rel[q] = eo[1];
+        }
         for (int64_t i = 0; i < n; ++i) {  // overland :382-399
             int64_t j = o + i;
             double total_in = m->ol_inwater[j] + m->ol_qin_avg[j];
@@ -1503,126 +1739,11 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
 
 }  // namespace
 
-// ====================================================================== reservoirs ======
-//
-// Reservoir update at a river node (routing/surface/reservoir.jl:583-628), with the outflow
-// functions of types 2 (free weir, without a linked lower reservoir), 3 (modified Puls) and 4
-// (simple), the observed-outflow override (reservoir.jl:524-545) and the linear storage
-// profile (S = A H). The river-side wrapper (surface_kinwave.jl:441-489) limits a negative
-// external inflow (abstraction) to 98 % of the storage per step and forms the net inflow.
-struct OrcReservoir {
-    int32_t outflow_type;  // 2 free weir, 3 modified Puls, 4 simple
-    double area, maximum_storage, threshold, rating_curve_coefficient, rating_curve_exponent;
-    double maximum_release, demand, target_minimum_fraction, target_full_fraction;
-    // boundary conditions of the step
-    double external_inflow, precipitation, evaporation, inflow_overland, inflow_subsurface, outflow_obs;
-    // state
-    double storage, waterlevel, outflow;
-    double inflow_cumulative, outflow_cumulative, actevap_cumulative, abstraction_cumulative;
-};
-
-namespace {
-
-// reservoir.jl:389-418
-void reservoir_simple(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
-                      double& outflow, double& storage) {
-    storage = r.storage + (inflow + precipitation - evaporation) * dt;
-    storage = jmax(storage, 0.0);
-    double fill_fraction = storage / r.maximum_storage;
-    double fac = scurve(fill_fraction, r.target_minimum_fraction, 1.0, 30.0);
-    double demand_release = jmin(fac * r.demand, storage / dt);
-    storage -= demand_release * dt;
-    double release_wanted = jmax(0.0, (storage - r.maximum_storage * r.target_full_fraction) / dt);
-    double overflow_q = jmax(0.0, (storage - r.maximum_storage) / dt);
-    double release_realized = jmin(release_wanted, overflow_q + r.maximum_release - demand_release);
-    storage -= release_realized * dt;
-    outflow = release_realized + demand_release;
-}
-
-// reservoir.jl:424-452
-void reservoir_modified_puls(const OrcReservoir& r, double precipitation, double evaporation, double inflow,
-                             double dt, double& outflow, double& storage) {
-    double res_factor = r.area / (dt * std::sqrt(r.rating_curve_coefficient));
-    double si_factor = r.storage / dt + precipitation - evaporation + inflow;
-    double si_factor_adj = si_factor - r.area * r.threshold / dt;
-    if (si_factor_adj > 0.0) {
-        double quadratic_sol_term = -res_factor + std::sqrt((res_factor * res_factor + 4 * si_factor_adj));
-        outflow = quadratic_sol_term > 0.0 ? 0.25 * quadratic_sol_term * quadratic_sol_term : 0.0;
-    } else {
-        outflow = 0.0;
-    }
-    outflow = jmin(outflow, si_factor);
-    storage = (si_factor - outflow) * dt;
-}
-
-// reservoir.jl:482-521 without a linked lower reservoir
-void reservoir_free_weir(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
-                         double& outflow, double& storage) {
-    double storage_input = jmax(r.storage / dt + precipitation - evaporation + inflow, 0.0);
-    if (r.waterlevel > r.threshold) {
-        double dh = r.waterlevel - r.threshold;
-        outflow = r.rating_curve_coefficient * jpow(dh, r.rating_curve_exponent);
-        double maxflow = dh * r.area / dt;
-        outflow = jmin(outflow, maxflow);
-    } else {
-        outflow = 0.0;
-    }
-    storage = (storage_input - outflow) * dt;
-}
-
-// reservoir.jl:524-545
-void reservoir_outflow_obs(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
-                           double& outflow, double& storage) {
-    double storage_input = jmax(r.storage / dt + precipitation - evaporation + inflow, 0.0);
-    outflow = jmin(r.outflow_obs, storage_input);
-    storage = (storage_input - outflow) * dt;
-    if (!std::isnan(r.maximum_storage)) {
-        double overflow = jmax(0.0, (storage - r.maximum_storage) / dt);
-        storage -= overflow * dt;
-        outflow += overflow;
-    }
-}
-
-// reservoir.jl:583-628
-void update_reservoir(OrcReservoir& r, double inflow, double dt) {
-    double precipitation = r.precipitation * r.area;
-    double available_storage = r.storage + (inflow + precipitation) * dt;
-    double potential_evaporation = r.evaporation * r.area;
-    double evaporation = jmin(available_storage / dt, potential_evaporation);
-    double outflow = 0.0, storage = r.storage;
-    if (!std::isnan(r.outflow_obs)) reservoir_outflow_obs(r, precipitation, evaporation, inflow, dt, outflow, storage);
-    else if (r.outflow_type == 2) reservoir_free_weir(r, precipitation, evaporation, inflow, dt, outflow, storage);
-    else if (r.outflow_type == 3) reservoir_modified_puls(r, precipitation, evaporation, inflow, dt, outflow, storage);
-    else reservoir_simple(r, precipitation, evaporation, inflow, dt, outflow, storage);
-    double waterlevel = r.waterlevel + (storage - r.storage) / r.area;  // linear profile
-    r.storage = storage;
-    r.waterlevel = waterlevel;
-    r.outflow = outflow;
-    r.inflow_cumulative += inflow * dt;
-    r.outflow_cumulative += outflow * dt;
-    r.actevap_cumulative += evaporation / r.area * dt;
-}
-
-// surface_kinwave.jl:441-489: net inflow of the reservoir at a river node whose discharge is q
-void update_reservoir_at_node(OrcReservoir& r, double q, double dt) {
-    double inflow;
-    if (r.external_inflow < 0.0) {
-        double abstraction = jmin(-r.external_inflow, (r.storage / dt) * 0.98);
-        r.abstraction_cumulative += abstraction * dt;
-        inflow = -abstraction;
-    } else {
-        inflow = r.external_inflow;
-    }
-    double net_inflow = q + r.inflow_overland + r.inflow_subsurface + inflow;
-    update_reservoir(r, net_inflow, dt);
-}
-
-}  // namespace
-
 extern "C" {
 // Reservoir at a river node with discharge q after the node's kinematic-wave update.
 void orc_reservoir_update(OrcReservoir* r, double q, double dt) { update_reservoir_at_node(*r, q, dt); }
 int32_t orc_reservoir_size() { return (int32_t)sizeof(OrcReservoir); }
+int64_t orc_model_reservoirs(const OrcModel* m) { return m->nres; }
 }  // extern "C"
 
 extern "C" {
@@ -1657,6 +1778,7 @@ static double* land_field(OrcModel* m, int field, std::vector<double>** vec) {
         case WF_F_SSF_STORAGE: *vec = &m->ssf_storage; break;
         case WF_F_SSF_TO_RIVER_AVERAGE: *vec = &m->ssf_tr_avg; break;
         case WF_F_LAND_Q_AVERAGE: *vec = &m->ol_q_avg; break;
+        case WF_F_LAND_QIN_AVERAGE: *vec = &m->ol_qin_avg; break;
         case WF_F_LAND_STORAGE: *vec = &m->ol_storage; break;
         case WF_F_LAND_TO_RIVER_AVERAGE: *vec = &m->ol_tr_avg; break;
         case WF_F_LAND_INWATER: *vec = &m->ol_inwater; break;
@@ -1708,8 +1830,37 @@ static double* river_field(OrcModel* m, int field) {
     }
 }
 
+// Reservoir fields, member-major [mbr * nres + k]: a pointer into the reservoir record or into
+// one of the per-step diagnostic arrays.
+static double* reservoir_field(OrcModel* m, int field, int64_t q) {
+    OrcReservoir& r = m->res[q];
+    switch (field) {
+        case WF_F_RESERVOIR_STORAGE: return &r.storage;
+        case WF_F_RESERVOIR_WATERLEVEL: return &r.waterlevel;
+        case WF_F_RESERVOIR_OUTFLOW: return &r.outflow;
+        case WF_F_RESERVOIR_OUTFLOW_AVERAGE: return &m->res_out_avg[q];
+        case WF_F_RESERVOIR_INFLOW_AVERAGE: return &m->res_in_avg[q];
+        case WF_F_RESERVOIR_ACTEVAP_AVERAGE: return &m->res_evap_avg[q];
+        case WF_F_RESERVOIR_ABSTRACTION_AVERAGE: return &m->res_abs_avg[q];
+        case WF_F_RESERVOIR_INFLOW_OVERLAND: return &r.inflow_overland;
+        case WF_F_RESERVOIR_INFLOW_SUBSURFACE: return &r.inflow_subsurface;
+        case WF_F_RESERVOIR_PRECIPITATION: return &r.precipitation;
+        case WF_F_RESERVOIR_EVAPORATION: return &r.evaporation;
+        case WF_F_RESERVOIR_EXTERNAL_INFLOW: return &r.external_inflow;
+        case WF_F_RESERVOIR_OUTFLOW_OBS: return &r.outflow_obs;
+        case WF_F_BALANCE_RESERVOIR_ERROR: return &m->res_err[q];
+        case WF_F_BALANCE_RESERVOIR_RELATIVE_ERROR: return &m->res_rel[q];
+        default: return nullptr;
+    }
+}
+
 int32_t orc_model_get(OrcModel* m, int32_t field, int32_t layer, double* out) {
     int64_t nm = m->n * m->M;
+    if (field >= WF_F_RESERVOIR_STORAGE) {
+        if (field >= WF_F_RESERVOIR_END_) return WF_ERR_INVALID;
+        for (int64_t q = 0; q < m->nres * m->M; ++q) out[q] = *reservoir_field(m, field, q);
+        return WF_OK;
+    }
     if (field >= WF_F_RIVER_Q) {
         double* src = river_field(m, field);
         if (!src) return WF_ERR_INVALID;
@@ -1733,6 +1884,11 @@ int32_t orc_model_get(OrcModel* m, int32_t field, int32_t layer, double* out) {
 
 int32_t orc_model_set(OrcModel* m, int32_t field, int32_t layer, const double* in) {
     int64_t nm = m->n * m->M;
+    if (field >= WF_F_RESERVOIR_STORAGE) {
+        if (field >= WF_F_RESERVOIR_END_) return WF_ERR_INVALID;
+        for (int64_t q = 0; q < m->nres * m->M; ++q) *reservoir_field(m, field, q) = in[q];
+        return WF_OK;
+    }
     if (field >= WF_F_RIVER_Q) {
         double* dst = river_field(m, field);
         if (!dst) return WF_ERR_INVALID;

@@ -130,6 +130,10 @@ double orc_quantile(double* v, int64_t n, double p);
 /* full model */
 typedef struct OrcModel OrcModel;
 int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p, OrcModel** out);
+/* the same with reservoirs (reservoir outlets cut the land and river upstream lists) */
+int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p,
+                                         const WfReservoirs* rs, OrcModel** out);
+int64_t orc_model_reservoirs(const OrcModel* m);
 void orc_model_destroy(OrcModel* m);
 const char* orc_model_error(const OrcModel* m);
 int32_t orc_model_set_forcing(OrcModel* m, const double* P, const double* PET, const double* T);

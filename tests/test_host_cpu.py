@@ -31,7 +31,8 @@ def test_synth_header_symbols_exported():
 
 
 def test_struct_sizes_match(lib):
-    for i, cls in enumerate([abi.WfConfig, abi.WfDomain, abi.WfParams, abi.WfMetrics, abi.WfTuning]):
+    for i, cls in enumerate([abi.WfConfig, abi.WfDomain, abi.WfParams, abi.WfMetrics, abi.WfTuning,
+                             abi.WfReservoirs]):
         assert lib.wf_struct_size(i) == C.sizeof(cls), cls.__name__
 
 

@@ -17,6 +17,7 @@
 #include "wf_kernels.h"
 #include "wf_launch.cuh"
 #include "wf_math.cuh"
+#include "wf_reservoir.cuh"
 #include "wf_walker.cuh"
 
 using wfm::jclamp;
@@ -832,6 +833,10 @@ struct OverlandPhys {
 
 // ------------------------------------------------------------------ river wavefront ------
 
+// RES: the model has reservoirs. A reservoir cell hands its reservoir's outflow, not its river
+// discharge, to the downstream cell: published for a light child, read from the reservoir's
+// outflow for the heavy child (which this lane updated at the previous chain position).
+template <bool RES>
 struct RiverPhys {
     WfDevFields F;
     WfDevGraph g;
@@ -862,6 +867,10 @@ struct RiverPhys {
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             double qu;
             if (!wfw::upstream_q(g, sw, RM[RV_Q], o, m, s, ep, F.status, qu)) return false;
+            if (RES && g.up_chain[o] < 0) {
+                const int32_t ru = F.res_of_rslot[g.up_slot[o]];
+                if (ru >= 0) qu = F.RS[RS_OUTFLOW][(int64_t)ru * M + m];
+            }
             qs = qs + qu;
         }
         const double qin = 0.0 + qs;
@@ -878,9 +887,14 @@ struct RiverPhys {
         double q, a;
         kinematic_wave(qin, RM[RV_Q][e], qlat + inflow, R[R_ALPHA][slot], dt_s, len, q, a);
         RM[RV_Q][e] = q;
+        double q_down = q;  // what the downstream cell receives
+        if (RES) {
+            const int32_t r = F.res_of_rslot[slot];
+            if (r >= 0) q_down = wfr::reservoir_node(F, r, m, q, dt_s);
+        }
         RM[RV_H][e] = a / R[R_WIDTH][slot];
         RM[RV_STORAGE][e] = len * a;
-        if (is_end) wfw::publish(g, chain, m, s, ep, q);
+        if (is_end) wfw::publish(g, chain, m, s, ep, q_down);
         const double c_q = (first ? 0.0 : RM[RV_Q_CUM][e]) + q * dt_s;
         const double c_qin = (first ? 0.0 : RM[RV_QIN_CUM][e]) + qin * dt_s;
         const double c_ab = (first ? 0.0 : RM[RV_ABS_CUM][e]) + absd * dt_s;
@@ -1042,7 +1056,75 @@ cudaError_t wf_fp64_overland(const WfDevFields& F, const WfDevGraph& g, const Wf
 }
 
 cudaError_t wf_fp64_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
-    return launch_walk(RiverPhys{F, g, sw}, c);
+    if (F.n_res > 0) return launch_walk(RiverPhys<true>{F, g, sw}, c);
+    return launch_walk(RiverPhys<false>{F, g, sw}, c);
+}
+
+// ------------------------------------------------------------------ reservoirs -----------
+// Kernels of both arithmetic forms (reservoir state is FP64 in both).
+
+// A member field of the land layout as FP64 (double-FP32 pair in the split form).
+__device__ __forceinline__ double land_member_d(const WfDevFields& F, int f, int64_t e) {
+    return F.split ? (double)F.Mh[f][e] + (double)F.Ml[f][e] : F.Mf[f][e];
+}
+
+// Before the river sweep: storage at the start of the step for the water balance
+// (mass_balance.jl:156-160), the inflow from the outlet cell's overland and subsurface flow
+// (update_inflow!, surface_kinwave.jl:771-802; the overland part excludes what goes to the
+// river, which the river's lateral inflow carries) and the reset of the step's cumulatives
+// (set_reservoir_vars!, surface_kinwave.jl:227-237).
+__global__ void __launch_bounds__(256) reservoir_prep_kernel(WfDevFields F) {
+    const int M = F.M;
+    const int64_t E = F.n_res * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / M;
+        const int m = (int)(e - r * M);
+        const int64_t le = F.res_land_slot[r] * M + m;
+        double* const* RS = F.RS;
+        if (F.mass_balance) RS[RS_PREV][e] = RS[RS_STORAGE][e];
+        RS[RS_IN_OL][e] = land_member_d(F, OL_Q_AVG, le);
+        RS[RS_IN_SSF][e] = land_member_d(F, SSF_Q_AVG, le);
+        RS[RS_IN_CUM][e] = 0.0;
+        RS[RS_OUT_CUM][e] = 0.0;
+        RS[RS_EVAP_CUM][e] = 0.0;
+        RS[RS_ABS_CUM][e] = 0.0;
+    }
+}
+
+// After the river sweep: step averages (average_reservoir_vars!, surface_kinwave.jl:244-258) and
+// the reservoir water balance (compute_flow_balance!, mass_balance.jl:261-284).
+__global__ void __launch_bounds__(256) reservoir_post_kernel(WfDevFields F) {
+    const int M = F.M;
+    const int64_t E = F.n_res * M;
+    const double dt = F.dt;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / M;
+        double* const* RS = F.RS;
+        RS[RS_OUT_AVG][e] = RS[RS_OUT_CUM][e] / dt;
+        RS[RS_IN_AVG][e] = RS[RS_IN_CUM][e] / dt;
+        RS[RS_ABS_AVG][e] = RS[RS_ABS_CUM][e] / dt;
+        if (!F.mass_balance) continue;
+        RS[RS_EVAP_AVG][e] = RS[RS_EVAP_CUM][e] / dt;
+        const double area = F.RP[RP_AREA][r];
+        const double tin = RS[RS_IN_AVG][e] + RS[RS_PRECIP][e] * area;
+        const double tout = RS[RS_OUT_AVG][e] + RS[RS_EVAP_AVG][e] * area;
+        double err, rel;
+        mb_error(tin, tout, (RS[RS_STORAGE][e] - RS[RS_PREV][e]) / dt, err, rel);
+        RS[RS_ERR][e] = err;
+        RS[RS_REL][e] = rel;
+    }
+}
+
+cudaError_t wf_reservoir_prep(const WfDevFields& F, const WfLaunchCfg& c) {
+    if (F.n_res <= 0) return cudaSuccess;
+    reservoir_prep_kernel<<<grid_for(F.n_res * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_reservoir_post(const WfDevFields& F, const WfLaunchCfg& c) {
+    if (F.n_res <= 0) return cudaSuccess;
+    reservoir_post_kernel<<<grid_for(F.n_res * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F);
+    return cudaGetLastError();
 }
 
 cudaError_t wf_fp64_balance(const WfDevFields& F, const WfLaunchCfg& c) {

@@ -23,6 +23,7 @@
 #include "wf_kernels.h"
 #include "wf_launch.cuh"
 #include "wf_math.cuh"
+#include "wf_reservoir.cuh"
 #include "wf_walker.cuh"
 #include "wf_ff.cuh"
 #include "wf_wave.cuh"
@@ -1413,7 +1414,10 @@ struct OlWave {
 // River flow (surface_process.jl:24-70 per node, routing/river_kinwave.jl sub-steps) in
 // double-FP32, with the abstraction of a negative external inflow limited to 80 % of the
 // storage. ADAPT as for OlWave.
-template <bool ADAPT>
+// RES: the model has reservoirs. At a reservoir cell the reservoir update follows the cell's
+// kinematic wave in every sub-step (FP64, wf_reservoir.cuh) and the reservoir's outflow, not the
+// cell's discharge, is handed downstream (heavy hand-off row and published chain end alike).
+template <bool ADAPT, bool RES>
 struct RvWave {
     static constexpr int kDepth = 2;
     WfDevFields F;
@@ -1422,6 +1426,7 @@ struct RvWave {
     struct In {
         wff::ff u, q, qlatt, invlen;
         float alpha, len, ext;
+        int32_t res;  // reservoir at this cell (RES only), or -1
         wfv::UpRec up;
     };
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
@@ -1433,6 +1438,7 @@ struct RvWave {
         x.alpha = F.Rf[R_ALPHA][slot];
         x.len = F.Rf[R_LENGTH][slot];
         x.ext = F.Rf[R_EXT_INFLOW][slot];
+        x.res = RES ? F.res_of_rslot[slot] : -1;
         wfv::load_rec<false>(g, slot, x.up);
     }
     __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
@@ -1469,8 +1475,13 @@ struct RvWave {
             kw_node_ff<ADAPT>(qin, qp, ql, u, x.invlen, dt_s, x.alpha, un, qn);
             u = un;
             qp = qn;
-            qh[s * stride] = wff::pack(qn);
-            if (is_end) wfv::publish(g, chain, m, s, qn);
+            wff::ff q_down = qn;
+            if (RES && x.res >= 0) {
+                const double dt_d = ADAPT ? sw.adt[m] : sw.dts[s];
+                q_down = wff::from_d(wfr::reservoir_node(F, x.res, m, wff::to_d(qn), dt_d));
+            }
+            qh[s * stride] = wff::pack(q_down);
+            if (is_end) wfv::publish(g, chain, m, s, q_down);
             qsum = wff::add(qsum, mul_dt(qn, dt_s));
         }
         float* const* RMh = F.RMh;
@@ -1734,8 +1745,12 @@ __global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph 
         str(F, RV_STORAGE, e, wff::mul(a, ldrs(F, R_LENGTH, slot)));
         ff qin = {0.0f, 0.0f};
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
-            const int64_t ue = g.up_slot[o] * M + m;
-            qin = wff::add(qin, ff{RMh[RV_QSUMH][ue], RMh[RV_QSUML][ue]});
+            const int64_t us = g.up_slot[o];
+            const int64_t ue = us * M + m;
+            const int32_t ru = F.n_res > 0 ? F.res_of_rslot[us] : -1;
+            // a reservoir cell contributes its reservoir's outflow (sum of outflow x sub-step)
+            qin = wff::add(qin, ru >= 0 ? wff::from_d(F.RS[RS_OUT_CUM][(int64_t)ru * M + m])
+                                        : ff{RMh[RV_QSUMH][ue], RMh[RV_QSUML][ue]});
         }
         str(F, RV_Q_AVG, e, wff::mul(ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]}, inv_dt));
         str(F, RV_QIN_AVG, e, wff::mul(qin, inv_dt));
@@ -1927,8 +1942,12 @@ cudaError_t wf_split_overland_wave(const WfDevFields& F, const WfDevGraph& g, co
 }
 
 cudaError_t wf_split_river_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
-    if (sw.aflag) return launch_wave(RvWave<true>{F, g, sw}, c);
-    return launch_wave(RvWave<false>{F, g, sw}, c);
+    if (F.n_res > 0) {
+        if (sw.aflag) return launch_wave(RvWave<true, true>{F, g, sw}, c);
+        return launch_wave(RvWave<false, true>{F, g, sw}, c);
+    }
+    if (sw.aflag) return launch_wave(RvWave<true, false>{F, g, sw}, c);
+    return launch_wave(RvWave<false, false>{F, g, sw}, c);
 }
 
 cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {

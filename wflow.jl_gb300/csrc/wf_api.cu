@@ -96,6 +96,7 @@ struct WfHandle {
     cudaEvent_t ev_fcopied = nullptr, ev_fconsumed = nullptr;
     double* fstage = nullptr;     // [3][n_land * M] staged forcing in external order
     double* outlets_buf = nullptr;  // [outlets * M] outlet discharge for wf_get_outlets
+    int64_t nres = 0;               // reservoirs
 };
 
 namespace {
@@ -444,6 +445,7 @@ FieldRef field_ref(WfHandle* h, int field, int layer) {
         case WF_F_SSF_STORAGE: r.idx = SSF_STORAGE; break;
         case WF_F_SSF_TO_RIVER_AVERAGE: r.idx = SSF_TR_AVG; break;
         case WF_F_LAND_Q_AVERAGE: r.idx = OL_Q_AVG; break;
+        case WF_F_LAND_QIN_AVERAGE: r.idx = OL_QIN_AVG; break;
         case WF_F_LAND_STORAGE: r.idx = OL_STORAGE; r.settable = true; break;
         case WF_F_LAND_TO_RIVER_AVERAGE: r.idx = OL_TR_AVG; break;
         case WF_F_LAND_INWATER: r.idx = OL_INWATER; break;
@@ -503,7 +505,46 @@ std::vector<StateItem> state_items(const WfHandle* h) {
                   WF_F_LAND_STORAGE, WF_F_RIVER_Q, WF_F_RIVER_H, WF_F_RIVER_STORAGE})
         v.push_back({f, 0});
     for (int k = 0; k < h->N; ++k) v.push_back({WF_F_UNSATURATED_LAYER_DEPTH, k});
+    if (h->nres > 0) {  // reservoir states (water level; storage kept alongside for exact restarts)
+        v.push_back({WF_F_RESERVOIR_STORAGE, 0});
+        v.push_back({WF_F_RESERVOIR_WATERLEVEL, 0});
+    }
     return v;
+}
+
+// Values per member of a field: reservoirs, river cells or land cells.
+int64_t field_extent(const WfHandle* h, int field) {
+    if (field >= WF_F_RESERVOIR_STORAGE) return h->nres;
+    return field >= WF_F_RIVER_Q ? h->nr : h->n;
+}
+
+// Reservoir fields: device arrays of element r * M + m to and from the member-major external
+// order. Exactly one of dst (get) and src (set) is non-null.
+int reservoir_io(WfHandle* h, int32_t field, double* dst, const double* src, int64_t offset, int64_t count) {
+    if (field < WF_F_RESERVOIR_STORAGE || field >= WF_F_RESERVOIR_END_ || h->nres <= 0)
+        return set_err(h, WF_ERR_INVALID, "unknown field or model without reservoirs");
+    const bool settable = field == WF_F_RESERVOIR_STORAGE || field == WF_F_RESERVOIR_WATERLEVEL ||
+                          field == WF_F_RESERVOIR_PRECIPITATION || field == WF_F_RESERVOIR_EVAPORATION ||
+                          field == WF_F_RESERVOIR_EXTERNAL_INFLOW || field == WF_F_RESERVOIR_OUTFLOW_OBS;
+    if (src && !settable) return set_err(h, WF_ERR_INVALID, "field is not settable");
+    const int64_t nres = h->nres, M = h->M, total = nres * M;
+    if (offset < 0 || count < 0 || offset + count > total) return set_err(h, WF_ERR_INVALID, "range out of bounds");
+    double* dev_p = h->F.RS[field - WF_F_RESERVOIR_STORAGE];
+    std::vector<double> dev((size_t)total), ext((size_t)total);
+    CK(cudaMemcpyAsync(dev.data(), dev_p, total * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int64_t r = 0; r < nres; ++r)
+        for (int64_t m = 0; m < M; ++m) ext[m * nres + r] = dev[r * M + m];
+    if (dst) {
+        if (count) std::memcpy(dst, ext.data() + offset, count * sizeof(double));
+        return WF_OK;
+    }
+    if (count) std::memcpy(ext.data() + offset, src, count * sizeof(double));
+    for (int64_t r = 0; r < nres; ++r)
+        for (int64_t m = 0; m < M; ++m) dev[r * M + m] = ext[m * nres + r];
+    CK(cudaMemcpyAsync(dev_p, dev.data(), total * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return WF_OK;
 }
 
 struct StateHeader {
@@ -532,6 +573,7 @@ int32_t wf_struct_size(int32_t which) {
         case 2: return (int32_t)sizeof(WfParams);
         case 3: return (int32_t)sizeof(WfMetrics);
         case 4: return (int32_t)sizeof(WfTuning);
+        case 5: return (int32_t)sizeof(WfReservoirs);
         default: return -1;
     }
 }
@@ -539,6 +581,11 @@ int32_t wf_struct_size(int32_t which) {
 const char* wf_last_error(const WfHandle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
 int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32_t device, WfHandle** out) {
+    return wf_create_with_reservoirs(c, d, p, nullptr, device, out);
+}
+
+int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p, const WfReservoirs* rs,
+                                  int32_t device, WfHandle** out) {
     WfHandle* h = nullptr;
     if (!out) return set_err(nullptr, WF_ERR_INVALID, "null output handle");
     *out = nullptr;
@@ -570,6 +617,42 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
                            !d->river_slope || !d->river_manning_n || !d->river_bankfull_depth))
         return set_err(nullptr, WF_ERR_INVALID, "river arrays missing");
     if (!d->land_downstream) return set_err(nullptr, WF_ERR_INVALID, "land_downstream missing");
+    // reservoirs: outlets at river cells with a downstream river cell, at most one reservoir
+    // draining into a river cell (ReservoirModel, reservoir.jl; surface_kinwave.jl:473-485)
+    const int64_t nres = rs ? rs->n : 0;
+    std::vector<int32_t> land_ds(d->land_downstream, d->land_downstream + d->n_land);
+    std::vector<int32_t> res_of_river;
+    if (nres < 0) return set_err(nullptr, WF_ERR_INVALID, "negative reservoir count");
+    if (nres > 0) {
+        if (!rs->river_index || !rs->outflow_curve_type || !rs->area || !rs->waterlevel)
+            return set_err(nullptr, WF_ERR_INVALID, "reservoir arrays missing");
+        res_of_river.assign(d->n_river, -1);
+        std::vector<uint8_t> fed(d->n_river, 0);
+        for (int64_t k = 0; k < nres; ++k) {
+            const int32_t v = rs->river_index[k];
+            if (v < 0 || v >= d->n_river) return set_err(nullptr, WF_ERR_INVALID, "reservoir river index out of range");
+            if (res_of_river[v] >= 0) return set_err(nullptr, WF_ERR_INVALID, "two reservoirs at one river cell");
+            const int32_t dv = d->river_downstream[v];
+            if (dv < 0 || dv >= d->n_river)
+                return set_err(nullptr, WF_ERR_INVALID, "a reservoir without a downstream river node is not supported");
+            if (fed[dv]) return set_err(nullptr, WF_ERR_UNSUPPORTED, "two reservoirs drain into one river cell");
+            const int32_t t = rs->outflow_curve_type[k];
+            if (t != WF_RES_FREE_WEIR && t != WF_RES_MODIFIED_PULS && t != WF_RES_SIMPLE)
+                return set_err(nullptr, WF_ERR_UNSUPPORTED, "reservoir outflow type must be 2, 3 or 4");
+            if (!(rs->area[k] > 0.0)) return set_err(nullptr, WF_ERR_INVALID, "reservoir area must be positive");
+            const bool simple_ok = rs->maximum_storage && rs->maximum_release && rs->demand &&
+                                   rs->target_minimum_fraction && rs->target_full_fraction;
+            const bool weir_ok = rs->threshold && rs->rating_curve_coefficient &&
+                                 (t != WF_RES_FREE_WEIR || rs->rating_curve_exponent);
+            if (t == WF_RES_SIMPLE ? !simple_ok : !weir_ok)
+                return set_err(nullptr, WF_ERR_INVALID, "reservoir parameter array missing for its outflow type");
+            fed[dv] = 1;
+            res_of_river[v] = (int32_t)k;
+            const int32_t li = d->river_land_index[v];
+            if (li < 0 || li >= d->n_land) return set_err(nullptr, WF_ERR_INVALID, "river_land_index out of range");
+            land_ds[li] = -1;  // the outlet cell is a pit of the land upstream lists (domain.jl:95-121)
+        }
+    }
 
     h = new WfHandle();
     h->cfg = *c;
@@ -645,7 +728,7 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
     const size_t cap = c->form == WF_FORM_SPLIT ? (size_t)wfv::MAX_GROUP : (size_t)32;
     const int cap_land = (int)std::min<size_t>(std::max(h->h_dts_land.size(), h->h_dts_ssf.size()), cap);
     const int cap_river = (int)std::min<size_t>(h->h_dts_river.size(), cap);
-    CKR(plan_graph(h, h->land, n, d->land_downstream, M, cap_land));
+    CKR(plan_graph(h, h->land, n, land_ds.data(), M, cap_land));
     CKR(plan_graph(h, h->river, nr, d->river_downstream ? d->river_downstream : nullptr, M, cap_river));
     const WfRoutingPlan& PL = h->land.plan;
     const WfRoutingPlan& PR = h->river.plan;
@@ -991,6 +1074,47 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
             if (d->river_downstream[r] < 0) h->outlet_slots.push_back(PR.slot_of_node[r]);
         if (!h->outlet_slots.empty()) CKR(upload(h, &h->d_outlet_slots, h->outlet_slots));
     }
+    // ---- reservoirs: parameters per reservoir, state per reservoir and member (r * M + m)
+    h->nres = nres;
+    F.n_res = nres;
+    if (nres > 0) {
+        std::vector<int32_t> rtype(nres), rofs(PR.n_slots, -1);
+        std::vector<int64_t> rls(nres);
+        for (int64_t k = 0; k < nres; ++k) {
+            const int32_t v = rs->river_index[k];
+            rtype[k] = rs->outflow_curve_type[k];
+            rofs[PR.slot_of_node[v]] = (int32_t)k;
+            rls[k] = PL.slot_of_node[d->river_land_index[v]];
+        }
+        int32_t *a32, *b32;
+        int64_t* c64;
+        CKR(upload(h, &a32, rtype));
+        CKR(upload(h, &b32, rofs));
+        CKR(upload(h, &c64, rls));
+        F.res_type = a32;
+        F.res_of_rslot = b32;
+        F.res_land_slot = c64;
+        const double* src[RP_COUNT] = {rs->area, rs->maximum_storage, rs->threshold, rs->rating_curve_coefficient,
+                                       rs->rating_curve_exponent, rs->maximum_release, rs->demand,
+                                       rs->target_minimum_fraction, rs->target_full_fraction};
+        for (int f = 0; f < RP_COUNT; ++f) {
+            std::vector<double> v(nres, NaN);
+            if (src[f]) v.assign(src[f], src[f] + nres);
+            CKR(upload(h, &F.RP[f], v));
+        }
+        for (int f = 0; f < RS_COUNT; ++f) {
+            std::vector<double> v((size_t)nres * M, 0.0);
+            for (int64_t k = 0; k < nres; ++k)
+                for (int m = 0; m < M; ++m) {
+                    double x = 0.0;
+                    if (f == RS_WATERLEVEL) x = rs->waterlevel[k];
+                    if (f == RS_STORAGE) x = rs->area[k] * rs->waterlevel[k];  // linear profile (reservoir.jl:343-360)
+                    if (f == RS_OUTFLOW || f == RS_OBS) x = NaN;
+                    v[(size_t)k * M + m] = x;
+                }
+            CKR(upload(h, &F.RS[f], v));
+        }
+    }
     F.land_slots = PL.n_slots;
     F.river_slots = PR.n_slots;
     F.N = N;
@@ -1180,6 +1304,7 @@ int32_t wf_step(WfHandle* h) {
 
 int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int64_t offset, int64_t count) {
     if (!h || !dst) return set_err(h, WF_ERR_INVALID, "null argument");
+    if (field >= WF_F_RESERVOIR_STORAGE) return reservoir_io(h, field, dst, nullptr, offset, count);
     FieldRef r = field_ref(h, field, layer);
     if (!r.p && !r.p32 && !r.derived_vwc) return set_err(h, WF_ERR_INVALID, "unknown field or layer");
     const int64_t n_ext = r.river ? h->nr : h->n;
@@ -1208,6 +1333,7 @@ int32_t wf_get_field(WfHandle* h, int32_t field, int32_t layer, double* dst, int
 
 int32_t wf_set_field(WfHandle* h, int32_t field, int32_t layer, const double* src, int64_t offset, int64_t count) {
     if (!h || !src) return set_err(h, WF_ERR_INVALID, "null argument");
+    if (field >= WF_F_RESERVOIR_STORAGE) return reservoir_io(h, field, nullptr, src, offset, count);
     FieldRef r = field_ref(h, field, layer);
     if ((!r.p && !r.p32) || !r.settable) return set_err(h, WF_ERR_INVALID, "field is not settable");
     const int64_t n_ext = r.river ? h->nr : h->n;
@@ -1273,7 +1399,7 @@ int32_t wf_get_state(WfHandle* h, void* dst, size_t* size) {
     if (!h || !size) return set_err(h, WF_ERR_INVALID, "null argument");
     auto items = state_items(h);
     size_t bytes = sizeof(StateHeader);
-    for (auto& it : items) bytes += (size_t)((it.field >= WF_F_RIVER_Q) ? h->nr : h->n) * h->M * sizeof(double);
+    for (auto& it : items) bytes += (size_t)field_extent(h, it.field) * h->M * sizeof(double);
     if (!dst) {
         *size = bytes;
         return WF_OK;
@@ -1290,7 +1416,7 @@ int32_t wf_get_state(WfHandle* h, void* dst, size_t* size) {
     std::memcpy(dst, &hd, sizeof(hd));
     char* p = (char*)dst + sizeof(hd);
     for (auto& it : items) {
-        const int64_t cnt = ((it.field >= WF_F_RIVER_Q) ? h->nr : h->n) * h->M;
+        const int64_t cnt = field_extent(h, it.field) * h->M;
         int rc = wf_get_field(h, it.field, it.layer, (double*)p, 0, cnt);
         if (rc) return rc;
         p += cnt * sizeof(double);
@@ -1311,7 +1437,7 @@ int32_t wf_set_state(WfHandle* h, const void* src, size_t size) {
     const char* p = (const char*)src + sizeof(hd);
     size_t used = sizeof(hd);
     for (auto& it : items) {
-        const int64_t cnt = ((it.field >= WF_F_RIVER_Q) ? h->nr : h->n) * h->M;
+        const int64_t cnt = field_extent(h, it.field) * h->M;
         used += cnt * sizeof(double);
         if (used > size) return set_err(h, WF_ERR_STATE, "state blob truncated");
         int rc = wf_set_field(h, it.field, it.layer, (const double*)p, 0, cnt);
@@ -1385,6 +1511,12 @@ int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_
     if (n_outlets) *n_outlets = (int64_t)h->outlet_slots.size();
     if (n_layers) *n_layers = h->N;
     if (n_members) *n_members = h->M;
+    return WF_OK;
+}
+
+int32_t wf_get_reservoir_count(WfHandle* h, int64_t* n_reservoirs) {
+    if (!h || !n_reservoirs) return WF_ERR_INVALID;
+    *n_reservoirs = h->nres;
     return WF_OK;
 }
 
@@ -1528,13 +1660,28 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         }
         return WF_OK;
     };
+    // reservoirs: inflow from the land routing before the river sweep, averages and balance after
+    auto res_prep = [&]() -> int {
+        if (h->nres <= 0) return WF_OK;
+        CK(wf_reservoir_prep(h->F, lc));
+        ++nl;
+        return WF_OK;
+    };
+    auto res_post = [&]() -> int {
+        if (h->nres <= 0) return WF_OK;
+        CK(wf_reservoir_post(h->F, lc));
+        ++nl;
+        return WF_OK;
+    };
     int rc;
     if (h->adaptive) {
         if ((rc = adaptive(h->land, gl, WF_ADAPT_SSF))) return rc;
         mark(2);
         if ((rc = adaptive(h->land, gl, WF_ADAPT_LAND))) return rc;
         mark(3);
+        if ((rc = res_prep())) return rc;
         if (h->nr > 0 && (rc = adaptive(h->river, gr, WF_ADAPT_RIVER))) return rc;
+        if ((rc = res_post())) return rc;
         mark(4);
     } else if (split) {
         if (h->F.ssf_single) rc = wave(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0);
@@ -1543,14 +1690,18 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         mark(2);
         if ((rc = wave(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
         mark(3);
+        if ((rc = res_prep())) return rc;
         if (h->nr > 0 && (rc = wave(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
+        if ((rc = res_post())) return rc;
         mark(4);
     } else {
         if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;
         mark(2);
         if ((rc = sweep(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
         mark(3);
+        if ((rc = res_prep())) return rc;
         if (h->nr > 0 && (rc = sweep(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
+        if ((rc = res_post())) return rc;
         mark(4);
     }
     CK(split ? wf_split_balance(h->F, lc) : wf_fp64_balance(h->F, lc));
@@ -1747,7 +1898,15 @@ int enqueue_step_static(WfHandle* h, unsigned char* base, int64_t* launches) {
     int rc;
     if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0, split && h->F.ssf_single))) return rc;
     if ((rc = sweep(h->land, gl, h->h_dts_land, h->dts_land, 1, split))) return rc;
+    if (h->nres > 0) {
+        CK(wf_reservoir_prep(h->F, lc));
+        ++nl;
+    }
     if (h->nr > 0 && (rc = sweep(h->river, gr, h->h_dts_river, h->dts_river, 2, split))) return rc;
+    if (h->nres > 0) {
+        CK(wf_reservoir_post(h->F, lc));
+        ++nl;
+    }
     CK(split ? wf_split_balance(h->F, lc) : wf_fp64_balance(h->F, lc));
     ++nl;
     if (launches) *launches = nl;

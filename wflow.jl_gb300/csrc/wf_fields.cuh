@@ -42,11 +42,25 @@
     X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL)                         \
     X(RV_UH) X(RV_UL) X(RV_QSUMH) X(RV_QSUML) X(RV_ABSH) X(RV_ABSL) X(RV_QLATTH) X(RV_QLATTL)
 
+// Reservoirs, per reservoir and member (element r * M + m), FP64 in both forms. The first
+// fifteen follow the order of the WF_F_RESERVOIR_* field ids (WF_F_RESERVOIR_STORAGE + i).
+#define WF_RS_FIELDS(X)                                                                            \
+    X(RS_STORAGE) X(RS_WATERLEVEL) X(RS_OUTFLOW) X(RS_OUT_AVG) X(RS_IN_AVG) X(RS_EVAP_AVG)          \
+    X(RS_ABS_AVG) X(RS_IN_OL) X(RS_IN_SSF) X(RS_PRECIP) X(RS_EVAP) X(RS_EXT) X(RS_OBS) X(RS_ERR)     \
+    X(RS_REL) X(RS_OUT_CUM) X(RS_IN_CUM) X(RS_EVAP_CUM) X(RS_ABS_CUM) X(RS_PREV)
+
+// Reservoir parameters, per reservoir.
+#define WF_RP_FIELDS(X)                                                                            \
+    X(RP_AREA) X(RP_MAXSTOR) X(RP_THRESHOLD) X(RP_RC_COEF) X(RP_RC_EXP) X(RP_MAXREL) X(RP_DEMAND)   \
+    X(RP_TMIN) X(RP_TFULL)
+
 #define WF_ENUM_ITEM(name) name,
 enum WfLandStatic { WF_L_FIELDS(WF_ENUM_ITEM) L_COUNT };
 enum WfLandMember { WF_M_FIELDS(WF_ENUM_ITEM) M_COUNT };
 enum WfRiverStatic { WF_R_FIELDS(WF_ENUM_ITEM) R_COUNT };
 enum WfRiverMember { WF_RM_FIELDS(WF_ENUM_ITEM) RM_COUNT };
+enum WfReservoirMember { WF_RS_FIELDS(WF_ENUM_ITEM) RS_COUNT };
+enum WfReservoirStatic { WF_RP_FIELDS(WF_ENUM_ITEM) RP_COUNT };
 #undef WF_ENUM_ITEM
 
 // Layered fields: N arrays each.
@@ -124,6 +138,13 @@ struct WfDevFields {
     double dt_ssf;        // subsurface sub-step when ssf_single
     double inv_dt_ssf;    // 1 / dt_ssf
     int32_t* status;  // device status word (0 = ok)
+    // reservoirs (none: n_res = 0 and null pointers)
+    int64_t n_res;
+    double* RS[RS_COUNT];          // [n_res * M]
+    double* RP[RP_COUNT];          // [n_res]
+    const int32_t* res_type;       // [n_res] WfReservoirOutflow
+    const int64_t* res_land_slot;  // [n_res] land slot of the reservoir outlet cell
+    const int32_t* res_of_rslot;   // [river slots] reservoir at a river slot, or -1
 };
 
 // Routing graph on the device (one per land / river graph).

@@ -36,6 +36,12 @@ cudaError_t wf_split_river_post(const WfDevFields& F, const WfDevGraph& g, const
 cudaError_t wf_split_sync_u(const WfDevFields& F, const WfLaunchCfg& c);
 cudaError_t wf_split_vwc(const WfDevFields& F, int layer, double* out, const WfLaunchCfg& c);
 
+// Reservoirs, both forms (kernels_fp64.cu): before the river sweep (start-of-step storage,
+// inflow from the outlet cell's land routing, reset of the step's cumulatives) and after it
+// (averages and water balance). No launch without reservoirs.
+cudaError_t wf_reservoir_prep(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_reservoir_post(const WfDevFields& F, const WfLaunchCfg& c);
+
 // Adaptive sub-stepping (kernels_adaptive.cu): size and flags of every member's next sub-step
 // of the sweep A.kind, from the current state; sets *A.more when a further sub-step follows.
 cudaError_t wf_adaptive_substep(const WfDevFields& F, const WfAdaptive& A, const WfLaunchCfg& c);

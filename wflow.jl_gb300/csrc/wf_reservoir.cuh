@@ -1,0 +1,106 @@
+// wf_reservoir.cuh -- reservoir update at a river node, inside the river wavefront.
+//
+// A reservoir sits at a river cell (its outlet). The river sweep computes the cell's discharge
+// with the kinematic wave as usual; the reservoir then takes that discharge plus the outlet
+// cell's overland and subsurface discharge and the external inflow as its net inflow, updates
+// its storage and water level, and its outflow (not the cell's river discharge) is what the
+// downstream river cell receives (Wflow/src/routing/surface/surface_kinwave.jl:441-489).
+// Reservoirs are few (hundreds in a large model) and their arithmetic is FP64 in both forms.
+//
+// Outflow functions (routing/surface/reservoir.jl): 2 free weir without a linked lower
+// reservoir (:482-521), 3 modified Puls (:424-452), 4 simple (:389-418), each replaced by the
+// observed outflow where one is given (:554-575); storage profile S = A H (:306-320, :612-621).
+#pragma once
+
+#include "wf_fields.cuh"
+#include "wf_math.cuh"
+
+namespace wfr {
+
+// Wflow.scurve (utils.jl:27-30)
+__device__ __forceinline__ double scurve(double x, double a, double b, double c) {
+    return 1.0 / (b + wfm::exp(-c * (x - a)));
+}
+
+// Net inflow, storage update and outflow of reservoir r for member m over a sub-step dt, with q
+// the river discharge of the reservoir's cell after its kinematic-wave update. Accumulates the
+// step's inflow, outflow, evaporation and abstraction; returns the outflow.
+__device__ inline double reservoir_node(const WfDevFields& F, int32_t r, int m, double q, double dt) {
+    using wfm::jmax;
+    using wfm::jmin;
+    const int64_t e = (int64_t)r * F.M + m;
+    double* const* RS = F.RS;
+    double* const* RP = F.RP;
+    const double area = RP[RP_AREA][r];
+    const double s0 = RS[RS_STORAGE][e];
+    const double wl0 = RS[RS_WATERLEVEL][e];
+    // negative external inflow: abstraction limited to 98 % of the storage (surface_kinwave.jl:461-469)
+    const double ext = RS[RS_EXT][e];
+    double inflow;
+    if (ext < 0.0) {
+        const double abstraction = jmin(-ext, (s0 / dt) * 0.98);
+        RS[RS_ABS_CUM][e] += abstraction * dt;
+        inflow = -abstraction;
+    } else {
+        inflow = ext;
+    }
+    const double net = q + RS[RS_IN_OL][e] + RS[RS_IN_SSF][e] + inflow;
+    // evaporation limited by the available volume (reservoir.jl:595-599)
+    const double precipitation = RS[RS_PRECIP][e] * area;
+    const double available = s0 + (net + precipitation) * dt;
+    const double potential_evaporation = RS[RS_EVAP][e] * area;
+    const double evaporation = jmin(available / dt, potential_evaporation);
+    const double obs = RS[RS_OBS][e];
+    const double smax = RP[RP_MAXSTOR][r];
+    double outflow, storage;
+    if (obs == obs) {  // observed outflow (reservoir.jl:554-575)
+        const double input = jmax(s0 / dt + precipitation - evaporation + net, 0.0);
+        outflow = jmin(obs, input);
+        storage = (input - outflow) * dt;
+        if (smax == smax) {
+            const double overflow = jmax(0.0, (storage - smax) / dt);
+            storage -= overflow * dt;
+            outflow += overflow;
+        }
+    } else if (F.res_type[r] == WF_RES_FREE_WEIR) {
+        const double input = jmax(s0 / dt + precipitation - evaporation + net, 0.0);
+        const double thr = RP[RP_THRESHOLD][r];
+        outflow = 0.0;
+        if (wl0 > thr) {
+            const double dh = wl0 - thr;
+            outflow = RP[RP_RC_COEF][r] * wfm::pow(dh, RP[RP_RC_EXP][r]);
+            outflow = jmin(outflow, dh * area / dt);
+        }
+        storage = (input - outflow) * dt;
+    } else if (F.res_type[r] == WF_RES_MODIFIED_PULS) {
+        const double res_factor = area / (dt * wfm::sqrt_(RP[RP_RC_COEF][r]));
+        const double si = s0 / dt + precipitation - evaporation + net;
+        const double si_adj = si - area * RP[RP_THRESHOLD][r] / dt;
+        outflow = 0.0;
+        if (si_adj > 0.0) {
+            const double t = -res_factor + wfm::sqrt_((res_factor * res_factor + 4.0 * si_adj));
+            outflow = t > 0.0 ? 0.25 * t * t : 0.0;
+        }
+        outflow = jmin(outflow, si);
+        storage = (si - outflow) * dt;
+    } else {  // simple reservoir
+        storage = jmax(s0 + (net + precipitation - evaporation) * dt, 0.0);
+        const double fac = scurve(storage / smax, RP[RP_TMIN][r], 1.0, 30.0);
+        const double demand_release = jmin(fac * RP[RP_DEMAND][r], storage / dt);
+        storage -= demand_release * dt;
+        const double wanted = jmax(0.0, (storage - smax * RP[RP_TFULL][r]) / dt);
+        const double overflow_q = jmax(0.0, (storage - smax) / dt);
+        const double realized = jmin(wanted, overflow_q + RP[RP_MAXREL][r] - demand_release);
+        storage -= realized * dt;
+        outflow = realized + demand_release;
+    }
+    RS[RS_WATERLEVEL][e] = wl0 + (storage - s0) / area;
+    RS[RS_STORAGE][e] = storage;
+    RS[RS_OUTFLOW][e] = outflow;
+    RS[RS_IN_CUM][e] += net * dt;
+    RS[RS_OUT_CUM][e] += outflow * dt;
+    RS[RS_EVAP_CUM][e] += evaporation / area * dt;
+    return outflow;
+}
+
+}  // namespace wfr

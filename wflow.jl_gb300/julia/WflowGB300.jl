@@ -83,12 +83,37 @@ struct WfParams
     ptrs::NTuple{34, Ptr{Float64}}
 end
 
+# reservoirs (WfReservoirs; ReservoirModel, Wflow/src/routing/surface/reservoir.jl)
+struct WfReservoirs
+    n::Int64
+    river_index::Ptr{Int32}
+    outflow_curve_type::Ptr{Int32}
+    area::Ptr{Float64}
+    waterlevel::Ptr{Float64}
+    maximum_storage::Ptr{Float64}
+    threshold::Ptr{Float64}
+    rating_curve_coefficient::Ptr{Float64}
+    rating_curve_exponent::Ptr{Float64}
+    maximum_release::Ptr{Float64}
+    demand::Ptr{Float64}
+    target_minimum_fraction::Ptr{Float64}
+    target_full_fraction::Ptr{Float64}
+end
+
 # WfField ids (enum WfField)
 const F_LAND = (:canopy_storage, :snow_storage, :snow_water, :soil_surface_temperature,
     :saturated_water_depth, :unsaturated_layer_depth, :ssf_q, :land_q, :land_h, :water_table_depth)
 const F_RIVER_Q = Int32(100)
 const F_RIVER_H = Int32(101)
 const F_RIVER_Q_AVERAGE = Int32(103)
+const F_RESERVOIR_STORAGE = Int32(200)
+const F_RESERVOIR_WATERLEVEL = Int32(201)
+const F_RESERVOIR_OUTFLOW = Int32(202)
+const F_RESERVOIR_OUTFLOW_AVERAGE = Int32(203)
+const F_RESERVOIR_PRECIPITATION = Int32(209)
+const F_RESERVOIR_EVAPORATION = Int32(210)
+const F_RESERVOIR_EXTERNAL_INFLOW = Int32(211)
+const F_RESERVOIR_OUTFLOW_OBS = Int32(212)
 
 mutable struct GpuStep
     handle::Ptr{Cvoid}
@@ -96,6 +121,7 @@ mutable struct GpuStep
     n_land::Int
     n_river::Int
     forcing::NTuple{3, Vector{Float64}}
+    n_reservoirs::Int
 end
 
 check(st, h, what) = st == 0 || error("$what failed ($st): " *
@@ -172,12 +198,29 @@ function GpuStep(model)
         src[:water_holding_capacity] = sp.water_holding_capacity
     end
     params = WfParams(ntuple(i -> haskey(src, PARAM_NAMES[i]) ? k(src[PARAM_NAMES[i]]) : Ptr{Float64}(0), 34))
+    # reservoirs at their outlet river cells, in the reservoir model's order
+    # (NetworkReservoir.river_indices, network.jl:333-350); the storage profile must be linear
+    nres = 0
+    res = WfReservoirs(0, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL,
+        C_NULL, C_NULL)
+    if config.model.reservoir__flag
+        rv = routing.river_flow.boundary_conditions.reservoir
+        p = rv.parameters
+        all(==(Wflow.ReservoirProfileType.linear), p.storage_curve_type) ||
+            error("the GPU step supports the linear reservoir storage profile only")
+        nres = length(p.area)
+        res = WfReservoirs(nres, k(Int32.(domain.reservoir.network.river_indices .- 1)),
+            k(Int32.(Integer.(p.outflow_curve_type))), k(p.area), k(rv.variables.waterlevel),
+            k(p.maximum_storage), k(p.threshold), k(p.rating_curve_coefficient), k(p.rating_curve_exponent),
+            k(p.maximum_release), k(p.demand), k(p.target_minimum_fraction), k(p.target_full_fraction))
+    end
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    st = ccall((:wf_create, LIB), Int32, (Ref{WfConfig}, Ref{WfDomain}, Ref{WfParams}, Int32, Ref{Ptr{Cvoid}}),
-        cfg, dom, params, Int32(0), h)
-    check(st, C_NULL, "wf_create")
+    st = ccall((:wf_create_with_reservoirs, LIB), Int32,
+        (Ref{WfConfig}, Ref{WfDomain}, Ref{WfParams}, Ref{WfReservoirs}, Int32, Ref{Ptr{Cvoid}}),
+        cfg, dom, params, res, Int32(0), h)
+    check(st, C_NULL, "wf_create_with_reservoirs")
     n = length(ds_land)
-    gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)))
+    gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)), nres)
     finalizer(g -> ccall((:wf_destroy, LIB), Cvoid, (Ptr{Cvoid},), g.handle), gpu)
     return gpu
 end
@@ -192,6 +235,15 @@ function gpu_update_model!(gpu::GpuStep, model)
     st = ccall((:wf_set_forcing, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
         gpu.handle, f.precipitation, f.potential_evaporation, f.temperature, gpu.n_land)
     check(st, gpu.handle, "wf_set_forcing")
+    if gpu.n_reservoirs > 0
+        # the reservoir inputs Wflow's forcing reader filled (io.jl:128-137) and the boundary
+        # conditions of the reservoir model
+        rv = model.routing.river_flow.boundary_conditions.reservoir
+        set_field!(gpu, F_RESERVOIR_PRECIPITATION, rv.boundary_conditions.precipitation)
+        set_field!(gpu, F_RESERVOIR_EVAPORATION, rv.boundary_conditions.evaporation)
+        set_field!(gpu, F_RESERVOIR_EXTERNAL_INFLOW, rv.boundary_conditions.external_inflow)
+        set_field!(gpu, F_RESERVOIR_OUTFLOW_OBS, rv.variables.outflow_obs)
+    end
     check(ccall((:wf_step, LIB), Int32, (Ptr{Cvoid},), gpu.handle), gpu.handle, "wf_step")
     sync_mirrors!(gpu, model)
     return nothing
@@ -222,6 +274,13 @@ function sync_mirrors!(gpu::GpuStep, model)
     get_field!(routing.overland_flow.variables.h, gpu, 8)
     get_field!(routing.subsurface_flow.variables.q, gpu, 6)
     get_field!(model.land.soil.variables.saturated_water_depth, gpu, 4)
+    if gpu.n_reservoirs > 0
+        rv = routing.river_flow.boundary_conditions.reservoir.variables
+        get_field!(rv.storage, gpu, F_RESERVOIR_STORAGE)
+        get_field!(rv.waterlevel, gpu, F_RESERVOIR_WATERLEVEL)
+        get_field!(rv.outflow, gpu, F_RESERVOIR_OUTFLOW)
+        get_field!(rv.outflow_average, gpu, F_RESERVOIR_OUTFLOW_AVERAGE)
+    end
     return nothing
 end
 

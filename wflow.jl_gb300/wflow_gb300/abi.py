@@ -101,6 +101,20 @@ class WfMetrics(C.Structure):
     ]
 
 
+# WfReservoirOutflow
+WF_RES_FREE_WEIR = 2
+WF_RES_MODIFIED_PULS = 3
+WF_RES_SIMPLE = 4
+RESERVOIR_PARAMS = ["area", "waterlevel", "maximum_storage", "threshold", "rating_curve_coefficient",
+                    "rating_curve_exponent", "maximum_release", "demand", "target_minimum_fraction",
+                    "target_full_fraction"]
+
+
+class WfReservoirs(C.Structure):
+    _fields_ = ([("n", _i64), ("river_index", _pi32), ("outflow_curve_type", _pi32)]
+                + [(k, _pd) for k in RESERVOIR_PARAMS])
+
+
 class WfTuning(C.Structure):
     _fields_ = [("vertical_block", _i32), ("routing_warps", _i32), ("routing_blocks_per_sm", _i32),
                 ("use_graph", _i32), ("reserved", _i32 * 4)]
@@ -117,11 +131,20 @@ _LAND_FIELDS = [
     "LAND_STORAGE", "LAND_TO_RIVER_AVERAGE", "LAND_INWATER", "TOTAL_STORAGE", "BALANCE_LAND_ERROR",
     "BALANCE_LAND_RELATIVE_ERROR", "BALANCE_OVERLAND_ERROR", "BALANCE_OVERLAND_RELATIVE_ERROR",
     "BALANCE_SUBSURFACE_ERROR", "BALANCE_SUBSURFACE_RELATIVE_ERROR", "VOLUMETRIC_WATER_CONTENT",
+    "LAND_QIN_AVERAGE",
 ]
 _RIVER_FIELDS = ["RIVER_Q", "RIVER_H", "RIVER_STORAGE", "RIVER_Q_AVERAGE", "RIVER_QIN_AVERAGE",
                  "RIVER_INWATER", "BALANCE_RIVER_ERROR", "BALANCE_RIVER_RELATIVE_ERROR"]
+_RESERVOIR_FIELDS = ["RESERVOIR_STORAGE", "RESERVOIR_WATERLEVEL", "RESERVOIR_OUTFLOW", "RESERVOIR_OUTFLOW_AVERAGE",
+                     "RESERVOIR_INFLOW_AVERAGE", "RESERVOIR_ACTEVAP_AVERAGE", "RESERVOIR_ABSTRACTION_AVERAGE",
+                     "RESERVOIR_INFLOW_OVERLAND", "RESERVOIR_INFLOW_SUBSURFACE", "RESERVOIR_PRECIPITATION",
+                     "RESERVOIR_EVAPORATION", "RESERVOIR_EXTERNAL_INFLOW", "RESERVOIR_OUTFLOW_OBS",
+                     "BALANCE_RESERVOIR_ERROR", "BALANCE_RESERVOIR_RELATIVE_ERROR"]
 FIELD = {name: i for i, name in enumerate(_LAND_FIELDS)}
 FIELD.update({name: 100 + i for i, name in enumerate(_RIVER_FIELDS)})
+FIELD.update({name: 200 + i for i, name in enumerate(_RESERVOIR_FIELDS)})
+RESERVOIR_INPUT_FIELDS = ["RESERVOIR_PRECIPITATION", "RESERVOIR_EVAPORATION", "RESERVOIR_EXTERNAL_INFLOW",
+                          "RESERVOIR_OUTFLOW_OBS"]
 LAYERED_FIELDS = {"UNSATURATED_LAYER_DEPTH", "VOLUMETRIC_WATER_CONTENT"}
 STATE_FIELDS = ["CANOPY_STORAGE", "SNOW_STORAGE", "SNOW_WATER", "SOIL_SURFACE_TEMPERATURE",
                 "SATURATED_WATER_DEPTH", "UNSATURATED_LAYER_DEPTH", "SSF_Q", "LAND_Q", "LAND_H",
@@ -129,7 +152,11 @@ STATE_FIELDS = ["CANOPY_STORAGE", "SNOW_STORAGE", "SNOW_WATER", "SOIL_SURFACE_TE
 
 
 def is_river_field(fid):
-    return fid >= 100
+    return 100 <= fid < 200
+
+
+def is_reservoir_field(fid):
+    return fid >= 200
 
 
 def as_ptr(arr, ctype=C.c_double):
@@ -206,6 +233,9 @@ def _declare(lib):
         "wf_get_kernel_times": (_i32, [H, _pd, C.POINTER(_i64)]),
         "wf_struct_size": (_i32, [_i32]),
         "wf_plan_routing": (_i32, [_i64, _pi32, _i32, C.POINTER(_i64), C.POINTER(_i64), _pi32, _pi32]),
+        "wf_create_with_reservoirs": (_i32, [C.POINTER(WfConfig), C.POINTER(WfDomain), C.POINTER(WfParams),
+                                             C.POINTER(WfReservoirs), _i32, C.POINTER(H)]),
+        "wf_get_reservoir_count": (_i32, [H, C.POINTER(_i64)]),
     }
     for name, (res, args) in extra.items():
         if hasattr(lib, name):

@@ -19,14 +19,21 @@ from . import abi, synthetic
 
 
 class Model:
-    def __init__(self, config, domain, params=None, device=0):
+    def __init__(self, config, domain, params=None, device=0, reservoirs=None):
         self.lib = abi.load_library(required=True)
         self.config = config
         self.domain = domain
         self._params = params if params is not None else domain.params
         self._d, self._p = synthetic.c_structs(domain, self._params)
         h = C.c_void_p()
-        st = self.lib.wf_create(C.byref(config), C.byref(self._d), C.byref(self._p), int(device), C.byref(h))
+        if reservoirs is not None:
+            # ReservoirModel (reservoir.jl:290-300) at the reservoirs' river cells
+            self._reservoirs = reservoirs
+            self._r = synthetic.c_reservoirs(reservoirs)
+            st = self.lib.wf_create_with_reservoirs(C.byref(config), C.byref(self._d), C.byref(self._p),
+                                                    C.byref(self._r), int(device), C.byref(h))
+        else:
+            st = self.lib.wf_create(C.byref(config), C.byref(self._d), C.byref(self._p), int(device), C.byref(h))
         if st != abi.WF_OK:
             msg = self.lib.wf_last_error(None)
             raise RuntimeError(f"wf_create failed with status {st}: {msg.decode() if msg else ''}")
@@ -35,6 +42,7 @@ class Model:
         self.nr = domain.n_river
         self.M = max(1, config.n_members)
         self.N = config.n_soil_layer_thickness + 1
+        self.nres = 0 if reservoirs is None else int(reservoirs["river_index"].size)
         self._tune_state = dict(vertical_block=0, routing_warps=0, routing_blocks_per_sm=0)
 
     def close(self):
@@ -86,9 +94,14 @@ class Model:
         self._check(self.lib.wf_synchronize(self.h), "wf_synchronize")
 
     # ---- BMI-like access
+    def _extent(self, fid):
+        if abi.is_reservoir_field(fid):
+            return self.nres
+        return self.nr if abi.is_river_field(fid) else self.n
+
     def get_value(self, field, layer=0, offset=0, count=None):
         fid = abi.FIELD[field] if isinstance(field, str) else int(field)
-        total = (self.nr if abi.is_river_field(fid) else self.n) * self.M
+        total = self._extent(fid) * self.M
         count = total - offset if count is None else count
         out = np.empty(count)
         self._check(self.lib.wf_get_field(self.h, fid, layer, abi.as_ptr(out), offset, count), "wf_get_field")

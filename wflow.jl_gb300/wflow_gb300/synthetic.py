@@ -272,3 +272,73 @@ def c_structs(dom, params=None):
     for k in abi.PARAM_FIELDS:
         setattr(p, k, abi.as_ptr(params.get(k)))
     return d, p
+
+
+def make_reservoirs(dom, n, seed=1, types=(abi.WF_RES_SIMPLE, abi.WF_RES_MODIFIED_PULS, abi.WF_RES_FREE_WEIR)):
+    """`n` reservoirs on river cells of the domain (outflow types cycling through `types`), at
+    cells with a downstream river cell, no two draining into the same cell. Parameters are of the
+    scale of the reference's reservoir unit test (test/routing_process.jl:310-331) with the area
+    scaled down so that a step's inflow moves the water level noticeably."""
+    rng = np.random.default_rng([int(seed), 77])
+    rds = dom.river["river_downstream"]
+    rland = dom.river["river_land_index"]
+    up = np.asarray(dom.upstream_cells)[rland]
+    order = np.argsort(-up, kind="stable")
+    cand = [int(v) for v in order if rds[v] >= 0][: max(4 * n, n)]
+    rng.shuffle(cand)
+    chosen, fed = [], set()
+    for v in cand:
+        if len(chosen) == n:
+            break
+        if v in chosen or int(rds[v]) in fed:
+            continue
+        chosen.append(v)
+        fed.add(int(rds[v]))
+    k = len(chosen)
+    t = np.array([types[i % len(types)] for i in range(k)], np.int32)
+    area = rng.uniform(2.0e4, 2.0e5, k)
+    wl = rng.uniform(2.0, 8.0, k)
+    nan = np.full(k, np.nan)
+    simple = t == abi.WF_RES_SIMPLE
+    weir = (t == abi.WF_RES_FREE_WEIR) | (t == abi.WF_RES_MODIFIED_PULS)
+    res = dict(
+        river_index=np.array(chosen, np.int32), outflow_curve_type=t, area=area, waterlevel=wl,
+        maximum_storage=np.where(simple, area * wl * rng.uniform(1.05, 1.4, k), nan),
+        threshold=np.where(weir, wl - rng.uniform(0.1, 1.0, k), nan),
+        rating_curve_coefficient=np.where(weir, rng.uniform(0.5, 5.0, k), nan),
+        rating_curve_exponent=np.where(t == abi.WF_RES_FREE_WEIR, rng.uniform(1.2, 2.0, k), nan),
+        maximum_release=np.where(simple, rng.uniform(0.5, 5.0, k), nan),
+        demand=np.where(simple, rng.uniform(0.01, 0.3, k), nan),
+        target_minimum_fraction=np.where(simple, rng.uniform(0.05, 0.2, k), nan),
+        target_full_fraction=np.where(simple, rng.uniform(0.6, 0.9, k), nan),
+    )
+    return {key: np.ascontiguousarray(v) for key, v in res.items()}
+
+
+def reservoir_forcing(dom, res, P, PET, M=1):
+    """Reservoir precipitation and evaporation of a step [m s-1], member-major, taken from the
+    land forcing at each reservoir's outlet cell (a one-cell reservoir area; Wflow averages the
+    forcing over the reservoir's area cells, io.jl:128-137)."""
+    cells = dom.river["river_land_index"][res["river_index"]]
+    n = dom.n_land
+    P = np.asarray(P).reshape(-1)
+    PET = np.asarray(PET).reshape(-1)
+    mp = P.size // n
+    rp = np.concatenate([P[(m if mp > 1 else 0) * n + cells] for m in range(M)])
+    re = np.concatenate([PET[(m if PET.size // n > 1 else 0) * n + cells] for m in range(M)])
+    return np.ascontiguousarray(rp), np.ascontiguousarray(re)
+
+
+def c_reservoirs(res):
+    """WfReservoirs struct pointing into the arrays of a reservoir dict (keep `res` alive)."""
+    import ctypes as C
+    r = abi.WfReservoirs()
+    if res is None:
+        r.n = 0
+        return r
+    r.n = int(res["river_index"].size)
+    r.river_index = abi.as_ptr(res["river_index"], C.c_int32)
+    r.outflow_curve_type = abi.as_ptr(res["outflow_curve_type"], C.c_int32)
+    for k in abi.RESERVOIR_PARAMS:
+        setattr(r, k, abi.as_ptr(res.get(k)))
+    return r
