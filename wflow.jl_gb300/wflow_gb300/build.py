@@ -26,6 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_UNITS = [
     ("wf_api.cu", []),
     ("wf_plan.cpp", None),
+    ("wf_netcdf.cpp", None),
     ("kernels_fp64.cu", ["--fmad=false"]),
     ("kernels_split.cu", ["-prec-div=false"]),
     ("kernels_adaptive.cu", ["--fmad=false"]),
@@ -63,7 +64,7 @@ def build_synth(force=False):
 
 
 def _headers():
-    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [REPO_ROOT / "include" / "wflow_gb300.h"]
+    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((REPO_ROOT / "include").glob("wflow_gb300*.h"))
 
 
 def build_cuda(force=False, verbose=False):
