@@ -230,3 +230,31 @@ def test_record_padding_matches_scipy(tmp_path, code, nctype, n_rec_vars):
         assert np.array_equal(r.variables["v"][:], vals)
         if n_rec_vars == 2:
             assert np.array_equal(r.variables["w"][:], w_vals)
+
+
+def test_one_dimensional_record_variable(tmp_path):
+    # a time coordinate (one value per record) beside a gridded record variable: its values are
+    # a record size apart in the file, not contiguous
+    p = tmp_path / "t.nc"
+    f = netcdf(str(p), "w", version=2)
+    f.createDimension("time", None)
+    f.createDimension("x", 3)
+    f.createVariable("time", "d", ("time",))[:] = [1.5, 2.5, 3.5, 4.5]
+    f.createVariable("v", "f", ("time", "x"))[:] = np.arange(12, dtype=np.float32).reshape(4, 3)
+    f.close()
+    r = ncio.NcFile(p)
+    assert np.array_equal(r.read("time"), [1.5, 2.5, 3.5, 4.5])
+    assert np.array_equal(r.read("time", start=[1], count=[2]), [2.5, 3.5])
+    q = tmp_path / "o.nc"
+    w = ncio.NcFile(q, "w", format=1)
+    w.def_dim("time", 0)
+    w.def_dim("x", 3)
+    w.def_var("time", ncio.NC_DOUBLE, ("time",))
+    w.def_var("v", ncio.NC_DOUBLE, ("time", "x"))
+    w.write("time", np.array([10.0, 20.0, 30.0]))
+    for k in range(3):
+        w.write("v", np.full((1, 3), float(k)), start=[k, 0])
+    w.close()
+    with netcdf(str(q), "r", mmap=False) as g:
+        assert np.array_equal(g.variables["time"][:], [10.0, 20.0, 30.0])
+        assert np.array_equal(g.variables["v"][:], np.repeat(np.arange(3.0)[:, None], 3, axis=1))

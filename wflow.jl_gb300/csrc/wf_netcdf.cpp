@@ -341,6 +341,14 @@ template <class Fn>
 bool for_runs(const WfNcFile* f, const NcVar& v, const int64_t* start, const int64_t* count, Fn fn) {
     const size_t nd = v.dimids.size();
     if (nd == 0) return fn(v.begin, (int64_t)0, (int64_t)1);
+    if (v.record && nd == 1) {  // one value per record: records are recsize apart, not contiguous
+        int64_t idx[1];
+        for (int64_t r = 0; r < count[0]; ++r) {
+            idx[0] = start[0] + r;
+            if (!fn(elem_offset(f, v, idx), r, (int64_t)1)) return false;
+        }
+        return true;
+    }
     int64_t idx[kMaxDims];
     for (size_t k = 0; k < nd; ++k) {
         if (count[k] == 0) return true;

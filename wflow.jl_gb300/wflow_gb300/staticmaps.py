@@ -301,7 +301,16 @@ def _reservoirs(S, cells, river_land):
                     ("target_minimum_fraction", "reservoir_water__target_min_volume_fraction"),
                     ("target_full_fraction", "reservoir_water__target_full_volume_fraction")]:
         res[key] = at(sn, nan)
-    return {k: np.ascontiguousarray(v) for k, v in res.items()}
+    out = {k: np.ascontiguousarray(v) for k, v in res.items()}
+    # the reservoirs' areas: grid cells (flat y * nx + x, active or not) of each reservoir id
+    # (network.jl:325-347), for averaging the forcing over them
+    ids_r = ids[ri]
+    if S.has("reservoir_area__count"):
+        area_map = S.read("reservoir_area__count").reshape(-1)
+        out["coverage_cells"] = [np.flatnonzero(area_map == v) for v in ids_r]
+    else:
+        out["coverage_cells"] = [np.array([cells[river_land[k]]]) for k in ri]
+    return out
 
 
 # ------------------------------------------------------------------ writing ------------------
