@@ -1739,6 +1739,67 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
 
 }  // namespace
 
+// ============================================================ lateral snow transport ======
+//
+// Transport of material downstream with a capacity-limited flux over the drainage graph in
+// topological order (accucapacityflux!, routing/utils.jl:82-110): each node passes
+// min(material / dt, capacity) downstream (a pit passes it out of the domain); and the lateral
+// snow transport built on it (lateral_snow_transport!, routing/surface/surface_process.jl:1-19):
+// a slope- and storage-dependent fraction of the dry snow and of the liquid water in the snow
+// moves downhill each step, the inflow of a cell being the sum of its upstream cells' outflow
+// (flux_in!, routing/utils.jl:160-166).
+namespace {
+
+void accucapacityflux(const int32_t* ds, const int64_t* order, int64_t n, double dt, const double* capacity,
+                      double* material, double* flux) {
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t v = order[k];
+        const double flux_val = jmin(material[v] / dt, capacity[v]);
+        const double update = flux_val * dt;
+        material[v] -= update;
+        flux[v] = flux_val;
+        if (ds[v] >= 0) material[ds[v]] += update;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+// accucapacityflux!: material is updated in place, flux overwritten.
+void orc_accucapacityflux(const int32_t* ds, const int64_t* order, int64_t n, double dt, const double* capacity,
+                          double* material, double* flux) {
+    accucapacityflux(ds, order, n, dt, capacity, material, flux);
+}
+
+// lateral_snow_transport!: snow_out and snow_in [m s-1] of every cell; the graph's upstream
+// lists for the inflow are `ups_ds` (the reservoir-cut lists of the domain; equal to ds
+// without reservoirs).
+void orc_lateral_snow_transport(const int32_t* ds, const int32_t* ups_ds, const int64_t* order, int64_t n, double dt,
+                                const double* slope, const double* snow_storage, const double* snow_water,
+                                double* snow_out, double* snow_in) {
+    const double TAN80 = 5.67;
+    const double snow_storage_max = 10.0;
+    std::vector<double> frac(n), maxflux(n), m1(snow_storage, snow_storage + n), m2(snow_water, snow_water + n),
+        f2(n), cap2(n);
+    for (int64_t i = 0; i < n; ++i) {
+        frac[i] = jmin(0.5, slope[i] / TAN80) * jmin(1.0, snow_storage[i] / snow_storage_max);
+        maxflux[i] = frac[i] * snow_storage[i] / dt;
+        cap2[i] = snow_water[i] * frac[i] / dt;
+    }
+    accucapacityflux(ds, order, n, dt, maxflux.data(), m1.data(), snow_out);
+    accucapacityflux(ds, order, n, dt, cap2.data(), m2.data(), f2.data());
+    for (int64_t i = 0; i < n; ++i) snow_out[i] += f2[i];
+    std::vector<std::vector<int64_t>> ups(n);  // upstream lists in ascending node order
+    for (int64_t i = 0; i < n; ++i)
+        if (ups_ds[i] >= 0) ups[ups_ds[i]].push_back(i);
+    for (int64_t v = 0; v < n; ++v) {
+        double acc = 0.0;
+        for (int64_t u : ups[v]) acc = acc + snow_out[u];
+        snow_in[v] = acc;
+    }
+}
+}  // extern "C"
+
 extern "C" {
 // Reservoir at a river node with discharge q after the node's kinematic-wave update.
 void orc_reservoir_update(OrcReservoir* r, double q, double dt) { update_reservoir_at_node(*r, q, dt); }

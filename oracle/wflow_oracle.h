@@ -127,6 +127,14 @@ double orc_kinwave_stable_timestep(const double* q, const double* alpha, const d
                                    int64_t n, double p);
 double orc_quantile(double* v, int64_t n, double p);
 
+/* capacity-limited transport over a drainage graph (routing/utils.jl:82-110) and the lateral
+ * snow transport built on it (routing/surface/surface_process.jl:1-19) */
+void orc_accucapacityflux(const int32_t* ds, const int64_t* order, int64_t n, double dt, const double* capacity,
+                          double* material, double* flux);
+void orc_lateral_snow_transport(const int32_t* ds, const int32_t* ups_ds, const int64_t* order, int64_t n, double dt,
+                                const double* slope, const double* snow_storage, const double* snow_water,
+                                double* snow_out, double* snow_in);
+
 /* full model */
 typedef struct OrcModel OrcModel;
 int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p, OrcModel** out);

@@ -305,6 +305,20 @@ def build():
                        reservoir_actevap_cumulative=num(R, 382)),
                   note="node 1 carries a simple reservoir (outflow type 4, linear storage profile) with an "
                        "abstraction; node 2 receives its outflow (the test's upstream list also keeps node 1)"))
+    # accucapacityflux on the 6-node graph of the PCRaster accucapacity example (exact)
+    edges = [nums(R, ln)[-2:] for ln in range(261, 266)]
+    ds = [-1] * 6
+    for a, b in edges:
+        ds[int(a) - 1] = int(b) - 1
+    dt_acc = num(R, 269)
+    K.append(case("accucapacityflux_1", "accucapacityflux", f"{R}:255-277",
+                  dict(downstream=ds, order=list(range(6)), dt=dt_acc, material=[dt_acc * v for v in nums(R, 270)],
+                       capacity=[nums(R, 271)[0]] * 6),
+                  dict(material=[dt_acc * v for v in nums(R, 274)], flux=nums(R, 275)), cmp="exact"))
+    K.append(case("accucapacityflux_2", "accucapacityflux", f"{R}:279-287",
+                  dict(downstream=ds, order=list(range(6)), dt=dt_acc, material=[dt_acc * nums(R, 280)[0]] * 6,
+                       capacity=nums(R, 281)),
+                  dict(material=[dt_acc * v for v in nums(R, 284)], flux=nums(R, 285)), cmp="exact"))
     # ------------------------------------------------------------------------ utils.jl
     K.append(case("scurve", "scurve", f"{U}:66-77",
                   dict(x=num(U, 71), a=num(U, 67), b=num(U, 68), c=num(U, 69)), dict(s=num(U, 73))))

@@ -140,6 +140,19 @@ def run_case(c, prev):
                 v = v[: len(c["expect"][k])]
             out[k] = v
         return out
+    if fn == "accucapacityflux":
+        import ctypes as C
+        ds = np.asarray(a["downstream"], np.int32)
+        order = np.asarray(a["order"], np.int64)
+        material = np.asarray(a["material"], float).copy()
+        cap = np.asarray(a["capacity"], float)
+        flux = np.zeros_like(material)
+        O.lib().orc_accucapacityflux(ds.ctypes.data_as(C.POINTER(C.c_int32)),
+                                     order.ctypes.data_as(C.POINTER(C.c_int64)), C.c_int64(len(ds)),
+                                     C.c_double(a["dt"]), cap.ctypes.data_as(C.POINTER(C.c_double)),
+                                     material.ctypes.data_as(C.POINTER(C.c_double)),
+                                     flux.ctypes.data_as(C.POINTER(C.c_double)))
+        return dict(material=material, flux=flux)
     if fn == "kinwave_river_update":
         import ctypes as C
         q = np.array(a["q"])
@@ -163,7 +176,7 @@ def run_case(c, prev):
 
 
 def test_fixture_is_complete():
-    assert len(KATS["cases"]) >= 59
+    assert len(KATS["cases"]) >= 61
     for c in KATS["cases"]:
         assert ".jl:" in c["src"]
 
