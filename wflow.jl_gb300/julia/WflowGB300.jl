@@ -139,6 +139,32 @@ function downstream_index(graph)
 end
 
 """
+    check_supported(config)
+
+Throw when the model uses a component outside the GPU step (the caller then keeps the
+reference's own `update_model!`): model type other than `sbm`, glaciers, gravitational snow
+transport, water demand, floodplains, drains, local-inertial or staggered routing, Kv profiles
+other than exponential / exponential_constant, reservoirs with tabulated curves.
+"""
+function check_supported(config)
+    m = config.model
+    bad = String[]
+    m.type == Wflow.ModelType.sbm || push!(bad, "model type $(m.type)")
+    m.glacier__flag && push!(bad, "glacier__flag")
+    m.snow_gravitational_transport__flag && push!(bad, "snow_gravitational_transport__flag")
+    Wflow.do_water_demand(config) && push!(bad, "water demand")
+    m.floodplain_1d__flag && push!(bad, "floodplain_1d__flag")
+    m.drain__flag && push!(bad, "drain__flag")
+    m.land_routing == Wflow.RoutingType.kinematic_wave || push!(bad, "land_routing $(m.land_routing)")
+    m.river_routing == Wflow.RoutingType.kinematic_wave || push!(bad, "river_routing $(m.river_routing)")
+    m.saturated_hydraulic_conductivity_profile in (Wflow.VerticalConductivityProfile.exponential,
+        Wflow.VerticalConductivityProfile.exponential_constant) ||
+        push!(bad, "saturated_hydraulic_conductivity_profile $(m.saturated_hydraulic_conductivity_profile)")
+    isempty(bad) || error("not supported by the GPU step: " * join(bad, ", "))
+    return nothing
+end
+
+"""
     GpuStep(model::Wflow.Model)
 
 Copy the model's domain, parameters (as read from the static maps, in SI) and current state
@@ -146,6 +172,7 @@ to a new library handle (`wf_create`, then `wf_set_field` for a warm state).
 """
 function GpuStep(model)
     (; domain, land, routing, config) = model
+    check_supported(config)
     lp = domain.land.parameters
     rp = domain.river.parameters
     soil = land.soil.parameters
