@@ -235,6 +235,7 @@ function GpuStep(model)
         p = rv.parameters
         all(==(Wflow.ReservoirProfileType.linear), p.storage_curve_type) ||
             error("the GPU step supports the linear reservoir storage profile only")
+        all(iszero, p.lower_reservoir_ind) || error("the GPU step does not support linked reservoirs")
         nres = length(p.area)
         res = WfReservoirs(nres, k(Int32.(domain.reservoir.network.river_indices .- 1)),
             k(Int32.(Integer.(p.outflow_curve_type))), k(p.area), k(rv.variables.waterlevel),
