@@ -258,3 +258,41 @@ def test_one_dimensional_record_variable(tmp_path):
     with netcdf(str(q), "r", mmap=False) as g:
         assert np.array_equal(g.variables["time"][:], [10.0, 20.0, 30.0])
         assert np.array_equal(g.variables["v"][:], np.repeat(np.arange(3.0)[:, None], 3, axis=1))
+
+
+def test_corrupted_files_are_rejected_or_read_without_crashing(tmp_path):
+    # bytes of a valid file's header flipped at random, or the file cut short: the reader either
+    # rejects the file with an error or reads it; it never reads out of bounds
+    p = tmp_path / "base.nc"
+    w = ncio.NcFile(p, "w", format=2)
+    w.def_dim("time", 0)
+    w.def_dim("y", 4)
+    w.def_dim("x", 5)
+    w.def_var("a", ncio.NC_DOUBLE, ("y", "x"), {"units": "mm", "_FillValue": -9.0})
+    w.def_var("t", ncio.NC_DOUBLE, ("time",))
+    w.def_var("r", ncio.NC_SHORT, ("time", "y", "x"))
+    w.write("a", np.arange(20.0).reshape(4, 5))
+    w.write("t", np.arange(3.0))
+    w.write("r", np.ones((3, 4, 5)))
+    w.close()
+    base = p.read_bytes()
+    rng = np.random.default_rng(0)
+    q = tmp_path / "fz.nc"
+    for _ in range(400):
+        b = bytearray(base)
+        for _ in range(int(rng.integers(1, 4))):
+            b[int(rng.integers(0, min(len(b), 300)))] = int(rng.integers(0, 256))
+        if rng.random() < 0.2:
+            b = b[: int(rng.integers(4, len(b)))]
+        q.write_bytes(bytes(b))
+        try:
+            f = ncio.NcFile(q)
+        except (OSError, ValueError):
+            continue
+        for name in list(f.variables):
+            try:
+                f.read(name)
+                f.attrs(name)
+            except (ValueError, KeyError, MemoryError):
+                pass
+        f.close()
