@@ -122,7 +122,7 @@ class NcFile:
         n, rec = C.c_int64(), C.c_int32()
         for i in range(self.lib.wf_nc_ndims(self.h)):
             self.lib.wf_nc_dim(self.h, i, buf, 1024, C.byref(n), C.byref(rec))
-            out[buf.value.decode()] = (n.value, bool(rec.value))
+            out[buf.value.decode(errors="replace")] = (n.value, bool(rec.value))
         return out
 
     @property
@@ -135,7 +135,7 @@ class NcFile:
         ids = (C.c_int32 * 16)()
         for i in range(self.lib.wf_nc_nvars(self.h)):
             self.lib.wf_nc_var(self.h, i, buf, 1024, C.byref(t), C.byref(nd), ids)
-            out[buf.value.decode()] = (t.value, tuple(dims[ids[k]] for k in range(nd.value)))
+            out[buf.value.decode(errors="replace")] = (t.value, tuple(dims[ids[k]] for k in range(nd.value)))
         return out
 
     def _varid(self, name):
@@ -168,7 +168,7 @@ class NcFile:
         out = []
         for i in range(max(0, self.lib.wf_nc_natts(self.h, vid))):
             self.lib.wf_nc_att_name(self.h, vid, i, buf, 1024)
-            out.append(buf.value.decode())
+            out.append(buf.value.decode(errors="replace"))
         return out
 
     def shape(self, name):
@@ -207,7 +207,7 @@ class NcFile:
         buf = C.create_string_buffer(1024)
         for i in range(self.lib.wf_nc_ndims(self.h)):
             self.lib.wf_nc_dim(self.h, i, buf, 1024, None, None)
-            out.append(buf.value.decode())
+            out.append(buf.value.decode(errors="replace"))
         return out
 
     def put_att(self, var, key, value, nctype=NC_DOUBLE):
