@@ -62,10 +62,11 @@ class ForcingFile:
         self.reservoirs = reservoirs
 
     def _entry(self, sn):
-        m = self.mapping.get(sn, sn)
-        if isinstance(m, dict):
-            return m.get("name", sn), float(m.get("scale", 1.0)), float(m.get("offset", 0.0))
-        return m, 1.0, 0.0
+        from .config import _entry
+        e = _entry(self.mapping.get(sn, sn))
+        if "value" in e:
+            raise ValueError(f"forcing `{sn}` must be a netCDF variable")
+        return e["name"], float(np.ravel(e.get("scale", 1.0))[0]), float(np.ravel(e.get("offset", 0.0))[0])
 
     def index(self, t):
         """The record used at model time t: the first at or after t (io.jl:9-22)."""

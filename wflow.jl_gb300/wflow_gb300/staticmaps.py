@@ -106,25 +106,50 @@ class _Maps:
         self.xc = np.sort(xc)
         self.yc = np.sort(yc)
 
-    def has(self, sn):
+    def _entry(self, sn):
+        """The mapping's entry for a standard name: {"name", "scale", "offset"} or {"value"}
+        (the three forms of a TOML [input] entry, config_init.jl:113-156)."""
+        from .config import _entry
         m = self.mapping.get(sn, sn)
-        return isinstance(m, dict) or m in self.vars
+        e = _entry(m)
+        if "layer" in e:
+            raise ValueError(f"`layer` selections of [input] entries are not supported ({sn})")
+        return e
+
+    def has(self, sn):
+        e = self._entry(sn)
+        return "value" in e or e["name"] in self.vars
 
     def read(self, sn, default=None, layered=False, n_layers=None):
         """(ny, nx) or (layer, ny, nx) array; a constant from the mapping ({"value": v}) or the
-        default when the variable is absent; KeyError when neither exists."""
-        m = self.mapping.get(sn, sn)
+        default when the variable is absent; KeyError when neither exists. The entry's scale
+        and offset are applied as apply_affine_transform! does (utils.jl:239-256)."""
+        e = self._entry(sn)
         shape = (len(self.yc), len(self.xc))
-        if isinstance(m, dict) and "value" in m:
-            v = np.asarray(m["value"], float)
+        if "value" in e:
+            v = np.asarray(e["value"], float)
             if layered:
                 return np.broadcast_to(v.reshape(-1, 1, 1), (v.size if v.ndim else n_layers,) + shape).copy()
             return np.full(shape, float(v))
+        m = e["name"]
         if m not in self.vars:
             if default is None:
                 raise KeyError(f"static map `{sn}` not found")
             return np.full(((n_layers,) if layered else ()) + shape, float(default))
-        a = self.nc.read(m)
+        a = self._standardise(m, self.nc.read(m))
+        scale = np.asarray(e.get("scale", 1.0), float)
+        offset = np.asarray(e.get("offset", 0.0), float)
+        if scale.ndim:  # per-layer vectors
+            scale = scale.reshape((-1,) + (1,) * (a.ndim - 1)) if scale.size > 1 else scale.reshape(())
+        if offset.ndim:
+            offset = offset.reshape((-1,) + (1,) * (a.ndim - 1)) if offset.size > 1 else offset.reshape(())
+        if np.any(scale != 1.0):
+            a = a * scale
+        if np.any(offset != 0.0):
+            a = a + offset
+        return a
+
+    def _standardise(self, m, a):
         dims = list(self.vars[m][1])
         ren = {self.xname: "x", self.yname: "y"}
         dims = [ren.get(d, d) for d in dims]
@@ -314,9 +339,11 @@ def _reservoirs(S, cells, river_land):
 
 
 # ------------------------------------------------------------------ writing ------------------
-def write_staticmaps(dom, path, grid=None, reservoirs=None, format=2):
+def write_staticmaps(dom, path, grid=None, reservoirs=None, format=2, names=None):
     """Write a domain's land, river and parameter arrays as a Wflow static-map file (standard
-    names, file units): the inverse of `load_staticmaps` for cell_length_in_meter grids."""
+    names, or the file names `names` maps them to; file units): the inverse of
+    `load_staticmaps` for cell_length_in_meter grids."""
+    names = names or {}
     grid = Grid.of_domain(dom) if grid is None else grid
     n = dom.n_land
     nc = ncio.NcFile(path, "w", format=format)
@@ -381,11 +408,11 @@ def write_staticmaps(dom, path, grid=None, reservoirs=None, format=2):
             maps[sn] = (ncio.NC_DOUBLE, grid_of(reservoirs[key], cells), np.nan)
     for sn, (t, a, fill) in maps.items():
         dims = ("layer", "y", "x") if a.ndim == 3 else ("y", "x")
-        nc.def_var(sn, t, dims, {"_FillValue": fill})
+        nc.def_var(names.get(sn, sn), t, dims, {"_FillValue": fill})
     nc.enddef()
     nc.write("x", grid.xc)
     nc.write("y", grid.yc)
     nc.write("layer", np.arange(1, N + 1, dtype=float))
     for sn, (t, a, fill) in maps.items():
-        nc.write(sn, a)
+        nc.write(names.get(sn, sn), a)
     nc.close()
