@@ -1800,6 +1800,109 @@ void orc_lateral_snow_transport(const int32_t* ds, const int32_t* ups_ds, const 
 }
 }  // extern "C"
 
+// ============================================================ local-inertial river =======
+//
+// River flow on a staggered grid by the local-inertial approximation (de Almeida et al. 2012):
+// discharge on the edges between river cells from the water-surface slope, friction and the
+// previous discharge (local_inertial_flow, routing/surface/surface_process.jl:88-163), water
+// depth on the cells from the edge discharges (update_water_depth_and_storage!,
+// routing/surface/surface_staggered_scheme.jl:723-760), edges first (update_river_channel_flow!,
+// :326-385), and the stable time step min over cells of alpha dx / sqrt(g h) (:1004-1020).
+// Channel only (no floodplain, no reservoirs at edges).
+namespace {
+
+constexpr double GRAVITY = 9.80665;
+
+// local_inertial_flow, general cross-section (surface_process.jl:88-115)
+double li_flow_area(double q0, double zs0, double zs1, double hf, double A, double R, double length,
+                    double mannings_n_sq, bool froude_limit, double dt) {
+    const double slope = (zs1 - zs0) / length;
+    const double pow_R = wcbrt(R * R * R * R);
+    double q = (q0 - GRAVITY * A * dt * slope) / (1.0 + GRAVITY * dt * mannings_n_sq * std::fabs(q0) / (pow_R * A));
+    const double fr = ((q / A) / std::sqrt(GRAVITY * hf)) * (froude_limit ? 1.0 : 0.0);
+    if (std::fabs(fr) > 1.0 && q > 0.0) q = std::sqrt(GRAVITY * hf) * A;
+    if (std::fabs(fr) > 1.0 && q < 0.0) q = -std::sqrt(GRAVITY * hf) * A;
+    return q;
+}
+
+// local_inertial_flow, rectangular cross-section with the theta weighting (:124-163)
+double li_flow_rect(double theta, double q0, double qd, double qu, double zs0, double zs1, double hf, double width,
+                    double length, double mannings_n_sq, bool froude_limit, double dt) {
+    const double slope = (zs1 - zs0) / length;
+    const double pow_hf = wcbrt(hf * hf * hf * hf * hf * hf * hf);
+    double q = ((theta * q0 + 0.5 * (1.0 - theta) * (qu + qd)) - GRAVITY * hf * width * dt * slope) /
+               (1.0 + GRAVITY * dt * mannings_n_sq * std::fabs(q0) / (pow_hf * width));
+    if (froude_limit) {
+        const double fr = (q / width / hf) / std::sqrt(GRAVITY * hf);
+        if (std::fabs(fr) > 1.0 && q > 0.0) q = hf * std::sqrt(GRAVITY * hf) * width;
+        else if (std::fabs(fr) > 1.0 && q < 0.0) q = -hf * std::sqrt(GRAVITY * hf) * width;
+    }
+    return q;
+}
+
+}  // namespace
+
+extern "C" {
+
+double orc_li_flow_area(double q0, double zs0, double zs1, double hf, double A, double R, double length,
+                        double mannings_n_sq, int32_t froude_limit, double dt) {
+    return li_flow_area(q0, zs0, zs1, hf, A, R, length, mannings_n_sq, froude_limit != 0, dt);
+}
+
+double orc_li_flow_rect(double theta, double q0, double qd, double qu, double zs0, double zs1, double hf,
+                        double width, double length, double mannings_n_sq, int32_t froude_limit, double dt) {
+    return li_flow_rect(theta, q0, qd, qu, zs0, zs1, hf, width, length, mannings_n_sq, froude_limit != 0, dt);
+}
+
+// One local-inertial river step over n cells and n_edges edges (edge k from src[k] to dst[k],
+// in the graph's edge order); the first n_active cells are updated (the others are boundary
+// cells of fixed depth). Arrays: zb, flow_length, flow_width, inwater [n]; zb_e, width_e,
+// length_e, nsq_e [n_edges]; state h, storage [n], q, q_prev, q_cum [n_edges].
+void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
+                       const double* zb, const double* flow_length, const double* flow_width, const double* inwater,
+                       const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
+                       double h_thresh, int32_t froude_limit, double dt, double* h, double* storage, double* q,
+                       double* q_prev, double* q_cum) {
+    for (int64_t k = 0; k < n_edges; ++k) q_prev[k] = q[k];
+    for (int64_t k = 0; k < n_edges; ++k) {  // update_river_channel_flow! (:326-385)
+        const int64_t a = src[k], b = dst[k];
+        const double zs_src = zb[a] + h[a];
+        const double zs_dst = zb[b] + h[b];
+        const double zs_e = jmax(zs_src, zs_dst);
+        const double hf = zs_e - zb_e[k];
+        const double A = width_e[k] * hf;
+        const double R = A / (2.0 * hf + width_e[k]);
+        double qk = hf > h_thresh ? li_flow_area(q_prev[k], zs_src, zs_dst, hf, A, R, length_e[k], nsq_e[k],
+                                                 froude_limit != 0, dt)
+                                  : 0.0;
+        if (h[a] <= 0.0) qk = jmin(qk, 0.0);
+        if (h[b] <= 0.0) qk = jmax(qk, 0.0);
+        q[k] = qk;
+        q_cum[k] += qk * dt;
+    }
+    // update_water_depth_and_storage! (:723-760), edges into / out of each cell in edge order
+    std::vector<double> qin(n, 0.0), qout(n, 0.0);
+    for (int64_t k = 0; k < n_edges; ++k) {
+        qin[dst[k]] = qin[dst[k]] + q[k];
+        qout[src[k]] = qout[src[k]] + q[k];
+    }
+    for (int64_t i = 0; i < n_active; ++i) {
+        storage[i] += (qin[i] - qout[i] + inwater[i] - 0.0) * dt;
+        if (storage[i] < 0.0) storage[i] = 0.0;
+        storage[i] += 0.0 * dt;
+        h[i] = storage[i] / (flow_length[i] * flow_width[i]);
+    }
+}
+
+// stable_timestep of the local-inertial river (:1004-1020)
+double orc_li_stable_timestep(int64_t n, const double* flow_length, const double* h, double alpha) {
+    double dt_min = std::numeric_limits<double>::infinity();
+    for (int64_t i = 0; i < n; ++i) dt_min = jmin(alpha * flow_length[i] / std::sqrt(GRAVITY * h[i]), dt_min);
+    return std::isinf(dt_min) ? 60.0 : dt_min;
+}
+
+}  // extern "C"
+
 extern "C" {
 // Reservoir at a river node with discharge q after the node's kinematic-wave update.
 void orc_reservoir_update(OrcReservoir* r, double q, double dt) { update_reservoir_at_node(*r, q, dt); }

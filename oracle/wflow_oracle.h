@@ -135,6 +135,19 @@ void orc_lateral_snow_transport(const int32_t* ds, const int32_t* ups_ds, const 
                                 const double* slope, const double* snow_storage, const double* snow_water,
                                 double* snow_out, double* snow_in);
 
+/* local-inertial river flow on a staggered grid (surface_process.jl:88-163,
+ * surface_staggered_scheme.jl:326-385, 723-760, 1004-1020) */
+double orc_li_flow_area(double q0, double zs0, double zs1, double hf, double A, double R, double length,
+                        double mannings_n_sq, int32_t froude_limit, double dt);
+double orc_li_flow_rect(double theta, double q0, double qd, double qu, double zs0, double zs1, double hf,
+                        double width, double length, double mannings_n_sq, int32_t froude_limit, double dt);
+void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
+                       const double* zb, const double* flow_length, const double* flow_width, const double* inwater,
+                       const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
+                       double h_thresh, int32_t froude_limit, double dt, double* h, double* storage, double* q,
+                       double* q_prev, double* q_cum);
+double orc_li_stable_timestep(int64_t n, const double* flow_length, const double* h, double alpha);
+
 /* full model */
 typedef struct OrcModel OrcModel;
 int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p, OrcModel** out);

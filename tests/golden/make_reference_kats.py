@@ -319,6 +319,24 @@ def build():
                   dict(downstream=ds, order=list(range(6)), dt=dt_acc, material=[dt_acc * nums(R, 280)[0]] * 6,
                        capacity=nums(R, 281)),
                   dict(material=[dt_acc * v for v in nums(R, 284)], flux=nums(R, 285)), cmp="exact"))
+    # local-inertial flow (surface_process.jl:88-163), both cross-sections
+    K.append(case("local_inertial_flow_area", "local_inertial_flow_area", f"{R}:1320-1344",
+                  dict(q0=num(R, 1322), zs0=num(R, 1323), zs1=num(R, 1324), hf=num(R, 1325), A=num(R, 1326),
+                       R=num(R, 1327), length=num(R, 1328), mannings_n_sq=num(R, 1329), froude_limit=1,
+                       dt=num(R, 1331)),
+                  dict(q=num(R, 1344))))
+    K.append(case("local_inertial_flow_rect", "local_inertial_flow_rect", f"{R}:1346-1373",
+                  dict(theta=num(R, 1347), q0=num(R, 1348), qd=num(R, 1349), qu=num(R, 1350), zs0=num(R, 1351),
+                       zs1=num(R, 1352), hf=num(R, 1353), width=num(R, 1354), length=num(R, 1355),
+                       mannings_n_sq=num(R, 1356), froude_limit=1, dt=num(R, 1358)),
+                  dict(q=num(R, 1373))))
+    # the long channel of MacDonald (1997) run to steady state with the local-inertial river
+    K.append(case("local_inertial_macdonald", "local_inertial_macdonald", f"{R}:1189-1318",
+                  dict(L=num(R, 1195), dx=num(R, 1196), width=nums(R, 1225)[0], mannings_n=nums(R, 1226)[0],
+                       h_thresh=num(R, 1265), alpha=num(R, 1270), epsilon=num(R, 1303), inflow=num(R, 1306)),
+                  dict(mean_abs_error=num(R, 1317)),
+                  note="bed levels integrate the analytical slope (the test's quadgk, rtol 1e-12); "
+                       "the analytical depth profile is MacDonald's (1997), restated from lines 1199-1211"))
     # ------------------------------------------------------------------------ utils.jl
     K.append(case("scurve", "scurve", f"{U}:66-77",
                   dict(x=num(U, 71), a=num(U, 67), b=num(U, 68), c=num(U, 69)), dict(s=num(U, 73))))

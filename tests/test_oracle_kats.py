@@ -153,6 +153,19 @@ def run_case(c, prev):
                                      material.ctypes.data_as(C.POINTER(C.c_double)),
                                      flux.ctypes.data_as(C.POINTER(C.c_double)))
         return dict(material=material, flux=flux)
+    if fn in ("local_inertial_flow_area", "local_inertial_flow_rect"):
+        import ctypes as C
+        L = O.lib()
+        f = getattr(L, "orc_li_flow_area" if fn.endswith("area") else "orc_li_flow_rect")
+        f.restype = C.c_double
+        keys = (["q0", "zs0", "zs1", "hf", "A", "R", "length", "mannings_n_sq", "froude_limit", "dt"]
+                if fn.endswith("area") else
+                ["theta", "q0", "qd", "qu", "zs0", "zs1", "hf", "width", "length", "mannings_n_sq", "froude_limit",
+                 "dt"])
+        vals = [C.c_int32(int(a[k])) if k == "froude_limit" else C.c_double(a[k]) for k in keys]
+        return dict(q=f(*vals))
+    if fn == "local_inertial_macdonald":
+        return dict(mean_abs_error=macdonald(a))
     if fn == "kinwave_river_update":
         import ctypes as C
         q = np.array(a["q"])
@@ -175,8 +188,61 @@ def run_case(c, prev):
     raise KeyError(fn)
 
 
+def macdonald(a):
+    """The long-channel case of MacDonald (1997): 1D local-inertial river to steady state
+    (routing_process.jl:1189-1318). Bed levels integrate the analytical channel slope from each
+    cell to the channel's end; depths start dry with the analytical depth at the last cell (a
+    boundary); the upstream cell receives a constant inflow; the run stops when the mean depth
+    changes by at most epsilon in a step."""
+    import ctypes as C
+    quad = pytest.importorskip("scipy.integrate").quad
+    g = 9.80665
+    Lc, dx = a["L"], a["dx"]
+    n = int(Lc / dx)
+
+    def h(x):  # MacDonald's depth profile for a 10 m wide channel, n = 0.03, Q = 20 m3/s
+        return np.cbrt(4 / g) * (1.0 + 0.5 * np.exp(-16.0 * (x / Lc - 0.5) ** 2))
+
+    def dh(x):
+        return -np.cbrt(4 / g) * 16.0 / Lc * (x / Lc - 0.5) * np.exp(-16 * (x / Lc - 0.5) ** 2)
+
+    def slope(x):
+        return (1.0 - 4.0 / (g * h(x) ** 3)) * dh(x) + 0.36 * (2 * h(x) + 10.0) ** (4.0 / 3.0) / (
+            (10.0 * h(x)) ** (10.0 / 3.0))
+
+    x = np.arange(1, n + 1) * dx
+    h_a = h(x)
+    zb = np.array([quad(slope, xi, Lc, epsrel=1e-12, epsabs=0.0)[0] for xi in x])
+    src = np.arange(n - 1, dtype=np.int64)
+    dst = src + 1
+    dl, width, nr = np.full(n, dx), np.full(n, a["width"]), np.full(n, a["mannings_n"])
+    zb_e = np.maximum(zb[src], zb[dst])
+    w_e = np.minimum(width[dst], width[src])
+    l_e = 0.5 * (dl[dst] + dl[src])
+    n_e = (nr[dst] * dl[dst] + nr[src] * dl[src]) / (dl[dst] + dl[src])
+    nsq_e = n_e * n_e
+    hh = np.zeros(n)
+    hh[-1] = h_a[-1]
+    st, inw = np.zeros(n), np.zeros(n)
+    q, qp, qc = np.zeros(n - 1), np.zeros(n - 1), np.zeros(n - 1)
+    L = O.lib()
+    pd = lambda v: v.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    pl = lambda v: v.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
+    L.orc_li_stable_timestep.restype = C.c_double
+    fixed = [C.c_int64(n), C.c_int64(n - 1), C.c_int64(n - 1), pl(src), pl(dst), pd(zb), pd(dl), pd(width), pd(inw),
+             pd(zb_e), pd(w_e), pd(l_e), pd(nsq_e), C.c_double(a["h_thresh"]), C.c_int32(1)]
+    for _ in range(1_000_000):
+        inw[0] = a["inflow"]
+        h0 = hh.mean()
+        dt = L.orc_li_stable_timestep(C.c_int64(n), pd(dl), pd(hh), C.c_double(a["alpha"]))
+        L.orc_li_river_step(*fixed, C.c_double(dt), pd(hh), pd(st), pd(q), pd(qp), pd(qc))
+        if abs(h0 - hh.mean()) <= a["epsilon"]:
+            break
+    return float(np.mean(np.abs(hh - h_a)))
+
+
 def test_fixture_is_complete():
-    assert len(KATS["cases"]) >= 61
+    assert len(KATS["cases"]) >= 64
     for c in KATS["cases"]:
         assert ".jl:" in c["src"]
 
