@@ -1894,6 +1894,137 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
     }
 }
 
+// ---- 2D overland local-inertial flow with a subgrid river (surface_staggered_scheme.jl
+// :1022-1040, 1202-1265, 1322-1546). Index arrays are 0-based; index n is the ghost cell
+// outside the grid (discharge arrays hold n + 1 values, the ghost's staying 0).
+
+// stable_timestep of the overland flow: cells without a river (:1022-1040)
+double orc_li_land_stable_timestep(int64_t n, const double* x_length, const double* y_length,
+                                   const int32_t* river_location, const double* h, double alpha) {
+    double dt_min = std::numeric_limits<double>::infinity();
+    for (int64_t i = 0; i < n; ++i) {
+        const double dt = river_location[i] == 0 ? alpha * jmin(x_length[i], y_length[i]) / std::sqrt(GRAVITY * h[i])
+                                                 : std::numeric_limits<double>::infinity();
+        dt_min = jmin(dt, dt_min);
+    }
+    return std::isinf(dt_min) ? 60.0 : dt_min;
+}
+
+// update_directional_flow! at cell i for one direction (:1202-1265): up / down are the
+// direction's upstream and downstream neighbour indices, width_e / zmax_e / nsq_e the edge
+// arrays, length the cell lengths along the direction.
+void orc_li_directional_flow(int64_t i, int64_t n, const int64_t* up, const int64_t* down, const double* width_e,
+                             const double* zmax_e, const double* length, const double* z, const double* h,
+                             const double* nsq_e, double theta, double h_thresh, int32_t froude_limit, double dt,
+                             double* q, const double* q_prev, double* q_cum) {
+    const int64_t u = up[i];
+    if (!(u < n && width_e[i] != 0.0)) return;
+    const double zs_current = z[i] + h[i];
+    const double zs_upstream = z[u] + h[u];
+    const double zs_max = jmax(zs_current, zs_upstream);
+    const double hf = zs_max - zmax_e[i];
+    if (hf > h_thresh) {
+        const double length_e = 0.5 * (length[i] + length[u]);
+        double qi = li_flow_rect(theta, q_prev[i], q_prev[down[i]], q_prev[u], zs_current, zs_upstream, hf,
+                                 width_e[i], length_e, nsq_e[i], froude_limit != 0, dt);
+        if (h[i] <= 0.0) qi = jmin(qi, 0.0);
+        if (h[u] <= 0.0) qi = jmax(qi, 0.0);
+        q[i] = qi;
+    } else {
+        q[i] = 0.0;
+    }
+    q_cum[i] += q[i] * dt;
+}
+
+// compute_land_storage_change (:1420-1433)
+double orc_li_land_storage_change(int64_t i, const double* qx, const double* qy, const int64_t* ind_x_down,
+                                  const int64_t* ind_y_down, const double* runoff, double dt) {
+    return (qx[ind_x_down[i]] - qx[i] + qy[ind_y_down[i]] - qy[i] + runoff[i]) * dt;
+}
+
+// compute_river_storage_change at a cell holding river cell r (:1322-1351): river discharge of
+// the edges into and out of r, overland fluxes, runoff and abstraction
+double orc_li_river_storage_change(int64_t i, const double* q_river, const int64_t* e_in, int64_t n_in,
+                                   const int64_t* e_out, int64_t n_out, const double* qx, const double* qy,
+                                   const int64_t* ind_x_down, const int64_t* ind_y_down, const double* runoff,
+                                   double abstraction, double dt) {
+    double s_in = 0.0, s_out = 0.0;
+    for (int64_t k = 0; k < n_in; ++k) s_in = s_in + q_river[e_in[k]];
+    for (int64_t k = 0; k < n_out; ++k) s_out = s_out + q_river[e_out[k]];
+    const double net_river_flow = s_in - s_out;
+    const double net_land_flow = qx[ind_x_down[i]] - qx[i] + qy[ind_y_down[i]] - qy[i];
+    const double net_flow = net_river_flow + net_land_flow + runoff[i] - abstraction;
+    return net_flow * dt;
+}
+
+// compute_external_inflow (:1358-1380): out2 = inflow, abstraction
+void orc_li_external_inflow(double external_inflow, double land_storage, double bankfull_storage,
+                            double river_storage, double dt, double* out2) {
+    if (external_inflow < 0.0) {
+        const double available = land_storage >= bankfull_storage ? bankfull_storage : river_storage;
+        const double a = jmin(-external_inflow, available / dt * 0.80);
+        out2[0] = -a;
+        out2[1] = a;
+    } else {
+        out2[0] = external_inflow;
+        out2[1] = 0.0;
+    }
+}
+
+// compute_water_depths (:1386-1414): out3 = river depth, land depth, river storage
+void orc_li_water_depths(double total_storage, double bankfull_storage, double bankfull_depth, double x_length,
+                         double y_length, double river_length, double river_width, double* out3) {
+    if (total_storage >= bankfull_storage) {
+        const double river_h = bankfull_depth + (total_storage - bankfull_storage) / (x_length * y_length);
+        out3[0] = river_h;
+        out3[1] = river_h - bankfull_depth;
+        out3[2] = river_h * river_length * river_width;
+    } else {
+        out3[0] = total_storage / (river_length * river_width);
+        out3[1] = 0.0;
+        out3[2] = total_storage;
+    }
+}
+
+// update_land_storage_and_depth! (:1481-1503)
+void orc_li_update_land_cell(int64_t i, const double* qx, const double* qy, const int64_t* ind_x_down,
+                             const int64_t* ind_y_down, const double* runoff, const double* x_length,
+                             const double* y_length, double dt, double* storage, double* error, double* h) {
+    storage[i] += orc_li_land_storage_change(i, qx, qy, ind_x_down, ind_y_down, runoff, dt);
+    if (storage[i] < 0.0) {
+        error[i] += std::fabs(storage[i]);
+        storage[i] = 0.0;
+    }
+    h[i] = storage[i] / (x_length[i] * y_length[i]);
+}
+
+// update_river_and_land_storage_and_depth! (:1440-1476) at cell i holding river cell r
+void orc_li_update_river_cell(int64_t i, const double* q_river, const int64_t* e_in, int64_t n_in,
+                              const int64_t* e_out, int64_t n_out, const double* qx, const double* qy,
+                              const int64_t* ind_x_down, const int64_t* ind_y_down, const double* runoff,
+                              double abstraction, double external_inflow, double bankfull_storage,
+                              double bankfull_depth, const double* x_length, const double* y_length,
+                              double river_length, double river_width, double dt, double* storage, double* error,
+                              double* h_land, double* h_river, double* storage_river,
+                              double* abstraction_cumulative) {
+    storage[i] += orc_li_river_storage_change(i, q_river, e_in, n_in, e_out, n_out, qx, qy, ind_x_down, ind_y_down,
+                                              runoff, abstraction, dt);
+    if (storage[i] < 0.0) {
+        error[i] += std::fabs(storage[i]);
+        storage[i] = 0.0;
+    }
+    double io[2];
+    orc_li_external_inflow(external_inflow, storage[i], bankfull_storage, *storage_river, dt, io);
+    storage[i] += io[0] * dt;
+    *abstraction_cumulative += io[1] * dt;
+    double d[3];
+    orc_li_water_depths(storage[i], bankfull_storage, bankfull_depth, x_length[i], y_length[i], river_length,
+                        river_width, d);
+    *h_river = d[0];
+    h_land[i] = d[1];
+    *storage_river = d[2];
+}
+
 // stable_timestep of the local-inertial river (:1004-1020)
 double orc_li_stable_timestep(int64_t n, const double* flow_length, const double* h, double alpha) {
     double dt_min = std::numeric_limits<double>::infinity();

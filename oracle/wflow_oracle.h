@@ -147,6 +147,35 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
                        double h_thresh, int32_t froude_limit, double dt, double* h, double* storage, double* q,
                        double* q_prev, double* q_cum);
 double orc_li_stable_timestep(int64_t n, const double* flow_length, const double* h, double alpha);
+/* 2D overland local-inertial flow with a subgrid river (surface_staggered_scheme.jl:1022-1040,
+ * 1202-1265, 1322-1546); 0-based indices, index n = the ghost cell outside the grid */
+double orc_li_land_stable_timestep(int64_t n, const double* x_length, const double* y_length,
+                                   const int32_t* river_location, const double* h, double alpha);
+void orc_li_directional_flow(int64_t i, int64_t n, const int64_t* up, const int64_t* down, const double* width_e,
+                             const double* zmax_e, const double* length, const double* z, const double* h,
+                             const double* nsq_e, double theta, double h_thresh, int32_t froude_limit, double dt,
+                             double* q, const double* q_prev, double* q_cum);
+double orc_li_land_storage_change(int64_t i, const double* qx, const double* qy, const int64_t* ind_x_down,
+                                  const int64_t* ind_y_down, const double* runoff, double dt);
+double orc_li_river_storage_change(int64_t i, const double* q_river, const int64_t* e_in, int64_t n_in,
+                                   const int64_t* e_out, int64_t n_out, const double* qx, const double* qy,
+                                   const int64_t* ind_x_down, const int64_t* ind_y_down, const double* runoff,
+                                   double abstraction, double dt);
+void orc_li_external_inflow(double external_inflow, double land_storage, double bankfull_storage,
+                            double river_storage, double dt, double* out2);
+void orc_li_water_depths(double total_storage, double bankfull_storage, double bankfull_depth, double x_length,
+                         double y_length, double river_length, double river_width, double* out3);
+void orc_li_update_land_cell(int64_t i, const double* qx, const double* qy, const int64_t* ind_x_down,
+                             const int64_t* ind_y_down, const double* runoff, const double* x_length,
+                             const double* y_length, double dt, double* storage, double* error, double* h);
+void orc_li_update_river_cell(int64_t i, const double* q_river, const int64_t* e_in, int64_t n_in,
+                              const int64_t* e_out, int64_t n_out, const double* qx, const double* qy,
+                              const int64_t* ind_x_down, const int64_t* ind_y_down, const double* runoff,
+                              double abstraction, double external_inflow, double bankfull_storage,
+                              double bankfull_depth, const double* x_length, const double* y_length,
+                              double river_length, double river_width, double dt, double* storage, double* error,
+                              double* h_land, double* h_river, double* storage_river,
+                              double* abstraction_cumulative);
 
 /* full model */
 typedef struct OrcModel OrcModel;

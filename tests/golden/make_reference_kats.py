@@ -330,6 +330,25 @@ def build():
                        zs1=num(R, 1352), hf=num(R, 1353), width=num(R, 1354), length=num(R, 1355),
                        mannings_n_sq=num(R, 1356), froude_limit=1, dt=num(R, 1358)),
                   dict(q=num(R, 1373))))
+    # 2D overland local-inertial flow at an edge, and the water depth update of land and river
+    # cells (1-based index lists as in the reference's test)
+    K.append(case("li_directional_flow", "li_directional_flow", f"{R}:989-1048",
+                  dict(i=int(num(R, 1040)), ywidth_e=nums(R, 1002), zx_max_e=nums(R, 1004), theta=num(R, 1005),
+                       h_thresh=num(R, 1006), nsq_e=span(R, 1009, 1011), z=nums(R, 1013), qx=nums(R, 1019),
+                       h=nums(R, 1020), ind_x_up=nums(R, 1029), ind_x_down=nums(R, 1030), x_length=nums(R, 1034),
+                       y_length=nums(R, 1035), river_location=nums(R, 1036), alpha=num(R, 995)),
+                  dict(dt=num(R, 1044), qx_i=num(R, 1047))))
+    K.append(case("li_water_depth", "li_water_depth", f"{R}:1050-1187",
+                  dict(qx=nums(R, 1060), qy=nums(R, 1061), storage=nums(R, 1062), h=nums(R, 1063),
+                       runoff=nums(R, 1067), bankfull_storage=nums(R, 1096)[0], bankfull_depth=nums(R, 1097)[0],
+                       q_river=nums(R, 1106), h_river=nums(R, 1109)[0], storage_river=nums(R, 1110)[0],
+                       ind_x_down=nums(R, 1121), ind_y_down=nums(R, 1122), x_length=nums(R, 1126),
+                       y_length=nums(R, 1127), river_width=nums(R, 1135)[0], river_length=nums(R, 1136)[0],
+                       alpha=num(R, 1085)),
+                  dict(dt=num(R, 1142), storage_change=num(R, 1152), external_inflow=[0.0, 0.0],
+                       depths=[num(R, 1156), num(R, 1157), num(R, 1158)], land_storage_change=num(R, 1181),
+                       land_storage=num(R, 1185), land_h=num(R, 1186)),
+                  note="river cell 1 sits on land cell 3 with river edge 1 in and edge 2 out"))
     # the long channel of MacDonald (1997) run to steady state with the local-inertial river
     K.append(case("local_inertial_macdonald", "local_inertial_macdonald", f"{R}:1189-1318",
                   dict(L=num(R, 1195), dx=num(R, 1196), width=nums(R, 1225)[0], mannings_n=nums(R, 1226)[0],

@@ -164,6 +164,72 @@ def run_case(c, prev):
                  "dt"])
         vals = [C.c_int32(int(a[k])) if k == "froude_limit" else C.c_double(a[k]) for k in keys]
         return dict(q=f(*vals))
+    if fn == "li_directional_flow":
+        import ctypes as C
+        L = O.lib()
+        pd = lambda v: v.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        pl = lambda v: v.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
+        n = len(a["h"])
+        f = {k: np.asarray(a[k], float) for k in ("ywidth_e", "zx_max_e", "nsq_e", "z", "qx", "h", "x_length",
+                                                  "y_length")}
+        up = np.asarray(a["ind_x_up"], np.int64) - 1
+        down = np.asarray(a["ind_x_down"], np.int64) - 1
+        rl = np.asarray(a["river_location"], np.int32)
+        L.orc_li_land_stable_timestep.restype = C.c_double
+        dt = L.orc_li_land_stable_timestep(C.c_int64(n), pd(f["x_length"]), pd(f["y_length"]),
+                                           rl.ctypes.data_as(C.POINTER(C.c_int32)), pd(f["h"]), C.c_double(a["alpha"]))
+        qx = f["qx"].copy()
+        qx0 = qx.copy()  # the test sets qx0 .= qx before the update
+        qcum = np.zeros_like(qx)
+        L.orc_li_directional_flow(C.c_int64(a["i"] - 1), C.c_int64(n), pl(up), pl(down), pd(f["ywidth_e"]),
+                                  pd(f["zx_max_e"]), pd(f["x_length"]), pd(f["z"]), pd(f["h"]), pd(f["nsq_e"]),
+                                  C.c_double(a["theta"]), C.c_double(a["h_thresh"]), C.c_int32(1), C.c_double(dt),
+                                  pd(qx), pd(qx0), pd(qcum))
+        return dict(dt=dt, qx_i=qx[a["i"] - 1])
+    if fn == "li_water_depth":
+        import ctypes as C
+        L = O.lib()
+        pd = lambda v: v.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        pl = lambda v: v.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
+        f = {k: np.asarray(a[k], float).copy() for k in ("qx", "qy", "storage", "h", "runoff", "q_river", "x_length",
+                                                         "y_length")}
+        xd = np.asarray(a["ind_x_down"], np.int64) - 1
+        yd = np.asarray(a["ind_y_down"], np.int64) - 1
+        e_in, e_out = np.array([0], np.int64), np.array([1], np.int64)
+        L.orc_li_stable_timestep.restype = C.c_double
+        rlen, rh = np.array([a["river_length"]]), np.array([a["h_river"]])
+        dt = L.orc_li_stable_timestep(C.c_int64(1), pd(rlen), pd(rh), C.c_double(a["alpha"]))
+        L.orc_li_river_storage_change.restype = C.c_double
+        i = 2  # land cell 3 holds river cell 1
+        change = L.orc_li_river_storage_change(C.c_int64(i), pd(f["q_river"]), pl(e_in), C.c_int64(1), pl(e_out),
+                                               C.c_int64(1), pd(f["qx"]), pd(f["qy"]), pl(xd), pl(yd),
+                                               pd(f["runoff"]), C.c_double(0.0), C.c_double(dt))
+        io = (C.c_double * 2)()
+        L.orc_li_external_inflow(C.c_double(0.0), C.c_double(f["storage"][i]), C.c_double(a["bankfull_storage"]),
+                                 C.c_double(a["storage_river"]), C.c_double(dt), io)
+        dep = (C.c_double * 3)()
+        L.orc_li_water_depths(C.c_double(f["storage"][i] + change), C.c_double(a["bankfull_storage"]),
+                              C.c_double(a["bankfull_depth"]), C.c_double(f["x_length"][i]),
+                              C.c_double(f["y_length"][i]), C.c_double(a["river_length"]),
+                              C.c_double(a["river_width"]), dep)
+        err = np.zeros(3)
+        h_river, st_river, abs_cum = C.c_double(a["h_river"]), C.c_double(a["storage_river"]), C.c_double(0.0)
+        L.orc_li_update_river_cell(C.c_int64(i), pd(f["q_river"]), pl(e_in), C.c_int64(1), pl(e_out), C.c_int64(1),
+                                   pd(f["qx"]), pd(f["qy"]), pl(xd), pl(yd), pd(f["runoff"]), C.c_double(0.0),
+                                   C.c_double(0.0), C.c_double(a["bankfull_storage"]), C.c_double(a["bankfull_depth"]),
+                                   pd(f["x_length"]), pd(f["y_length"]), C.c_double(a["river_length"]),
+                                   C.c_double(a["river_width"]), C.c_double(dt), pd(f["storage"]), pd(err), pd(f["h"]),
+                                   C.byref(h_river), C.byref(st_river), C.byref(abs_cum))
+        # the composite update gives the depths of compute_water_depths (the test asserts both)
+        assert [h_river.value, f["h"][i], st_river.value] == list(dep)
+        L.orc_li_land_storage_change.restype = C.c_double
+        land_change = L.orc_li_land_storage_change(C.c_int64(1), pd(f["qx"]), pd(f["qy"]), pl(xd), pl(yd),
+                                                   pd(f["runoff"]), C.c_double(dt))
+        L.orc_li_update_land_cell(C.c_int64(1), pd(f["qx"]), pd(f["qy"]), pl(xd), pl(yd), pd(f["runoff"]),
+                                  pd(f["x_length"]), pd(f["y_length"]), C.c_double(dt), pd(f["storage"]), pd(err),
+                                  pd(f["h"]))
+        return dict(dt=dt, storage_change=change, external_inflow=list(io), depths=list(dep),
+                    land_storage_change=land_change, land_storage=f["storage"][1], land_h=f["h"][1])
     if fn == "local_inertial_macdonald":
         return dict(mean_abs_error=macdonald(a))
     if fn == "kinwave_river_update":
@@ -242,7 +308,7 @@ def macdonald(a):
 
 
 def test_fixture_is_complete():
-    assert len(KATS["cases"]) >= 64
+    assert len(KATS["cases"]) >= 66
     for c in KATS["cases"]:
         assert ".jl:" in c["src"]
 
