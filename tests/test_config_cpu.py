@@ -7,7 +7,6 @@ The TOML here follows the reference's schema (Wflow/src/config_structure.jl): do
 up from it runs like the model built from the arrays the files were written from.
 """
 
-import datetime as dt
 
 import numpy as np
 import pytest

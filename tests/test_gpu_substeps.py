@@ -21,7 +21,7 @@ import pytest
 from wflow_gb300 import abi, synthetic
 from wflow_gb300.model import Model
 import oracle_py as O
-from test_gpu_parity import LAND, RIVER, RTOL, assert_parity, compare, split_errors
+from test_gpu_parity import LAND, RIVER, assert_parity, compare, split_errors
 
 pytestmark = pytest.mark.gpu
 

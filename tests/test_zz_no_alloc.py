@@ -4,7 +4,6 @@ This file is collected last on purpose: it must pass after every other test (the
 scratch keeps the contents of earlier calls) as well as alone in a fresh process (the first
 call on the device looks the scratch address up).
 """
-import ctypes as C
 
 import numpy as np
 import pytest

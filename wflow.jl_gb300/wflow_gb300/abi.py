@@ -6,7 +6,6 @@ synthetic-input library (`_build/libwflow_synth.so`) are built in-tree by
 """
 
 import ctypes as C
-import os
 from pathlib import Path
 
 PKG_ROOT = Path(__file__).resolve().parent.parent          # .../wflow.jl_gb300
