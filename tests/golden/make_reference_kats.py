@@ -357,6 +357,18 @@ def build():
                   note="bed levels integrate the analytical slope (the test's quadgk, rtol 1e-12); "
                        "the analytical depth profile is MacDonald's (1997), restated from lines 1199-1211"))
     # ------------------------------------------------------------------------ utils.jl
+    # units (the file helpers' conversions) and the affine transform of [input] entries
+    K.append(case("units_absolute_degrees", "to_si", f"{U}:40-45", dict(value=0.0, unit="degC"),
+                  dict(si=num(U, 44)), cmp="exact"))
+    K.append(case("units_per_step", "to_si_factor_per_step", f"{U}:51-54", dict(dt=num(U, 51)),
+                  dict(factor=1.0 / num(U, 51)), cmp="exact",
+                  note="to_SI_factor(Unit(m = 1, dt = -1); dt_val = dt) == inv(dt)"))
+    v = nums(U, 294)
+    K.append(case("affine_scale", "affine", f"{U}:291-296", dict(v=v, scale=nums(U, 296)[:1]),
+                  dict(out=[nums(U, 296)[0] * x for x in v]), cmp="exact"))
+    K.append(case("affine_scale_offset", "affine", f"{U}:291-305", dict(v=v, scale=[6.0], offset=[7.0] * 3),
+                  dict(out=[6.0 * x + 7.0 for x in v]), cmp="exact",
+                  note="scale = [6.0], offset = fill(7.0, 3) (utils.jl:301-304)"))
     K.append(case("scurve", "scurve", f"{U}:66-77",
                   dict(x=num(U, 71), a=num(U, 67), b=num(U, 68), c=num(U, 69)), dict(s=num(U, 73))))
     K.append(case("mass_balance_zero", "compute_mass_balance_error", f"{U}:105-112",

@@ -230,6 +230,16 @@ def run_case(c, prev):
                                   pd(f["h"]))
         return dict(dt=dt, storage_change=change, external_inflow=list(io), depths=list(dep),
                     land_storage_change=land_change, land_storage=f["storage"][1], land_h=f["h"][1])
+    if fn == "to_si":
+        from wflow_gb300 import states
+        return dict(si=states.to_si(a["value"], a["unit"]))
+    if fn == "to_si_factor_per_step":
+        from wflow_gb300 import forcing
+        return dict(factor=forcing.to_si_factor_per_step(a["dt"], length_factor=1.0))  # Unit(m = 1, dt = -1)
+    if fn == "affine":
+        from wflow_gb300 import staticmaps
+        return dict(out=list(staticmaps.apply_affine_transform(np.asarray(a["v"]), a.get("scale", [1.0]),
+                                                               a.get("offset", [0.0]))))
     if fn == "local_inertial_macdonald":
         return dict(mean_abs_error=macdonald(a))
     if fn == "kinwave_river_update":
@@ -308,7 +318,7 @@ def macdonald(a):
 
 
 def test_fixture_is_complete():
-    assert len(KATS["cases"]) >= 66
+    assert len(KATS["cases"]) >= 70
     for c in KATS["cases"]:
         assert ".jl:" in c["src"]
 

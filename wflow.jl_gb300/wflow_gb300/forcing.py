@@ -26,6 +26,12 @@ _UNIT_SECONDS = {"second": 1.0, "seconds": 1.0, "s": 1.0, "minute": 60.0, "minut
                  "hours": 3600.0, "h": 3600.0, "day": 86400.0, "days": 86400.0, "d": 86400.0}
 
 
+def to_si_factor_per_step(dt, length_factor=1e-3):
+    """Factor of a unit "length per model step" to SI (units.jl:256-269): the length's factor
+    times dt^-1 (mm per step by default)."""
+    return length_factor * (1.0 / float(dt))
+
+
 def parse_time_units(units):
     """CF time units "<unit> since <date>[ <time>]" -> (seconds per unit, epoch datetime)."""
     m = re.match(r"\s*(\w+)\s+since\s+(\d{1,4})-(\d{1,2})-(\d{1,2})(?:[ T](\d{1,2}):(\d{1,2})(?::(\d{1,2}(?:\.\d*)?))?)?",
@@ -100,8 +106,8 @@ class ForcingFile:
         """(P, PET, T) in SI on the land cells for the step ending at model time t, and with
         reservoirs the reservoirs' precipitation and evaporation (both [m s-1])."""
         i = self.index(t)
-        # Unit(mm = 1, dt = -1): 1e-3 * dt^-1 (units.jl:256-269)
-        to_si = {PRECIP: 1e-3 * (1.0 / self.dt), PET: 1e-3 * (1.0 / self.dt)}
+        f = to_si_factor_per_step(self.dt)  # Unit(mm = 1, dt = -1)
+        to_si = {PRECIP: f, PET: f}
         out, res_out = {}, {}
         for sn in (PRECIP, PET, TEMP):
             g = self._grid_at(sn, i)
@@ -145,7 +151,7 @@ def write_forcing(path, grid, times, precip, pet, temp, dt, time_units="days sin
     nc.write("y", grid.yc)
     nc.write("time", np.array([(t - epoch).total_seconds() / scale for t in times]))
     for k in range(len(times)):
-        f = 1e-3 * (1.0 / dt)
+        f = to_si_factor_per_step(dt)
         for sn, arr, conv in ((PRECIP, precip, lambda v: v / f), (PET, pet, lambda v: v / f),
                               (TEMP, temp, lambda v: v - 273.15)):
             buf = np.full((grid.ny, grid.nx), np.nan)

@@ -88,6 +88,24 @@ def lattometres(lat):
     return longlen, latlen
 
 
+def apply_affine_transform(a, scale=1.0, offset=0.0):
+    """a * scale + offset as apply_affine_transform! does (utils.jl:239-256): the scaling only
+    when a scale differs from 1, the offset only when one differs from 0; a vector of several
+    scales or offsets applies along the first axis (the layers of a layered map)."""
+    a = np.asarray(a, float)
+    scale = np.asarray(scale, float)
+    offset = np.asarray(offset, float)
+    if scale.ndim:
+        scale = scale.reshape((-1,) + (1,) * (a.ndim - 1)) if scale.size > 1 else scale.reshape(())
+    if offset.ndim:
+        offset = offset.reshape((-1,) + (1,) * (a.ndim - 1)) if offset.size > 1 else offset.reshape(())
+    if np.any(scale != 1.0):
+        a = a * scale
+    if np.any(offset != 0.0):
+        a = a + offset
+    return a
+
+
 class _Maps:
     """Variables of a static-map file on the standardised grid, by standard name."""
 
@@ -137,17 +155,7 @@ class _Maps:
                 raise KeyError(f"static map `{sn}` not found")
             return np.full(((n_layers,) if layered else ()) + shape, float(default))
         a = self._standardise(m, self.nc.read(m))
-        scale = np.asarray(e.get("scale", 1.0), float)
-        offset = np.asarray(e.get("offset", 0.0), float)
-        if scale.ndim:  # per-layer vectors
-            scale = scale.reshape((-1,) + (1,) * (a.ndim - 1)) if scale.size > 1 else scale.reshape(())
-        if offset.ndim:
-            offset = offset.reshape((-1,) + (1,) * (a.ndim - 1)) if offset.size > 1 else offset.reshape(())
-        if np.any(scale != 1.0):
-            a = a * scale
-        if np.any(offset != 0.0):
-            a = a + offset
-        return a
+        return apply_affine_transform(a, e.get("scale", 1.0), e.get("offset", 0.0))
 
     def _standardise(self, m, a):
         dims = list(self.vars[m][1])
