@@ -16,9 +16,12 @@ def lib():
     return abi.load_library()
 
 
-def test_header_symbols_exported(lib):
-    names = abi.header_symbols()
-    assert "wf_create" in names and "wf_step" in names
+@pytest.mark.parametrize("header,must", [("wflow_gb300.h", ("wf_create", "wf_step")),
+                                          ("wflow_gb300_nc.h", ("wf_nc_open", "wf_nc_get")),
+                                          ("wflow_gb300_li.h", ("wf_li_river_create", "wf_li_river_step"))])
+def test_header_symbols_exported(lib, header, must):
+    names = abi.header_symbols(header)
+    assert all(m in names for m in must)
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 

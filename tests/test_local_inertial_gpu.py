@@ -1,0 +1,148 @@
+"""The local-inertial river on the GPU (include/wflow_gb300_li.h) against the CPU oracle.
+
+The component runs Wflow's river_routing = "local_inertial" for a channel without floodplain:
+edge discharge from local_inertial_flow (routing/surface/surface_process.jl:88-115), cell
+storage and depth (surface_staggered_scheme.jl:326-385, 723-760), sub-steps of the stable time
+step (:1004-1020) inside a model step (update_river_flow_model!, :800-826). The arithmetic is
+FP64 in the oracle's order, so every field is held to relative 1e-9 (the drop-in bar); the
+sub-step counts must be equal. MacDonald's long channel (routing_process.jl:1189-1318) run on
+the GPU to steady state reproduces the reference's mean absolute depth error
+0.01873574206931199 within Julia's default isapprox tolerance (sqrt(eps)).
+
+The argument checks of wf_li_river_create run before any device call and are tested on CPU.
+"""
+
+import numpy as np
+import pytest
+
+from li_cases import OracleLi, macdonald_case, random_river
+
+FIELDS = ("h", "storage", "q", "q_cumulative", "q_average")
+ORACLE_ATTR = {"h": "h", "storage": "storage", "q": "q", "q_cumulative": "q_cum", "q_average": "q_avg"}
+
+
+def _river(net, **kw):
+    from wflow_gb300.li_river import LiRiver
+    return LiRiver(net["src"], net["dst"], net["zb"], net["flow_length"], net["flow_width"], net["h"], net["zb_e"],
+                   net["w_e"], net["l_e"], net["nsq_e"], net["n_active"], **kw)
+
+
+def _max_rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    if a.size == 0:
+        return 0.0
+    return float(np.max(np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-300)))
+
+
+def _assert_same(gpu, orc, tag):
+    for f in FIELDS:
+        g, o = gpu.get(f), getattr(orc, ORACLE_ATTR[f])
+        assert g.shape == o.shape, (tag, f)
+        assert _max_rel(g, o) <= 1e-9, (tag, f, _max_rel(g, o))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [0, 1])
+def test_random_river_steps(gpu_lib, seed):
+    """Three hourly model steps of a 3000-cell river tree with confluences, four outlets of
+    fixed depth, wet, dry and near-threshold starting depths and lateral inflow."""
+    net = random_river(seed)
+    gpu, orc = _river(net), OracleLi(net)
+    for m in (gpu, orc):
+        m.set_state(net["h"])
+        m.set_inwater(net["inwater"])
+    for step in range(3):
+        k_gpu, k_orc = gpu.step(3600.0), orc.step(3600.0)
+        assert k_gpu == k_orc, (seed, step, k_gpu, k_orc)
+        _assert_same(gpu, orc, (seed, step))
+    gpu.close()
+
+
+@pytest.mark.gpu
+def test_substeps_and_warm_discharge(gpu_lib):
+    """Explicit sub-steps from a warm state with discharge on the edges, and the stable time
+    step of each, without lateral inflow (the network drains and cells fall dry)."""
+    net = random_river(7, n_active=500, n_bound=2)
+    rng = np.random.default_rng(7)
+    q0 = rng.uniform(-2.0, 20.0, len(net["src"]))
+    gpu, orc = _river(net, h_thresh=1e-3, froude_limit=False, alpha=0.5), OracleLi(net, froude=False, alpha=0.5)
+    for m in (gpu, orc):
+        m.set_state(net["h"], q0)
+        m.set_inwater(np.zeros(net["n"]))
+    for s in range(40):
+        dt_g, dt_o = gpu.stable_timestep(), orc.stable_timestep()
+        assert _max_rel(dt_g, dt_o) <= 1e-12, (s, dt_g, dt_o)
+        gpu.substep(dt_o)
+        orc.substep(dt_o)
+    for f in ("h", "storage", "q", "q_cumulative"):
+        assert _max_rel(gpu.get(f), getattr(orc, ORACLE_ATTR[f])) <= 1e-9, f
+    gpu.close()
+
+
+@pytest.mark.gpu
+def test_dry_network_time_step(gpu_lib):
+    """Every cell dry: the stable time step is the 60 s default and a sub-step moves nothing."""
+    net = random_river(3, n_active=300, n_bound=2)
+    net = dict(net, h=np.zeros(net["n"]))
+    gpu = _river(net)
+    assert gpu.stable_timestep() == 60.0
+    gpu.substep(60.0)
+    for f in FIELDS[:4]:
+        assert not np.any(gpu.get(f)), f
+    gpu.close()
+
+
+@pytest.mark.gpu
+def test_macdonald_steady_state(gpu_lib):
+    pytest.importorskip("scipy.integrate")
+    a = dict(L=1000.0, dx=5.0, width=10.0, mannings_n=0.03, h_thresh=1e-3, alpha=0.7, epsilon=1e-12, inflow=20.0)
+    net, h_a = macdonald_case(a)
+    runs = {}
+    for name, m in (("gpu", _river(net, h_thresh=a["h_thresh"], alpha=a["alpha"])),
+                    ("oracle", OracleLi(net, h_thresh=a["h_thresh"], alpha=a["alpha"]))):
+        inw = np.zeros(net["n"])
+        inw[0] = a["inflow"]
+        m.set_inwater(inw)
+        h = np.array(net["h"], float)
+        for it in range(1_000_000):
+            h0 = h.mean()
+            m.substep(m.stable_timestep())
+            h = m.get("h") if name == "gpu" else m.h
+            if abs(h0 - h.mean()) <= a["epsilon"]:
+                break
+        runs[name] = (it, float(np.mean(np.abs(h - h_a))))
+    assert runs["gpu"][0] == runs["oracle"][0], runs
+    assert _max_rel(runs["gpu"][1], runs["oracle"][1]) <= 1e-9, runs
+    assert np.isclose(runs["gpu"][1], 0.01873574206931199, rtol=np.sqrt(np.finfo(float).eps), atol=0.0), runs
+
+
+def test_create_rejects_bad_networks():
+    """Argument checks of wf_li_river_create (no device call is reached)."""
+    from wflow_gb300 import abi, build
+    from wflow_gb300.li_river import LiRiver
+    build.build_all()
+    net = random_river(1, n_active=20, n_bound=1)
+
+    def make(**over):
+        t = dict(net, **over)
+        return LiRiver(t["src"], t["dst"], t["zb"], t["flow_length"], t["flow_width"], t["h"], t["zb_e"], t["w_e"],
+                       t["l_e"], t["nsq_e"], t.get("n_active", net["n_active"]), alpha=t.get("alpha", 0.7))
+
+    bad_dst = net["dst"].copy()
+    bad_dst[3] = net["n"]
+    with pytest.raises(RuntimeError, match=f"failed \\({abi.WF_ERR_INVALID}\\).*out of range"):
+        make(dst=bad_dst)
+    self_loop = net["dst"].copy()
+    self_loop[2] = net["src"][2]
+    with pytest.raises(RuntimeError, match="out of range"):
+        make(dst=self_loop)
+    fl = net["flow_length"].copy()
+    fl[0] = 0.0
+    with pytest.raises(RuntimeError, match="positive on active cells"):
+        make(flow_length=fl)
+    with pytest.raises(RuntimeError, match="sizes out of range"):
+        make(n_active=net["n"] + 1)
+    with pytest.raises(RuntimeError, match="alpha must be positive"):
+        make(alpha=0.0)
+    with pytest.raises(ValueError, match="zb_edge"):
+        make(zb_e=net["zb_e"][:-1])

@@ -266,55 +266,21 @@ def run_case(c, prev):
 
 def macdonald(a):
     """The long-channel case of MacDonald (1997): 1D local-inertial river to steady state
-    (routing_process.jl:1189-1318). Bed levels integrate the analytical channel slope from each
-    cell to the channel's end; depths start dry with the analytical depth at the last cell (a
-    boundary); the upstream cell receives a constant inflow; the run stops when the mean depth
-    changes by at most epsilon in a step."""
-    import ctypes as C
-    quad = pytest.importorskip("scipy.integrate").quad
-    g = 9.80665
-    Lc, dx = a["L"], a["dx"]
-    n = int(Lc / dx)
-
-    def h(x):  # MacDonald's depth profile for a 10 m wide channel, n = 0.03, Q = 20 m3/s
-        return np.cbrt(4 / g) * (1.0 + 0.5 * np.exp(-16.0 * (x / Lc - 0.5) ** 2))
-
-    def dh(x):
-        return -np.cbrt(4 / g) * 16.0 / Lc * (x / Lc - 0.5) * np.exp(-16 * (x / Lc - 0.5) ** 2)
-
-    def slope(x):
-        return (1.0 - 4.0 / (g * h(x) ** 3)) * dh(x) + 0.36 * (2 * h(x) + 10.0) ** (4.0 / 3.0) / (
-            (10.0 * h(x)) ** (10.0 / 3.0))
-
-    x = np.arange(1, n + 1) * dx
-    h_a = h(x)
-    zb = np.array([quad(slope, xi, Lc, epsrel=1e-12, epsabs=0.0)[0] for xi in x])
-    src = np.arange(n - 1, dtype=np.int64)
-    dst = src + 1
-    dl, width, nr = np.full(n, dx), np.full(n, a["width"]), np.full(n, a["mannings_n"])
-    zb_e = np.maximum(zb[src], zb[dst])
-    w_e = np.minimum(width[dst], width[src])
-    l_e = 0.5 * (dl[dst] + dl[src])
-    n_e = (nr[dst] * dl[dst] + nr[src] * dl[src]) / (dl[dst] + dl[src])
-    nsq_e = n_e * n_e
-    hh = np.zeros(n)
-    hh[-1] = h_a[-1]
-    st, inw = np.zeros(n), np.zeros(n)
-    q, qp, qc = np.zeros(n - 1), np.zeros(n - 1), np.zeros(n - 1)
-    L = O.lib()
-    pd = lambda v: v.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
-    pl = lambda v: v.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
-    L.orc_li_stable_timestep.restype = C.c_double
-    fixed = [C.c_int64(n), C.c_int64(n - 1), C.c_int64(n - 1), pl(src), pl(dst), pd(zb), pd(dl), pd(width), pd(inw),
-             pd(zb_e), pd(w_e), pd(l_e), pd(nsq_e), C.c_double(a["h_thresh"]), C.c_int32(1)]
+    (routing_process.jl:1189-1318). The upstream cell receives a constant inflow; the run stops
+    when the mean depth changes by at most epsilon in a step."""
+    pytest.importorskip("scipy.integrate")
+    from li_cases import OracleLi, macdonald_case
+    net, h_a = macdonald_case(a)
+    m = OracleLi(net, h_thresh=a["h_thresh"], froude=True, alpha=a["alpha"])
+    inw = np.zeros(net["n"])
     for _ in range(1_000_000):
         inw[0] = a["inflow"]
-        h0 = hh.mean()
-        dt = L.orc_li_stable_timestep(C.c_int64(n), pd(dl), pd(hh), C.c_double(a["alpha"]))
-        L.orc_li_river_step(*fixed, C.c_double(dt), pd(hh), pd(st), pd(q), pd(qp), pd(qc))
-        if abs(h0 - hh.mean()) <= a["epsilon"]:
+        m.set_inwater(inw)
+        h0 = m.h.mean()
+        m.substep(m.stable_timestep())
+        if abs(h0 - m.h.mean()) <= a["epsilon"]:
             break
-    return float(np.mean(np.abs(hh - h_a)))
+    return float(np.mean(np.abs(m.h - h_a)))
 
 
 def test_fixture_is_complete():

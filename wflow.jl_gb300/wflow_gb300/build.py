@@ -30,6 +30,7 @@ CUDA_UNITS = [
     ("kernels_fp64.cu", ["--fmad=false"]),
     ("kernels_split.cu", ["-prec-div=false"]),
     ("kernels_adaptive.cu", ["--fmad=false"]),
+    ("kernels_li.cu", ["--fmad=false"]),
 ]
 
 
