@@ -1,0 +1,96 @@
+"""The local-inertial river scheme's arithmetic (wflow.jl_gb300/csrc/li_scheme.cuh, the functions
+the GPU kernels call) built for the host and compared with the oracle, bit for bit.
+
+Random river trees with confluences, outlets of fixed depth, dry and near-threshold cells and
+lateral inflow over hourly model steps (update_river_flow_model!, surface_staggered_scheme.jl:
+800-826), and MacDonald's long channel (routing_process.jl:1189-1318) run to steady state with
+the reference's mean depth error 0.01873574206931199 within Julia's isapprox tolerance.
+"""
+
+import ctypes as C
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from li_cases import OracleLi, _pd, _pl, macdonald_case, random_river
+
+REPO = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    out = tmp_path_factory.mktemp("li_host") / "li_host.so"
+    subprocess.run([cxx, "-O2", "-ffp-contract=off", "-std=c++17", "-shared", "-fPIC",
+                    "-I", str(REPO / "wflow.jl_gb300" / "csrc"), "-I", str(REPO / "include"),
+                    str(REPO / "tests" / "li_host_driver.cpp"), "-o", str(out)], check=True)
+    lib = C.CDLL(str(out))
+    lib.host_li_stable_timestep.restype = C.c_double
+    return lib
+
+
+class HostLi(OracleLi):
+    """OracleLi's driver over the host build of the product's scheme functions."""
+
+    def __init__(self, lib, net, **kw):
+        super().__init__(net, **kw)
+        self.H = lib
+
+    def stable_timestep(self):
+        return self.H.host_li_stable_timestep(C.c_int64(self.n), _pd(self.net["flow_length"]), _pd(self.h),
+                                              C.c_double(self.alpha))
+
+    def substep(self, dt):
+        t = self.net
+        self.H.host_li_substep(C.c_int64(self.n), C.c_int64(self.na), C.c_int64(self.ne), _pl(t["src"]), _pl(t["dst"]),
+                               _pd(t["zb"]), _pd(t["flow_length"]), _pd(t["flow_width"]), _pd(self.inwater),
+                               _pd(t["zb_e"]), _pd(t["w_e"]), _pd(t["l_e"]), _pd(t["nsq_e"]),
+                               C.c_double(self.h_thresh), C.c_int32(int(self.froude)), C.c_double(dt), _pd(self.h),
+                               _pd(self.storage), _pd(self.q), _pd(self.q_prev), _pd(self.q_cum))
+
+
+@pytest.mark.parametrize("seed,froude,alpha", [(0, True, 0.7), (1, False, 0.5)])
+def test_random_river_bit_identical(host_lib, seed, froude, alpha):
+    net = random_river(seed, n_active=1500)
+    a, b = OracleLi(net, froude=froude, alpha=alpha), HostLi(host_lib, net, froude=froude, alpha=alpha)
+    for m in (a, b):
+        m.set_state(net["h"])
+        m.set_inwater(net["inwater"])
+    for step in range(2):
+        assert a.step(3600.0) == b.step(3600.0)
+        for f in ("h", "storage", "q", "q_prev", "q_cum", "q_avg"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), (seed, step, f)
+    assert (net["h"] == 0.0).any() and (np.abs(net["h"] - 1e-3) < 5e-4).any()  # dry and near-threshold starts
+    assert np.abs(a.q).max() > 0.0
+
+
+def test_macdonald_bit_identical(host_lib):
+    pytest.importorskip("scipy.integrate")
+    a = dict(L=1000.0, dx=5.0, width=10.0, mannings_n=0.03, h_thresh=1e-3, alpha=0.7, epsilon=1e-12, inflow=20.0)
+    net, h_a = macdonald_case(a)
+    runs = []
+    for m in (OracleLi(net, alpha=a["alpha"]), HostLi(host_lib, net, alpha=a["alpha"])):
+        inw = np.zeros(net["n"])
+        inw[0] = a["inflow"]
+        m.set_inwater(inw)
+        for it in range(1_000_000):
+            h0 = m.h.mean()
+            m.substep(m.stable_timestep())
+            if abs(h0 - m.h.mean()) <= a["epsilon"]:
+                break
+        runs.append((it, m.h.copy()))
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][1], runs[1][1])
+    err = float(np.mean(np.abs(runs[1][1] - h_a)))
+    assert np.isclose(err, 0.01873574206931199, rtol=np.sqrt(np.finfo(float).eps), atol=0.0), err
+
+
+def test_dry_network_default_time_step(host_lib):
+    net = random_river(3, n_active=200, n_bound=2)
+    m = HostLi(host_lib, dict(net, h=np.zeros(net["n"])))
+    assert m.stable_timestep() == 60.0
