@@ -58,6 +58,104 @@ int32_t wf_li_river_step(WfLiRiver* r, double dt, int64_t* substeps);
  * model step [n_edges]. */
 int32_t wf_li_river_get(WfLiRiver* r, int32_t field, double* dst);
 
+/* ---- Local-inertial overland flow on the land grid coupled with the river ----------------
+ *
+ * Wflow's land_routing = "local_inertial" with river_routing = "local_inertial"
+ * (update_overland_flow_model!, routing/surface/surface_staggered_scheme.jl:1153-1193): per
+ * sub-step of min(river, land) stable time step, the x and y discharges on the land cell edges
+ * (update_directional_flow!, :1202-1265, local_inertial_flow with theta weighting,
+ * surface_process.jl:124-163), the river edge discharges (update_river_channel_flow!), then the
+ * storage and depths of every land cell, river cells sharing one storage between channel and
+ * floodplain with the spill above bankfull (local_inertial_update_water_depth!, :1322-1546).
+ * No reservoirs and no 1D floodplain. FP64 in the reference's operation order. */
+
+typedef struct WfLiDomain WfLiDomain;
+
+/* The land grid: n cells, 0-based neighbour indices (the value n marks outside the grid),
+ * river_index[i] the river cell in land cell i or -1. Per cell: x and y length [m], elevation
+ * [m], Manning's n, and the effective flow widths at the x and y edges [m] (the cell widths
+ * reduced by the river, set_effective_flowwidth!, Wflow/src/utils.jl:604-680). */
+typedef struct WfLiLandGrid {
+    int64_t n;
+    const int64_t* ind_x_up;
+    const int64_t* ind_x_down;
+    const int64_t* ind_y_up;
+    const int64_t* ind_y_down;
+    const int64_t* river_index;
+    const double* x_length;
+    const double* y_length;
+    const double* elevation;
+    const double* mannings_n;
+    const double* xwidth_at_edge;
+    const double* ywidth_at_edge;
+    double theta;
+    double h_thresh;
+    double alpha;
+    int32_t froude_limit;
+} WfLiLandGrid;
+
+/* The river network as for wf_li_river_create, plus the bankfull depth of every cell [m]. */
+typedef struct WfLiRiverNetwork {
+    int64_t n, n_active, n_edges;
+    const int64_t* src;
+    const int64_t* dst;
+    const double* zb;
+    const double* flow_length;
+    const double* flow_width;
+    const double* bankfull_depth;
+    const double* zb_edge;
+    const double* width_edge;
+    const double* length_edge;
+    const double* mannings_n_sq_edge;
+    double h_thresh;
+    double alpha;
+    int32_t froude_limit;
+} WfLiRiverNetwork;
+
+/* Fields of wf_li_domain_get. Land: depth, storage (river cells: channel plus floodplain),
+ * the storage clipped at zero (error), the x and y discharges and their averages over the last
+ * model step [n each]. River: depth, storage, discharge, its average, the cumulative actual
+ * abstraction [river n or n_edges]. */
+enum WfLiDomainField {
+    WF_LI_LAND_H = 0,
+    WF_LI_LAND_STORAGE = 1,
+    WF_LI_LAND_ERROR = 2,
+    WF_LI_LAND_QX = 3,
+    WF_LI_LAND_QY = 4,
+    WF_LI_LAND_QX_AVERAGE = 5,
+    WF_LI_LAND_QY_AVERAGE = 6,
+    WF_LI_RIVER_H = 7,
+    WF_LI_RIVER_STORAGE = 8,
+    WF_LI_RIVER_Q = 9,
+    WF_LI_RIVER_Q_AVERAGE = 10,
+    WF_LI_RIVER_ABSTRACTION_CUMULATIVE = 11
+};
+
+/* Both structs are read during the call only. river_index must map distinct land cells to
+ * distinct active river cells, and every active river cell must lie in a land cell. The state
+ * starts dry (Wflow's cold start) except for the river depths h_river [river n], which hold
+ * the boundary depths of the ghost cells. */
+int32_t wf_li_domain_create(const WfLiLandGrid* land, const WfLiRiverNetwork* river, const double* h_river,
+                            int32_t device, WfLiDomain** out);
+void wf_li_domain_destroy(WfLiDomain* d);
+const char* wf_li_domain_last_error(const WfLiDomain* d);
+/* A warm state (Wflow/src/sbm_model.jl:135-172): land depths [n], river depths [river n], and
+ * unless NULL the x and y discharges [n] and river discharges [n_edges]. The land storage of a
+ * river cell is h_land x_length y_length + bankfull storage where h_land > 0, else the river
+ * storage; the river storage of an active cell is h_river flow_width flow_length. */
+int32_t wf_li_domain_set_state(WfLiDomain* d, const double* h_land, const double* h_river, const double* qx,
+                               const double* qy, const double* q_river);
+/* Inputs of the coming steps: land runoff [m3 s-1, n]; river external inflow and abstraction
+ * [m3 s-1, river n] (NULL: zero). */
+int32_t wf_li_domain_set_inputs(WfLiDomain* d, const double* runoff, const double* external_inflow,
+                                const double* abstraction);
+/* min of the river and land stable time steps, each 60 s where all its cells are dry. */
+int32_t wf_li_domain_stable_timestep(WfLiDomain* d, double* dt);
+int32_t wf_li_domain_substep(WfLiDomain* d, double dt_s);
+/* A model step: cumulative discharges and abstraction restart, sub-steps until dt, averages. */
+int32_t wf_li_domain_step(WfLiDomain* d, double dt, int64_t* substeps);
+int32_t wf_li_domain_get(WfLiDomain* d, int32_t field, double* dst);
+
 #ifdef __cplusplus
 }
 #endif

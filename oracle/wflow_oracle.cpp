@@ -1858,13 +1858,13 @@ double orc_li_flow_rect(double theta, double q0, double qd, double qu, double zs
 // in the graph's edge order); the first n_active cells are updated (the others are boundary
 // cells of fixed depth). Arrays: zb, flow_length, flow_width, inwater [n]; zb_e, width_e,
 // length_e, nsq_e [n_edges]; state h, storage [n], q, q_prev, q_cum [n_edges].
-void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
-                       const double* zb, const double* flow_length, const double* flow_width, const double* inwater,
-                       const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
-                       double h_thresh, int32_t froude_limit, double dt, double* h, double* storage, double* q,
-                       double* q_prev, double* q_cum) {
+// update_river_channel_flow! (:326-385): the discharge of every river edge
+static void li_river_edges(int64_t n_edges, const int64_t* src, const int64_t* dst, const double* zb,
+                           const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
+                           double h_thresh, int32_t froude_limit, double dt, const double* h, double* q,
+                           double* q_prev, double* q_cum) {
     for (int64_t k = 0; k < n_edges; ++k) q_prev[k] = q[k];
-    for (int64_t k = 0; k < n_edges; ++k) {  // update_river_channel_flow! (:326-385)
+    for (int64_t k = 0; k < n_edges; ++k) {
         const int64_t a = src[k], b = dst[k];
         const double zs_src = zb[a] + h[a];
         const double zs_dst = zb[b] + h[b];
@@ -1880,6 +1880,15 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
         q[k] = qk;
         q_cum[k] += qk * dt;
     }
+}
+
+void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
+                       const double* zb, const double* flow_length, const double* flow_width, const double* inwater,
+                       const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
+                       double h_thresh, int32_t froude_limit, double dt, double* h, double* storage, double* q,
+                       double* q_prev, double* q_cum) {
+    li_river_edges(n_edges, src, dst, zb, zb_e, width_e, length_e, nsq_e, h_thresh, froude_limit, dt, h, q, q_prev,
+                   q_cum);
     // update_water_depth_and_storage! (:723-760), edges into / out of each cell in edge order
     std::vector<double> qin(n, 0.0), qout(n, 0.0);
     for (int64_t k = 0; k < n_edges; ++k) {
@@ -2030,6 +2039,68 @@ double orc_li_stable_timestep(int64_t n, const double* flow_length, const double
     double dt_min = std::numeric_limits<double>::infinity();
     for (int64_t i = 0; i < n; ++i) dt_min = jmin(alpha * flow_length[i] / std::sqrt(GRAVITY * h[i]), dt_min);
     return std::isinf(dt_min) ? 60.0 : dt_min;
+}
+
+// The coupled scheme's sub-step in the reference's order (update_overland_flow_model!,
+// :1170-1183): local_inertial_update_fluxes! (:1271-1290; x then y at each cell from the
+// previous discharges), staggered_scheme_river_update! without the depth update (:763-797),
+// local_inertial_update_water_depth! (:1518-1546). Edge parameters of the land grid as its
+// constructor derives them (:894-946): zx_max / zy_max the higher elevation of a cell and its
+// upstream neighbour, Manning's n squared; bankfull storage = depth * width * length (:118).
+void orc_li_domain_substep(const WfLiLandGrid* L, const WfLiRiverNetwork* R, const double* runoff,
+                           const double* external_inflow, const double* abstraction, double dt, OrcLiState* st) {
+    const int64_t n = L->n;
+    std::vector<double> zx_max(n, 0.0), zy_max(n, 0.0), nsq(n);
+    for (int64_t i = 0; i < n; ++i) {
+        if (L->ind_x_up[i] < n) zx_max[i] = jmax(L->elevation[i], L->elevation[L->ind_x_up[i]]);
+        if (L->ind_y_up[i] < n) zy_max[i] = jmax(L->elevation[i], L->elevation[L->ind_y_up[i]]);
+        nsq[i] = L->mannings_n[i] * L->mannings_n[i];
+    }
+    for (int64_t i = 0; i <= n; ++i) {
+        st->qx0[i] = st->qx[i];
+        st->qy0[i] = st->qy[i];
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        orc_li_directional_flow(i, n, L->ind_x_up, L->ind_x_down, L->ywidth_at_edge, zx_max.data(), L->x_length,
+                                L->elevation, st->h_land, nsq.data(), L->theta, L->h_thresh, L->froude_limit, dt,
+                                st->qx, st->qx0, st->qx_cum);
+        orc_li_directional_flow(i, n, L->ind_y_up, L->ind_y_down, L->xwidth_at_edge, zy_max.data(), L->y_length,
+                                L->elevation, st->h_land, nsq.data(), L->theta, L->h_thresh, L->froude_limit, dt,
+                                st->qy, st->qy0, st->qy_cum);
+    }
+    li_river_edges(R->n_edges, R->src, R->dst, R->zb, R->zb_edge, R->width_edge, R->length_edge,
+                   R->mannings_n_sq_edge, R->h_thresh, R->froude_limit, dt, st->h_river, st->q, st->q_prev, st->q_cum);
+    std::vector<std::vector<int64_t>> e_in(R->n), e_out(R->n);  // ascending edge order (findall)
+    for (int64_t k = 0; k < R->n_edges; ++k) {
+        e_in[R->dst[k]].push_back(k);
+        e_out[R->src[k]].push_back(k);
+    }
+    std::vector<double> zero(R->n, 0.0);
+    const double* ext = external_inflow ? external_inflow : zero.data();
+    const double* abs_ = abstraction ? abstraction : zero.data();
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t r = L->river_index[i];
+        if (r >= 0) {
+            const double bankfull_storage = R->bankfull_depth[r] * R->flow_width[r] * R->flow_length[r];
+            orc_li_update_river_cell(i, st->q, e_in[r].data(), (int64_t)e_in[r].size(), e_out[r].data(),
+                                     (int64_t)e_out[r].size(), st->qx, st->qy, L->ind_x_down, L->ind_y_down, runoff,
+                                     abs_[r], ext[r], bankfull_storage, R->bankfull_depth[r], L->x_length,
+                                     L->y_length, R->flow_length[r], R->flow_width[r], dt, st->storage, st->error,
+                                     st->h_land, &st->h_river[r], &st->storage_river[r], &st->abstraction_cum[r]);
+        } else {
+            orc_li_update_land_cell(i, st->qx, st->qy, L->ind_x_down, L->ind_y_down, runoff, L->x_length, L->y_length,
+                                    dt, st->storage, st->error, st->h_land);
+        }
+    }
+}
+
+double orc_li_domain_stable_timestep(const WfLiLandGrid* L, const WfLiRiverNetwork* R, const OrcLiState* st) {
+    std::vector<int32_t> river_location(L->n);
+    for (int64_t i = 0; i < L->n; ++i) river_location[i] = L->river_index[i] >= 0 ? 1 : 0;
+    const double dt_river = orc_li_stable_timestep(R->n, R->flow_length, st->h_river, R->alpha);
+    const double dt_land =
+        orc_li_land_stable_timestep(L->n, L->x_length, L->y_length, river_location.data(), st->h_land, L->alpha);
+    return jmin(dt_river, dt_land);
 }
 
 }  // extern "C"

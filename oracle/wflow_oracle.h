@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include "../include/wflow_gb300.h"
+#include "../include/wflow_gb300_li.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -176,6 +177,19 @@ void orc_li_update_river_cell(int64_t i, const double* q_river, const int64_t* e
                               double river_length, double river_width, double dt, double* storage, double* error,
                               double* h_land, double* h_river, double* storage_river,
                               double* abstraction_cumulative);
+/* The coupled land + river local-inertial scheme over the product's input description
+ * (include/wflow_gb300_li.h): the state arrays of one domain; qx, qy, qx0, qy0, qx_cum, qy_cum
+ * hold n + 1 values (the last, outside the grid, stays 0). */
+typedef struct OrcLiState {
+    double *h_land, *storage, *error, *qx, *qy, *qx0, *qy0, *qx_cum, *qy_cum;
+    double *h_river, *storage_river, *q, *q_prev, *q_cum, *abstraction_cum;
+} OrcLiState;
+/* One sub-step (the loop body of update_overland_flow_model!, surface_staggered_scheme.jl:
+ * 1170-1183, without reservoirs): land fluxes, river edges, then the depths of every land cell. */
+void orc_li_domain_substep(const WfLiLandGrid* land, const WfLiRiverNetwork* river, const double* runoff,
+                           const double* external_inflow, const double* abstraction, double dt, OrcLiState* st);
+/* min(river, land) stable time step, each 60 s when infinite (:1171-1174) */
+double orc_li_domain_stable_timestep(const WfLiLandGrid* land, const WfLiRiverNetwork* river, const OrcLiState* st);
 
 /* full model */
 typedef struct OrcModel OrcModel;

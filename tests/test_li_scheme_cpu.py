@@ -94,3 +94,71 @@ def test_dry_network_default_time_step(host_lib):
     net = random_river(3, n_active=200, n_bound=2)
     m = HostLi(host_lib, dict(net, h=np.zeros(net["n"])))
     assert m.stable_timestep() == 60.0
+
+
+# ---- the land grid with its river -----------------------------------------------------------
+
+DOMAIN_FIELDS = ("h_land", "storage", "error", "qx", "qy", "qx_average", "qy_average", "h_river", "storage_river",
+                 "q_river", "q_river_average", "abstraction_cumulative")
+
+
+def _host_domain_class(lib):
+    from li_cases import OracleLiDomain, OrcLiState
+
+    class HostLiDomain(OracleLiDomain):
+        """OracleLiDomain's driver over the host build of the product's scheme functions, with
+        the device's two swapped discharge buffers per direction."""
+
+        def stable_timestep(self):
+            return lib.host_li_domain_stable_timestep(C.byref(self.g), C.byref(self.r), C.byref(self.st))
+
+        def substep(self, dt):
+            a = self.a
+            a["qx"], a["qx0"] = a["qx0"], a["qx"]
+            a["qy"], a["qy0"] = a["qy0"], a["qy"]
+            self.st = OrcLiState(**{k: _pd(v) for k, v in a.items()})
+            lib.host_li_domain_substep(C.byref(self.g), C.byref(self.r), _pd(self.runoff), _pd(self.ext),
+                                       _pd(self.abs), C.c_double(dt), C.byref(self.st))
+
+    lib.host_li_domain_stable_timestep.restype = C.c_double
+    return HostLiDomain
+
+
+def test_struct_sizes_match_python(host_lib):
+    from wflow_gb300.li_river import WfLiLandGrid, WfLiRiverNetwork
+    out = np.zeros(2, np.int64)
+    host_lib.host_li_struct_sizes(_pl(out))
+    assert list(out) == [C.sizeof(WfLiLandGrid), C.sizeof(WfLiRiverNetwork)]
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_land_domain_bit_identical(host_lib, seed):
+    """Two hourly steps of a 36 x 28 grid with a main river, a tributary, closed edges, an
+    abstraction, a negative and a positive external inflow, from a warm state with cells over
+    bankfull: every land and river field equal to the oracle's, with equal sub-step counts."""
+    from li_cases import OracleLiDomain, random_land_domain
+    land, river, h_river, state, inputs = random_land_domain(seed)
+    a = OracleLiDomain(land, river, h_river)
+    b = _host_domain_class(host_lib)(land, river, h_river)
+    for m in (a, b):
+        m.set_state(**state)
+        m.set_inputs(**inputs)
+    for step in range(2):
+        assert a.step(3600.0) == b.step(3600.0)
+        for f in DOMAIN_FIELDS:
+            assert np.array_equal(a.get(f), b.get(f)), (seed, step, f)
+    assert a.get("abstraction_cumulative").sum() > 0.0 and a.get("error").sum() > 0.0
+    assert (a.get("h_land")[land["river_index"] >= 0] > 0.0).any()  # some river cells over bankfull
+
+
+def test_land_domain_dry_time_step(host_lib):
+    """A dry grid with a dry river (but the ghost cell): the river's minimum sets the step; all
+    dry, both minima are infinite and the step is the 60 s default."""
+    from li_cases import random_land_domain
+    land, river, h_river, _, _ = random_land_domain(2, nx=12, ny=10)
+    H = _host_domain_class(host_lib)
+    m = H(land, river, np.zeros_like(h_river))
+    assert m.stable_timestep() == 60.0
+    m = H(land, river, h_river)
+    g = 9.80665
+    assert m.stable_timestep() == min(60.0, river["alpha"] * river["flow_length"][-1] / np.sqrt(g * h_river[-1]))

@@ -9,7 +9,11 @@ sub-step counts must be equal. MacDonald's long channel (routing_process.jl:1189
 the GPU to steady state reproduces the reference's mean absolute depth error
 0.01873574206931199 within Julia's default isapprox tolerance (sqrt(eps)).
 
-The argument checks of wf_li_river_create run before any device call and are tested on CPU.
+The land grid with its river (wf_li_domain_*, update_overland_flow_model!, :1153-1193) is held to
+the same bar on a grid with a main river and a tributary, from a warm and a cold state.
+
+The argument checks of wf_li_river_create and wf_li_domain_create run before any device call and
+are tested on CPU.
 """
 
 import numpy as np
@@ -114,6 +118,84 @@ def test_macdonald_steady_state(gpu_lib):
     assert runs["gpu"][0] == runs["oracle"][0], runs
     assert _max_rel(runs["gpu"][1], runs["oracle"][1]) <= 1e-9, runs
     assert np.isclose(runs["gpu"][1], 0.01873574206931199, rtol=np.sqrt(np.finfo(float).eps), atol=0.0), runs
+
+
+DOMAIN_FIELDS = ("h_land", "storage", "error", "qx", "qy", "qx_average", "qy_average", "h_river", "storage_river",
+                 "q_river", "q_river_average", "abstraction_cumulative")
+
+
+def _domain(land, river, h_river):
+    from wflow_gb300.li_river import LiDomain
+    return LiDomain(land, river, h_river)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [0, 1])
+def test_land_domain_steps(gpu_lib, seed):
+    """Two hourly steps of the land grid with its river (update_overland_flow_model!,
+    surface_staggered_scheme.jl:1153-1193): a 36 x 28 grid, main river and tributary, closed
+    edges, an abstraction, a negative and a positive external inflow, a warm state with cells over
+    bankfull. Every land and river field within relative 1e-9 of the oracle, equal sub-step
+    counts, and the stable time step of the final state."""
+    from li_cases import OracleLiDomain, random_land_domain
+    land, river, h_river, state, inputs = random_land_domain(seed)
+    gpu, orc = _domain(land, river, h_river), OracleLiDomain(land, river, h_river)
+    for m in (gpu, orc):
+        m.set_state(**state)
+        m.set_inputs(**inputs)
+    for step in range(2):
+        k_gpu, k_orc = gpu.step(3600.0), orc.step(3600.0)
+        assert k_gpu == k_orc, (seed, step, k_gpu, k_orc)
+        for f in DOMAIN_FIELDS:
+            assert _max_rel(gpu.get(f), orc.get(f)) <= 1e-9, (seed, step, f)
+    assert _max_rel(gpu.stable_timestep(), orc.stable_timestep()) <= 1e-12
+    gpu.close()
+
+
+@pytest.mark.gpu
+def test_land_domain_cold_start_substeps(gpu_lib):
+    """A cold start (dry land and river but the ghost cell) under runoff, by explicit sub-steps."""
+    from li_cases import OracleLiDomain, random_land_domain
+    land, river, h_river, _, inputs = random_land_domain(4, nx=20, ny=16)
+    gpu, orc = _domain(land, river, h_river), OracleLiDomain(land, river, h_river)
+    for m in (gpu, orc):
+        m.set_inputs(inputs["runoff"])
+    for s in range(60):
+        dt_g, dt_o = gpu.stable_timestep(), orc.stable_timestep()
+        assert _max_rel(dt_g, dt_o) <= 1e-12, (s, dt_g, dt_o)
+        gpu.substep(dt_o)
+        orc.substep(dt_o)
+    for f in ("h_land", "storage", "error", "qx", "qy", "h_river", "storage_river", "q_river"):
+        assert _max_rel(gpu.get(f), orc.get(f)) <= 1e-9, f
+    gpu.close()
+
+
+def test_domain_create_rejects_bad_grids():
+    """Argument checks of wf_li_domain_create (no device call is reached)."""
+    from wflow_gb300 import build
+    from li_cases import random_land_domain
+    build.build_all()
+    land, river, h_river, _, _ = random_land_domain(5, nx=10, ny=8)
+    ri = land["river_index"]
+    r0 = int(np.flatnonzero(ri == 0)[0])
+    dup = ri.copy()
+    dup[np.flatnonzero(ri < 0)[0]] = 0
+    with pytest.raises(RuntimeError, match="two land cells hold one river cell"):
+        _domain(dict(land, river_index=dup), river, h_river)
+    gap = ri.copy()
+    gap[r0] = -1
+    with pytest.raises(RuntimeError, match="lies in no land cell"):
+        _domain(dict(land, river_index=gap), river, h_river)
+    bad = land["ind_x_down"].copy()
+    bad[0] = len(bad) + 1
+    with pytest.raises(RuntimeError, match="neighbour index out of range"):
+        _domain(dict(land, ind_x_down=bad), river, h_river)
+    ghost = ri.copy()
+    ghost[r0] = river["n_active"]
+    with pytest.raises(RuntimeError, match="active river cell"):
+        _domain(dict(land, river_index=ghost), river, h_river)
+    with pytest.raises(ValueError, match="h_river"):
+        _domain(land, river, h_river[:-1])
 
 
 def test_create_rejects_bad_networks():

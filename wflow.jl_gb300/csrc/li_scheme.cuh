@@ -87,6 +87,156 @@ WF_HD double finish_timestep(double dt_min) {
     return dt_min == wfm::from_bits(0x7ff0000000000000ULL) ? 60.0 : dt_min;
 }
 
+// ---- overland flow on the land grid, coupled with the river --------------------------------
+
+// The land grid of the coupled scheme. Neighbour index n marks outside the grid; the discharge
+// arrays hold n + 1 values, the last staying zero. qx0 / qy0 are the discharges of the previous
+// sub-step (the device swaps the two buffers each sub-step). river[i] is the river cell in land
+// cell i or -1.
+struct LiLand {
+    int64_t n;
+    const int64_t *ixu, *ixd, *iyu, *iyd, *river;
+    const double *xl, *yl, *z, *nsq, *xw, *yw, *zx_max, *zy_max;
+    const double* runoff;
+    double *h, *storage, *error;
+    const double *qx0, *qy0;
+    double *qx, *qy, *qx_cum, *qy_cum, *dt_min;
+    double theta, h_thresh, alpha;
+    int32_t froude;
+};
+
+// Per river cell boundary data of the coupled scheme.
+struct LiRiverBC {
+    const double *bankfull_depth, *bankfull_storage, *external_inflow, *abstraction;
+    double* abstraction_cum;
+};
+
+// local_inertial_flow, rectangular cross-section with the theta weighting
+// (surface_process.jl:124-163)
+WF_HD double flow_rect(double theta, double q0, double qd, double qu, double zs0, double zs1, double hf, double width,
+                       double length, double nsq, bool froude, double dt) {
+    const double slope = (zs1 - zs0) / length;
+    const double pow_hf = wfm::cbrt(hf * hf * hf * hf * hf * hf * hf);
+    double q = ((theta * q0 + 0.5 * (1.0 - theta) * (qu + qd)) - GRAVITY * hf * width * dt * slope) /
+               (1.0 + GRAVITY * dt * nsq * wfm::fabs_(q0) / (pow_hf * width));
+    if (froude) {
+        const double fr = (q / width / hf) / wfm::sqrt_(GRAVITY * hf);
+        if (wfm::fabs_(fr) > 1.0 && q > 0.0)
+            q = hf * wfm::sqrt_(GRAVITY * hf) * width;
+        else if (wfm::fabs_(fr) > 1.0 && q < 0.0)
+            q = -hf * wfm::sqrt_(GRAVITY * hf) * width;
+    }
+    return q;
+}
+
+// update_directional_flow! at land cell i (surface_staggered_scheme.jl:1202-1265). An edge
+// without an upstream cell or with zero effective width keeps its discharge.
+WF_HD void land_direction(const LiLand& L, int64_t i, double dt, bool x_dir) {
+    const int64_t u = x_dir ? L.ixu[i] : L.iyu[i];
+    const int64_t dn = x_dir ? L.ixd[i] : L.iyd[i];
+    const double width = x_dir ? L.yw[i] : L.xw[i];
+    const double* q0 = x_dir ? L.qx0 : L.qy0;
+    double* q = x_dir ? L.qx : L.qy;
+    if (!(u < L.n && width != 0.0)) {
+        q[i] = q0[i];
+        return;
+    }
+    const double* len = x_dir ? L.xl : L.yl;
+    const double zs_current = L.z[i] + L.h[i];
+    const double zs_upstream = L.z[u] + L.h[u];
+    const double zs_max = wfm::jmax(zs_current, zs_upstream);
+    const double hf = zs_max - (x_dir ? L.zx_max[i] : L.zy_max[i]);
+    double qi = 0.0;
+    if (hf > L.h_thresh) {
+        const double length_e = 0.5 * (len[i] + len[u]);
+        qi = flow_rect(L.theta, q0[i], q0[dn], q0[u], zs_current, zs_upstream, hf, width, length_e, L.nsq[i],
+                       L.froude != 0, dt);
+        if (L.h[i] <= 0.0) qi = wfm::jmin(qi, 0.0);
+        if (L.h[u] <= 0.0) qi = wfm::jmax(qi, 0.0);
+    }
+    q[i] = qi;
+    (x_dir ? L.qx_cum : L.qy_cum)[i] += qi * dt;
+}
+
+// storage and depths of land cell i (local_inertial_update_water_depth!, :1518-1546): a cell
+// without a river from its edge discharges and runoff (:1420-1433, 1481-1503); a river cell
+// from those and its river edges, with the external inflow or abstraction, the channel holding
+// the storage up to bankfull and the rest spilling over the cell (:1322-1414, 1440-1476)
+WF_HD void land_depth(const LiLand& L, const LiNet& R, const LiRiverBC& B, int64_t i, double dt) {
+    const int64_t r = L.river[i];
+    const int64_t xd = L.ixd[i], yd = L.iyd[i];
+    if (r < 0) {
+        double s = L.storage[i] + (L.qx[xd] - L.qx[i] + L.qy[yd] - L.qy[i] + L.runoff[i]) * dt;
+        if (s < 0.0) {
+            L.error[i] += wfm::fabs_(s);
+            s = 0.0;
+        }
+        L.storage[i] = s;
+        L.h[i] = s / (L.xl[i] * L.yl[i]);
+        return;
+    }
+    double s_in = 0.0, s_out = 0.0;
+    for (int64_t o = R.in_ptr[r]; o < R.in_ptr[r + 1]; ++o) s_in = s_in + R.q[R.in_edge[o]];
+    for (int64_t o = R.out_ptr[r]; o < R.out_ptr[r + 1]; ++o) s_out = s_out + R.q[R.out_edge[o]];
+    const double net_river = s_in - s_out;
+    const double net_land = L.qx[xd] - L.qx[i] + L.qy[yd] - L.qy[i];
+    const double net = net_river + net_land + L.runoff[i] - B.abstraction[r];
+    double s = L.storage[i] + net * dt;
+    if (s < 0.0) {
+        L.error[i] += wfm::fabs_(s);
+        s = 0.0;
+    }
+    const double ext = B.external_inflow[r];
+    double inflow = ext, taken = 0.0;
+    if (ext < 0.0) {
+        const double available = s >= B.bankfull_storage[r] ? B.bankfull_storage[r] : R.storage[r];
+        taken = wfm::jmin(-ext, available / dt * 0.80);
+        inflow = -taken;
+    }
+    s += inflow * dt;
+    B.abstraction_cum[r] += taken * dt;
+    L.storage[i] = s;
+    if (s >= B.bankfull_storage[r]) {
+        const double river_h = B.bankfull_depth[r] + (s - B.bankfull_storage[r]) / (L.xl[i] * L.yl[i]);
+        R.h[r] = river_h;
+        L.h[i] = river_h - B.bankfull_depth[r];
+        R.storage[r] = river_h * R.flow_length[r] * R.flow_width[r];
+    } else {
+        R.h[r] = s / (R.flow_length[r] * R.flow_width[r]);
+        L.h[i] = 0.0;
+        R.storage[r] = s;
+    }
+}
+
+// the stable sub-step of land cell i: cells without a river only (:1022-1040)
+WF_HD double land_timestep(const LiLand& L, int64_t i) {
+    return L.river[i] < 0 ? L.alpha * wfm::jmin(L.xl[i], L.yl[i]) / wfm::sqrt_(GRAVITY * L.h[i])
+                          : wfm::from_bits(0x7ff0000000000000ULL);
+}
+
+// Edge parameters of the land grid as LocalInertialOverlandFlowParameters derives them
+// (surface_staggered_scheme.jl:894-946): the higher elevation of a cell and its upstream
+// neighbour in x and y (0 without one) and Manning's n squared. Host code.
+inline void land_edge_parameters(int64_t n, const int64_t* ind_x_up, const int64_t* ind_y_up, const double* elevation,
+                                 const double* mannings_n, std::vector<double>& zx_max, std::vector<double>& zy_max,
+                                 std::vector<double>& nsq) {
+    zx_max.assign(n, 0.0);
+    zy_max.assign(n, 0.0);
+    nsq.assign(n, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        if (ind_x_up[i] < n) zx_max[i] = wfm::jmax(elevation[i], elevation[ind_x_up[i]]);
+        if (ind_y_up[i] < n) zy_max[i] = wfm::jmax(elevation[i], elevation[ind_y_up[i]]);
+        nsq[i] = mannings_n[i] * mannings_n[i];
+    }
+}
+
+// bankfull_depth .* flow_width .* flow_length (RiverFlowStaggeredParameters, :118). Host code.
+inline void bankfull_storage(int64_t n, const double* bankfull_depth, const double* flow_width,
+                             const double* flow_length, std::vector<double>& out) {
+    out.assign(n, 0.0);
+    for (int64_t r = 0; r < n; ++r) out[r] = bankfull_depth[r] * flow_width[r] * flow_length[r];
+}
+
 // CSR lists of the edges into and out of each of n cells, each list in ascending edge order
 // (the order in which sum_at adds them). Host code; indices must already be checked in range.
 inline void build_csr(int64_t n, int64_t n_edges, const int64_t* src, const int64_t* dst, std::vector<int64_t>& in_ptr,

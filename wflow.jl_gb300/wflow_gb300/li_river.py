@@ -1,9 +1,13 @@
-"""Local-inertial river flow on the GPU (include/wflow_gb300_li.h), over ctypes.
+"""Local-inertial routing on the GPU (include/wflow_gb300_li.h), over ctypes.
 
 `LiRiver` holds a river network on a staggered grid (cells and the edges between them) with
 its state on the device; `substep`, `stable_timestep` and `step` mirror Wflow's
 staggered_scheme_river_update!, stable_timestep and update_river_flow_model! for a channel
 without floodplain (Wflow/src/routing/surface/surface_staggered_scheme.jl).
+
+`LiDomain` adds the land grid: overland flow on the x and y cell edges coupled with the river
+(update_overland_flow_model!, surface_staggered_scheme.jl:1153-1193), river cells sharing one
+storage between channel and floodplain.
 """
 
 import ctypes as C
@@ -32,6 +36,16 @@ def _lib():
             "wf_li_river_substep": (i32, [P, d]),
             "wf_li_river_step": (i32, [P, d, pl]),
             "wf_li_river_get": (i32, [P, i32, pd]),
+            "wf_li_domain_create": (i32, [C.POINTER(WfLiLandGrid), C.POINTER(WfLiRiverNetwork), pd, i32,
+                                          C.POINTER(P)]),
+            "wf_li_domain_destroy": (None, [P]),
+            "wf_li_domain_last_error": (C.c_char_p, [P]),
+            "wf_li_domain_set_state": (i32, [P, pd, pd, pd, pd, pd]),
+            "wf_li_domain_set_inputs": (i32, [P, pd, pd, pd]),
+            "wf_li_domain_stable_timestep": (i32, [P, pd]),
+            "wf_li_domain_substep": (i32, [P, d]),
+            "wf_li_domain_step": (i32, [P, d, pl]),
+            "wf_li_domain_get": (i32, [P, i32, pd]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -43,6 +57,75 @@ def _lib():
 
 def _pd(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _pl(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+_PL, _PD = C.POINTER(C.c_int64), C.POINTER(C.c_double)
+
+
+class WfLiLandGrid(C.Structure):
+    _fields_ = [("n", C.c_int64)] + [(f, _PL) for f in ("ind_x_up", "ind_x_down", "ind_y_up", "ind_y_down",
+                                                         "river_index")] + \
+               [(f, _PD) for f in ("x_length", "y_length", "elevation", "mannings_n", "xwidth_at_edge",
+                                   "ywidth_at_edge")] + \
+               [("theta", C.c_double), ("h_thresh", C.c_double), ("alpha", C.c_double), ("froude_limit", C.c_int32)]
+
+
+class WfLiRiverNetwork(C.Structure):
+    _fields_ = [("n", C.c_int64), ("n_active", C.c_int64), ("n_edges", C.c_int64), ("src", _PL), ("dst", _PL)] + \
+               [(f, _PD) for f in ("zb", "flow_length", "flow_width", "bankfull_depth", "zb_edge", "width_edge",
+                                   "length_edge", "mannings_n_sq_edge")] + \
+               [("h_thresh", C.c_double), ("alpha", C.c_double), ("froude_limit", C.c_int32)]
+
+
+LAND_INT = ("ind_x_up", "ind_x_down", "ind_y_up", "ind_y_down", "river_index")
+LAND_DBL = ("x_length", "y_length", "elevation", "mannings_n", "xwidth_at_edge", "ywidth_at_edge")
+RIVER_INT = ("src", "dst")
+RIVER_CELL = ("zb", "flow_length", "flow_width", "bankfull_depth")
+RIVER_EDGE = ("zb_edge", "width_edge", "length_edge", "mannings_n_sq_edge")
+
+
+def land_grid(land, keep):
+    """A WfLiLandGrid over the arrays of `land` (a dict; the arrays are kept alive in `keep`)."""
+    n = len(land["x_length"])
+    g = WfLiLandGrid()
+    g.n = n
+    for f in LAND_INT:
+        a = np.ascontiguousarray(land[f], np.int64)
+        if a.shape != (n,):
+            raise ValueError(f"{f} must have {n} values")
+        keep.append(a)
+        setattr(g, f, _pl(a))
+    for f in LAND_DBL:
+        a = np.ascontiguousarray(land[f], np.float64)
+        if a.shape != (n,):
+            raise ValueError(f"{f} must have {n} values")
+        keep.append(a)
+        setattr(g, f, _pd(a))
+    g.theta, g.h_thresh, g.alpha = float(land["theta"]), float(land["h_thresh"]), float(land["alpha"])
+    g.froude_limit = int(bool(land["froude_limit"]))
+    return g
+
+
+def river_network(river, keep):
+    """A WfLiRiverNetwork over the arrays of `river` (a dict)."""
+    n, ne = len(river["zb"]), len(river["src"])
+    r = WfLiRiverNetwork()
+    r.n, r.n_active, r.n_edges = n, int(river["n_active"]), ne
+    for f in RIVER_INT + RIVER_CELL + RIVER_EDGE:
+        dt = np.int64 if f in RIVER_INT else np.float64
+        a = np.ascontiguousarray(river[f], dt)
+        m = n if f in RIVER_CELL else ne
+        if a.shape != (m,):
+            raise ValueError(f"{f} must have {m} values")
+        keep.append(a)
+        setattr(r, f, _pl(a) if f in RIVER_INT else _pd(a))
+    r.h_thresh, r.alpha = float(river["h_thresh"]), float(river["alpha"])
+    r.froude_limit = int(bool(river["froude_limit"]))
+    return r
 
 
 class LiRiver:
@@ -120,4 +203,83 @@ class LiRiver:
         f = self.FIELDS[field]
         out = np.empty(self.n if f <= 1 else self.n_edges)
         self._check(self.lib.wf_li_river_get(self.h, f, _pd(out)), "wf_li_river_get")
+        return out
+
+
+class LiDomain:
+    """The land grid with its river (wf_li_domain_*). `land` and `river` are dicts with the
+    fields of WfLiLandGrid and WfLiRiverNetwork; h_river the starting river depths (the ghost
+    cells' boundary depths)."""
+
+    FIELDS = {"h_land": 0, "storage": 1, "error": 2, "qx": 3, "qy": 4, "qx_average": 5, "qy_average": 6,
+              "h_river": 7, "storage_river": 8, "q_river": 9, "q_river_average": 10, "abstraction_cumulative": 11}
+
+    def __init__(self, land, river, h_river, device=0):
+        self.lib = _lib()
+        self._keep = []
+        g, r = land_grid(land, self._keep), river_network(river, self._keep)
+        self.n, self.nr, self.ne = g.n, r.n, r.n_edges
+        hr = np.ascontiguousarray(h_river, np.float64)
+        if hr.shape != (self.nr,):
+            raise ValueError(f"h_river must have {self.nr} values")
+        self.h = C.c_void_p()
+        st = self.lib.wf_li_domain_create(C.byref(g), C.byref(r), _pd(hr), int(device), C.byref(self.h))
+        if st != 0:
+            msg = self.lib.wf_li_domain_last_error(None)
+            raise RuntimeError(f"wf_li_domain_create failed ({st}): {msg.decode() if msg else ''}")
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.lib.wf_li_domain_last_error(self.h)
+            raise RuntimeError(f"{what} failed ({st}): {msg.decode() if msg else ''}")
+
+    def _vec(self, a, m, name):
+        if a is None:
+            return None
+        v = np.ascontiguousarray(a, np.float64)
+        if v.shape != (m,):
+            raise ValueError(f"{name} must have {m} values")
+        return v
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wf_li_domain_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, h_land, h_river, qx=None, qy=None, q_river=None):
+        v = [self._vec(h_land, self.n, "h_land"), self._vec(h_river, self.nr, "h_river"), self._vec(qx, self.n, "qx"),
+             self._vec(qy, self.n, "qy"), self._vec(q_river, self.ne, "q_river")]
+        self._check(self.lib.wf_li_domain_set_state(self.h, *[None if a is None else _pd(a) for a in v]),
+                    "wf_li_domain_set_state")
+
+    def set_inputs(self, runoff, external_inflow=None, abstraction=None):
+        v = [self._vec(runoff, self.n, "runoff"), self._vec(external_inflow, self.nr, "external_inflow"),
+             self._vec(abstraction, self.nr, "abstraction")]
+        self._check(self.lib.wf_li_domain_set_inputs(self.h, *[None if a is None else _pd(a) for a in v]),
+                    "wf_li_domain_set_inputs")
+
+    def stable_timestep(self):
+        dt = C.c_double()
+        self._check(self.lib.wf_li_domain_stable_timestep(self.h, C.byref(dt)), "wf_li_domain_stable_timestep")
+        return dt.value
+
+    def substep(self, dt_s):
+        self._check(self.lib.wf_li_domain_substep(self.h, float(dt_s)), "wf_li_domain_substep")
+
+    def step(self, dt):
+        k = C.c_int64()
+        self._check(self.lib.wf_li_domain_step(self.h, float(dt), C.byref(k)), "wf_li_domain_step")
+        return k.value
+
+    def get(self, field):
+        f = self.FIELDS[field]
+        m = self.n if f <= 6 else (self.ne if f in (9, 10) else self.nr)
+        out = np.empty(m)
+        self._check(self.lib.wf_li_domain_get(self.h, f, _pd(out)), "wf_li_domain_get")
         return out
