@@ -43,6 +43,10 @@ const char* wf_li_river_last_error(const WfLiRiver* r);
  * [n_edges]; the storage of the active cells becomes h * flow_width * flow_length (as Wflow sets
  * it after reading a state file, Wflow/src/sbm_model.jl:168-172). */
 int32_t wf_li_river_set_state(WfLiRiver* r, const double* h, const double* q);
+/* The stable time step is the minimum over cells 0..n_cells-1 (default: all n cells, as the
+ * reference's MacDonald test sets its boundary cell inside n; a Wflow model's river has its ghost
+ * cells after its RiverFlowStaggeredParameters.n real cells and passes that n). */
+int32_t wf_li_river_set_timestep_cells(WfLiRiver* r, int64_t n_cells);
 /* Lateral inflow of every cell [m3 s-1] (inwater). */
 int32_t wf_li_river_set_inwater(WfLiRiver* r, const double* inwater);
 /* The stable sub-step of the current depths (60 s when every cell is dry). */
@@ -149,7 +153,8 @@ int32_t wf_li_domain_set_state(WfLiDomain* d, const double* h_land, const double
  * [m3 s-1, river n] (NULL: zero). */
 int32_t wf_li_domain_set_inputs(WfLiDomain* d, const double* runoff, const double* external_inflow,
                                 const double* abstraction);
-/* min of the river and land stable time steps, each 60 s where all its cells are dry. */
+/* min of the river and land stable time steps, each 60 s where all its cells are dry; the
+ * river's over its active cells (not the ghost cells), the land's over cells without a river. */
 int32_t wf_li_domain_stable_timestep(WfLiDomain* d, double* dt);
 int32_t wf_li_domain_substep(WfLiDomain* d, double dt_s);
 /* A model step: cumulative discharges and abstraction restart, sub-steps until dt, averages. */

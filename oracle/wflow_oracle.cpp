@@ -2097,7 +2097,8 @@ void orc_li_domain_substep(const WfLiLandGrid* L, const WfLiRiverNetwork* R, con
 double orc_li_domain_stable_timestep(const WfLiLandGrid* L, const WfLiRiverNetwork* R, const OrcLiState* st) {
     std::vector<int32_t> river_location(L->n);
     for (int64_t i = 0; i < L->n; ++i) river_location[i] = L->river_index[i] >= 0 ? 1 : 0;
-    const double dt_river = orc_li_stable_timestep(R->n, R->flow_length, st->h_river, R->alpha);
+    // the river's real cells: stable_timestep loops over parameters.n, the ghosts come after
+    const double dt_river = orc_li_stable_timestep(R->n_active, R->flow_length, st->h_river, R->alpha);
     const double dt_land =
         orc_li_land_stable_timestep(L->n, L->x_length, L->y_length, river_location.data(), st->h_land, L->alpha);
     return jmin(dt_river, dt_land);

@@ -188,7 +188,8 @@ typedef struct OrcLiState {
  * 1170-1183, without reservoirs): land fluxes, river edges, then the depths of every land cell. */
 void orc_li_domain_substep(const WfLiLandGrid* land, const WfLiRiverNetwork* river, const double* runoff,
                            const double* external_inflow, const double* abstraction, double dt, OrcLiState* st);
-/* min(river, land) stable time step, each 60 s when infinite (:1171-1174) */
+/* min(river, land) stable time step, each 60 s when infinite (:1171-1174); the river's over its
+ * active cells (parameters.n, without the ghost cells), the land's over cells without a river */
 double orc_li_domain_stable_timestep(const WfLiLandGrid* land, const WfLiRiverNetwork* river, const OrcLiState* st);
 
 /* full model */

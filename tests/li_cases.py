@@ -114,8 +114,12 @@ class OracleLi:
         self.q_avg = np.zeros(self.ne)
         self.inwater = np.zeros(self.n)
         self.h_thresh, self.froude, self.alpha = h_thresh, froude, alpha
+        self.n_dt = self.n
         self.L = O.lib()
         self.L.orc_li_stable_timestep.restype = C.c_double
+
+    def set_timestep_cells(self, n_cells):
+        self.n_dt = int(n_cells)
 
     def set_state(self, h, q=None):
         """Wflow's warm start: storage of active cells = h * flow_width * flow_length."""
@@ -130,7 +134,7 @@ class OracleLi:
         self.inwater = np.array(v, float)
 
     def stable_timestep(self):
-        return self.L.orc_li_stable_timestep(C.c_int64(self.n), _pd(self.net["flow_length"]), _pd(self.h),
+        return self.L.orc_li_stable_timestep(C.c_int64(self.n_dt), _pd(self.net["flow_length"]), _pd(self.h),
                                              C.c_double(self.alpha))
 
     def substep(self, dt):

@@ -189,7 +189,7 @@ double host_li_domain_stable_timestep(const WfLiLandGrid* g, const WfLiRiverNetw
     HostDomain h;
     host_domain(h, g, r, nullptr, nullptr, nullptr, st);
     const double dt_river = wfli::finish_timestep(
-        host_block_min(r->n, [](const HostDomain& d, int64_t i) { return wfli::cell_timestep(d.R, i); }, h));
+        host_block_min(r->n_active, [](const HostDomain& d, int64_t i) { return wfli::cell_timestep(d.R, i); }, h));
     const double dt_land = wfli::finish_timestep(
         host_block_min(g->n, [](const HostDomain& d, int64_t i) { return wfli::land_timestep(d.L, i); }, h));
     return wfm::jmin(dt_river, dt_land);

@@ -42,7 +42,7 @@ class HostLi(OracleLi):
         self.H = lib
 
     def stable_timestep(self):
-        return self.H.host_li_stable_timestep(C.c_int64(self.n), _pd(self.net["flow_length"]), _pd(self.h),
+        return self.H.host_li_stable_timestep(C.c_int64(self.n_dt), _pd(self.net["flow_length"]), _pd(self.h),
                                               C.c_double(self.alpha))
 
     def substep(self, dt):
@@ -160,13 +160,16 @@ def test_land_domain_bit_identical(host_lib, seed, variant):
 
 
 def test_land_domain_dry_time_step(host_lib):
-    """A dry grid with a dry river (but the ghost cell): the river's minimum sets the step; all
-    dry, both minima are infinite and the step is the 60 s default."""
+    """A dry grid whose river is dry but for its ghost cell: the ghost cells are outside the
+    river's minimum (stable_timestep loops over parameters.n, the real river cells), so both
+    minima are infinite and the step is the 60 s default; one wet river cell sets it."""
     from li_cases import random_land_domain
     land, river, h_river, _, _ = random_land_domain(2, nx=12, ny=10)
     H = _host_domain_class(host_lib)
-    m = H(land, river, np.zeros_like(h_river))
-    assert m.stable_timestep() == 60.0
     m = H(land, river, h_river)
+    assert h_river[-1] > 0.0 and m.stable_timestep() == 60.0
+    wet = h_river.copy()
+    wet[3] = 0.4
+    m = H(land, river, wet)
     g = 9.80665
-    assert m.stable_timestep() == min(60.0, river["alpha"] * river["flow_length"][-1] / np.sqrt(g * h_river[-1]))
+    assert m.stable_timestep() == min(60.0, river["alpha"] * river["flow_length"][3] / np.sqrt(g * 0.4))

@@ -84,6 +84,21 @@ def test_substeps_and_warm_discharge(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_time_step_over_real_cells(gpu_lib):
+    """A Wflow model's river: the stable time step over the real cells only, the outlets' ghost
+    cells (fixed depth) after them (stable_timestep loops over parameters.n)."""
+    net = random_river(11, n_active=800, n_bound=3)
+    gpu, orc = _river(net), OracleLi(net)
+    for m in (gpu, orc):
+        m.set_timestep_cells(net["n_active"])
+        m.set_state(net["h"])
+        m.set_inwater(net["inwater"])
+    assert gpu.step(3600.0) == orc.step(3600.0)
+    _assert_same(gpu, orc, "real cells")
+    gpu.close()
+
+
+@pytest.mark.gpu
 def test_dry_network_time_step(gpu_lib):
     """Every cell dry: the stable time step is the 60 s default and a sub-step moves nothing."""
     net = random_river(3, n_active=300, n_bound=2)

@@ -63,7 +63,7 @@ __device__ double block_min(double m, double* red) {
 __global__ void li_dt_kernel(LiDev d) {
     __shared__ double red[LI_DT_THREADS];
     double m = wfm::from_bits(INF_BITS);
-    for (int64_t i = threadIdx.x; i < d.n; i += LI_DT_THREADS) m = wfm::jmin(wfli::cell_timestep(d, i), m);
+    for (int64_t i = threadIdx.x; i < d.n_dt; i += LI_DT_THREADS) m = wfm::jmin(wfli::cell_timestep(d, i), m);
     const double v = block_min(m, red);
     if (threadIdx.x == 0) *d.dt_min = wfli::finish_timestep(v);
 }
@@ -88,11 +88,12 @@ __global__ void li_land_depth_kernel(wfli::LiLand L, LiDev R, wfli::LiRiverBC B,
 }
 
 // min(river minimum, land minimum), each 60 s when infinite (surface_staggered_scheme.jl:
-// 1171-1173)
+// 1171-1173); the river minimum covers its real cells, not the ghost cells (:1004-1020 loops
+// over parameters.n, the river cells without the ghosts)
 __global__ void li_domain_dt_kernel(wfli::LiLand L, LiDev R) {
     __shared__ double red[LI_DT_THREADS];
     double m = wfm::from_bits(INF_BITS);
-    for (int64_t i = threadIdx.x; i < R.n; i += LI_DT_THREADS) m = wfm::jmin(wfli::cell_timestep(R, i), m);
+    for (int64_t i = threadIdx.x; i < R.n_dt; i += LI_DT_THREADS) m = wfm::jmin(wfli::cell_timestep(R, i), m);
     const double dt_river = wfli::finish_timestep(block_min(m, red));
     m = wfm::from_bits(INF_BITS);
     for (int64_t i = threadIdx.x; i < L.n; i += LI_DT_THREADS) m = wfm::jmin(wfli::land_timestep(L, i), m);
@@ -196,6 +197,7 @@ int li_upload_river(LiOwner* o, LiDev& d, int64_t n, int64_t n_active, int64_t n
     d.n = n;
     d.n_active = n_active;
     d.n_edges = n_edges;
+    d.n_dt = n;
     d.h_thresh = h_thresh;
     d.alpha = alpha;
     d.froude = froude_limit;
@@ -304,6 +306,12 @@ void wf_li_river_destroy(WfLiRiver* r) {
     if (!r) return;
     li_release(r);
     delete r;
+}
+
+int32_t wf_li_river_set_timestep_cells(WfLiRiver* r, int64_t n_cells) {
+    if (!r || n_cells < 0 || n_cells > r->d.n) return li_fail(r, WF_ERR_INVALID, "cell count out of range");
+    r->d.n_dt = n_cells;
+    return WF_OK;
 }
 
 int32_t wf_li_river_set_inwater(WfLiRiver* r, const double* inwater) {
@@ -454,6 +462,7 @@ int32_t wf_li_domain_create(const WfLiLandGrid* land, const WfLiRiverNetwork* ri
         wf_li_domain_destroy(d);
         return rc;
     }
+    d->R.n_dt = rv.n_active;  // the river's stable time step over its real cells
     L.ixu = p_ixu;
     L.ixd = p_ixd;
     L.iyu = p_iyu;

@@ -20,10 +20,10 @@ constexpr double GRAVITY = 9.80665;  // Wflow.GRAVITATIONAL_ACCELERATION (Wflow.
 
 // A river network on a staggered grid, all arrays in device (or, for a host build, host)
 // memory. Cells 0..n_active-1 are updated; cells n_active..n-1 are boundary cells of fixed
-// depth. Edge k runs from cell src[k] to cell dst[k]; in_ptr/in_edge and out_ptr/out_edge are
+// depth; the stable time step is the minimum over cells 0..n_dt-1. Edge k runs from cell src[k] to cell dst[k]; in_ptr/in_edge and out_ptr/out_edge are
 // the CSR lists of the edges into and out of each cell, in ascending edge order.
 struct LiNet {
-    int64_t n, n_active, n_edges;
+    int64_t n, n_active, n_edges, n_dt;
     const int64_t *src, *dst;
     const int64_t *in_ptr, *in_edge, *out_ptr, *out_edge;
     const double *zb, *flow_length, *flow_width, *zb_e, *width_e, *length_e, *nsq_e;

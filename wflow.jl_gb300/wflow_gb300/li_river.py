@@ -31,6 +31,7 @@ def _lib():
             "wf_li_river_destroy": (None, [P]),
             "wf_li_river_last_error": (C.c_char_p, [P]),
             "wf_li_river_set_state": (i32, [P, pd, pd]),
+            "wf_li_river_set_timestep_cells": (i32, [P, i64]),
             "wf_li_river_set_inwater": (i32, [P, pd]),
             "wf_li_river_stable_timestep": (i32, [P, pd]),
             "wf_li_river_substep": (i32, [P, d]),
@@ -179,6 +180,11 @@ class LiRiver:
             raise ValueError(f"q must have {self.n_edges} values")
         self._check(self.lib.wf_li_river_set_state(self.h, _pd(hv), None if qv is None else _pd(qv)),
                     "wf_li_river_set_state")
+
+    def set_timestep_cells(self, n_cells):
+        """The stable time step over cells 0..n_cells-1 (default all; a Wflow model's river
+        passes its real cells, the ghost cells coming after them)."""
+        self._check(self.lib.wf_li_river_set_timestep_cells(self.h, int(n_cells)), "wf_li_river_set_timestep_cells")
 
     def set_inwater(self, inwater):
         v = np.ascontiguousarray(inwater, np.float64)
