@@ -77,8 +77,9 @@ typedef struct WfLiDomain WfLiDomain;
 
 /* The land grid: n cells, 0-based neighbour indices (the value n marks outside the grid),
  * river_index[i] the river cell in land cell i or -1. Per cell: x and y length [m], elevation
- * [m], Manning's n, and the effective flow widths at the x and y edges [m] (the cell widths
- * reduced by the river, set_effective_flowwidth!, Wflow/src/utils.jl:604-680). */
+ * [m], Manning's n squared (mannings_n_sq_at_edge of LocalInertialOverlandFlowParameters), and
+ * the effective flow widths at the x and y edges [m] (the cell widths reduced by the river,
+ * set_effective_flowwidth!, Wflow/src/utils.jl:604-680). */
 typedef struct WfLiLandGrid {
     int64_t n;
     const int64_t* ind_x_up;
@@ -89,7 +90,7 @@ typedef struct WfLiLandGrid {
     const double* x_length;
     const double* y_length;
     const double* elevation;
-    const double* mannings_n;
+    const double* mannings_n_sq;
     const double* xwidth_at_edge;
     const double* ywidth_at_edge;
     double theta;

@@ -2045,27 +2045,27 @@ double orc_li_stable_timestep(int64_t n, const double* flow_length, const double
 // :1170-1183): local_inertial_update_fluxes! (:1271-1290; x then y at each cell from the
 // previous discharges), staggered_scheme_river_update! without the depth update (:763-797),
 // local_inertial_update_water_depth! (:1518-1546). Edge parameters of the land grid as its
-// constructor derives them (:894-946): zx_max / zy_max the higher elevation of a cell and its
-// upstream neighbour, Manning's n squared; bankfull storage = depth * width * length (:118).
+// constructor derives them (:929-939): zx_max / zy_max the higher elevation of a cell and its
+// upstream neighbour; bankfull storage = depth * width * length (:118).
 void orc_li_domain_substep(const WfLiLandGrid* L, const WfLiRiverNetwork* R, const double* runoff,
                            const double* external_inflow, const double* abstraction, double dt, OrcLiState* st) {
     const int64_t n = L->n;
-    std::vector<double> zx_max(n, 0.0), zy_max(n, 0.0), nsq(n);
+    std::vector<double> zx_max(n, 0.0), zy_max(n, 0.0);
     for (int64_t i = 0; i < n; ++i) {
         if (L->ind_x_up[i] < n) zx_max[i] = jmax(L->elevation[i], L->elevation[L->ind_x_up[i]]);
         if (L->ind_y_up[i] < n) zy_max[i] = jmax(L->elevation[i], L->elevation[L->ind_y_up[i]]);
-        nsq[i] = L->mannings_n[i] * L->mannings_n[i];
     }
+    const double* nsq = L->mannings_n_sq;
     for (int64_t i = 0; i <= n; ++i) {
         st->qx0[i] = st->qx[i];
         st->qy0[i] = st->qy[i];
     }
     for (int64_t i = 0; i < n; ++i) {
         orc_li_directional_flow(i, n, L->ind_x_up, L->ind_x_down, L->ywidth_at_edge, zx_max.data(), L->x_length,
-                                L->elevation, st->h_land, nsq.data(), L->theta, L->h_thresh, L->froude_limit, dt,
+                                L->elevation, st->h_land, nsq, L->theta, L->h_thresh, L->froude_limit, dt,
                                 st->qx, st->qx0, st->qx_cum);
         orc_li_directional_flow(i, n, L->ind_y_up, L->ind_y_down, L->xwidth_at_edge, zy_max.data(), L->y_length,
-                                L->elevation, st->h_land, nsq.data(), L->theta, L->h_thresh, L->froude_limit, dt,
+                                L->elevation, st->h_land, nsq, L->theta, L->h_thresh, L->froude_limit, dt,
                                 st->qy, st->qy0, st->qy_cum);
     }
     li_river_edges(R->n_edges, R->src, R->dst, R->zb, R->zb_edge, R->width_edge, R->length_edge,

@@ -218,7 +218,7 @@ def random_land_domain(seed, nx=36, ny=28):
     ywidth[rng.random(n) < 0.03] = 0.0
     land = dict(ind_x_up=ind_x_up, ind_x_down=ind_x_down, ind_y_up=ind_y_up, ind_y_down=ind_y_down,
                 river_index=river_index, x_length=x_length, y_length=y_length, elevation=elevation,
-                mannings_n=mannings_n, xwidth_at_edge=xwidth, ywidth_at_edge=ywidth, theta=0.8, h_thresh=1e-3,
+                mannings_n_sq=mannings_n * mannings_n, xwidth_at_edge=xwidth, ywidth_at_edge=ywidth, theta=0.8, h_thresh=1e-3,
                 alpha=0.7, froude_limit=True)
     river = dict(n_active=nra, src=src, dst=dst, zb=zb, flow_length=flow_length, flow_width=flow_width,
                  bankfull_depth=bankfull_depth, zb_edge=zb_e, width_edge=w_e, length_edge=l_e,

@@ -89,12 +89,12 @@ struct HostDomain {
     wfli::LiNet R{};
     wfli::LiRiverBC B{};
     std::vector<int64_t> ip, ie, op, oe;
-    std::vector<double> zx_max, zy_max, nsq, bankfull, zero;
+    std::vector<double> zx_max, zy_max, bankfull, zero;
 };
 
 static void host_domain(HostDomain& h, const WfLiLandGrid* g, const WfLiRiverNetwork* r, const double* runoff,
                         const double* ext, const double* abstraction, HostLiState* st) {
-    wfli::land_edge_parameters(g->n, g->ind_x_up, g->ind_y_up, g->elevation, g->mannings_n, h.zx_max, h.zy_max, h.nsq);
+    wfli::land_edge_parameters(g->n, g->ind_x_up, g->ind_y_up, g->elevation, h.zx_max, h.zy_max);
     wfli::bankfull_storage(r->n, r->bankfull_depth, r->flow_width, r->flow_length, h.bankfull);
     wfli::build_csr(r->n, r->n_edges, r->src, r->dst, h.ip, h.ie, h.op, h.oe);
     h.zero.assign(r->n, 0.0);
@@ -108,7 +108,7 @@ static void host_domain(HostDomain& h, const WfLiLandGrid* g, const WfLiRiverNet
     L.xl = g->x_length;
     L.yl = g->y_length;
     L.z = g->elevation;
-    L.nsq = h.nsq.data();
+    L.nsq = g->mannings_n_sq;
     L.xw = g->xwidth_at_edge;
     L.yw = g->ywidth_at_edge;
     L.zx_max = h.zx_max.data();

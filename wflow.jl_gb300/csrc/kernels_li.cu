@@ -400,7 +400,7 @@ int32_t wf_li_domain_create(const WfLiLandGrid* land, const WfLiRiverNetwork* ri
     const int64_t n = ld.n;
     if (n <= 0) return li_fail(nullptr, WF_ERR_INVALID, "land cell count must be positive");
     if (!ld.ind_x_up || !ld.ind_x_down || !ld.ind_y_up || !ld.ind_y_down || !ld.river_index || !ld.x_length ||
-        !ld.y_length || !ld.elevation || !ld.mannings_n || !ld.xwidth_at_edge || !ld.ywidth_at_edge)
+        !ld.y_length || !ld.elevation || !ld.mannings_n_sq || !ld.xwidth_at_edge || !ld.ywidth_at_edge)
         return li_fail(nullptr, WF_ERR_INVALID, "missing input array");
     if (!(ld.alpha > 0.0)) return li_fail(nullptr, WF_ERR_INVALID, "alpha must be positive");
     std::vector<int32_t> seen(rv.n_active, 0);
@@ -417,8 +417,8 @@ int32_t wf_li_domain_create(const WfLiLandGrid* land, const WfLiRiverNetwork* ri
     }
     for (int64_t r = 0; r < rv.n_active; ++r)
         if (!seen[r]) return li_fail(nullptr, WF_ERR_INVALID, "an active river cell lies in no land cell");
-    std::vector<double> zx_max, zy_max, nsq, bankfull;
-    wfli::land_edge_parameters(n, ld.ind_x_up, ld.ind_y_up, ld.elevation, ld.mannings_n, zx_max, zy_max, nsq);
+    std::vector<double> zx_max, zy_max, bankfull;
+    wfli::land_edge_parameters(n, ld.ind_x_up, ld.ind_y_up, ld.elevation, zx_max, zy_max);
     wfli::bankfull_storage(rv.n, rv.bankfull_depth, rv.flow_width, rv.flow_length, bankfull);
 
     WfLiDomain* d = new WfLiDomain();
@@ -430,7 +430,7 @@ int32_t wf_li_domain_create(const WfLiLandGrid* land, const WfLiRiverNetwork* ri
     L.froude = ld.froude_limit;
     int64_t *p_ixu, *p_ixd, *p_iyu, *p_iyd, *p_riv;
     double *p_xl, *p_yl, *p_z, *p_nsq, *p_xw, *p_yw, *p_zx, *p_zy, *p_bd, *p_bs;
-    const double *c_nsq = nsq.data(), *c_zx = zx_max.data(), *c_zy = zy_max.data(), *c_bs = bankfull.data();
+    const double *c_zx = zx_max.data(), *c_zy = zy_max.data(), *c_bs = bankfull.data();
     if ((rc = li_open(d, device)) ||
         (rc = li_upload_river(d, d->R, rv.n, rv.n_active, rv.n_edges, rv.src, rv.dst, rv.zb, rv.flow_length,
                               rv.flow_width, h_river, rv.zb_edge, rv.width_edge, rv.length_edge,
@@ -439,7 +439,7 @@ int32_t wf_li_domain_create(const WfLiLandGrid* land, const WfLiRiverNetwork* ri
         (rc = li_upload(d, &p_iyu, ld.ind_y_up, n)) || (rc = li_upload(d, &p_iyd, ld.ind_y_down, n)) ||
         (rc = li_upload(d, &p_riv, ld.river_index, n)) || (rc = li_upload(d, &p_xl, ld.x_length, n)) ||
         (rc = li_upload(d, &p_yl, ld.y_length, n)) || (rc = li_upload(d, &p_z, ld.elevation, n)) ||
-        (rc = li_upload(d, &p_nsq, c_nsq, n)) || (rc = li_upload(d, &p_xw, ld.xwidth_at_edge, n)) ||
+        (rc = li_upload(d, &p_nsq, ld.mannings_n_sq, n)) || (rc = li_upload(d, &p_xw, ld.xwidth_at_edge, n)) ||
         (rc = li_upload(d, &p_yw, ld.ywidth_at_edge, n)) || (rc = li_upload(d, &p_zx, c_zx, n)) ||
         (rc = li_upload(d, &p_zy, c_zy, n)) || (rc = li_upload(d, &p_bd, rv.bankfull_depth, rv.n)) ||
         (rc = li_upload(d, &p_bs, c_bs, rv.n)) || (rc = li_upload<double>(d, &d->runoff, nullptr, n)) ||

@@ -214,19 +214,16 @@ WF_HD double land_timestep(const LiLand& L, int64_t i) {
                           : wfm::from_bits(0x7ff0000000000000ULL);
 }
 
-// Edge parameters of the land grid as LocalInertialOverlandFlowParameters derives them
-// (surface_staggered_scheme.jl:894-946): the higher elevation of a cell and its upstream
-// neighbour in x and y (0 without one) and Manning's n squared. Host code.
+// Edge elevations of the land grid as LocalInertialOverlandFlowParameters derives them
+// (surface_staggered_scheme.jl:929-939): the higher elevation of a cell and its upstream
+// neighbour in x and y (0 without one). Host code.
 inline void land_edge_parameters(int64_t n, const int64_t* ind_x_up, const int64_t* ind_y_up, const double* elevation,
-                                 const double* mannings_n, std::vector<double>& zx_max, std::vector<double>& zy_max,
-                                 std::vector<double>& nsq) {
+                                 std::vector<double>& zx_max, std::vector<double>& zy_max) {
     zx_max.assign(n, 0.0);
     zy_max.assign(n, 0.0);
-    nsq.assign(n, 0.0);
     for (int64_t i = 0; i < n; ++i) {
         if (ind_x_up[i] < n) zx_max[i] = wfm::jmax(elevation[i], elevation[ind_x_up[i]]);
         if (ind_y_up[i] < n) zy_max[i] = wfm::jmax(elevation[i], elevation[ind_y_up[i]]);
-        nsq[i] = mannings_n[i] * mannings_n[i];
     }
 }
 

@@ -70,7 +70,7 @@ _PL, _PD = C.POINTER(C.c_int64), C.POINTER(C.c_double)
 class WfLiLandGrid(C.Structure):
     _fields_ = [("n", C.c_int64)] + [(f, _PL) for f in ("ind_x_up", "ind_x_down", "ind_y_up", "ind_y_down",
                                                          "river_index")] + \
-               [(f, _PD) for f in ("x_length", "y_length", "elevation", "mannings_n", "xwidth_at_edge",
+               [(f, _PD) for f in ("x_length", "y_length", "elevation", "mannings_n_sq", "xwidth_at_edge",
                                    "ywidth_at_edge")] + \
                [("theta", C.c_double), ("h_thresh", C.c_double), ("alpha", C.c_double), ("froude_limit", C.c_int32)]
 
@@ -83,7 +83,7 @@ class WfLiRiverNetwork(C.Structure):
 
 
 LAND_INT = ("ind_x_up", "ind_x_down", "ind_y_up", "ind_y_down", "river_index")
-LAND_DBL = ("x_length", "y_length", "elevation", "mannings_n", "xwidth_at_edge", "ywidth_at_edge")
+LAND_DBL = ("x_length", "y_length", "elevation", "mannings_n_sq", "xwidth_at_edge", "ywidth_at_edge")
 RIVER_INT = ("src", "dst")
 RIVER_CELL = ("zb", "flow_length", "flow_width", "bankfull_depth")
 RIVER_EDGE = ("zb_edge", "width_edge", "length_edge", "mannings_n_sq_edge")
