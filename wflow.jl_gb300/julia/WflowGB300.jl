@@ -312,4 +312,177 @@ function sync_mirrors!(gpu::GpuStep, model)
     return nothing
 end
 
+# ---- local-inertial routing (include/wflow_gb300_li.h) -----------------------------------------
+
+struct WfLiLandGrid
+    n::Int64
+    ind_x_up::Ptr{Int64}
+    ind_x_down::Ptr{Int64}
+    ind_y_up::Ptr{Int64}
+    ind_y_down::Ptr{Int64}
+    river_index::Ptr{Int64}
+    x_length::Ptr{Float64}
+    y_length::Ptr{Float64}
+    elevation::Ptr{Float64}
+    mannings_n_sq::Ptr{Float64}
+    xwidth_at_edge::Ptr{Float64}
+    ywidth_at_edge::Ptr{Float64}
+    theta::Float64
+    h_thresh::Float64
+    alpha::Float64
+    froude_limit::Int32
+end
+
+struct WfLiRiverNetwork
+    n::Int64
+    n_active::Int64
+    n_edges::Int64
+    src::Ptr{Int64}
+    dst::Ptr{Int64}
+    zb::Ptr{Float64}
+    flow_length::Ptr{Float64}
+    flow_width::Ptr{Float64}
+    bankfull_depth::Ptr{Float64}
+    zb_edge::Ptr{Float64}
+    width_edge::Ptr{Float64}
+    length_edge::Ptr{Float64}
+    mannings_n_sq_edge::Ptr{Float64}
+    h_thresh::Float64
+    alpha::Float64
+    froude_limit::Int32
+end
+
+# enum WfLiDomainField
+const LI_LAND_H, LI_LAND_STORAGE, LI_LAND_ERROR, LI_LAND_QX, LI_LAND_QY, LI_LAND_QX_AVERAGE,
+      LI_LAND_QY_AVERAGE, LI_RIVER_H, LI_RIVER_STORAGE, LI_RIVER_Q, LI_RIVER_Q_AVERAGE,
+      LI_RIVER_ABSTRACTION_CUMULATIVE = Int32.(0:11)
+
+mutable struct GpuLocalInertial
+    handle::Ptr{Cvoid}
+    keep::Vector{Any}
+    n_land::Int
+    n_river::Int       # river cells with the ghost cells after them
+    n_edges::Int
+end
+
+li_check(st, h, what) = st == 0 || error("$what failed ($st): " *
+                                         unsafe_string(ccall((:wf_li_domain_last_error, LIB), Cstring,
+                                                             (Ptr{Cvoid},), h)))
+
+# 0-based copy of a 1-based index vector (the value n + 1, outside, becomes n)
+zero_based(v) = Int64.(v) .- 1
+
+# a river cell vector padded to the ghost cells (their lengths and widths are not used; their
+# inflows are zero)
+pad_river(v, n_total) = vcat(Float64.(v), ones(n_total - length(v)))
+pad_zero(v, n_total) = vcat(Float64.(v), zeros(n_total - length(v)))
+
+"""
+    GpuLocalInertial(model)
+
+The land grid and river of a model with `land_routing = "local_inertial"` and `river_routing =
+"local_inertial"` (no reservoirs, no 1D floodplain) as a `wf_li_domain` handle: the land edge
+indices, river locations, lengths, elevation, Manning's n squared and effective widths of
+`LocalInertialOverlandFlowParameters`, the river network and `RiverFlowStaggeredParameters`,
+and the current state (`wf_li_domain_set_state`).
+"""
+function GpuLocalInertial(model)
+    (; domain, routing, config) = model
+    m = config.model
+    (m.land_routing == Wflow.RoutingType.local_inertial &&
+     m.river_routing == Wflow.RoutingType.local_inertial) ||
+        error("GpuLocalInertial needs local-inertial land and river routing")
+    (m.reservoir__flag || m.floodplain_1d__flag) &&
+        error("GpuLocalInertial: reservoirs and the 1D floodplain are not supported")
+    land, river = routing.overland_flow, routing.river_flow
+    lp, rp = land.parameters, river.parameters
+    ei = domain.land.network.edge_indices
+    riv_loc = domain.land.parameters.river_location
+    riv_idx = domain.land.network.river_indices
+    n = lp.n
+    n_total = length(river.variables.h)
+    keep = Any[
+        zero_based(ei.ind_x_up), zero_based(ei.ind_x_down), zero_based(ei.ind_y_up), zero_based(ei.ind_y_down),
+        Int64[riv_loc[i] ? riv_idx[i] - 1 : -1 for i in 1:n],
+        Float64.(domain.land.parameters.x_length), Float64.(domain.land.parameters.y_length), lp.z,
+        lp.mannings_n_sq_at_edge, lp.xwidth_at_edge, lp.ywidth_at_edge,
+    ]
+    g = WfLiLandGrid(n, pointer(keep[1]), pointer(keep[2]), pointer(keep[3]), pointer(keep[4]),
+        pointer(keep[5]), pointer(keep[6]), pointer(keep[7]), pointer(keep[8]), pointer(keep[9]),
+        pointer(keep[10]), pointer(keep[11]), lp.theta, lp.h_thresh, land.timestepping.alpha_coefficient,
+        Int32(lp.froude_limit))
+    nae = domain.river.network.nodes_at_edge
+    rk = Any[
+        zero_based(nae.src), zero_based(nae.dst), Float64.(rp.zb),
+        pad_river(domain.river.parameters.flow_length, n_total),
+        pad_river(domain.river.parameters.flow_width, n_total), pad_river(rp.bankfull_depth, n_total),
+        rp.zb_at_edge, rp.flow_width_at_edge, rp.flow_length_at_edge, rp.mannings_n_sq_at_edge,
+        copy(river.variables.h),
+    ]
+    length(rk[3]) == n_total || error("river bed levels must cover the ghost cells")
+    append!(keep, rk)
+    r = WfLiRiverNetwork(n_total, rp.n, rp.n_edges, pointer(rk[1]), pointer(rk[2]), pointer(rk[3]),
+        pointer(rk[4]), pointer(rk[5]), pointer(rk[6]), pointer(rk[7]), pointer(rk[8]), pointer(rk[9]),
+        pointer(rk[10]), rp.h_thresh, river.timestepping.alpha_coefficient, Int32(rp.froude_limit))
+    handle = Ref{Ptr{Cvoid}}(C_NULL)
+    st = GC.@preserve keep ccall((:wf_li_domain_create, LIB), Int32,
+        (Ref{WfLiLandGrid}, Ref{WfLiRiverNetwork}, Ptr{Float64}, Int32, Ref{Ptr{Cvoid}}),
+        g, r, rk[11], Int32(0), handle)
+    li_check(st, C_NULL, "wf_li_domain_create")
+    gpu = GpuLocalInertial(handle[], keep, n, n_total, rp.n_edges)
+    finalizer(x -> ccall((:wf_li_domain_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.handle), gpu)
+    lv = land.variables
+    st = ccall((:wf_li_domain_set_state, LIB), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        gpu.handle, lv.h, river.variables.h, lv.qx, lv.qy, river.variables.q)
+    li_check(st, gpu.handle, "wf_li_domain_set_state")
+    return gpu
+end
+
+li_get!(dst, gpu::GpuLocalInertial, field) =
+    li_check(ccall((:wf_li_domain_get, LIB), Int32, (Ptr{Cvoid}, Int32, Ptr{Float64}), gpu.handle, field, dst),
+        gpu.handle, "wf_li_domain_get")
+
+"""
+    gpu_update_local_inertial!(gpu::GpuLocalInertial, model, dt)
+
+In place of `update_overland_flow_model!(overland, river, domain, clock, dt)`
+(Wflow/src/routing/surface/surface_staggered_scheme.jl:1153-1193): uploads the runoff, external
+inflow and abstraction, runs the model step's sub-steps on the GPU and copies the land and river
+variables back into the model.
+"""
+function gpu_update_local_inertial!(gpu::GpuLocalInertial, model, dt)
+    land, river = model.routing.overland_flow, model.routing.river_flow
+    rbc = river.boundary_conditions
+    ext = pad_zero(rbc.external_inflow, gpu.n_river)
+    abst = pad_zero(rbc.abstraction, gpu.n_river)
+    st = ccall((:wf_li_domain_set_inputs, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        gpu.handle, land.boundary_conditions.runoff, ext, abst)
+    li_check(st, gpu.handle, "wf_li_domain_set_inputs")
+    li_check(ccall((:wf_li_domain_step, LIB), Int32, (Ptr{Cvoid}, Float64, Ptr{Int64}), gpu.handle, dt, C_NULL),
+        gpu.handle, "wf_li_domain_step")
+    lv, rv = land.variables, river.variables
+    n = gpu.n_land
+    for (field, v) in ((LI_LAND_H, lv.h), (LI_LAND_STORAGE, lv.storage), (LI_LAND_ERROR, lv.error))
+        li_get!(v, gpu, field)
+    end
+    tmp = Vector{Float64}(undef, n)
+    for (field, v) in ((LI_LAND_QX, lv.qx), (LI_LAND_QY, lv.qy), (LI_LAND_QX_AVERAGE, lv.qx_average),
+                       (LI_LAND_QY_AVERAGE, lv.qy_average))
+        li_get!(tmp, gpu, field)
+        v[1:n] .= tmp      # the n + 1-th value (outside the grid) stays zero
+    end
+    li_get!(rv.h, gpu, LI_RIVER_H)
+    rs = Vector{Float64}(undef, gpu.n_river)
+    li_get!(rs, gpu, LI_RIVER_STORAGE)
+    rv.storage .= rs[1:length(rv.storage)]
+    li_get!(rv.q, gpu, LI_RIVER_Q)
+    li_get!(rv.q_average, gpu, LI_RIVER_Q_AVERAGE)
+    li_get!(rs, gpu, LI_RIVER_ABSTRACTION_CUMULATIVE)
+    rbc.actual_external_abstraction_cumulative .= rs[1:length(rbc.actual_external_abstraction_cumulative)]
+    # average_flow_vars! (surface_kinwave.jl:283-290)
+    rbc.actual_external_abstraction_average .= rbc.actual_external_abstraction_cumulative ./ dt
+    return nothing
+end
+
 end # module
