@@ -173,3 +173,26 @@ def test_land_domain_dry_time_step(host_lib):
     m = H(land, river, wet)
     g = 9.80665
     assert m.stable_timestep() == min(60.0, river["alpha"] * river["flow_length"][3] / np.sqrt(g * 0.4))
+
+
+def test_bench_grid_is_valid_and_matches_oracle(host_lib):
+    """The throughput grid of wflow_gb300.li_bench: every river cell in one land cell, edges in
+    range, and its first sub-steps on the host build equal to the oracle's."""
+    from li_cases import OracleLiDomain
+    from wflow_gb300 import li_bench
+    land, river, h_river, h_land, runoff = li_bench.grid(96, 100)
+    ri, nra = land["river_index"], river["n_active"]
+    assert sorted(ri[ri >= 0].tolist()) == list(range(nra))
+    assert river["src"].max() < nra and river["dst"].max() < len(river["zb"])
+    a = OracleLiDomain(land, river, h_river)
+    b = _host_domain_class(host_lib)(land, river, h_river)
+    for m in (a, b):
+        m.set_state(h_land, h_river)
+        m.set_inputs(runoff)
+    for _ in range(5):
+        dt = a.stable_timestep()
+        assert dt == b.stable_timestep()
+        a.substep(dt)
+        b.substep(dt)
+    for f in DOMAIN_FIELDS[:5] + DOMAIN_FIELDS[7:10]:
+        assert np.array_equal(a.get(f), b.get(f)), f
