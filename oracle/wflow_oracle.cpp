@@ -1771,23 +1771,25 @@ void orc_accucapacityflux(const int32_t* ds, const int64_t* order, int64_t n, do
     accucapacityflux(ds, order, n, dt, capacity, material, flux);
 }
 
-// lateral_snow_transport!: snow_out and snow_in [m s-1] of every cell; the graph's upstream
+// lateral_snow_transport!: snow_out and snow_in [m s-1] of every cell, and the snow storage and
+// snow water moved downhill in place (the non-mutating-named accucapacityflux passes its
+// material to accucapacityflux!, routing/utils.jl:144-148, so Wflow's snow states move); the
+// fraction and both capacities come from the states before the move. The graph's upstream
 // lists for the inflow are `ups_ds` (the reservoir-cut lists of the domain; equal to ds
 // without reservoirs).
 void orc_lateral_snow_transport(const int32_t* ds, const int32_t* ups_ds, const int64_t* order, int64_t n, double dt,
-                                const double* slope, const double* snow_storage, const double* snow_water,
-                                double* snow_out, double* snow_in) {
+                                const double* slope, double* snow_storage, double* snow_water, double* snow_out,
+                                double* snow_in) {
     const double TAN80 = 5.67;
     const double snow_storage_max = 10.0;
-    std::vector<double> frac(n), maxflux(n), m1(snow_storage, snow_storage + n), m2(snow_water, snow_water + n),
-        f2(n), cap2(n);
+    std::vector<double> frac(n), maxflux(n), f2(n), cap2(n);
     for (int64_t i = 0; i < n; ++i) {
         frac[i] = jmin(0.5, slope[i] / TAN80) * jmin(1.0, snow_storage[i] / snow_storage_max);
         maxflux[i] = frac[i] * snow_storage[i] / dt;
-        cap2[i] = snow_water[i] * frac[i] / dt;
     }
-    accucapacityflux(ds, order, n, dt, maxflux.data(), m1.data(), snow_out);
-    accucapacityflux(ds, order, n, dt, cap2.data(), m2.data(), f2.data());
+    accucapacityflux(ds, order, n, dt, maxflux.data(), snow_storage, snow_out);
+    for (int64_t i = 0; i < n; ++i) cap2[i] = snow_water[i] * frac[i] / dt;
+    accucapacityflux(ds, order, n, dt, cap2.data(), snow_water, f2.data());
     for (int64_t i = 0; i < n; ++i) snow_out[i] += f2[i];
     std::vector<std::vector<int64_t>> ups(n);  // upstream lists in ascending node order
     for (int64_t i = 0; i < n; ++i)

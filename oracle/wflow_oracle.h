@@ -129,12 +129,14 @@ double orc_kinwave_stable_timestep(const double* q, const double* alpha, const d
 double orc_quantile(double* v, int64_t n, double p);
 
 /* capacity-limited transport over a drainage graph (routing/utils.jl:82-110) and the lateral
- * snow transport built on it (routing/surface/surface_process.jl:1-19) */
+ * snow transport built on it (routing/surface/surface_process.jl:1-19), which moves the snow
+ * storage and snow water in place (accucapacityflux hands its material to accucapacityflux!,
+ * routing/utils.jl:144-148) */
 void orc_accucapacityflux(const int32_t* ds, const int64_t* order, int64_t n, double dt, const double* capacity,
                           double* material, double* flux);
 void orc_lateral_snow_transport(const int32_t* ds, const int32_t* ups_ds, const int64_t* order, int64_t n, double dt,
-                                const double* slope, const double* snow_storage, const double* snow_water,
-                                double* snow_out, double* snow_in);
+                                const double* slope, double* snow_storage, double* snow_water, double* snow_out,
+                                double* snow_in);
 
 /* local-inertial river flow on a staggered grid (surface_process.jl:88-163,
  * surface_staggered_scheme.jl:326-385, 723-760, 1004-1020) */
