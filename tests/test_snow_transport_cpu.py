@@ -12,6 +12,7 @@ domain's snow falls by exactly what left through the pits.
 import ctypes as C
 
 import numpy as np
+import pytest
 
 from wflow_gb300 import synthetic
 import oracle_py as O
@@ -65,3 +66,80 @@ def test_snow_transport_conserves_and_respects_capacity():
     lost = (snow.sum() + water.sum()) - (snow_after.sum() + water_after.sum())
     assert abs(lost - out[pits].sum() * dt) <= 1e-9 * (snow.sum() + water.sum())
     assert not np.array_equal(snow_after, snow)
+
+
+def _setup(seed, size=24):
+    dom = synthetic.make_domain(size, 250.0, seed=seed)
+    rng = np.random.default_rng(seed)
+    n = dom.n_land
+    slope = np.ascontiguousarray(dom.land["slope"] * 50.0)
+    snow = rng.uniform(0.0, 20.0, n)
+    snow[::7] = 0.0
+    water = snow * rng.uniform(0.0, 0.1, n)
+    return dom, slope, snow, water
+
+
+def _order(ds):
+    n = len(ds)
+    indeg = np.zeros(n, np.int64)
+    np.add.at(indeg, ds[ds >= 0], 1)
+    order = list(np.flatnonzero(indeg == 0))
+    k = 0
+    while k < len(order):
+        d = ds[order[k]]
+        if d >= 0:
+            indeg[d] -= 1
+            if indeg[d] == 0:
+                order.append(d)
+        k += 1
+    return np.asarray(order, np.int64)
+
+
+@pytest.fixture(scope="module")
+def snow_host_lib(tmp_path_factory):
+    import shutil
+    import subprocess
+    from pathlib import Path
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    repo = Path(__file__).resolve().parent.parent
+    out = tmp_path_factory.mktemp("snow_host") / "snow_host.so"
+    subprocess.run([cxx, "-O2", "-ffp-contract=off", "-std=c++17", "-shared", "-fPIC",
+                    "-I", str(repo / "wflow.jl_gb300" / "csrc"), str(repo / "tests" / "snow_host_driver.cpp"),
+                    "-o", str(out)], check=True)
+    return C.CDLL(str(out))
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_host_build_bit_identical(snow_host_lib, seed):
+    """The product's per-cell arithmetic (snow_scheme.cuh) on its level schedule equals the
+    oracle's sequential sweep bit for bit: states, snow_out and snow_in."""
+    dom, slope, snow, water = _setup(seed)
+    ds = np.ascontiguousarray(dom.land["land_downstream"], np.int32)
+    order = _order(ds)
+    n, dt = len(ds), 86400.0
+    out_o, in_o, s_o, w_o = transport(dom, slope, snow, water, dt)
+    s_h, w_h, out_h, in_h = np.array(snow), np.array(water), np.zeros(n), np.zeros(n)
+    p = lambda a, t=C.c_double: a.ctypes.data_as(C.POINTER(t))  # noqa: E731
+    snow_host_lib.host_snow_transport(C.c_int64(n), p(ds, C.c_int32), p(order, C.c_int64), p(ds, C.c_int32),
+                                      p(slope), C.c_double(dt), p(s_h), p(w_h), p(out_h), p(in_h))
+    for a, b in ((s_o, s_h), (w_o, w_h), (out_o, out_h), (in_o, in_h)):
+        assert np.array_equal(a, b)
+
+
+def test_create_rejects_bad_orders():
+    from wflow_gb300 import build
+    from wflow_gb300.snow_transport import SnowTransport
+    build.build_all()
+    dom, slope, _, _ = _setup(5, size=12)
+    ds = np.ascontiguousarray(dom.land["land_downstream"], np.int32)
+    order = _order(ds)
+    with pytest.raises(RuntimeError, match="not a permutation"):
+        SnowTransport(ds, np.concatenate([order[:-1], order[:1]]), slope)
+    with pytest.raises(RuntimeError, match="after its downstream cell"):
+        SnowTransport(ds, order[::-1].copy(), slope)
+    bad = ds.copy()
+    bad[0] = len(ds)
+    with pytest.raises(RuntimeError, match="out of range"):
+        SnowTransport(bad, order, slope)

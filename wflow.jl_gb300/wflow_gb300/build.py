@@ -31,6 +31,7 @@ CUDA_UNITS = [
     ("kernels_split.cu", ["-prec-div=false"]),
     ("kernels_adaptive.cu", ["--fmad=false"]),
     ("kernels_li.cu", ["--fmad=false"]),
+    ("kernels_snow.cu", ["--fmad=false"]),
 ]
 
 
