@@ -38,6 +38,24 @@ int32_t wf_snow_transport_run(WfSnowTransport* t, double dt, double* snow_storag
 /* Number of topological levels (kernel launches per material sweep). */
 int64_t wf_snow_transport_levels(const WfSnowTransport* t);
 
+/* ---- HBV glacier ----------------------------------------------------------------------------
+ * update_glacier_model! (Wflow/src/glacier/glacier.jl:122-154, glacier_hbv in
+ * glacier/glacier_process.jl): snow on the glacier part of a cell turns into firn at
+ * snow_to_ice_fraction of the snow per step (at most maximum_snow_to_ice_rate), and the glacier
+ * melts by degree-day above the melt threshold once the snow is nearly gone. Per cell: glacier
+ * fraction, melt threshold temperature [K], degree-day factor [m K-1 s-1], snow-to-ice fraction
+ * [s-1]; maximum_snow_to_ice_rate [m s-1]. */
+typedef struct WfGlacier WfGlacier;
+int32_t wf_glacier_create(int64_t n, const double* glacier_fraction, const double* temperature_threshold_melt,
+                          const double* degree_day_factor, const double* snow_to_ice_fraction,
+                          double maximum_snow_to_ice_rate, int32_t device, WfGlacier** out);
+void wf_glacier_destroy(WfGlacier* g);
+const char* wf_glacier_last_error(const WfGlacier* g);
+/* One step: temperature [K]; snow_storage and glacier_store [m] updated in place; glacier_melt
+ * [m s-1] written. Host arrays of n values. */
+int32_t wf_glacier_run(WfGlacier* g, double dt, const double* temperature, double* snow_storage,
+                       double* glacier_store, double* glacier_melt);
+
 #ifdef __cplusplus
 }
 #endif

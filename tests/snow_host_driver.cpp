@@ -57,3 +57,17 @@ extern "C" void host_snow_transport(int64_t n, const int32_t* ds, const int64_t*
     for (int64_t i = 0; i < n; ++i) wfsn::out_cell(d, i);
     for (int64_t i = 0; i < n; ++i) wfsn::in_cell(d, i);
 }
+
+// the glacier kernel's loop body over n cells
+extern "C" void host_glacier(int64_t n, const double* fraction, const double* ttm, const double* cfmax,
+                             const double* sifrac, double max_rate, double dt, const double* temperature,
+                             double* snow_storage, double* glacier_store, double* glacier_melt) {
+    for (int64_t i = 0; i < n; ++i) {
+        double snow, store, melt;
+        wfsn::glacier_hbv(fraction[i], glacier_store[i], snow_storage[i], temperature[i], ttm[i], cfmax[i], sifrac[i],
+                          max_rate, dt, &snow, &store, &melt);
+        snow_storage[i] = snow;
+        glacier_store[i] = store;
+        glacier_melt[i] = melt;
+    }
+}

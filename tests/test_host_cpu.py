@@ -19,7 +19,7 @@ def lib():
 @pytest.mark.parametrize("header,must", [("wflow_gb300.h", ("wf_create", "wf_step")),
                                           ("wflow_gb300_nc.h", ("wf_nc_open", "wf_nc_get")),
                                           ("wflow_gb300_li.h", ("wf_li_river_create", "wf_li_river_step")),
-                                          ("wflow_gb300_snow.h", ("wf_snow_transport_create", "wf_snow_transport_run"))])
+                                          ("wflow_gb300_snow.h", ("wf_snow_transport_create", "wf_snow_transport_run", "wf_glacier_run"))])
 def test_header_symbols_exported(lib, header, must):
     names = abi.header_symbols(header)
     assert all(m in names for m in must)

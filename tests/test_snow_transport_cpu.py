@@ -143,3 +143,41 @@ def test_create_rejects_bad_orders():
     bad[0] = len(ds)
     with pytest.raises(RuntimeError, match="out of range"):
         SnowTransport(bad, order, slope)
+
+
+def glacier_case(seed, n=5000):
+    """Glacier inputs with the branches of glacier_hbv: no glacier, the snow-to-ice rate capped,
+    temperatures below and above the melt threshold, snow above and below 10 mm."""
+    rng = np.random.default_rng(seed)
+    frac = rng.uniform(0.0, 1.0, n) * (rng.random(n) < 0.7)
+    ttm = 273.15 + rng.uniform(-1.0, 1.0, n)
+    cfmax = rng.uniform(2.0, 6.0, n) * 1e-3 / 86400.0
+    sifrac = rng.uniform(0.0, 0.005, n) / 86400.0
+    temp = 273.15 + rng.uniform(-10.0, 10.0, n)
+    snow = rng.uniform(0.0, 0.5, n) * (rng.random(n) < 0.6)
+    store = rng.uniform(0.0, 50.0, n)
+    return frac, ttm, cfmax, sifrac, 8e-3 / 86400.0, temp, snow, store
+
+
+def oracle_glacier(frac, ttm, cfmax, sifrac, max_rate, dt, temp, snow, store):
+    out = np.empty(4)
+    s, g, m = np.empty_like(snow), np.empty_like(store), np.empty_like(snow)
+    for i in range(len(snow)):
+        O.lib().orc_glacier_hbv(C.c_double(frac[i]), C.c_double(store[i]), C.c_double(snow[i]), C.c_double(temp[i]),
+                                C.c_double(ttm[i]), C.c_double(cfmax[i]), C.c_double(sifrac[i]), C.c_double(max_rate),
+                                C.c_double(dt), out.ctypes.data_as(C.POINTER(C.c_double)))
+        s[i], g[i], m[i] = out[0], out[2], out[3]
+    return s, g, m
+
+
+def test_glacier_host_build_bit_identical(snow_host_lib):
+    frac, ttm, cfmax, sifrac, max_rate, temp, snow, store = glacier_case(1)
+    dt = 86400.0
+    s_o, g_o, m_o = oracle_glacier(frac, ttm, cfmax, sifrac, max_rate, dt, temp, snow, store)
+    s_h, g_h, m_h = snow.copy(), store.copy(), np.zeros_like(snow)
+    p = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    snow_host_lib.host_glacier(C.c_int64(len(snow)), p(frac), p(ttm), p(cfmax), p(sifrac), C.c_double(max_rate),
+                               C.c_double(dt), p(temp), p(s_h), p(g_h), p(m_h))
+    for a, b in ((s_o, s_h), (g_o, g_h), (m_o, m_h)):
+        assert np.array_equal(a, b)
+    assert (m_o > 0).any() and (m_o == 0).any() and (frac == 0).any()

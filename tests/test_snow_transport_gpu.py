@@ -36,3 +36,17 @@ def test_snow_transport_matches_oracle(gpu_lib, seed, size):
                        ("snow_in", in_o, in_g)):
         assert _max_rel(a, b) <= 1e-12, name
     t.close()
+
+
+def test_glacier_matches_oracle(gpu_lib):
+    from test_snow_transport_cpu import glacier_case, oracle_glacier
+    from wflow_gb300.snow_transport import Glacier
+    frac, ttm, cfmax, sifrac, max_rate, temp, snow, store = glacier_case(2, n=20000)
+    dt = 86400.0
+    s_o, g_o, m_o = oracle_glacier(frac, ttm, cfmax, sifrac, max_rate, dt, temp, snow, store)
+    g = Glacier(frac, ttm, cfmax, sifrac, max_rate)
+    s_g, g_g = snow.copy(), store.copy()
+    m_g = g.run(dt, temp, s_g, g_g)
+    for name, a, b in (("snow_storage", s_o, s_g), ("glacier_store", g_o, g_g), ("glacier_melt", m_o, m_g)):
+        assert _max_rel(a, b) <= 1e-12, name
+    g.close()

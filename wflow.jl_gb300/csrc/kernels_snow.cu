@@ -1,4 +1,6 @@
-// kernels_snow.cu -- lateral snow transport on the GPU (include/wflow_gb300_snow.h).
+// kernels_snow.cu -- lateral snow transport and the HBV glacier on the GPU
+// (include/wflow_gb300_snow.h). The glacier is one element-wise kernel over the cells
+// (glacier_hbv in snow_scheme.cuh).
 //
 // The capacities of all cells come first (from the states before the move); then the cells are
 // swept level by level from the leaves (a cell's level is one more than its highest upstream
@@ -37,6 +39,24 @@ __global__ void snow_out_kernel(SnowNet d) {
         wfsn::out_cell(d, i);
 }
 
+struct GlacierDev {
+    int64_t n;
+    const double *fraction, *ttm, *cfmax, *sifrac, *temperature;
+    double *snow, *store, *melt;
+    double max_rate;
+};
+
+__global__ void glacier_kernel(GlacierDev g, double dt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+        double snow, store, melt;
+        wfsn::glacier_hbv(g.fraction[i], g.store[i], g.snow[i], g.temperature[i], g.ttm[i], g.cfmax[i], g.sifrac[i],
+                          g.max_rate, dt, &snow, &store, &melt);
+        g.snow[i] = snow;
+        g.store[i] = store;
+        g.melt[i] = melt;
+    }
+}
+
 __global__ void snow_in_kernel(SnowNet d) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x)
         wfsn::in_cell(d, i);
@@ -50,6 +70,13 @@ int grid_of(int64_t n) {
 thread_local std::string g_snow_error;
 
 }  // namespace
+
+struct WfGlacier {
+    GlacierDev g{};
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    std::string err;
+};
 
 struct WfSnowTransport {
     SnowNet d{};
@@ -217,6 +244,97 @@ int32_t wf_snow_transport_run(WfSnowTransport* t, double dt, double* snow_storag
         cudaMemcpyAsync(snow_in, d.snow_in, bytes, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
         cudaStreamSynchronize(t->stream) != cudaSuccess)
         return snow_fail(t, WF_ERR_CUDA, "snow transport failed");
+    return WF_OK;
+}
+
+// ---------------------------------------------------------------- glacier ------------------
+
+namespace {
+
+int glacier_fail(WfGlacier* g, int code, const std::string& msg) {
+    if (g) g->err = msg;
+    else g_snow_error = msg;
+    return code;
+}
+
+int glacier_alloc(WfGlacier* g, double** p, const double* src, int64_t n) {
+    if (cudaMalloc((void**)p, (size_t)n * sizeof(double)) != cudaSuccess)
+        return glacier_fail(g, WF_ERR_NOMEM, "cudaMalloc failed");
+    g->allocs.push_back(*p);
+    if (src && cudaMemcpy(*p, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+        return glacier_fail(g, WF_ERR_CUDA, "cudaMemcpy failed");
+    return WF_OK;
+}
+
+}  // namespace
+
+const char* wf_glacier_last_error(const WfGlacier* g) { return g ? g->err.c_str() : g_snow_error.c_str(); }
+
+void wf_glacier_destroy(WfGlacier* g) {
+    if (!g) return;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    for (void* p : g->allocs) cudaFree(p);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+int32_t wf_glacier_create(int64_t n, const double* glacier_fraction, const double* temperature_threshold_melt,
+                          const double* degree_day_factor, const double* snow_to_ice_fraction,
+                          double maximum_snow_to_ice_rate, int32_t device, WfGlacier** out) {
+    if (!out) return glacier_fail(nullptr, WF_ERR_INVALID, "null output");
+    *out = nullptr;
+    if (n <= 0 || !glacier_fraction || !temperature_threshold_melt || !degree_day_factor || !snow_to_ice_fraction)
+        return glacier_fail(nullptr, WF_ERR_INVALID, "missing input");
+    WfGlacier* g = new WfGlacier();
+    GlacierDev& d = g->g;
+    d.n = n;
+    d.max_rate = maximum_snow_to_ice_rate;
+    double *p_f, *p_t, *p_c, *p_s, *p_temp;
+    int rc;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess)
+        rc = glacier_fail(g, WF_ERR_CUDA, "no CUDA device or stream");
+    else if ((rc = glacier_alloc(g, &p_f, glacier_fraction, n)) ||
+             (rc = glacier_alloc(g, &p_t, temperature_threshold_melt, n)) ||
+             (rc = glacier_alloc(g, &p_c, degree_day_factor, n)) ||
+             (rc = glacier_alloc(g, &p_s, snow_to_ice_fraction, n)) || (rc = glacier_alloc(g, &p_temp, nullptr, n)) ||
+             (rc = glacier_alloc(g, &d.snow, nullptr, n)) || (rc = glacier_alloc(g, &d.store, nullptr, n)) ||
+             (rc = glacier_alloc(g, &d.melt, nullptr, n)))
+        ;
+    else if (cudaDeviceSynchronize() != cudaSuccess)  // the uploads ran on the legacy stream
+        rc = glacier_fail(g, WF_ERR_CUDA, "upload failed");
+    if (rc) {
+        g_snow_error = g->err;
+        wf_glacier_destroy(g);
+        return rc;
+    }
+    d.fraction = p_f;
+    d.ttm = p_t;
+    d.cfmax = p_c;
+    d.sifrac = p_s;
+    d.temperature = p_temp;
+    *out = g;
+    return WF_OK;
+}
+
+int32_t wf_glacier_run(WfGlacier* g, double dt, const double* temperature, double* snow_storage,
+                       double* glacier_store, double* glacier_melt) {
+    if (!g || !temperature || !snow_storage || !glacier_store || !glacier_melt || !(dt > 0.0))
+        return glacier_fail(g, WF_ERR_INVALID, "null argument or non-positive dt");
+    const GlacierDev& d = g->g;
+    const size_t bytes = (size_t)d.n * sizeof(double);
+    if (cudaMemcpyAsync((void*)d.temperature, temperature, bytes, cudaMemcpyHostToDevice, g->stream) != cudaSuccess ||
+        cudaMemcpyAsync(d.snow, snow_storage, bytes, cudaMemcpyHostToDevice, g->stream) != cudaSuccess ||
+        cudaMemcpyAsync(d.store, glacier_store, bytes, cudaMemcpyHostToDevice, g->stream) != cudaSuccess)
+        return glacier_fail(g, WF_ERR_CUDA, "upload failed");
+    glacier_kernel<<<grid_of(d.n), 256, 0, g->stream>>>(d, dt);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return glacier_fail(g, WF_ERR_CUDA, std::string("glacier: ") + cudaGetErrorString(e));
+    if (cudaMemcpyAsync(snow_storage, d.snow, bytes, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
+        cudaMemcpyAsync(glacier_store, d.store, bytes, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
+        cudaMemcpyAsync(glacier_melt, d.melt, bytes, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
+        cudaStreamSynchronize(g->stream) != cudaSuccess)
+        return glacier_fail(g, WF_ERR_CUDA, "glacier step failed");
     return WF_OK;
 }
 

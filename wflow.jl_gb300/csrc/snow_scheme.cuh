@@ -64,4 +64,22 @@ WF_HD void in_cell(const SnowNet& d, int64_t i) {
     d.snow_in[i] = acc;
 }
 
+// glacier_hbv (glacier/glacier_process.jl): firn from the snow on the glacier part, then
+// degree-day glacier melt once the snow is below 10 mm. Returns the new snow storage, glacier
+// store and melt through the pointers.
+WF_HD void glacier_hbv(double glacier_fraction, double glacier_store, double snow_storage, double temperature,
+                       double ttm, double cfmax, double sifrac, double max_rate, double dt, double* snow_out,
+                       double* store_out, double* melt_out) {
+    double snow_to_glacier = glacier_fraction > 0.0 ? sifrac * snow_storage : 0.0;
+    snow_to_glacier = wfm::jmin(snow_to_glacier, max_rate);
+    snow_storage -= snow_to_glacier * glacier_fraction * dt;
+    glacier_store += snow_to_glacier * dt;
+    const double potential_melt = temperature > ttm ? cfmax * (temperature - ttm) : 0.0;
+    const double melt = snow_storage < 1e-2 ? wfm::jmin(potential_melt, glacier_store / dt) : 0.0;
+    glacier_store -= melt * dt;
+    *snow_out = snow_storage;
+    *store_out = glacier_store;
+    *melt_out = melt;
+}
+
 }  // namespace wfsn

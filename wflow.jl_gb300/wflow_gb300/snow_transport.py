@@ -84,3 +84,69 @@ class SnowTransport:
             self.close()
         except Exception:
             pass
+
+
+def _glacier_lib():
+    lib = _lib()
+    if not getattr(lib, "_glacier_declared", False):
+        P, i32, i64, d = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+        pd = C.POINTER(C.c_double)
+        for name, res, args in (("wf_glacier_create", i32, [i64, pd, pd, pd, pd, d, i32, C.POINTER(P)]),
+                                ("wf_glacier_destroy", None, [P]),
+                                ("wf_glacier_last_error", C.c_char_p, [P]),
+                                ("wf_glacier_run", i32, [P, d, pd, pd, pd, pd])):
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        lib._glacier_declared = True
+    return lib
+
+
+class Glacier:
+    """The HBV glacier of every cell (wf_glacier_*, update_glacier_model!,
+    Wflow/src/glacier/glacier.jl:122-154)."""
+
+    def __init__(self, glacier_fraction, temperature_threshold_melt, degree_day_factor, snow_to_ice_fraction,
+                 maximum_snow_to_ice_rate, device=0):
+        self.lib = _glacier_lib()
+        self._keep = [np.ascontiguousarray(a, np.float64) for a in (glacier_fraction, temperature_threshold_melt,
+                                                                    degree_day_factor, snow_to_ice_fraction)]
+        self.n = len(self._keep[0])
+        if any(a.shape != (self.n,) for a in self._keep):
+            raise ValueError(f"the glacier parameters must have {self.n} values each")
+        pd = C.POINTER(C.c_double)
+        self.h = C.c_void_p()
+        st = self.lib.wf_glacier_create(self.n, *[a.ctypes.data_as(pd) for a in self._keep],
+                                        float(maximum_snow_to_ice_rate), int(device), C.byref(self.h))
+        if st != 0:
+            msg = self.lib.wf_glacier_last_error(None)
+            raise RuntimeError(f"wf_glacier_create failed ({st}): {msg.decode() if msg else ''}")
+
+    def run(self, dt, temperature, snow_storage, glacier_store):
+        """Updates snow_storage and glacier_store in place; returns the glacier melt [m s-1]."""
+        t = np.ascontiguousarray(temperature, np.float64)
+        for name, a in (("snow_storage", snow_storage), ("glacier_store", glacier_store)):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.shape == (self.n,)
+                    and a.flags.c_contiguous):
+                raise ValueError(f"{name} must be a contiguous float64 array of {self.n} values")
+        if t.shape != (self.n,):
+            raise ValueError(f"temperature must have {self.n} values")
+        melt = np.empty(self.n)
+        pd = C.POINTER(C.c_double)
+        st = self.lib.wf_glacier_run(self.h, float(dt), t.ctypes.data_as(pd), snow_storage.ctypes.data_as(pd),
+                                     glacier_store.ctypes.data_as(pd), melt.ctypes.data_as(pd))
+        if st != 0:
+            msg = self.lib.wf_glacier_last_error(self.h)
+            raise RuntimeError(f"wf_glacier_run failed ({st}): {msg.decode() if msg else ''}")
+        return melt
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wf_glacier_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
