@@ -8,8 +8,8 @@
  * (update_river_channel_flow! and update_water_depth_and_storage!,
  * routing/surface/surface_staggered_scheme.jl:326-385, 723-760), with sub-steps of the
  * stable time step min over cells of alpha dx / sqrt(g h) (:1004-1020, update_river_flow_model!
- * :800-860). Channel only: no floodplain, no reservoirs at edges, no external inflow or
- * abstraction. FP64 in the reference's operation order.
+ * :800-860). Channel only: no floodplain, no reservoirs at edges. FP64 in the reference's
+ * operation order.
  *
  * A standalone component: it holds its own network and state on the device; the SBM step of
  * wflow_gb300.h routes rivers by the kinematic wave.
@@ -47,6 +47,10 @@ int32_t wf_li_river_set_state(WfLiRiver* r, const double* h, const double* q);
  * reference's MacDonald test sets its boundary cell inside n; a Wflow model's river has its ghost
  * cells after its RiverFlowStaggeredParameters.n real cells and passes that n). */
 int32_t wf_li_river_set_timestep_cells(WfLiRiver* r, int64_t n_cells);
+/* External inflow and abstraction of every cell [m3 s-1] (RiverFlowBC.external_inflow and
+ * .abstraction; NULL: zero). A negative external inflow is an abstraction limited to 80 % of the
+ * storage per step. */
+int32_t wf_li_river_set_boundary(WfLiRiver* r, const double* external_inflow, const double* abstraction);
 /* Lateral inflow of every cell [m3 s-1] (inwater). */
 int32_t wf_li_river_set_inwater(WfLiRiver* r, const double* inwater);
 /* The stable sub-step of the current depths (60 s when every cell is dry). */
@@ -59,7 +63,8 @@ int32_t wf_li_river_substep(WfLiRiver* r, double dt_s);
 int32_t wf_li_river_step(WfLiRiver* r, double dt, int64_t* substeps);
 /* Copy a field to host: 0 depth h [n], 1 storage [n], 2 discharge q [n_edges],
  * 3 cumulative discharge, the sum of q * dt_s [n_edges], 4 average discharge of the last
- * model step [n_edges]. */
+ * model step [n_edges], 5 storage clipped at zero (error) [n], 6 actual abstraction of the
+ * model step [m3, n]. */
 int32_t wf_li_river_get(WfLiRiver* r, int32_t field, double* dst);
 
 /* ---- Local-inertial overland flow on the land grid coupled with the river ----------------

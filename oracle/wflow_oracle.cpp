@@ -1859,7 +1859,9 @@ double orc_li_flow_rect(double theta, double q0, double qd, double qu, double zs
 // One local-inertial river step over n cells and n_edges edges (edge k from src[k] to dst[k],
 // in the graph's edge order); the first n_active cells are updated (the others are boundary
 // cells of fixed depth). Arrays: zb, flow_length, flow_width, inwater [n]; zb_e, width_e,
-// length_e, nsq_e [n_edges]; state h, storage [n], q, q_prev, q_cum [n_edges].
+// length_e, nsq_e [n_edges]; state h, storage [n], q, q_prev, q_cum [n_edges]; abstraction,
+// external_inflow, error and abstraction_cum [n] (update_water_depth_and_storage!, :723-760;
+// each may be NULL: zero inflows, nothing recorded).
 // update_river_channel_flow! (:326-385): the discharge of every river edge
 static void li_river_edges(int64_t n_edges, const int64_t* src, const int64_t* dst, const double* zb,
                            const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
@@ -1888,7 +1890,8 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
                        const double* zb, const double* flow_length, const double* flow_width, const double* inwater,
                        const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
                        double h_thresh, int32_t froude_limit, double dt, double* h, double* storage, double* q,
-                       double* q_prev, double* q_cum) {
+                       double* q_prev, double* q_cum, const double* abstraction, const double* external_inflow,
+                       double* error, double* abstraction_cum) {
     li_river_edges(n_edges, src, dst, zb, zb_e, width_e, length_e, nsq_e, h_thresh, froude_limit, dt, h, q, q_prev,
                    q_cum);
     // update_water_depth_and_storage! (:723-760), edges into / out of each cell in edge order
@@ -1897,10 +1900,21 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
         qin[dst[k]] = qin[dst[k]] + q[k];
         qout[src[k]] = qout[src[k]] + q[k];
     }
-    for (int64_t i = 0; i < n_active; ++i) {
-        storage[i] += (qin[i] - qout[i] + inwater[i] - 0.0) * dt;
-        if (storage[i] < 0.0) storage[i] = 0.0;
-        storage[i] += 0.0 * dt;
+    for (int64_t i = 0; i < n_active; ++i) {  // NULL boundary arrays: zero
+        const double abs_i = abstraction ? abstraction[i] : 0.0;
+        const double ext_i = external_inflow ? external_inflow[i] : 0.0;
+        storage[i] += (qin[i] - qout[i] + inwater[i] - abs_i) * dt;
+        if (storage[i] < 0.0) {
+            if (error) error[i] = error[i] + std::fabs(storage[i]);
+            storage[i] = 0.0;
+        }
+        double inflow = ext_i;
+        if (ext_i < 0.0) {  // limit negative external inflow
+            const double taken = jmin(-ext_i, storage[i] / dt * 0.80);
+            if (abstraction_cum) abstraction_cum[i] += taken * dt;
+            inflow = -taken;
+        }
+        storage[i] += inflow * dt;
         h[i] = storage[i] / (flow_length[i] * flow_width[i]);
     }
 }

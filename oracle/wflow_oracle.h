@@ -148,7 +148,8 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
                        const double* zb, const double* flow_length, const double* flow_width, const double* inwater,
                        const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
                        double h_thresh, int32_t froude_limit, double dt, double* h, double* storage, double* q,
-                       double* q_prev, double* q_cum);
+                       double* q_prev, double* q_cum, const double* abstraction, const double* external_inflow,
+                       double* error, double* abstraction_cum);
 double orc_li_stable_timestep(int64_t n, const double* flow_length, const double* h, double alpha);
 /* 2D overland local-inertial flow with a subgrid river (surface_staggered_scheme.jl:1022-1040,
  * 1202-1265, 1322-1546); 0-based indices, index n = the ghost cell outside the grid */

@@ -63,8 +63,14 @@ def random_river(seed, n_active=3000, n_bound=4):
     src, dst = src[order], dst[order]
     zb_e, w_e, l_e, nsq_e = edge_attributes(src, dst, zb, flow_length, width, mannings_n)
     inwater = rng.uniform(0.0, 5.0, n) * (rng.random(n) < 0.7)
+    external_inflow = np.zeros(n)
+    pick = rng.choice(n_active, size=max(2, n_active // 50), replace=False)
+    external_inflow[pick] = rng.uniform(-20.0, 10.0, len(pick))
+    abstraction = np.zeros(n)
+    abstraction[rng.choice(n_active, size=max(2, n_active // 100), replace=False)] = rng.uniform(0.0, 8.0)
     return dict(n=n, n_active=n_active, src=src, dst=dst, zb=zb, flow_length=flow_length, flow_width=width,
-                h=h, zb_e=zb_e, w_e=w_e, l_e=l_e, nsq_e=nsq_e, inwater=inwater)
+                h=h, zb_e=zb_e, w_e=w_e, l_e=l_e, nsq_e=nsq_e, inwater=inwater, external_inflow=external_inflow,
+                abstraction=abstraction)
 
 
 def macdonald_case(a):
@@ -113,6 +119,8 @@ class OracleLi:
         self.q_cum = np.zeros(self.ne)
         self.q_avg = np.zeros(self.ne)
         self.inwater = np.zeros(self.n)
+        self.abstraction, self.external_inflow = np.zeros(self.n), np.zeros(self.n)
+        self.error, self.abs_cum = np.zeros(self.n), np.zeros(self.n)
         self.h_thresh, self.froude, self.alpha = h_thresh, froude, alpha
         self.n_dt = self.n
         self.L = O.lib()
@@ -133,6 +141,10 @@ class OracleLi:
     def set_inwater(self, v):
         self.inwater = np.array(v, float)
 
+    def set_boundary(self, external_inflow=None, abstraction=None):
+        self.external_inflow = np.zeros(self.n) if external_inflow is None else np.array(external_inflow, float)
+        self.abstraction = np.zeros(self.n) if abstraction is None else np.array(abstraction, float)
+
     def stable_timestep(self):
         return self.L.orc_li_stable_timestep(C.c_int64(self.n_dt), _pd(self.net["flow_length"]), _pd(self.h),
                                              C.c_double(self.alpha))
@@ -143,13 +155,15 @@ class OracleLi:
                                  _pl(t["dst"]), _pd(t["zb"]), _pd(t["flow_length"]), _pd(t["flow_width"]),
                                  _pd(self.inwater), _pd(t["zb_e"]), _pd(t["w_e"]), _pd(t["l_e"]), _pd(t["nsq_e"]),
                                  C.c_double(self.h_thresh), C.c_int32(int(self.froude)), C.c_double(dt), _pd(self.h),
-                                 _pd(self.storage), _pd(self.q), _pd(self.q_prev), _pd(self.q_cum))
+                                 _pd(self.storage), _pd(self.q), _pd(self.q_prev), _pd(self.q_cum),
+                                 _pd(self.abstraction), _pd(self.external_inflow), _pd(self.error), _pd(self.abs_cum))
 
     def step(self, dt):
         """update_river_flow_model! (surface_staggered_scheme.jl:800-826) without reservoirs or
         floodplain: q_cumulative restarts, sub-steps of the stable time step (cut at dt,
         check_timestepsize) until dt, q_average = q_cumulative / dt. Returns the sub-step count."""
         self.q_cum[:] = 0.0
+        self.abs_cum[:] = 0.0
         t, k = 0.0, 0
         while t < dt:
             dt_s = self.stable_timestep()

@@ -12,7 +12,8 @@ void host_li_substep(int64_t n, int64_t n_active, int64_t n_edges, const int64_t
                      const double* zb, const double* flow_length, const double* flow_width, double* inwater,
                      const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
                      double h_thresh, int32_t froude, double dt, double* h, double* storage, double* q, double* q_prev,
-                     double* q_cum) {
+                     double* q_cum, const double* abstraction, const double* external_inflow, double* error,
+                     double* abstraction_cum) {
     std::vector<int64_t> ip, ie, op, oe;
     wfli::build_csr(n, n_edges, src, dst, ip, ie, op, oe);
     wfli::LiNet d{};
@@ -38,6 +39,10 @@ void host_li_substep(int64_t n, int64_t n_active, int64_t n_edges, const int64_t
     d.q_prev = q_prev;
     d.q_cum = q_cum;
     d.inwater = inwater;
+    d.abstraction = abstraction;
+    d.external_inflow = external_inflow;
+    d.error = error;
+    d.abstraction_cum = abstraction_cum;
     d.h_thresh = h_thresh;
     d.froude = froude;
     for (int64_t k = 0; k < n_edges; ++k) wfli::update_edge(d, k, dt);

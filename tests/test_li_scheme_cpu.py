@@ -51,7 +51,8 @@ class HostLi(OracleLi):
                                _pd(t["zb"]), _pd(t["flow_length"]), _pd(t["flow_width"]), _pd(self.inwater),
                                _pd(t["zb_e"]), _pd(t["w_e"]), _pd(t["l_e"]), _pd(t["nsq_e"]),
                                C.c_double(self.h_thresh), C.c_int32(int(self.froude)), C.c_double(dt), _pd(self.h),
-                               _pd(self.storage), _pd(self.q), _pd(self.q_prev), _pd(self.q_cum))
+                               _pd(self.storage), _pd(self.q), _pd(self.q_prev), _pd(self.q_cum),
+                               _pd(self.abstraction), _pd(self.external_inflow), _pd(self.error), _pd(self.abs_cum))
 
 
 @pytest.mark.parametrize("seed,froude,alpha", [(0, True, 0.7), (1, False, 0.5)])
@@ -61,10 +62,12 @@ def test_random_river_bit_identical(host_lib, seed, froude, alpha):
     for m in (a, b):
         m.set_state(net["h"])
         m.set_inwater(net["inwater"])
+        m.set_boundary(net["external_inflow"], net["abstraction"])
     for step in range(2):
         assert a.step(3600.0) == b.step(3600.0)
-        for f in ("h", "storage", "q", "q_prev", "q_cum", "q_avg"):
+        for f in ("h", "storage", "q", "q_prev", "q_cum", "q_avg", "error", "abs_cum"):
             assert np.array_equal(getattr(a, f), getattr(b, f)), (seed, step, f)
+    assert a.abs_cum.sum() > 0.0
     assert (net["h"] == 0.0).any() and (np.abs(net["h"] - 1e-3) < 5e-4).any()  # dry and near-threshold starts
     assert np.abs(a.q).max() > 0.0
 

@@ -21,8 +21,9 @@ import pytest
 
 from li_cases import OracleLi, macdonald_case, random_river
 
-FIELDS = ("h", "storage", "q", "q_cumulative", "q_average")
-ORACLE_ATTR = {"h": "h", "storage": "storage", "q": "q", "q_cumulative": "q_cum", "q_average": "q_avg"}
+FIELDS = ("h", "storage", "q", "q_cumulative", "q_average", "error", "abstraction_cumulative")
+ORACLE_ATTR = {"h": "h", "storage": "storage", "q": "q", "q_cumulative": "q_cum", "q_average": "q_avg",
+               "error": "error", "abstraction_cumulative": "abs_cum"}
 
 
 def _river(net, **kw):
@@ -49,12 +50,14 @@ def _assert_same(gpu, orc, tag):
 @pytest.mark.parametrize("seed", [0, 1])
 def test_random_river_steps(gpu_lib, seed):
     """Three hourly model steps of a 3000-cell river tree with confluences, four outlets of
-    fixed depth, wet, dry and near-threshold starting depths and lateral inflow."""
+    fixed depth, wet, dry and near-threshold starting depths, lateral inflow, abstractions and
+    positive and negative external inflows."""
     net = random_river(seed)
     gpu, orc = _river(net), OracleLi(net)
     for m in (gpu, orc):
         m.set_state(net["h"])
         m.set_inwater(net["inwater"])
+        m.set_boundary(net["external_inflow"], net["abstraction"])
     for step in range(3):
         k_gpu, k_orc = gpu.step(3600.0), orc.step(3600.0)
         assert k_gpu == k_orc, (seed, step, k_gpu, k_orc)

@@ -215,8 +215,13 @@ int li_upload_river(LiOwner* o, LiDev& d, int64_t n, int64_t n_active, int64_t n
         (rc = li_upload(o, &d.h, h_init, n)) || (rc = li_upload<double>(o, &d.storage, nullptr, n)) ||
         (rc = li_upload<double>(o, &d.q, nullptr, n_edges)) || (rc = li_upload<double>(o, &d.q_prev, nullptr, n_edges)) ||
         (rc = li_upload<double>(o, &d.q_cum, nullptr, n_edges)) || (rc = li_upload<double>(o, &d.inwater, nullptr, n)) ||
-        (rc = li_upload<double>(o, &d.dt_min, nullptr, 1)))
+        (rc = li_upload<double>(o, &d.dt_min, nullptr, 1)) || (rc = li_upload<double>(o, &d.error, nullptr, n)) ||
+        (rc = li_upload<double>(o, &d.abstraction_cum, nullptr, n)))
         return rc;
+    double *p_abs, *p_ext;
+    if ((rc = li_upload<double>(o, &p_abs, nullptr, n)) || (rc = li_upload<double>(o, &p_ext, nullptr, n))) return rc;
+    d.abstraction = p_abs;
+    d.external_inflow = p_ext;
     d.src = p_src;
     d.dst = p_dst;
     d.in_ptr = p_ip;
@@ -319,6 +324,19 @@ int32_t wf_li_river_set_inwater(WfLiRiver* r, const double* inwater) {
     return li_copy_in(r, r->d.inwater, inwater, r->d.n);
 }
 
+int32_t wf_li_river_set_boundary(WfLiRiver* r, const double* external_inflow, const double* abstraction) {
+    if (!r) return li_fail(r, WF_ERR_INVALID, "null argument");
+    const int64_t n = r->d.n;
+    std::vector<double> zero;
+    if (!external_inflow || !abstraction) zero.assign(n, 0.0);
+    int rc;
+    if ((rc = li_copy_in(r, const_cast<double*>(r->d.external_inflow), external_inflow ? external_inflow : zero.data(),
+                         n)) ||
+        (rc = li_copy_in(r, const_cast<double*>(r->d.abstraction), abstraction ? abstraction : zero.data(), n)))
+        return rc;
+    return WF_OK;
+}
+
 int32_t wf_li_river_stable_timestep(WfLiRiver* r, double* dt) {
     if (!r || !dt) return li_fail(r, WF_ERR_INVALID, "null argument");
     li_dt_kernel<<<1, LI_DT_THREADS, 0, r->stream>>>(r->d);
@@ -336,8 +354,10 @@ int32_t wf_li_river_substep(WfLiRiver* r, double dt_s) {
 
 int32_t wf_li_river_step(WfLiRiver* r, double dt, int64_t* substeps) {
     if (!r || !(dt > 0.0)) return li_fail(r, WF_ERR_INVALID, "step must be positive");
-    // set_flow_vars!: the cumulative discharge restarts each model step
-    if (r->d.n_edges > 0 && cudaMemsetAsync(r->d.q_cum, 0, r->d.n_edges * sizeof(double), r->stream) != cudaSuccess)
+    // set_flow_vars!: the cumulative discharge and abstraction restart each model step
+    if ((r->d.n_edges > 0 &&
+         cudaMemsetAsync(r->d.q_cum, 0, r->d.n_edges * sizeof(double), r->stream) != cudaSuccess) ||
+        cudaMemsetAsync(r->d.abstraction_cum, 0, r->d.n * sizeof(double), r->stream) != cudaSuccess)
         return li_fail(r, WF_ERR_CUDA, "reset of the cumulative discharge failed");
     double t = 0.0;
     int64_t k = 0;
@@ -377,9 +397,11 @@ int32_t wf_li_river_get(WfLiRiver* r, int32_t field, double* dst) {
                         : field == 2 ? r->d.q
                         : field == 3 ? r->d.q_cum
                         : field == 4 ? r->q_avg
+                        : field == 5 ? r->d.error
+                        : field == 6 ? r->d.abstraction_cum
                                      : nullptr;
     if (!src) return li_fail(r, WF_ERR_INVALID, "unknown field");
-    return li_copy_out(r, dst, src, field <= 1 ? r->d.n : r->d.n_edges);
+    return li_copy_out(r, dst, src, (field <= 1 || field >= 5) ? r->d.n : r->d.n_edges);
 }
 
 // ---------------------------------------------------------------- land with river ---------

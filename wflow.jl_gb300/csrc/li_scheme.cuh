@@ -28,6 +28,8 @@ struct LiNet {
     const int64_t *in_ptr, *in_edge, *out_ptr, *out_edge;
     const double *zb, *flow_length, *flow_width, *zb_e, *width_e, *length_e, *nsq_e;
     double *h, *storage, *q, *q_prev, *q_cum, *inwater, *dt_min;
+    const double *abstraction, *external_inflow;  // river alone: boundary inflows [m3 s-1]
+    double *error, *abstraction_cum;              // river alone: clipped storage, actual abstraction [m3]
     double h_thresh, alpha;
     int32_t froude;
 };
@@ -65,14 +67,26 @@ WF_HD void update_edge(const LiNet& d, int64_t k, double dt) {
     d.q_cum[k] += q * dt;
 }
 
-// storage and depth of active cell i over dt (no external inflow, abstraction or floodplain)
+// storage and depth of active cell i over dt: edge discharges, lateral inflow and abstraction,
+// the storage clipped at zero (the clipped volume counted as error), then the external inflow,
+// a negative one limited to 80 % of the storage per step (no floodplain)
 WF_HD void update_cell(const LiNet& d, int64_t i, double dt) {
     double qin = 0.0, qout = 0.0;
     for (int64_t o = d.in_ptr[i]; o < d.in_ptr[i + 1]; ++o) qin = qin + d.q[d.in_edge[o]];
     for (int64_t o = d.out_ptr[i]; o < d.out_ptr[i + 1]; ++o) qout = qout + d.q[d.out_edge[o]];
-    double s = d.storage[i] + (qin - qout + d.inwater[i] - 0.0) * dt;
-    if (s < 0.0) s = 0.0;
-    s += 0.0 * dt;
+    double s = d.storage[i] + (qin - qout + d.inwater[i] - d.abstraction[i]) * dt;
+    if (s < 0.0) {
+        d.error[i] = d.error[i] + wfm::fabs_(s);
+        s = 0.0;
+    }
+    const double ext = d.external_inflow[i];
+    double inflow = ext;
+    if (ext < 0.0) {
+        const double taken = wfm::jmin(-ext, s / dt * 0.80);
+        d.abstraction_cum[i] += taken * dt;
+        inflow = -taken;
+    }
+    s += inflow * dt;
     d.storage[i] = s;
     d.h[i] = s / (d.flow_length[i] * d.flow_width[i]);
 }

@@ -32,6 +32,7 @@ def _lib():
             "wf_li_river_last_error": (C.c_char_p, [P]),
             "wf_li_river_set_state": (i32, [P, pd, pd]),
             "wf_li_river_set_timestep_cells": (i32, [P, i64]),
+            "wf_li_river_set_boundary": (i32, [P, pd, pd]),
             "wf_li_river_set_inwater": (i32, [P, pd]),
             "wf_li_river_stable_timestep": (i32, [P, pd]),
             "wf_li_river_substep": (i32, [P, d]),
@@ -130,7 +131,8 @@ def river_network(river, keep):
 
 
 class LiRiver:
-    FIELDS = {"h": 0, "storage": 1, "q": 2, "q_cumulative": 3, "q_average": 4}
+    FIELDS = {"h": 0, "storage": 1, "q": 2, "q_cumulative": 3, "q_average": 4, "error": 5,
+              "abstraction_cumulative": 6}
 
     def __init__(self, src, dst, zb, flow_length, flow_width, h_init, zb_edge, width_edge, length_edge,
                  mannings_n_sq_edge, n_active, h_thresh=1e-3, froude_limit=True, alpha=0.7, device=0):
@@ -186,6 +188,14 @@ class LiRiver:
         passes its real cells, the ghost cells coming after them)."""
         self._check(self.lib.wf_li_river_set_timestep_cells(self.h, int(n_cells)), "wf_li_river_set_timestep_cells")
 
+    def set_boundary(self, external_inflow=None, abstraction=None):
+        """External inflow and abstraction of every cell [m3 s-1] (None: zero)."""
+        v = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (external_inflow, abstraction)]
+        if any(a is not None and a.shape != (self.n,) for a in v):
+            raise ValueError(f"boundary arrays must have {self.n} values")
+        self._check(self.lib.wf_li_river_set_boundary(self.h, *[None if a is None else _pd(a) for a in v]),
+                    "wf_li_river_set_boundary")
+
     def set_inwater(self, inwater):
         v = np.ascontiguousarray(inwater, np.float64)
         if v.shape != (self.n,):
@@ -207,7 +217,7 @@ class LiRiver:
 
     def get(self, field):
         f = self.FIELDS[field]
-        out = np.empty(self.n if f <= 1 else self.n_edges)
+        out = np.empty(self.n if (f <= 1 or f >= 5) else self.n_edges)
         self._check(self.lib.wf_li_river_get(self.h, f, _pd(out)), "wf_li_river_get")
         return out
 
