@@ -485,4 +485,84 @@ function gpu_update_local_inertial!(gpu::GpuLocalInertial, model, dt)
     return nothing
 end
 
+"""
+    GpuLocalInertialRiver(model)
+
+The river of a model with `river_routing = "local_inertial"` (kinematic-wave land, no
+reservoirs, no 1D floodplain) as a `wf_li_river` handle, with the stable time step over the real
+river cells (the ghost cells follow them) and the current depths and discharges.
+"""
+mutable struct GpuLocalInertialRiver
+    handle::Ptr{Cvoid}
+    keep::Vector{Any}
+    n_river::Int
+    n_real::Int
+end
+
+function GpuLocalInertialRiver(model)
+    (; domain, routing, config) = model
+    m = config.model
+    m.river_routing == Wflow.RoutingType.local_inertial || error("GpuLocalInertialRiver needs local-inertial rivers")
+    (m.reservoir__flag || m.floodplain_1d__flag) &&
+        error("GpuLocalInertialRiver: reservoirs and the 1D floodplain are not supported")
+    river = routing.river_flow
+    rp = river.parameters
+    n_total = length(river.variables.h)
+    nae = domain.river.network.nodes_at_edge
+    keep = Any[zero_based(nae.src), zero_based(nae.dst), Float64.(rp.zb),
+        pad_river(domain.river.parameters.flow_length, n_total), pad_river(domain.river.parameters.flow_width, n_total),
+        copy(river.variables.h), rp.zb_at_edge, rp.flow_width_at_edge, rp.flow_length_at_edge,
+        rp.mannings_n_sq_at_edge]
+    handle = Ref{Ptr{Cvoid}}(C_NULL)
+    st = GC.@preserve keep ccall((:wf_li_river_create, LIB), Int32,
+        (Int64, Int64, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Float64, Int32, Float64, Int32, Ref{Ptr{Cvoid}}),
+        n_total, rp.n, rp.n_edges, keep[1], keep[2], keep[3], keep[4], keep[5], keep[6], keep[7], keep[8], keep[9],
+        keep[10], rp.h_thresh, Int32(rp.froude_limit), river.timestepping.alpha_coefficient, Int32(0), handle)
+    riv_check(st, C_NULL, "wf_li_river_create")
+    gpu = GpuLocalInertialRiver(handle[], keep, n_total, rp.n)
+    finalizer(x -> ccall((:wf_li_river_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.handle), gpu)
+    riv_check(ccall((:wf_li_river_set_timestep_cells, LIB), Int32, (Ptr{Cvoid}, Int64), gpu.handle, rp.n),
+        gpu.handle, "wf_li_river_set_timestep_cells")
+    riv_check(ccall((:wf_li_river_set_state, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
+            gpu.handle, river.variables.h, river.variables.q), gpu.handle, "wf_li_river_set_state")
+    return gpu
+end
+
+riv_check(st, h, what) = st == 0 || error("$what failed ($st): " *
+                                          unsafe_string(ccall((:wf_li_river_last_error, LIB), Cstring,
+                                                              (Ptr{Cvoid},), h)))
+
+"""
+    gpu_update_river_flow_model!(gpu::GpuLocalInertialRiver, model, dt)
+
+In place of `update_river_flow_model!` for a local-inertial river
+(Wflow/src/routing/surface/surface_staggered_scheme.jl:800-826): uploads `inwater`, the external
+inflow and the abstraction, runs the step on the GPU and copies the river variables back.
+"""
+function gpu_update_river_flow_model!(gpu::GpuLocalInertialRiver, model, dt)
+    river = model.routing.river_flow
+    bc, v = river.boundary_conditions, river.variables
+    n = gpu.n_river
+    riv_check(ccall((:wf_li_river_set_inwater, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}), gpu.handle,
+            pad_zero(bc.inwater, n)), gpu.handle, "wf_li_river_set_inwater")
+    riv_check(ccall((:wf_li_river_set_boundary, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), gpu.handle,
+            pad_zero(bc.external_inflow, n), pad_zero(bc.abstraction, n)), gpu.handle, "wf_li_river_set_boundary")
+    riv_check(ccall((:wf_li_river_step, LIB), Int32, (Ptr{Cvoid}, Float64, Ptr{Int64}), gpu.handle, dt, C_NULL),
+        gpu.handle, "wf_li_river_step")
+    tmp = Vector{Float64}(undef, n)
+    get!(f) = riv_check(ccall((:wf_li_river_get, LIB), Int32, (Ptr{Cvoid}, Int32, Ptr{Float64}), gpu.handle,
+                              Int32(f), f in (2, 3, 4) ? qbuf : tmp), gpu.handle, "wf_li_river_get")
+    qbuf = similar(v.q)
+    get!(0); v.h .= tmp[1:length(v.h)]
+    get!(1); v.storage .= tmp[1:length(v.storage)]
+    get!(5); v.error .= tmp[1:length(v.error)]
+    get!(6); bc.actual_external_abstraction_cumulative .= tmp[1:length(bc.actual_external_abstraction_cumulative)]
+    bc.actual_external_abstraction_average .= bc.actual_external_abstraction_cumulative ./ dt
+    get!(2); v.q .= qbuf
+    get!(3); v.q_cumulative .= qbuf
+    get!(4); v.q_average .= qbuf
+    return nothing
+end
+
 end # module
