@@ -551,17 +551,17 @@ function gpu_update_river_flow_model!(gpu::GpuLocalInertialRiver, model, dt)
     riv_check(ccall((:wf_li_river_step, LIB), Int32, (Ptr{Cvoid}, Float64, Ptr{Int64}), gpu.handle, dt, C_NULL),
         gpu.handle, "wf_li_river_step")
     tmp = Vector{Float64}(undef, n)
-    get!(f) = riv_check(ccall((:wf_li_river_get, LIB), Int32, (Ptr{Cvoid}, Int32, Ptr{Float64}), gpu.handle,
+    fetch_field!(f) = riv_check(ccall((:wf_li_river_get, LIB), Int32, (Ptr{Cvoid}, Int32, Ptr{Float64}), gpu.handle,
                               Int32(f), f in (2, 3, 4) ? qbuf : tmp), gpu.handle, "wf_li_river_get")
     qbuf = similar(v.q)
-    get!(0); v.h .= tmp[1:length(v.h)]
-    get!(1); v.storage .= tmp[1:length(v.storage)]
-    get!(5); v.error .= tmp[1:length(v.error)]
-    get!(6); bc.actual_external_abstraction_cumulative .= tmp[1:length(bc.actual_external_abstraction_cumulative)]
+    fetch_field!(0); v.h .= tmp[1:length(v.h)]
+    fetch_field!(1); v.storage .= tmp[1:length(v.storage)]
+    fetch_field!(5); v.error .= tmp[1:length(v.error)]
+    fetch_field!(6); bc.actual_external_abstraction_cumulative .= tmp[1:length(bc.actual_external_abstraction_cumulative)]
     bc.actual_external_abstraction_average .= bc.actual_external_abstraction_cumulative ./ dt
-    get!(2); v.q .= qbuf
-    get!(3); v.q_cumulative .= qbuf
-    get!(4); v.q_average .= qbuf
+    fetch_field!(2); v.q .= qbuf
+    fetch_field!(3); v.q_cumulative .= qbuf
+    fetch_field!(4); v.q_average .= qbuf
     return nothing
 end
 
