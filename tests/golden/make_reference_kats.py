@@ -7,8 +7,8 @@ copies each literal from the cited line. Each case records the function, its inp
 expected outputs, the comparison Julia uses (`==` or `≈`, i.e. rtol = sqrt(eps)), and the
 file:line every number came from.
 
-Usage: python tests/golden/make_reference_kats.py [path-to-Wflow.jl-checkout]
-The default checkout path is the read-only reference mount of the build container.
+Usage: python tests/golden/make_reference_kats.py <path-to-Wflow.jl-checkout>
+(or with the checkout path in the environment variable WFLOW_JL_CHECKOUT).
 """
 
 import json
@@ -16,7 +16,16 @@ import re
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference") / "Wflow" / "test"
+
+def _checkout():
+    import os
+    p = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("WFLOW_JL_CHECKOUT")
+    if not p:
+        sys.exit("usage: make_reference_kats.py <path-to-Wflow.jl-checkout> (or set WFLOW_JL_CHECKOUT)")
+    return Path(p)
+
+
+REF = _checkout() / "Wflow" / "test"
 OUT = Path(__file__).with_name("reference_kats.json")
 
 _lines_cache = {}

@@ -109,10 +109,22 @@ def test_settings_and_paths(setup):
 
 def test_unsupported_options_are_refused(setup):
     root, _ = setup
-    text = TOML.replace('type = "sbm"', 'type = "sbm"\nglacier__flag = true\nland_routing = "local_inertial"')
+    text = TOML.replace('type = "sbm"', 'type = "sbm"\ndrain__flag = true\nland_routing = "local_inertial"')
     (root / "g.toml").write_text(text)
-    with pytest.raises(ValueError, match="glacier__flag.*land_routing"):
+    with pytest.raises(ValueError, match="drain__flag.*land_routing"):
         WflowConfig(root / "g.toml").wf_config()
+
+
+def test_snow_transport_and_glacier_flags(setup):
+    root, _ = setup
+    text = TOML.replace('type = "sbm"', 'type = "sbm"\nglacier__flag = true\nsnow_gravitational_transport__flag = true')
+    (root / "sg.toml").write_text(text)
+    c = WflowConfig(root / "sg.toml").wf_config()
+    assert c.snow == 1 and c.glacier == 1 and c.snow_gravitational_transport == 1
+    # a glacier needs the snow model (sbm.jl:45-49); the transport without snow does nothing
+    (root / "ns.toml").write_text(text.replace("snow__flag = true", "snow__flag = false"))
+    with pytest.raises(ValueError, match="glacier__flag without snow"):
+        WflowConfig(root / "ns.toml").wf_config()
 
 
 def test_model_from_the_toml_runs_like_the_arrays(setup):
@@ -158,3 +170,52 @@ def test_scale_and_offset_entries(setup):
     # file value (mm) * 0.5 + 100 mm, then to metres
     expect = ((base.params["soil_thickness"] / 1e-3) * 0.5 + 100.0) * 1e-3
     np.testing.assert_allclose(got.params["soil_thickness"], expect, rtol=1e-15)
+
+
+# ---- the reference's own test configurations (tests/golden/reference_configs.json, copied from
+# Wflow/test by tests/golden/make_reference_configs.py)
+def _reference_config(tmp_path, name):
+    import json
+    from pathlib import Path
+    data = json.loads((Path(__file__).parent / "golden" / "reference_configs.json").read_text())
+    p = tmp_path / name
+    p.write_text(data[name]["text"])
+    return WflowConfig(p)
+
+
+def test_reference_sbm_config_parses(tmp_path):
+    cfg = _reference_config(tmp_path, "sbm_config.toml")
+    root = tmp_path
+    assert cfg.dt == 86400.0
+    assert (cfg.starttime.year, cfg.starttime.month, cfg.starttime.day) == (2000, 1, 1)
+    assert (cfg.endtime.year, cfg.endtime.month, cfg.endtime.day) == (2000, 2, 1)
+    assert len(cfg.times()) == 31
+    assert cfg.path_static == root / "data" / "input" / "staticmaps-moselle.nc"
+    assert cfg.path_forcing == root / "data" / "input" / "forcing-moselle.nc"
+    assert cfg.state_input == root / "data" / "input" / "instates-moselle.nc"
+    assert cfg.state_output == root / "data" / "output" / "outstates-moselle.nc"
+    assert cfg.static["basin__local_drain_direction"] == {"name": "wflow_ldd"}
+    assert cfg.static["soil_surface_water__vertical_saturated_hydraulic_conductivity"] == {
+        "name": "KsatVer", "scale": 1.0, "offset": 0.0}
+    assert cfg.forcing["atmosphere_water__precipitation_volume_flux"] == {"name": "precip"}
+    assert cfg.state_ncnames["soil_water_saturated_zone__depth"] == "satwaterdepth"
+    assert cfg.reservoirs and cfg.cold_start
+    # outside the GPU step: leaf-area-index driven interception, and snow transport with reservoirs
+    with pytest.raises(ValueError) as e:
+        cfg.wf_config()
+    assert "cyclic LAI" in str(e.value) and "snow_gravitational_transport__flag with reservoir__flag" in str(e.value)
+
+
+def test_reference_sbm_simple_parses(tmp_path):
+    cfg = _reference_config(tmp_path, "sbm_simple.toml")
+    assert cfg.dt == 86400.0  # the reference's default time step
+    assert (cfg.endtime.year, cfg.endtime.month, cfg.endtime.day) == (2000, 1, 10)
+    assert cfg.static["soil__thickness"] == {"name": "SoilThickness"}
+    assert not cfg.reservoirs
+    with pytest.raises(ValueError, match="cyclic LAI"):
+        cfg.wf_config()
+    # without the cyclic LAI the rest of the [model] section maps onto the step's configuration
+    cfg.raw["input"].pop("cyclic")
+    c = cfg.wf_config()
+    assert c.n_soil_layer_thickness == 3 and c.snow == 0 and c.glacier == 0
+    assert abs(c.soil_layer_thickness[2] - 0.8) < 1e-15

@@ -49,6 +49,26 @@ def test_static_step_matches_step(gpu_lib, form, dt):
     assert m["steps"] == 2
 
 
+def test_static_step_leaves_device_memory_unchanged(gpu_lib):
+    # after the first call (set-up: the scratch address lookup), further calls allocate nothing
+    import torch
+    dom = synthetic.make_domain(32, 1000.0, seed=7)
+    cfg = synthetic.make_config(3600.0, form=abi.WF_FORM_SPLIT)
+    sta = Model(cfg, dom)
+    P, PET, T = synthetic.forcing(0, 3600.0, dom.n_land, seed=7)
+    sta.set_forcing(P, PET, T)
+    assert sta.lib.wf_step_static(sta.h) == abi.WF_OK
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for s in range(1, 4):
+        P, PET, T = synthetic.forcing(s, 3600.0, dom.n_land, seed=7)
+        sta.set_forcing(P, PET, T)
+        assert sta.lib.wf_step_static(sta.h) == abi.WF_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(0)[0] == free0
+    assert sta.metrics()["steps"] == 4
+
+
 def test_static_step_rejects_models_beyond_the_scratch(gpu_lib):
     # daily steps with 3600 s overland sub-steps: 24 published discharges per land chain end and
     # member in one launch

@@ -2,8 +2,9 @@
 
 Follows the reference's configuration schema (Wflow/src/config_structure.jl, config_init.jl):
   [time]             starttime, endtime, timestepsecs, calendar, time_units
-  [model]            the flags of the SBM path (snow, reservoirs, adaptive kinematic-wave
-                     sub-steps, sub-step sizes, soil layers, Kv profile, mass balance, ...)
+  [model]            the flags of the SBM path (snow, gravitational snow transport, glacier,
+                     reservoirs, adaptive kinematic-wave sub-steps, sub-step sizes, soil layers, Kv
+                     profile, mass balance, ...)
   [input]            path_static, path_forcing and the domain maps (LDD, river, subbasin, ...)
   [input.static]     standard name -> netCDF variable (Option 3: a name), a constant
                      ({value = v}, Option 2) or {netcdf_variable_name, scale, offset, layer}
@@ -26,8 +27,7 @@ except ImportError:  # Python < 3.11
     _toml = None
 
 # options of the reference that this step does not run (the caller keeps Wflow's own update)
-UNSUPPORTED_FLAGS = ("glacier__flag", "snow_gravitational_transport__flag", "floodplain_1d__flag", "drain__flag",
-                     "constanthead__flag", "pit__flag")
+UNSUPPORTED_FLAGS = ("floodplain_1d__flag", "drain__flag", "constanthead__flag", "pit__flag")
 
 
 def _entry(v):
@@ -108,6 +108,11 @@ class WflowConfig:
             bad.append(f"saturated_hydraulic_conductivity_profile {prof}")
         if "vegetation__leaf_area_index" in self.raw.get("input", {}).get("cyclic", {}):
             bad.append("leaf-area-index driven interception (cyclic LAI)")
+        snow = self.model.get("snow__flag", False)
+        if self.model.get("glacier__flag", False) and not snow:
+            bad.append("glacier__flag without snow__flag (the reference refuses it, sbm.jl:45-49)")
+        if snow and self.model.get("snow_gravitational_transport__flag", False) and self.reservoirs:
+            bad.append("snow_gravitational_transport__flag with reservoir__flag")
         if bad:
             raise ValueError("not supported by the GPU step: " + ", ".join(bad))
 
@@ -124,6 +129,9 @@ class WflowConfig:
         for i, t in enumerate(layers):
             c.soil_layer_thickness[i] = t * 1e-3
         c.snow = int(bool(m.get("snow__flag", False)))
+        # without snow the transport is a no-op in the reference (surface_process.jl:21)
+        c.snow_gravitational_transport = int(c.snow and bool(m.get("snow_gravitational_transport__flag", False)))
+        c.glacier = int(bool(m.get("glacier__flag", False)))
         c.soil_infiltration_reduction = int(bool(m.get("soil_infiltration_reduction__flag", False)))
         c.water_mass_balance = int(bool(m.get("water_mass_balance__flag", False)))
         c.adaptive_timestep = int(bool(m.get("kinematic_wave__adaptive_time_step_flag", False)))
