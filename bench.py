@@ -15,7 +15,9 @@ library's stream). `e2e` times the same K steps through the public C ABI with ho
 from pinned memory copied in (wf_set_forcing_async: the copy of step k+1 overlaps step k) and
 the outlet discharge copied out every step. Other workloads: `--workload
 large_4096_adaptive_hourly` (4096 x 4096 at 100 m, Courant sub-steps, rain x3) and
-`--workload ragged200_daily` (200 independent catchments of 10^3 - 10^6 cells). The model state
+`--workload ragged200_daily` (200 independent catchments of 10^3 - 10^6 cells), and
+`--workload li_domain_2048_hourly` (local-inertial overland and river routing alone on a 2048 x
+2048 grid, its own JSON line). The model state
 (tens of GB for the ensemble, over 1 GB for one 1024^2 domain) is far larger than the 129 MB
 L2, so no L2 flush is needed between steps.
 """
@@ -46,6 +48,11 @@ WORKLOADS = {
     # uneven batch: 200 independent catchments of 10^3 - 10^6 cells (log-uniform), daily
     "ragged200_daily": (0, 1000.0, 86400.0, 1, 365),
 }
+# Local-inertial routing of the land grid with its river (include/wflow_gb300_li.h), measured by
+# its own driver (run_li): side x side cells of 100 m, a river every 64th row, hourly model steps
+# with the sub-step loop on the device.
+LI_WORKLOADS = {"li_domain_2048_hourly": 2048}
+LI_BYTES_PER_CELL_SUBSTEP = 224 + 96  # land fluxes + land depths per land cell and sub-step
 WORKLOAD_OPTIONS = {
     "large_4096_adaptive_hourly": {"adaptive": True, "precip_scale": 3.0},
     "ragged200_daily": {"ragged": 200},
@@ -363,6 +370,8 @@ def run_gpu(args):
     if form == abi.WF_FORM_SPLIT and not args.no_fp64_leg:
         result.update(fp64_leg(args, cfg, dom, params, resident, W, K, dt, members, n, dev))
         result["split_over_fp64"] = value / result["fp64_plain"]["value"]
+    elif not args.no_fp64_leg:
+        result["accuracy"] = accuracy_leg(args, cfg, dom, params, resident, W + K, dt, members, n, dev)
     model.close()
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(args) if not args.no_cpu_baseline else None
@@ -373,8 +382,7 @@ def run_gpu(args):
 
 def fp64_leg(args, cfg, dom, params, resident, W, K, dt, members, n, dev):
     """Time the FP64 plain form on the same resident forcing (fewer steps: it is slower), then
-    replay both forms over the same steps from the same cold state and compare outlet discharge
-    and the split form's land-balance closure."""
+    measure both forms against the oracle over the warm-up and timed steps (accuracy_leg)."""
     import copy
 
     import torch
@@ -404,42 +412,110 @@ def fp64_leg(args, cfg, dom, params, resident, W, K, dt, members, n, dev):
     m64.synchronize()
     ms64 = ev0.elapsed_time(ev1)
     m64.close()
-    # accuracy: both forms from the cold state over the same steps
+    cells = n * members
+    out = {"fp64_plain": {"value": cells * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
+                          "unit": "cell-timesteps/s"}}
+    out["accuracy"] = accuracy_leg(args, cfg, dom, params, resident, W + K, dt, members, n, dev)
+    return out
+
+
+def closure_of(err, rel):
+    """(max |relative error| as the reference defines it, error / mean of in- and outflow; max of
+    |error| / max(local mean flux, median mean flux)), over the cells of one balance. The local mean
+    flux is |error / relative error| where the relative error is non-zero."""
+    err, rel = np.asarray(err), np.asarray(rel)
+    nz = rel != 0.0
+    flux = np.zeros_like(err)
+    flux[nz] = np.abs(err[nz] / rel[nz])
+    med = float(np.median(flux[nz])) if nz.any() else 1.0
+    return float(np.max(np.abs(rel))), float(np.max(np.abs(err) / np.maximum(flux, med)))
+
+
+def accuracy_leg(args, cfg, dom, params, resident, steps, dt, members, n, dev):
+    """Both GPU forms and the FP64 oracle from the cold state over the warm-up and timed steps (the
+    oracle on the first member of an ensemble, whose parameters and forcing it takes): outlet
+    discharge and storage errors of each form against the oracle, and the land-balance closure of
+    each form and of the oracle, by the reference's definition and against max(local, median) flux.
+    The oracle's cost bounds the steps on the largest workloads (about a minute of host time)."""
+    import copy
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py
+
+    from wflow_gb300 import abi, synthetic
+    from wflow_gb300.model import Model
+
+    steps = max(2, min(steps, int(60 * 1.5e6 / max(n, 1))))
+    cfg64 = copy.copy(cfg)
+    cfg64.form = abi.WF_FORM_FP64
     cfg_s = copy.copy(cfg)
     cfg_s.form = abi.WF_FORM_SPLIT
+    cfg_o = synthetic.make_config(dt, n_members=1, form=abi.WF_FORM_FP64, adaptive=bool(cfg.adaptive_timestep))
+    p0 = dict(params)
+    for k in ("kv_0", "f"):
+        p0[k] = np.ascontiguousarray(np.asarray(params[k])[:n])
     a = Model(cfg64, dom, params=params, device=dev.index or 0)
     b_ = Model(cfg_s, dom, params=params, device=dev.index or 0)
-    worst_q = 0.0
-    closure = {"split": [0.0, 0.0], "fp64": [0.0, 0.0]}  # [max relative error, max |error| / median flux]
-    for s in range(min(W + K, 8)):
+    orc = oracle_py.OracleModel(cfg_o, dom, params=p0)
+    threads = os.cpu_count() or 1
+    slots = a.slot_order()
+    valid = slots >= 0
+    n_out = len(dom.outlets)
+    worst = {"fp64": {"outlet_q": 0.0, "soil_storage": 0.0}, "split": {"outlet_q": 0.0, "soil_storage": 0.0,
+                                                                         "snow_storage": 0.0}}
+    clos = {k: [0.0, 0.0] for k in ("split", "fp64", "oracle")}  # the member the oracle runs
+    if members > 1:
+        clos.update({k: [0.0, 0.0] for k in ("split_all_members", "fp64_all_members")})
+    for s in range(steps):
         r = resident[s]
         for mdl in (a, b_):
             mdl.set_forcing_device_slots(r[0].data_ptr(), r[1].data_ptr(), r[2].data_ptr())
             mdl.update_model()
-        qa, qb = a.outlets(1), b_.outlets(1)
-        worst_q = max(worst_q, float(np.max(np.abs(qb - qa) / np.maximum(np.abs(qa), 1e-12))))
+        # the oracle takes member 0's forcing in cell order (the resident arrays hold slot order)
+        f0 = []
+        for x in r:
+            v = x.reshape(-1, members)[:, 0].cpu().numpy()
+            c = np.zeros(n)
+            c[slots[valid]] = v[valid]
+            f0.append(c)
+        orc.set_forcing(*f0)
+        orc.step(threads)
+        qo = orc.outlets(0)
+        so = orc.get(abi.FIELD["TOTAL_SOIL_WATER_STORAGE"])
+        wo = orc.get(abi.FIELD["SNOW_STORAGE"])
         for name, mdl in (("fp64", a), ("split", b_)):
-            err = mdl.get_value("BALANCE_LAND_ERROR")
-            rel = mdl.get_value("BALANCE_LAND_RELATIVE_ERROR")
-            nz = rel != 0.0
-            flux = np.median(np.abs(err[nz] / rel[nz])) if nz.any() else 1.0
-            closure[name][0] = max(closure[name][0], float(np.max(np.abs(rel))))
-            closure[name][1] = max(closure[name][1], float(np.max(np.abs(err)) / flux))
+            q = mdl.outlets(0)[:n_out]
+            w = worst[name]
+            w["outlet_q"] = max(w["outlet_q"], float(np.max(np.abs(q - qo) / np.maximum(np.abs(qo), 1e-12))))
+            sg = mdl.get_value("TOTAL_SOIL_WATER_STORAGE", count=n)
+            w["soil_storage"] = max(w["soil_storage"], float(np.max(np.abs(sg - so) / so)))
+            if name == "split":
+                wg = mdl.get_value("SNOW_STORAGE", count=n)
+                big = wo > 1e-4
+                if big.any():
+                    w["snow_storage"] = max(w["snow_storage"], float(np.max(np.abs(wg - wo)[big] / wo[big])))
+        for name, get in (("fp64", a.get_value), ("split", b_.get_value),
+                          ("oracle", lambda f: orc.get(abi.FIELD[f]))):
+            err, rel = get("BALANCE_LAND_ERROR"), get("BALANCE_LAND_RELATIVE_ERROR")
+            for key, sl in ((name, slice(0, n)), (name + "_all_members", slice(None))):
+                if key not in clos or (name == "oracle" and sl.stop is None):
+                    continue
+                rel_, flux_ = closure_of(err[sl], rel[sl])
+                clos[key][0] = max(clos[key][0], rel_)
+                clos[key][1] = max(clos[key][1], flux_)
     a.close()
     b_.close()
-    cells = n * members
-    return {"fp64_plain": {"value": cells * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
-                           "unit": "cell-timesteps/s"},
-            "accuracy": {"outlet_q_rel_err_max": worst_q,
-                         "land_balance_closure_rel_max": {"split": closure["split"][0], "fp64": closure["fp64"][0]},
-                         "land_balance_closure_over_median_flux": {"split": closure["split"][1],
-                                                                   "fp64": closure["fp64"][1]},
-                         "closure_note": "relative error as the reference defines it (error / mean of in- and "
-                                         "outflow) peaks in cells whose fluxes are ~1e-12 m/s, for the FP64 "
-                                         "form as well; the flux-normalised figure divides by the median flux",
-                         "steps": min(W + K, 8),
-                         "against": "FP64 plain form on the GPU (bit-identical to the FP64 oracle in the parity "
-                                    "tests)"}}
+    return {"against": "FP64 oracle (CPU restatement of the reference)" +
+                       (", first member of the ensemble" if members > 1 else ""),
+            "steps": steps,
+            "outlet_q_rel_err_max": worst["split"]["outlet_q"],
+            "split": worst["split"], "fp64": worst["fp64"],
+            "land_balance_closure_rel_max": {k: clos[k][0] for k in clos},
+            "land_balance_closure_over_flux": {k: clos[k][1] for k in clos},
+            "closure_note": "rel: error / mean of in- and outflow per cell (mass_balance.jl:84-93), which peaks "
+                            "in cells whose fluxes are ~1e-12 m/s for the oracle as well; over_flux: error / "
+                            "max(local mean flux, median mean flux over the cells), the closure bar of the "
+                            "split form (<= 1e-7)"}
 
 
 def traffic_from_profiles(kernel, workload):
@@ -554,13 +630,74 @@ def run_profile(args):
     dom, params, cfg, pfac = build_workload(args.workload, form, seed=args.seed)
     side, cell, dt, members, _ = WORKLOADS[args.workload]
     model = Model(cfg, dom, params=params)
-    model.set_tuning(vertical_block=128, routing_warps=2, routing_blocks_per_sm=0, use_graph=0, kernel_timing=1)
+    model.set_tuning(vertical_block=128, routing_warps=2, routing_blocks_per_sm=0, use_graph=0, kernel_timing=1,
+                     substep_lanes=args.sub_lanes)
     for s in range(args.steps):
         P, PET, T = member_forcing(s, dt, dom.n_land, members, pfac, seed=args.seed)
         model.run_timestep(P, PET, T)
     kt, calls = model.kernel_times()
     log(f"[profile] {args.workload} {args.form}: ms per step {({k: round(v / max(calls, 1), 3) for k, v in kt.items()})}")
     model.close()
+
+
+def run_li(args):
+    """Local-inertial overland and river routing (wf_li_domain_step) on a synthetic grid: hourly
+    model steps with the sub-step loop on the device (one cooperative launch and one read-back per
+    step), then the same steps driven from the host (a time-step read-back per sub-step) for
+    comparison; land cell-timesteps/s and the achieved bandwidth of the land kernels per
+    sub-step."""
+    import torch
+
+    from wflow_gb300 import build, synthetic
+    from wflow_gb300.li_river import LiDomain
+
+    torch.cuda.set_device(0)
+    build.build_all()
+    side = LI_WORKLOADS[args.workload]
+    land, river, h_river, h_land, runoff = synthetic.li_grid(side, side)
+    n = len(h_land)
+    dt = 3600.0
+    d = LiDomain(land, river, h_river)
+    d.set_state(h_land, h_river)
+    d.set_inputs(runoff)
+    for _ in range(args.warmup):
+        d.step(dt)
+    clocks = ClockSampler(0)
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    k = sum(d.step(dt) for _ in range(args.steps))
+    el = time.perf_counter() - t0
+    clk = clocks.stop()
+    d.set_host_loop(True)
+    t1 = time.perf_counter()
+    k_host = sum(d.step(dt) for _ in range(args.steps))
+    el_host = time.perf_counter() - t1
+    d.close()
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = n * LI_BYTES_PER_CELL_SUBSTEP * k / el / 1e9
+    result = {
+        "metric": "cell-timesteps/s", "value": n * args.steps / el, "unit": "cell-timesteps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (square land grid with a river every 64th row, 5 mm/h runoff, warm state)",
+        "config": {"workload": args.workload, "cells": n, "river_cells": int(river["n_active"]), "dt_s": dt,
+                   "substeps_per_step": k / args.steps,
+                   "l2": "the grid's state (~1 GB) exceeds the 129 MB L2; no flush"},
+        "cell_substeps_per_s": n * k / el,
+        "host_driven_loop": {"ms_per_step": el_host / args.steps * 1e3, "substeps": k_host,
+                             "speedup_of_device_loop": el_host / el},
+        "roofline": {"kernel": "land fluxes + land depths", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+        "clocks": clk,
+    }
+    print(json.dumps(result), flush=True)
 
 
 def main():
@@ -570,17 +707,24 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--form", default="split", choices=["fp64", "split"])
-    ap.add_argument("--workload", default="ensemble64_1024_hourly", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default="ensemble64_1024_hourly", choices=list(WORKLOADS) + list(LI_WORKLOADS))
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64 plain comparison leg")
+    ap.add_argument("--sub-lanes", type=int, default=0,
+                    help="profiler driver: cap of the routing sweeps' sub-step lanes (0: the library default)")
     ap.add_argument("--profile", action="store_true",
                     help="profiler driver: run --steps eager steps of the workload and exit (no JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and not args.profile:
         args.warmup = 3
-    if args.profile:
+    if args.workload in LI_WORKLOADS:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the local-inertial workload has no CPU arm"}))
+        else:
+            run_li(args)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args)
