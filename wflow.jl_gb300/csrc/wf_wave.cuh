@@ -137,22 +137,21 @@ __device__ __forceinline__ void load_ends(const WfDevGraph& g, const WfSweep& sw
 
 // Weighted upstream sum at sub-step s: qin = sum w*q (w = 1 - fraction to river on land, 1 on
 // rivers) in double-FP32, heavy child first, then the light children. `qh` is the heavy child's
-// word of this sub-step, `heavy` whether the node has one (chain position > 0).
+// word of this sub-step, `heavy` whether the node has one (chain position > 0); w0 / w1 are the
+// end_q words of light children 0 / 1 at sub-step s loaded earlier (SENTINEL when not loaded or
+// not yet published).
 template <bool WEIGHTED>
-__device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, const UpRec& r, const Ends& x,
-                                       int64_t slot, int m, int s, bool heavy, unsigned long long qh, int32_t* status,
-                                       wff::ff& qin) {
+__device__ __forceinline__ bool gather_w(const WfDevGraph& g, const WfSweep& sw, const UpRec& r, unsigned long long w0,
+                                         unsigned long long w1, int64_t slot, int m, int s, bool heavy,
+                                         unsigned long long qh, int32_t* status, wff::ff& qin) {
     wff::ff acc = {0.0f, 0.0f};
     if (heavy) {
         const wff::ff q = wff::unpack(qh);
         acc = WEIGHTED ? wff::mul(q, r.w_hv) : q;
     }
     if (r.lt0 >= 0) {
-        unsigned long long first = SENTINEL;
-#pragma unroll
-        for (int j = 0; j < PREFETCH_SUBSTEPS; ++j)
-            if (j == s) first = x.lq0[j];
         const int64_t idx = end_index(g, r.lt0, m, s);
+        unsigned long long first = w0;
         if (first == SENTINEL) first = ld_relaxed(&g.end_q[idx]);
         unsigned long long w;
         if (!await_end(g, sw, idx, first, status, w)) return false;
@@ -161,7 +160,7 @@ __device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, c
     }
     if (r.lt1 >= 0) {
         const int64_t idx = end_index(g, r.lt1, m, s);
-        unsigned long long first = s == 0 ? x.lq1 : SENTINEL;
+        unsigned long long first = w1;
         if (first == SENTINEL) first = ld_relaxed(&g.end_q[idx]);
         unsigned long long w;
         if (!await_end(g, sw, idx, first, status, w)) return false;
@@ -182,6 +181,33 @@ __device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, c
     }
     qin = acc;
     return true;
+}
+
+// The prefetched word of light child 0 at sub-step s (SENTINEL beyond the prefetched ones).
+__device__ __forceinline__ unsigned long long end_word0(const Ends& x, int s) {
+    unsigned long long w = SENTINEL;
+#pragma unroll
+    for (int j = 0; j < PREFETCH_SUBSTEPS; ++j)
+        if (j == s) w = x.lq0[j];
+    return w;
+}
+
+// gather_w with the words of a node-major walk (light child 0 prefetched for the first
+// sub-steps, light child 1 for sub-step 0).
+template <bool WEIGHTED>
+__device__ __forceinline__ bool gather(const WfDevGraph& g, const WfSweep& sw, const UpRec& r, const Ends& x,
+                                       int64_t slot, int m, int s, bool heavy, unsigned long long qh, int32_t* status,
+                                       wff::ff& qin) {
+    return gather_w<WEIGHTED>(g, sw, r, end_word0(x, s), s == 0 ? x.lq1 : SENTINEL, slot, m, s, heavy, qh, status,
+                              qin);
+}
+
+// The end_q words of light children 0 and 1 of record r at sub-step s (SENTINEL for a missing
+// child); a load that finds the producer not yet done also returns the sentinel.
+__device__ __forceinline__ void load_words(const WfDevGraph& g, int m, const UpRec& r, int s, unsigned long long& w0,
+                                           unsigned long long& w1) {
+    w0 = r.lt0 >= 0 ? ld_relaxed(&g.end_q[end_index(g, r.lt0, m, s)]) : SENTINEL;
+    w1 = r.lt1 >= 0 ? ld_relaxed(&g.end_q[end_index(g, r.lt1, m, s)]) : SENTINEL;
 }
 
 // Work items are (chunk, member group) pairs in dependency (chain length) order. One ticket takes
@@ -330,6 +356,222 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
             ck = nk;
             nit = nnit;
             nk = nnk;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------- diagonal schedule ---------
+//
+// A launch of S > 1 fixed sub-steps: sub-step s of the node at chain position k depends only on
+// (k - 1, s) (the heavy child) and (k, s - 1) (the node's own previous state), so the walker
+// gives every chain-member pair SL lanes (a power of two, sw.SL) and runs the sub-steps on a
+// diagonal: in round r lane l takes sub-step r * SL + l, and at time step t it works on the
+// position t - l of the item sequence. A chain of L positions takes ceil(S / SL) rounds of
+// L + SL - 1 time steps instead of the node-major L * S. Lane 0 loads the node inputs (its
+// prefetch pipeline as in walk); at the end of each time step every lane hands the node's
+// inputs, its state after its sub-step and the end_q words of the node's light children for the
+// next sub-step (loaded during the step) to the next lane with one warp shuffle. The heavy
+// child's discharge of a lane's sub-step is the value the lane itself computed one time step
+// earlier. The lane of the last sub-step of a round stores the node state; the next round's lane
+// 0 loads it again.
+//
+// Phys interface beyond walk():
+//   struct St;                                   state carried from sub-step to sub-step
+//   void start(const In&, St&)                   state at the start of a round (from In)
+//   bool sub(const In&, St&, w0, w1, slot, e, m, s, chain, is_end, heavy, qh_in, qh_out)
+//     one sub-step: w0 / w1 the light children's end_q words of sub-step s (or SENTINEL),
+//     qh_in the heavy child's packed discharge of sub-step s, qh_out this node's. False to abort.
+//   void finish(const St&, e, add_stored)        stores after the last sub-step of a round
+//                                                (add_stored: add the stored cumulative sums)
+
+template <class T>
+__device__ __forceinline__ void shfl_up_pod(T& v, int width) {
+    static_assert(sizeof(T) % 4 == 0, "shuffled structs are whole 32-bit words");
+    uint32_t w[sizeof(T) / 4];
+    memcpy(w, &v, sizeof(T));
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) / 4); ++i) w[i] = __shfl_up_sync(0xffffffffu, w[i], 1, width);
+    memcpy(&v, w, sizeof(T));
+}
+
+struct DiagBatch {  // per-warp shared descriptors of the items of the current ticket
+    long long base[BATCH];
+    long long chain0[BATCH];
+    int L[BATCH];
+    int Gc[BATCH];
+    int p0[BATCH];        // first chain-member pair of the item
+    int len[BATCH][32];   // length of each lane's chain (0: the lane idles in that item)
+};
+
+__host__ __device__ constexpr size_t diag_smem(int threads) { return (size_t)(threads / 32) * sizeof(DiagBatch); }
+
+template <class Phys>
+__device__ __forceinline__ void walk_diag(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
+    extern __shared__ unsigned long long wave_smem[];
+    constexpr int DEPTH = Phys::kDepth;
+    using In = typename Phys::In;
+    using St = typename Phys::St;
+    const unsigned lane = threadIdx.x & 31u;
+    DiagBatch* wb = reinterpret_cast<DiagBatch*>(wave_smem) + (threadIdx.x >> 5);
+    const int M = g.M;
+    const int SL = sw.SL;
+    const int J = 32 / SL;
+    const int sl = (int)lane % SL;
+    const int j = (int)lane / SL;
+    const int64_t ipc = wf_items_per_chunk(g.G, M, SL);
+    const int64_t n_items = g.n_chunks * ipc;
+    const int64_t prio = sw.prio_items;
+    const int64_t n_norm = n_items - prio;
+    const int64_t n_short = min(g.n_short_chunks * ipc, n_norm);
+    const int64_t n_sb = (n_short + BATCH - 1) / BATCH;
+    const uint64_t n_tickets = (uint64_t)(prio + n_sb + (n_norm - n_short));
+    const int rounds = (sw.S + SL - 1) / SL;
+    const bool launch_first = sw.first == 0;
+    while (true) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(g.ticket, 1ULL);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n_tickets) return;
+        int64_t first;
+        int count = 1;
+        if ((int64_t)t < prio) {
+            first = n_items - 1 - (int64_t)t;
+        } else {
+            const int64_t u = (int64_t)t - prio;
+            if (u < n_sb) {
+                first = u * BATCH;
+                count = (int)min((int64_t)BATCH, n_short - first);
+            } else {
+                first = n_short + (u - n_sb);
+            }
+        }
+        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
+        if ((int)lane < count) {
+            const int64_t item = first + lane;
+            const int64_t chunk = item / ipc;
+            wb->base[lane] = g.chunk_base[chunk];
+            wb->chain0[lane] = g.chunk_chain0[chunk];
+            wb->L[lane] = g.chunk_len[chunk];
+            wb->Gc[lane] = g.chunk_g[chunk];
+            wb->p0[lane] = (int)(item % ipc) * J;
+        }
+        __syncwarp();
+        int npos = 0, work = 0;
+        for (int it = 0; it < count; ++it) {
+            const int p = wb->p0[it] + j;
+            const int gi = M <= 32 ? p / M : 0;
+            const bool ok = M <= 32 ? gi < wb->Gc[it] : p < M;
+            const int len = ok ? g.chain_len[wb->chain0[it] + gi] : 0;
+            wb->len[it][lane] = len;
+            work |= len;
+            npos += wb->L[it];
+        }
+        __syncwarp();
+        if (!__any_sync(0xffffffffu, work > 0)) continue;  // items past their chunks' pairs
+        auto gi_of = [&](int it) { return M <= 32 ? (wb->p0[it] + j) / M : 0; };
+        auto m_of = [&](int it) { return M <= 32 ? (wb->p0[it] + j) % M : wb->p0[it] + j; };
+        auto slot_of = [&](int it, int k) { return wb->base[it] + (int64_t)k * wb->Gc[it] + gi_of(it); };
+        auto valid = [&](int it, int k) { return it < count && k < wb->len[it][lane]; };
+        auto advance = [&](int& it, int& k) {
+            if (k + 1 < wb->L[it]) {
+                ++k;
+            } else {
+                ++it;
+                k = 0;
+            }
+        };
+        for (int r = 0; r < rounds; ++r) {
+            const int s = r * SL + sl;
+            const int s0 = r * SL;  // lane 0's sub-step
+            const bool last_lane = (s == sw.S - 1) || (sl == SL - 1);
+            // lane 0's pipeline over the sequence positions: cur (this time step), nxt, nn
+            In cur, nxt;
+            unsigned long long c0 = SENTINEL, c1 = SENTINEL, n0 = SENTINEL, n1 = SENTINEL;
+            int cit = 0, ck = 0;
+            if (sl == 0 && valid(cit, ck)) {
+                const int64_t sl0 = slot_of(cit, ck);
+                const int mm = m_of(cit);
+                phys.load(sl0, sl0 * M + mm, mm, cur);
+                load_words(g, mm, cur.up, s0, c0, c1);
+            }
+            int nit = cit, nk = ck;
+            advance(nit, nk);
+            if (DEPTH > 1 && sl == 0 && valid(nit, nk)) {
+                const int64_t sl1 = slot_of(nit, nk);
+                const int mm = m_of(nit);
+                phys.load(sl1, sl1 * M + mm, mm, nxt);
+            }
+            // what this lane works on at the current time step
+            In x;
+            St st;
+            unsigned long long w0 = SENTINEL, w1 = SENTINEL;
+            int pit = count, pk = 0;
+            unsigned long long hq = 0ull;
+            for (int tt = 0; tt < npos + SL - 1; ++tt) {
+                if (sl == 0) {
+                    x = cur;
+                    w0 = c0;
+                    w1 = c1;
+                    pit = cit;
+                    pk = ck;
+                    phys.start(x, st);
+                    // advance the pipeline: the words of nxt, the inputs of the position after it
+                    int nnit = nit, nnk = nk;
+                    if (nnit < count) advance(nnit, nnk);
+                    In nn;
+                    if (DEPTH > 1) {
+                        if (valid(nit, nk)) load_words(g, m_of(nit), nxt.up, s0, n0, n1);
+                        if (valid(nnit, nnk)) {
+                            const int64_t sl2 = slot_of(nnit, nnk);
+                            const int mm = m_of(nnit);
+                            phys.load(sl2, sl2 * M + mm, mm, nn);
+                        }
+                    } else if (valid(nit, nk)) {
+                        const int64_t sl1 = slot_of(nit, nk);
+                        const int mm = m_of(nit);
+                        phys.load(sl1, sl1 * M + mm, mm, nxt);
+                        load_words(g, mm, nxt.up, s0, n0, n1);
+                    }
+                    cur = nxt;
+                    c0 = n0;
+                    c1 = n1;
+                    n0 = n1 = SENTINEL;
+                    if (DEPTH > 1) nxt = nn;
+                    cit = nit;
+                    ck = nk;
+                    nit = nnit;
+                    nk = nnk;
+                }
+                bool ok = true;
+                unsigned long long v0 = SENTINEL, v1 = SENTINEL;  // words of sub-step s + 1 for the next lane
+                if (pit < count && pk < wb->len[pit][lane] && s < sw.S) {
+                    const int64_t slot = slot_of(pit, pk);
+                    const int mm = m_of(pit);
+                    const int64_t e = slot * M + mm;
+                    if (sl + 1 < SL && s + 1 < sw.S) load_words(g, mm, x.up, s + 1, v0, v1);
+                    unsigned long long out = 0ull;
+                    ok = phys.sub(x, st, w0, w1, slot, e, mm, s, wb->chain0[pit] + gi_of(pit),
+                                  pk == wb->len[pit][lane] - 1, pk > 0, hq, out);
+                    hq = out;
+                    if (ok && last_lane) phys.finish(st, e, r > 0 || !launch_first);
+                }
+                if (__any_sync(0xffffffffu, !ok)) return;
+                // hand the node to the next lane
+                shfl_up_pod(x, SL);
+                shfl_up_pod(st, SL);
+                const int pit_up = __shfl_up_sync(0xffffffffu, pit, 1, SL);
+                const int pk_up = __shfl_up_sync(0xffffffffu, pk, 1, SL);
+                const unsigned long long v0_up = __shfl_up_sync(0xffffffffu, v0, 1, SL);
+                const unsigned long long v1_up = __shfl_up_sync(0xffffffffu, v1, 1, SL);
+                if (sl > 0) {
+                    pit = pit_up;
+                    pk = pk_up;
+                    w0 = v0_up;
+                    w1 = v1_up;
+                }
+                __syncwarp();
+            }
         }
         __syncwarp();
     }

@@ -2,10 +2,12 @@
 
 The wavefront kernels are bound by the latency of the longest chain and by how many warps
 share an SM's FP64 pipe while the short chains drain, so the best number of resident warps
-depends on the graph (chain-length distribution) and the form; the per-cell kernels depend on
-the block size. The tuner times a few steps of each candidate with per-kernel CUDA events
-and keeps the fastest for each kernel family. Candidates only change the schedule, never
-the result: the wavefront produces the same values for any dispatch order.
+depends on the graph (chain-length distribution) and the form; a sweep of several sub-steps also
+depends on how many lanes share a chain-member pair on the diagonal schedule (more lanes: a
+shorter critical path, fewer pairs per warp); the per-cell kernels depend on the block size. The
+tuner times a few steps of each candidate with per-kernel CUDA events and keeps the fastest for
+each kernel family. Candidates only change the schedule, never the result: the wavefront
+produces the same values for any dispatch order and any lane count.
 """
 
 import itertools
@@ -27,12 +29,12 @@ def _time_steps(model: Model, forcing, steps):
 def tune(model: Model, forcing, steps=1, verbose=False):
     """Pick routing warps/blocks per SM and the per-cell block size; returns the choice and the
     measured milliseconds per step of each candidate."""
-    model._tune_state = dict(vertical_block=0, routing_warps=0, routing_blocks_per_sm=0)
+    model._tune_state = dict(vertical_block=0, routing_warps=0, routing_blocks_per_sm=0, substep_lanes=0)
     _time_steps(model, forcing, 1)  # warm-up
     results = []
     best_route, best_route_t = None, float("inf")
     for warps, bps in itertools.product([2, 4], [1, 2, 4, 0]):
-        model._tune_state = dict(vertical_block=0, routing_warps=warps, routing_blocks_per_sm=bps)
+        model._tune_state = dict(vertical_block=0, routing_warps=warps, routing_blocks_per_sm=bps, substep_lanes=0)
         t = _time_steps(model, forcing, steps)
         route = t["subsurface"] + t["overland"] + t["river"]
         results.append(("routing", warps, bps, route))
@@ -40,17 +42,34 @@ def tune(model: Model, forcing, steps=1, verbose=False):
             print(f"routing warps={warps} blocks/SM={bps}: {route:.3f} ms")
         if route < best_route_t:
             best_route, best_route_t = (warps, bps), route
+    # sub-step lanes of the sweeps with several sub-steps per launch (river 900 s in an hourly
+    # step, daily overland and river)
+    m = model.metrics()
+    best_lanes = 0
+    if m["steps"] > 0 and max(m["substeps_land"], m["substeps_river"]) > m["steps"]:
+        best_lanes_t = best_route_t
+        for lanes in [1, 2, 4, 16]:  # 0 (the default, 8) was measured above
+            model._tune_state = dict(vertical_block=0, routing_warps=best_route[0],
+                                     routing_blocks_per_sm=best_route[1], substep_lanes=lanes)
+            t = _time_steps(model, forcing, steps)
+            route = t["subsurface"] + t["overland"] + t["river"]
+            results.append(("lanes", lanes, 0, route))
+            if verbose:
+                print(f"sub-step lanes={lanes}: {route:.3f} ms")
+            if route < best_lanes_t:
+                best_lanes, best_lanes_t = lanes, route
     best_block, best_block_t = 0, float("inf")
     for block in [128, 256]:
         model._tune_state = dict(vertical_block=block, routing_warps=best_route[0],
-                                 routing_blocks_per_sm=best_route[1])
+                                 routing_blocks_per_sm=best_route[1], substep_lanes=best_lanes)
         t = _time_steps(model, forcing, steps)
         results.append(("vertical", block, 0, t["vertical"]))
         if verbose:
             print(f"vertical block={block}: {t['vertical']:.3f} ms")
         if t["vertical"] < best_block_t:
             best_block, best_block_t = block, t["vertical"]
-    choice = dict(vertical_block=best_block, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1])
+    choice = dict(vertical_block=best_block, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1],
+                  substep_lanes=best_lanes)
     model._tune_state = choice
     model.set_tuning(**choice, use_graph=1)
     return choice, results

@@ -137,13 +137,17 @@ class Model:
         return {k: getattr(m, k) for k, _ in abi.WfMetrics._fields_}
 
     def set_tuning(self, vertical_block=0, routing_warps=0, routing_blocks_per_sm=0, use_graph=1,
-                   wait_budget_us=0, wait_offset=0, kernel_timing=0):
+                   wait_budget_us=0, wait_offset=0, kernel_timing=0, substep_lanes=0):
+        """Launch shape of the step's kernels (results do not depend on it): threads per block of
+        the per-cell kernels, warps per block and blocks per SM of the routing sweeps, the cap of
+        the sub-step lanes of their diagonal schedule (0: default), the CUDA graph, and test hooks."""
         t = abi.WfTuning()
         t.vertical_block, t.routing_warps, t.routing_blocks_per_sm, t.use_graph = (
             vertical_block, routing_warps, routing_blocks_per_sm, use_graph)
         t.reserved[0] = wait_budget_us
         t.reserved[1] = wait_offset
         t.reserved[2] = kernel_timing
+        t.reserved[3] = substep_lanes
         self._check(self.lib.wf_set_tuning(self.h, C.byref(t)), "wf_set_tuning")
 
     def stream(self):
