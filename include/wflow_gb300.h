@@ -6,8 +6,8 @@
  *   compute_mass_balance!(model)  Wflow/src/mass_balance.jl:541-545
  * which Wflow calls through the `update_func` seam of
  *   run_timestep!(model; update_func = update_model!)  Wflow/src/Wflow.jl:311-322
- * A Julia caller binds these entry points with `ccall`; every argument
- * is a plain pointer, size or POD struct. All device memory, the CUDA stream and the
+ * A Julia caller binds these entry points with `ccall`; every argument is a plain pointer,
+ * size or POD struct. All device memory, the CUDA stream and the
  * captured CUDA graph of a step belong to the handle. Input arrays are copied at call time
  * and never retained.
  *
@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define WF_ABI_VERSION 1
+#define WF_ABI_VERSION 2
 #define WF_MAX_LAYERS 8
 
 typedef enum WfStatus {
@@ -72,7 +72,9 @@ typedef struct WfConfig {
     int32_t form;                                     /* WfForm */
     int32_t n_members;                                /* ensemble members sharing the domain (>= 1) */
     int32_t per_member_soil;                          /* kv_0 and f given per member (n_land*n_members) */
-    int32_t reserved[7];
+    int32_t snow_gravitational_transport;             /* snow_gravitational_transport__flag (with snow) */
+    int32_t glacier;                                  /* glacier__flag (with snow, sbm.jl:36-53) */
+    int32_t reserved[5];
 } WfConfig;
 
 /* Drainage network and shared geometry (Wflow/src/domain.jl:1-45, network.jl:47-258).
@@ -146,6 +148,13 @@ typedef struct WfParams {
     const double* kv_factor;                           /* [n_land * n_layers] */
     /* lateral subsurface (routing/subsurface/lateral_subsurface_flow.jl:87-132) */
     const double* horizontal_to_vertical_ratio;        /* KsatHorFrac [-] */
+    /* HBV glacier (glacier/glacier.jl:58-98), read with the glacier flag; NULL takes the
+     * reference's default (standard_name/standard_name_sbm.jl:70-108) */
+    const double* glacier_fraction;                    /* glacier_surface__area_fraction [-] (0) */
+    const double* glacier_temperature_threshold_melt;  /* [K] (273.15) */
+    const double* glacier_degree_day_factor;           /* [m K-1 s-1] (3 mm degC-1 d-1) */
+    const double* glacier_snow_to_ice_fraction;        /* [s-1] (0.001 d-1) */
+    const double* glacier_initial_store;               /* glacier_ice__initial_leq_depth [m] (5.5) */
 } WfParams;
 
 /* Per-cell and per-river-cell variables exposed through get/set (BMI get_value/set_value,
@@ -194,6 +203,10 @@ typedef enum WfField {
     WF_F_BALANCE_SUBSURFACE_RELATIVE_ERROR,
     WF_F_VOLUMETRIC_WATER_CONTENT,  /* layered */
     WF_F_LAND_QIN_AVERAGE,          /* overland inflow from upstream cells, step average [m3 s-1] */
+    WF_F_GLACIER_STORE,             /* glacier_ice__leq_depth [m] (glacier flag) */
+    WF_F_GLACIER_MELT,              /* glacier_ice__melt_volume_flux [m s-1] (glacier flag) */
+    WF_F_SNOW_IN,                   /* snow moved in from upstream cells [m s-1] (transport flag) */
+    WF_F_SNOW_OUT,                  /* snow moved on to the downstream cell [m s-1] (transport flag) */
     WF_F_LAND_END_,
     /* river */
     WF_F_RIVER_Q = 100,
@@ -284,7 +297,8 @@ typedef struct WfTuning {
     int32_t routing_warps;    /* warps per block of the routing wavefront kernels */
     int32_t routing_blocks_per_sm;
     int32_t use_graph;        /* capture the step in a CUDA graph (1 = yes, default) */
-    int32_t reserved[4];
+    int32_t reserved[4];      /* [0] wait budget (us), [1] test hook (0), [2] per-kernel timing,
+                               * [3] cap of the routing sweeps' sub-step lanes (0 = default 8) */
 } WfTuning;
 
 /* Library version / ABI check. */
@@ -345,7 +359,10 @@ int32_t wf_step_async(WfHandle* h);
  *     8 * chains * members * sub-steps per launch) bytes for the larger of the land and river
  *     graphs, are rejected with WF_ERR_UNSUPPORTED and a message giving the need.
  *   - The first call on a device looks the array's address up (cudaGetSymbolAddress, with that
- *     device current); make that first call before any stream capture.
+ *     device current). Under CUDA's lazy module loading (the default) that lookup can also be
+ *     what loads the library's module and with it the array, so make the first call at set-up:
+ *     before any stream capture and before the host hands the rest of the device memory to a
+ *     pool of its own. Later calls load and allocate nothing.
  *   - Every call on a device shares the array, which keeps the last call's contents; each sweep
  *     clears what must start at zero before it runs. Calls that overlap on the GPU (handles
  *     stepped concurrently from different streams or threads) race on the array and must be

@@ -59,8 +59,15 @@ int32_t wf_li_river_stable_timestep(WfLiRiver* r, double* dt);
 int32_t wf_li_river_substep(WfLiRiver* r, double dt_s);
 /* A model step of dt (update_river_flow_model!): the cumulative discharge restarts at zero,
  * sub-steps of the stable time step run until dt, and the average discharge becomes the
- * cumulative discharge / dt; the number of sub-steps taken goes to *substeps (may be NULL). */
+ * cumulative discharge / dt; the number of sub-steps taken goes to *substeps (may be NULL).
+ * The sub-step loop runs on the device in one cooperative launch (the time step is reduced, the
+ * edges and then the cells updated, with grid barriers between; one read-back per step); every
+ * barrier wait is bounded, and one that runs out returns WF_ERR_SPIN. */
 int32_t wf_li_river_step(WfLiRiver* r, double dt, int64_t* substeps);
+/* host_loop != 0: drive the sub-steps of wf_li_river_step from the host instead (one time step
+ * read-back and two kernel launches per sub-step; the same results). No counterpart in the
+ * reference. */
+int32_t wf_li_river_set_host_loop(WfLiRiver* r, int32_t host_loop);
 /* Copy a field to host: 0 depth h [n], 1 storage [n], 2 discharge q [n_edges],
  * 3 cumulative discharge, the sum of q * dt_s [n_edges], 4 average discharge of the last
  * model step [n_edges], 5 storage clipped at zero (error) [n], 6 actual abstraction of the
@@ -163,8 +170,11 @@ int32_t wf_li_domain_set_inputs(WfLiDomain* d, const double* runoff, const doubl
  * river's over its active cells (not the ghost cells), the land's over cells without a river. */
 int32_t wf_li_domain_stable_timestep(WfLiDomain* d, double* dt);
 int32_t wf_li_domain_substep(WfLiDomain* d, double dt_s);
-/* A model step: cumulative discharges and abstraction restart, sub-steps until dt, averages. */
+/* A model step: cumulative discharges and abstraction restart, sub-steps until dt, averages.
+ * The sub-step loop runs on the device in one cooperative launch, as for wf_li_river_step. */
 int32_t wf_li_domain_step(WfLiDomain* d, double dt, int64_t* substeps);
+/* host_loop != 0: drive the sub-steps of wf_li_domain_step from the host (the same results). */
+int32_t wf_li_domain_set_host_loop(WfLiDomain* d, int32_t host_loop);
 int32_t wf_li_domain_get(WfLiDomain* d, int32_t field, double* dst);
 
 #ifdef __cplusplus

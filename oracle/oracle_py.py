@@ -51,6 +51,8 @@ def lib():
         L.orc_model_set.argtypes = [C.c_void_p, _i32, _i32, _pd]
         L.orc_model_outlets.argtypes = [C.c_void_p, _i32, _pd, C.POINTER(_i64)]
         L.orc_model_substeps.argtypes = [C.c_void_p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]
+        L.orc_topo_order_dfs.restype = _i32
+        L.orc_topo_order_dfs.argtypes = [_i64, C.POINTER(_i32), C.POINTER(_i64)]
         for name in ["orc_head_brooks_corey", "orc_vwc_brooks_corey", "orc_feddes_h3", "orc_rwu_reduction_feddes",
                      "orc_soil_temperature", "orc_infiltration_reduction_factor",
                      "orc_soil_evaporation_unsaturated_store", "orc_soil_evaporation_saturated_store", "orc_scurve",

@@ -1009,6 +1009,11 @@ struct OrcModel {
     std::vector<double> P, PET, T;
     std::vector<double> canopy_storage, canopy_potevap, interception_rate, throughfall, stemflow;
     std::vector<double> snow_storage, snow_water, swe, snow_melt, snow_runoff;
+    // lateral snow transport and glacier (snow_gravitational_transport__flag, glacier__flag)
+    bool snow_transport = false, glacier = false;
+    std::vector<int64_t> dfs_order;                  // topological_sort_by_dfs of the land graph
+    std::vector<double> g_frac, g_ttm, g_ddf, g_sifrac;  // per cell
+    std::vector<double> glacier_store, glacier_melt, snow_in, snow_out;  // per member and cell
     std::vector<double> wfs, runoff_river, net_runoff_river, runoff_land, ae_land, ae_river;
     std::vector<double> ssf_zi, ssf_head, ssf_exf_cum, ssf_exf_avg, ssf_q, ssf_q_cum, ssf_q_avg, ssf_qin,
         ssf_qin_cum, ssf_qin_avg, ssf_tr_cum, ssf_tr_avg, ssf_qnet, ssf_qnet_cum, ssf_qnet_avg, ssf_storage;
@@ -1050,6 +1055,36 @@ void build_ups(int64_t n, const int32_t* ds, std::vector<std::vector<int32_t>>& 
     ups.assign(n, {});
     for (int64_t i = 0; i < n; ++i)
         if (ds[i] >= 0) ups[ds[i]].push_back((int32_t)i);  // ascending i
+}
+
+// Graphs.jl v1.14 topological_sort_by_dfs (Wflow's network.order, network.jl:99), restated for a
+// graph of out-degree <= 1: vertices are visited in index order; from an unvisited vertex the
+// search follows the downstream links while they lead to unvisited vertices and finishes the
+// path from its downstream end back; the order is the reverse of the finishing order.
+bool topo_sort_dfs(int64_t n, const int32_t* ds, std::vector<int64_t>& order) {
+    std::vector<uint8_t> color(n, 0);
+    std::vector<int64_t> verts, stack;
+    verts.reserve(n);
+    for (int64_t v = 0; v < n; ++v) {
+        if (color[v]) continue;
+        stack.assign(1, v);
+        color[v] = 1;
+        while (!stack.empty()) {
+            const int64_t u = stack.back();
+            const int32_t w = ds[u];
+            if (w >= 0 && color[w] == 1) return false;  // a cycle
+            if (w >= 0 && color[w] == 0) {
+                color[w] = 1;
+                stack.push_back(w);
+            } else {
+                color[u] = 2;
+                verts.push_back(u);
+                stack.pop_back();
+            }
+        }
+    }
+    order.assign(verts.rbegin(), verts.rend());
+    return true;
 }
 
 inline double prm(const double* p, int64_t i, double dflt) { return p ? p[i] : dflt; }
@@ -1133,6 +1168,30 @@ int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p
     cp(m->tti, p->temperature_interval_snowfall, n);
     cp(m->ttm, p->temperature_threshold_melt, n);
     cp(m->whc, p->water_holding_capacity, n);
+    // lateral snow transport and glacier (sbm.jl:36-53: a glacier needs the snow model)
+    m->snow_transport = c->snow_gravitational_transport != 0;
+    m->glacier = c->glacier != 0;
+    if ((m->snow_transport || m->glacier) && !c->snow) {
+        m->err = "gravitational snow transport and glaciers need the snow model (snow__flag)";
+        *out = m;
+        return WF_ERR_INVALID;
+    }
+    if (m->snow_transport && !topo_sort_dfs(n, m->ds.data(), m->dfs_order)) {
+        m->err = "cycle in land drainage graph";
+        *out = m;
+        return WF_ERR_CYCLE;
+    }
+    m->g_frac.assign(n, 0.0);
+    m->g_ttm.assign(n, 0.0);
+    m->g_ddf.assign(n, 0.0);
+    m->g_sifrac.assign(n, 0.0);
+    for (int64_t i = 0; i < n && m->glacier; ++i) {  // defaults: standard_name_sbm.jl:70-108, to SI
+        // without a glacier model the fraction is zero (NoGlacierModel, glacier.jl:160-166)
+        m->g_frac[i] = prm(p->glacier_fraction, i, 0.0);
+        m->g_ttm[i] = prm(p->glacier_temperature_threshold_melt, i, 0.0 + ABSOLUTE_ZERO_C);
+        m->g_ddf[i] = prm(p->glacier_degree_day_factor, i, 3.0 * MM_PER_DAY_FACTOR);
+        m->g_sifrac[i] = prm(p->glacier_snow_to_ice_fraction, i, 0.001 * (1.0 / 86400.0));
+    }
 
     // soil parameters (soil.jl:319-617) and cold state (soil.jl:152-200), per member
     const int64_t nm = n * M;
@@ -1237,6 +1296,10 @@ int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p
     z(m->throughfall, nm, 0.0); z(m->stemflow, nm, 0.0);
     z(m->snow_storage, nm, 0.0); z(m->snow_water, nm, 0.0); z(m->swe, nm, 0.0); z(m->snow_melt, nm, 0.0);
     z(m->snow_runoff, nm, 0.0);
+    z(m->glacier_store, nm, 0.0); z(m->glacier_melt, nm, 0.0); z(m->snow_in, nm, 0.0); z(m->snow_out, nm, 0.0);
+    if (m->glacier)
+        for (int mbr = 0; mbr < M; ++mbr)
+            for (int64_t i = 0; i < n; ++i) m->glacier_store[mbr * n + i] = prm(p->glacier_initial_store, i, 5.5);
     z(m->wfs, nm, 0.0); z(m->runoff_river, nm, 0.0); z(m->net_runoff_river, nm, 0.0); z(m->runoff_land, nm, 0.0);
     z(m->ae_land, nm, 0.0); z(m->ae_river, nm, 0.0);
     for (auto* v : {&m->ssf_head, &m->ssf_exf_cum, &m->ssf_exf_avg, &m->ssf_q, &m->ssf_q_cum, &m->ssf_q_avg,
@@ -1285,6 +1348,14 @@ int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p
 
 void orc_model_destroy(OrcModel* m) { delete m; }
 
+// The land graph order of the snow transport (topological_sort_by_dfs); 0, or -3 on a cycle.
+int32_t orc_topo_order_dfs(int64_t n, const int32_t* ds, int64_t* order) {
+    std::vector<int64_t> v;
+    if (!topo_sort_dfs(n, ds, v)) return WF_ERR_CYCLE;
+    for (int64_t k = 0; k < n; ++k) order[k] = v[k];
+    return WF_OK;
+}
+
 // The model with reservoirs (ReservoirModel, routing/surface/reservoir.jl:290-300). Reservoir
 // outlet cells are pits of the land and river upstream lists (domain.jl:95-121,
 // utils.jl:61-71); the topological orders stay those of the full graphs, which remain valid.
@@ -1301,6 +1372,7 @@ int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, c
     };
     if (nres < 0 || !rs->river_index || !rs->outflow_curve_type || !rs->area || !rs->waterlevel)
         return fail("reservoir arrays missing");
+    if (m->snow_transport) return fail("gravitational snow transport with reservoirs is not supported");
     m->nres = nres;
     m->res_of_river.assign(nr, -1);
     m->res_land.assign(nres, -1);
@@ -1383,7 +1455,8 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
     if (c.water_mass_balance) {
         for (int64_t i = 0; i < n; ++i) {
             m->bl_prev[o + i] = soil[i].total_soil_water_storage + m->canopy_storage[o + i] +
-                                (m->snow_storage[o + i] + m->snow_water[o + i]) + 0.0 * 0.0 + 0.0;
+                                (m->snow_storage[o + i] + m->snow_water[o + i]) +
+                                m->glacier_store[o + i] * m->g_frac[i] + 0.0;
             m->bo_prev[o + i] = m->ol_storage[o + i];
         }
         for (int64_t r = 0; r < nr; ++r) m->br_prev[orr + r] = m->rv_storage[orr + r];
@@ -1409,7 +1482,6 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
         m->stemflow[j] = out[2];
         m->canopy_storage[j] = out[3];
         // snow (snow.jl:238-293)
-        double wfs_runoff;
         if (c.snow) {
             double effective_precip = m->throughfall[j] + m->stemflow[j];
             double sp[2];
@@ -1421,11 +1493,32 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
             m->swe[j] = out[2];
             m->snow_melt[j] = out[3];
             m->snow_runoff[j] = out[4];
-            wfs_runoff = m->snow_runoff[j] + 0.0 * 0.0;  // runoff.jl:49-58 (no glacier)
         } else {
-            wfs_runoff = m->throughfall[j] + m->stemflow[j];  // runoff.jl:37-46
+            m->wfs[j] = m->throughfall[j] + m->stemflow[j];  // runoff.jl:37-46
         }
-        m->wfs[j] = wfs_runoff;
+    }
+    // ---- lateral_snow_transport! (surface_process.jl:1-19), in the land graph's topological
+    // order (sbm.jl:97-99)
+    if (m->snow_transport)
+        orc_lateral_snow_transport(m->ds.data(), m->ds.data(), m->dfs_order.data(), n, dt, m->slope.data(),
+                                   m->snow_storage.data() + o, m->snow_water.data() + o, m->snow_out.data() + o,
+                                   m->snow_in.data() + o);
+#pragma omp parallel for num_threads(n_threads) schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t j = o + i;
+        const double PET = m->PET[j], T = m->T[j];
+        double out[5];
+        // update_glacier_model! (glacier.jl:122-154, sbm.jl:102)
+        if (m->glacier) {
+            glacier_hbv(m->g_frac[i], m->glacier_store[j], m->snow_storage[j], T, m->g_ttm[i], m->g_ddf[i],
+                        m->g_sifrac[i], 8.0 * MM_PER_DAY_FACTOR, dt, out);
+            m->snow_storage[j] = out[0];
+            m->glacier_store[j] = out[2];
+            m->glacier_melt[j] = out[3];
+        }
+        // water flux at the surface (runoff.jl:49-58)
+        if (c.snow) m->wfs[j] = m->snow_runoff[j] + m->glacier_melt[j] * m->g_frac[i];
+        const double wfs_runoff = m->wfs[j];
         // open water runoff (runoff.jl:61-111)
         double wd_land = m->ol_h[j];
         int32_t r = m->land_river[i];
@@ -1437,7 +1530,7 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
         m->net_runoff_river[j] = m->runoff_river[j] - m->ae_river[j];
         // soil_fraction! (soil.jl:643-655)
         OrcSoil& s = soil[i];
-        s.soil_fraction = jmax(m->gap[i] - m->water_fraction[i] - m->river_fraction[i] - 0.0, 0.0);
+        s.soil_fraction = jmax(m->gap[i] - m->water_fraction[i] - m->river_fraction[i] - m->g_frac[i], 0.0);
         update_bc_soil_model(s, m->canopy_potevap[j], m->interception_rate[j], PET, wfs_runoff, m->runoff_river[j],
                              m->runoff_land[j]);
         update_soil_water_flow(s, T, c.snow != 0, c.soil_infiltration_reduction != 0, m->ae_river[j], m->ae_land[j],
@@ -1668,7 +1761,8 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
     }
     for (int64_t i = 0; i < n; ++i) {
         int64_t j = o + i;
-        m->total_storage[j] += m->snow_storage[j] + m->snow_water[j] + 0.0 * 0.0 + m->canopy_storage[j] + 0.0;
+        m->total_storage[j] += m->snow_storage[j] + m->snow_water[j] + m->glacier_store[j] * m->g_frac[i] +
+                               m->canopy_storage[j] + 0.0;
         double sub_surface = soil[i].unsaturated_store_depth + soil[i].saturated_water_depth;
         double lateral = m->ol_h[j] * (1.0 - m->river_fraction[i]);
         m->total_storage[j] += sub_surface + lateral;
@@ -1680,14 +1774,14 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
             int64_t j = o + i;
             double area_i = m->area[i];
             double subsurface_flux_in = m->ssf_qin_avg[j] / area_i;
-            double total_in = subsurface_flux_in + (m->P[j] + 0.0) + 0.0 + 0.0 / m->area[i];
+            double total_in = subsurface_flux_in + (m->P[j] + 0.0) + m->snow_in[j] + 0.0 / m->area[i];
             double subsurface_flux_out = m->ssf_q_avg[j] / area_i;
             const OrcSoil& s = soil[i];
             double vertical_flux_out =
                 s.net_runoff + s.actual_evapotranspiration + m->net_runoff_river[j] + s.actual_leakage + 0.0;
-            double total_out = subsurface_flux_out + vertical_flux_out + 0.0 + 0.0 / m->area[i];
+            double total_out = subsurface_flux_out + vertical_flux_out + m->snow_out[j] + 0.0 / m->area[i];
             double storage = s.total_soil_water_storage + m->canopy_storage[j] +
-                             (m->snow_storage[j] + m->snow_water[j]) + 0.0 * 0.0 + 0.0;
+                             (m->snow_storage[j] + m->snow_water[j]) + m->glacier_store[j] * m->g_frac[i] + 0.0;
             double storage_rate = (storage - m->bl_prev[j]) / dt;
             compute_mass_balance_error(total_in, total_out, storage_rate, eo);
             m->bl_err[j] = eo[0];
@@ -2172,6 +2266,10 @@ static double* land_field(OrcModel* m, int field, std::vector<double>** vec) {
         case WF_F_BALANCE_OVERLAND_RELATIVE_ERROR: *vec = &m->bo_rel; break;
         case WF_F_BALANCE_SUBSURFACE_ERROR: *vec = &m->bs_err; break;
         case WF_F_BALANCE_SUBSURFACE_RELATIVE_ERROR: *vec = &m->bs_rel; break;
+        case WF_F_GLACIER_STORE: *vec = &m->glacier_store; break;
+        case WF_F_GLACIER_MELT: *vec = &m->glacier_melt; break;
+        case WF_F_SNOW_IN: *vec = &m->snow_in; break;
+        case WF_F_SNOW_OUT: *vec = &m->snow_out; break;
         default: break;
     }
     return *vec ? (*vec)->data() : nullptr;

@@ -134,6 +134,9 @@ double orc_quantile(double* v, int64_t n, double p);
  * routing/utils.jl:144-148) */
 void orc_accucapacityflux(const int32_t* ds, const int64_t* order, int64_t n, double dt, const double* capacity,
                           double* material, double* flux);
+/* Graphs.jl topological_sort_by_dfs of a graph of out-degree <= 1 (Wflow's network.order):
+ * the order in which the model's snow transport hands material on. 0, or -3 on a cycle. */
+int32_t orc_topo_order_dfs(int64_t n, const int32_t* ds, int64_t* order);
 void orc_lateral_snow_transport(const int32_t* ds, const int32_t* ups_ds, const int64_t* order, int64_t n, double dt,
                                 const double* slope, double* snow_storage, double* snow_water, double* snow_out,
                                 double* snow_in);

@@ -179,11 +179,12 @@ def test_land_domain_dry_time_step(host_lib):
 
 
 def test_bench_grid_is_valid_and_matches_oracle(host_lib):
-    """The throughput grid of wflow_gb300.li_bench: every river cell in one land cell, edges in
-    range, and its first sub-steps on the host build equal to the oracle's."""
+    """The throughput grid of the local-inertial benchmark workload (synthetic.li_grid): every
+    river cell in one land cell, edges in range, and its first sub-steps on the host build equal
+    to the oracle's."""
     from li_cases import OracleLiDomain
-    from wflow_gb300 import li_bench
-    land, river, h_river, h_land, runoff = li_bench.grid(96, 100)
+    from wflow_gb300 import synthetic
+    land, river, h_river, h_land, runoff = synthetic.li_grid(96, 100)
     ri, nra = land["river_index"], river["n_active"]
     assert sorted(ri[ri >= 0].tolist()) == list(range(nra))
     assert river["src"].max() < nra and river["dst"].max() < len(river["zb"])

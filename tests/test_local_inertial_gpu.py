@@ -246,3 +246,34 @@ def test_create_rejects_bad_networks():
         make(alpha=0.0)
     with pytest.raises(ValueError, match="zb_edge"):
         make(zb_e=net["zb_e"][:-1])
+
+
+@pytest.mark.gpu
+def test_device_and_host_sub_step_loops_agree(gpu_lib):
+    """The device-side sub-step loop (one cooperative launch per model step, grid barriers) and
+    the host-driven loop take the same sub-steps to the same states, bit for bit, for the river
+    alone and for the land grid with its river."""
+    from li_cases import random_land_domain
+    net = random_river(2)
+    a, b = _river(net), _river(net)
+    b.set_host_loop(True)
+    for m in (a, b):
+        m.set_state(net["h"])
+        m.set_inwater(net["inwater"])
+        m.set_boundary(net["external_inflow"], net["abstraction"])
+    for step in range(3):
+        assert a.step(3600.0) == b.step(3600.0), step
+        for f in FIELDS:
+            assert np.array_equal(a.get(f), b.get(f)), (step, f)
+    land, river, h_river, state, inputs = random_land_domain(3)
+    c, d = _domain(land, river, h_river), _domain(land, river, h_river)
+    d.set_host_loop(True)
+    for m in (c, d):
+        m.set_state(**state)
+        m.set_inputs(**inputs)
+    for step in range(3):
+        assert c.step(3600.0) == d.step(3600.0), step
+        for f in DOMAIN_FIELDS:
+            assert np.array_equal(c.get(f), d.get(f)), (step, f)
+    for m in (a, b, c, d):
+        m.close()

@@ -18,6 +18,8 @@
 #include "wf_launch.cuh"
 #include "wf_math.cuh"
 #include "wf_reservoir.cuh"
+#include "snow_scheme.cuh"
+#include "wf_ff.cuh"
 #include "wf_walker.cuh"
 
 using wfm::jclamp;
@@ -395,7 +397,31 @@ __device__ void kinematic_wave_ssf(double q_in, double q_prev, double zi_prev, d
 
 // ----------------------------------------------------------------- vertical kernel ------
 
-template <int MAXN>
+// glacier_store * glacier_fraction of a cell (compute_total_storage, mass_balance.jl:96-113); the
+// reference's zero term without a glacier
+__device__ __forceinline__ double glacier_storage(const WfDevFields& F, int64_t e, int64_t slot) {
+    return F.glacier ? F.GM[GM_STORE][e] * F.G[G_FRAC][slot] : 0.0 * 0.0;
+}
+
+// update_glacier_model! (glacier.jl:122-154) of one cell: glacier_hbv (snow_scheme.cuh) on its
+// snow storage and glacier store. Returns the melt rate.
+__device__ __forceinline__ double glacier_update(const WfDevFields& F, int64_t e, int64_t slot, double T, double dt,
+                                                 double& snow) {
+    double store, melt;
+    wfsn::glacier_hbv(F.G[G_FRAC][slot], F.GM[GM_STORE][e], snow, T, F.G[G_TTM][slot], F.G[G_DDF][slot],
+                      F.G[G_SIFRAC][slot], F.g_max_rate, dt, &snow, &store, &melt);
+    F.GM[GM_STORE][e] = store;
+    F.GM[GM_MELT][e] = melt;
+    return melt;
+}
+
+// Parts of the per-cell update. VERT_ALL: the whole update_land_hydrology_model! (sbm.jl:82-132).
+// With gravitational snow transport the transport sweep runs between VERT_SNOW (interception and
+// snow, sbm.jl:92-96, and the transport capacities) and VERT_SOIL (glacier, open-water runoff and
+// soil, sbm.jl:102-131).
+enum VertPhase { VERT_ALL = 0, VERT_SNOW = 1, VERT_SOIL = 2 };
+
+template <int MAXN, int PHASE>
 __global__ void __launch_bounds__(256) vertical_kernel(WfDevFields F) {
     const int M = F.M;
     const int64_t E = F.land_slots * M;
@@ -409,19 +435,20 @@ __global__ void __launch_bounds__(256) vertical_kernel(WfDevFields F) {
         const double Pr = Mf[PRECIP][e], PET = Mf[POTEVAP][e], T = Mf[TEMP][e];
         double canopy = Mf[CANOPY][e];
         double snow = Mf[SNOW][e], snow_water = Mf[SNOW_WATER][e];
-        // storage_prev! of the land balance (mass_balance.jl:95-125, Wflow.jl:315)
-        if (F.mass_balance) Mf[BL_PREV][e] = Mf[TSWS][e] + canopy + (snow + snow_water) + 0.0 * 0.0 + 0.0;
-        // ---- interception (canopy.jl:213-226 Gash, :259-271 Rutter)
         const double gap = L[GAP][slot], cmax = L[CMAX][slot];
         const double potevap = L[KC][slot] * PET * (1.0 - gap);
-        double tf, ic, sf;
+        double tf = 0.0, ic, sf = 0.0, srunoff = 0.0;
+        if (PHASE != VERT_SOIL) {
+        // storage_prev! of the land balance (mass_balance.jl:95-125, Wflow.jl:315)
+        if (F.mass_balance)
+            Mf[BL_PREV][e] = Mf[TSWS][e] + canopy + (snow + snow_water) + glacier_storage(F, e, slot) + 0.0;
+        // ---- interception (canopy.jl:213-226 Gash, :259-271 Rutter)
         if (F.gash) {
             interception_gash(cmax, L[E_R][slot], gap, Pr, potevap, dt, tf, ic, sf);
         } else {
             interception_modrut(Pr, potevap, canopy, gap, cmax, dt, tf, ic, sf);
         }
         // ---- snow (snow.jl:238-293, snow_process.jl:26-116)
-        double wfs;
         if (F.snow) {
             const double eff = tf + sf;
             const double tti = L[TTI][slot], tt = L[TT][slot];
@@ -450,7 +477,6 @@ __global__ void __launch_bounds__(256) vertical_kernel(WfDevFields F) {
             snow += sp * dt;
             snow_water += lp * dt;
             const double maxsw = snow * whc;
-            double srunoff;
             if (snow_water > maxsw) {
                 srunoff = (snow_water - maxsw) / dt;
                 snow_water = maxsw;
@@ -458,7 +484,35 @@ __global__ void __launch_bounds__(256) vertical_kernel(WfDevFields F) {
                 srunoff = 0.0;
             }
             Mf[SWE][e] = snow_water + snow;
-            wfs = srunoff + 0.0 * 0.0;
+        }
+        if (PHASE == VERT_SNOW) {
+            // lateral_snow_transport! capacities from the updated states (surface_process.jl:9-19)
+            Mf[CANOPY][e] = canopy;
+            Mf[SNOW][e] = snow;
+            Mf[SNOW_WATER][e] = snow_water;
+            F.GM[GM_SRUNOFF][e] = srunoff;
+            F.GM[GM_IC][e] = ic;
+            const double frac = jmin(0.5, L[SLOPE][slot] / 5.67) * jmin(1.0, snow / 10.0);
+            F.GM[GM_CAP][e] = frac * snow / dt;
+            F.GM[GM_CAPW][e] = snow_water * frac / dt;
+            continue;
+        }
+        } else {
+            // after the transport sweep: the moved snow states, the interception and snow runoff
+            // of VERT_SNOW
+            ic = F.GM[GM_IC][e];
+            srunoff = F.GM[GM_SRUNOFF][e];
+        }
+        // ---- glacier (glacier.jl:122-154) and the water flux at the surface (runoff.jl:37-58)
+        double wfs, gfrac = 0.0;
+        if (F.snow) {
+            if (F.glacier) {
+                gfrac = F.G[G_FRAC][slot];
+                const double gmelt = glacier_update(F, e, slot, T, dt, snow);
+                wfs = srunoff + gmelt * gfrac;
+            } else {
+                wfs = srunoff + 0.0 * 0.0;
+            }
         } else {
             wfs = tf + sf;
         }
@@ -472,7 +526,7 @@ __global__ void __launch_bounds__(256) vertical_kernel(WfDevFields F) {
         const double ae_river = rfrac * jmin(wd_river / dt, PET);
         const double ae_land = wfrac * jmin(wd_land / dt, PET);
         // ---- soil (soil.jl:643-682, 1150-1211)
-        const double soil_fraction = jmax(gap - wfrac - rfrac - 0.0, 0.0);
+        const double soil_fraction = jmax(gap - wfrac - rfrac - gfrac, 0.0);
         const double pot_trans = jmax(0.0, potevap - ic);
         double pot_soilevap = soil_fraction * PET;
         pot_soilevap -= 0.0;
@@ -679,7 +733,8 @@ struct SsfPhys {
     WfDevGraph g;
     WfSweep sw;
 
-    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
+    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end,
+                         double& hq) {
         double* const* Mf = F.Mf;
         double* const* L = F.L;
         double dt_s;
@@ -696,7 +751,7 @@ struct SsfPhys {
         double qin = 0.0, tr = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             double qu;
-            if (!wfw::upstream_q(g, sw, Mf[SSF_Q], o, m, s, ep, F.status, qu)) return false;
+            if (!wfw::upstream_q(g, sw, hq, o, m, s, ep, F.status, qu)) return false;
             const double fr = L[FRAC_TO_RIVER][g.up_slot[o]];
             qin = qin + qu * (1.0 - fr);
             tr = tr + qu * fr;
@@ -716,6 +771,7 @@ struct SsfPhys {
                                  L[FLOW_WIDTH][slot], Mf[Q_MAX][e], kh0, col, q, zi_new, exfilt, netflux);
         const bool early = (qin + q_prev == 0.0 && q_net <= 0.0);
         Mf[SSF_Q][e] = q;
+        hq = q;
         Mf[SSF_ZI][e] = zi_new;
         Mf[SSF_STORAGE][e] = L[SY][slot] * (d - zi_new) * area;
         // cumulative fluxes (set_flux_vars! zeroes them at the start of the model step)
@@ -788,7 +844,8 @@ struct OverlandPhys {
     WfDevGraph g;
     WfSweep sw;
 
-    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
+    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end,
+                         double& hq) {
         double* const* Mf = F.Mf;
         double* const* L = F.L;
         double dt_s;
@@ -799,7 +856,7 @@ struct OverlandPhys {
         double tr = 0.0, qin = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             double qu;
-            if (!wfw::upstream_q(g, sw, Mf[OL_Q], o, m, s, ep, F.status, qu)) return false;
+            if (!wfw::upstream_q(g, sw, hq, o, m, s, ep, F.status, qu)) return false;
             const double fr = L[FRAC_TO_RIVER][g.up_slot[o]];
             tr = tr + qu * fr;
             qin = qin + qu * (1.0 - fr);
@@ -811,6 +868,7 @@ struct OverlandPhys {
         double h = Mf[OL_H][e];
         if (sfw > 0.0) h = a / sfw;
         Mf[OL_Q][e] = q;
+        hq = q;
         Mf[OL_H][e] = h;
         Mf[OL_STORAGE][e] = fl * sfw * h;
         if (is_end) wfw::publish(g, chain, m, s, ep, q);
@@ -834,15 +892,16 @@ struct OverlandPhys {
 // ------------------------------------------------------------------ river wavefront ------
 
 // RES: the model has reservoirs. A reservoir cell hands its reservoir's outflow, not its river
-// discharge, to the downstream cell: published for a light child, read from the reservoir's
-// outflow for the heavy child (which this lane updated at the previous chain position).
+// discharge, to the downstream cell: published for a light child, in the walker's hand-off
+// register for the heavy child.
 template <bool RES>
 struct RiverPhys {
     WfDevFields F;
     WfDevGraph g;
     WfSweep sw;
 
-    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
+    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end,
+                         double& hq) {
         double* const* RM = F.RM;
         double* const* R = F.R;
         const int M = F.M;
@@ -866,11 +925,7 @@ struct RiverPhys {
         double qs = 0.0;
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             double qu;
-            if (!wfw::upstream_q(g, sw, RM[RV_Q], o, m, s, ep, F.status, qu)) return false;
-            if (RES && g.up_chain[o] < 0) {
-                const int32_t ru = F.res_of_rslot[g.up_slot[o]];
-                if (ru >= 0) qu = F.RS[RS_OUTFLOW][(int64_t)ru * M + m];
-            }
+            if (!wfw::upstream_q(g, sw, hq, o, m, s, ep, F.status, qu)) return false;
             qs = qs + qu;
         }
         const double qin = 0.0 + qs;
@@ -892,6 +947,7 @@ struct RiverPhys {
             const int32_t r = F.res_of_rslot[slot];
             if (r >= 0) q_down = wfr::reservoir_node(F, r, m, q, dt_s);
         }
+        hq = q_down;
         RM[RV_H][e] = a / R[R_WIDTH][slot];
         RM[RV_STORAGE][e] = len * a;
         if (is_end) wfw::publish(g, chain, m, s, ep, q_down);
@@ -911,6 +967,64 @@ struct RiverPhys {
         return true;
     }
 };
+
+// --------------------------------------------------------- gravitational snow transport ----
+
+// One material of lateral_snow_transport! (surface_process.jl:9-19): accucapacityflux! over the
+// land graph (routing/utils.jl:82-104, 144-148). A cell's material is its own plus the hand-offs
+// of its upstream cells, added in the order of the graph's topological sort (the order in which
+// the reference's sweep hands them on); it passes min(material / dt, capacity) on to its
+// downstream cell and keeps the rest. MAT 0: snow storage (snow_out = its flux), MAT 1: snow
+// water (snow_out += its flux). FP64 in both forms (the split form's double-FP32 states are
+// converted on the way in and out).
+template <int MAT>
+struct SnowPhys {
+    WfDevFields F;
+    WfDevGraph g;
+    WfSweep sw;
+
+    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end,
+                         double& hq) {
+        const int f = MAT == 0 ? SNOW : SNOW_WATER;
+        double material = F.split ? (double)F.Mh[f][e] + (double)F.Ml[f][e] : F.Mf[f][e];
+        const int32_t o0 = g.up_ptr[slot], o1 = g.up_ptr[slot + 1];
+        for (int32_t k = o0; k < o1; ++k) {
+            double upd;
+            if (!wfw::upstream_q(g, sw, hq, g.snow_up[k], m, s, ep, F.status, upd)) return false;
+            material += upd;
+        }
+        const double dt = sw.dt;
+        const double flux = jmin(material / dt, F.GM[MAT == 0 ? GM_CAP : GM_CAPW][e]);
+        const double update = flux * dt;
+        material -= update;
+        if (F.split) {
+            const wff::ff v = wff::from_d(material);
+            F.Mh[f][e] = v.hi;
+            F.Ml[f][e] = v.lo;
+        } else {
+            F.Mf[f][e] = material;
+        }
+        F.GM[GM_SNOW_OUT][e] = MAT == 0 ? flux : F.GM[GM_SNOW_OUT][e] + flux;
+        hq = update;
+        if (is_end) wfw::publish(g, chain, m, s, ep, update);
+        return true;
+    }
+};
+
+// flux_in! (routing/utils.jl:160-166): snow_in = the snow_out of the upstream cells, summed in
+// the upstream lists' (ascending) order.
+__global__ void __launch_bounds__(256) snow_in_kernel(WfDevFields F, WfDevGraph g) {
+    const int M = F.M;
+    const int64_t E = F.land_slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t slot = e / M;
+        if (F.land_node_of_slot[slot] < 0) continue;
+        const int m = (int)(e - slot * M);
+        double acc = 0.0;
+        for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) acc = acc + F.GM[GM_SNOW_OUT][g.up_slot[o] * M + m];
+        F.GM[GM_SNOW_IN][e] = acc;
+    }
+}
 
 template <class Phys>
 __global__ void __launch_bounds__(128) walk_kernel(Phys phys) {
@@ -956,7 +1070,8 @@ __global__ void __launch_bounds__(256) balance_kernel(WfDevFields F) {
         double ts = 0.0;
         if (rs >= 0) ts = ((F.RM[RV_H][rs * M + m] * F.R[R_WIDTH][rs] * F.R[R_LENGTH][rs]) / (area));
         const double snow = Mf[SNOW][e], sw = Mf[SNOW_WATER][e], canopy = Mf[CANOPY][e];
-        ts += snow + sw + 0.0 * 0.0 + canopy + 0.0;
+        const double glacier = glacier_storage(F, e, slot);
+        ts += snow + sw + glacier + canopy + 0.0;
         const double sub_surface = Mf[USTOREDEPTH][e] + Mf[SAT][e];
         const double lateral = Mf[OL_H][e] * (1.0 - L[RIVER_FRACTION][slot]);
         ts += sub_surface + lateral;
@@ -966,10 +1081,12 @@ __global__ void __launch_bounds__(256) balance_kernel(WfDevFields F) {
         // land hydrology balance (mass_balance.jl:215-253)
         {
             const double Pv = F.split ? (double)F.Mh[PRECIP][e] : Mf[PRECIP][e];
-            const double tin = Mf[SSF_QIN_AVG][e] / area + (Pv + 0.0) + 0.0 + 0.0 / area;
+            const double snow_in = F.snow_transport ? F.GM[GM_SNOW_IN][e] : 0.0;
+            const double snow_out = F.snow_transport ? F.GM[GM_SNOW_OUT][e] : 0.0;
+            const double tin = Mf[SSF_QIN_AVG][e] / area + (Pv + 0.0) + snow_in + 0.0 / area;
             const double vout = Mf[NET_RUNOFF][e] + Mf[AET][e] + Mf[NET_RUNOFF_RIVER][e] + Mf[LEAKAGE][e] + 0.0;
-            const double tout = Mf[SSF_Q_AVG][e] / area + vout + 0.0 + 0.0 / area;
-            const double storage = Mf[TSWS][e] + canopy + (snow + sw) + 0.0 * 0.0 + 0.0;
+            const double tout = Mf[SSF_Q_AVG][e] / area + vout + snow_out + 0.0 / area;
+            const double storage = Mf[TSWS][e] + canopy + (snow + sw) + glacier + 0.0;
             mb_error(tin, tout, (storage - Mf[BL_PREV][e]) / dt, err, rel);
             Mf[BL_ERR][e] = err;
             Mf[BL_REL][e] = rel;
@@ -1028,7 +1145,9 @@ cudaError_t launch_walk(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
     int blocks;
     Phys p = phys;
-    cudaError_t err = wave_grid(walk_kernel<Phys>, threads, 0, c, p.g, blocks, p.sw.prio_items);
+    p.sw.SL = p.sw.aflag ? 1 : wave_sub_lanes(p.sw.S, c);
+    cudaError_t err = wave_grid(walk_kernel<Phys>, threads, 0, c, p.g, blocks, p.sw.prio_items,
+                                wf_items_per_chunk(p.g.G, p.g.M, p.sw.SL));
     if (err != cudaSuccess) return err;
     walk_kernel<Phys><<<blocks, threads, 0, c.stream>>>(p);
     return cudaGetLastError();
@@ -1036,19 +1155,39 @@ cudaError_t launch_walk(const Phys& phys, const WfLaunchCfg& c) {
 
 }  // namespace
 
-cudaError_t wf_fp64_vertical(const WfDevFields& F, const WfLaunchCfg& c) {
+template <int PHASE>
+cudaError_t launch_vertical(const WfDevFields& F, const WfLaunchCfg& c) {
     const int block = c.vertical_block > 0 ? c.vertical_block : 128;
     const int grid = grid_for(F.land_slots * F.M, block, c.num_sms);
     if (F.N <= 4)
-        vertical_kernel<4><<<grid, block, 0, c.stream>>>(F);
+        vertical_kernel<4, PHASE><<<grid, block, 0, c.stream>>>(F);
     else
-        vertical_kernel<WF_MAX_LAYERS><<<grid, block, 0, c.stream>>>(F);
+        vertical_kernel<WF_MAX_LAYERS, PHASE><<<grid, block, 0, c.stream>>>(F);
     return cudaGetLastError();
+}
+
+cudaError_t wf_fp64_vertical(const WfDevFields& F, const WfLaunchCfg& c) { return launch_vertical<VERT_ALL>(F, c); }
+cudaError_t wf_fp64_vertical_snow(const WfDevFields& F, const WfLaunchCfg& c) {
+    return launch_vertical<VERT_SNOW>(F, c);
+}
+cudaError_t wf_fp64_vertical_soil(const WfDevFields& F, const WfLaunchCfg& c) {
+    return launch_vertical<VERT_SOIL>(F, c);
 }
 
 cudaError_t wf_fp64_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
     if (F.N <= 4) return launch_walk(SsfPhys<4>{F, g, sw}, c);
     return launch_walk(SsfPhys<WF_MAX_LAYERS>{F, g, sw}, c);
+}
+
+cudaError_t wf_snow_transport_sweep(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, int material,
+                                    const WfLaunchCfg& c) {
+    if (material == 0) return launch_walk(SnowPhys<0>{F, g, sw}, c);
+    return launch_walk(SnowPhys<1>{F, g, sw}, c);
+}
+
+cudaError_t wf_snow_in(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {
+    snow_in_kernel<<<grid_for(F.land_slots * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F, g);
+    return cudaGetLastError();
 }
 
 cudaError_t wf_fp64_overland(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {

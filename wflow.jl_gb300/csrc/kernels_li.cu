@@ -20,6 +20,7 @@
 // the CPU oracle's. The per-edge and per-cell arithmetic lives in li_scheme.cuh.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -106,12 +107,229 @@ int grid_of(int64_t n) {
     return (int)(g < 1 ? 1 : (g > 65535 ? 65535 : g));
 }
 
+// ---- device-side sub-step loops ----------------------------------------------------------------
+// One persistent cooperative launch per model step runs the reference's sub-step loop
+// (update_river_flow_model!, surface_staggered_scheme.jl:800-826; update_overland_flow_model!,
+// :1153-1193) on the device: the stable time step (a grid-wide min-reduction), check_timestepsize
+// (routing/timestepping.jl:11-16), the edge and then the cell updates, separated by grid barriers,
+// until the step is covered. The host reads the sub-step count and the status once per model
+// step instead of the time step every sub-step. Every thread takes the same sub-step sizes (the
+// same minimum and the same FP64 operations), so the results equal the host-driven loop's.
+
+struct LiLoop {
+    unsigned count, gen;                  // grid barrier: arrivals and generation
+    int status;                           // 1: a barrier wait ran out of its budget, 2: too many sub-steps
+    int pad;
+    unsigned long long minbits[2][2];     // [sub-step parity][river, land] minimum stable sub-step (bits)
+    int nanflag[2][2];                    // a NaN among the candidates (Julia's min propagates NaN)
+    long long substeps;
+    double t;
+};
+
+constexpr uint64_t LI_BARRIER_BUDGET_NS = 10ull * 1000 * 1000 * 1000;  // a safety net: a wait lasts one phase
+constexpr long long LI_MAX_SUBSTEPS = 10000000;
+
+__device__ __forceinline__ uint64_t li_now_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid barrier of a cooperative launch (all blocks resident), every wait bounded: a wait that runs
+// out sets the status and every block returns false.
+__device__ bool li_grid_sync(LiLoop* s) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned* gen = &s->gen;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&s->count, 1u) == gridDim.x - 1) {
+            atomicExch(&s->count, 0u);
+            __threadfence();
+            atomicAdd(&s->gen, 1u);
+        } else {
+            const uint64_t t0 = li_now_ns();
+            while (*gen == g) {
+                __nanosleep(32);
+                if (*(volatile int*)&s->status) {
+                    ok = 0;
+                    break;
+                }
+                if (li_now_ns() - t0 > LI_BARRIER_BUDGET_NS) {
+                    atomicOr(&s->status, 1);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        ok_s = ok && !*(volatile int*)&s->status;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// Block minimum of the non-NaN candidates into minbits[p][w] (the bit patterns of non-negative
+// doubles order as the values), and the NaN flag.
+__device__ void li_reduce_min(LiLoop* s, int p, int w, double m, bool nan) {
+    __shared__ double red[32];
+    __shared__ int nan_s;
+    if (threadIdx.x == 0) nan_s = 0;
+    __syncthreads();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    if (nan) nan_s = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = red[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) b = fmin(b, red[k]);
+        atomicMin(&s->minbits[p][w], (unsigned long long)__double_as_longlong(b));
+        if (nan_s) atomicOr(&s->nanflag[p][w], 1);
+    }
+}
+
+__device__ __forceinline__ double li_read_min(LiLoop* s, int p, int w) {
+    if (*(volatile int*)&s->nanflag[p][w]) return __longlong_as_double(0x7ff8000000000000LL);
+    return __longlong_as_double((long long)*(volatile unsigned long long*)&s->minbits[p][w]);
+}
+
+__global__ void li_loop_init_kernel(LiLoop* s) {
+    s->count = 0;
+    s->gen = 0;
+    s->status = 0;
+    for (int p = 0; p < 2; ++p)
+        for (int w = 0; w < 2; ++w) {
+            s->minbits[p][w] = INF_BITS;
+            s->nanflag[p][w] = 0;
+        }
+    s->substeps = 0;
+    s->t = 0.0;
+}
+
+// the river alone (wf_li_river_step)
+__global__ void __launch_bounds__(256) li_river_loop_kernel(LiDev d, LiLoop* s, double dt) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+    double t = 0.0;
+    long long k = 0;
+    while (t < dt) {
+        const int p = (int)(k & 1);
+        double m = wfm::from_bits(INF_BITS);
+        bool nan = false;
+        for (int64_t i = tid; i < d.n_dt; i += nt) {
+            const double v = wfli::cell_timestep(d, i);
+            if (v != v) nan = true;
+            else m = fmin(m, v);
+        }
+        li_reduce_min(s, p, 0, m, nan);
+        if (!li_grid_sync(s)) return;
+        if (tid == 0) {  // the other parity's slot serves the next sub-step
+            s->minbits[p ^ 1][0] = INF_BITS;
+            s->nanflag[p ^ 1][0] = 0;
+        }
+        double dt_s = wfli::finish_timestep(li_read_min(s, p, 0));
+        if (t + dt_s > dt) dt_s = dt - t;
+        for (int64_t e = tid; e < d.n_edges; e += nt) wfli::update_edge(d, e, dt_s);
+        if (!li_grid_sync(s)) return;
+        for (int64_t i = tid; i < d.n_active; i += nt) wfli::update_cell(d, i, dt_s);
+        t += dt_s;
+        ++k;
+        if (!li_grid_sync(s)) return;
+        if (k >= LI_MAX_SUBSTEPS) {
+            if (tid == 0) atomicOr(&s->status, 2);
+            return;
+        }
+    }
+    if (tid == 0) {
+        s->substeps = k;
+        s->t = t;
+    }
+}
+
+// the land grid with its river (wf_li_domain_step); qx_buf / qy_buf hold the discharges of the
+// last two sub-steps, buffer cur0 the latest at the start
+__global__ void __launch_bounds__(256) li_domain_loop_kernel(wfli::LiLand L, LiDev R, wfli::LiRiverBC B, LiLoop* s,
+                                                             double dt, double* qx0b, double* qx1b, double* qy0b,
+                                                             double* qy1b, int cur0) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+    double t = 0.0;
+    long long k = 0;
+    while (t < dt) {
+        const int p = (int)(k & 1);
+        double mr = wfm::from_bits(INF_BITS), ml = wfm::from_bits(INF_BITS);
+        bool nr = false, nl = false;
+        for (int64_t i = tid; i < R.n_dt; i += nt) {
+            const double v = wfli::cell_timestep(R, i);
+            if (v != v) nr = true;
+            else mr = fmin(mr, v);
+        }
+        for (int64_t i = tid; i < L.n; i += nt) {
+            const double v = wfli::land_timestep(L, i);
+            if (v != v) nl = true;
+            else ml = fmin(ml, v);
+        }
+        li_reduce_min(s, p, 0, mr, nr);
+        li_reduce_min(s, p, 1, ml, nl);
+        if (!li_grid_sync(s)) return;
+        if (tid == 0) {
+            s->minbits[p ^ 1][0] = s->minbits[p ^ 1][1] = INF_BITS;
+            s->nanflag[p ^ 1][0] = s->nanflag[p ^ 1][1] = 0;
+        }
+        const double dt_river = wfli::finish_timestep(li_read_min(s, p, 0));
+        const double dt_land = wfli::finish_timestep(li_read_min(s, p, 1));
+        double dt_s = wfm::jmin(dt_river, dt_land);
+        if (t + dt_s > dt) dt_s = dt - t;
+        const int prev = (cur0 + (int)(k & 1)) & 1;
+        L.qx0 = prev ? qx1b : qx0b;
+        L.qy0 = prev ? qy1b : qy0b;
+        L.qx = prev ? qx0b : qx1b;
+        L.qy = prev ? qy0b : qy1b;
+        for (int64_t i = tid; i < L.n; i += nt) {
+            wfli::land_direction(L, i, dt_s, true);
+            wfli::land_direction(L, i, dt_s, false);
+        }
+        for (int64_t e = tid; e < R.n_edges; e += nt) wfli::update_edge(R, e, dt_s);
+        if (!li_grid_sync(s)) return;
+        for (int64_t i = tid; i < L.n; i += nt) wfli::land_depth(L, R, B, i, dt_s);
+        t += dt_s;
+        ++k;
+        if (!li_grid_sync(s)) return;
+        if (k >= LI_MAX_SUBSTEPS) {
+            if (tid == 0) atomicOr(&s->status, 2);
+            return;
+        }
+    }
+    if (tid == 0) {
+        s->substeps = k;
+        s->t = t;
+    }
+}
+
+// Blocks of a cooperative loop launch: every block resident (occupancy x SMs), no more than the
+// work needs.
+template <class Kernel>
+int li_loop_blocks(Kernel kernel, int device, int64_t work) {
+    int per_sm = 0, sms = 0, coop = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
+    const int64_t need = (work + 255) / 256;
+    int64_t b = (int64_t)per_sm * sms;
+    if (b > need) b = need;
+    return (int)(b < 1 ? 1 : b);
+}
+
 // device memory, stream and error text of a handle
 struct LiOwner {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     std::string err;
+    LiLoop* loop = nullptr;      // state of the device-side sub-step loop
+    LiLoop* loop_host = nullptr; // pinned read-back of it
+    bool host_loop = false;      // drive the sub-steps from the host (no cooperative launch)
 };
 
 thread_local std::string g_li_error;
@@ -150,7 +368,30 @@ int li_sync(LiOwner* o, const char* what) {
 void li_release(LiOwner* o) {
     if (o->stream) cudaStreamSynchronize(o->stream);
     for (void* p : o->allocs) cudaFree(p);
+    if (o->loop_host) cudaFreeHost(o->loop_host);
     if (o->stream) cudaStreamDestroy(o->stream);
+}
+
+// Device-side loop state of a handle (at create).
+int li_alloc_loop(LiOwner* o) {
+    if (cudaMalloc((void**)&o->loop, sizeof(LiLoop)) != cudaSuccess) return li_fail(o, WF_ERR_NOMEM, "cudaMalloc failed");
+    o->allocs.push_back(o->loop);
+    if (cudaHostAlloc((void**)&o->loop_host, sizeof(LiLoop), cudaHostAllocDefault) != cudaSuccess)
+        return li_fail(o, WF_ERR_NOMEM, "cudaHostAlloc failed");
+    return WF_OK;
+}
+
+// After a loop launch: the sub-step count (and the status) back to the host, one read per step.
+int li_finish_loop(LiOwner* o, int64_t* substeps) {
+    if (cudaMemcpyAsync(o->loop_host, o->loop, sizeof(LiLoop), cudaMemcpyDeviceToHost, o->stream) != cudaSuccess)
+        return li_fail(o, WF_ERR_CUDA, "read-back of the sub-step loop failed");
+    int rc = li_sync(o, "sub-step loop");
+    if (rc) return rc;
+    if (o->loop_host->status & 1)
+        return li_fail(o, WF_ERR_SPIN, "a grid barrier of the sub-step loop ran out of its wait budget");
+    if (o->loop_host->status & 2) return li_fail(o, WF_ERR_INVALID, "more than 1e7 sub-steps in one step");
+    if (substeps) *substeps = o->loop_host->substeps;
+    return WF_OK;
 }
 
 int li_open(LiOwner* o, int device) {
@@ -296,7 +537,8 @@ int32_t wf_li_river_create(int64_t n, int64_t n_active, int64_t n_edges, const i
     if ((rc = li_open(r, device)) ||
         (rc = li_upload_river(r, r->d, n, n_active, n_edges, src, dst, zb, flow_length, flow_width, h_init, zb_edge,
                               width_edge, length_edge, mannings_n_sq_edge, h_thresh, froude_limit, alpha)) ||
-        (rc = li_upload<double>(r, &r->q_avg, nullptr, n_edges)) || (rc = li_finish_uploads(r))) {
+        (rc = li_upload<double>(r, &r->q_avg, nullptr, n_edges)) || (rc = li_alloc_loop(r)) ||
+        (rc = li_finish_uploads(r))) {
         g_li_error = r->err;
         wf_li_river_destroy(r);
         return rc;
@@ -359,6 +601,21 @@ int32_t wf_li_river_step(WfLiRiver* r, double dt, int64_t* substeps) {
          cudaMemsetAsync(r->d.q_cum, 0, r->d.n_edges * sizeof(double), r->stream) != cudaSuccess) ||
         cudaMemsetAsync(r->d.abstraction_cum, 0, r->d.n * sizeof(double), r->stream) != cudaSuccess)
         return li_fail(r, WF_ERR_CUDA, "reset of the cumulative discharge failed");
+    const int blocks = r->host_loop ? 0 : li_loop_blocks(li_river_loop_kernel, r->device,
+                                                          std::max(r->d.n, r->d.n_edges));
+    if (blocks > 0) {  // the sub-step loop on the device, one launch
+        li_loop_init_kernel<<<1, 1, 0, r->stream>>>(r->loop);
+        LiDev dd = r->d;
+        LiLoop* lp = r->loop;
+        double dtv = dt;
+        void* args[] = {&dd, &lp, &dtv};
+        if (cudaLaunchCooperativeKernel((const void*)li_river_loop_kernel, blocks, 256, args, 0, r->stream) !=
+            cudaSuccess)
+            return li_fail(r, WF_ERR_CUDA, "cooperative launch of the sub-step loop failed");
+        if (r->d.n_edges > 0)
+            li_average_kernel<<<grid_of(r->d.n_edges), 256, 0, r->stream>>>(r->d.q_cum, r->q_avg, r->d.n_edges, dt);
+        return li_finish_loop(r, substeps);
+    }
     double t = 0.0;
     int64_t k = 0;
     while (t < dt) {
@@ -376,6 +633,12 @@ int32_t wf_li_river_step(WfLiRiver* r, double dt, int64_t* substeps) {
         if (rc) return rc;
     }
     if (substeps) *substeps = k;
+    return WF_OK;
+}
+
+int32_t wf_li_river_set_host_loop(WfLiRiver* r, int32_t host_loop) {
+    if (!r) return WF_ERR_INVALID;
+    r->host_loop = host_loop != 0;
     return WF_OK;
 }
 
@@ -479,7 +742,7 @@ int32_t wf_li_domain_create(const WfLiLandGrid* land, const WfLiRiverNetwork* ri
         (rc = li_upload<double>(d, &d->qx_avg, nullptr, n + 1)) ||
         (rc = li_upload<double>(d, &d->qy_avg, nullptr, n + 1)) ||
         (rc = li_upload<double>(d, &d->q_avg, nullptr, rv.n_edges)) ||
-        (rc = li_upload<double>(d, &L.dt_min, nullptr, 1)) || (rc = li_finish_uploads(d))) {
+        (rc = li_upload<double>(d, &L.dt_min, nullptr, 1)) || (rc = li_alloc_loop(d)) || (rc = li_finish_uploads(d))) {
         g_li_error = d->err;
         wf_li_domain_destroy(d);
         return rc;
@@ -589,6 +852,31 @@ int32_t wf_li_domain_step(WfLiDomain* d, double dt, int64_t* substeps) {
         cudaMemsetAsync(d->L.qx_cum, 0, (n + 1) * sizeof(double), d->stream) != cudaSuccess ||
         cudaMemsetAsync(d->L.qy_cum, 0, (n + 1) * sizeof(double), d->stream) != cudaSuccess)
         return li_fail(d, WF_ERR_CUDA, "reset of the cumulative discharges failed");
+    const int blocks = d->host_loop ? 0 : li_loop_blocks(li_domain_loop_kernel, d->device,
+                                                          std::max(std::max(n + 1, d->R.n), ne));
+    if (blocks > 0) {  // the sub-step loop on the device, one launch
+        li_loop_init_kernel<<<1, 1, 0, d->stream>>>(d->loop);
+        wfli::LiLand LL = d->L;
+        LiDev RR = d->R;
+        wfli::LiRiverBC BB = d->B;
+        LiLoop* lp = d->loop;
+        double dtv = dt;
+        double *qx0b = d->qx_buf[0], *qx1b = d->qx_buf[1], *qy0b = d->qy_buf[0], *qy1b = d->qy_buf[1];
+        int cur0 = d->cur;
+        void* args[] = {&LL, &RR, &BB, &lp, &dtv, &qx0b, &qx1b, &qy0b, &qy1b, &cur0};
+        if (cudaLaunchCooperativeKernel((const void*)li_domain_loop_kernel, blocks, 256, args, 0, d->stream) !=
+            cudaSuccess)
+            return li_fail(d, WF_ERR_CUDA, "cooperative launch of the sub-step loop failed");
+        if (ne > 0) li_average_kernel<<<grid_of(ne), 256, 0, d->stream>>>(d->R.q_cum, d->q_avg, ne, dt);
+        li_average_kernel<<<grid_of(n + 1), 256, 0, d->stream>>>(d->L.qx_cum, d->qx_avg, n + 1, dt);
+        li_average_kernel<<<grid_of(n + 1), 256, 0, d->stream>>>(d->L.qy_cum, d->qy_avg, n + 1, dt);
+        int64_t k = 0;
+        const int rc = li_finish_loop(d, &k);
+        if (rc) return rc;
+        d->cur = (int)((d->cur + k) & 1);  // the buffer of the last sub-step's discharges
+        if (substeps) *substeps = k;
+        return WF_OK;
+    }
     double t = 0.0;
     int64_t k = 0;
     while (t < dt) {
@@ -606,6 +894,12 @@ int32_t wf_li_domain_step(WfLiDomain* d, double dt, int64_t* substeps) {
     const int rc = li_sync(d, "average discharge");
     if (rc) return rc;
     if (substeps) *substeps = k;
+    return WF_OK;
+}
+
+int32_t wf_li_domain_set_host_loop(WfLiDomain* d, int32_t host_loop) {
+    if (!d) return WF_ERR_INVALID;
+    d->host_loop = host_loop != 0;
     return WF_OK;
 }
 

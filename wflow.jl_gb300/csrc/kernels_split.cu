@@ -24,6 +24,7 @@
 #include "wf_launch.cuh"
 #include "wf_math.cuh"
 #include "wf_reservoir.cuh"
+#include "snow_scheme.cuh"
 #include "wf_walker.cuh"
 #include "wf_ff.cuh"
 #include "wf_wave.cuh"
@@ -276,7 +277,10 @@ template <int MAXN>
 struct ColG {
     int N, nl, nu;
     float act[MAXN], cum[MAXN + 1], thick[MAXN];
-    __device__ __forceinline__ void set(const WfDevFields& F, int64_t slot, double zi) {
+    // from the field arrays, or (s32, s64 non-null) from a staged copy: layer thicknesses and
+    // bottom depths (FP32) at s32[0..MAXN) and s32[MAXN..2 MAXN), bottom depths (FP64) at s64
+    __device__ __forceinline__ void set(const WfDevFields& F, int64_t slot, double zi, const float* s32 = nullptr,
+                                        const double* s64 = nullptr) {
         N = F.N;
         nl = F.nlayers[slot];
         nu = N;
@@ -286,9 +290,9 @@ struct ColG {
         for (int k = 0; k < MAXN; ++k) {
             float t = __int_as_float(0x7fc00000);
             if (k < N) {
-                act[k] = F.LYf[LY_ACT_THICK][k][slot];
-                const double c1 = F.LY[LY_CUM][k][slot];
-                cum[k + 1] = F.LYf[LY_CUM][k][slot];
+                act[k] = s32 ? s32[k] : F.LYf[LY_ACT_THICK][k][slot];
+                const double c1 = s64 ? s64[k] : F.LY[LY_CUM][k][slot];
+                cum[k + 1] = s32 ? s32[MAXN + k] : F.LYf[LY_CUM][k][slot];
                 if (zi > c1) {
                     t = act[k];
                 } else if (zi > c0) {
@@ -390,6 +394,81 @@ __device__ __forceinline__ void stage_vertical(const WfDevFields& F, int64_t e, 
     cp_async8(f64 + VD_TSWS * st, F.Mf[TSWS] + e);
 }
 
+// Per-cell parameters of the vertical kernel, staged once per warp. With a multiple of 32 members
+// the 32 lanes of a warp compute 32 members of one cell (members are innermost), so the cell's
+// parameters are the same for the whole warp: its lanes copy them (cp.async) into a per-warp
+// shared row for the warp's next element, and every lane reads them back as broadcasts. They
+// then occupy no registers while the element computes and cost no global round trip.
+#define WF_VW_LFIELDS(X)                                                                            \
+    X(ALPHA_H1) X(CAP_COMP) X(CAP_HMAX) X(CAP_N) X(CF_SOIL) X(CMAX) X(COMPACT_FRAC) X(DDF) X(E_R) X(GAP) X(H1) X(H2) \
+    X(H3_HIGH) X(H3_LOW) X(H4) X(KC) X(KH_RATIO) X(MAX_LEAKAGE) X(PSI_B) X(RIVER_FRACTION) X(ROOTDISTPAR)          \
+    X(ROOTING_DEPTH) X(SLOPE) X(SOIL_THICKNESS) X(SSF_DTDX) X(SWC) X(SY) X(THETA_FC) X(THETA_R) X(THETA_S) X(TT)  \
+    X(TTI) X(TTM) X(WATER_FRACTION) X(WHC) X(W_SOIL) X(Z_EXP)
+#define WF_VW_ITEM(name) VW_##name,
+enum VW32 {
+    WF_VW_LFIELDS(WF_VW_ITEM)
+    VW_CMAX_LO, VW_AREA_HI, VW_AREA_LO, VW_LY  // then per layer: thickness, bottom depth, Kv factor, c, root fraction
+};
+#undef WF_VW_ITEM
+enum VW64 { VW_D_SOIL_THICKNESS, VW_D_INV_TE, VW_D_SLOPE, VW_D_CUM };  // then one bottom depth per layer
+template <int MAXN>
+struct VWarp {
+    static constexpr int N32 = VW_LY + 5 * MAXN;
+    static constexpr int N64 = VW_D_CUM + MAXN + 2;  // + node and river slot (int64)
+    static constexpr size_t bytes = ((size_t)N64 * 8 + (size_t)N32 * 4 + 7) / 8 * 8;  // one buffer
+};
+
+// Lanes of a warp copy the parameters of cell `slot` into the warp's buffer (w64: doubles and
+// the two slot indices, w32: floats).
+template <int MAXN>
+__device__ __forceinline__ void stage_vertical_warp(const WfDevFields& F, int64_t slot, double* w64, float* w32,
+                                                    int lane) {
+    constexpr int N32 = VWarp<MAXN>::N32;
+    for (int i = lane; i < N32; i += 32) {
+        const float* src = nullptr;
+        if (i < VW_CMAX_LO) {
+#define WF_VW_SRC(name) if (i == VW_##name) src = F.Lf[name];
+            WF_VW_LFIELDS(WF_VW_SRC)
+#undef WF_VW_SRC
+        } else if (i == VW_CMAX_LO) {
+            src = F.Ll[CMAX];
+        } else if (i == VW_AREA_HI) {
+            src = F.Lf[AREA];
+        } else if (i == VW_AREA_LO) {
+            src = F.Ll[AREA];
+        } else {
+            const int k = (i - VW_LY) % MAXN, which = (i - VW_LY) / MAXN;
+            if (k < F.N) {
+#pragma unroll
+                for (int kk = 0; kk < MAXN; ++kk) {
+                    if (kk != k) continue;
+                    src = which == 0   ? F.LYf[LY_ACT_THICK][kk]
+                          : which == 1 ? F.LYf[LY_CUM][kk]
+                          : which == 2 ? F.LYf[LY_KVFRAC][kk]
+                          : which == 3 ? F.LYf[LY_C][kk]
+                                       : F.LYf[LY_ROOTFRAC][kk];
+                }
+            }
+        }
+        if (src) cp_async4(w32 + i, src + slot);
+    }
+    if (lane < VW_D_CUM + MAXN) {
+        const double* src = nullptr;
+        if (lane == VW_D_SOIL_THICKNESS) src = F.L[SOIL_THICKNESS];
+        else if (lane == VW_D_INV_TE) src = F.L[INV_TE];
+        else if (lane == VW_D_SLOPE) src = F.L[SLOPE];
+        else {
+#pragma unroll
+            for (int kk = 0; kk < MAXN; ++kk)
+                if (lane - VW_D_CUM == kk && kk < F.N) src = F.LY[LY_CUM][kk];
+        }
+        if (src) cp_async8(w64 + lane, src + slot);
+    } else if (lane < VW_D_CUM + MAXN + 2) {
+        const int64_t* src = lane == VW_D_CUM + MAXN ? F.land_node_of_slot : F.land_river_slot;
+        cp_async8(w64 + lane, src + slot);
+    }
+}
+
 // ----------------------------------------------------------------- vertical kernel ------
 //
 // GB300 issues FP64 instructions (arithmetic, compares and FP32<->FP64 conversions alike) at
@@ -398,7 +477,14 @@ __device__ __forceinline__ void stage_vertical(const WfDevFields& F, int64_t e, 
 // unsaturated layers) and every flux that enters the water balance is a double-FP32 pair
 // (wf_ff.cuh); stores take the step's FP32 increments exactly (TwoSum/TwoProd); partitions of
 // a flux are exact residuals, so the parts always sum to the whole.
-template <int MAXN>
+// Parts of the per-cell update, as in the FP64 form: VERT_ALL the whole update; with gravitational
+// snow transport VERT_SNOW (interception, snow, transport capacities) and VERT_SOIL (glacier,
+// open water, soil) around the transport sweep.
+enum VertPhase { VERT_ALL = 0, VERT_SNOW = 1, VERT_SOIL = 2 };
+
+// WS: the members of a cell fill whole warps (a multiple of 32 members), and the cell's
+// parameters are staged once per warp (stage_vertical_warp).
+template <int MAXN, int PHASE, bool WS>
 __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
     using wff::ff;
     const int M = F.M;
@@ -412,68 +498,90 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
     constexpr int N32 = VStage<MAXN>::N32;
     double* const my64 = vstage_smem + threadIdx.x;  // buffer b: my64 + b * VD_COUNT * bd
     float* const my32 = reinterpret_cast<float*>(vstage_smem + (size_t)2 * VD_COUNT * bd) + threadIdx.x;
+    // per-warp double buffer of the cell's parameters (WS)
+    const int lane = (int)(threadIdx.x & 31u);
+    unsigned char* const wbase = reinterpret_cast<unsigned char*>(vstage_smem + (size_t)2 * VD_COUNT * bd) +
+                                 (size_t)2 * N32 * bd * sizeof(float) +
+                                 (size_t)(threadIdx.x >> 5) * 2 * VWarp<MAXN>::bytes;
+    auto w64 = [&](int b) { return reinterpret_cast<double*>(wbase + (size_t)b * VWarp<MAXN>::bytes); };
+    auto w32 = [&](int b) {
+        return reinterpret_cast<float*>(wbase + (size_t)b * VWarp<MAXN>::bytes + (size_t)VWarp<MAXN>::N64 * 8);
+    };
     const int64_t stride = (int64_t)gridDim.x * bd;
     int64_t e = blockIdx.x * (int64_t)bd + threadIdx.x;
-    if (e < E) stage_vertical<MAXN>(F, e, my32, my64, bd);
+    if (e < E) {
+        stage_vertical<MAXN>(F, e, my32, my64, bd);
+        if (WS) stage_vertical_warp<MAXN>(F, e / M, w64(0), w32(0), lane);
+    }
     cp_async_commit();
     for (int buf = 0; e < E; e += stride, buf ^= 1) {
         // stage the next element while this one computes
-        if (e + stride < E)
+        if (e + stride < E) {
             stage_vertical<MAXN>(F, e + stride, my32 + (buf ^ 1) * N32 * bd, my64 + (buf ^ 1) * VD_COUNT * bd, bd);
+            if (WS) stage_vertical_warp<MAXN>(F, (e + stride) / M, w64(buf ^ 1), w32(buf ^ 1), lane);
+        }
         cp_async_commit();
         cp_async_wait_prev();
+        if (WS) __syncwarp();  // the warp's parameter row was copied by all of its lanes
         const float* const vs = my32 + buf * N32 * bd;
         const double* const vd = my64 + buf * VD_COUNT * bd;
+        const float* const W32 = w32(buf);
+        const double* const W64 = w64(buf);
         auto V = [&](int i) { return vs[i * bd]; };
         auto VF = [&](int ih, int il) { return ff{vs[ih * bd], vs[il * bd]}; };
         const int64_t slot = e / M;
-        if (F.land_node_of_slot[slot] < 0) continue;
+        const int64_t node =
+            WS ? (int64_t)__double_as_longlong(W64[VW_D_CUM + MAXN]) : F.land_node_of_slot[slot];
+        if (node < 0) continue;
         const int m = (int)(e - slot * M);
         float* const* Mh = F.Mh;
         float* const* Lf = F.Lf;
+#define VP(name) (WS ? W32[VW_##name] : Lf[name][slot])
         // per-cell parameters, loaded up front so that the loads are in flight together
-        const float p_alpha_h1 = Lf[ALPHA_H1][slot];
-        const float p_cap_comp = Lf[CAP_COMP][slot];
-        const float p_cap_hmax = Lf[CAP_HMAX][slot];
-        const float p_cap_n = Lf[CAP_N][slot];
-        const float p_cf_soil = Lf[CF_SOIL][slot];
-        const float p_cmax = Lf[CMAX][slot];
-        const float p_compact_frac = Lf[COMPACT_FRAC][slot];
-        const float p_ddf = Lf[DDF][slot];
-        const float p_e_r = Lf[E_R][slot];
-        const float p_gap = Lf[GAP][slot];
-        const float p_h1 = Lf[H1][slot];
-        const float p_h2 = Lf[H2][slot];
-        const float p_h3_high = Lf[H3_HIGH][slot];
-        const float p_h3_low = Lf[H3_LOW][slot];
-        const float p_h4 = Lf[H4][slot];
-        const float p_kc = Lf[KC][slot];
-        const float p_kh_ratio = Lf[KH_RATIO][slot];
-        const float p_max_leakage = Lf[MAX_LEAKAGE][slot];
-        const float p_psi_b = Lf[PSI_B][slot];
-        const float p_river_fraction = Lf[RIVER_FRACTION][slot];
-        const float p_rootdistpar = Lf[ROOTDISTPAR][slot];
-        const float p_rooting_depth = Lf[ROOTING_DEPTH][slot];
-        const float p_slope = Lf[SLOPE][slot];
-        const float p_soil_thickness = Lf[SOIL_THICKNESS][slot];
-        const float p_ssf_dtdx = Lf[SSF_DTDX][slot];
-        const float p_swc = Lf[SWC][slot];
-        const float p_sy = Lf[SY][slot];
-        const float p_theta_fc = Lf[THETA_FC][slot];
-        const float p_theta_r = Lf[THETA_R][slot];
-        const float p_theta_s = Lf[THETA_S][slot];
-        const float p_tt = Lf[TT][slot];
-        const float p_tti = Lf[TTI][slot];
-        const float p_ttm = Lf[TTM][slot];
-        const float p_water_fraction = Lf[WATER_FRACTION][slot];
-        const float p_whc = Lf[WHC][slot];
-        const float p_w_soil = Lf[W_SOIL][slot];
-        const float p_z_exp = Lf[Z_EXP][slot];
+        const float p_alpha_h1 = VP(ALPHA_H1);
+        const float p_cap_comp = VP(CAP_COMP);
+        const float p_cap_hmax = VP(CAP_HMAX);
+        const float p_cap_n = VP(CAP_N);
+        const float p_cf_soil = VP(CF_SOIL);
+        const float p_cmax = VP(CMAX);
+        const float p_compact_frac = VP(COMPACT_FRAC);
+        const float p_ddf = VP(DDF);
+        const float p_e_r = VP(E_R);
+        const float p_gap = VP(GAP);
+        const float p_h1 = VP(H1);
+        const float p_h2 = VP(H2);
+        const float p_h3_high = VP(H3_HIGH);
+        const float p_h3_low = VP(H3_LOW);
+        const float p_h4 = VP(H4);
+        const float p_kc = VP(KC);
+        const float p_kh_ratio = VP(KH_RATIO);
+        const float p_max_leakage = VP(MAX_LEAKAGE);
+        const float p_psi_b = VP(PSI_B);
+        const float p_river_fraction = VP(RIVER_FRACTION);
+        const float p_rootdistpar = VP(ROOTDISTPAR);
+        const float p_rooting_depth = VP(ROOTING_DEPTH);
+        const float p_slope = VP(SLOPE);
+        const float p_soil_thickness = VP(SOIL_THICKNESS);
+        const float p_ssf_dtdx = VP(SSF_DTDX);
+        const float p_swc = VP(SWC);
+        const float p_sy = VP(SY);
+        const float p_theta_fc = VP(THETA_FC);
+        const float p_theta_r = VP(THETA_R);
+        const float p_theta_s = VP(THETA_S);
+        const float p_tt = VP(TT);
+        const float p_tti = VP(TTI);
+        const float p_ttm = VP(TTM);
+        const float p_water_fraction = VP(WATER_FRACTION);
+        const float p_whc = VP(WHC);
+        const float p_w_soil = VP(W_SOIL);
+        const float p_z_exp = VP(Z_EXP);
         const float Pf = V(VS_PRECIP), PETf = V(VS_POTEVAP), Tf = V(VS_TEMP);
         const ff canopy0 = VF(VS_CANOPY_H, VS_CANOPY_L);
         const ff snow0 = F.snow ? VF(VS_SNOW_H, VS_SNOW_L) : ff{0.0f, 0.0f};
         const ff sw0 = F.snow ? VF(VS_SW_H, VS_SW_L) : ff{0.0f, 0.0f};
-        if (F.mass_balance) F.Mf[BL_PREV][e] = vd[VD_TSWS * bd] + wff::to_d(wff::add(canopy0, wff::add(snow0, sw0)));
+        if (F.mass_balance && PHASE != VERT_SOIL)
+            F.Mf[BL_PREV][e] = vd[VD_TSWS * bd] + wff::to_d(wff::add(canopy0, wff::add(snow0, sw0))) +
+                               (F.glacier ? F.GM[GM_STORE][e] * F.G[G_FRAC][slot] : 0.0);
         // ---- interception (canopy.jl:213-226 Gash, :259-271 Rutter)
         const float gapf = p_gap, cmaxf = p_cmax;
         const float potevap_f = p_kc * PETf * (1.0f - gapf);
@@ -481,7 +589,12 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         float icf, sff;
         Store canopy;
         canopy.init(canopy0);
-        if (F.gash) {
+        if (PHASE == VERT_SOIL) {  // after the transport sweep: the interception of VERT_SNOW
+            ic = wff::from_d(F.GM[GM_IC][e]);
+            icf = wff::to_f(ic);
+            tf = {0.0f, 0.0f};
+            sff = 0.0f;
+        } else if (F.gash) {
             if (cmaxf > 0.0f) {
                 const float e_r = p_e_r;
                 float fs, fi, psat;
@@ -517,7 +630,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
             }
             sff = fs * Pf;
             tf = wff::sub(wff::two_sum(Pf, -sff), pcf);
-            const ff cmax = lds(F, CMAX, slot);
+            const ff cmax = WS ? ff{W32[VW_CMAX], W32[VW_CMAX_LO]} : lds(F, CMAX, slot);
             if (wff::gt(canopy0, cmax)) {
                 tf = wff::add(tf, wff::mul(wff::sub(canopy0, cmax), inv_dt));
                 canopy.set(cmax);
@@ -543,7 +656,11 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         ff wfs;
         float swe_out = 0.0f;
         Store snow, sw;
-        if (F.snow) {
+        if (PHASE == VERT_SOIL) {  // the moved snow states and the snow runoff of VERT_SNOW
+            snow.init(snow0);
+            sw.init(sw0);
+            wfs = wff::from_d(F.GM[GM_SRUNOFF][e]);
+        } else if (F.snow) {
             snow.init(snow0);
             sw.init(sw0);
             const ff eff = wff::add(tf, sff);
@@ -586,10 +703,40 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         } else {
             wfs = wff::add(tf, sff);
         }
+        if (PHASE == VERT_SNOW) {
+            // lateral_snow_transport! capacities from the updated states (surface_process.jl:9-19)
+            if (!F.gash && canopy.changed()) stm(F, CANOPY, e, canopy.value());
+            stm(F, SNOW, e, snow.value());
+            stm(F, SNOW_WATER, e, sw.value());
+            Mh[SWE][e] = swe_out;
+            Mh[INTERCEPTION][e] = icf;
+            F.GM[GM_IC][e] = wff::to_d(ic);
+            F.GM[GM_SRUNOFF][e] = wff::to_d(wfs);
+            const double snow_d = wff::to_d(snow.value()), sw_d = wff::to_d(sw.value());
+            const double frac = fmin(0.5, (WS ? W64[VW_D_SLOPE] : F.L[SLOPE][slot]) / wfsn::TAN80) *
+                                fmin(1.0, snow_d / wfsn::SNOW_STORAGE_MAX);
+            F.GM[GM_CAP][e] = frac * snow_d / F.dt;
+            F.GM[GM_CAPW][e] = sw_d * frac / F.dt;
+            continue;
+        }
+        // glacier (glacier.jl:122-154, FP64) and its melt in the water flux at the surface
+        // (runoff.jl:49-58)
+        float gfrac_f = 0.0f;
+        if (F.glacier) {
+            const double gfrac = F.G[G_FRAC][slot];
+            double snow_d = wff::to_d(snow.value()), store, melt;
+            wfsn::glacier_hbv(gfrac, F.GM[GM_STORE][e], snow_d, (double)Tf, F.G[G_TTM][slot], F.G[G_DDF][slot],
+                              F.G[G_SIFRAC][slot], F.g_max_rate, F.dt, &snow_d, &store, &melt);
+            F.GM[GM_STORE][e] = store;
+            F.GM[GM_MELT][e] = melt;
+            snow.set(wff::from_d(snow_d));
+            wfs = wff::from_d(wff::to_d(wfs) + melt * gfrac);
+            gfrac_f = (float)gfrac;
+        }
         // ---- open water (runoff.jl open-water runoff and evaporation)
         const float rfrac_f = p_river_fraction, wfrac_f = p_water_fraction;
         const float wd_land = V(VS_OL_H);
-        const int64_t rs = F.land_river_slot[slot];
+        const int64_t rs = WS ? (int64_t)__double_as_longlong(W64[VW_D_CUM + MAXN + 1]) : F.land_river_slot[slot];
         const float wd_river = rs >= 0 ? F.RMh[RV_H][rs * M + m] : 0.0f;
         const ff runoff_river = wff::mul(wfs, fminf(1.0f, rfrac_f));
         const ff runoff_land = wff::mul(wfs, fminf(1.0f, wfrac_f));
@@ -597,14 +744,14 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         const float ae_land_f = wfrac_f * fminf(wd_land * inv_dtf, PETf);
         // ---- soil (soil.jl update! of SbmSoilModel)
         const ff wfs_soil = wff::fmax0(wff::sub(wff::sub(wfs, runoff_river), runoff_land));
-        const float soil_fraction = fmaxf(gapf - wfrac_f - rfrac_f, 0.0f);
+        const float soil_fraction = fmaxf(gapf - wfrac_f - rfrac_f - gfrac_f, 0.0f);
         const float pot_trans = fmaxf(0.0f, potevap_f - icf);
         const float pot_soilevap = soil_fraction * PETf;
-        const double d_soil = F.L[SOIL_THICKNESS][slot];
+        const double d_soil = WS ? W64[VW_D_SOIL_THICKNESS] : F.L[SOIL_THICKNESS][slot];
         const double sat = vd[VD_SAT * bd];
-        const double zi = fmax(0.0, fma(-sat, F.L[INV_TE][slot], d_soil));
+        const double zi = fmax(0.0, fma(-sat, WS ? W64[VW_D_INV_TE] : F.L[INV_TE][slot], d_soil));
         ColG<MAXN> g;
-        g.set(F, slot, zi);
+        g.set(F, slot, zi, WS ? W32 + VW_LY : nullptr, WS ? W64 + VW_D_CUM : nullptr);
         const float zif = (float)zi, df = p_soil_thickness, satf = (float)sat;
         const float ts = p_theta_s, tr = p_theta_r, tfc = p_theta_fc;
         const float te = ts - tr;
@@ -617,9 +764,9 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         for (int k = 0; k < MAXN; ++k) {
             if (k < g.N) {
                 us[k].init(VF(VS_USLD_H + k, VS_USLD_H + MAXN + k));
-                kvf[k] = F.LYf[LY_KVFRAC][k][slot];
-                cexp[k] = F.LYf[LY_C][k][slot];
-                rfr[k] = F.LYf[LY_ROOTFRAC][k][slot];
+                kvf[k] = WS ? W32[VW_LY + 2 * MAXN + k] : F.LYf[LY_KVFRAC][k][slot];
+                cexp[k] = WS ? W32[VW_LY + 3 * MAXN + k] : F.LYf[LY_C][k][slot];
+                rfr[k] = WS ? W32[VW_LY + 4 * MAXN + k] : F.LYf[LY_ROOTFRAC][k][slot];
             } else {
                 us[k].init({0.0f, 0.0f});
                 kvf[k] = cexp[k] = rfr[k] = 0.0f;
@@ -759,12 +906,18 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
             drain -= act_sat_f * dtf;
         }
         // actual infiltration: water above the capacity of a layer moves up, the top layer's
-        // excess leaves the soil (soil.jl)
+        // excess leaves the soil (soil.jl). The capacity thick * te is FP32 here, while the
+        // subsurface completion decides how far a rising water table saturates a layer from the
+        // double-FP32 capacity; a layer left fuller than that by FP32 rounding would lose the
+        // surplus when the table saturates it, so the capacities that fill layers (this one and the
+        // capillary rise below) are taken a relative 1e-6 short of the FP32 figure (its error is
+        // below 2e-7).
+        const float cap_short = 1.0f - 1e-6f;
         float excess = 0.0f;
 #pragma unroll
         for (int k = MAXN; k >= 1; --k) {
             if (k > g.nu) continue;
-            excess = fmaxf(0.0f, us[k - 1].val() - g.thick[k - 1] * te);
+            excess = fmaxf(0.0f, us[k - 1].val() - g.thick[k - 1] * te * cap_short);
             us[k - 1].add(-excess);
             if (k > 1) us[k - 2].add(excess);
         }
@@ -788,7 +941,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
             for (int k = MAXN; k >= 1; --k) {
                 if (k > g.nu) continue;
                 const float toadd =
-                    fminf(capflux, fmaxf((g.thick[k - 1] * te - us[k - 1].val()) * inv_dtf, 0.0f));
+                    fminf(capflux, fmaxf((g.thick[k - 1] * te * cap_short - us[k - 1].val()) * inv_dtf, 0.0f));
                 us[k - 1].add_prod(toadd, dtf);
                 capflux -= toadd;
                 capacc.add(toadd);
@@ -803,10 +956,12 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         const ff aet = wff::add(wff::add(wff::add(wff::add(soilevap, transpiration), ae_river_f), ae_land_f), ic);
         // ---- write back
         if (!F.gash && canopy.changed()) stm(F, CANOPY, e, canopy.value());
-        if (F.snow) {
+        if (F.snow && PHASE == VERT_ALL) {
             stm(F, SNOW, e, snow.value());
             stm(F, SNOW_WATER, e, sw.value());
             Mh[SWE][e] = swe_out;
+        } else if (PHASE == VERT_SOIL && F.glacier) {
+            stm(F, SNOW, e, snow.value());
         }
         Mh[TSOIL][e] = tsoil;
 #pragma unroll
@@ -826,7 +981,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         stm(F, INFEX, e, infex);
         stm(F, RUNOFF_LAND, e, runoff_land);
         stm(F, AE_LAND, e, wff::from_f(ae_land_f));
-        Mh[INTERCEPTION][e] = icf;
+        if (PHASE == VERT_ALL) Mh[INTERCEPTION][e] = icf;
         Mh[TRANSPIRATION][e] = wff::to_f(transpiration);
         Mh[SOIL_EVAP][e] = wff::to_f(soilevap);
         Mh[ACT_INFILT][e] = wff::to_f(act_infilt);
@@ -838,7 +993,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         // terms of the subsurface solve that do not depend on the upstream discharge: the
         // double-FP32 recharge flux for the exact bookkeeping, FP32 inputs of the walker
         if (F.ssf_single) {
-            ff flux = wff::mul(recharge, lds(F, AREA, slot));  // recharge flux of the subsurface model
+            ff flux = wff::mul(recharge, WS ? ff{W32[VW_AREA_HI], W32[VW_AREA_LO]} : lds(F, AREA, slot));  // recharge flux of the subsurface model
             if (zi >= d_soil) flux = wff::fmax0(flux);
             stm(F, SSF_QNET, e, flux);
             Mh[SSF_QNETF][e] = wff::to_f(flux);
@@ -866,6 +1021,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         }
     }
 }
+#undef VP
 
 // ------------------------------------------------------------------ SSF wavefront -------
 
@@ -909,7 +1065,10 @@ struct SsfSplitPhys {
     WfDevGraph g;
     WfSweep sw;
 
-    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end) {
+    // the heavy child's discharge is read from the double-FP32 field (hq is unused): this walker
+    // runs one sub-step per launch (adaptive sub-steps), one lane per chain-member pair
+    __device__ bool node(int64_t slot, int64_t e, int m, int s, uint32_t ep, int64_t chain, bool is_end,
+                         double& /*hq*/) {
         const FFMem Mf{F};
         double* const* L = F.L;
         double dt_s;
@@ -1374,6 +1533,46 @@ struct OlWave {
         x.sfw_pos = F.Lf[SFW][slot] > 0.0f;
         wfv::load_rec<true>(g, slot, x.up);
     }
+    struct St {
+        wff::ff u, qp, qsum;
+    };
+    __device__ __forceinline__ void start(const In& x, St& st) const {
+        st.u = x.u;
+        st.qp = x.q;
+        st.qsum = {0.0f, 0.0f};
+    }
+    // sub-step s of the node
+    __device__ __forceinline__ bool sub(const In& x, St& st, unsigned long long w0, unsigned long long w1,
+                                        int64_t slot, int64_t e, int m, int s, int64_t chain, bool is_end, bool heavy,
+                                        unsigned long long qh_in, unsigned long long& qh_out) const {
+        using DT = typename std::conditional<ADAPT, wff::ff, float>::type;
+        DT dt_s;
+        if constexpr (ADAPT) dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
+        else dt_s = sw.dts_f[s];
+        wff::ff qin;
+        if (!wfv::gather_w<true>(g, sw, x.up, w0, w1, slot, m, s, heavy, qh_in, F.status, qin)) return false;
+        if (!x.sfw_pos) qin = {0.0f, 0.0f};
+        wff::ff un, qn;
+        kw_node_ff<ADAPT>(qin, st.qp, x.qlat, st.u, x.invdx, dt_s, x.alpha, un, qn);
+        st.u = un;
+        st.qp = qn;
+        qh_out = wff::pack(qn);
+        if (is_end) wfv::publish(g, chain, m, s, qn);
+        st.qsum = wff::add(st.qsum, mul_dt(qn, dt_s));
+        return true;
+    }
+    // the node's state after the last sub-step of the launch (or of a round of the diagonal
+    // schedule); add_stored: the step's cumulative discharge so far is added
+    __device__ __forceinline__ void finish(const St& st, int64_t e, bool add_stored) const {
+        float* const* Mh = F.Mh;
+        Mh[OL_UH][e] = st.u.hi;
+        Mh[OL_UL][e] = st.u.lo;
+        stm(F, OL_Q, e, st.qp);
+        wff::ff qsum = st.qsum;
+        if (add_stored) qsum = wff::add(qsum, wff::ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]});
+        Mh[OL_QSUMH][e] = qsum.hi;
+        Mh[OL_QSUML][e] = qsum.lo;
+    }
     __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
                                          int64_t chain, bool is_end, bool heavy, unsigned long long* qh) {
         const int stride = blockDim.x;
@@ -1383,30 +1582,16 @@ struct OlWave {
             if (!(f & WF_SUB_ACTIVE)) return true;
             first = (f & WF_SUB_FIRST) != 0;
         }
-        wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f};
+        St st;
+        start(x, st);
         for (int s = 0; s < sw.S; ++s) {
-            using DT = typename std::conditional<ADAPT, wff::ff, float>::type;
-            DT dt_s;
-            if constexpr (ADAPT) dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
-            else dt_s = sw.dts_f[s];
-            wff::ff qin;
-            if (!wfv::gather<true>(g, sw, x.up, ends, slot, m, s, heavy, qh[s * stride], F.status, qin)) return false;
-            if (!x.sfw_pos) qin = {0.0f, 0.0f};
-            wff::ff un, qn;
-            kw_node_ff<ADAPT>(qin, qp, x.qlat, u, x.invdx, dt_s, x.alpha, un, qn);
-            u = un;
-            qp = qn;
-            qh[s * stride] = wff::pack(qn);
-            if (is_end) wfv::publish(g, chain, m, s, qn);
-            qsum = wff::add(qsum, mul_dt(qn, dt_s));
+            unsigned long long out;
+            if (!sub(x, st, wfv::end_word0(ends, s), s == 0 ? ends.lq1 : wfv::SENTINEL, slot, e, m, s, chain, is_end,
+                     heavy, qh[s * stride], out))
+                return false;
+            qh[s * stride] = out;
         }
-        float* const* Mh = F.Mh;
-        Mh[OL_UH][e] = u.hi;
-        Mh[OL_UL][e] = u.lo;
-        stm(F, OL_Q, e, qp);
-        if (!first) qsum = wff::add(qsum, wff::ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]});
-        Mh[OL_QSUMH][e] = qsum.hi;
-        Mh[OL_QSUML][e] = qsum.lo;
+        finish(st, e, !first);
         return true;
     }
 };
@@ -1441,6 +1626,69 @@ struct RvWave {
         x.res = RES ? F.res_of_rslot[slot] : -1;
         wfv::load_rec<false>(g, slot, x.up);
     }
+    struct St {
+        wff::ff u, qp, qsum, asum;
+    };
+    __device__ __forceinline__ void start(const In& x, St& st) const {
+        st.u = x.u;
+        st.qp = x.q;
+        st.qsum = {0.0f, 0.0f};
+        st.asum = {0.0f, 0.0f};
+    }
+    // sub-step s of the node
+    __device__ __forceinline__ bool sub(const In& x, St& st, unsigned long long w0, unsigned long long w1,
+                                        int64_t slot, int64_t e, int m, int s, int64_t chain, bool is_end, bool heavy,
+                                        unsigned long long qh_in, unsigned long long& qh_out) const {
+        using DT = typename std::conditional<ADAPT, wff::ff, float>::type;
+        DT dt_s;
+        float dt_f;
+        if constexpr (ADAPT) {
+            dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
+            dt_f = dt_s.hi;
+        } else {
+            dt_s = sw.dts_f[s];
+            dt_f = dt_s;
+        }
+        wff::ff qin;
+        if (!wfv::gather_w<false>(g, sw, x.up, w0, w1, slot, m, s, heavy, qh_in, F.status, qin)) return false;
+        wff::ff ql = x.qlatt;
+        if (x.ext < 0.0f) {  // abstraction: qlatt holds the lateral inflow alone
+            const float storage = x.len * (x.alpha * (st.u.hi * st.u.hi * st.u.hi));
+            const float absd = fminf(-x.ext, (storage / dt_f) * 0.80f);
+            ql = wff::add(ql, wff::mul(x.invlen, -absd));
+            st.asum = wff::add(st.asum, mul_dt(wff::ff{absd, 0.0f}, dt_s));
+        }
+        wff::ff un, qn;
+        kw_node_ff<ADAPT>(qin, st.qp, ql, st.u, x.invlen, dt_s, x.alpha, un, qn);
+        st.u = un;
+        st.qp = qn;
+        wff::ff q_down = qn;
+        if (RES && x.res >= 0) {
+            const double dt_d = ADAPT ? sw.adt[m] : sw.dts[s];
+            q_down = wff::from_d(wfr::reservoir_node(F, x.res, m, wff::to_d(qn), dt_d));
+        }
+        qh_out = wff::pack(q_down);
+        if (is_end) wfv::publish(g, chain, m, s, q_down);
+        st.qsum = wff::add(st.qsum, mul_dt(qn, dt_s));
+        return true;
+    }
+    // the node's state after the last sub-step of the launch (or of a round of the diagonal
+    // schedule); add_stored: the step's cumulative discharge and abstraction so far are added
+    __device__ __forceinline__ void finish(const St& st, int64_t e, bool add_stored) const {
+        float* const* RMh = F.RMh;
+        RMh[RV_UH][e] = st.u.hi;
+        RMh[RV_UL][e] = st.u.lo;
+        str(F, RV_Q, e, st.qp);
+        wff::ff qsum = st.qsum, asum = st.asum;
+        if (add_stored) {
+            qsum = wff::add(qsum, wff::ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]});
+            asum = wff::add(asum, wff::ff{RMh[RV_ABSH][e], RMh[RV_ABSL][e]});
+        }
+        RMh[RV_QSUMH][e] = qsum.hi;
+        RMh[RV_QSUML][e] = qsum.lo;
+        RMh[RV_ABSH][e] = asum.hi;
+        RMh[RV_ABSL][e] = asum.lo;
+    }
     __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
                                          int64_t chain, bool is_end, bool heavy, unsigned long long* qh) {
         const int stride = blockDim.x;
@@ -1450,52 +1698,16 @@ struct RvWave {
             if (!(f & WF_SUB_ACTIVE)) return true;
             first = (f & WF_SUB_FIRST) != 0;
         }
-        wff::ff u = x.u, qp = x.q, qsum = {0.0f, 0.0f}, asum = {0.0f, 0.0f};
+        St st;
+        start(x, st);
         for (int s = 0; s < sw.S; ++s) {
-            using DT = typename std::conditional<ADAPT, wff::ff, float>::type;
-            DT dt_s;
-            float dt_f;
-            if constexpr (ADAPT) {
-                dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
-                dt_f = dt_s.hi;
-            } else {
-                dt_s = sw.dts_f[s];
-                dt_f = dt_s;
-            }
-            wff::ff qin;
-            if (!wfv::gather<false>(g, sw, x.up, ends, slot, m, s, heavy, qh[s * stride], F.status, qin)) return false;
-            wff::ff ql = x.qlatt;
-            if (x.ext < 0.0f) {  // abstraction: qlatt holds the lateral inflow alone
-                const float storage = x.len * (x.alpha * (u.hi * u.hi * u.hi));
-                const float absd = fminf(-x.ext, (storage / dt_f) * 0.80f);
-                ql = wff::add(ql, wff::mul(x.invlen, -absd));
-                asum = wff::add(asum, mul_dt(wff::ff{absd, 0.0f}, dt_s));
-            }
-            wff::ff un, qn;
-            kw_node_ff<ADAPT>(qin, qp, ql, u, x.invlen, dt_s, x.alpha, un, qn);
-            u = un;
-            qp = qn;
-            wff::ff q_down = qn;
-            if (RES && x.res >= 0) {
-                const double dt_d = ADAPT ? sw.adt[m] : sw.dts[s];
-                q_down = wff::from_d(wfr::reservoir_node(F, x.res, m, wff::to_d(qn), dt_d));
-            }
-            qh[s * stride] = wff::pack(q_down);
-            if (is_end) wfv::publish(g, chain, m, s, q_down);
-            qsum = wff::add(qsum, mul_dt(qn, dt_s));
+            unsigned long long out;
+            if (!sub(x, st, wfv::end_word0(ends, s), s == 0 ? ends.lq1 : wfv::SENTINEL, slot, e, m, s, chain, is_end,
+                     heavy, qh[s * stride], out))
+                return false;
+            qh[s * stride] = out;
         }
-        float* const* RMh = F.RMh;
-        RMh[RV_UH][e] = u.hi;
-        RMh[RV_UL][e] = u.lo;
-        str(F, RV_Q, e, qp);
-        if (!first) {
-            qsum = wff::add(qsum, wff::ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]});
-            asum = wff::add(asum, wff::ff{RMh[RV_ABSH][e], RMh[RV_ABSL][e]});
-        }
-        RMh[RV_QSUMH][e] = qsum.hi;
-        RMh[RV_QSUML][e] = qsum.lo;
-        RMh[RV_ABSH][e] = asum.hi;
-        RMh[RV_ABSL][e] = asum.lo;
+        finish(st, e, !first);
         return true;
     }
 };
@@ -1506,14 +1718,38 @@ __global__ void __launch_bounds__(128) wave_kernel(Phys phys) {
 }
 
 template <class Phys>
+__global__ void __launch_bounds__(128) wave_diag_kernel(Phys phys) {
+    wfv::walk_diag(phys.g, phys.sw, phys, phys.F.status);
+}
+
+template <class Phys>
 cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
     const size_t smem = wfv::walk_smem(threads, phys.sw.S);
     int blocks;
     Phys p = phys;
+    p.sw.SL = 1;
     cudaError_t err = wave_grid(wave_kernel<Phys>, threads, smem, c, p.g, blocks, p.sw.prio_items);
     if (err != cudaSuccess) return err;
     wave_kernel<Phys><<<blocks, threads, smem, c.stream>>>(p);
+    return cudaGetLastError();
+}
+
+// Overland and river launches of several fixed sub-steps run on the diagonal schedule
+// (wfv::walk_diag); one sub-step per launch (and the subsurface sweep) node-major.
+template <class Phys>
+cudaError_t launch_wave_sub(const Phys& phys, const WfLaunchCfg& c) {
+    const int SL = wave_sub_lanes(phys.sw.S, c);
+    if (phys.sw.aflag || SL <= 1) return launch_wave(phys, c);
+    const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
+    const size_t smem = wfv::diag_smem(threads);
+    int blocks;
+    Phys p = phys;
+    p.sw.SL = SL;
+    cudaError_t err = wave_grid(wave_diag_kernel<Phys>, threads, smem, c, p.g, blocks, p.sw.prio_items,
+                                wf_items_per_chunk(p.g.G, p.g.M, SL));
+    if (err != cudaSuccess) return err;
+    wave_diag_kernel<Phys><<<blocks, threads, smem, c.stream>>>(p);
     return cudaGetLastError();
 }
 
@@ -1794,7 +2030,9 @@ __global__ void __launch_bounds__(256, 4) balance_split_kernel(WfDevFields F) {
         const ff inv_area = lds(F, INV_AREA, slot);
         const ff snow = ldm(F, SNOW, e), sw = ldm(F, SNOW_WATER, e), canopy = ldm(F, CANOPY, e);
         const double tsws = F.Mf[TSWS][e];
-        ff ts = wff::add(wff::add(wff::add(snow, sw), canopy), wff::from_d(tsws));
+        // glacier store x fraction (FP64, mass_balance.jl:96-113)
+        const double glacier = F.glacier ? F.GM[GM_STORE][e] * F.G[G_FRAC][slot] : 0.0;
+        ff ts = wff::add(wff::add(wff::add(snow, sw), canopy), wff::from_d(tsws + glacier));
         ts = wff::add(ts, wff::mul(ldm(F, OL_H, e), 1.0f - F.Lf[RIVER_FRACTION][slot]));
         if (rs >= 0)
             ts = wff::add(ts, wff::mul(wff::mul(wff::mul(ldr(F, RV_H, rs * M + m), ldrs(F, R_WIDTH, rs)),
@@ -1803,12 +2041,17 @@ __global__ void __launch_bounds__(256, 4) balance_split_kernel(WfDevFields F) {
         stm(F, TOTAL_STORAGE, e, ts);
         if (!F.mass_balance) continue;
         {
-            const ff tin = wff::add(wff::mul(ldm(F, SSF_QIN_AVG, e), inv_area), F.Mh[PRECIP][e]);
+            ff tin = wff::add(wff::mul(ldm(F, SSF_QIN_AVG, e), inv_area), F.Mh[PRECIP][e]);
             const ff vout = wff::add(wff::add(wff::add(ldm(F, NET_RUNOFF, e), ldm(F, AET, e)),
                                               ldm(F, NET_RUNOFF_RIVER, e)),
                                      ldm(F, LEAKAGE, e));
-            const ff tout = wff::add(wff::mul(ldm(F, SSF_Q_AVG, e), inv_area), vout);
-            const double ds = (tsws - F.Mf[BL_PREV][e]) + wff::to_d(wff::add(canopy, wff::add(snow, sw)));
+            ff tout = wff::add(wff::mul(ldm(F, SSF_Q_AVG, e), inv_area), vout);
+            if (F.snow_transport) {  // snow moved in and out (mass_balance.jl:236-244)
+                tin = wff::add(tin, wff::from_d(F.GM[GM_SNOW_IN][e]));
+                tout = wff::add(tout, wff::from_d(F.GM[GM_SNOW_OUT][e]));
+            }
+            const double ds =
+                (tsws - F.Mf[BL_PREV][e]) + glacier + wff::to_d(wff::add(canopy, wff::add(snow, sw)));
             mb_error_ff(tin, tout, wff::mul(wff::from_d(ds), inv_dt), err, rel);
             stm(F, BL_ERR, e, err);
             stm(F, BL_REL, e, rel);
@@ -1883,6 +2126,7 @@ cudaError_t launch_walk_split(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
     int blocks;
     Phys p = phys;
+    p.sw.SL = 1;
     cudaError_t err = wave_grid(walk_split_kernel<Phys>, threads, 0, c, p.g, blocks, p.sw.prio_items);
     if (err != cudaSuccess) return err;
     walk_split_kernel<Phys><<<blocks, threads, 0, c.stream>>>(p);
@@ -1898,23 +2142,38 @@ int grid_for(int64_t n, int block, int num_sms) {
 
 }  // namespace
 
-cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c) {
+namespace {
+template <int MAXN, int PHASE, bool WS>
+cudaError_t launch_vertical_split_n(const WfDevFields& F, int grid, int block, cudaStream_t st) {
+    size_t smem = 2 * VStage<MAXN>::bytes_per_thread * block;
+    if (WS) smem += (size_t)(block / 32) * 2 * VWarp<MAXN>::bytes;
+    cudaError_t e = cudaFuncSetAttribute(vertical_split_kernel<MAXN, PHASE, WS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    vertical_split_kernel<MAXN, PHASE, WS><<<grid, block, smem, st>>>(F);
+    return cudaGetLastError();
+}
+
+template <int PHASE>
+cudaError_t launch_vertical_split(const WfDevFields& F, const WfLaunchCfg& c) {
     const int block = c.vertical_block > 0 ? c.vertical_block : 256;
     const int grid = grid_for(F.land_slots * F.M, block, c.num_sms);
-    if (F.N <= 4) {
-        const size_t smem = 2 * VStage<4>::bytes_per_thread * block;
-        cudaError_t e = cudaFuncSetAttribute(vertical_split_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        vertical_split_kernel<4><<<grid, block, smem, c.stream>>>(F);
-    } else {
-        const size_t smem = 2 * VStage<WF_MAX_LAYERS>::bytes_per_thread * block;
-        cudaError_t e = cudaFuncSetAttribute(vertical_split_kernel<WF_MAX_LAYERS>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        vertical_split_kernel<WF_MAX_LAYERS><<<grid, block, smem, c.stream>>>(F);
-    }
-    return cudaGetLastError();
+    // the cell's parameters once per warp when its members fill whole warps
+    const bool ws = F.M % 32 == 0 && block % 32 == 0;
+    if (F.N <= 4)
+        return ws ? launch_vertical_split_n<4, PHASE, true>(F, grid, block, c.stream)
+                  : launch_vertical_split_n<4, PHASE, false>(F, grid, block, c.stream);
+    return ws ? launch_vertical_split_n<WF_MAX_LAYERS, PHASE, true>(F, grid, block, c.stream)
+              : launch_vertical_split_n<WF_MAX_LAYERS, PHASE, false>(F, grid, block, c.stream);
+}
+}  // namespace
+
+cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c) { return launch_vertical_split<VERT_ALL>(F, c); }
+cudaError_t wf_split_vertical_snow(const WfDevFields& F, const WfLaunchCfg& c) {
+    return launch_vertical_split<VERT_SNOW>(F, c);
+}
+cudaError_t wf_split_vertical_soil(const WfDevFields& F, const WfLaunchCfg& c) {
+    return launch_vertical_split<VERT_SOIL>(F, c);
 }
 
 cudaError_t wf_split_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
@@ -1938,16 +2197,16 @@ cudaError_t wf_split_ssf_wave(const WfDevFields& F, const WfDevGraph& g, const W
 cudaError_t wf_split_overland_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw,
                                    const WfLaunchCfg& c) {
     if (sw.aflag) return launch_wave(OlWave<true>{F, g, sw}, c);
-    return launch_wave(OlWave<false>{F, g, sw}, c);
+    return launch_wave_sub(OlWave<false>{F, g, sw}, c);
 }
 
 cudaError_t wf_split_river_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c) {
     if (F.n_res > 0) {
         if (sw.aflag) return launch_wave(RvWave<true, true>{F, g, sw}, c);
-        return launch_wave(RvWave<false, true>{F, g, sw}, c);
+        return launch_wave_sub(RvWave<false, true>{F, g, sw}, c);
     }
     if (sw.aflag) return launch_wave(RvWave<true, false>{F, g, sw}, c);
-    return launch_wave(RvWave<false, false>{F, g, sw}, c);
+    return launch_wave_sub(RvWave<false, false>{F, g, sw}, c);
 }
 
 cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {

@@ -43,6 +43,7 @@ struct DevGraphAlloc {
     double* end_q = nullptr;
     unsigned long long* ticket = nullptr;
     int32_t s_cap = 1;
+    int32_t* snow_up = nullptr;  // land graph with snow transport: up entries in topological-sort order
 };
 
 }  // namespace
@@ -240,7 +241,37 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.end_q = G.end_q;
     g.ticket = G.ticket;
     g.s_cap = G.s_cap;
+    g.snow_up = G.snow_up;
     return g;
+}
+
+// Graphs.jl v1.14 topological_sort_by_dfs (Wflow's network.order, network.jl:99) of a graph of
+// out-degree <= 1: vertices in index order; from an unvisited vertex follow the downstream links
+// to unvisited vertices, finish the path from its downstream end back; the order is the reverse
+// of the finishing order. Empty on a cycle.
+std::vector<int64_t> topo_order_dfs(int64_t n, const int32_t* ds) {
+    std::vector<uint8_t> color((size_t)n, 0);
+    std::vector<int64_t> verts, stack;
+    verts.reserve((size_t)n);
+    for (int64_t v = 0; v < n; ++v) {
+        if (color[v]) continue;
+        stack.assign(1, v);
+        color[v] = 1;
+        while (!stack.empty()) {
+            const int64_t u = stack.back();
+            const int32_t w = ds[u];
+            if (w >= 0 && color[w] == 1) return {};
+            if (w >= 0 && color[w] == 0) {
+                color[w] = 1;
+                stack.push_back(w);
+            } else {
+                color[u] = 2;
+                verts.push_back(u);
+                stack.pop_back();
+            }
+        }
+    }
+    return std::vector<int64_t>(verts.rbegin(), verts.rend());
 }
 
 // fixed sub-steps of a sweep (routing/timestepping.jl:11-16 with the while loop of the
@@ -307,6 +338,7 @@ WfLaunchCfg launch_cfg(const WfHandle* h) {
     c.vertical_block = h->tuning.vertical_block;
     c.walk_warps = h->tuning.routing_warps;
     c.walk_blocks = h->tuning.routing_blocks_per_sm > 0 ? h->tuning.routing_blocks_per_sm * h->num_sms : 0;
+    c.sub_lanes = h->tuning.reserved[3];
     return c;
 }
 
@@ -459,6 +491,13 @@ FieldRef field_ref(WfHandle* h, int field, int layer) {
         case WF_F_VOLUMETRIC_WATER_CONTENT:
             r.derived_vwc = (layer >= 0 && layer < h->N);
             break;
+        case WF_F_GLACIER_STORE:
+            r.p = h->F.glacier ? h->F.GM[GM_STORE] : nullptr;
+            r.settable = true;
+            break;
+        case WF_F_GLACIER_MELT: r.p = h->F.glacier ? h->F.GM[GM_MELT] : nullptr; break;
+        case WF_F_SNOW_IN: r.p = h->F.snow_transport ? h->F.GM[GM_SNOW_IN] : nullptr; break;
+        case WF_F_SNOW_OUT: r.p = h->F.snow_transport ? h->F.GM[GM_SNOW_OUT] : nullptr; break;
         case WF_F_RIVER_Q: r.idx = RV_Q; r.river = true; r.settable = true; break;
         case WF_F_RIVER_H: r.idx = RV_H; r.river = true; r.settable = true; break;
         case WF_F_RIVER_STORAGE: r.idx = RV_STORAGE; r.river = true; r.settable = true; break;
@@ -505,6 +544,7 @@ std::vector<StateItem> state_items(const WfHandle* h) {
                   WF_F_LAND_STORAGE, WF_F_RIVER_Q, WF_F_RIVER_H, WF_F_RIVER_STORAGE})
         v.push_back({f, 0});
     for (int k = 0; k < h->N; ++k) v.push_back({WF_F_UNSATURATED_LAYER_DEPTH, k});
+    if (h->F.glacier) v.push_back({WF_F_GLACIER_STORE, 0});
     if (h->nres > 0) {  // reservoir states (water level; storage kept alongside for exact restarts)
         v.push_back({WF_F_RESERVOIR_STORAGE, 0});
         v.push_back({WF_F_RESERVOIR_WATERLEVEL, 0});
@@ -613,6 +653,11 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
     if (c->snow && (!p->degree_day_factor || !p->temperature_threshold_snowfall || !p->temperature_interval_snowfall ||
                     !p->temperature_threshold_melt || !p->water_holding_capacity))
         return set_err(nullptr, WF_ERR_INVALID, "snow parameters missing");
+    if ((c->snow_gravitational_transport || c->glacier) && !c->snow)
+        return set_err(nullptr, WF_ERR_INVALID,
+                       "gravitational snow transport and glaciers need the snow model (snow__flag, sbm.jl:45-49)");
+    if (c->snow_gravitational_transport && rs && rs->n > 0)
+        return set_err(nullptr, WF_ERR_UNSUPPORTED, "gravitational snow transport with reservoirs is not supported");
     if (d->n_river > 0 && (!d->river_land_index || !d->river_downstream || !d->river_width || !d->river_length ||
                            !d->river_slope || !d->river_manning_n || !d->river_bankfull_depth))
         return set_err(nullptr, WF_ERR_INVALID, "river arrays missing");
@@ -929,6 +974,48 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
         }
         if (F.split && wf_split_ff_member(f)) CKR(upload_slots_ff(h, &F.Mh[f], &F.Ml[f], *src, PL, M, n, true));
         else CKR(upload_slots(h, &F.Mf[f], *src, PL, M, n, true));
+    }
+    // ---- gravitational snow transport and glacier (FP64 in both forms)
+    F.snow_transport = c->snow_gravitational_transport != 0;
+    F.glacier = c->glacier != 0;
+    F.g_max_rate = 8.0 * ((1.0 / 86400.0) * 1e-3);  // to_SI(8.0, MM_PER_DAY) (glacier.jl:90)
+    if (F.glacier) {  // defaults: standard_name_sbm.jl:70-108, in SI
+        CKR(upload_slots(h, &F.G[G_FRAC], ext_vec(p->glacier_fraction, 0.0), PL, M, n, false));
+        CKR(upload_slots(h, &F.G[G_TTM], ext_vec(p->glacier_temperature_threshold_melt, 0.0 + 273.15), PL, M, n,
+                         false));
+        CKR(upload_slots(h, &F.G[G_DDF], ext_vec(p->glacier_degree_day_factor, 3.0 * ((1.0 / 86400.0) * 1e-3)), PL,
+                         M, n, false));
+        CKR(upload_slots(h, &F.G[G_SIFRAC], ext_vec(p->glacier_snow_to_ice_fraction, 0.001 * (1.0 / 86400.0)), PL,
+                         M, n, false));
+    }
+    if (F.glacier || F.snow_transport) {
+        for (int f = 0; f < GM_COUNT; ++f) {
+            std::vector<double> v((size_t)n * M, 0.0);
+            if (f == GM_STORE && F.glacier)
+                for (int m = 0; m < M; ++m)
+                    for (int64_t i = 0; i < n; ++i)
+                        v[(size_t)m * n + i] = p->glacier_initial_store ? p->glacier_initial_store[i] : 5.5;
+            CKR(upload_slots(h, &F.GM[f], v, PL, M, n, true));
+        }
+    }
+    if (F.snow_transport) {
+        // each slot's upstream entries in the order of the land graph's topological sort
+        const std::vector<int64_t> order = topo_order_dfs(n, d->land_downstream);
+        if ((int64_t)order.size() != n) {
+            set_err(h, WF_ERR_CYCLE, "the land drainage graph has a cycle (routing/utils.jl:26-31)");
+            return fail(WF_ERR_CYCLE);
+        }
+        std::vector<int64_t> pos((size_t)n);
+        for (int64_t k = 0; k < n; ++k) pos[order[k]] = k;
+        std::vector<int32_t> su(std::max<size_t>(PL.up_slot.size(), 1), 0);
+        for (int64_t sl = 0; sl < PL.n_slots; ++sl) {
+            const int32_t o0 = PL.up_ptr[sl], o1 = PL.up_ptr[sl + 1];
+            for (int32_t o = o0; o < o1; ++o) su[o] = o;
+            std::sort(su.begin() + o0, su.begin() + o1, [&](int32_t a, int32_t b) {
+                return pos[PL.node_of_slot[PL.up_slot[a]]] < pos[PL.node_of_slot[PL.up_slot[b]]];
+            });
+        }
+        CKR(upload(h, &h->land.snow_up, su));
     }
     // ---- river fields
     std::vector<double> r_width(nr), r_length(nr), r_alpha(nr), r_ext(nr), r_area(nr), r_inv_len(nr), r_inv_w(nr), r_inv_len_lo(nr);
@@ -1470,9 +1557,11 @@ int32_t wf_set_tuning(WfHandle* h, const WfTuning* t) {
     if (t->vertical_block < 0 || t->vertical_block > 1024 || (t->vertical_block % 32) != 0 || t->routing_warps < 0 ||
         t->routing_warps > 32 || t->routing_blocks_per_sm < 0 || t->routing_blocks_per_sm > 64)
         return set_err(h, WF_ERR_INVALID, "tuning out of range");
+    if (t->reserved[3] < 0 || t->reserved[3] > 32) return set_err(h, WF_ERR_INVALID, "sub-step lanes out of range");
     h->tuning = *t;
     h->graph_valid = false;
-    // test hooks in reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset
+    // reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset (test hooks),
+    // [2] = per-kernel event timing, [3] = cap of the routing sweeps' sub-step lanes (0 = default)
     if (t->reserved[0] > 0) h->wait_ns = (uint64_t)t->reserved[0] * 1000ull;
     h->wait_offset = (uint32_t)t->reserved[1];
     h->kernel_timing = t->reserved[2] != 0;
@@ -1526,6 +1615,41 @@ namespace {
 
 constexpr int64_t kMaxAdaptiveSubsteps = 100000;
 
+// The per-cell update of the step. With gravitational snow transport its snow part, the two
+// material sweeps over the land graph (one sub-step of the model step each, in the land graph's
+// wavefront scratch) and the inflow kernel run before its soil part (sbm.jl:92-131).
+int enqueue_vertical(WfHandle* h, const WfLaunchCfg& lc, const WfDevGraph& gl, int64_t& nl) {
+    const bool split = h->cfg.form == WF_FORM_SPLIT;
+    if (!h->F.snow_transport) {
+        CK(split ? wf_split_vertical(h->F, lc) : wf_fp64_vertical(h->F, lc));
+        ++nl;
+        return WF_OK;
+    }
+    CK(split ? wf_split_vertical_snow(h->F, lc) : wf_fp64_vertical_snow(h->F, lc));
+    ++nl;
+    for (int material = 0; material < 2; ++material) {
+        WfSweep sw{};
+        sw.S = 1;
+        sw.first = 0;
+        sw.last_of_step = 1;
+        sw.total = 1;
+        sw.epoch0 = 1;
+        sw.dt = h->cfg.dt;
+        sw.dts = h->dts_ssf;
+        sw.wait_ns = h->wait_ns;
+        sw.wait_offset = h->wait_offset;
+        CK(cudaMemsetAsync(gl.flags, 0, (size_t)h->land.plan.n_chains * h->M * sizeof(uint32_t), h->stream));
+        CK(cudaMemsetAsync(gl.ticket, 0, sizeof(unsigned long long), h->stream));
+        CK(wf_snow_transport_sweep(h->F, gl, sw, material, lc));
+        ++nl;
+    }
+    CK(wf_snow_in(h->F, gl, lc));
+    ++nl;
+    CK(split ? wf_split_vertical_soil(h->F, lc) : wf_fp64_vertical_soil(h->F, lc));
+    ++nl;
+    return WF_OK;
+}
+
 // Enqueue one model step on the handle's stream (with adaptive sub-steps the host waits for
 // the device after every sub-step, see below).
 int enqueue_step(WfHandle* h, int64_t* launches) {
@@ -1538,8 +1662,8 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         if (timing) cudaEventRecord(h->kev[i], h->stream);
     };
     mark(0);
-    CK(split ? wf_split_vertical(h->F, lc) : wf_fp64_vertical(h->F, lc));
-    ++nl;
+    int rcv = enqueue_vertical(h, lc, gl, nl);
+    if (rcv) return rcv;
     mark(1);
     auto sweep = [&](DevGraphAlloc& G, const WfDevGraph& g, const std::vector<double>& dts, double* d_dts,
                      int which) -> int {
@@ -1845,8 +1969,8 @@ int enqueue_step_static(WfHandle* h, unsigned char* base, int64_t* launches) {
     const bool split = h->cfg.form == WF_FORM_SPLIT;
     int64_t nl = 0;
     const WfDevGraph gl = static_graph(h->land, h->M, base), gr = static_graph(h->river, h->M, base);
-    CK(split ? wf_split_vertical(h->F, lc) : wf_fp64_vertical(h->F, lc));
-    ++nl;
+    int rcv = enqueue_vertical(h, lc, gl, nl);
+    if (rcv) return rcv;
     auto clear = [&](const DevGraphAlloc& G, const WfDevGraph& g, bool sentinel) -> int {
         const size_t slots = (size_t)G.plan.n_chains * h->M;
         CK(cudaMemsetAsync(g.ticket, 0, sizeof(unsigned long long), h->stream));

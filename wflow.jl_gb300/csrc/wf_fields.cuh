@@ -54,6 +54,14 @@
     X(RP_AREA) X(RP_MAXSTOR) X(RP_THRESHOLD) X(RP_RC_COEF) X(RP_RC_EXP) X(RP_MAXREL) X(RP_DEMAND)   \
     X(RP_TMIN) X(RP_TFULL)
 
+// Gravitational snow transport and the HBV glacier (FP64 in both forms; allocated only when the
+// model runs them): per-slot glacier parameters, and per element the glacier store and melt, the
+// snow moved in and out, and the terms the vertical kernel hands to the transport sweep and to
+// its soil part (the snow runoff, the interception rate, the two transport capacities).
+#define WF_G_FIELDS(X) X(G_FRAC) X(G_TTM) X(G_DDF) X(G_SIFRAC)
+#define WF_GM_FIELDS(X)                                                                            \
+    X(GM_STORE) X(GM_MELT) X(GM_SNOW_IN) X(GM_SNOW_OUT) X(GM_SRUNOFF) X(GM_IC) X(GM_CAP) X(GM_CAPW)
+
 #define WF_ENUM_ITEM(name) name,
 enum WfLandStatic { WF_L_FIELDS(WF_ENUM_ITEM) L_COUNT };
 enum WfLandMember { WF_M_FIELDS(WF_ENUM_ITEM) M_COUNT };
@@ -61,6 +69,8 @@ enum WfRiverStatic { WF_R_FIELDS(WF_ENUM_ITEM) R_COUNT };
 enum WfRiverMember { WF_RM_FIELDS(WF_ENUM_ITEM) RM_COUNT };
 enum WfReservoirMember { WF_RS_FIELDS(WF_ENUM_ITEM) RS_COUNT };
 enum WfReservoirStatic { WF_RP_FIELDS(WF_ENUM_ITEM) RP_COUNT };
+enum WfGlacierStatic { WF_G_FIELDS(WF_ENUM_ITEM) G_COUNT };
+enum WfSnowGlacierMember { WF_GM_FIELDS(WF_ENUM_ITEM) GM_COUNT };
 #undef WF_ENUM_ITEM
 
 // Layered fields: N arrays each.
@@ -145,6 +155,12 @@ struct WfDevFields {
     const int32_t* res_type;       // [n_res] WfReservoirOutflow
     const int64_t* res_land_slot;  // [n_res] land slot of the reservoir outlet cell
     const int32_t* res_of_rslot;   // [river slots] reservoir at a river slot, or -1
+    // gravitational snow transport and glacier (off: flags 0 and null pointers)
+    int32_t snow_transport;
+    int32_t glacier;
+    double g_max_rate;             // maximum snow-to-ice rate [m s-1]
+    double* G[G_COUNT];            // [land slots]
+    double* GM[GM_COUNT];          // [land slots * M]
 };
 
 // Routing graph on the device (one per land / river graph).
@@ -179,11 +195,24 @@ struct WfDevGraph {
     double* end_q;        // [n_chains * M * s_cap] q of each chain end per sub-step
     unsigned long long* ticket;  // work counter of the current launch
     int32_t s_cap;        // sub-steps per launch
+    // land graph with snow transport: for each slot's upstream entries up_ptr[slot] ..
+    // up_ptr[slot + 1], the entry indices in the order of the graph's topological sort (the
+    // order in which the transport hands material on)
+    const int32_t* snow_up;
 };
+
+// Work items per chunk of a wavefront launch with SL sub-step lanes per chain-member pair: a
+// chunk holds G chains x M members (M <= 32) or one chain x M members, 32 / SL pairs per item.
+__host__ __device__ __forceinline__ int64_t wf_items_per_chunk(int G, int M, int SL) {
+    const int64_t pairs = M <= 32 ? (int64_t)G * M : M;
+    const int64_t per_item = 32 / (SL > 1 ? SL : 1);
+    return (pairs + per_item - 1) / per_item;
+}
 
 // Sub-stepping of one routing sweep launch.
 struct WfSweep {
     int32_t S;            // sub-steps in this launch
+    int32_t SL;           // sub-step lanes of the diagonal schedule (a power of two; 0 or 1: one lane)
     int32_t first;        // index of the first sub-step within the model step
     int32_t last_of_step; // 1 when the launch ends the model step's sub-stepping
     int32_t total;        // total sub-steps of the model step

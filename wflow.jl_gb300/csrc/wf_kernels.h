@@ -11,6 +11,7 @@ struct WfLaunchCfg {
     int vertical_block;   // threads per block of per-cell kernels
     int walk_warps;       // warps per block of wavefront kernels
     int walk_blocks;      // blocks of the persistent wavefront grid (0 = occupancy)
+    int sub_lanes;        // cap of the sub-step lanes of the diagonal schedule (0 = default)
 };
 
 // FP64 plain form (kernels_fp64.cu)
@@ -20,9 +21,21 @@ cudaError_t wf_fp64_overland(const WfDevFields& F, const WfDevGraph& g, const Wf
 cudaError_t wf_fp64_river(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
 cudaError_t wf_fp64_balance(const WfDevFields& F, const WfLaunchCfg& c);
 cudaError_t wf_fp64_vwc(const WfDevFields& F, int layer, double* out, const WfLaunchCfg& c);
+// the per-cell update split at the gravitational snow transport: interception and snow, then
+// glacier, open water and soil
+cudaError_t wf_fp64_vertical_snow(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_fp64_vertical_soil(const WfDevFields& F, const WfLaunchCfg& c);
+
+// Gravitational snow transport, both forms (kernels_fp64.cu): one material's sweep over the land
+// graph (0 snow storage, 1 snow water; one sub-step of the model step) and the inflow per cell.
+cudaError_t wf_snow_transport_sweep(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, int material,
+                                    const WfLaunchCfg& c);
+cudaError_t wf_snow_in(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
 
 // FP32/FP64 split form (kernels_split.cu)
 cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_split_vertical_snow(const WfDevFields& F, const WfLaunchCfg& c);
+cudaError_t wf_split_vertical_soil(const WfDevFields& F, const WfLaunchCfg& c);
 cudaError_t wf_split_ssf(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
 cudaError_t wf_split_balance(const WfDevFields& F, const WfLaunchCfg& c);
 // slim wavefronts of the split form (wf_wave.cuh) and their per-cell completion kernels

@@ -44,7 +44,9 @@ struct WfConfig
     form::Int32
     n_members::Int32
     per_member_soil::Int32
-    reserved::NTuple{7, Int32}
+    snow_gravitational_transport::Int32
+    glacier::Int32
+    reserved::NTuple{5, Int32}
 end
 
 struct WfDomain
@@ -77,10 +79,12 @@ const PARAM_NAMES = (:canopy_gap_fraction, :maximum_canopy_storage, :crop_coeffi
     :theta_r, :kv_0, :f, :soil_thickness, :air_entry_pressure, :h1, :h2, :h3_high, :h3_low, :h4,
     :alpha_h1, :infiltration_capacity_compacted_soil, :compacted_soil_area_fraction,
     :wet_root_distribution_parameter, :cap_hmax, :cap_n, :maximum_leakage, :w_soil, :cf_soil, :z_exp,
-    :brooks_corey_exponent, :kv_factor, :horizontal_to_vertical_ratio)
+    :brooks_corey_exponent, :kv_factor, :horizontal_to_vertical_ratio, :glacier_fraction,
+    :glacier_temperature_threshold_melt, :glacier_degree_day_factor, :glacier_snow_to_ice_fraction,
+    :glacier_initial_store)
 
 struct WfParams
-    ptrs::NTuple{34, Ptr{Float64}}
+    ptrs::NTuple{39, Ptr{Float64}}
 end
 
 # reservoirs (WfReservoirs; ReservoirModel, Wflow/src/routing/surface/reservoir.jl)
@@ -103,6 +107,10 @@ end
 # WfField ids (enum WfField)
 const F_LAND = (:canopy_storage, :snow_storage, :snow_water, :soil_surface_temperature,
     :saturated_water_depth, :unsaturated_layer_depth, :ssf_q, :land_q, :land_h, :water_table_depth)
+const F_GLACIER_STORE = Int32(41)
+const F_GLACIER_MELT = Int32(42)
+const F_SNOW_IN = Int32(43)
+const F_SNOW_OUT = Int32(44)
 const F_RIVER_Q = Int32(100)
 const F_RIVER_H = Int32(101)
 const F_RIVER_Q_AVERAGE = Int32(103)
@@ -142,16 +150,17 @@ end
     check_supported(config)
 
 Throw when the model uses a component outside the GPU step (the caller then keeps the
-reference's own `update_model!`): model type other than `sbm`, glaciers, gravitational snow
-transport, water demand, floodplains, drains, local-inertial or staggered routing, Kv profiles
-other than exponential / exponential_constant, reservoirs with tabulated curves.
+reference's own `update_model!`): model type other than `sbm`, water demand, floodplains,
+drains, local-inertial or staggered routing, Kv profiles other than exponential /
+exponential_constant, reservoirs with tabulated curves, gravitational snow transport together
+with reservoirs. Glaciers and gravitational snow transport run on the GPU.
 """
 function check_supported(config)
     m = config.model
     bad = String[]
     m.type == Wflow.ModelType.sbm || push!(bad, "model type $(m.type)")
-    m.glacier__flag && push!(bad, "glacier__flag")
-    m.snow_gravitational_transport__flag && push!(bad, "snow_gravitational_transport__flag")
+    m.snow_gravitational_transport__flag && m.reservoir__flag &&
+        push!(bad, "snow_gravitational_transport__flag with reservoir__flag")
     Wflow.do_water_demand(config) && push!(bad, "water demand")
     m.floodplain_1d__flag && push!(bad, "floodplain_1d__flag")
     m.drain__flag && push!(bad, "drain__flag")
@@ -189,7 +198,8 @@ function GpuStep(model)
         config.model.land_kinematic_wave__time_step, config.model.river_kinematic_wave__time_step,
         config.model.subsurface_kinematic_wave__time_step,
         config.model.subsurface_kinematic_wave__alpha_coefficient, Int32(0), Int32(1), Int32(0),
-        ntuple(_ -> Int32(0), 7))
+        Int32(config.model.snow__flag && config.model.snow_gravitational_transport__flag),
+        Int32(config.model.snow__flag && config.model.glacier__flag), ntuple(_ -> Int32(0), 5))
     land_n = routing.overland_flow.parameters.mannings_n
     dom = WfDomain(length(ds_land), k(ds_land), k(lp.area), k(lp.flow_width), k(lp.flow_length),
         k(lp.surface_flow_width), k(lp.slope), k(lp.flow_fraction_to_river), k(lp.river_fraction),
@@ -224,7 +234,15 @@ function GpuStep(model)
         src[:temperature_threshold_melt] = sp.temperature_threshold_melt
         src[:water_holding_capacity] = sp.water_holding_capacity
     end
-    params = WfParams(ntuple(i -> haskey(src, PARAM_NAMES[i]) ? k(src[PARAM_NAMES[i]]) : Ptr{Float64}(0), 34))
+    if config.model.snow__flag && config.model.glacier__flag
+        gp = land.glacier.parameters
+        src[:glacier_fraction] = gp.glacier_fraction
+        src[:glacier_temperature_threshold_melt] = gp.temperature_threshold_melt
+        src[:glacier_degree_day_factor] = gp.degree_day_factor
+        src[:glacier_snow_to_ice_fraction] = gp.snow_to_ice_fraction
+        src[:glacier_initial_store] = land.glacier.variables.glacier_store
+    end
+    params = WfParams(ntuple(i -> haskey(src, PARAM_NAMES[i]) ? k(src[PARAM_NAMES[i]]) : Ptr{Float64}(0), 39))
     # reservoirs at their outlet river cells, in the reservoir model's order
     # (NetworkReservoir.river_indices, network.jl:333-350); the storage profile must be linear
     nres = 0
@@ -302,6 +320,20 @@ function sync_mirrors!(gpu::GpuStep, model)
     get_field!(routing.overland_flow.variables.h, gpu, 8)
     get_field!(routing.subsurface_flow.variables.q, gpu, 6)
     get_field!(model.land.soil.variables.saturated_water_depth, gpu, 4)
+    (; config) = model
+    if config.model.snow__flag
+        sv = model.land.snow.variables
+        get_field!(sv.snow_storage, gpu, 1)
+        get_field!(sv.snow_water, gpu, 2)
+        if config.model.snow_gravitational_transport__flag
+            get_field!(sv.snow_in, gpu, F_SNOW_IN)
+            get_field!(sv.snow_out, gpu, F_SNOW_OUT)
+        end
+        if config.model.glacier__flag
+            get_field!(model.land.glacier.variables.glacier_store, gpu, F_GLACIER_STORE)
+            get_field!(model.land.glacier.variables.glacier_melt, gpu, F_GLACIER_MELT)
+        end
+    end
     if gpu.n_reservoirs > 0
         rv = routing.river_flow.boundary_conditions.reservoir.variables
         get_field!(rv.storage, gpu, F_RESERVOIR_STORAGE)

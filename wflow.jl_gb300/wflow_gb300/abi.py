@@ -55,7 +55,9 @@ class WfConfig(C.Structure):
         ("form", _i32),
         ("n_members", _i32),
         ("per_member_soil", _i32),
-        ("reserved", _i32 * 7),
+        ("snow_gravitational_transport", _i32),
+        ("glacier", _i32),
+        ("reserved", _i32 * 5),
     ]
 
 
@@ -83,6 +85,8 @@ PARAM_FIELDS = [
     "infiltration_capacity_compacted_soil", "compacted_soil_area_fraction",
     "wet_root_distribution_parameter", "cap_hmax", "cap_n", "maximum_leakage", "w_soil", "cf_soil",
     "z_exp", "brooks_corey_exponent", "kv_factor", "horizontal_to_vertical_ratio",
+    "glacier_fraction", "glacier_temperature_threshold_melt", "glacier_degree_day_factor",
+    "glacier_snow_to_ice_fraction", "glacier_initial_store",
 ]
 
 
@@ -130,7 +134,7 @@ _LAND_FIELDS = [
     "LAND_STORAGE", "LAND_TO_RIVER_AVERAGE", "LAND_INWATER", "TOTAL_STORAGE", "BALANCE_LAND_ERROR",
     "BALANCE_LAND_RELATIVE_ERROR", "BALANCE_OVERLAND_ERROR", "BALANCE_OVERLAND_RELATIVE_ERROR",
     "BALANCE_SUBSURFACE_ERROR", "BALANCE_SUBSURFACE_RELATIVE_ERROR", "VOLUMETRIC_WATER_CONTENT",
-    "LAND_QIN_AVERAGE",
+    "LAND_QIN_AVERAGE", "GLACIER_STORE", "GLACIER_MELT", "SNOW_IN", "SNOW_OUT",
 ]
 _RIVER_FIELDS = ["RIVER_Q", "RIVER_H", "RIVER_STORAGE", "RIVER_Q_AVERAGE", "RIVER_QIN_AVERAGE",
                  "RIVER_INWATER", "BALANCE_RIVER_ERROR", "BALANCE_RIVER_RELATIVE_ERROR"]

@@ -37,6 +37,7 @@ def _lib():
             "wf_li_river_stable_timestep": (i32, [P, pd]),
             "wf_li_river_substep": (i32, [P, d]),
             "wf_li_river_step": (i32, [P, d, pl]),
+            "wf_li_river_set_host_loop": (i32, [P, i32]),
             "wf_li_river_get": (i32, [P, i32, pd]),
             "wf_li_domain_create": (i32, [C.POINTER(WfLiLandGrid), C.POINTER(WfLiRiverNetwork), pd, i32,
                                           C.POINTER(P)]),
@@ -47,6 +48,7 @@ def _lib():
             "wf_li_domain_stable_timestep": (i32, [P, pd]),
             "wf_li_domain_substep": (i32, [P, d]),
             "wf_li_domain_step": (i32, [P, d, pl]),
+            "wf_li_domain_set_host_loop": (i32, [P, i32]),
             "wf_li_domain_get": (i32, [P, i32, pd]),
         }
         for name, (res, args) in sig.items():
@@ -211,9 +213,15 @@ class LiRiver:
         self._check(self.lib.wf_li_river_substep(self.h, float(dt_s)), "wf_li_river_substep")
 
     def step(self, dt):
+        """update_river_flow_model! over dt: the sub-step loop on the device (one cooperative
+        launch); returns the number of sub-steps."""
         k = C.c_int64()
         self._check(self.lib.wf_li_river_step(self.h, float(dt), C.byref(k)), "wf_li_river_step")
         return k.value
+
+    def set_host_loop(self, on=True):
+        """Drive the sub-steps of step() from the host instead (the same results)."""
+        self._check(self.lib.wf_li_river_set_host_loop(self.h, int(bool(on))), "wf_li_river_set_host_loop")
 
     def get(self, field):
         f = self.FIELDS[field]
@@ -289,9 +297,15 @@ class LiDomain:
         self._check(self.lib.wf_li_domain_substep(self.h, float(dt_s)), "wf_li_domain_substep")
 
     def step(self, dt):
+        """update_overland_flow_model! over dt: the sub-step loop on the device; returns the
+        number of sub-steps."""
         k = C.c_int64()
         self._check(self.lib.wf_li_domain_step(self.h, float(dt), C.byref(k)), "wf_li_domain_step")
         return k.value
+
+    def set_host_loop(self, on=True):
+        """Drive the sub-steps of step() from the host instead (the same results)."""
+        self._check(self.lib.wf_li_domain_set_host_loop(self.h, int(bool(on))), "wf_li_domain_set_host_loop")
 
     def get(self, field):
         f = self.FIELDS[field]

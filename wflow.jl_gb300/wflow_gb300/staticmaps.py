@@ -68,10 +68,19 @@ PARAMS = {
                                      1.0, None, False),
     "z_exp": ("soil_exponential_vertical_saturated_hydraulic_conductivity_profile_below_surface__depth", MM, None,
               False),
+    # HBV glacier (glacier.jl:58-98, standard_name_sbm.jl:70-108)
+    "glacier_fraction": ("glacier_surface__area_fraction", 1.0, 0.0, False),
+    "glacier_temperature_threshold_melt": ("glacier_ice__melting_temperature_threshold", None, 0.0, False),
+    "glacier_degree_day_factor": ("glacier_ice__degree_day_coefficient", MM_D, 3.0, False),
+    "glacier_snow_to_ice_fraction": ("glacier_firn_accumulation__snowpack_dry_snow_leq_depth_fraction",
+                                     1.0 / 86400.0, 0.001, False),
+    "glacier_initial_store": ("glacier_ice__initial_leq_depth", MM, 5500.0, False),
 }
 # read only when present: the snow parameters all have defaults; z_exp only serves the
-# exponential_constant Kv profile
-OPTIONAL_PARAMS = {"z_exp"}
+# exponential_constant Kv profile; the glacier parameters only the glacier model (the library
+# applies the reference's defaults to the ones not given)
+OPTIONAL_PARAMS = {"z_exp", "glacier_fraction", "glacier_temperature_threshold_melt", "glacier_degree_day_factor",
+                   "glacier_snow_to_ice_fraction", "glacier_initial_store"}
 
 # PCRaster local drain direction -> (dx, dy) on the standardised grid (utils.jl:3-13)
 PCR_DX = np.array([0, -1, 0, 1, -1, 0, 1, -1, 0, 1])
