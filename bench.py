@@ -12,7 +12,8 @@ outlet-discharge and closure errors against it (`accuracy`).
 
 `value` times K steps with the step's forcing already resident in HBM (CUDA events on the
 library's stream). `e2e` times the same K steps through the public C ABI with host forcing
-from pinned memory copied in (wf_set_forcing_async: the copy of step k+1 overlaps step k) and
+from pinned memory copied in (wf_set_forcing_async, FP32 arrays for the split form: the copy
+of step k+1 overlaps step k) and
 the outlet discharge copied out every step. Other workloads: `--workload
 large_4096_adaptive_hourly` (4096 x 4096 at 100 m, Courant sub-steps, rain x3) and
 `--workload ragged200_daily` (200 independent catchments of 10^3 - 10^6 cells), and
@@ -257,15 +258,19 @@ def run_gpu(args):
     value, job_s = whole_job_rate(elapsed_ms / 1e3, cells, K, device=dev)
     elapsed_ms = job_s * 1e3
     # ---- end to end through the public API: pinned host forcing in, outlet discharge out
+    # the split form computes with FP32 forcing, so it is handed FP32 arrays (wf_set_forcing_f32,
+    # half the bytes to copy, the same state); the FP64 form takes FP64 arrays
+    f32 = form == abi.WF_FORM_SPLIT
+    fdt = np.float32 if f32 else np.float64
     host = []
     for s in range(W, W + K):
         P, PET, T = member_forcing(s, dt, n, members, pfac, seed=args.seed)
-        pin = [torch.from_numpy(x).pin_memory() for x in (P, PET, T)]
+        pin = [torch.from_numpy(np.ascontiguousarray(x, dtype=fdt)).pin_memory() for x in (P, PET, T)]
         host.append(pin)
     # The first device access to a freshly pinned host buffer maps its pages (about 30 GB/s
     # instead of 200 GB/s on this host); a model run reads its forcing into the same buffers
     # every step, so each buffer is touched once before the timed region.
-    scratch = torch.empty(n * members, dtype=torch.float64, device=dev)
+    scratch = torch.empty(n * members, dtype=torch.float32 if f32 else torch.float64, device=dev)
     for pin in host:
         for x in pin:
             scratch[: x.numel()].copy_(x, non_blocking=True)
@@ -278,10 +283,13 @@ def run_gpu(args):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    set_async = lib.wf_set_forcing_async_f32 if f32 else lib.wf_set_forcing_async
+    ptr_t = abi._pf if f32 else abi._pd
+
     def set_forcing_async(s):
         P, PET, T = host[s]
-        st = lib.wf_set_forcing_async(model.h, C.cast(P.data_ptr(), abi._pd), C.cast(PET.data_ptr(), abi._pd),
-                                      C.cast(T.data_ptr(), abi._pd), P.numel())
+        st = set_async(model.h, C.cast(P.data_ptr(), ptr_t), C.cast(PET.data_ptr(), ptr_t),
+                       C.cast(T.data_ptr(), ptr_t), P.numel())
         if st:
             raise RuntimeError(f"wf_set_forcing_async failed {st}")
 
@@ -331,8 +339,9 @@ def run_gpu(args):
                    "chains_land": mt["n_chains_land"], "max_chain_land": mt["max_chain_land"],
                    "max_chain_river": mt["max_chain_river"], "parallelism": f"replicas{ws}",
                    "tuning": tuning},
-        "e2e": {"value": e2e_value, "unit": "cell-timesteps/s", "h2d_bytes_per_step": 3 * 8 * cells,
-                "d2h_bytes_per_step": 8 * n_out},
+        "e2e": {"value": e2e_value, "unit": "cell-timesteps/s",
+                "h2d_bytes_per_step": 3 * np.dtype(fdt).itemsize * cells, "d2h_bytes_per_step": 8 * n_out,
+                "forcing_dtype": np.dtype(fdt).name},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": kt,
         "clocks": clk,

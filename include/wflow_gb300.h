@@ -335,6 +335,13 @@ int32_t wf_set_forcing(WfHandle* h, const double* precipitation, const double* p
  * pipelined. */
 int32_t wf_set_forcing_async(WfHandle* h, const double* precipitation, const double* potential_evaporation,
                              const double* temperature, int64_t count);
+/* The same from FP32 arrays (forcing files usually hold FP32), half the bytes to copy: the split
+ * form keeps its forcing in FP32 anyway; the FP64 form widens the values exactly. No counterpart
+ * in the reference (Wflow converts forcing to Float64 on reading, io.jl:108-160). */
+int32_t wf_set_forcing_f32(WfHandle* h, const float* precipitation, const float* potential_evaporation,
+                           const float* temperature, int64_t count);
+int32_t wf_set_forcing_async_f32(WfHandle* h, const float* precipitation, const float* potential_evaporation,
+                                 const float* temperature, int64_t count);
 /* Same from device pointers already in the library's slot order (see wf_get_slot_order). */
 int32_t wf_set_forcing_device_slots(WfHandle* h, const void* precipitation,
                                     const void* potential_evaporation, const void* temperature);
@@ -403,6 +410,11 @@ int32_t wf_get_stream(WfHandle* h, void** stream);
 int32_t wf_get_kernel_times(WfHandle* h, double* ms5, int64_t* calls);
 
 /* Number of land cells, river cells, river pits and layer count of a handle. */
+/* Adaptive sub-steps (a diagnostic with no counterpart in the reference): for every member the
+ * sum of the squared sizes of the sub-steps that the last model step took in sweep `kind`
+ * (0 subsurface, 1 overland, 2 river) [s2]; members whose sequences of sub-steps differ show
+ * different sums. */
+int32_t wf_get_substep_signature(WfHandle* h, int32_t kind, double* sig, int32_t n_members);
 int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_outlets,
                      int32_t* n_layers, int32_t* n_members);
 /* Number of reservoirs of a handle. */

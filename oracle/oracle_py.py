@@ -51,6 +51,8 @@ def lib():
         L.orc_model_set.argtypes = [C.c_void_p, _i32, _i32, _pd]
         L.orc_model_outlets.argtypes = [C.c_void_p, _i32, _pd, C.POINTER(_i64)]
         L.orc_model_substeps.argtypes = [C.c_void_p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]
+        L.orc_model_substep_signature.restype = _i32
+        L.orc_model_substep_signature.argtypes = [C.c_void_p, _i32, _pd]
         L.orc_topo_order_dfs.restype = _i32
         L.orc_topo_order_dfs.argtypes = [_i64, C.POINTER(_i32), C.POINTER(_i64)]
         for name in ["orc_head_brooks_corey", "orc_vwc_brooks_corey", "orc_feddes_h3", "orc_rwu_reduction_feddes",
@@ -202,6 +204,14 @@ class OracleModel:
         n = C.c_int64()
         lib().orc_model_outlets(self.h, which, out.ctypes.data_as(_pd), C.byref(n))
         return out[: n.value].copy()
+
+    def substep_signature(self, kind):
+        """Per member, the sum of the squared sub-step sizes of the last step (0 subsurface, 1 land,
+        2 river)."""
+        out = np.empty(self.M)
+        if lib().orc_model_substep_signature(self.h, int(kind), out.ctypes.data_as(_pd)) != 0:
+            raise RuntimeError("no sub-step signature")
+        return out
 
     def substeps(self):
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()

@@ -1031,6 +1031,7 @@ struct OrcModel {
     std::vector<int32_t> res_land;      // [nres] land cell of the reservoir outlet
     std::vector<double> res_out_avg, res_in_avg, res_evap_avg, res_abs_avg, res_prev, res_err, res_rel;
     int64_t last_sub_land = 0, last_sub_river = 0, last_sub_ssf = 0;
+    std::vector<double> sig[3];  // per member: sum of the squared sub-step sizes (subsurface, land, river)
     std::vector<double> buf;
 };
 
@@ -1451,6 +1452,10 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
     const int64_t n = m->n, nr = m->nr;
     const int64_t o = (int64_t)mbr * n, orr = (int64_t)mbr * nr;
     OrcSoil* soil = m->soil.data() + o;
+    for (auto& v : m->sig) {
+        if ((int)v.size() != m->M) v.assign(m->M, 0.0);
+        v[mbr] = 0.0;
+    }
     // ---- storage_prev! (mass_balance.jl:170-183)
     if (c.water_mass_balance) {
         for (int64_t i = 0; i < n; ++i) {
@@ -1574,6 +1579,7 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
                 dt_s = c.subsurface_dt_fixed;
             }
             dt_s = check_timestepsize(dt_s, t, dt);
+            m->sig[0][mbr] += dt_s * dt_s;  // sub-step signature (a diagnostic)
             // update_fluxes! -> recharge flux! (boundary_conditions.jl:219-236, check_flux :12-21)
             for (int64_t i = 0; i < n; ++i) {
                 int64_t j = o + i;
@@ -1642,6 +1648,7 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
                                                                         m->flow_length.data(), n, 0.02, m->buf)
                                               : c.land_dt_fixed;
             dt_s = check_timestepsize(dt_s, t, dt);
+            m->sig[1][mbr] += dt_s * dt_s;  // sub-step signature (a diagnostic)
             // kinwave_land_update! (surface_kinwave.jl:293-341)
             for (int64_t i = 0; i < n; ++i) m->ol_qin[o + i] = 0.0;
             for (int64_t v : m->topo) {
@@ -1704,6 +1711,7 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
                                                                         m->r_length.data(), nr, 0.05, m->buf)
                                               : c.river_dt_fixed;
             dt_s = check_timestepsize(dt_s, t, dt);
+            m->sig[2][mbr] += dt_s * dt_s;  // sub-step signature (a diagnostic)
             // kinwave_river_update! (surface_kinwave.jl:492-566)
             for (int64_t r = 0; r < nr; ++r) m->rv_qin[orr + r] = 0.0;
             for (int64_t v : m->r_topo) {
@@ -2228,6 +2236,14 @@ extern "C" {
 int32_t orc_model_step(OrcModel* m, int32_t n_threads) {
     if (n_threads < 1) n_threads = 1;
     for (int mbr = 0; mbr < m->M; ++mbr) member_step(m, mbr, n_threads);
+    return WF_OK;
+}
+
+// Sum of the squared sub-step sizes of the last model step per member (kind 0 subsurface,
+// 1 land, 2 river): the same diagnostic as wf_get_substep_signature.
+int32_t orc_model_substep_signature(OrcModel* m, int32_t kind, double* out) {
+    if (kind < 0 || kind > 2 || (int)m->sig[kind].size() != m->M) return WF_ERR_INVALID;
+    for (int k = 0; k < m->M; ++k) out[k] = m->sig[kind][k];
     return WF_OK;
 }
 

@@ -201,6 +201,9 @@ double orc_li_domain_stable_timestep(const WfLiLandGrid* land, const WfLiRiverNe
 /* full model */
 typedef struct OrcModel OrcModel;
 int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p, OrcModel** out);
+/* Per member, the sum of the squared sub-step sizes of the last model step (kind 0 subsurface,
+ * 1 land, 2 river). */
+int32_t orc_model_substep_signature(OrcModel* m, int32_t kind, double* out);
 /* the same with reservoirs (reservoir outlets cut the land and river upstream lists) */
 int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p,
                                          const WfReservoirs* rs, OrcModel** out);

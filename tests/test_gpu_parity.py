@@ -307,3 +307,19 @@ def test_six_soil_layers_and_constant_kv_both_forms(gpu_lib):
     assert w["outlet_q"] <= 1e-4, w
     assert w["soil_storage"] <= 1e-4, w
     assert w["closure"] <= 1e-7, w
+
+
+def test_fp32_forcing_matches_fp64_forcing(gpu_lib):
+    # wf_set_forcing_f32 / wf_set_forcing_async_f32: the split form computes with FP32 forcing, so
+    # FP32 arrays give the same state as FP64 ones; the FP64 form widens them exactly
+    dom = synthetic.make_domain(32, 1000.0, seed=23)
+    for form in (abi.WF_FORM_SPLIT, abi.WF_FORM_FP64):
+        cfg = synthetic.make_config(86400.0, form=form)
+        a, b = Model(cfg, dom), Model(cfg, dom)
+        for s in range(4):
+            P, PET, T = (x.astype(np.float32).astype(np.float64) for x in synthetic.forcing(s, cfg.dt, dom.n_land, seed=23))
+            a.run_timestep(P, PET, T)
+            b.set_forcing_f32(P, PET, T, asynchronous=s % 2 == 1)
+            b.update_model()
+        for f in ["SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE", "SATURATED_WATER_DEPTH", "SNOW_STORAGE"]:
+            assert np.array_equal(a.get_value(f), b.get_value(f)), (form, f)

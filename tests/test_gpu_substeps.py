@@ -95,13 +95,15 @@ def test_adaptive_split_accuracy(gpu_lib):
 
 # The reference's Courant quantile counts every cell with Q > 1e-30 (surface_kinwave.jl:687), so
 # its rank, and with it the sub-step, moves with the number of cells holding a tiny flow. A
-# river cell that evaporation drains within a step ends at 1e-22 m3/s or at the 1e-30 floor
-# depending on the sign of a cancellation (storage minus evaporation) that the FP32 fluxes of
-# the split form resolve to 1e-7 of the terms only. The split form reproduces the floor and the
-# Newton early stop of the reference (kw_node_ff) but not that rounding, so now and then a
-# member's sub-step differs from the FP64 form's while the sub-step counts agree; that, not the
-# arithmetic, bounds the agreement of an adaptive hourly ensemble (measured: 1e-3 to 4e-3). The
-# daily single-member case above holds the benchmark's 1e-4.
+# river cell that evaporation drains within a step ends at a tiny flow or at the 1e-30 floor
+# depending on the sign of a cancellation (its storage minus its evaporation) that the reference
+# itself decides at the level of FP64 rounding. The split form reproduces the floor and the
+# Newton early stop of the reference (kw_node_ff) but cannot reproduce that rounding, so now and
+# then a member takes a different sequence of sub-steps than the oracle. The test identifies
+# those members from the sub-step signature (the sum of the squared sub-step sizes of every
+# step, wf_get_substep_signature, against the oracle's) and holds every member whose sub-steps
+# matched to the benchmark's 1e-4 on outlet discharge; the others are reported and bounded at
+# 1e-2 (their discharge follows a different but equally valid time discretisation).
 @pytest.mark.parametrize("rain", [1.0, 3.0])
 def test_adaptive_split_ensemble_accuracy(gpu_lib, rain):
     dom = synthetic.make_domain(32, 250.0, seed=14)
@@ -110,11 +112,38 @@ def test_adaptive_split_ensemble_accuracy(gpu_lib, rain):
     params = dict(dom.params, kv_0=kv0, f=f)
     cfg = synthetic.make_config(3600.0, n_members=M, form=abi.WF_FORM_SPLIT, adaptive=True, per_member_soil=True)
     cfg.subsurface_alpha = 1e-3
-    w = split_errors(dom, cfg, 12, params=params, precip_scale=pfac * rain)
-    print(f"split adaptive hourly ensemble errors (rain x{rain})", w)
-    assert w["outlet_q"] <= 1e-2, w
-    assert w["soil_storage"] <= 1e-4, w
-    assert w["closure"] <= 1e-7, w
+    cfg64 = copy.copy(cfg)
+    cfg64.form = abi.WF_FORM_FP64
+    gpu = Model(cfg, dom, params=params)
+    orc = O.OracleModel(cfg64, dom, params=params)
+    n_out = len(dom.outlets)
+    matched = np.ones(M, bool)
+    err = np.zeros(M)
+    soil = closure = 0.0
+    for s in range(12):
+        P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=1)
+        P = np.concatenate([P * (pfac[m] * rain) for m in range(M)])
+        PET, T = np.tile(PET, M), np.tile(T, M)
+        gpu.run_timestep(P, PET, T)
+        orc.set_forcing(P, PET, T)
+        orc.step()
+        for kind in (1, 2):
+            sg, so = gpu.substep_signature(kind), orc.substep_signature(kind)
+            matched &= np.abs(sg - so) <= 1e-6 * so
+        qo, qg = orc.outlets(0).reshape(M, n_out), gpu.outlets(0).reshape(M, n_out)
+        err = np.maximum(err, np.max(np.abs(qg - qo) / np.maximum(np.abs(qo), 1e-12), axis=1))
+        so_, sg_ = orc.get(abi.FIELD["TOTAL_SOIL_WATER_STORAGE"]), gpu.get_value("TOTAL_SOIL_WATER_STORAGE")
+        soil = max(soil, float(np.max(np.abs(sg_ - so_) / so_)))
+        rel = np.abs(gpu.get_value("BALANCE_LAND_RELATIVE_ERROR"))
+        closure = max(closure, float(rel.max()))
+    print(f"split adaptive hourly ensemble (rain x{rain}): members with the oracle's sub-steps "
+          f"{int(matched.sum())}/{M}, their outlet error {err[matched].max() if matched.any() else 0.0:.2e}; "
+          f"other members {err[~matched].round(6).tolist()}; soil {soil:.2e}; closure {closure:.2e}")
+    assert matched.sum() >= M // 2, matched
+    assert err[matched].max() <= 1e-4, err[matched]
+    assert err.max() <= 1e-2, err
+    assert soil <= 1e-4
+    assert closure <= 1e-7
 
 
 def fixed_short_substeps(cfg):

@@ -307,6 +307,7 @@ __global__ void substep_kernel(WfAdaptive A) {
             A.dt_hi[m] = hi;
             A.dt_lo[m] = (float)(ts - (double)hi);
             A.nsub[m] += 1;
+            A.sig[m] += ts * ts;
         }
         A.flags[m] = fl;
         if (A.kind == WF_ADAPT_SSF) {

@@ -321,6 +321,7 @@ int alloc_adaptive(WfHandle* h) {
         if ((rc = dalloc(h, &A.dt_lo, (size_t)M))) return rc;
         if ((rc = dalloc(h, &A.flags, (size_t)M))) return rc;
         if ((rc = dalloc(h, &A.nsub, (size_t)M))) return rc;
+        if ((rc = dalloc(h, &A.sig, (size_t)M))) return rc;
         if ((rc = dalloc(h, &A.more, 1))) return rc;
         CK(cudaMemset(A.hist, 0, (size_t)2 * M * 256 * sizeof(uint32_t)));
         CK(cudaMemset(A.count, 0, (size_t)M * sizeof(long long)));
@@ -401,6 +402,21 @@ __global__ void outlets_ff_kernel(const float* hi, const float* lo, const int64_
 __global__ void to_f32_kernel(const double* src, float* dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = (float)src[i];
+}
+// FP32 forcing of n_ext cells per member (member-major, or one set for every member when
+// `broadcast`) into the slot order: FP32 destination (split form) or FP64 (FP64 form).
+__global__ void gather_from_f32_kernel(const float* src, float* dst32, double* dst64, const int64_t* node_of_slot,
+                                       int64_t slots, int M, int64_t n_ext, int broadcast) {
+    const int64_t E = slots * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / M;
+        const int m = (int)(e - s * M);
+        const int64_t node = node_of_slot[s];
+        if (node < 0) continue;
+        const float x = src[(broadcast ? 0 : (int64_t)m * n_ext) + node];
+        if (dst32) dst32[e] = x;
+        else dst64[e] = (double)x;
+    }
 }
 __global__ void broadcast_member_f32_kernel(const double* src, float* dst, const int64_t* node_of_slot, int64_t slots,
                                             int M) {
@@ -1296,9 +1312,63 @@ int enqueue_forcing_gathers(WfHandle* h, double* const stg_of[3], int64_t count)
     return WF_OK;
 }
 
+// The gathers of FP32 forcing staged at stg[k] (count values each).
+int enqueue_forcing_gathers_f32(WfHandle* h, float* const stg[3], int64_t count) {
+    const int dst[3] = {PRECIP, POTEVAP, TEMP};
+    const int g = grid_of(h->F.land_slots * h->M, 256);
+    const int broadcast = count != h->n * h->M;
+    for (int k = 0; k < 3; ++k) {
+        gather_from_f32_kernel<<<g, 256, 0, h->stream>>>(stg[k], h->F.split ? h->F.Mh[dst[k]] : nullptr,
+                                                         h->F.split ? nullptr : h->F.Mf[dst[k]],
+                                                         h->F.land_node_of_slot, h->F.land_slots, h->M, h->n,
+                                                         broadcast);
+        CK(cudaGetLastError());
+    }
+    return WF_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int32_t wf_set_forcing_f32(WfHandle* h, const float* P, const float* PET, const float* T, int64_t count) {
+    if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
+    const int64_t full = h->n * h->M;
+    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
+    const float* src[3] = {P, PET, T};
+    float* stg[3];
+    for (int k = 0; k < 3; ++k) {
+        stg[k] = reinterpret_cast<float*>(h->staging + (size_t)k * std::max(h->n, h->nr) * h->M);
+        CK(cudaMemcpyAsync(stg[k], src[k], count * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    }
+    return enqueue_forcing_gathers_f32(h, stg, count);
+}
+
+int32_t wf_set_forcing_async_f32(WfHandle* h, const float* P, const float* PET, const float* T, int64_t count) {
+    if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
+    const int64_t full = h->n * h->M;
+    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
+    if (!h->copy_stream) {  // first call: copy stream, events and a staging buffer of its own
+        CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_fcopied, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_fconsumed, cudaEventDisableTiming));
+        int rc = dalloc(h, &h->fstage, (size_t)3 * full);
+        if (rc) return rc;
+    }
+    CK(cudaStreamWaitEvent(h->copy_stream, h->ev_fconsumed, 0));
+    const float* src[3] = {P, PET, T};
+    float* stg[3];
+    for (int k = 0; k < 3; ++k) {
+        stg[k] = reinterpret_cast<float*>(h->fstage + (size_t)k * full);
+        CK(cudaMemcpyAsync(stg[k], src[k], count * sizeof(float), cudaMemcpyHostToDevice, h->copy_stream));
+    }
+    CK(cudaEventRecord(h->ev_fcopied, h->copy_stream));
+    CK(cudaStreamWaitEvent(h->stream, h->ev_fcopied, 0));
+    int rc = enqueue_forcing_gathers_f32(h, stg, count);
+    if (rc) return rc;
+    CK(cudaEventRecord(h->ev_fconsumed, h->stream));
+    return WF_OK;
+}
 
 int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const double* T, int64_t count) {
     if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
@@ -1603,6 +1673,14 @@ int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_
     return WF_OK;
 }
 
+int32_t wf_get_substep_signature(WfHandle* h, int32_t kind, double* sig, int32_t n_members) {
+    if (!h || !sig || kind < 0 || kind > 2 || n_members != h->M) return set_err(h, WF_ERR_INVALID, "invalid argument");
+    if (!h->adaptive) return set_err(h, WF_ERR_INVALID, "the model takes fixed sub-steps");
+    CK(cudaMemcpyAsync(sig, h->ad[kind].sig, (size_t)h->M * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return WF_OK;
+}
+
 int32_t wf_get_reservoir_count(WfHandle* h, int64_t* n_reservoirs) {
     if (!h || !n_reservoirs) return WF_ERR_INVALID;
     *n_reservoirs = h->nres;
@@ -1730,6 +1808,7 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         WfAdaptive& A = h->ad[kind];
         CK(cudaMemsetAsync(A.t, 0, (size_t)h->M * sizeof(double), h->stream));
         CK(cudaMemsetAsync(A.nsub, 0, (size_t)h->M * sizeof(int32_t), h->stream));
+        CK(cudaMemsetAsync(A.sig, 0, (size_t)h->M * sizeof(double), h->stream));
         const bool slim = split && kind != WF_ADAPT_SSF;
         int64_t it = 0;
         while (true) {

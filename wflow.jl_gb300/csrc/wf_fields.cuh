@@ -279,6 +279,7 @@ struct WfAdaptive {
     float* dt_lo;
     uint8_t* flags;         // [M] WF_SUB_* bits of the current sub-step
     int32_t* nsub;          // [M] sub-steps taken in this model step
+    double* sig;            // [M] sum of the squared sub-step sizes of this model step (a diagnostic)
     int32_t* more;          // 1 when some member has not reached the end of the step
 };
 

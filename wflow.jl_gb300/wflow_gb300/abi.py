@@ -36,6 +36,7 @@ WF_KV_EXPONENTIAL_CONSTANT = 1
 
 _i32, _i64, _dbl = C.c_int32, C.c_int64, C.c_double
 _pd, _pi32 = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+_pf = C.POINTER(C.c_float)
 
 
 class WfConfig(C.Structure):
@@ -211,6 +212,8 @@ def _declare(lib):
         "wf_last_error": (C.c_char_p, [H]),
         "wf_set_forcing": (_i32, [H, _pd, _pd, _pd, _i64]),
         "wf_set_forcing_async": (_i32, [H, _pd, _pd, _pd, _i64]),
+        "wf_set_forcing_f32": (_i32, [H, _pf, _pf, _pf, _i64]),
+        "wf_set_forcing_async_f32": (_i32, [H, _pf, _pf, _pf, _i64]),
         "wf_set_forcing_device_slots": (_i32, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
         "wf_step": (_i32, [H]),
         "wf_step_async": (_i32, [H]),
@@ -239,6 +242,7 @@ def _declare(lib):
         "wf_create_with_reservoirs": (_i32, [C.POINTER(WfConfig), C.POINTER(WfDomain), C.POINTER(WfParams),
                                              C.POINTER(WfReservoirs), _i32, C.POINTER(H)]),
         "wf_get_reservoir_count": (_i32, [H, C.POINTER(_i64)]),
+        "wf_get_substep_signature": (_i32, [H, _i32, _pd, _i32]),
     }
     for name, (res, args) in extra.items():
         if hasattr(lib, name):

@@ -75,6 +75,15 @@ class Model:
         self._check(self.lib.wf_set_forcing_async(self.h, *[abi.as_ptr(a) for a in arrs], arrs[0].size),
                     "wf_set_forcing_async")
 
+    def set_forcing_f32(self, precipitation, potential_evaporation, temperature, asynchronous=False):
+        """wf_set_forcing_f32 / wf_set_forcing_async_f32: the forcing as FP32 arrays (half the bytes
+        to copy; the split form computes with FP32 forcing anyway)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (precipitation, potential_evaporation, temperature)]
+        if asynchronous:
+            self._pending_forcing = arrs
+        f = self.lib.wf_set_forcing_async_f32 if asynchronous else self.lib.wf_set_forcing_f32
+        self._check(f(self.h, *[abi.as_ptr(a, C.c_float) for a in arrs], arrs[0].size), "wf_set_forcing_f32")
+
     def update_model(self):
         self._check(self.lib.wf_step(self.h), "wf_step")
 
@@ -119,6 +128,14 @@ class Model:
         out = np.empty(max(1, no.value * self.M))
         self._check(self.lib.wf_get_outlets(self.h, which, abi.as_ptr(out), out.size, C.byref(n_out)), "wf_get_outlets")
         return out[: n_out.value].copy()
+
+    def substep_signature(self, kind):
+        """Adaptive sub-steps: per member, the sum of the squared sub-step sizes of the last step
+        in sweep `kind` (0 subsurface, 1 overland, 2 river)."""
+        out = np.empty(self.M)
+        self._check(self.lib.wf_get_substep_signature(self.h, int(kind), abi.as_ptr(out), self.M),
+                    "wf_get_substep_signature")
+        return out
 
     def save_state(self):
         size = C.c_size_t(0)
