@@ -596,6 +596,20 @@ def cpu_baseline(args, steps=None):
                       f"after 1 warm-up step), {el:.1f} s"}
 
 
+def probe_julia():
+    """Whether the reference's own runtime is on this host: `julia --version` on the PATH."""
+    import shutil
+
+    exe = shutil.which("julia")
+    if exe is None:
+        return "julia not found on PATH"
+    try:
+        out = subprocess.run([exe, "--version"], capture_output=True, text=True, timeout=60)
+        return f"{exe}: {(out.stdout or out.stderr).strip()} (exit {out.returncode})"
+    except Exception as e:  # a broken install counts as absent
+        return f"{exe}: {type(e).__name__}: {e}"
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -619,8 +633,9 @@ def run_reference(args):
                    "form": "fp64 (the reference's arithmetic)"},
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": "cell-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "Julia (the reference's own runtime) is not installed on this host; the reference arm is the "
-                "C++ restatement of Wflow.jl's algorithm (oracle/) on all host threads",
+        "julia_probe": probe_julia(),
+        "note": "the reference arm is the C++ restatement of Wflow.jl's algorithm (oracle/) on all host "
+                "threads: Wflow.jl needs Julia and its package depot, which this host lacks (julia_probe)",
     }
     print(json.dumps(result), flush=True)
 

@@ -515,6 +515,8 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
     }
     cp_async_commit();
     for (int buf = 0; e < E; e += stride, buf ^= 1) {
+        // every lane is done reading the warp buffer about to be refilled (the previous element's)
+        if (WS) __syncwarp();
         // stage the next element while this one computes
         if (e + stride < E) {
             stage_vertical<MAXN>(F, e + stride, my32 + (buf ^ 1) * N32 * bd, my64 + (buf ^ 1) * VD_COUNT * bd, bd);

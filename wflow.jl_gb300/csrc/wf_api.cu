@@ -70,6 +70,7 @@ struct WfHandle {
     std::vector<int64_t> outlet_slots;
     int64_t* d_outlet_slots = nullptr;  // river slots of river pits
     int64_t* d_land_node_of_slot = nullptr;
+    int64_t* d_land_slot_of_node = nullptr;  // [n] land slot of each external cell (forcing tiles)
     WfTuning tuning{};
     WfMetrics metrics{};
     cudaGraph_t graph = nullptr;
@@ -403,6 +404,60 @@ __global__ void to_f32_kernel(const double* src, float* dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = (float)src[i];
 }
+// Member-major forcing (external cell order) into the slot order, through a shared-memory tile
+// of 32 cells x 32 members: a warp reads 32 consecutive cells of one member (coalesced) and
+// writes the 32 members of one cell (one contiguous run of the slot-order array), where an
+// element-wise gather would read one isolated word per member. FP32 destination (split form) or
+// FP64. Grid: (ceil(n / 32), ceil(M / 32)); block 32 x 8.
+template <typename S>
+__global__ void __launch_bounds__(256) forcing_tile_kernel(const S* src, float* dst32, double* dst64,
+                                                           const int64_t* slot_of_node, int64_t n, int M) {
+    __shared__ S tile[32][33];
+    const int64_t node0 = (int64_t)blockIdx.x * 32;
+    const int m0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int j = ty; j < 32; j += 8) {
+        const int m = m0 + j;
+        const int64_t node = node0 + tx;
+        if (m < M && node < n) tile[j][tx] = src[(int64_t)m * n + node];
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        const int64_t node = node0 + k;
+        const int m = m0 + tx;
+        if (node >= n || m >= M) continue;
+        const int64_t e = slot_of_node[node] * M + m;
+        if (dst32) dst32[e] = (float)tile[tx][k];
+        else dst64[e] = (double)tile[tx][k];
+    }
+}
+// The same for fewer than 32 members: one thread per (member, cell) in external order (coalesced
+// reads; the writes follow the slot permutation).
+template <typename S>
+__global__ void forcing_scatter_small_kernel(const S* src, float* dst32, double* dst64, const int64_t* slot_of_node,
+                                             int64_t n, int M) {
+    const int64_t E = n * M;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < E; i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = (int)(i / n);
+        const int64_t node = i - (int64_t)m * n;
+        const int64_t e = slot_of_node[node] * M + m;
+        if (dst32) dst32[e] = (float)src[i];
+        else dst64[e] = (double)src[i];
+    }
+}
+int grid_of(int64_t n, int block);
+template <typename S>
+void launch_forcing_full(const WfHandle* h, const S* src, float* dst32, double* dst64) {
+    if (h->M >= 32) {
+        const dim3 grid((unsigned)((h->n + 31) / 32), (unsigned)((h->M + 31) / 32));
+        forcing_tile_kernel<S><<<grid, dim3(32, 8), 0, h->stream>>>(src, dst32, dst64, h->d_land_slot_of_node, h->n,
+                                                                     h->M);
+    } else {
+        forcing_scatter_small_kernel<S><<<grid_of(h->n * h->M, 256), 256, 0, h->stream>>>(
+            src, dst32, dst64, h->d_land_slot_of_node, h->n, h->M);
+    }
+}
+
 // FP32 forcing of n_ext cells per member (member-major, or one set for every member when
 // `broadcast`) into the slot order: FP32 destination (split form) or FP64 (FP64 form).
 __global__ void gather_from_f32_kernel(const float* src, float* dst32, double* dst64, const int64_t* node_of_slot,
@@ -1176,6 +1231,7 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
         for (int64_t r = 0; r < nr; ++r)
             if (d->river_downstream[r] < 0) h->outlet_slots.push_back(PR.slot_of_node[r]);
         if (!h->outlet_slots.empty()) CKR(upload(h, &h->d_outlet_slots, h->outlet_slots));
+        CKR(upload(h, &h->d_land_slot_of_node, PL.slot_of_node));
     }
     // ---- reservoirs: parameters per reservoir, state per reservoir and member (r * M + m)
     h->nres = nres;
@@ -1293,16 +1349,12 @@ int enqueue_forcing_gathers(WfHandle* h, double* const stg_of[3], int64_t count)
     for (int k = 0; k < 3; ++k) {
         double* stg = stg_of[k];
         const int g = grid_of(h->F.land_slots * h->M, block);
-        if (h->F.split) {
-            if (count == full)
-                gather_f32_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mh[dst[k]], h->F.land_node_of_slot,
-                                                              h->F.land_slots, h->M, h->n);
-            else
-                broadcast_member_f32_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mh[dst[k]], h->F.land_node_of_slot,
-                                                                        h->F.land_slots, h->M);
-        } else if (count == full) {
-            gather_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mf[dst[k]], h->F.land_node_of_slot, h->F.land_slots,
-                                                      h->M, h->n);
+        if (count == full) {
+            launch_forcing_full<double>(h, stg, h->F.split ? h->F.Mh[dst[k]] : nullptr,
+                                        h->F.split ? nullptr : h->F.Mf[dst[k]]);
+        } else if (h->F.split) {
+            broadcast_member_f32_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mh[dst[k]], h->F.land_node_of_slot,
+                                                                    h->F.land_slots, h->M);
         } else {
             broadcast_member_kernel<<<g, block, 0, h->stream>>>(stg, h->F.Mf[dst[k]], h->F.land_node_of_slot,
                                                                 h->F.land_slots, h->M, nullptr);
@@ -1318,10 +1370,13 @@ int enqueue_forcing_gathers_f32(WfHandle* h, float* const stg[3], int64_t count)
     const int g = grid_of(h->F.land_slots * h->M, 256);
     const int broadcast = count != h->n * h->M;
     for (int k = 0; k < 3; ++k) {
-        gather_from_f32_kernel<<<g, 256, 0, h->stream>>>(stg[k], h->F.split ? h->F.Mh[dst[k]] : nullptr,
-                                                         h->F.split ? nullptr : h->F.Mf[dst[k]],
-                                                         h->F.land_node_of_slot, h->F.land_slots, h->M, h->n,
-                                                         broadcast);
+        float* d32 = h->F.split ? h->F.Mh[dst[k]] : nullptr;
+        double* d64 = h->F.split ? nullptr : h->F.Mf[dst[k]];
+        if (broadcast)
+            gather_from_f32_kernel<<<g, 256, 0, h->stream>>>(stg[k], d32, d64, h->F.land_node_of_slot,
+                                                             h->F.land_slots, h->M, h->n, 1);
+        else
+            launch_forcing_full<float>(h, stg[k], d32, d64);
         CK(cudaGetLastError());
     }
     return WF_OK;
