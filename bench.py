@@ -308,6 +308,12 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value, e2e_s = whole_job_rate(e2e_s, cells, K, device=dev)
+    # the forcing upload alone (copies and gathers, no step): what the step has to hide
+    t1 = time.perf_counter()
+    for s in range(K):
+        set_forcing_async(s)
+    model.synchronize()
+    upload_ms = (time.perf_counter() - t1) / K * 1e3
     # ---- per-kernel times (eager launches with events between kernels) for the roofline
     model.set_tuning(**(tuning or {}), use_graph=0, kernel_timing=1)
     for s in range(min(K, 5)):
@@ -341,7 +347,7 @@ def run_gpu(args):
                    "tuning": tuning},
         "e2e": {"value": e2e_value, "unit": "cell-timesteps/s",
                 "h2d_bytes_per_step": 3 * np.dtype(fdt).itemsize * cells, "d2h_bytes_per_step": 8 * n_out,
-                "forcing_dtype": np.dtype(fdt).name},
+                "forcing_dtype": np.dtype(fdt).name, "upload_only_ms_per_step": upload_ms},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": kt,
         "clocks": clk,

@@ -11,13 +11,16 @@
  * :800-860). Channel only: no floodplain, no reservoirs at edges. FP64 in the reference's
  * operation order.
  *
- * A standalone component: it holds its own network and state on the device; the SBM step of
- * wflow_gb300.h routes rivers by the kinematic wave.
+ * The components hold their own network and state on the device. A land grid with its river
+ * (WfLiDomain) can also route an SBM model's land and river inside its step, in place of the
+ * kinematic waves (wf_attach_local_inertial).
  */
 #ifndef WFLOW_GB300_LI_H
 #define WFLOW_GB300_LI_H
 
 #include <stdint.h>
+
+#include "wflow_gb300.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -176,6 +179,22 @@ int32_t wf_li_domain_step(WfLiDomain* d, double dt, int64_t* substeps);
 /* host_loop != 0: drive the sub-steps of wf_li_domain_step from the host (the same results). */
 int32_t wf_li_domain_set_host_loop(WfLiDomain* d, int32_t host_loop);
 int32_t wf_li_domain_get(WfLiDomain* d, int32_t field, double* dst);
+
+/* Route an SBM model's land and river by this domain inside wf_step, in place of the kinematic
+ * waves: Wflow's surface_routing! for local-inertial land and river routing
+ * (Wflow/src/routing/surface/surface_routing.jl:62-89). Every step the land runoff
+ * (net_runoff + net_runoff_river) * area, plus the subsurface flow to the river at river cells
+ * (update_bc_overland_flow_model!, surface_staggered_scheme.jl:1080-1097), drives the domain's
+ * step (update_overland_flow_model!, :1153-1193) on the model's stream; the model's overland and
+ * river depths and storages (read by the next step's open-water evaporation and by the total
+ * storage) are the domain's, its river discharge that of each river cell's outgoing edge, and its
+ * overland balance the domain's per land cell (mass_balance.jl:402-461). Needs the FP64 form, one
+ * member, no reservoirs and fixed kinematic-wave settings; the domain's land cells are the
+ * model's land cells and its active river cells the model's river cells (river_index of the land
+ * cell of river cell r is r). The model takes the domain's state at the call; the domain must
+ * outlive the model and is stepped only through it afterwards. No CUDA graph and no
+ * wf_step_static for such a model (the loop's status is read back every step). */
+int32_t wf_attach_local_inertial(WfHandle* h, WfLiDomain* d);
 
 #ifdef __cplusplus
 }

@@ -199,6 +199,29 @@ class OracleModel:
         v = np.ascontiguousarray(values, dtype=np.float64)
         lib().orc_model_set(self.h, field, layer, v.ctypes.data_as(_pd))
 
+    def attach_li(self, land, river, h_land, h_river):
+        """orc_model_attach_li: local-inertial land and river routing in the step (the dicts of
+        wflow_gb300.li_river's structs)."""
+        from wflow_gb300.li_river import land_grid, river_network
+        keep = []
+        g, r = land_grid(land, keep), river_network(river, keep)
+        hl = np.ascontiguousarray(h_land, np.float64)
+        hr = np.ascontiguousarray(h_river, np.float64)
+        st = lib().orc_model_attach_li(self.h, C.byref(g), C.byref(r), hl.ctypes.data_as(_pd), hr.ctypes.data_as(_pd))
+        if st != 0:
+            raise RuntimeError(f"orc_model_attach_li failed {st}: {lib().orc_model_error(self.h)}")
+        self.n_river_total = len(river["zb"])
+        self.n_edges = len(river["src"])
+
+    def li_get(self, field):
+        """A WfLiDomainField of the coupled scheme (-1: the sub-steps of the last step)."""
+        n = {-1: 1, 7: self.n_river_total, 8: self.n_river_total, 11: self.n_river_total, 9: self.n_edges,
+             10: self.n_edges}.get(field, self.n)
+        out = np.empty(n)
+        if lib().orc_model_li_get(self.h, field, out.ctypes.data_as(_pd)) != 0:
+            raise KeyError(field)
+        return out
+
     def outlets(self, which=0):
         out = np.empty(max(1, self.nr * self.M))
         n = C.c_int64()

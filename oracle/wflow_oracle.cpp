@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -980,6 +981,23 @@ void update_reservoir_at_node(OrcReservoir& r, double q, double dt) {
 
 // ======================================================================= full model =====
 
+// The land grid with its river routed by the local-inertial scheme in place of the kinematic
+// waves (surface_routing.jl:62-89): copies of the grid and network arrays, the scheme's state
+// (OrcLiState), its inputs and the averages of the last step.
+struct OrcLiCoupled {
+    std::vector<int64_t> ixu, ixd, iyu, iyd, riv, src, dst;
+    std::vector<double> xl, yl, z, nsq, xw, yw, zb, fl, fw, bd, zbe, we, le, nsqe;
+    WfLiLandGrid g{};
+    WfLiRiverNetwork r{};
+    std::vector<double> h_land, storage, error, qx, qy, qx0, qy0, qx_cum, qy_cum;
+    std::vector<double> h_river, storage_river, q, q_prev, q_cum, abstraction_cum;
+    std::vector<double> runoff, ext, abstraction, qx_avg, qy_avg, q_avg;
+    std::vector<int64_t> out_edge;                  // per river cell: its outgoing edge, or -1
+    std::vector<std::vector<int64_t>> e_in, e_out;  // edges_at_node.src / .dst (ascending)
+    OrcLiState st{};
+    int64_t substeps = 0;
+};
+
 struct OrcModel {
     WfConfig cfg{};
     int N = 0;  // maximum_number_of_layers
@@ -1033,6 +1051,7 @@ struct OrcModel {
     int64_t last_sub_land = 0, last_sub_river = 0, last_sub_ssf = 0;
     std::vector<double> sig[3];  // per member: sum of the squared sub-step sizes (subsurface, land, river)
     std::vector<double> buf;
+    std::unique_ptr<OrcLiCoupled> li;  // local-inertial land and river routing (one member)
 };
 
 namespace {
@@ -1349,6 +1368,146 @@ int32_t orc_model_create(const WfConfig* c, const WfDomain* d, const WfParams* p
 
 void orc_model_destroy(OrcModel* m) { delete m; }
 
+// Couple the land grid with its river (local-inertial) to the model's step (li_surface_routing):
+// one member, no reservoirs, fixed kinematic-wave settings unused; the grid's land cells are the
+// model's land cells and its active river cells the model's river cells (river_index of the
+// land cell of river cell r is r). Warm state as wf_li_domain_set_state.
+int32_t orc_model_attach_li(OrcModel* m, const WfLiLandGrid* land, const WfLiRiverNetwork* river,
+                            const double* h_land, const double* h_river) {
+    if (!m || !land || !river || !h_land || !h_river) return WF_ERR_INVALID;
+    if (m->M != 1 || m->nres > 0 || m->cfg.adaptive_timestep) {
+        m->err = "local-inertial routing in the step needs one member, no reservoirs and fixed sub-steps";
+        return WF_ERR_UNSUPPORTED;
+    }
+    if (land->n != m->n || river->n_active != m->nr) {
+        m->err = "the grid's land and active river cells must be the model's";
+        return WF_ERR_INVALID;
+    }
+    for (int64_t r = 0; r < m->nr; ++r)
+        if (land->river_index[m->r_land[r]] != r) {
+            m->err = "river_index must map the land cell of river cell r to r";
+            return WF_ERR_INVALID;
+        }
+    auto c = std::make_unique<OrcLiCoupled>();
+    const int64_t n = land->n, nrt = river->n, ne = river->n_edges;
+    auto cpi = [](std::vector<int64_t>& v, const int64_t* p, int64_t k) { v.assign(p, p + k); };
+    auto cpd = [](std::vector<double>& v, const double* p, int64_t k) { v.assign(p, p + k); };
+    cpi(c->ixu, land->ind_x_up, n);
+    cpi(c->ixd, land->ind_x_down, n);
+    cpi(c->iyu, land->ind_y_up, n);
+    cpi(c->iyd, land->ind_y_down, n);
+    cpi(c->riv, land->river_index, n);
+    cpd(c->xl, land->x_length, n);
+    cpd(c->yl, land->y_length, n);
+    cpd(c->z, land->elevation, n);
+    cpd(c->nsq, land->mannings_n_sq, n);
+    cpd(c->xw, land->xwidth_at_edge, n);
+    cpd(c->yw, land->ywidth_at_edge, n);
+    cpi(c->src, river->src, ne);
+    cpi(c->dst, river->dst, ne);
+    cpd(c->zb, river->zb, nrt);
+    cpd(c->fl, river->flow_length, nrt);
+    cpd(c->fw, river->flow_width, nrt);
+    cpd(c->bd, river->bankfull_depth, nrt);
+    cpd(c->zbe, river->zb_edge, ne);
+    cpd(c->we, river->width_edge, ne);
+    cpd(c->le, river->length_edge, ne);
+    cpd(c->nsqe, river->mannings_n_sq_edge, ne);
+    c->g = *land;
+    c->g.ind_x_up = c->ixu.data();
+    c->g.ind_x_down = c->ixd.data();
+    c->g.ind_y_up = c->iyu.data();
+    c->g.ind_y_down = c->iyd.data();
+    c->g.river_index = c->riv.data();
+    c->g.x_length = c->xl.data();
+    c->g.y_length = c->yl.data();
+    c->g.elevation = c->z.data();
+    c->g.mannings_n_sq = c->nsq.data();
+    c->g.xwidth_at_edge = c->xw.data();
+    c->g.ywidth_at_edge = c->yw.data();
+    c->r = *river;
+    c->r.src = c->src.data();
+    c->r.dst = c->dst.data();
+    c->r.zb = c->zb.data();
+    c->r.flow_length = c->fl.data();
+    c->r.flow_width = c->fw.data();
+    c->r.bankfull_depth = c->bd.data();
+    c->r.zb_edge = c->zbe.data();
+    c->r.width_edge = c->we.data();
+    c->r.length_edge = c->le.data();
+    c->r.mannings_n_sq_edge = c->nsqe.data();
+    for (auto* v : {&c->h_land, &c->storage, &c->error, &c->runoff}) v->assign(n, 0.0);
+    for (auto* v : {&c->qx, &c->qy, &c->qx0, &c->qy0, &c->qx_cum, &c->qy_cum, &c->qx_avg, &c->qy_avg})
+        v->assign(n + 1, 0.0);
+    for (auto* v : {&c->h_river, &c->storage_river, &c->abstraction_cum, &c->ext, &c->abstraction})
+        v->assign(nrt, 0.0);
+    for (auto* v : {&c->q, &c->q_prev, &c->q_cum, &c->q_avg}) v->assign(ne, 0.0);
+    c->out_edge.assign(nrt, -1);
+    c->e_in.assign(nrt, {});
+    c->e_out.assign(nrt, {});
+    for (int64_t e = 0; e < ne; ++e) {
+        c->e_in[c->dst[e]].push_back(e);
+        c->e_out[c->src[e]].push_back(e);
+        if (c->out_edge[c->src[e]] < 0) c->out_edge[c->src[e]] = e;
+    }
+    // warm state (sbm_model.jl:135-172)
+    for (int64_t i = 0; i < n; ++i) {
+        c->h_land[i] = h_land[i];
+        const int64_t r = c->riv[i];
+        if (r >= 0)
+            c->storage[i] = h_land[i] > 0.0 ? h_land[i] * c->xl[i] * c->yl[i] + c->bd[r] * c->fw[r] * c->fl[r]
+                                            : h_river[r] * c->fw[r] * c->fl[r];
+        else
+            c->storage[i] = h_land[i] * c->xl[i] * c->yl[i];
+    }
+    for (int64_t r = 0; r < nrt; ++r) {
+        c->h_river[r] = h_river[r];
+        if (r < river->n_active) c->storage_river[r] = h_river[r] * c->fw[r] * c->fl[r];
+    }
+    c->st = OrcLiState{c->h_land.data(), c->storage.data(), c->error.data(), c->qx.data(), c->qy.data(),
+                       c->qx0.data(), c->qy0.data(), c->qx_cum.data(), c->qy_cum.data(), c->h_river.data(),
+                       c->storage_river.data(), c->q.data(), c->q_prev.data(), c->q_cum.data(),
+                       c->abstraction_cum.data()};
+    for (int64_t i = 0; i < n; ++i) {
+        m->ol_h[i] = c->h_land[i];
+        m->ol_storage[i] = c->storage[i];
+    }
+    for (int64_t r = 0; r < m->nr; ++r) {
+        m->rv_h[r] = c->h_river[r];
+        m->rv_storage[r] = c->storage_river[r];
+    }
+    m->li = std::move(c);
+    return WF_OK;
+}
+
+// A field of the coupled scheme (the WfLiDomainField ids of wf_li_domain_get), and the sub-steps
+// of the last step (field -1, one value).
+int32_t orc_model_li_get(OrcModel* m, int32_t field, double* out) {
+    if (!m || !m->li || !out) return WF_ERR_INVALID;
+    const OrcLiCoupled& c = *m->li;
+    const int64_t n = m->n;
+    const std::vector<double>* v = nullptr;
+    int64_t cnt = 0;
+    switch (field) {
+        case -1: out[0] = (double)c.substeps; return WF_OK;
+        case 0: v = &c.h_land; cnt = n; break;
+        case 1: v = &c.storage; cnt = n; break;
+        case 2: v = &c.error; cnt = n; break;
+        case 3: v = &c.qx; cnt = n; break;
+        case 4: v = &c.qy; cnt = n; break;
+        case 5: v = &c.qx_avg; cnt = n; break;
+        case 6: v = &c.qy_avg; cnt = n; break;
+        case 7: v = &c.h_river; cnt = c.r.n; break;
+        case 8: v = &c.storage_river; cnt = c.r.n; break;
+        case 9: v = &c.q; cnt = c.r.n_edges; break;
+        case 10: v = &c.q_avg; cnt = c.r.n_edges; break;
+        case 11: v = &c.abstraction_cum; cnt = c.r.n; break;
+        default: return WF_ERR_INVALID;
+    }
+    std::copy(v->begin(), v->begin() + cnt, out);
+    return WF_OK;
+}
+
 // The land graph order of the snow transport (topological_sort_by_dfs); 0, or -3 on a cycle.
 int32_t orc_topo_order_dfs(int64_t n, const int32_t* ds, int64_t* order) {
     std::vector<int64_t> v;
@@ -1446,6 +1605,85 @@ namespace {
 
 // One member's step. Follows sbm_model.jl:60-92 then mass_balance.jl:541-545; the storage_prev!
 // of run_timestep! (Wflow.jl:315) runs first.
+// surface_routing! of the local-inertial land and river (surface_routing.jl:62-89) for member 0:
+// update_bc_overland_flow_model! (surface_staggered_scheme.jl:1080-1097) then
+// update_overland_flow_model! (:1153-1193) without reservoirs; the model's overland and river
+// variables then hold the scheme's depths, storages and the discharge of each river cell's
+// outgoing edge.
+void li_surface_routing(OrcModel* m, const OrcSoil* soil, double dt) {
+    OrcLiCoupled& c = *m->li;
+    const int64_t n = m->n, nr = m->nr;
+    for (int64_t i = 0; i < n; ++i) c.runoff[i] = (soil[i].net_runoff + m->net_runoff_river[i]) * m->area[i];
+    for (int64_t r = 0; r < nr; ++r) {
+        const int64_t li = m->r_land[r];
+        c.runoff[li] += m->ssf_tr_avg[li];  // get_flux_to_river (lateral_subsurface_flow.jl:346-347)
+        c.ext[r] = m->r_ext_inflow[r];
+    }
+    for (auto* v : {&c.q_cum, &c.abstraction_cum, &c.qx_cum, &c.qy_cum}) std::fill(v->begin(), v->end(), 0.0);
+    double t = 0.0;
+    int64_t k = 0;
+    while (t < dt) {
+        double dt_s = orc_li_domain_stable_timestep(&c.g, &c.r, &c.st);
+        dt_s = check_timestepsize(dt_s, t, dt);
+        orc_li_domain_substep(&c.g, &c.r, c.runoff.data(), c.ext.data(), c.abstraction.data(), dt_s, &c.st);
+        t += dt_s;
+        ++k;
+    }
+    c.substeps = k;
+    for (int64_t e = 0; e < c.r.n_edges; ++e) c.q_avg[e] = c.q_cum[e] / dt;
+    for (int64_t i = 0; i <= n; ++i) {
+        c.qx_avg[i] = c.qx_cum[i] / dt;
+        c.qy_avg[i] = c.qy_cum[i] / dt;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        m->ol_h[i] = c.h_land[i];
+        m->ol_storage[i] = c.storage[i];
+        m->ol_q[i] = 0.0;
+        m->ol_q_avg[i] = 0.0;
+    }
+    for (int64_t r = 0; r < nr; ++r) {
+        m->rv_h[r] = c.h_river[r];
+        m->rv_storage[r] = c.storage_river[r];
+        const int64_t e = c.out_edge[r];
+        m->rv_q[r] = e >= 0 ? c.q[e] : 0.0;
+        m->rv_q_avg[r] = e >= 0 ? c.q_avg[e] : 0.0;
+    }
+}
+
+// compute_flow_balance! of the local-inertial land and river (mass_balance.jl:402-461): per land
+// cell, the x and y discharges, the runoff and at river cells the river edges, the positive
+// external inflow and the actual abstraction; no reservoirs.
+void li_overland_balance(OrcModel* m, double dt) {
+    OrcLiCoupled& c = *m->li;
+    double eo[2];
+    for (int64_t i = 0; i < m->n; ++i) {
+        double tin = 0.0, tout = 0.0;
+        for (double q : {c.qx_avg[c.g.ind_x_down[i]], c.qy_avg[c.g.ind_y_down[i]], c.runoff[i]}) {  // add_inflow
+            if (q > 0.0) tin += q;
+            else tout -= q;
+        }
+        for (double q : {c.qx_avg[i], c.qy_avg[i]}) {  // add_outflow
+            if (q > 0.0) tout += q;
+            else tin -= q;
+        }
+        const int64_t k = c.g.river_index[i];
+        if (k >= 0) {
+            double q_src = 0.0, q_dst = 0.0;
+            for (int64_t e : c.e_in[k]) q_src += c.q_avg[e];
+            if (q_src > 0.0) tin += q_src;
+            else tout -= q_src;
+            tin += jmax(0.0, c.ext[k]);
+            for (int64_t e : c.e_out[k]) q_dst += c.q_avg[e];
+            if (q_dst > 0.0) tout += q_dst;
+            else tin -= q_dst;
+            tout += c.abstraction_cum[k] / dt + c.abstraction[k];
+        }
+        compute_mass_balance_error(tin, tout, (c.storage[i] - m->bo_prev[i]) / dt, eo);
+        m->bo_err[i] = eo[0];
+        m->bo_rel[i] = eo[1];
+    }
+}
+
 void member_step(OrcModel* m, int mbr, int n_threads) {
     const WfConfig& c = m->cfg;
     const double dt = c.dt;
@@ -1630,6 +1868,10 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
         int64_t j = o + i;
         update_soil_water_storage(soil[i], m->ssf_exf_avg[j], m->runoff_land[j], m->ae_land[j], dt);
     }
+    OrcReservoir* res = m->nres ? m->res.data() + (size_t)mbr * m->nres : nullptr;
+    if (m->li) {
+        li_surface_routing(m, soil, dt);
+    } else {
     // ---- surface_routing! (surface_routing.jl:7-46)
     // overland lateral inflow (surface_kinwave.jl:740-766)
     for (int64_t i = 0; i < n; ++i) {
@@ -1693,7 +1935,6 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
     // reservoir inflow from the outlet cell's overland and subsurface flow (update_inflow!,
     // surface_kinwave.jl:771-802) and the reset of the step's cumulatives (set_reservoir_vars!,
     // :227-237)
-    OrcReservoir* res = m->nres ? m->res.data() + (size_t)mbr * m->nres : nullptr;
     for (int64_t k = 0; k < m->nres; ++k) {
         OrcReservoir& r = res[k];
         r.inflow_overland = m->ol_q_avg[o + m->res_land[k]];
@@ -1761,6 +2002,7 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
         m->res_in_avg[q] = res[k].inflow_cumulative / dt;
         m->res_abs_avg[q] = res[k].abstraction_cumulative / dt;
     }
+    }  // kinematic-wave surface routing
     // ---- update_total_water_storage! (sbm.jl:143-182)
     for (int64_t i = 0; i < n; ++i) m->total_storage[o + i] = 0.0;
     for (int64_t r = 0; r < nr; ++r) {
@@ -1795,7 +2037,11 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
             m->bl_err[j] = eo[0];
             m->bl_rel[j] = eo[1];
         }
-        for (int64_t r = 0; r < nr; ++r) {  // river :290-313
+        for (int64_t r = 0; r < nr && m->li; ++r) {  // local-inertial routing: no river balance (:516-536)
+            m->br_err[orr + r] = 0.0;
+            m->br_rel[orr + r] = 0.0;
+        }
+        for (int64_t r = 0; r < nr && !m->li; ++r) {  // river :290-313
             int64_t j = orr + r;
             double total_in = m->rv_inwater[j] + m->rv_qin_avg[j] + jmax(0.0, m->r_ext_inflow[r]);
             double total_out = m->rv_q_avg[j] + m->rv_abs_avg[j] + 0.0;
@@ -1816,7 +2062,8 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
             m->res_err[q] = eo[0];
             m->res_rel[q] = eo[1];
         }
-        for (int64_t i = 0; i < n; ++i) {  // overland :382-399
+        if (m->li) li_overland_balance(m, dt);
+        for (int64_t i = 0; i < n && !m->li; ++i) {  // overland :382-399
             int64_t j = o + i;
             double total_in = m->ol_inwater[j] + m->ol_qin_avg[j];
             double total_out = m->ol_q_avg[j];

@@ -208,6 +208,13 @@ int32_t orc_model_substep_signature(OrcModel* m, int32_t kind, double* out);
 int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p,
                                          const WfReservoirs* rs, OrcModel** out);
 int64_t orc_model_reservoirs(const OrcModel* m);
+/* Route the land grid with its river by the local-inertial scheme inside the step, in place of
+ * the kinematic waves (surface_routing.jl:62-89): one member, no reservoirs, fixed sub-steps;
+ * the grid's land and active river cells are the model's. Warm state h_land [n], h_river [river n]. */
+int32_t orc_model_attach_li(OrcModel* m, const WfLiLandGrid* land, const WfLiRiverNetwork* river,
+                            const double* h_land, const double* h_river);
+/* A WfLiDomainField of the coupled scheme; field -1: the sub-steps of the last step. */
+int32_t orc_model_li_get(OrcModel* m, int32_t field, double* out);
 void orc_model_destroy(OrcModel* m);
 const char* orc_model_error(const OrcModel* m);
 int32_t orc_model_set_forcing(OrcModel* m, const double* P, const double* PET, const double* T);

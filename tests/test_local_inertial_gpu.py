@@ -277,3 +277,72 @@ def test_device_and_host_sub_step_loops_agree(gpu_lib):
             assert np.array_equal(c.get(f), d.get(f)), (step, f)
     for m in (a, b, c, d):
         m.close()
+
+
+# ---- local-inertial land and river routing inside the SBM step (wf_attach_local_inertial) ----
+
+COUPLED_FIELDS = ["LAND_H", "LAND_STORAGE", "RIVER_H", "RIVER_STORAGE", "RIVER_Q", "TOTAL_STORAGE",
+                  "SATURATED_WATER_DEPTH", "SSF_Q", "NET_RUNOFF", "BALANCE_LAND_ERROR", "BALANCE_OVERLAND_ERROR"]
+
+
+def _coupled_pair(dom, dt, warm, seed):
+    from wflow_gb300 import abi, synthetic
+    from wflow_gb300.li_river import LiDomain
+    from wflow_gb300.model import Model
+    import oracle_py as O
+    cfg = synthetic.make_config(dt, form=abi.WF_FORM_FP64)
+    land, river, h_land, h_river = synthetic.li_coupling(dom, seed=seed, warm=warm)
+    d = LiDomain(land, river, h_river)
+    d.set_state(h_land, h_river)
+    gpu = Model(cfg, dom)
+    gpu.attach_local_inertial(d)
+    orc = O.OracleModel(cfg, dom)
+    orc.attach_li(land, river, h_land, h_river)
+    return cfg, gpu, orc, d
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dt,warm,side", [(86400.0, True, 32), (3600.0, False, 48)])
+def test_coupled_sbm_step_matches_oracle(gpu_lib, dt, warm, side):
+    from wflow_gb300 import abi, synthetic
+    import os
+    dom = synthetic.make_domain(side, 250.0, seed=8)
+    cfg, gpu, orc, d = _coupled_pair(dom, dt, warm, seed=8)
+    threads = os.cpu_count() or 1
+    total = 0
+    for s in range(6):
+        P, PET, T = synthetic.forcing(s, dt, dom.n_land, seed=8, precip_scale=4.0)
+        gpu.run_timestep(P, PET, T)
+        orc.set_forcing(P, PET, T)
+        orc.step(threads)
+        qo, qg = orc.outlets(0), gpu.outlets(0)
+        assert _max_rel(qg, qo) <= 1e-9, (s, _max_rel(qg, qo))
+        for f in COUPLED_FIELDS:
+            g, o = gpu.get_value(f), orc.get(abi.FIELD[f])
+            if "ERROR" in f:  # balance errors: absolute, against the step's fluxes
+                assert np.max(np.abs(g - o)) <= 1e-9 * (np.max(np.abs(o)) + 1e-12), (s, f)
+            else:
+                assert _max_rel(g, o) <= 1e-9, (s, f, _max_rel(g, o))
+        total += int(orc.li_get(-1)[0])
+        assert gpu.metrics()["substeps_land"] == total, s  # the same sub-steps as the oracle
+    for name, field in (("h_land", 0), ("storage", 1), ("qx_average", 5), ("h_river", 7), ("q_river", 9)):
+        assert _max_rel(d.get(name), orc.li_get(field)[:len(d.get(name))]) <= 1e-9, name
+    assert np.all(gpu.get_value("BALANCE_RIVER_ERROR") == 0.0)
+    assert d.get("h_land").max() > 0.0
+
+
+@pytest.mark.gpu
+def test_coupling_refuses_what_it_cannot_take(gpu_lib):
+    from wflow_gb300 import abi, synthetic
+    from wflow_gb300.li_river import LiDomain
+    from wflow_gb300.model import Model
+    dom = synthetic.make_domain(16, 250.0, seed=9)
+    land, river, h_land, h_river = synthetic.li_coupling(dom, seed=9)
+    d = LiDomain(land, river, h_river)
+    for kw in (dict(form=abi.WF_FORM_SPLIT), dict(n_members=2), dict(adaptive=True)):
+        m = Model(synthetic.make_config(86400.0, **{"form": abi.WF_FORM_FP64, **kw}), dom)
+        with pytest.raises(RuntimeError):
+            m.attach_local_inertial(d)
+    other = synthetic.make_domain(12, 250.0, seed=9)
+    with pytest.raises(RuntimeError):
+        Model(synthetic.make_config(86400.0, form=abi.WF_FORM_FP64), other).attach_local_inertial(d)

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include "wf_fields.cuh"
+#include "wf_li_couple.cuh"
 #include "wf_kernels.h"
 #include "wf_launch.cuh"
 #include "wf_math.cuh"
@@ -1047,7 +1048,7 @@ __global__ void __launch_bounds__(256) balance_kernel(WfDevFields F) {
     double* const* L = F.L;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < EL + ER; e += (int64_t)gridDim.x * blockDim.x) {
         if (e >= EL) {
-            if (!F.mass_balance) continue;
+            if (!F.mass_balance || F.li_coupled) continue;
             const int64_t re = e - EL;
             const int64_t rs = re / M;
             if (F.river_node_of_slot[rs] < 0) continue;
@@ -1091,11 +1092,14 @@ __global__ void __launch_bounds__(256) balance_kernel(WfDevFields F) {
             Mf[BL_ERR][e] = err;
             Mf[BL_REL][e] = rel;
         }
-        // overland balance (mass_balance.jl:382-399)
-        mb_error(Mf[OL_INWATER][e] + Mf[OL_QIN_AVG][e], Mf[OL_Q_AVG][e], (Mf[OL_STORAGE][e] - Mf[BO_PREV][e]) / dt,
-                 err, rel);
-        Mf[BO_ERR][e] = err;
-        Mf[BO_REL][e] = rel;
+        // overland balance (mass_balance.jl:382-399); the local-inertial one is written by
+        // li_couple_out_kernel
+        if (!F.li_coupled) {
+            mb_error(Mf[OL_INWATER][e] + Mf[OL_QIN_AVG][e], Mf[OL_Q_AVG][e],
+                     (Mf[OL_STORAGE][e] - Mf[BO_PREV][e]) / dt, err, rel);
+            Mf[BO_ERR][e] = err;
+            Mf[BO_REL][e] = rel;
+        }
         // subsurface balance (mass_balance.jl:470-490, groundwater.jl:671-695)
         {
             const double flux = Mf[RCH_FLUX_AVG][e];
@@ -1105,6 +1109,94 @@ __global__ void __launch_bounds__(256) balance_kernel(WfDevFields F) {
             Mf[BS_ERR][e] = err;
             Mf[BS_REL][e] = rel;
         }
+    }
+}
+
+// ---------------------------------------------------- local-inertial routing in the step ----
+// (wf_li_couple.cuh; one member, FP64 form: element = slot)
+
+// update_bc_overland_flow_model! (surface_staggered_scheme.jl:1080-1097): the land runoff of
+// the step into the scheme's input, in its node order; the river's external inflow; the overland
+// storage before the step for the balance (storage_prev!, mass_balance.jl:170-183).
+__global__ void __launch_bounds__(256) li_couple_in_kernel(WfDevFields F, WfLiCoupleView v) {
+    double* const* Mf = F.Mf;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < F.land_slots;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = F.land_node_of_slot[s];
+        if (node < 0) continue;
+        double ro = (Mf[NET_RUNOFF][s] + Mf[NET_RUNOFF_RIVER][s]) * F.L[AREA][s];
+        const int64_t rs = F.land_river_slot[s];
+        if (rs >= 0) {
+            ro += Mf[SSF_TR_AVG][s];  // get_flux_to_river (lateral_subsurface_flow.jl:346-347)
+            v.ext[F.river_node_of_slot[rs]] = F.R[R_EXT_INFLOW][rs];
+        }
+        v.runoff[node] = ro;
+        if (F.mass_balance) Mf[BO_PREV][s] = Mf[OL_STORAGE][s];
+    }
+}
+
+// After the scheme's step: its depths, storages and the discharge of each river cell's outgoing
+// edge into the model's overland and river fields, and the overland balance of every land cell
+// (compute_flow_balance!, mass_balance.jl:402-461; add_inflow / add_outflow :355-376) with the
+// river balance cleared (the reference computes none for this routing).
+__global__ void __launch_bounds__(256) li_couple_out_kernel(WfDevFields F, WfLiCoupleView v, int balance) {
+    double* const* Mf = F.Mf;
+    double* const* RM = F.RM;
+    const double dt = F.dt;
+    const int64_t EL = F.land_slots, ER = F.river_slots;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < EL + ER;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i >= EL) {
+            const int64_t rs = i - EL;
+            const int64_t r = F.river_node_of_slot[rs];
+            if (r < 0) continue;
+            RM[RV_H][rs] = v.h_river[r];
+            RM[RV_STORAGE][rs] = v.storage_river[r];
+            const int64_t e = v.out_ptr[r] < v.out_ptr[r + 1] ? v.out_edge[v.out_ptr[r]] : -1;
+            RM[RV_Q][rs] = e >= 0 ? v.q[e] : 0.0;
+            RM[RV_Q_AVG][rs] = e >= 0 ? v.q_avg[e] : 0.0;
+            if (F.mass_balance && balance) {
+                RM[BR_ERR][rs] = 0.0;
+                RM[BR_REL][rs] = 0.0;
+            }
+            continue;
+        }
+        const int64_t s = i;
+        const int64_t node = F.land_node_of_slot[s];
+        if (node < 0) continue;
+        Mf[OL_H][s] = v.h_land[node];
+        Mf[OL_STORAGE][s] = v.storage[node];
+        Mf[OL_Q][s] = 0.0;
+        Mf[OL_Q_AVG][s] = 0.0;
+        if (!F.mass_balance || !balance) continue;
+        double tin = 0.0, tout = 0.0;
+        auto add_in = [&](double q) {
+            if (q > 0.0) tin += q;
+            else tout -= q;
+        };
+        auto add_out = [&](double q) {
+            if (q > 0.0) tout += q;
+            else tin -= q;
+        };
+        add_in(v.qx_avg[v.ixd[node]]);
+        add_in(v.qy_avg[v.iyd[node]]);
+        add_in(v.runoff[node]);
+        add_out(v.qx_avg[node]);
+        add_out(v.qy_avg[node]);
+        const int64_t k = v.river_index[node];
+        if (k >= 0) {
+            double q_src = 0.0, q_dst = 0.0;
+            for (int64_t o = v.in_ptr[k]; o < v.in_ptr[k + 1]; ++o) q_src += v.q_avg[v.in_edge[o]];
+            add_in(q_src);
+            tin += jmax(0.0, v.ext[k]);
+            for (int64_t o = v.out_ptr[k]; o < v.out_ptr[k + 1]; ++o) q_dst += v.q_avg[v.out_edge[o]];
+            add_out(q_dst);
+            tout += v.abstraction_cum[k] / dt + v.abstraction[k];
+        }
+        double err, rel;
+        mb_error(tin, tout, (v.storage[node] - Mf[BO_PREV][s]) / dt, err, rel);
+        Mf[BO_ERR][s] = err;
+        Mf[BO_REL][s] = rel;
     }
 }
 
@@ -1187,6 +1279,16 @@ cudaError_t wf_snow_transport_sweep(const WfDevFields& F, const WfDevGraph& g, c
 
 cudaError_t wf_snow_in(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {
     snow_in_kernel<<<grid_for(F.land_slots * F.M, 256, c.num_sms), 256, 0, c.stream>>>(F, g);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_fp64_li_couple_in(const WfDevFields& F, const WfLiCoupleView& v, const WfLaunchCfg& c) {
+    li_couple_in_kernel<<<grid_for(F.land_slots, 256, c.num_sms), 256, 0, c.stream>>>(F, v);
+    return cudaGetLastError();
+}
+cudaError_t wf_fp64_li_couple_out(const WfDevFields& F, const WfLiCoupleView& v, int balance, const WfLaunchCfg& c) {
+    li_couple_out_kernel<<<grid_for(F.land_slots + F.river_slots, 256, c.num_sms), 256, 0, c.stream>>>(F, v,
+                                                                                                     balance);
     return cudaGetLastError();
 }
 

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "li_scheme.cuh"
+#include "wf_li_couple.cuh"
 #include "wflow_gb300.h"
 #include "wflow_gb300_li.h"
 
@@ -843,40 +844,59 @@ int32_t wf_li_domain_substep(WfLiDomain* d, double dt_s) {
     return li_sync(d, "sub-step");
 }
 
+namespace {
+// set_flow_vars! of the river and the land (:1165-1166), the device sub-step loop (one
+// cooperative launch) and the averages, on stream st; 0 blocks when the device cannot run it.
+int li_domain_launch(WfLiDomain* d, double dt, cudaStream_t st, int blocks) {
+    const int64_t n = d->L.n, ne = d->R.n_edges;
+    if ((ne > 0 && cudaMemsetAsync(d->R.q_cum, 0, ne * sizeof(double), st) != cudaSuccess) ||
+        cudaMemsetAsync(d->B.abstraction_cum, 0, d->R.n * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(d->L.qx_cum, 0, (n + 1) * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(d->L.qy_cum, 0, (n + 1) * sizeof(double), st) != cudaSuccess)
+        return li_fail(d, WF_ERR_CUDA, "reset of the cumulative discharges failed");
+    li_loop_init_kernel<<<1, 1, 0, st>>>(d->loop);
+    wfli::LiLand LL = d->L;
+    LiDev RR = d->R;
+    wfli::LiRiverBC BB = d->B;
+    LiLoop* lp = d->loop;
+    double dtv = dt;
+    double *qx0b = d->qx_buf[0], *qx1b = d->qx_buf[1], *qy0b = d->qy_buf[0], *qy1b = d->qy_buf[1];
+    int cur0 = d->cur;
+    void* args[] = {&LL, &RR, &BB, &lp, &dtv, &qx0b, &qx1b, &qy0b, &qy1b, &cur0};
+    if (cudaLaunchCooperativeKernel((const void*)li_domain_loop_kernel, blocks, 256, args, 0, st) != cudaSuccess)
+        return li_fail(d, WF_ERR_CUDA, "cooperative launch of the sub-step loop failed");
+    if (ne > 0) li_average_kernel<<<grid_of(ne), 256, 0, st>>>(d->R.q_cum, d->q_avg, ne, dt);
+    li_average_kernel<<<grid_of(n + 1), 256, 0, st>>>(d->L.qx_cum, d->qx_avg, n + 1, dt);
+    li_average_kernel<<<grid_of(n + 1), 256, 0, st>>>(d->L.qy_cum, d->qy_avg, n + 1, dt);
+    return li_check(d, "sub-step loop");
+}
+
+int li_domain_blocks(WfLiDomain* d) {
+    const int64_t n = d->L.n, ne = d->R.n_edges;
+    return li_loop_blocks(li_domain_loop_kernel, d->device, std::max(std::max(n + 1, d->R.n), ne));
+}
+}  // namespace
+
 int32_t wf_li_domain_step(WfLiDomain* d, double dt, int64_t* substeps) {
     if (!d || !(dt > 0.0)) return li_fail(d, WF_ERR_INVALID, "step must be positive");
-    // set_flow_vars! of the river and the land (:1165-1166)
     const int64_t n = d->L.n, ne = d->R.n_edges;
-    if ((ne > 0 && cudaMemsetAsync(d->R.q_cum, 0, ne * sizeof(double), d->stream) != cudaSuccess) ||
-        cudaMemsetAsync(d->B.abstraction_cum, 0, d->R.n * sizeof(double), d->stream) != cudaSuccess ||
-        cudaMemsetAsync(d->L.qx_cum, 0, (n + 1) * sizeof(double), d->stream) != cudaSuccess ||
-        cudaMemsetAsync(d->L.qy_cum, 0, (n + 1) * sizeof(double), d->stream) != cudaSuccess)
-        return li_fail(d, WF_ERR_CUDA, "reset of the cumulative discharges failed");
-    const int blocks = d->host_loop ? 0 : li_loop_blocks(li_domain_loop_kernel, d->device,
-                                                          std::max(std::max(n + 1, d->R.n), ne));
+    const int blocks = d->host_loop ? 0 : li_domain_blocks(d);
     if (blocks > 0) {  // the sub-step loop on the device, one launch
-        li_loop_init_kernel<<<1, 1, 0, d->stream>>>(d->loop);
-        wfli::LiLand LL = d->L;
-        LiDev RR = d->R;
-        wfli::LiRiverBC BB = d->B;
-        LiLoop* lp = d->loop;
-        double dtv = dt;
-        double *qx0b = d->qx_buf[0], *qx1b = d->qx_buf[1], *qy0b = d->qy_buf[0], *qy1b = d->qy_buf[1];
-        int cur0 = d->cur;
-        void* args[] = {&LL, &RR, &BB, &lp, &dtv, &qx0b, &qx1b, &qy0b, &qy1b, &cur0};
-        if (cudaLaunchCooperativeKernel((const void*)li_domain_loop_kernel, blocks, 256, args, 0, d->stream) !=
-            cudaSuccess)
-            return li_fail(d, WF_ERR_CUDA, "cooperative launch of the sub-step loop failed");
-        if (ne > 0) li_average_kernel<<<grid_of(ne), 256, 0, d->stream>>>(d->R.q_cum, d->q_avg, ne, dt);
-        li_average_kernel<<<grid_of(n + 1), 256, 0, d->stream>>>(d->L.qx_cum, d->qx_avg, n + 1, dt);
-        li_average_kernel<<<grid_of(n + 1), 256, 0, d->stream>>>(d->L.qy_cum, d->qy_avg, n + 1, dt);
+        int rc = li_domain_launch(d, dt, d->stream, blocks);
+        if (rc) return rc;
         int64_t k = 0;
-        const int rc = li_finish_loop(d, &k);
+        rc = li_finish_loop(d, &k);
         if (rc) return rc;
         d->cur = (int)((d->cur + k) & 1);  // the buffer of the last sub-step's discharges
         if (substeps) *substeps = k;
         return WF_OK;
     }
+    // set_flow_vars! of the river and the land (:1165-1166)
+    if ((ne > 0 && cudaMemsetAsync(d->R.q_cum, 0, ne * sizeof(double), d->stream) != cudaSuccess) ||
+        cudaMemsetAsync(d->B.abstraction_cum, 0, d->R.n * sizeof(double), d->stream) != cudaSuccess ||
+        cudaMemsetAsync(d->L.qx_cum, 0, (n + 1) * sizeof(double), d->stream) != cudaSuccess ||
+        cudaMemsetAsync(d->L.qy_cum, 0, (n + 1) * sizeof(double), d->stream) != cudaSuccess)
+        return li_fail(d, WF_ERR_CUDA, "reset of the cumulative discharges failed");
     double t = 0.0;
     int64_t k = 0;
     while (t < dt) {
@@ -924,3 +944,61 @@ int32_t wf_li_domain_get(WfLiDomain* d, int32_t field, double* dst) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- coupling to the SBM step ---
+
+int wf_li_domain_couple_view(WfLiDomain* d, WfLiCoupleView* v, const int64_t** river_index_host) {
+    if (!d || !v) return WF_ERR_INVALID;
+    v->n = d->L.n;
+    v->nr_total = d->R.n;
+    v->n_active = d->R.n_active;
+    v->n_edges = d->R.n_edges;
+    v->runoff = d->runoff;
+    v->ext = d->ext;
+    v->abstraction = d->abstraction;
+    v->abstraction_cum = d->B.abstraction_cum;
+    v->h_land = d->L.h;
+    v->storage = d->L.storage;
+    v->h_river = d->R.h;
+    v->storage_river = d->R.storage;
+    v->q = d->R.q;
+    v->q_avg = d->q_avg;
+    v->qx_avg = d->qx_avg;
+    v->qy_avg = d->qy_avg;
+    v->ixd = d->L.ixd;
+    v->iyd = d->L.iyd;
+    v->river_index = d->L.river;
+    v->in_ptr = d->R.in_ptr;
+    v->in_edge = d->R.in_edge;
+    v->out_ptr = d->R.out_ptr;
+    v->out_edge = d->R.out_edge;
+    if (river_index_host) *river_index_host = d->river_index.data();
+    return WF_OK;
+}
+
+int wf_li_domain_enqueue_step(WfLiDomain* d, double dt, cudaStream_t stream) {
+    if (!d || !(dt > 0.0)) return WF_ERR_INVALID;
+    const int blocks = li_domain_blocks(d);
+    if (blocks <= 0) return li_fail(d, WF_ERR_UNSUPPORTED, "the device cannot run the cooperative sub-step loop");
+    return li_domain_launch(d, dt, stream, blocks);
+}
+
+int wf_li_domain_complete_step(WfLiDomain* d, int64_t* substeps, const char** err) {
+    if (!d) return WF_ERR_INVALID;
+    LiLoop host{};
+    if (cudaMemcpy(&host, d->loop, sizeof(LiLoop), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        if (err) *err = "read-back of the local-inertial sub-step loop failed";
+        return WF_ERR_CUDA;
+    }
+    if (host.status & 1) {
+        if (err) *err = "a grid barrier of the local-inertial sub-step loop ran out of its wait budget";
+        return WF_ERR_SPIN;
+    }
+    if (host.status & 2) {
+        if (err) *err = "more than 1e7 local-inertial sub-steps in one step";
+        return WF_ERR_INVALID;
+    }
+    d->cur = (int)((d->cur + host.substeps) & 1);
+    if (substeps) *substeps = host.substeps;
+    return WF_OK;
+}

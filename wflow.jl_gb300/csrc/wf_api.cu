@@ -19,6 +19,7 @@
 
 #include "wf_fields.cuh"
 #include "wf_kernels.h"
+#include "wf_li_couple.cuh"
 #include "wf_wave.cuh"
 #include "wf_math.cuh"
 #include "wf_plan.h"
@@ -99,6 +100,12 @@ struct WfHandle {
     double* fstage = nullptr;     // [3][n_land * M] staged forcing in external order
     double* outlets_buf = nullptr;  // [outlets * M] outlet discharge for wf_get_outlets
     int64_t nres = 0;               // reservoirs
+    std::vector<int32_t> river_land;  // [nr] land cell of each river cell
+    // local-inertial land and river routing in place of the kinematic waves
+    // (wf_attach_local_inertial; the domain stays the caller's)
+    WfLiDomain* li = nullptr;
+    WfLiCoupleView liv{};
+    int64_t li_substeps = 0;
 };
 
 namespace {
@@ -1098,6 +1105,7 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
         r_inv_len_lo[r] = r_inv_len[r] - (double)(float)r_inv_len[r];
         r_ext[r] = d->river_external_inflow ? d->river_external_inflow[r] : 0.0;
         r_area[r] = d->area[d->river_land_index[r]];
+        h->river_land.push_back(d->river_land_index[r]);
         const double wp = d->river_width[r] + d->river_bankfull_depth[r];
         r_alpha[r] = wfm::pow(d->river_manning_n[r] / wfm::sqrt_(d->river_slope[r]), 0.6) *
                      wfm::pow(wp, (2.0 / 3.0) * 0.6);
@@ -1742,6 +1750,31 @@ int32_t wf_get_reservoir_count(WfHandle* h, int64_t* n_reservoirs) {
     return WF_OK;
 }
 
+int32_t wf_attach_local_inertial(WfHandle* h, WfLiDomain* d) {
+    if (!h || !d) return set_err(h, WF_ERR_INVALID, "null argument");
+    if (h->cfg.form != WF_FORM_FP64 || h->M != 1 || h->nres > 0 || h->adaptive)
+        return set_err(h, WF_ERR_UNSUPPORTED,
+                       "local-inertial routing in the step needs the FP64 form, one member, no reservoirs and "
+                       "fixed kinematic-wave sub-steps");
+    WfLiCoupleView v{};
+    const int64_t* ri = nullptr;
+    if (wf_li_domain_couple_view(d, &v, &ri) != WF_OK) return set_err(h, WF_ERR_INVALID, "invalid domain");
+    if (v.n != h->n || v.n_active != h->nr)
+        return set_err(h, WF_ERR_INVALID, "the grid's land and active river cells must be the model's");
+    for (int64_t r = 0; r < h->nr; ++r)
+        if (ri[h->river_land[r]] != r)
+            return set_err(h, WF_ERR_INVALID, "river_index must map the land cell of river cell r to r");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaDeviceSynchronize());  // the domain's own stream may still be setting its state
+    h->li = d;
+    h->liv = v;
+    h->F.li_coupled = 1;
+    h->graph_valid = false;
+    CK(wf_fp64_li_couple_out(h->F, v, 0, launch_cfg(h)));  // the model starts from the scheme's depths
+    CK(cudaStreamSynchronize(h->stream));
+    return WF_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -1952,6 +1985,19 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         if (h->nr > 0 && (rc = wave(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
         if ((rc = res_post())) return rc;
         mark(4);
+    } else if (h->li) {
+        // local-inertial land and river routing (surface_routing.jl:62-89) after the subsurface
+        if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;
+        mark(2);
+        CK(wf_fp64_li_couple_in(h->F, h->liv, lc));
+        ++nl;
+        if ((rc = wf_li_domain_enqueue_step(h->li, h->cfg.dt, h->stream)))
+            return set_err(h, rc, "local-inertial step could not be enqueued");
+        nl += 4;
+        mark(3);
+        CK(wf_fp64_li_couple_out(h->F, h->liv, 1, lc));
+        ++nl;
+        mark(4);
     } else {
         if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;
         mark(2);
@@ -1984,7 +2030,7 @@ int run_step(WfHandle* h) {
         if (h->cfg.form == WF_FORM_SPLIT) CK(wf_split_sync_u(h->F, launch_cfg(h)));
         h->u_dirty = false;
     }
-    if (h->tuning.use_graph && !h->adaptive) {
+    if (h->tuning.use_graph && !h->adaptive && !h->li) {
         if (!h->graph_valid) {
             if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
             if (h->graph) cudaGraphDestroy(h->graph);
@@ -2013,6 +2059,18 @@ int run_step(WfHandle* h) {
     h->metrics.steps += 1;
     h->metrics.cell_steps += h->n * h->M;
     h->metrics.kernel_launches += launches;
+    if (h->li) {  // the scheme's loop status and sub-step count (one read per step)
+        CK(cudaStreamSynchronize(h->stream));
+        const char* msg = nullptr;
+        int64_t k = 0;
+        const int rc = wf_li_domain_complete_step(h->li, &k, &msg);
+        if (rc) return set_err(h, rc, msg ? msg : "local-inertial step failed");
+        h->li_substeps = k;
+        h->metrics.substeps_subsurface += (int64_t)h->h_dts_ssf.size();
+        h->metrics.substeps_land += k;
+        h->metrics.substeps_river += k;
+        return WF_OK;
+    }
     if (h->adaptive) {
         h->metrics.substeps_subsurface += h->last_substeps[WF_ADAPT_SSF];
         h->metrics.substeps_land += h->last_substeps[WF_ADAPT_LAND];
@@ -2178,6 +2236,9 @@ extern "C" int32_t wf_step_static(WfHandle* h) {
     if (h->adaptive)
         return set_err(h, WF_ERR_UNSUPPORTED,
                        "wf_step_static: adaptive sub-stepping synchronises with the host every sub-step; use wf_step");
+    if (h->li)
+        return set_err(h, WF_ERR_UNSUPPORTED,
+                       "wf_step_static: the local-inertial routing reads its loop status back every step; use wf_step");
     const size_t need = std::max(static_need(h->land, h->M), h->nr > 0 ? static_need(h->river, h->M) : (size_t)0);
     if (need > (size_t)WF_STATIC_SCRATCH_BYTES) {
         char msg[256];

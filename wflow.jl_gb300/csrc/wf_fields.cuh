@@ -161,6 +161,9 @@ struct WfDevFields {
     double g_max_rate;             // maximum snow-to-ice rate [m s-1]
     double* G[G_COUNT];            // [land slots]
     double* GM[GM_COUNT];          // [land slots * M]
+    // local-inertial land and river routing in place of the kinematic waves (wf_li_couple.cuh):
+    // the overland and river balances are the scheme's
+    int32_t li_coupled;
 };
 
 // Routing graph on the device (one per land / river graph).

@@ -32,6 +32,12 @@ cudaError_t wf_snow_transport_sweep(const WfDevFields& F, const WfDevGraph& g, c
                                     const WfLaunchCfg& c);
 cudaError_t wf_snow_in(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
 
+// Local-inertial land and river routing in the step (wf_li_couple.cuh; FP64 form, one member):
+// the scheme's inputs before its step, its results and (balance != 0) the overland balance after it.
+struct WfLiCoupleView;
+cudaError_t wf_fp64_li_couple_in(const WfDevFields& F, const WfLiCoupleView& v, const WfLaunchCfg& c);
+cudaError_t wf_fp64_li_couple_out(const WfDevFields& F, const WfLiCoupleView& v, int balance, const WfLaunchCfg& c);
+
 // FP32/FP64 split form (kernels_split.cu)
 cudaError_t wf_split_vertical(const WfDevFields& F, const WfLaunchCfg& c);
 cudaError_t wf_split_vertical_snow(const WfDevFields& F, const WfLaunchCfg& c);

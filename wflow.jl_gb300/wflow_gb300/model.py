@@ -75,6 +75,13 @@ class Model:
         self._check(self.lib.wf_set_forcing_async(self.h, *[abi.as_ptr(a) for a in arrs], arrs[0].size),
                     "wf_set_forcing_async")
 
+    def attach_local_inertial(self, domain):
+        """wf_attach_local_inertial: route the land and river by `domain` (a li_river.LiDomain over
+        this model's cells) inside every step, in place of the kinematic waves. The model keeps a
+        reference to the domain."""
+        self._check(self.lib.wf_attach_local_inertial(self.h, domain.h), "wf_attach_local_inertial")
+        self._li = domain
+
     def set_forcing_f32(self, precipitation, potential_evaporation, temperature, asynchronous=False):
         """wf_set_forcing_f32 / wf_set_forcing_async_f32: the forcing as FP32 arrays (half the bytes
         to copy; the split form computes with FP32 forcing anyway)."""

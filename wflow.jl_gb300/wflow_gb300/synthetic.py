@@ -390,3 +390,98 @@ def li_grid(nx, ny, seed=1, river_every=64, cell=100.0):
     h_land[cells] = 0.0
     runoff = np.full(n, 5e-3 / 3600.0 * cell * cell)  # 5 mm/h over every cell [m3 s-1]
     return land, river, h_river, h_land, runoff
+
+
+def li_coupling(dom, seed=1, warm=True, theta=0.8, alpha=0.7, h_thresh=1e-3):
+    """The local-inertial land grid with its river for the cells of `dom` (a square grid from
+    make_domain), as Wflow builds it for land_routing = river_routing = "local_inertial":
+    edge_indices of the staggered grid (network.jl:136-154: ind_x_up the cell at x + 1, ind_x_down
+    at x - 1, likewise y; n outside), land edge widths reduced by the river widths along the river's
+    D8 directions (set_effective_flowwidth!, utils.jl:604-680), a ghost cell after the active river
+    cells at every pit with the pit's width, length, Manning's n and bed (get_river_parameters,
+    surface_staggered_scheme.jl:40-74), bed level = bank elevation - bankfull depth, edge values as
+    RiverFlowStaggeredParameters derives them (:96-156). Returns (land, river, h_land, h_river) for
+    li_river.LiDomain / OracleModel.attach_li; `warm` starts the river 0.2-1 m deep and a few land
+    cells ponded, else dry (the ghost cells stay at 0 m)."""
+    rng = np.random.default_rng([seed, 77])
+    nx, ny, n = dom.nx, dom.ny, dom.n_land
+    idx = np.arange(n)
+    row, col = np.divmod(idx, nx)
+    cell = dom.cell_size
+    land = dict(ind_x_up=np.where(col < nx - 1, idx + 1, n), ind_x_down=np.where(col > 0, idx - 1, n),
+                ind_y_up=np.where(row < ny - 1, idx + nx, n), ind_y_down=np.where(row > 0, idx - nx, n),
+                x_length=np.full(n, cell), y_length=np.full(n, cell),
+                elevation=np.asarray(dom.land["elevation"], float).copy(),
+                mannings_n_sq=np.asarray(dom.land["land_manning_n"], float) ** 2,
+                theta=theta, h_thresh=h_thresh, alpha=alpha, froude_limit=True)
+    rl = np.asarray(dom.river["river_land_index"], np.int64)
+    rds = np.asarray(dom.river["river_downstream"], np.int64)
+    nra = len(rl)
+    river_index = np.full(n, -1, np.int64)
+    river_index[rl] = np.arange(nra)
+    land["river_index"] = river_index
+    pits = np.nonzero(rds < 0)[0]
+    ghost = np.full(nra, -1, np.int64)
+    ghost[pits] = nra + np.arange(len(pits))
+    width = np.concatenate([dom.river["river_width"], dom.river["river_width"][pits]])
+    length = np.concatenate([dom.river["river_length"], dom.river["river_length"][pits]])
+    mann = np.concatenate([dom.river["river_manning_n"], dom.river["river_manning_n"][pits]])
+    bankfull = np.concatenate([dom.river["river_bankfull_depth"], dom.river["river_bankfull_depth"][pits]])
+    bank_elev = np.concatenate([land["elevation"][rl], land["elevation"][rl[pits]]])
+    zb = bank_elev - bankfull
+    src = np.arange(nra, dtype=np.int64)  # one outgoing edge per river cell, in cell order
+    dst = np.where(rds >= 0, rds, ghost).astype(np.int64)
+    n_e = (mann[dst] * length[dst] + mann[src] * length[src]) / (length[dst] + length[src])
+    river = dict(n_active=nra, src=src, dst=dst, zb=zb, flow_length=length, flow_width=width,
+                 bankfull_depth=bankfull, zb_edge=np.maximum(zb[src], zb[dst]),
+                 width_edge=np.minimum(width[dst], width[src]), length_edge=0.5 * (length[dst] + length[src]),
+                 mannings_n_sq_edge=n_e * n_e, h_thresh=h_thresh, alpha=alpha, froude_limit=True)
+    # effective land edge widths along the river's D8 directions (PCRaster codes: x right, y down
+    # the rows; code -> (dx, dy) as Wflow's PCR_DIR)
+    pcr = {1: (-1, -1), 2: (0, -1), 3: (1, -1), 4: (-1, 0), 6: (1, 0), 7: (-1, 1), 8: (0, 1), 9: (1, 1)}
+    we_x, we_y = land["x_length"].copy(), land["y_length"].copy()
+    ldd = np.asarray(dom.ldd).reshape(-1)
+    xd, yd = land["ind_x_down"], land["ind_y_down"]
+    for v in range(nra):
+        if rds[v] < 0:
+            continue
+        w = min(width[v], width[rds[v]])
+        i = rl[v]
+        d = pcr.get(int(ldd[i]))
+        if d is None:
+            continue
+        half = 0.5 * w
+        if d == (1, 1):
+            we_x[i] = max(we_x[i] - half, 0.0)
+            we_y[i] = max(we_y[i] - half, 0.0)
+        elif d == (-1, -1):
+            if xd[i] < n:
+                we_y[xd[i]] = max(we_y[xd[i]] - half, 0.0)
+            if yd[i] < n:
+                we_x[yd[i]] = max(we_x[yd[i]] - half, 0.0)
+        elif d == (1, 0):
+            we_y[i] = max(we_y[i] - w, 0.0)
+        elif d == (0, 1):
+            we_x[i] = max(we_x[i] - w, 0.0)
+        elif d == (-1, 0):
+            if xd[i] < n:
+                we_y[xd[i]] = max(we_y[xd[i]] - w, 0.0)
+        elif d == (0, -1):
+            if yd[i] < n:
+                we_x[yd[i]] = max(we_x[yd[i]] - w, 0.0)
+        elif d == (1, -1):
+            we_y[i] = max(we_y[i] - half, 0.0)
+            if yd[i] < n:
+                we_x[yd[i]] = max(we_x[yd[i]] - half, 0.0)
+        elif d == (-1, 1):
+            if xd[i] < n:
+                we_y[xd[i]] = max(we_y[xd[i]] - half, 0.0)
+            we_x[i] = max(we_x[i] - half, 0.0)
+    land["xwidth_at_edge"], land["ywidth_at_edge"] = we_x, we_y
+    h_river = np.zeros(nra + len(pits))
+    h_land = np.zeros(n)
+    if warm:
+        h_river[:nra] = rng.uniform(0.2, 1.0, nra)
+        pond = (rng.random(n) < 0.05) & (river_index < 0)
+        h_land[pond] = rng.uniform(0.0, 0.05, int(pond.sum()))
+    return land, river, h_land, h_river
