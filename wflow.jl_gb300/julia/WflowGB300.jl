@@ -130,6 +130,7 @@ mutable struct GpuStep
     n_river::Int
     forcing::NTuple{3, Vector{Float64}}
     n_reservoirs::Int
+    li::Any                        # GpuLocalInertial routing the land and river in the step, or nothing
 end
 
 check(st, h, what) = st == 0 || error("$what failed ($st): " *
@@ -151,10 +152,16 @@ end
 
 Throw when the model uses a component outside the GPU step (the caller then keeps the
 reference's own `update_model!`): model type other than `sbm`, water demand, floodplains,
-drains, local-inertial or staggered routing, Kv profiles other than exponential /
-exponential_constant, reservoirs with tabulated curves, gravitational snow transport together
-with reservoirs. Glaciers and gravitational snow transport run on the GPU.
+drains, staggered Manning routing, local-inertial routing of the river alone or of the land alone,
+local-inertial routing with reservoirs or adaptive kinematic-wave steps, Kv profiles other than
+exponential / exponential_constant, reservoirs with tabulated curves, gravitational snow transport
+together with reservoirs. Glaciers, gravitational snow transport and local-inertial routing of the
+land with its river run on the GPU.
 """
+"Land and river both routed by the local-inertial scheme (surface_routing.jl:62-89)."
+local_inertial_both(config) = config.model.land_routing == Wflow.RoutingType.local_inertial &&
+                              config.model.river_routing == Wflow.RoutingType.local_inertial
+
 function check_supported(config)
     m = config.model
     bad = String[]
@@ -164,8 +171,12 @@ function check_supported(config)
     Wflow.do_water_demand(config) && push!(bad, "water demand")
     m.floodplain_1d__flag && push!(bad, "floodplain_1d__flag")
     m.drain__flag && push!(bad, "drain__flag")
-    m.land_routing == Wflow.RoutingType.kinematic_wave || push!(bad, "land_routing $(m.land_routing)")
-    m.river_routing == Wflow.RoutingType.kinematic_wave || push!(bad, "river_routing $(m.river_routing)")
+    kin = m.land_routing == Wflow.RoutingType.kinematic_wave && m.river_routing == Wflow.RoutingType.kinematic_wave
+    li = local_inertial_both(config)
+    (kin || li) || push!(bad, "land_routing $(m.land_routing) with river_routing $(m.river_routing)")
+    li && m.reservoir__flag && push!(bad, "local-inertial routing with reservoir__flag")
+    li && m.kinematic_wave__adaptive_time_step_flag &&
+        push!(bad, "local-inertial routing with kinematic_wave__adaptive_time_step_flag")
     m.saturated_hydraulic_conductivity_profile in (Wflow.VerticalConductivityProfile.exponential,
         Wflow.VerticalConductivityProfile.exponential_constant) ||
         push!(bad, "saturated_hydraulic_conductivity_profile $(m.saturated_hydraulic_conductivity_profile)")
@@ -200,7 +211,8 @@ function GpuStep(model)
         config.model.subsurface_kinematic_wave__alpha_coefficient, Int32(0), Int32(1), Int32(0),
         Int32(config.model.snow__flag && config.model.snow_gravitational_transport__flag),
         Int32(config.model.snow__flag && config.model.glacier__flag), ntuple(_ -> Int32(0), 5))
-    land_n = routing.overland_flow.parameters.mannings_n
+    # the kinematic-wave land roughness; unused when the local-inertial scheme routes the land
+    land_n = local_inertial_both(config) ? fill(0.072, length(ds_land)) : routing.overland_flow.parameters.mannings_n
     dom = WfDomain(length(ds_land), k(ds_land), k(lp.area), k(lp.flow_width), k(lp.flow_length),
         k(lp.surface_flow_width), k(lp.slope), k(lp.flow_fraction_to_river), k(lp.river_fraction),
         k(lp.water_fraction), k(routing.subsurface_flow.parameters.top), k(land_n), length(ds_river),
@@ -266,8 +278,15 @@ function GpuStep(model)
         cfg, dom, params, res, Int32(0), h)
     check(st, C_NULL, "wf_create_with_reservoirs")
     n = length(ds_land)
-    gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)), nres)
+    gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)), nres, nothing)
     finalizer(g -> ccall((:wf_destroy, LIB), Cvoid, (Ptr{Cvoid},), g.handle), gpu)
+    if local_inertial_both(config)
+        # the land grid with its river routes inside wf_step (wf_attach_local_inertial); the
+        # domain handle outlives the step handle through gpu.li
+        gpu.li = GpuLocalInertial(model)
+        check(ccall((:wf_attach_local_inertial, LIB), Int32, (Ptr{Cvoid}, Ptr{Cvoid}), gpu.handle, gpu.li.handle),
+            gpu.handle, "wf_attach_local_inertial")
+    end
     return gpu
 end
 
@@ -292,6 +311,7 @@ function gpu_update_model!(gpu::GpuStep, model)
     end
     check(ccall((:wf_step, LIB), Int32, (Ptr{Cvoid},), gpu.handle), gpu.handle, "wf_step")
     sync_mirrors!(gpu, model)
+    gpu.li === nothing || li_copy_back!(gpu.li, model, tosecond(model.clock.dt))
     return nothing
 end
 
@@ -313,11 +333,13 @@ end
 "Refresh the host vectors Wflow's BMI and writers read after a GPU step."
 function sync_mirrors!(gpu::GpuStep, model)
     (; routing) = model
-    get_field!(routing.river_flow.variables.q, gpu, F_RIVER_Q)
-    get_field!(routing.river_flow.variables.h, gpu, F_RIVER_H)
-    get_field!(routing.river_flow.variables.q_average, gpu, F_RIVER_Q_AVERAGE)
-    get_field!(routing.overland_flow.variables.q, gpu, 7)
-    get_field!(routing.overland_flow.variables.h, gpu, 8)
+    if gpu.li === nothing  # local-inertial routing: li_copy_back! copies the scheme's variables
+        get_field!(routing.river_flow.variables.q, gpu, F_RIVER_Q)
+        get_field!(routing.river_flow.variables.h, gpu, F_RIVER_H)
+        get_field!(routing.river_flow.variables.q_average, gpu, F_RIVER_Q_AVERAGE)
+        get_field!(routing.overland_flow.variables.q, gpu, 7)
+        get_field!(routing.overland_flow.variables.h, gpu, 8)
+    end
     get_field!(routing.subsurface_flow.variables.q, gpu, 6)
     get_field!(model.land.soil.variables.saturated_water_depth, gpu, 4)
     (; config) = model
@@ -493,6 +515,14 @@ function gpu_update_local_inertial!(gpu::GpuLocalInertial, model, dt)
     li_check(st, gpu.handle, "wf_li_domain_set_inputs")
     li_check(ccall((:wf_li_domain_step, LIB), Int32, (Ptr{Cvoid}, Float64, Ptr{Int64}), gpu.handle, dt, C_NULL),
         gpu.handle, "wf_li_domain_step")
+    li_copy_back!(gpu, model, dt)
+    return nothing
+end
+
+"The land and river variables of the local-inertial domain into the model (after its step)."
+function li_copy_back!(gpu::GpuLocalInertial, model, dt)
+    land, river = model.routing.overland_flow, model.routing.river_flow
+    rbc = river.boundary_conditions
     lv, rv = land.variables, river.variables
     n = gpu.n_land
     for (field, v) in ((LI_LAND_H, lv.h), (LI_LAND_STORAGE, lv.storage), (LI_LAND_ERROR, lv.error))
