@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define WF_ABI_VERSION 2
+#define WF_ABI_VERSION 3
 #define WF_MAX_LAYERS 8
 
 typedef enum WfStatus {
@@ -297,8 +297,10 @@ typedef struct WfTuning {
     int32_t routing_warps;    /* warps per block of the routing wavefront kernels */
     int32_t routing_blocks_per_sm;
     int32_t use_graph;        /* capture the step in a CUDA graph (1 = yes, default) */
-    int32_t reserved[4];      /* [0] wait budget (us), [1] test hook (0), [2] per-kernel timing,
-                               * [3] cap of the routing sweeps' sub-step lanes (0 = default 8) */
+    int32_t reserved[8];      /* [0] wait budget (us), [1] test hook (0), [2] per-kernel timing,
+                               * [3] cap of the routing sweeps' sub-step lanes (0 = default 8),
+                               * [4] inputs of the node-major sweeps: 0 default (staged in shared
+                               * memory), 1 staged, 2 held in registers; [5..7] 0 */
 } WfTuning;
 
 /* Library version / ABI check. */

@@ -1446,6 +1446,45 @@ struct SsfWave {
         x.qprev_zero = F.Mh[SSF_Q][e] == 0.0f;
         wfv::load_rec<true>(g, slot, x.up);
     }
+    // the same inputs staged in shared memory (wfv::walk_ring)
+    static constexpr int kWords = 15;
+    static constexpr bool kWeighted = true;
+    __device__ __forceinline__ void sources(int64_t slot, int64_t e, const void** src) const {
+        float* const* Mh = F.Mh;
+        float* const* Lf = F.Lf;
+        src[0] = &Mh[SSF_QNETF][e];
+        src[1] = &Mh[SSF_T2][e];
+        src[2] = &Mh[SSF_RDF][e];
+        src[3] = &Mh[SSF_ZIF][e];
+        src[4] = &Mh[SSF_RTH][e];
+        src[5] = &Mh[SSF_RCAP][e];
+        src[6] = &Mh[SSF_RRHO][e];
+        src[7] = &Mh[Q_MAX][e];
+        src[8] = &Lf[FLOW_WIDTH][slot];
+        src[9] = &Lf[SOIL_THICKNESS][slot];
+        src[10] = &Lf[SSF_DTDX][slot];
+        src[11] = &Lf[SSF_IDWDX][slot];
+        src[12] = &Lf[SSF_DTSY][slot];
+        src[13] = &Lf[SSF_K2][slot];
+        src[14] = &Mh[SSF_Q][e];
+    }
+    __device__ __forceinline__ void from_words(const uint32_t* w, int st, In& x) const {
+        auto f = [&](int i) { return __uint_as_float(w[i * st]); };
+        x.qnet = f(0);
+        x.t2 = f(1);
+        x.rdf = f(2);
+        x.zi = f(3);
+        x.rth = f(4);
+        x.rcap = f(5);
+        x.rrho = f(6);
+        x.qmaxdw = f(7) * f(8);
+        x.d = f(9);
+        x.dtdx = f(10);
+        x.idwdx = f(11);
+        x.dtsy = f(12);
+        x.k2 = f(13);
+        x.qprev_zero = f(14) == 0.0f;
+    }
     __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
                                          int64_t chain, bool is_end, bool heavy, unsigned long long* qh) {
         wff::ff qinff;
@@ -1534,6 +1573,30 @@ struct OlWave {
         x.alpha = F.Lf[OL_ALPHA][slot];
         x.sfw_pos = F.Lf[SFW][slot] > 0.0f;
         wfv::load_rec<true>(g, slot, x.up);
+    }
+    // the same inputs staged in shared memory (wfv::walk_ring)
+    static constexpr int kWords = 10;
+    static constexpr bool kWeighted = true;
+    __device__ __forceinline__ void sources(int64_t slot, int64_t e, const void** src) const {
+        src[0] = &F.Mh[OL_UH][e];
+        src[1] = &F.Mh[OL_UL][e];
+        src[2] = &F.Mh[OL_Q][e];
+        src[3] = &F.Ml[OL_Q][e];
+        src[4] = &F.Mh[OL_QLAT][e];
+        src[5] = &F.Ml[OL_QLAT][e];
+        src[6] = &F.Lf[INV_FLOW_LENGTH][slot];
+        src[7] = &F.Lf[INV_DX_LO][slot];
+        src[8] = &F.Lf[OL_ALPHA][slot];
+        src[9] = &F.Lf[SFW][slot];
+    }
+    __device__ __forceinline__ void from_words(const uint32_t* w, int st, In& x) const {
+        auto f = [&](int i) { return __uint_as_float(w[i * st]); };
+        x.u = {f(0), f(1)};
+        x.q = {f(2), f(3)};
+        x.qlat = {f(4), f(5)};
+        x.invdx = {f(6), f(7)};
+        x.alpha = f(8);
+        x.sfw_pos = f(9) > 0.0f;
     }
     struct St {
         wff::ff u, qp, qsum;
@@ -1627,6 +1690,35 @@ struct RvWave {
         x.ext = F.Rf[R_EXT_INFLOW][slot];
         x.res = RES ? F.res_of_rslot[slot] : -1;
         wfv::load_rec<false>(g, slot, x.up);
+    }
+    // the same inputs staged in shared memory (wfv::walk_ring)
+    static constexpr int kWords = 12;
+    static constexpr bool kWeighted = false;
+    __device__ __forceinline__ void sources(int64_t slot, int64_t e, const void** src) const {
+        float* const* RMh = F.RMh;
+        src[0] = &RMh[RV_UH][e];
+        src[1] = &RMh[RV_UL][e];
+        src[2] = &F.RMh[RV_Q][e];
+        src[3] = &F.RMl[RV_Q][e];
+        src[4] = &RMh[RV_QLATTH][e];
+        src[5] = &RMh[RV_QLATTL][e];
+        src[6] = &F.Rf[R_INV_LENGTH][slot];
+        src[7] = &F.Rf[R_INV_LEN_LO][slot];
+        src[8] = &F.Rf[R_ALPHA][slot];
+        src[9] = &F.Rf[R_LENGTH][slot];
+        src[10] = &F.Rf[R_EXT_INFLOW][slot];
+        src[11] = RES ? (const void*)&F.res_of_rslot[slot] : (const void*)&F.Rf[R_ALPHA][slot];
+    }
+    __device__ __forceinline__ void from_words(const uint32_t* w, int st, In& x) const {
+        auto f = [&](int i) { return __uint_as_float(w[i * st]); };
+        x.u = {f(0), f(1)};
+        x.q = {f(2), f(3)};
+        x.qlatt = {f(4), f(5)};
+        x.invlen = {f(6), f(7)};
+        x.alpha = f(8);
+        x.len = f(9);
+        x.ext = f(10);
+        x.res = RES ? (int32_t)w[11 * st] : -1;
     }
     struct St {
         wff::ff u, qp, qsum, asum;
@@ -1725,12 +1817,29 @@ __global__ void __launch_bounds__(128) wave_diag_kernel(Phys phys) {
 }
 
 template <class Phys>
+__global__ void __launch_bounds__(128) wave_ring_kernel(Phys phys) {
+    wfv::walk_ring(phys.g, phys.sw, phys, phys.F.status);
+}
+
+// Node-major sweeps: inputs staged in shared memory (walk_ring) unless the tuning asks for the
+// register pipeline (walk).
+template <class Phys>
 cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
-    const size_t smem = wfv::walk_smem(threads, phys.sw.S);
     int blocks;
     Phys p = phys;
     p.sw.SL = 1;
+    if (c.walk_inputs != 2) {
+        const size_t smem = wfv::ring_smem(threads, phys.sw.S, Phys::kWords);
+        cudaError_t err = cudaFuncSetAttribute(wave_ring_kernel<Phys>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+        if (err != cudaSuccess) return err;
+        err = wave_grid(wave_ring_kernel<Phys>, threads, smem, c, p.g, blocks, p.sw.prio_items);
+        if (err != cudaSuccess) return err;
+        wave_ring_kernel<Phys><<<blocks, threads, smem, c.stream>>>(p);
+        return cudaGetLastError();
+    }
+    const size_t smem = wfv::walk_smem(threads, phys.sw.S);
     cudaError_t err = wave_grid(wave_kernel<Phys>, threads, smem, c, p.g, blocks, p.sw.prio_items);
     if (err != cudaSuccess) return err;
     wave_kernel<Phys><<<blocks, threads, smem, c.stream>>>(p);

@@ -116,6 +116,8 @@ int set_err(WfHandle* h, int code, const std::string& msg) {
     return code;
 }
 
+int static_scratch(WfHandle* h, unsigned char** out);  // wf_step_static's scratch (below)
+
 #define CK(call)                                                                                   \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \
@@ -348,6 +350,7 @@ WfLaunchCfg launch_cfg(const WfHandle* h) {
     c.walk_warps = h->tuning.routing_warps;
     c.walk_blocks = h->tuning.routing_blocks_per_sm > 0 ? h->tuning.routing_blocks_per_sm * h->num_sms : 0;
     c.sub_lanes = h->tuning.reserved[3];
+    c.walk_inputs = h->tuning.reserved[4];
     return c;
 }
 
@@ -1317,6 +1320,12 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
     h->metrics.padding_slots_land = (int32_t)(PL.n_slots - n);
     if (h->adaptive) CKR(alloc_adaptive(h));
     CK(cudaDeviceSynchronize());
+    {
+        // the static scratch of wf_step_static is looked up (and its module loaded) now, at set-up,
+        // so that its first call allocates nothing even under lazy module loading
+        unsigned char* scratch = nullptr;
+        CKR(static_scratch(h, &scratch));
+    }
 #undef CKR
     *out = h;
     return WF_OK;
@@ -1691,10 +1700,14 @@ int32_t wf_set_tuning(WfHandle* h, const WfTuning* t) {
         t->routing_warps > 32 || t->routing_blocks_per_sm < 0 || t->routing_blocks_per_sm > 64)
         return set_err(h, WF_ERR_INVALID, "tuning out of range");
     if (t->reserved[3] < 0 || t->reserved[3] > 32) return set_err(h, WF_ERR_INVALID, "sub-step lanes out of range");
+    if (t->reserved[4] < 0 || t->reserved[4] > 2) return set_err(h, WF_ERR_INVALID, "sweep input mode out of range");
+    for (int k = 5; k < 8; ++k)
+        if (t->reserved[k] != 0) return set_err(h, WF_ERR_INVALID, "reserved tuning fields must be 0");
     h->tuning = *t;
     h->graph_valid = false;
     // reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset (test hooks),
-    // [2] = per-kernel event timing, [3] = cap of the routing sweeps' sub-step lanes (0 = default)
+    // [2] = per-kernel event timing, [3] = cap of the routing sweeps' sub-step lanes (0 = default),
+    // [4] = inputs of the node-major sweeps (0 / 1 staged in shared memory, 2 in registers)
     if (t->reserved[0] > 0) h->wait_ns = (uint64_t)t->reserved[0] * 1000ull;
     h->wait_offset = (uint32_t)t->reserved[1];
     h->kernel_timing = t->reserved[2] != 0;
@@ -2115,7 +2128,7 @@ std::mutex g_static_mu;
 unsigned char* g_static_ptr[kStaticMaxDevices] = {};
 
 // Device address of the static scratch on the handle's device, looked up once per device with
-// that device current (the first wf_step_static call on a device does this).
+// that device current (wf_create does this, so that wf_step_static itself allocates nothing).
 int static_scratch(WfHandle* h, unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_static_mu);
     if (h->device < 0 || h->device >= kStaticMaxDevices)

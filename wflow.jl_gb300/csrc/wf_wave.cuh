@@ -24,6 +24,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 
 #include "wf_ff.cuh"
 #include "wf_fields.cuh"
@@ -358,6 +359,199 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
             nk = nnk;
         }
         __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------- staged walk ---------------
+//
+// The walk above keeps the next positions' inputs in registers, one or two positions ahead, and a
+// position whose loads have not landed waits for them: on a long chain every position then costs
+// a memory round trip. The staged walk copies the inputs of the next RING_D positions of every
+// lane into a per-warp ring in shared memory with asynchronous copies (cp.async, one commit group
+// per position, issued whether or not the lane has work there), so a position's inputs have had
+// RING_D positions to arrive; the light children's end_q words are loaded two positions ahead from
+// the staged records. Each lane reads back only what it copied itself, so the waits are per thread
+// (cp.async.wait_group) and no barrier is involved. The computation is the node-major walk's.
+//
+// Phys staged interface:
+//   static constexpr int kWords;                          32-bit input words per position
+//   void sources(int64_t slot, int64_t e, const void** src)   their global addresses
+//   void from_words(const uint32_t* w, int stride, In&)   the inputs from the staged words (and
+//                                                         the record, set by the walk)
+//   static constexpr bool kWeighted;                      the land graph's weights (load_rec)
+constexpr int RING_D = 6;           // positions staged ahead
+constexpr int RING_R = RING_D + 1;  // ring slots (the slot refilled is the one read a position ago)
+
+__device__ __forceinline__ void cpa4(void* smem, const void* gmem) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpa16(void* smem, const void* gmem) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cpa_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Bytes of one warp's ring: per slot, kWords words of 32 lanes, then 32 records (16 B each).
+__host__ __device__ constexpr size_t ring_slot_bytes(int words) { return (size_t)words * 128 + 512; }
+__host__ __device__ constexpr size_t ring_smem(int threads, int substeps, int words) {
+    return (walk_smem(threads, substeps) + 15) / 16 * 16 + (size_t)(threads / 32) * RING_R * ring_slot_bytes(words);
+}
+
+template <class Phys>
+__device__ __forceinline__ void walk_ring(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
+    extern __shared__ unsigned long long wave_smem[];
+    constexpr int KW = Phys::kWords;
+    using In = typename Phys::In;
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long* qh = wave_smem + threadIdx.x;
+    WarpBatch* wb = reinterpret_cast<WarpBatch*>(wave_smem + (size_t)blockDim.x * sw.S) + (threadIdx.x >> 5);
+    unsigned char* const ring =
+        reinterpret_cast<unsigned char*>(wave_smem) + (walk_smem(blockDim.x, sw.S) + 15) / 16 * 16 +
+        (size_t)(threadIdx.x >> 5) * RING_R * ring_slot_bytes(KW);
+    auto words_of = [&](int r) { return reinterpret_cast<uint32_t*>(ring + (size_t)r * ring_slot_bytes(KW)); };
+    auto rec_of = [&](int r) {
+        return reinterpret_cast<int4*>(ring + (size_t)r * ring_slot_bytes(KW) + (size_t)KW * 128) + lane;
+    };
+    const int M = g.M;
+    const int gpc = M > 32 ? M / 32 : 1;
+    const int gi = M <= 32 ? (int)lane / M : 0;
+    const int64_t n_items = g.n_chunks * gpc;
+    const int64_t prio = sw.prio_items;
+    const int64_t n_norm = n_items - prio;
+    const int64_t n_short = min(g.n_short_chunks * gpc, n_norm);
+    const int64_t n_sb = (n_short + BATCH - 1) / BATCH;
+    const uint64_t n_tickets = (uint64_t)(prio + n_sb + (n_norm - n_short));
+    const int m_fixed = (int)lane % (M <= 32 ? M : 32);
+    while (true) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(g.ticket, 1ULL);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n_tickets) return;
+        int64_t first;
+        int count = 1;
+        if ((int64_t)t < prio) {
+            first = n_items - 1 - (int64_t)t;
+        } else {
+            const int64_t u = (int64_t)t - prio;
+            if (u < n_sb) {
+                first = u * BATCH;
+                count = (int)min((int64_t)BATCH, n_short - first);
+            } else {
+                first = n_short + (u - n_sb);
+            }
+        }
+        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
+        if ((int)lane < count) {
+            const int64_t item = first + lane;
+            const int64_t chunk = item / gpc;
+            wb->base[lane] = g.chunk_base[chunk];
+            wb->chain0[lane] = g.chunk_chain0[chunk];
+            wb->L[lane] = g.chunk_len[chunk];
+            wb->Gc[lane] = g.chunk_g[chunk];
+            wb->mbase[lane] = (int)(item % gpc) * 32;
+        }
+        __syncwarp();
+        int npos = 0;
+        for (int j = 0; j < count; ++j) {
+            const int Gc = wb->Gc[j];
+            wb->len[j][lane] = gi < Gc ? g.chain_len[wb->chain0[j] + gi] : 0;
+            npos += wb->L[j];
+        }
+        __syncwarp();
+        auto valid = [&](int it, int k) { return it < count && k < wb->len[it][lane]; };
+        auto slot_of = [&](int it, int k) { return wb->base[it] + (int64_t)k * wb->Gc[it] + gi; };
+        auto member = [&](int it) { return M > 32 ? wb->mbase[it] + (int)lane : m_fixed; };
+        auto advance = [&](int& it, int& k) {
+            if (k + 1 < wb->L[it]) {
+                ++k;
+            } else {
+                ++it;
+                k = 0;
+            }
+        };
+        // stage position (it, k) into ring slot r (one commit group, possibly empty)
+        auto stage = [&](int it, int k, int r) {
+            if (valid(it, k)) {
+                const int64_t sl = slot_of(it, k);
+                const void* src[KW];
+                phys.sources(sl, sl * M + member(it), src);
+                uint32_t* w = words_of(r) + lane;
+#pragma unroll
+                for (int i = 0; i < KW; ++i) cpa4(w + i * 32, src[i]);
+                cpa16(rec_of(r), &g.up_rec[sl]);
+            }
+            cpa_commit();
+        };
+        // the record of a staged position and its light children's words (issued, not awaited)
+        auto ends_of = [&](int it, int k, int r, UpRec& up, Ends& ex) {
+            if (valid(it, k)) {
+                const int64_t sl = slot_of(it, k);
+                const int4 v = *rec_of(r);
+                up.lt0 = v.x;
+                up.lt1 = v.y;
+                up.w_lt0 = Phys::kWeighted ? __int_as_float(v.z) : 1.0f;
+                up.w_lt1 = Phys::kWeighted ? __int_as_float(v.w) : 1.0f;
+                up.w_hv = Phys::kWeighted ? g.up_whv[sl] : 1.0f;
+                up.n_lt = g.up_nlt[sl];
+                load_ends(g, sw, member(it), up, ex);
+            }
+        };
+        int sit = 0, sk = 0;  // staging cursor, RING_D positions ahead of the walk
+        for (int d = 0; d < RING_D; ++d) {
+            stage(sit, sk, d);
+            if (sit < count) advance(sit, sk);
+        }
+        // the records and end words of positions 0 and 1 (groups 0 and 1 complete)
+        cpa_wait<RING_D - 2>();
+        UpRec u0, u1, u2;
+        Ends e0, e1, e2;
+        int it1 = 0, k1 = 0;
+        ends_of(0, 0, 0, u0, e0);
+        advance(it1, k1);
+        ends_of(it1, k1, 1, u1, e1);
+        int cit = 0, ck = 0, nit = it1, nk = k1;  // positions t and t + 1
+        int t2it = it1, t2k = k1;
+        if (t2it < count) advance(t2it, t2k);    // position t + 2
+        bool ok = true;
+        for (int tpos = 0; tpos < npos && cit < count; ++tpos) {
+            // groups up to position t + 2 complete: read its record and issue its end words
+            cpa_wait<RING_D - 3>();
+            ends_of(t2it, t2k, (tpos + 2) % RING_R, u2, e2);
+            // position t's inputs from its slot, then refill the slot read a position ago
+            In x;
+            if (valid(cit, ck)) {
+                phys.from_words(words_of(tpos % RING_R) + lane, 32, x);
+                x.up = u0;
+            }
+            stage(sit, sk, (tpos + RING_D) % RING_R);
+            if (sit < count) advance(sit, sk);
+            if (valid(cit, ck)) {
+                const int64_t sl = slot_of(cit, ck);
+                const int mm = member(cit);
+                ok = phys.node(x, e0, sl, sl * M + mm, mm, wb->chain0[cit] + gi, ck == wb->len[cit][lane] - 1,
+                               ck > 0, qh);
+            }
+            if (__any_sync(0xffffffffu, !ok)) break;
+            __syncwarp();
+            u0 = u1;
+            e0 = e1;
+            u1 = u2;
+            e1 = e2;
+            cit = nit;
+            ck = nk;
+            nit = t2it;
+            nk = t2k;
+            if (t2it < count) advance(t2it, t2k);
+        }
+        cpa_wait_all();  // the ring is refilled by the next ticket
+        __syncwarp();
+        if (!ok) return;
     }
 }
 

@@ -121,7 +121,7 @@ class WfReservoirs(C.Structure):
 
 class WfTuning(C.Structure):
     _fields_ = [("vertical_block", _i32), ("routing_warps", _i32), ("routing_blocks_per_sm", _i32),
-                ("use_graph", _i32), ("reserved", _i32 * 4)]
+                ("use_graph", _i32), ("reserved", _i32 * 8)]
 
 
 # WfField ids (enum WfField in the header)
