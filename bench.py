@@ -314,6 +314,18 @@ def run_gpu(args):
         set_forcing_async(s)
     model.synchronize()
     upload_ms = (time.perf_counter() - t1) / K * 1e3
+    # the same loop with the forcing already on the device (no copies): the cost of the uploads
+    # the step did not hide is e2e minus this
+    t1 = time.perf_counter()
+    for s in range(K):
+        b = resident[W + s]
+        model.set_forcing_device_slots(b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr())
+        model.step_async()
+        st = lib.wf_get_outlets(model.h, 0, C.cast(out.data_ptr(), abi._pd), n_out, C.byref(n_written))
+        if st:
+            raise RuntimeError(f"wf_get_outlets failed {st}")
+    model.synchronize()
+    loop_resident_ms = (time.perf_counter() - t1) / K * 1e3
     # ---- per-kernel times (eager launches with events between kernels) for the roofline
     model.set_tuning(**(tuning or {}), use_graph=0, kernel_timing=1)
     for s in range(min(K, 5)):
@@ -347,7 +359,8 @@ def run_gpu(args):
                    "tuning": tuning},
         "e2e": {"value": e2e_value, "unit": "cell-timesteps/s",
                 "h2d_bytes_per_step": 3 * np.dtype(fdt).itemsize * cells, "d2h_bytes_per_step": 8 * n_out,
-                "forcing_dtype": np.dtype(fdt).name, "upload_only_ms_per_step": upload_ms},
+                "forcing_dtype": np.dtype(fdt).name, "upload_only_ms_per_step": upload_ms,
+                "loop_with_resident_forcing_ms_per_step": loop_resident_ms},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": kt,
         "clocks": clk,
@@ -661,7 +674,7 @@ def run_profile(args):
     side, cell, dt, members, _ = WORKLOADS[args.workload]
     model = Model(cfg, dom, params=params)
     model.set_tuning(vertical_block=128, routing_warps=2, routing_blocks_per_sm=0, use_graph=0, kernel_timing=1,
-                     substep_lanes=args.sub_lanes)
+                     substep_lanes=args.sub_lanes, sweep_inputs=args.sweep_inputs)
     for s in range(args.steps):
         P, PET, T = member_forcing(s, dt, dom.n_land, members, pfac, seed=args.seed)
         model.run_timestep(P, PET, T)
@@ -744,6 +757,9 @@ def main():
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64 plain comparison leg")
     ap.add_argument("--sub-lanes", type=int, default=0,
                     help="profiler driver: cap of the routing sweeps' sub-step lanes (0: the library default)")
+    ap.add_argument("--sweep-inputs", type=int, default=0,
+                    help="profiler driver: inputs of the node-major sweeps (0 default, 1 staged in shared "
+                         "memory, 2 held in registers)")
     ap.add_argument("--profile", action="store_true",
                     help="profiler driver: run --steps eager steps of the workload and exit (no JSON line)")
     args = ap.parse_args()

@@ -29,6 +29,20 @@
 #include "wf_ff.cuh"
 #include "wf_wave.cuh"
 
+// Compile-time loop: fn(std::integral_constant<int, k>) for k = B, B + S, ... while k != E
+// (S = 1 or -1). The layer loops of the vertical kernel use it so that every per-layer array is
+// indexed by constants from the start and stays in registers.
+namespace wfu {
+template <int B, int E, int S, class Fn>
+__device__ __forceinline__ void static_for(Fn&& fn) {
+    if constexpr (B != E) {
+        fn(std::integral_constant<int, B>{});
+        static_for<B + S, E, S>(fn);
+    }
+}
+}  // namespace wfu
+
+
 using wfm::jclamp;
 using wfm::jmax;
 using wfm::jmin;
@@ -762,8 +776,8 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         Store us[MAXN];
         float kvf[MAXN], cexp[MAXN], rfr[MAXN];
         float usd = 0.0f;
-#pragma unroll
-        for (int k = 0; k < MAXN; ++k) {
+        wfu::static_for<0, MAXN, 1>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
             if (k < g.N) {
                 us[k].init(VF(VS_USLD_H + k, VS_USLD_H + MAXN + k));
                 kvf[k] = WS ? W32[VW_LY + 2 * MAXN + k] : F.LYf[LY_KVFRAC][k][slot];
@@ -774,7 +788,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
                 kvf[k] = cexp[k] = rfr[k] = 0.0f;
             }
             if (k < g.nl) usd += us[k].val();
-        }
+        });
         // Kv at depth z of layer n (1-based); the layer's factor is selected without dynamic
         // indexing so that the per-layer arrays stay in registers
 #define WF_KV_AT(z_, n_)                                           \
@@ -782,7 +796,9 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         float zz_ = (z_);                                          \
         if (kv_const && !(zz_ < zexp)) zz_ = zexp;                 \
         float kf_ = 0.0f;                                          \
-        _Pragma("unroll") for (int j_ = 0; j_ < MAXN; ++j_) if (j_ == (n_) - 1) kf_ = kvf[j_]; \
+        wfu::static_for<0, MAXN, 1>([&](auto jc_) {                \
+            if (decltype(jc_)::value == (n_) - 1) kf_ = kvf[decltype(jc_)::value]; \
+        });                                                        \
         return kf_ * kv0 * expf(-fsc * zz_);                       \
     }())
         float drain = (df - zif) * fmaxf(ts - tfc, 0.02f);
@@ -809,9 +825,9 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         if (g.nu > 0) {
             float z = 0.0f;
             ff flow = infil;  // inflow of the layer as a rate
-#pragma unroll
-            for (int k = 0; k < MAXN; ++k) {
-                if (k >= g.nu) continue;
+            wfu::static_for<0, MAXN, 1>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
+                if (k >= g.nu) return;
                 z += g.thick[k];
                 const float l_sat = g.thick[k] * te;
                 const float kv_z = WF_KV_AT(z, k + 1);
@@ -820,7 +836,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
                 if (u <= 0.0f) {
                     us[k].zero();
                     flow = {0.0f, 0.0f};
-                    continue;
+                    return;
                 }
                 bool drained;
                 const float rate = unsat_rate(u, kv_z, l_sat, cexp[k], dtf, drained);
@@ -830,7 +846,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
                     us[k].add_prod(-rate, dtf);
                     flow = wff::from_f(rate);
                 }
-            }
+            });
             transfer = flow;
         }
         // soil evaporation (soil.jl soil_evaporation!)
@@ -869,18 +885,18 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
             const float h3l = p_h3_low, h3h = p_h3_high;
             const float h3 = tpd <= 1.0f ? h3l : (tpd < 5.0f ? h3l + (h3h - h3l) * (tpd - 1.0f) / 4.0f : h3h);
             float sum_rf = 0.0f, rf_low = 0.0f;
-#pragma unroll
-            for (int k = 1; k <= MAXN; ++k) {
+            wfu::static_for<1, MAXN + 1, 1>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
                 if (k <= g.nu) {
                     float r = rfr[k - 1];
                     if (k == g.nu && zif < rd) r = r * (g.thick[k - 1] / fminf(g.act[k - 1], rd - g.cum[k - 1]));
                     sum_rf += r;
                     rf_low = r;
                 }
-            }
-#pragma unroll
-            for (int k = 1; k <= MAXN; ++k) {
-                if (k > g.nu) continue;
+            });
+            wfu::static_for<1, MAXN + 1, 1>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
+                if (k > g.nu) return;
                 const float r = k < g.nu ? rfr[k - 1] : rf_low;
                 const float rs_ = rd > 0.0f ? fmaxf(1.0f / sum_rf, 1.0f) * r : 0.0f;
                 const float uk = us[k - 1].val();
@@ -901,7 +917,7 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
                     actevap = wff::add(actevap, a);
                     actevap_f += a;
                 }
-            }
+            });
             const float wetroots = 1.0f / (1.0f + expf(-p_rootdistpar * (zif - rd)));
             const float alpha0 = rwu_feddes_f(0.0f, h1, h2, h3, h4, a1);
             act_sat_f = fminf((pot_trans - actevap_f) * (wetroots * alpha0), drain * inv_dtf);
@@ -916,19 +932,20 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
         // below 2e-7).
         const float cap_short = 1.0f - 1e-6f;
         float excess = 0.0f;
-#pragma unroll
-        for (int k = MAXN; k >= 1; --k) {
-            if (k > g.nu) continue;
+        wfu::static_for<MAXN, 0, -1>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            if (k > g.nu) return;
             excess = fmaxf(0.0f, us[k - 1].val() - g.thick[k - 1] * te * cap_short);
             us[k - 1].add(-excess);
-            if (k > 1) us[k - 2].add(excess);
-        }
+            if constexpr (k > 1) us[k - 2].add(excess);
+        });
         const ff act_infilt = wff::sub(infil, wff::mul(inv_dt, excess));
         const ff satex = wff::sub(wff::sub(wfs_soil, act_infilt), infex);
         usd = 0.0f;
-#pragma unroll
-        for (int k = 0; k < MAXN; ++k)
+        wfu::static_for<0, MAXN, 1>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
             if (k < g.nl) usd += us[k].val();
+        });
         ucap = p_swc - satf - usd;
         // capillary rise (soil.jl capillary_flux!)
         Store capacc;
@@ -939,15 +956,15 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
             const float rd = p_rooting_depth;
             const float chmax = p_cap_hmax;
             float capflux = zif > rd ? maxcap * powj(1.0f - fminf(zif, chmax) / chmax, p_cap_n) : 0.0f;
-#pragma unroll
-            for (int k = MAXN; k >= 1; --k) {
-                if (k > g.nu) continue;
+            wfu::static_for<MAXN, 0, -1>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
+                if (k > g.nu) return;
                 const float toadd =
                     fminf(capflux, fmaxf((g.thick[k - 1] * te * cap_short - us[k - 1].val()) * inv_dtf, 0.0f));
                 us[k - 1].add_prod(toadd, dtf);
                 capflux -= toadd;
                 capacc.add(toadd);
-            }
+            });
         }
         const ff capflux = wff::fast_two_sum(capacc.hi, capacc.lo);
         const float deepksat = WF_KV_AT(df, g.nl);
@@ -966,13 +983,14 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
             stm(F, SNOW, e, snow.value());
         }
         Mh[TSOIL][e] = tsoil;
-#pragma unroll
-        for (int k = 0; k < MAXN; ++k)
+        wfu::static_for<0, MAXN, 1>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
             if (k < g.N && us[k].changed()) {
                 const ff v = us[k].value();
                 F.LYf[LY_USLD][k][e] = v.hi;
                 F.LYl[k][e] = v.lo;
             }
+        });
         F.Mf[ZI][e] = zi;
         F.Mf[SSF_ZI][e] = zi;
         stm(F, RECHARGE, e, recharge);
