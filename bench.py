@@ -758,8 +758,8 @@ def main():
     ap.add_argument("--sub-lanes", type=int, default=0,
                     help="profiler driver: cap of the routing sweeps' sub-step lanes (0: the library default)")
     ap.add_argument("--sweep-inputs", type=int, default=0,
-                    help="profiler driver: inputs of the node-major sweeps (0 default, 1 staged in shared "
-                         "memory, 2 held in registers)")
+                    help="profiler driver: bit k keeps the inputs of node-major sweep k (0 subsurface, 1 "
+                         "overland, 2 river) in registers instead of staging them in shared memory")
     ap.add_argument("--profile", action="store_true",
                     help="profiler driver: run --steps eager steps of the workload and exit (no JSON line)")
     args = ap.parse_args()

@@ -299,8 +299,9 @@ typedef struct WfTuning {
     int32_t use_graph;        /* capture the step in a CUDA graph (1 = yes, default) */
     int32_t reserved[8];      /* [0] wait budget (us), [1] test hook (0), [2] per-kernel timing,
                                * [3] cap of the routing sweeps' sub-step lanes (0 = default 8),
-                               * [4] inputs of the node-major sweeps: 0 default (staged in shared
-                               * memory), 1 staged, 2 held in registers; [5..7] 0 */
+                               * [4] bit k set: node-major sweep k (0 subsurface, 1 overland,
+                               * 2 river) holds its inputs in registers instead of staging them
+                               * in shared memory (0 = all staged); [5..7] 0 */
 } WfTuning;
 
 /* Library version / ABI check. */

@@ -361,13 +361,16 @@ struct VStage {
 
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
     const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(gmem) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(gmem));
 }
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(a), "l"(gmem) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(a), "l"(gmem));
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// No compiler memory clobber on the copies and the commit (it would make the compiler reload every
+// shared value it holds after each copy); the wait has one, and the loop of the vertical kernel
+// puts a compiler barrier before each refill of a buffer that was read in the previous iteration.
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Stage the member fields of element e into buffer (f32, f64) of this thread (stride = block
@@ -529,8 +532,10 @@ __global__ void __launch_bounds__(256, 2) vertical_split_kernel(WfDevFields F) {
     }
     cp_async_commit();
     for (int buf = 0; e < E; e += stride, buf ^= 1) {
-        // every lane is done reading the warp buffer about to be refilled (the previous element's)
+        // every lane is done reading the warp buffer about to be refilled (the previous element's),
+        // and the compiler keeps this thread's reads of the buffer before its refill
         if (WS) __syncwarp();
+        asm volatile("" ::: "memory");
         // stage the next element while this one computes
         if (e + stride < E) {
             stage_vertical<MAXN>(F, e + stride, my32 + (buf ^ 1) * N32 * bd, my64 + (buf ^ 1) * VD_COUNT * bd, bd);
@@ -1465,6 +1470,7 @@ struct SsfWave {
         wfv::load_rec<true>(g, slot, x.up);
     }
     // the same inputs staged in shared memory (wfv::walk_ring)
+    static constexpr int kSweep = 0;  // bit of WfLaunchCfg::walk_inputs
     static constexpr int kWords = 15;
     static constexpr bool kWeighted = true;
     __device__ __forceinline__ void sources(int64_t slot, int64_t e, const void** src) const {
@@ -1593,6 +1599,7 @@ struct OlWave {
         wfv::load_rec<true>(g, slot, x.up);
     }
     // the same inputs staged in shared memory (wfv::walk_ring)
+    static constexpr int kSweep = 1;
     static constexpr int kWords = 10;
     static constexpr bool kWeighted = true;
     __device__ __forceinline__ void sources(int64_t slot, int64_t e, const void** src) const {
@@ -1710,6 +1717,7 @@ struct RvWave {
         wfv::load_rec<false>(g, slot, x.up);
     }
     // the same inputs staged in shared memory (wfv::walk_ring)
+    static constexpr int kSweep = 2;
     static constexpr int kWords = 12;
     static constexpr bool kWeighted = false;
     __device__ __forceinline__ void sources(int64_t slot, int64_t e, const void** src) const {
@@ -1840,14 +1848,14 @@ __global__ void __launch_bounds__(128) wave_ring_kernel(Phys phys) {
 }
 
 // Node-major sweeps: inputs staged in shared memory (walk_ring) unless the tuning asks for the
-// register pipeline (walk).
+// register pipeline (walk) for this sweep (bit Phys::kSweep of walk_inputs).
 template <class Phys>
 cudaError_t launch_wave(const Phys& phys, const WfLaunchCfg& c) {
     const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
     int blocks;
     Phys p = phys;
     p.sw.SL = 1;
-    if (c.walk_inputs != 2) {
+    if (!((c.walk_inputs >> Phys::kSweep) & 1)) {
         const size_t smem = wfv::ring_smem(threads, phys.sw.S, Phys::kWords);
         cudaError_t err = cudaFuncSetAttribute(wave_ring_kernel<Phys>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem);

@@ -1700,14 +1700,15 @@ int32_t wf_set_tuning(WfHandle* h, const WfTuning* t) {
         t->routing_warps > 32 || t->routing_blocks_per_sm < 0 || t->routing_blocks_per_sm > 64)
         return set_err(h, WF_ERR_INVALID, "tuning out of range");
     if (t->reserved[3] < 0 || t->reserved[3] > 32) return set_err(h, WF_ERR_INVALID, "sub-step lanes out of range");
-    if (t->reserved[4] < 0 || t->reserved[4] > 2) return set_err(h, WF_ERR_INVALID, "sweep input mode out of range");
+    if (t->reserved[4] < 0 || t->reserved[4] > 7) return set_err(h, WF_ERR_INVALID, "sweep input mask out of range");
     for (int k = 5; k < 8; ++k)
         if (t->reserved[k] != 0) return set_err(h, WF_ERR_INVALID, "reserved tuning fields must be 0");
     h->tuning = *t;
     h->graph_valid = false;
     // reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset (test hooks),
     // [2] = per-kernel event timing, [3] = cap of the routing sweeps' sub-step lanes (0 = default),
-    // [4] = inputs of the node-major sweeps (0 / 1 staged in shared memory, 2 in registers)
+    // [4] = bit k: node-major sweep k (0 subsurface, 1 overland, 2 river) keeps its inputs in
+    // registers instead of staging them in shared memory
     if (t->reserved[0] > 0) h->wait_ns = (uint64_t)t->reserved[0] * 1000ull;
     h->wait_offset = (uint32_t)t->reserved[1];
     h->kernel_timing = t->reserved[2] != 0;

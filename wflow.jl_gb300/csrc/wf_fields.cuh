@@ -171,7 +171,7 @@ struct WfDevGraph {
     int64_t n_slots;
     int64_t n_chunks;
     int64_t n_chains;
-    int64_t n_long_chunks;  // trailing chunks of the longest chains (dispatched first)
+    int64_t n_long_chunks;  // trailing chunks of the first-dispatched group (one chain each)
     int64_t n_short_chunks; // leading chunks of at most 8 positions (batched per work ticket)
     int32_t G;
     int32_t M;

@@ -12,7 +12,8 @@ struct WfLaunchCfg {
     int walk_warps;       // warps per block of wavefront kernels
     int walk_blocks;      // blocks of the persistent wavefront grid (0 = occupancy)
     int sub_lanes;        // cap of the sub-step lanes of the diagonal schedule (0 = default)
-    int walk_inputs;      // node-major sweeps' inputs: 0 / 1 staged in shared memory, 2 in registers
+    int walk_inputs;      // bit k: node-major sweep k (0 subsurface, 1 overland, 2 river) holds its inputs
+                          // in registers instead of staging them in shared memory
 };
 
 // FP64 plain form (kernels_fp64.cu)

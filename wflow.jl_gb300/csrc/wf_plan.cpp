@@ -96,15 +96,79 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
     });
     const int G = P.G;
     const int64_t nc_real = (int64_t)chains.size();
-    // The longest chains carry the critical path of every sweep; packing them G to a warp would
-    // make each of their steps pay for the divergent paths of G chains, so (when G > 1) they get
-    // a chunk of their own: chains of at least max(64, longest / 8) nodes, the 4096 longest at
-    // most. The remaining chains are packed G per chunk (padded to a multiple of G).
+    // Dispatch order. The sweeps first dispatch, all at once, the chains at the end of the order
+    // (one chain per chunk; wave_grid caps them at half the resident warps), then the others in
+    // length order, which is a dependency order (a light child is strictly shorter than its
+    // consumer), short chains batched. The first group holds up to kFirst chains: the longest
+    // ones (at least max(64, longest / 8) nodes), which carry the critical path, and then the
+    // most urgent of the rest: with one time unit per position, a chain ending at position k of
+    // its consumer must start by LS(c) = LS(consumer) + k - len(c) (a chain ending at a pit by
+    // longest - len(c)), and the chains of smallest LS are the short tributaries the critical
+    // chains would otherwise wait for while the bulk of the short chains is walked. A consumer
+    // never has a later LS than its light children and is longer, so the group holds the
+    // consumer of every chain in it. Within the group the order is by latest finish LS + len,
+    // again a dependency order (a light child finishes strictly before its consumer), the
+    // longest-finishing chain (the main stem) last, so dispatched first.
+    constexpr int64_t kFirst = 256;
     int64_t n_solo = 0;
-    if (G > 1 && nc_real > 0) {
+    if (nc_real > 0) {
         const int32_t longest = chains.back().len;
+        std::vector<int64_t> chain_of(n, -1), pos_of(n, -1);
+        for (int64_t c = 0; c < nc_real; ++c) {
+            int64_t u = chains[c].start;
+            for (int32_t k = 0; k < chains[c].len; ++k) {
+                chain_of[u] = c;
+                pos_of[u] = k;
+                u = ds[u];
+            }
+        }
+        std::vector<int64_t> ls(nc_real, 0);
+        for (int64_t c = nc_real - 1; c >= 0; --c) {  // consumers (longer) before their light children
+            const int64_t d = ds[chains[c].end];
+            ls[c] = d < 0 ? (int64_t)longest - chains[c].len : ls[chain_of[d]] + pos_of[d] - chains[c].len;
+        }
+        std::vector<char> first(nc_real, 0);
         const int32_t thr = std::max<int32_t>(64, longest / 8);
-        while (n_solo < nc_real && n_solo < 4096 && chains[nc_real - 1 - n_solo].len >= thr) ++n_solo;
+        for (int64_t c = nc_real - 1; c >= 0 && n_solo < kFirst && chains[c].len >= thr; --c) {
+            first[c] = 1;
+            ++n_solo;
+        }
+        std::vector<int64_t> by_ls(nc_real);
+        for (int64_t c = 0; c < nc_real; ++c) by_ls[c] = c;
+        std::stable_sort(by_ls.begin(), by_ls.end(), [&](int64_t x, int64_t y) {
+            return ls[x] != ls[y] ? ls[x] < ls[y] : chains[x].len > chains[y].len;
+        });
+        for (int64_t i = 0; i < nc_real && n_solo < kFirst; ++i)
+            if (!first[by_ls[i]]) {
+                first[by_ls[i]] = 1;
+                ++n_solo;
+            }
+        // the first group's consumers: the urgent prefix is closed under consumers, the long
+        // chains too (a consumer is longer); add any consumer missed at the budget's edge
+        for (bool grew = true; grew;) {
+            grew = false;
+            for (int64_t c = 0; c < nc_real; ++c) {
+                const int64_t d = ds[chains[c].end];
+                if (first[c] && d >= 0 && !first[chain_of[d]]) {
+                    first[chain_of[d]] = 1;
+                    ++n_solo;
+                    grew = true;
+                }
+            }
+        }
+        std::vector<int64_t> grp;
+        std::vector<Chain> re;
+        re.reserve(nc_real);
+        for (int64_t c = 0; c < nc_real; ++c) {
+            if (first[c]) grp.push_back(c);
+            else re.push_back(chains[c]);  // length order kept
+        }
+        std::stable_sort(grp.begin(), grp.end(), [&](int64_t x, int64_t y) {
+            const int64_t fx = ls[x] + chains[x].len, fy = ls[y] + chains[y].len;
+            return fx != fy ? fx < fy : chains[x].len < chains[y].len;
+        });
+        for (int64_t c : grp) re.push_back(chains[c]);
+        chains.swap(re);
     }
     const int64_t n_packed = nc_real - n_solo;
     const int64_t packed_chains = (n_packed + G - 1) / G * G;
@@ -133,12 +197,7 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
         P.max_len = std::max(P.max_len, mx);
     }
     P.n_slots = P.chunk_base[P.n_chunks];
-    {
-        const int32_t thr = std::max<int32_t>(64, P.max_len / 8);
-        P.n_long_chunks = 0;
-        while (P.n_long_chunks < P.n_chunks && P.chunk_len[P.n_chunks - 1 - P.n_long_chunks] >= thr)
-            ++P.n_long_chunks;
-    }
+    P.n_long_chunks = n_solo;  // the first group, dispatched first
     P.slot_of_node.assign(n, -1);
     P.node_of_slot.assign(P.n_slots, -1);
     P.chain_of_node.assign(n, -1);
@@ -181,9 +240,10 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
 }
 
 bool wf_check_plan(const WfRoutingPlan& P, const int32_t* ds, std::string& err) {
-    // chain lengths sorted (padding chains have length 0)
+    // chain lengths sorted before the first-dispatched group (padding chains have length 0);
+    // every chain waits only for chains of smaller index (checked per node below)
     int32_t prev = 0;
-    for (int64_t c = 0; c < P.n_chains; ++c) {
+    for (int64_t c = 0; c < P.n_chains - P.n_long_chunks; ++c) {
         if (P.chain_len[c] == 0) continue;
         if (P.chain_len[c] < prev) {
             err = "chains not sorted by length";

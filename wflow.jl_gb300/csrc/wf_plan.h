@@ -10,8 +10,11 @@
 // sorted by length form a valid dependency order: a lane only ever waits for chains dispatched
 // before its own, which guarantees forward progress of the persistent kernels.
 //
-// Chains are packed G per chunk (G = 32 / members for <= 32 members, else 1; the longest chains,
-// which carry the critical path, get a chunk each) and chunks are laid out
+// A first group of chains is placed at the end, one chain per chunk: the longest chains (which
+// carry the critical path) and the most urgent tributaries (smallest latest start;
+// wf_build_plan), in an order that is itself a dependency order; the sweeps dispatch them first
+// and all at once. The other chains keep the length order and are packed G per chunk (G = 32 /
+// members for <= 32 members, else 1); chunks are laid out
 // node-position-major: slot(c, k, g) = chunk_base[c] + k * G_c + g. With M members per
 // node the element index is slot * M + m, so one warp touches 32 consecutive elements at
 // every step of the walk. Every kernel of the step uses this slot layout.
@@ -29,7 +32,7 @@ struct WfRoutingPlan {
     int64_t n_chunks = 0;
     int64_t n_slots = 0;    // node slots including padding
     int32_t max_len = 0;    // longest chain = graph height + 1
-    int64_t n_long_chunks = 0;  // trailing chunks of chains of at least max(64, max_len / 8) nodes
+    int64_t n_long_chunks = 0;  // trailing chunks of the first-dispatched group (one chain each)
     std::vector<int64_t> chunk_base;    // [n_chunks + 1]
     std::vector<int32_t> chunk_len;     // [n_chunks]
     std::vector<int32_t> chunk_g;       // [n_chunks] chains in the chunk (G, or 1 for a long chain)

@@ -36,14 +36,17 @@ constexpr unsigned long long QUIET_NAN = 0x7FC000007FC00000ULL;  // published in
 constexpr int MAX_GROUP = 16;                                    // sub-steps per launch of the slim walker
 constexpr int PREFETCH_SUBSTEPS = 4;                             // light-child values prefetched per node
 
+// The relaxed loads and stores of published discharges carry no ordering duty (a consumer uses
+// only the value it reads), so they have no compiler memory clobber: a clobber would make the
+// compiler reload every shared-memory value it holds in registers after each of them.
 __device__ __forceinline__ unsigned long long ld_relaxed(const void* p) {
     unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
     return v;
 }
 __device__ __forceinline__ void st_relaxed(void* p, unsigned long long v) {
     if (v == SENTINEL) v = QUIET_NAN;
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v));
 }
 __device__ __forceinline__ uint64_t now_ns() {
     uint64_t t;
@@ -379,18 +382,22 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
 //   void from_words(const uint32_t* w, int stride, In&)   the inputs from the staged words (and
 //                                                         the record, set by the walk)
 //   static constexpr bool kWeighted;                      the land graph's weights (load_rec)
+// The copies and their commit carry no compiler memory clobber (it would force every shared
+// value held in registers to be reloaded after each copy); cp.async.wait_group has one, so the
+// reads of a slot stay after the wait that covers it, and a slot's earlier reads stay before the
+// next wait, which precedes its refill.
 constexpr int RING_D = 6;           // positions staged ahead
 constexpr int RING_R = RING_D + 1;  // ring slots (the slot refilled is the one read a position ago)
 
 __device__ __forceinline__ void cpa4(void* smem, const void* gmem) {
     const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(gmem) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(gmem));
 }
 __device__ __forceinline__ void cpa16(void* smem, const void* gmem) {
     const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(a), "l"(gmem) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(a), "l"(gmem));
 }
-__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;"); }
 template <int N>
 __device__ __forceinline__ void cpa_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
@@ -519,7 +526,12 @@ __device__ __forceinline__ void walk_ring(const WfDevGraph& g, const WfSweep& sw
         int t2it = it1, t2k = k1;
         if (t2it < count) advance(t2it, t2k);    // position t + 2
         bool ok = true;
-        for (int tpos = 0; tpos < npos && cit < count; ++tpos) {
+        int tpos = 0;
+        // One position: uc / ec hold its record and end words (issued two positions ago), u2 / e2
+        // receive those of position t + 2. The three register sets rotate by unrolling (below)
+        // rather than by copies: a copy of a register whose load is in flight would wait for it.
+        auto step = [&](UpRec& uc, Ends& ec, UpRec& u2, Ends& e2) -> bool {
+            if (tpos >= npos || cit >= count) return false;
             // groups up to position t + 2 complete: read its record and issue its end words
             cpa_wait<RING_D - 3>();
             ends_of(t2it, t2k, (tpos + 2) % RING_R, u2, e2);
@@ -527,27 +539,30 @@ __device__ __forceinline__ void walk_ring(const WfDevGraph& g, const WfSweep& sw
             In x;
             if (valid(cit, ck)) {
                 phys.from_words(words_of(tpos % RING_R) + lane, 32, x);
-                x.up = u0;
+                x.up = uc;
             }
             stage(sit, sk, (tpos + RING_D) % RING_R);
             if (sit < count) advance(sit, sk);
             if (valid(cit, ck)) {
                 const int64_t sl = slot_of(cit, ck);
                 const int mm = member(cit);
-                ok = phys.node(x, e0, sl, sl * M + mm, mm, wb->chain0[cit] + gi, ck == wb->len[cit][lane] - 1,
+                ok = phys.node(x, ec, sl, sl * M + mm, mm, wb->chain0[cit] + gi, ck == wb->len[cit][lane] - 1,
                                ck > 0, qh);
             }
-            if (__any_sync(0xffffffffu, !ok)) break;
+            if (__any_sync(0xffffffffu, !ok)) {
+                ok = false;
+                return false;
+            }
             __syncwarp();
-            u0 = u1;
-            e0 = e1;
-            u1 = u2;
-            e1 = e2;
             cit = nit;
             ck = nk;
             nit = t2it;
             nk = t2k;
             if (t2it < count) advance(t2it, t2k);
+            ++tpos;
+            return true;
+        };
+        while (step(u0, e0, u2, e2) && step(u1, e1, u0, e0) && step(u2, e2, u1, e1)) {
         }
         cpa_wait_all();  // the ring is refilled by the next ticket
         __syncwarp();

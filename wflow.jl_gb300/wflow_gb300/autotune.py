@@ -58,10 +58,24 @@ def tune(model: Model, forcing, steps=1, verbose=False):
                 print(f"sub-step lanes={lanes}: {route:.3f} ms")
             if route < best_lanes_t:
                 best_lanes, best_lanes_t = lanes, route
+    # inputs of the node-major sweeps: staged in shared memory or held in registers, per sweep
+    # (both runs time every sweep; each keeps its faster mode)
+    base = dict(vertical_block=0, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1],
+                substep_lanes=best_lanes)
+    model._tune_state = dict(base, sweep_inputs=0)
+    staged = _time_steps(model, forcing, steps)
+    model._tune_state = dict(base, sweep_inputs=7)
+    regs = _time_steps(model, forcing, steps)
+    best_inputs = sum(1 << k for k, name in enumerate(("subsurface", "overland", "river"))
+                      if regs[name] < staged[name])
+    results.append(("inputs", best_inputs, 0, 0.0))
+    if verbose:
+        print(f"sweep inputs held in registers (bit mask): {best_inputs}")
     best_block, best_block_t = 0, float("inf")
     for block in [128, 256]:
         model._tune_state = dict(vertical_block=block, routing_warps=best_route[0],
-                                 routing_blocks_per_sm=best_route[1], substep_lanes=best_lanes)
+                                 routing_blocks_per_sm=best_route[1], substep_lanes=best_lanes,
+                                 sweep_inputs=best_inputs)
         t = _time_steps(model, forcing, steps)
         results.append(("vertical", block, 0, t["vertical"]))
         if verbose:
@@ -69,7 +83,7 @@ def tune(model: Model, forcing, steps=1, verbose=False):
         if t["vertical"] < best_block_t:
             best_block, best_block_t = block, t["vertical"]
     choice = dict(vertical_block=best_block, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1],
-                  substep_lanes=best_lanes)
+                  substep_lanes=best_lanes, sweep_inputs=best_inputs)
     model._tune_state = choice
     model.set_tuning(**choice, use_graph=1)
     return choice, results

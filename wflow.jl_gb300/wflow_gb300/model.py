@@ -172,7 +172,7 @@ class Model:
         t.reserved[1] = wait_offset
         t.reserved[2] = kernel_timing
         t.reserved[3] = substep_lanes
-        t.reserved[4] = sweep_inputs  # 0 / 1: staged in shared memory, 2: held in registers
+        t.reserved[4] = sweep_inputs  # bit k: sweep k (subsurface, overland, river) keeps its inputs in registers
         self._check(self.lib.wf_set_tuning(self.h, C.byref(t)), "wf_set_tuning")
 
     def stream(self):
