@@ -50,6 +50,14 @@ int32_t wf_li_river_set_state(WfLiRiver* r, const double* h, const double* q);
  * reference's MacDonald test sets its boundary cell inside n; a Wflow model's river has its ghost
  * cells after its RiverFlowStaggeredParameters.n real cells and passes that n). */
 int32_t wf_li_river_set_timestep_cells(WfLiRiver* r, int64_t n_cells);
+/* Route by Manning's equation on the staggered grid instead (river_routing = "manning_staggered",
+ * Wflow/src/routing/surface/surface_staggered_scheme.jl:386-434): each edge takes the upstream
+ * cell's depth, q = R^(2/3) sqrt(slope) A / n above the depth threshold, limited to the upstream
+ * storage over the sub-step, and the stable sub-step is alpha length / celerity of each edge
+ * (:1050-1075). Per edge: slope [-] (Wflow clamps it at 1e-5) and Manning's n [s m-1/3], both
+ * positive; the edge bed levels given at create are the upstream cells' (compute_value_at_edge
+ * with `first`), the Manning's n squared are unused. Froude limit unused. Before the first step. */
+int32_t wf_li_river_set_manning(WfLiRiver* r, const double* slope_edge, const double* mannings_n_edge);
 /* External inflow and abstraction of every cell [m3 s-1] (RiverFlowBC.external_inflow and
  * .abstraction; NULL: zero). A negative external inflow is an abstraction limited to 80 % of the
  * storage per step. */

@@ -2235,6 +2235,11 @@ static void li_river_edges(int64_t n_edges, const int64_t* src, const int64_t* d
     }
 }
 
+static void li_river_cells(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
+                           const double* flow_length, const double* flow_width, const double* inwater, double dt,
+                           double* h, double* storage, const double* q, const double* abstraction,
+                           const double* external_inflow, double* error, double* abstraction_cum);
+
 void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
                        const double* zb, const double* flow_length, const double* flow_width, const double* inwater,
                        const double* zb_e, const double* width_e, const double* length_e, const double* nsq_e,
@@ -2243,7 +2248,54 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
                        double* error, double* abstraction_cum) {
     li_river_edges(n_edges, src, dst, zb, zb_e, width_e, length_e, nsq_e, h_thresh, froude_limit, dt, h, q, q_prev,
                    q_cum);
-    // update_water_depth_and_storage! (:723-760), edges into / out of each cell in edge order
+    li_river_cells(n, n_active, n_edges, src, dst, flow_length, flow_width, inwater, dt, h, storage, q, abstraction,
+                   external_inflow, error, abstraction_cum);
+}
+
+// Manning's equation on the staggered grid (river_routing = "manning_staggered"): the edge update
+// of update_river_channel_flow! (surface_staggered_scheme.jl:386-434; upwind depth, the
+// discharge limited to the upstream storage over dt; manning_flow, surface_process.jl:166-169),
+// then the same cell update as the local-inertial river.
+void orc_manning_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
+                            const double* flow_length, const double* flow_width, const double* inwater,
+                            const double* width_e, const double* slope_e, const double* n_e, double h_thresh,
+                            double dt, double* h, double* storage, double* q, double* q_cum, double* hf_e,
+                            const double* abstraction, const double* external_inflow, double* error,
+                            double* abstraction_cum) {
+    for (int64_t k = 0; k < n_edges; ++k) {
+        const int64_t a = src[k];
+        const double hf = h[a];
+        hf_e[k] = hf;
+        const double A = width_e[k] * hf;
+        const double R = A / (2.0 * hf + width_e[k]);
+        double qk = hf > h_thresh ? ((wcbrt(R * R) * std::sqrt(slope_e[k])) * A) / n_e[k] : 0.0;
+        qk = jmin(qk, storage[a] / dt);
+        q[k] = qk;
+        q_cum[k] += qk * dt;
+    }
+    li_river_cells(n, n_active, n_edges, src, dst, flow_length, flow_width, inwater, dt, h, storage, q, abstraction,
+                   external_inflow, error, abstraction_cum);
+}
+
+// stable_timestep of the Manning river (:1050-1075): wave celerity of a wide rectangular channel
+// at each edge's last depth, 60 s when every edge is dry
+double orc_manning_stable_timestep(int64_t n_edges, const double* width_e, const double* length_e,
+                                   const double* slope_e, const double* n_e, const double* hf_e, double alpha) {
+    double dt_min = std::numeric_limits<double>::infinity();
+    for (int64_t k = 0; k < n_edges; ++k) {
+        const double h_r = (width_e[k] * hf_e[k]) / (2.0 * hf_e[k] + width_e[k]);
+        const double celerity = ((wcbrt(h_r * h_r) * std::sqrt(slope_e[k])) / n_e[k]) / 0.6;
+        const double dt = alpha * length_e[k] / celerity;
+        dt_min = jmin(dt, dt_min);
+    }
+    return std::isinf(dt_min) ? 60.0 : dt_min;
+}
+
+// update_water_depth_and_storage! (:723-760), edges into / out of each cell in edge order
+static void li_river_cells(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
+                           const double* flow_length, const double* flow_width, const double* inwater, double dt,
+                           double* h, double* storage, const double* q, const double* abstraction,
+                           const double* external_inflow, double* error, double* abstraction_cum) {
     std::vector<double> qin(n, 0.0), qout(n, 0.0);
     for (int64_t k = 0; k < n_edges; ++k) {
         qin[dst[k]] = qin[dst[k]] + q[k];

@@ -154,6 +154,18 @@ void orc_li_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64
                        double* q_prev, double* q_cum, const double* abstraction, const double* external_inflow,
                        double* error, double* abstraction_cum);
 double orc_li_stable_timestep(int64_t n, const double* flow_length, const double* h, double alpha);
+/* Manning's equation on the staggered grid (river_routing = "manning_staggered",
+ * surface_staggered_scheme.jl:386-434, 1050-1075): one sub-step (edge discharges from the
+ * upstream depth, limited to the upstream storage over dt; hf_e keeps each edge's depth), and
+ * the stable sub-step from the edges' last depths. */
+void orc_manning_river_step(int64_t n, int64_t n_active, int64_t n_edges, const int64_t* src, const int64_t* dst,
+                            const double* flow_length, const double* flow_width, const double* inwater,
+                            const double* width_e, const double* slope_e, const double* n_e, double h_thresh,
+                            double dt, double* h, double* storage, double* q, double* q_cum, double* hf_e,
+                            const double* abstraction, const double* external_inflow, double* error,
+                            double* abstraction_cum);
+double orc_manning_stable_timestep(int64_t n_edges, const double* width_e, const double* length_e,
+                                   const double* slope_e, const double* n_e, const double* hf_e, double alpha);
 /* 2D overland local-inertial flow with a subgrid river (surface_staggered_scheme.jl:1022-1040,
  * 1202-1265, 1322-1546); 0-based indices, index n = the ghost cell outside the grid */
 double orc_li_land_stable_timestep(int64_t n, const double* x_length, const double* y_length,

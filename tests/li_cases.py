@@ -70,7 +70,19 @@ def random_river(seed, n_active=3000, n_bound=4):
     abstraction[rng.choice(n_active, size=max(2, n_active // 100), replace=False)] = rng.uniform(0.0, 8.0)
     return dict(n=n, n_active=n_active, src=src, dst=dst, zb=zb, flow_length=flow_length, flow_width=width,
                 h=h, zb_e=zb_e, w_e=w_e, l_e=l_e, nsq_e=nsq_e, inwater=inwater, external_inflow=external_inflow,
-                abstraction=abstraction)
+                abstraction=abstraction, mannings_n=mannings_n)
+
+
+def manning_edges(net):
+    """Edge slope and Manning's n of the Manning river on the staggered grid, as
+    RiverFlowStaggeredParameters derives them (surface_staggered_scheme.jl:96-156): the bed slope
+    over the mean edge length, at least 1e-5 (compute_slope_at_edge, routing/utils.jl:194-202), and
+    the length-weighted Manning's n (compute_mannings_n_at_edge)."""
+    src, dst, zb, fl, n = net["src"], net["dst"], net["zb"], net["flow_length"], net["mannings_n"]
+    length_e = 0.5 * (fl[dst] + fl[src])
+    slope_e = np.maximum((zb[src] - zb[dst]) / length_e, 1e-5)
+    n_e = (n[dst] * fl[dst] + n[src] * fl[src]) / (fl[dst] + fl[src])
+    return slope_e, n_e
 
 
 def macdonald_case(a):
@@ -129,6 +141,12 @@ class OracleLi:
     def set_timestep_cells(self, n_cells):
         self.n_dt = int(n_cells)
 
+    def set_manning(self, slope_e, n_e):
+        """Manning's equation on the staggered grid (orc_manning_river_step)."""
+        self.manning = (np.array(slope_e, float), np.array(n_e, float))
+        self.hf_e = np.zeros(self.ne)
+        self.L.orc_manning_stable_timestep.restype = C.c_double
+
     def set_state(self, h, q=None):
         """Wflow's warm start: storage of active cells = h * flow_width * flow_length."""
         self.h = np.array(h, float)
@@ -146,11 +164,24 @@ class OracleLi:
         self.abstraction = np.zeros(self.n) if abstraction is None else np.array(abstraction, float)
 
     def stable_timestep(self):
+        if getattr(self, "manning", None) is not None:
+            return self.L.orc_manning_stable_timestep(C.c_int64(self.ne), _pd(self.net["w_e"]), _pd(self.net["l_e"]),
+                                                      _pd(self.manning[0]), _pd(self.manning[1]), _pd(self.hf_e),
+                                                      C.c_double(self.alpha))
         return self.L.orc_li_stable_timestep(C.c_int64(self.n_dt), _pd(self.net["flow_length"]), _pd(self.h),
                                              C.c_double(self.alpha))
 
     def substep(self, dt):
         t = self.net
+        if getattr(self, "manning", None) is not None:
+            self.L.orc_manning_river_step(C.c_int64(self.n), C.c_int64(self.na), C.c_int64(self.ne), _pl(t["src"]),
+                                          _pl(t["dst"]), _pd(t["flow_length"]), _pd(t["flow_width"]),
+                                          _pd(self.inwater), _pd(t["w_e"]), _pd(self.manning[0]),
+                                          _pd(self.manning[1]), C.c_double(self.h_thresh), C.c_double(dt),
+                                          _pd(self.h), _pd(self.storage), _pd(self.q), _pd(self.q_cum),
+                                          _pd(self.hf_e), _pd(self.abstraction), _pd(self.external_inflow),
+                                          _pd(self.error), _pd(self.abs_cum))
+            return
         self.L.orc_li_river_step(C.c_int64(self.n), C.c_int64(self.na), C.c_int64(self.ne), _pl(t["src"]),
                                  _pl(t["dst"]), _pd(t["zb"]), _pd(t["flow_length"]), _pd(t["flow_width"]),
                                  _pd(self.inwater), _pd(t["zb_e"]), _pd(t["w_e"]), _pd(t["l_e"]), _pd(t["nsq_e"]),

@@ -200,3 +200,24 @@ def test_bench_grid_is_valid_and_matches_oracle(host_lib):
         b.substep(dt)
     for f in DOMAIN_FIELDS[:5] + DOMAIN_FIELDS[7:10]:
         assert np.array_equal(a.get(f), b.get(f)), f
+
+
+def test_manning_river_oracle_conserves_water():
+    # Manning's equation on the staggered grid (river_routing = "manning_staggered") in the oracle:
+    # discharge flows downhill only, never takes more than the upstream storage over a sub-step,
+    # and the water of the active cells changes by the inflows minus the outflow to the boundary
+    from li_cases import OracleLi, manning_edges, random_river
+    net = random_river(5, n_active=600)
+    o = OracleLi(net, alpha=0.7)
+    o.set_manning(*manning_edges(net))
+    o.set_state(net["h"])
+    o.set_inwater(net["inwater"])
+    na = net["n_active"]
+    before = o.storage[:na].sum()
+    k = o.step(3600.0)
+    assert k > 1
+    assert np.all(o.q >= 0.0) and np.all(o.storage[:na] >= 0.0)
+    to_boundary = o.q_cum[net["dst"] >= na].sum()
+    change = o.storage[:na].sum() - before
+    inflow = net["inwater"][:na].sum() * 3600.0
+    assert abs(change - (inflow - to_boundary) - o.error[:na].sum()) <= 1e-9 * (before + inflow)

@@ -346,3 +346,29 @@ def test_coupling_refuses_what_it_cannot_take(gpu_lib):
     other = synthetic.make_domain(12, 250.0, seed=9)
     with pytest.raises(RuntimeError):
         Model(synthetic.make_config(86400.0, form=abi.WF_FORM_FP64), other).attach_local_inertial(d)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("host_loop", [False, True])
+def test_manning_river_matches_oracle(gpu_lib, host_loop):
+    # river_routing = "manning_staggered": Manning's equation at the edges (upstream depth,
+    # discharge limited to the upstream storage), the edges' stable sub-step
+    from li_cases import manning_edges
+    net = random_river(7, n_active=2000)
+    slope_e, n_e = manning_edges(net)
+    gpu = _river(net)
+    gpu.set_manning(slope_e, n_e)
+    gpu.set_host_loop(host_loop)
+    orc = OracleLi(net)
+    orc.set_manning(slope_e, n_e)
+    gpu.set_state(net["h"])
+    orc.set_state(net["h"])
+    gpu.set_inwater(net["inwater"])
+    orc.set_inwater(net["inwater"])
+    gpu.set_boundary(net["external_inflow"], net["abstraction"])
+    orc.set_boundary(net["external_inflow"], net["abstraction"])
+    for s in range(3):
+        kg, ko = gpu.step(3600.0), orc.step(3600.0)
+        assert kg == ko, (s, kg, ko)
+        _assert_same(gpu, orc, f"manning step {s}")
+    assert np.all(gpu.get("q") >= 0.0)

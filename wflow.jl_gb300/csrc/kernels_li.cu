@@ -35,8 +35,10 @@ using LiDev = wfli::LiNet;
 
 __global__ void li_edge_kernel(LiDev d, double dt) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < d.n_edges;
-         k += (int64_t)gridDim.x * blockDim.x)
-        wfli::update_edge(d, k, dt);
+         k += (int64_t)gridDim.x * blockDim.x) {
+        if (d.manning) wfli::update_edge_manning(d, k, dt);
+        else wfli::update_edge(d, k, dt);
+    }
 }
 
 __global__ void li_cell_kernel(LiDev d, double dt) {
@@ -65,7 +67,11 @@ __device__ double block_min(double m, double* red) {
 __global__ void li_dt_kernel(LiDev d) {
     __shared__ double red[LI_DT_THREADS];
     double m = wfm::from_bits(INF_BITS);
-    for (int64_t i = threadIdx.x; i < d.n_dt; i += LI_DT_THREADS) m = wfm::jmin(wfli::cell_timestep(d, i), m);
+    if (d.manning)
+        for (int64_t k = threadIdx.x; k < d.n_edges; k += LI_DT_THREADS)
+            m = wfm::jmin(wfli::edge_timestep_manning(d, k), m);
+    else
+        for (int64_t i = threadIdx.x; i < d.n_dt; i += LI_DT_THREADS) m = wfm::jmin(wfli::cell_timestep(d, i), m);
     const double v = block_min(m, red);
     if (threadIdx.x == 0) *d.dt_min = wfli::finish_timestep(v);
 }
@@ -219,8 +225,9 @@ __global__ void __launch_bounds__(256) li_river_loop_kernel(LiDev d, LiLoop* s, 
         const int p = (int)(k & 1);
         double m = wfm::from_bits(INF_BITS);
         bool nan = false;
-        for (int64_t i = tid; i < d.n_dt; i += nt) {
-            const double v = wfli::cell_timestep(d, i);
+        const int64_t nv = d.manning ? d.n_edges : d.n_dt;  // Manning: the edges' sub-steps
+        for (int64_t i = tid; i < nv; i += nt) {
+            const double v = d.manning ? wfli::edge_timestep_manning(d, i) : wfli::cell_timestep(d, i);
             if (v != v) nan = true;
             else m = fmin(m, v);
         }
@@ -232,7 +239,10 @@ __global__ void __launch_bounds__(256) li_river_loop_kernel(LiDev d, LiLoop* s, 
         }
         double dt_s = wfli::finish_timestep(li_read_min(s, p, 0));
         if (t + dt_s > dt) dt_s = dt - t;
-        for (int64_t e = tid; e < d.n_edges; e += nt) wfli::update_edge(d, e, dt_s);
+        for (int64_t e = tid; e < d.n_edges; e += nt) {
+            if (d.manning) wfli::update_edge_manning(d, e, dt_s);
+            else wfli::update_edge(d, e, dt_s);
+        }
         if (!li_grid_sync(s)) return;
         for (int64_t i = tid; i < d.n_active; i += nt) wfli::update_cell(d, i, dt_s);
         t += dt_s;
@@ -559,6 +569,24 @@ void wf_li_river_destroy(WfLiRiver* r) {
 int32_t wf_li_river_set_timestep_cells(WfLiRiver* r, int64_t n_cells) {
     if (!r || n_cells < 0 || n_cells > r->d.n) return li_fail(r, WF_ERR_INVALID, "cell count out of range");
     r->d.n_dt = n_cells;
+    return WF_OK;
+}
+
+int32_t wf_li_river_set_manning(WfLiRiver* r, const double* slope_edge, const double* mannings_n_edge) {
+    if (!r || !slope_edge || !mannings_n_edge) return li_fail(r, WF_ERR_INVALID, "null argument");
+    const int64_t ne = r->d.n_edges;
+    for (int64_t k = 0; k < ne; ++k)
+        if (!(slope_edge[k] > 0.0) || !(mannings_n_edge[k] > 0.0))
+            return li_fail(r, WF_ERR_INVALID, "edge slope and Manning's n must be positive");
+    double *ps, *pn, *ph;
+    int rc;
+    if ((rc = li_upload(r, &ps, slope_edge, ne)) || (rc = li_upload(r, &pn, mannings_n_edge, ne)) ||
+        (rc = li_upload<double>(r, &ph, nullptr, ne)) || (rc = li_finish_uploads(r)))
+        return rc;
+    r->d.slope_e = ps;
+    r->d.n_e = pn;
+    r->d.hf_e = ph;
+    r->d.manning = 1;
     return WF_OK;
 }
 

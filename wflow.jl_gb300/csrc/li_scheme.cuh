@@ -32,7 +32,14 @@ struct LiNet {
     double *error, *abstraction_cum;              // river alone: clipped storage, actual abstraction [m3]
     double h_thresh, alpha;
     int32_t froude;
+    // Manning's equation on the staggered grid (river_routing = "manning_staggered") instead of
+    // the local-inertial edge update: per edge slope and Manning's n, and each edge's last depth
+    int32_t manning;
+    const double *slope_e, *n_e;
+    double* hf_e;
 };
+
+constexpr double BETA_KINWAVE = 0.6;  // Wflow.BETA_KINWAVE (routing/surface/surface_kinwave.jl:2)
 
 // local_inertial_flow for a general cross-section of area A and hydraulic radius R
 WF_HD double flow(double q0, double zs0, double zs1, double hf, double A, double R, double length, double nsq,
@@ -65,6 +72,31 @@ WF_HD void update_edge(const LiNet& d, int64_t k, double dt) {
     if (d.h[b] <= 0.0) q = wfm::jmax(q, 0.0);
     d.q[k] = q;
     d.q_cum[k] += q * dt;
+}
+
+// Manning's equation at edge k over dt (update_river_channel_flow! for ManningStaggered,
+// surface_staggered_scheme.jl:386-434): the upstream ("upwind") depth, a rectangular channel,
+// manning_flow (surface_process.jl:166-169) above the depth threshold, the discharge limited to
+// the upstream storage over dt; q dt into the cumulative discharge
+WF_HD void update_edge_manning(const LiNet& d, int64_t k, double dt) {
+    const int64_t a = d.src[k];
+    const double hf = d.h[a];
+    d.hf_e[k] = hf;
+    const double A = d.width_e[k] * hf;
+    const double R = A / (2.0 * hf + d.width_e[k]);
+    double q = hf > d.h_thresh ? ((wfm::cbrt(R * R) * wfm::sqrt_(d.slope_e[k])) * A) / d.n_e[k] : 0.0;
+    q = wfm::jmin(q, d.storage[a] / dt);
+    d.q[k] = q;
+    d.q_cum[k] += q * dt;
+}
+
+// the stable sub-step at edge k for Manning's equation (stable_timestep, :1050-1075): the wave
+// celerity of a wide rectangular channel at the edge's last depth (inf for a dry edge)
+WF_HD double edge_timestep_manning(const LiNet& d, int64_t k) {
+    const double hf = d.hf_e[k];
+    const double h_r = (d.width_e[k] * hf) / (2.0 * hf + d.width_e[k]);
+    const double celerity = ((wfm::cbrt(h_r * h_r) * wfm::sqrt_(d.slope_e[k])) / d.n_e[k]) / BETA_KINWAVE;
+    return d.alpha * d.length_e[k] / celerity;
 }
 
 // storage and depth of active cell i over dt: edge discharges, lateral inflow and abstraction,

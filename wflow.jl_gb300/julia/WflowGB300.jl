@@ -550,9 +550,10 @@ end
 """
     GpuLocalInertialRiver(model)
 
-The river of a model with `river_routing = "local_inertial"` (kinematic-wave land, no
-reservoirs, no 1D floodplain) as a `wf_li_river` handle, with the stable time step over the real
-river cells (the ghost cells follow them) and the current depths and discharges.
+The river of a model with `river_routing = "local_inertial"` or `"manning_staggered"`
+(kinematic-wave land, no reservoirs, no 1D floodplain) as a `wf_li_river` handle, with the stable
+time step over the real river cells (the ghost cells follow them) and the current depths and
+discharges.
 """
 mutable struct GpuLocalInertialRiver
     handle::Ptr{Cvoid}
@@ -564,7 +565,9 @@ end
 function GpuLocalInertialRiver(model)
     (; domain, routing, config) = model
     m = config.model
-    m.river_routing == Wflow.RoutingType.local_inertial || error("GpuLocalInertialRiver needs local-inertial rivers")
+    manning = m.river_routing == Wflow.RoutingType.manning_staggered
+    (m.river_routing == Wflow.RoutingType.local_inertial || manning) ||
+        error("GpuLocalInertialRiver needs local-inertial or staggered Manning rivers")
     (m.reservoir__flag || m.floodplain_1d__flag) &&
         error("GpuLocalInertialRiver: reservoirs and the 1D floodplain are not supported")
     river = routing.river_flow
@@ -574,7 +577,7 @@ function GpuLocalInertialRiver(model)
     keep = Any[zero_based(nae.src), zero_based(nae.dst), Float64.(rp.zb),
         pad_river(domain.river.parameters.flow_length, n_total), pad_river(domain.river.parameters.flow_width, n_total),
         copy(river.variables.h), rp.zb_at_edge, rp.flow_width_at_edge, rp.flow_length_at_edge,
-        rp.mannings_n_sq_at_edge]
+        manning ? ones(rp.n_edges) : rp.mannings_n_sq_at_edge]  # (unused by the Manning scheme)
     handle = Ref{Ptr{Cvoid}}(C_NULL)
     st = GC.@preserve keep ccall((:wf_li_river_create, LIB), Int32,
         (Int64, Int64, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
@@ -586,6 +589,11 @@ function GpuLocalInertialRiver(model)
     finalizer(x -> ccall((:wf_li_river_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.handle), gpu)
     riv_check(ccall((:wf_li_river_set_timestep_cells, LIB), Int32, (Ptr{Cvoid}, Int64), gpu.handle, rp.n),
         gpu.handle, "wf_li_river_set_timestep_cells")
+    if manning  # river_routing = "manning_staggered" (surface_staggered_scheme.jl:386-434)
+        push!(gpu.keep, rp.slope_at_edge, rp.mannings_n_at_edge)
+        riv_check(ccall((:wf_li_river_set_manning, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
+                gpu.handle, rp.slope_at_edge, rp.mannings_n_at_edge), gpu.handle, "wf_li_river_set_manning")
+    end
     riv_check(ccall((:wf_li_river_set_state, LIB), Int32, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
             gpu.handle, river.variables.h, river.variables.q), gpu.handle, "wf_li_river_set_state")
     return gpu

@@ -190,6 +190,15 @@ class LiRiver:
         passes its real cells, the ghost cells coming after them)."""
         self._check(self.lib.wf_li_river_set_timestep_cells(self.h, int(n_cells)), "wf_li_river_set_timestep_cells")
 
+    def set_manning(self, slope_edge, mannings_n_edge):
+        """Manning's equation on the staggered grid instead of the local-inertial edge update
+        (river_routing = "manning_staggered"): per edge slope and Manning's n."""
+        s_ = np.ascontiguousarray(slope_edge, np.float64)
+        n_ = np.ascontiguousarray(mannings_n_edge, np.float64)
+        if s_.shape != (self.n_edges,) or n_.shape != (self.n_edges,):
+            raise ValueError(f"edge arrays must have {self.n_edges} values")
+        self._check(self.lib.wf_li_river_set_manning(self.h, _pd(s_), _pd(n_)), "wf_li_river_set_manning")
+
     def set_boundary(self, external_inflow=None, abstraction=None):
         """External inflow and abstraction of every cell [m3 s-1] (None: zero)."""
         v = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (external_inflow, abstraction)]
