@@ -262,9 +262,14 @@ def run_gpu(args):
     # half the bytes to copy, the same state); the FP64 form takes FP64 arrays
     f32 = form == abi.WF_FORM_SPLIT
     fdt = np.float32 if f32 else np.float64
+    # an ensemble perturbs the precipitation of every member; the potential evaporation and the
+    # temperature are the same for all members, and the split form's FP32 upload takes them once
+    shared = f32 and members > 1
     host = []
     for s in range(W, W + K):
         P, PET, T = member_forcing(s, dt, n, members, pfac, seed=args.seed)
+        if shared:
+            PET, T = PET[:n], T[:n]
         pin = [torch.from_numpy(np.ascontiguousarray(x, dtype=fdt)).pin_memory() for x in (P, PET, T)]
         host.append(pin)
     # The first device access to a freshly pinned host buffer maps its pages (about 30 GB/s
@@ -283,13 +288,17 @@ def run_gpu(args):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    set_async = lib.wf_set_forcing_async_f32 if f32 else lib.wf_set_forcing_async
     ptr_t = abi._pf if f32 else abi._pd
 
     def set_forcing_async(s):
         P, PET, T = host[s]
-        st = set_async(model.h, C.cast(P.data_ptr(), ptr_t), C.cast(PET.data_ptr(), ptr_t),
-                       C.cast(T.data_ptr(), ptr_t), P.numel())
+        if f32:
+            st = lib.wf_set_forcing_counts_async_f32(model.h, C.cast(P.data_ptr(), ptr_t), P.numel(),
+                                                     C.cast(PET.data_ptr(), ptr_t), PET.numel(),
+                                                     C.cast(T.data_ptr(), ptr_t), T.numel())
+        else:
+            st = lib.wf_set_forcing_async(model.h, C.cast(P.data_ptr(), ptr_t), C.cast(PET.data_ptr(), ptr_t),
+                                          C.cast(T.data_ptr(), ptr_t), P.numel())
         if st:
             raise RuntimeError(f"wf_set_forcing_async failed {st}")
 
@@ -358,8 +367,11 @@ def run_gpu(args):
                    "max_chain_river": mt["max_chain_river"], "parallelism": f"replicas{ws}",
                    "tuning": tuning},
         "e2e": {"value": e2e_value, "unit": "cell-timesteps/s",
-                "h2d_bytes_per_step": 3 * np.dtype(fdt).itemsize * cells, "d2h_bytes_per_step": 8 * n_out,
-                "forcing_dtype": np.dtype(fdt).name, "upload_only_ms_per_step": upload_ms,
+                "h2d_bytes_per_step": sum(x.numel() * x.element_size() for x in host[0]),
+                "d2h_bytes_per_step": 8 * n_out, "forcing_dtype": np.dtype(fdt).name,
+                "forcing_layout": ("precipitation per member, potential evaporation and temperature once for "
+                                   "every member" if shared else "every array per member"),
+                "upload_only_ms_per_step": upload_ms,
                 "loop_with_resident_forcing_ms_per_step": loop_resident_ms},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": kt,

@@ -345,6 +345,15 @@ int32_t wf_set_forcing_f32(WfHandle* h, const float* precipitation, const float*
                            const float* temperature, int64_t count);
 int32_t wf_set_forcing_async_f32(WfHandle* h, const float* precipitation, const float* potential_evaporation,
                                  const float* temperature, int64_t count);
+/* The same with a count per array, each n_land * n_members (one set per member) or n_land (one set
+ * for every member): an ensemble that perturbs only the precipitation copies the potential
+ * evaporation and the temperature once. */
+int32_t wf_set_forcing_counts_f32(WfHandle* h, const float* precipitation, int64_t count_precipitation,
+                                  const float* potential_evaporation, int64_t count_potential_evaporation,
+                                  const float* temperature, int64_t count_temperature);
+int32_t wf_set_forcing_counts_async_f32(WfHandle* h, const float* precipitation, int64_t count_precipitation,
+                                        const float* potential_evaporation, int64_t count_potential_evaporation,
+                                        const float* temperature, int64_t count_temperature);
 /* Same from device pointers already in the library's slot order (see wf_get_slot_order). */
 int32_t wf_set_forcing_device_slots(WfHandle* h, const void* precipitation,
                                     const void* potential_evaporation, const void* temperature);

@@ -323,3 +323,20 @@ def test_fp32_forcing_matches_fp64_forcing(gpu_lib):
             b.update_model()
         for f in ["SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE", "SATURATED_WATER_DEPTH", "SNOW_STORAGE"]:
             assert np.array_equal(a.get_value(f), b.get_value(f)), (form, f)
+
+
+def test_fp32_forcing_with_shared_arrays(gpu_lib):
+    # wf_set_forcing_counts_(async_)f32: per-member precipitation with the potential evaporation
+    # and temperature given once for every member equals the tiled arrays
+    dom = synthetic.make_domain(24, 1000.0, seed=29)
+    M = 4
+    cfg = synthetic.make_config(86400.0, form=abi.WF_FORM_SPLIT, n_members=M)
+    a, b = Model(cfg, dom), Model(cfg, dom)
+    for s in range(3):
+        P, PET, T = (x.astype(np.float32).astype(np.float64) for x in synthetic.forcing(s, cfg.dt, dom.n_land, seed=29))
+        Pm = np.concatenate([P * f for f in (0.5, 1.0, 1.5, 2.0)])
+        a.run_timestep(Pm, np.tile(PET, M), np.tile(T, M))
+        b.set_forcing_f32(Pm, PET, T, asynchronous=s == 1)
+        b.update_model()
+    for f in ["SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE", "SNOW_STORAGE"]:
+        assert np.array_equal(a.get_value(f), b.get_value(f)), f

@@ -1382,14 +1382,13 @@ int enqueue_forcing_gathers(WfHandle* h, double* const stg_of[3], int64_t count)
 }
 
 // The gathers of FP32 forcing staged at stg[k] (count values each).
-int enqueue_forcing_gathers_f32(WfHandle* h, float* const stg[3], int64_t count) {
+int enqueue_forcing_gathers_f32(WfHandle* h, float* const stg[3], const int64_t count[3]) {
     const int dst[3] = {PRECIP, POTEVAP, TEMP};
     const int g = grid_of(h->F.land_slots * h->M, 256);
-    const int broadcast = count != h->n * h->M;
     for (int k = 0; k < 3; ++k) {
         float* d32 = h->F.split ? h->F.Mh[dst[k]] : nullptr;
         double* d64 = h->F.split ? nullptr : h->F.Mf[dst[k]];
-        if (broadcast)
+        if (count[k] != h->n * h->M)
             gather_from_f32_kernel<<<g, 256, 0, h->stream>>>(stg[k], d32, d64, h->F.land_node_of_slot,
                                                              h->F.land_slots, h->M, h->n, 1);
         else
@@ -1403,23 +1402,30 @@ int enqueue_forcing_gathers_f32(WfHandle* h, float* const stg[3], int64_t count)
 
 extern "C" {
 
-int32_t wf_set_forcing_f32(WfHandle* h, const float* P, const float* PET, const float* T, int64_t count) {
+int32_t wf_set_forcing_counts_f32(WfHandle* h, const float* P, int64_t count_p, const float* PET, int64_t count_pet,
+                                  const float* T, int64_t count_t) {
     if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
     const int64_t full = h->n * h->M;
-    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
     const float* src[3] = {P, PET, T};
+    const int64_t cnt[3] = {count_p, count_pet, count_t};
     float* stg[3];
     for (int k = 0; k < 3; ++k) {
+        if (cnt[k] != full && cnt[k] != h->n)
+            return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
         stg[k] = reinterpret_cast<float*>(h->staging + (size_t)k * std::max(h->n, h->nr) * h->M);
-        CK(cudaMemcpyAsync(stg[k], src[k], count * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(stg[k], src[k], cnt[k] * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     }
-    return enqueue_forcing_gathers_f32(h, stg, count);
+    return enqueue_forcing_gathers_f32(h, stg, cnt);
 }
 
-int32_t wf_set_forcing_async_f32(WfHandle* h, const float* P, const float* PET, const float* T, int64_t count) {
+int32_t wf_set_forcing_counts_async_f32(WfHandle* h, const float* P, int64_t count_p, const float* PET,
+                                        int64_t count_pet, const float* T, int64_t count_t) {
     if (!h || !P || !PET || !T) return set_err(h, WF_ERR_INVALID, "null forcing");
     const int64_t full = h->n * h->M;
-    if (count != full && count != h->n) return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
+    const int64_t cnt[3] = {count_p, count_pet, count_t};
+    for (int k = 0; k < 3; ++k)
+        if (cnt[k] != full && cnt[k] != h->n)
+            return set_err(h, WF_ERR_INVALID, "forcing count must be n_land*n_members or n_land");
     if (!h->copy_stream) {  // first call: copy stream, events and a staging buffer of its own
         CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&h->ev_fcopied, cudaEventDisableTiming));
@@ -1432,14 +1438,22 @@ int32_t wf_set_forcing_async_f32(WfHandle* h, const float* P, const float* PET, 
     float* stg[3];
     for (int k = 0; k < 3; ++k) {
         stg[k] = reinterpret_cast<float*>(h->fstage + (size_t)k * full);
-        CK(cudaMemcpyAsync(stg[k], src[k], count * sizeof(float), cudaMemcpyHostToDevice, h->copy_stream));
+        CK(cudaMemcpyAsync(stg[k], src[k], cnt[k] * sizeof(float), cudaMemcpyHostToDevice, h->copy_stream));
     }
     CK(cudaEventRecord(h->ev_fcopied, h->copy_stream));
     CK(cudaStreamWaitEvent(h->stream, h->ev_fcopied, 0));
-    int rc = enqueue_forcing_gathers_f32(h, stg, count);
+    int rc = enqueue_forcing_gathers_f32(h, stg, cnt);
     if (rc) return rc;
     CK(cudaEventRecord(h->ev_fconsumed, h->stream));
     return WF_OK;
+}
+
+int32_t wf_set_forcing_f32(WfHandle* h, const float* P, const float* PET, const float* T, int64_t count) {
+    return wf_set_forcing_counts_f32(h, P, count, PET, count, T, count);
+}
+
+int32_t wf_set_forcing_async_f32(WfHandle* h, const float* P, const float* PET, const float* T, int64_t count) {
+    return wf_set_forcing_counts_async_f32(h, P, count, PET, count, T, count);
 }
 
 int32_t wf_set_forcing(WfHandle* h, const double* P, const double* PET, const double* T, int64_t count) {

@@ -214,6 +214,8 @@ def _declare(lib):
         "wf_set_forcing_async": (_i32, [H, _pd, _pd, _pd, _i64]),
         "wf_set_forcing_f32": (_i32, [H, _pf, _pf, _pf, _i64]),
         "wf_set_forcing_async_f32": (_i32, [H, _pf, _pf, _pf, _i64]),
+        "wf_set_forcing_counts_f32": (_i32, [H, _pf, _i64, _pf, _i64, _pf, _i64]),
+        "wf_set_forcing_counts_async_f32": (_i32, [H, _pf, _i64, _pf, _i64, _pf, _i64]),
         "wf_set_forcing_device_slots": (_i32, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
         "wf_step": (_i32, [H]),
         "wf_step_async": (_i32, [H]),

@@ -88,8 +88,10 @@ class Model:
         arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (precipitation, potential_evaporation, temperature)]
         if asynchronous:
             self._pending_forcing = arrs
-        f = self.lib.wf_set_forcing_async_f32 if asynchronous else self.lib.wf_set_forcing_f32
-        self._check(f(self.h, *[abi.as_ptr(a, C.c_float) for a in arrs], arrs[0].size), "wf_set_forcing_f32")
+        # each array: one set per member, or one set for every member
+        f = self.lib.wf_set_forcing_counts_async_f32 if asynchronous else self.lib.wf_set_forcing_counts_f32
+        args = [x for a in arrs for x in (abi.as_ptr(a, C.c_float), a.size)]
+        self._check(f(self.h, *args), "wf_set_forcing_f32")
 
     def update_model(self):
         self._check(self.lib.wf_step(self.h), "wf_step")
