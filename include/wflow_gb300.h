@@ -301,7 +301,9 @@ typedef struct WfTuning {
                                * [3] cap of the routing sweeps' sub-step lanes (0 = default 8),
                                * [4] bit k set: node-major sweep k (0 subsurface, 1 overland,
                                * 2 river) holds its inputs in registers instead of staging them
-                               * in shared memory (0 = all staged); [5..7] 0 */
+                               * in shared memory (0 = all staged); [5] blocks per SM of the
+                               * split vertical kernel's grid-stride loop, which sets the elements
+                               * each thread walks (0 = 16); [6..7] 0 */
 } WfTuning;
 
 /* Library version / ABI check. */

@@ -180,6 +180,28 @@ def test_graph_and_eager_paths_agree(gpu_lib):
     assert a.metrics()["kernel_launches"] > 0
 
 
+def test_launch_tuning_leaves_split_results_unchanged(gpu_lib):
+    # the launch shapes the autotuner picks (resident warps, sub-step lanes, staged or register
+    # sweep inputs, the vertical kernel's block and grid) change no arithmetic of the split form
+    dom = synthetic.make_domain(48, 1000.0, seed=12)
+    M = 32
+    cfg = synthetic.make_config(3600.0, n_members=M, form=abi.WF_FORM_SPLIT)
+    a = Model(cfg, dom)
+    b = Model(cfg, dom)
+    b.set_tuning(routing_warps=2, routing_blocks_per_sm=3, substep_lanes=4, sweep_inputs=5,
+                 vertical_block=128, vertical_blocks_per_sm=1)
+    for s in range(4):
+        P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=12)
+        P, PET, T = (np.tile(x, M) for x in (P, PET, T))
+        a.run_timestep(P, PET, T)
+        b.run_timestep(P, PET, T)
+    for f in ["SATURATED_WATER_DEPTH", "SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE"]:
+        assert np.array_equal(a.get_value(f), b.get_value(f)), f
+    for bad in (dict(vertical_blocks_per_sm=-1), dict(vertical_blocks_per_sm=65), dict(sweep_inputs=8)):
+        with pytest.raises(RuntimeError):
+            b.set_tuning(**bad)
+
+
 def test_bounded_wait_reports_error_and_recovers(gpu_lib):
     # a wait on an epoch nothing publishes must end within its budget with WF_ERR_SPIN
     dom = synthetic.make_domain(16, 1000.0, seed=10)

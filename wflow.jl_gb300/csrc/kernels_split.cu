@@ -2294,7 +2294,9 @@ cudaError_t launch_vertical_split_n(const WfDevFields& F, int grid, int block, c
 template <int PHASE>
 cudaError_t launch_vertical_split(const WfDevFields& F, const WfLaunchCfg& c) {
     const int block = c.vertical_block > 0 ? c.vertical_block : 256;
-    const int grid = grid_for(F.land_slots * F.M, block, c.num_sms);
+    // blocks per SM of the grid-stride loop (tuning; each thread walks E / (grid x block) elements)
+    int grid = grid_for(F.land_slots * F.M, block, c.num_sms);
+    if (c.vertical_blocks_per_sm > 0) grid = std::min(grid, c.num_sms * c.vertical_blocks_per_sm);
     // the cell's parameters once per warp when its members fill whole warps
     const bool ws = F.M % 32 == 0 && block % 32 == 0;
     if (F.N <= 4)

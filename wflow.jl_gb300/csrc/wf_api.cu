@@ -351,6 +351,7 @@ WfLaunchCfg launch_cfg(const WfHandle* h) {
     c.walk_blocks = h->tuning.routing_blocks_per_sm > 0 ? h->tuning.routing_blocks_per_sm * h->num_sms : 0;
     c.sub_lanes = h->tuning.reserved[3];
     c.walk_inputs = h->tuning.reserved[4];
+    c.vertical_blocks_per_sm = h->tuning.reserved[5];
     return c;
 }
 
@@ -1715,14 +1716,17 @@ int32_t wf_set_tuning(WfHandle* h, const WfTuning* t) {
         return set_err(h, WF_ERR_INVALID, "tuning out of range");
     if (t->reserved[3] < 0 || t->reserved[3] > 32) return set_err(h, WF_ERR_INVALID, "sub-step lanes out of range");
     if (t->reserved[4] < 0 || t->reserved[4] > 7) return set_err(h, WF_ERR_INVALID, "sweep input mask out of range");
-    for (int k = 5; k < 8; ++k)
+    if (t->reserved[5] < 0 || t->reserved[5] > 64)
+        return set_err(h, WF_ERR_INVALID, "vertical blocks per SM out of range");
+    for (int k = 6; k < 8; ++k)
         if (t->reserved[k] != 0) return set_err(h, WF_ERR_INVALID, "reserved tuning fields must be 0");
     h->tuning = *t;
     h->graph_valid = false;
     // reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset (test hooks),
     // [2] = per-kernel event timing, [3] = cap of the routing sweeps' sub-step lanes (0 = default),
     // [4] = bit k: node-major sweep k (0 subsurface, 1 overland, 2 river) keeps its inputs in
-    // registers instead of staging them in shared memory
+    // registers instead of staging them in shared memory, [5] = blocks per SM of the split
+    // vertical kernel's grid-stride loop (0 = 16)
     if (t->reserved[0] > 0) h->wait_ns = (uint64_t)t->reserved[0] * 1000ull;
     h->wait_offset = (uint32_t)t->reserved[1];
     h->kernel_timing = t->reserved[2] != 0;

@@ -12,6 +12,7 @@ struct WfLaunchCfg {
     int walk_warps;       // warps per block of wavefront kernels
     int walk_blocks;      // blocks of the persistent wavefront grid (0 = occupancy)
     int sub_lanes;        // cap of the sub-step lanes of the diagonal schedule (0 = default)
+    int vertical_blocks_per_sm;  // grid of the split vertical kernel (0 = 16 per SM)
     int walk_inputs;      // bit k: node-major sweep k (0 subsurface, 1 overland, 2 river) holds its inputs
                           // in registers instead of staging them in shared memory
 };

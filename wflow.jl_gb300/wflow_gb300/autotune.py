@@ -4,7 +4,9 @@ The wavefront kernels are bound by the latency of the longest chain and by how m
 share an SM's FP64 pipe while the short chains drain, so the best number of resident warps
 depends on the graph (chain-length distribution) and the form; a sweep of several sub-steps also
 depends on how many lanes share a chain-member pair on the diagonal schedule (more lanes: a
-shorter critical path, fewer pairs per warp); the per-cell kernels depend on the block size. The
+shorter critical path, fewer pairs per warp), and each node-major sweep on whether its inputs are
+staged in shared memory or held in registers; the per-cell kernel depends on its block size and
+on its grid, which sets how many elements each thread walks. The
 tuner times a few steps of each candidate with per-kernel CUDA events and keeps the fastest for
 each kernel family. Candidates only change the schedule, never the result: the wavefront
 produces the same values for any dispatch order and any lane count.
@@ -71,19 +73,21 @@ def tune(model: Model, forcing, steps=1, verbose=False):
     results.append(("inputs", best_inputs, 0, 0.0))
     if verbose:
         print(f"sweep inputs held in registers (bit mask): {best_inputs}")
-    best_block, best_block_t = 0, float("inf")
-    for block in [128, 256]:
+    # the per-cell kernel: block size and grid (the elements each thread walks in its grid-stride
+    # loop: one wave of resident blocks, a few waves, or the default 16 blocks per SM)
+    best_block, best_bps, best_block_t = 0, 0, float("inf")
+    for block, vbps in itertools.product([128, 256], [0, 4, 8]):
         model._tune_state = dict(vertical_block=block, routing_warps=best_route[0],
                                  routing_blocks_per_sm=best_route[1], substep_lanes=best_lanes,
-                                 sweep_inputs=best_inputs)
+                                 sweep_inputs=best_inputs, vertical_blocks_per_sm=vbps)
         t = _time_steps(model, forcing, steps)
-        results.append(("vertical", block, 0, t["vertical"]))
+        results.append(("vertical", block, vbps, t["vertical"]))
         if verbose:
-            print(f"vertical block={block}: {t['vertical']:.3f} ms")
+            print(f"vertical block={block} blocks/SM={vbps}: {t['vertical']:.3f} ms")
         if t["vertical"] < best_block_t:
-            best_block, best_block_t = block, t["vertical"]
+            best_block, best_bps, best_block_t = block, vbps, t["vertical"]
     choice = dict(vertical_block=best_block, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1],
-                  substep_lanes=best_lanes, sweep_inputs=best_inputs)
+                  substep_lanes=best_lanes, sweep_inputs=best_inputs, vertical_blocks_per_sm=best_bps)
     model._tune_state = choice
     model.set_tuning(**choice, use_graph=1)
     return choice, results
