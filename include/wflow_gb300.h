@@ -240,7 +240,9 @@ typedef enum WfField {
 
 /* Outflow functions of a reservoir (ReservoirOutflowType, Wflow/src/routing/surface/reservoir.jl). */
 typedef enum WfReservoirOutflow {
-    WF_RES_FREE_WEIR = 2,     /* Q = b (H - H0)^e, no linked lower reservoir (reservoir.jl:482-521) */
+    WF_RES_RATING_CURVE = 1,  /* Q = f(H) from the H-Q table of the day of year (reservoir.jl:455-479);
+                               * needs WfReservoirTables */
+    WF_RES_FREE_WEIR = 2,     /* Q = b (H - H0)^e, optionally linked to a lower reservoir (reservoir.jl:482-521) */
     WF_RES_MODIFIED_PULS = 3, /* Q = b (H - H0)^2 by the modified Puls approach (reservoir.jl:424-452) */
     WF_RES_SIMPLE = 4         /* simple reservoir (reservoir.jl:389-418) */
 } WfReservoirOutflow;
@@ -269,6 +271,29 @@ typedef struct WfReservoirs {
     const double* target_minimum_fraction;  /* reservoir_water__target_min_volume_fraction */
     const double* target_full_fraction;     /* reservoir_water__target_full_volume_fraction */
 } WfReservoirs;
+
+/* Storage profiles of a reservoir (ReservoirProfileType, reservoir.jl:2). */
+typedef enum WfReservoirProfile {
+    WF_RES_PROFILE_LINEAR = 1,        /* S = A H */
+    WF_RES_PROFILE_INTERPOLATION = 2  /* S = f(H) interpolated in the S-H table (reservoir.jl:306-320) */
+} WfReservoirProfile;
+
+/* The table inputs of reservoirs (ReservoirParameters, reservoir.jl:5-44; the CSV files
+ * reservoir_sh_<id>.csv and reservoir_hq_<id>.csv read by read_sh_csv / read_hq_csv,
+ * io.jl:1129-1147) and the links between reservoirs. Tables are concatenated over the
+ * reservoirs in WfReservoirs order; reservoir k owns rows offset[k] .. offset[k + 1] - 1.
+ * Any pointer may be NULL: all profiles linear, no H-Q tables, no links. */
+typedef struct WfReservoirTables {
+    const int32_t* storage_curve_type; /* [n] WfReservoirProfile (reservoir_water__storage_curve_type_count) */
+    const int64_t* sh_offset;          /* [n + 1] rows of the S-H tables (empty for a linear profile) */
+    const double* sh_h;                /* water level H [m], strictly increasing within a table */
+    const double* sh_s;                /* storage S [m3], strictly increasing within a table */
+    const int64_t* hq_offset;          /* [n + 1] rows of the H-Q tables (empty unless outflow type 1) */
+    const double* hq_h;                /* water level H [m], strictly increasing within a table */
+    const double* hq_q;                /* [rows x 365] discharge [m3 s-1] of each day of the year, row-major */
+    const int32_t* lower_reservoir;    /* [n] linked lower reservoir (0-based index), -1 none
+                                        * (reservoir_lower_location__count) */
+} WfReservoirTables;
 
 typedef struct WfHandle WfHandle;
 
@@ -321,6 +346,18 @@ int32_t wf_create(const WfConfig* config, const WfDomain* domain, const WfParams
  * type, a non-positive area. */
 int32_t wf_create_with_reservoirs(const WfConfig* config, const WfDomain* domain, const WfParams* params,
                                   const WfReservoirs* reservoirs, int32_t device, WfHandle** out);
+/* The same with the reservoirs' tables and links (tables may be NULL). The initial storage of
+ * an interpolated profile and the maximum storage of a rating curve follow initialize_storage
+ * and get_maximum_storage (reservoir.jl:322-360). A free weir linked to a lower reservoir reads
+ * the lower reservoir's level and, when that is higher, moves water back from it within the
+ * same sub-step (reservoir.jl:482-521); the lower reservoir must lie downstream of the upper one
+ * on the river, the river paths between linked pairs must not join, and the river then routes
+ * one sub-step per sweep launch. Rejected as well: a table that is not strictly increasing in
+ * H (or in S), a rating curve without its H-Q table, an interpolated profile without its S-H
+ * table, a link to itself or out of range. */
+int32_t wf_create_with_reservoir_tables(const WfConfig* config, const WfDomain* domain, const WfParams* params,
+                                        const WfReservoirs* reservoirs, const WfReservoirTables* tables,
+                                        int32_t device, WfHandle** out);
 void wf_destroy(WfHandle* h);
 
 /* Message of the last error on this handle (or of the last failed wf_create when h is NULL). */
@@ -433,10 +470,14 @@ int32_t wf_get_sizes(WfHandle* h, int64_t* n_land, int64_t* n_river, int64_t* n_
                      int32_t* n_layers, int32_t* n_members);
 /* Number of reservoirs of a handle. */
 int32_t wf_get_reservoir_count(WfHandle* h, int64_t* n_reservoirs);
+/* Day of the year (1..365, leap days not counted) whose column of the H-Q tables the next steps
+ * read: update_index_hq! (reservoir.jl:376-382) sets it to julian_day(time - dt) before each
+ * step. Default 1. */
+int32_t wf_set_rating_curve_day(WfHandle* h, int32_t day_of_year);
 
 /* ---- diagnostics (no counterpart in the reference) ---------------------------------------
  * Size of the ABI structs for binding checks: 0 WfConfig, 1 WfDomain, 2 WfParams,
- * 3 WfMetrics, 4 WfTuning, 5 WfReservoirs; -1 otherwise. */
+ * 3 WfMetrics, 4 WfTuning, 5 WfReservoirs, 6 WfReservoirTables; -1 otherwise. */
 int32_t wf_struct_size(int32_t which);
 /* Host-only planning of a drainage graph's wavefront schedule (no GPU needed):
  * out_counts = {n_chains, n_chunks, n_slots, max_chain_len}; slot_of_node optional [n];

@@ -114,10 +114,15 @@ class Reservoir(C.Structure):
         "maximum_release", "demand", "target_minimum_fraction", "target_full_fraction",
         "external_inflow", "precipitation", "evaporation", "inflow_overland", "inflow_subsurface", "outflow_obs",
         "storage", "waterlevel", "outflow",
-        "inflow_cumulative", "outflow_cumulative", "actevap_cumulative", "abstraction_cumulative")]
+        "inflow_cumulative", "outflow_cumulative", "actevap_cumulative", "abstraction_cumulative")] + [
+        ("storage_curve_type", C.c_int32), ("lower", C.c_int32), ("sh_n", C.c_int64), ("hq_n", C.c_int64),
+        ("sh_h", C.POINTER(C.c_double)), ("sh_s", C.POINTER(C.c_double)), ("hq_h", C.POINTER(C.c_double)),
+        ("hq_q", C.POINTER(C.c_double)), ("hq_day", C.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()
+        self.storage_curve_type = 1
+        self.hq_day = 1
         nan = float("nan")
         for n in ("maximum_storage", "threshold", "rating_curve_coefficient", "rating_curve_exponent",
                   "maximum_release", "demand", "target_minimum_fraction", "target_full_fraction", "outflow_obs"):
@@ -128,6 +133,20 @@ class Reservoir(C.Structure):
 
 def reservoir_update(r, q, dt):
     lib().orc_reservoir_update(C.byref(r), C.c_double(q), C.c_double(dt))
+
+
+def reservoir_update_model(res, i, inflow, dt):
+    """update_reservoir_model!(reservoir_model, i, inflow, dt) on reservoir i (0-based) of the
+    ctypes array `res` (Reservoir * n), whose `lower` fields are 1-based indices into it."""
+    lib().orc_reservoir_update_model(res, C.c_int64(i), C.c_double(inflow), C.c_double(dt))
+
+
+def interpolate_linear(x, xp, fp):
+    xp = np.ascontiguousarray(xp, np.float64)
+    fp = np.ascontiguousarray(fp, np.float64)
+    f = lib().orc_interpolate_linear
+    f.restype = C.c_double
+    return f(C.c_double(x), xp.ctypes.data_as(_pd), fp.ctypes.data_as(_pd), C.c_int64(xp.size))
 
 
 def call_out(fname, *args, nout):
@@ -162,8 +181,10 @@ class OracleModel:
         self._reservoirs = reservoirs
         if reservoirs is not None:
             self._r = synthetic.c_reservoirs(reservoirs)
-            st = lib().orc_model_create_with_reservoirs(C.byref(cfg), C.byref(self._d), C.byref(self._p),
-                                                        C.byref(self._r), C.byref(h))
+            self._rt = synthetic.c_reservoir_tables(reservoirs)
+            st = lib().orc_model_create_with_reservoir_tables(
+                C.byref(cfg), C.byref(self._d), C.byref(self._p), C.byref(self._r),
+                C.byref(self._rt) if self._rt is not None else None, C.byref(h))
         else:
             st = lib().orc_model_create(C.byref(cfg), C.byref(self._d), C.byref(self._p), C.byref(h))
         self.h = h
@@ -183,6 +204,10 @@ class OracleModel:
     def set_forcing(self, P, PET, T):
         P, PET, T = (np.ascontiguousarray(x, dtype=np.float64) for x in (P, PET, T))
         lib().orc_model_set_forcing(self.h, P.ctypes.data_as(_pd), PET.ctypes.data_as(_pd), T.ctypes.data_as(_pd))
+
+    def set_rating_curve_day(self, day):
+        if lib().orc_model_set_rating_curve_day(self.h, int(day)) != 0:
+            raise ValueError(day)
 
     def step(self, threads=1):
         lib().orc_model_step(self.h, threads)

@@ -866,12 +866,14 @@ inline double check_timestepsize(double ts, double t, double end) { return t + t
 // ====================================================================== reservoirs ======
 //
 // Reservoir update at a river node (routing/surface/reservoir.jl:583-628), with the outflow
-// functions of types 2 (free weir, without a linked lower reservoir), 3 (modified Puls) and 4
-// (simple), the observed-outflow override (reservoir.jl:524-545) and the linear storage
-// profile (S = A H). The river-side wrapper (surface_kinwave.jl:441-489) limits a negative
-// external inflow (abstraction) to 98 % of the storage per step and forms the net inflow.
+// functions of types 1 (rating curve from an H-Q table, :455-479), 2 (free weir, with a linked
+// lower reservoir, :482-521), 3 (modified Puls, :424-452) and 4 (simple, :389-418), the
+// observed-outflow override (:524-545) and the storage profiles S = A H and S = f(H) from an
+// S-H table (:306-320, :612-621). The river-side wrapper (surface_kinwave.jl:441-489) limits a
+// negative external inflow (abstraction) to 98 % of the storage per step and forms the net
+// inflow.
 struct OrcReservoir {
-    int32_t outflow_type;  // 2 free weir, 3 modified Puls, 4 simple
+    int32_t outflow_type;  // 1 rating curve, 2 free weir, 3 modified Puls, 4 simple
     double area, maximum_storage, threshold, rating_curve_coefficient, rating_curve_exponent;
     double maximum_release, demand, target_minimum_fraction, target_full_fraction;
     // boundary conditions of the step
@@ -879,9 +881,56 @@ struct OrcReservoir {
     // state
     double storage, waterlevel, outflow;
     double inflow_cumulative, outflow_cumulative, actevap_cumulative, abstraction_cumulative;
+    // storage_curve_type: 1 (or 0) S = A H, 2 interpolated from the S-H table (sh_n rows of
+    // sh_h, sh_s); the H-Q table of outflow type 1 has hq_n rows of hq_h and 365 discharges per
+    // row (hq_q row-major), read in column hq_day (col_index_hq, 1..365); lower: the linked lower
+    // reservoir as a 1-based index into the member's reservoirs (lower_reservoir_ind), 0 none
+    int32_t storage_curve_type, lower;
+    int64_t sh_n, hq_n;
+    const double *sh_h, *sh_s, *hq_h, *hq_q;
+    int32_t hq_day;
 };
 
 namespace {
+
+// reservoir.jl:363-375 (the bounds are the minimum and maximum of the table's columns)
+double interpolate_linear(double x, const double* xp, const double* fp, int64_t n) {
+    double xmin = xp[0], xmax = xp[0], fmin = fp[0], fmax = fp[0];
+    for (int64_t i = 1; i < n; ++i) {
+        xmin = jmin(xmin, xp[i]);
+        xmax = jmax(xmax, xp[i]);
+        fmin = jmin(fmin, fp[i]);
+        fmax = jmax(fmax, fp[i]);
+    }
+    if (x <= xmin) return fmin;
+    if (x >= xmax) return fmax;
+    int64_t i1 = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (xp[i] <= x) i1 = i;
+    const int64_t i2 = i1 + 1;
+    return fp[i1] * (1.0 - (x - xp[i1]) / (xp[i2] - xp[i1])) + fp[i2] * (x - xp[i1]) / (xp[i2] - xp[i1]);
+}
+
+// Column `day` (1..365) of an H-Q table: the discharges of every row on that day.
+std::vector<double> hq_column(const OrcReservoir& r) {
+    std::vector<double> q((size_t)r.hq_n);
+    for (int64_t i = 0; i < r.hq_n; ++i) q[(size_t)i] = r.hq_q[i * 365 + (r.hq_day - 1)];
+    return q;
+}
+
+// initialize_storage (reservoir.jl:343-360)
+double initial_storage(const OrcReservoir& r) {
+    if (r.storage_curve_type == 2) return interpolate_linear(r.waterlevel, r.sh_h, r.sh_s, r.sh_n);
+    return r.area * r.waterlevel;
+}
+
+// get_maximum_storage (reservoir.jl:322-340): the storage at the highest level of the H-Q table
+double rating_curve_maximum_storage(const OrcReservoir& r) {
+    double hmax = r.hq_h[0];
+    for (int64_t i = 1; i < r.hq_n; ++i) hmax = jmax(hmax, r.hq_h[i]);
+    if (r.storage_curve_type == 2) return interpolate_linear(hmax, r.sh_h, r.sh_s, r.sh_n);
+    return r.area * hmax;
+}
 
 // reservoir.jl:389-418
 void reservoir_simple(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
@@ -915,19 +964,59 @@ void reservoir_modified_puls(const OrcReservoir& r, double precipitation, double
     storage = (si_factor - outflow) * dt;
 }
 
-// reservoir.jl:482-521 without a linked lower reservoir
-void reservoir_free_weir(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
-                         double& outflow, double& storage) {
+// reservoir.jl:455-479
+void reservoir_hq(const OrcReservoir& r, double precipitation, double evaporation, double inflow, double dt,
+                  double& outflow, double& storage) {
+    double storage_input = r.storage / dt + precipitation - evaporation + inflow;
+    const std::vector<double> q = hq_column(r);
+    outflow = interpolate_linear(r.waterlevel, r.hq_h, q.data(), r.hq_n);
+    outflow = jmin(outflow, storage_input);
+    storage = (storage_input - outflow) * dt;
+    double overflow = jmax(0.0, (storage - r.maximum_storage) / dt);
+    storage = jmin(storage, r.maximum_storage);
+    outflow += overflow;
+}
+
+// reservoir.jl:482-521. With a linked lower reservoir `lo` whose level is above this one's, the
+// flow runs back from the lower reservoir (a negative outflow), and the lower reservoir's
+// storage, level, outflow and cumulative outflow change at once.
+void reservoir_free_weir(OrcReservoir* res, int64_t i, double precipitation, double evaporation, double inflow,
+                         double dt, double& outflow, double& storage) {
+    OrcReservoir& r = res[i];
+    const bool has_lower = r.lower != 0;
+    OrcReservoir* lo = has_lower ? &res[r.lower - 1] : nullptr;
+    double diff_wl = has_lower ? r.waterlevel - lo->waterlevel : 0.0;
     double storage_input = jmax(r.storage / dt + precipitation - evaporation + inflow, 0.0);
-    if (r.waterlevel > r.threshold) {
-        double dh = r.waterlevel - r.threshold;
-        outflow = r.rating_curve_coefficient * jpow(dh, r.rating_curve_exponent);
-        double maxflow = dh * r.area / dt;
-        outflow = jmin(outflow, maxflow);
+    if (diff_wl >= 0.0) {
+        if (r.waterlevel > r.threshold) {
+            double dh = r.waterlevel - r.threshold;
+            outflow = r.rating_curve_coefficient * jpow(dh, r.rating_curve_exponent);
+            double maxflow = dh * r.area / dt;
+            outflow = jmin(outflow, maxflow);
+        } else {
+            outflow = 0.0;
+        }
     } else {
-        outflow = 0.0;
+        if (lo->waterlevel > r.threshold) {
+            double dh = lo->waterlevel - r.threshold;
+            outflow = -r.rating_curve_coefficient * jpow(dh, r.rating_curve_exponent);
+            double maxflow = dh * lo->area / dt;
+            outflow = jmax(outflow, -maxflow);
+        } else {
+            outflow = 0.0;
+        }
     }
     storage = (storage_input - outflow) * dt;
+    if (diff_wl < 0.0) {
+        double lower_res_storage = lo->storage + outflow * dt;
+        double lower_res_waterlevel = lo->storage_curve_type == 2
+                                          ? interpolate_linear(lower_res_storage, lo->sh_s, lo->sh_h, lo->sh_n)
+                                          : lo->waterlevel + (lower_res_storage - lo->storage) / lo->area;
+        lo->outflow = -outflow;
+        lo->outflow_cumulative -= outflow * dt;
+        lo->storage = lower_res_storage;
+        lo->waterlevel = lower_res_waterlevel;
+    }
 }
 
 // reservoir.jl:524-545
@@ -943,18 +1032,21 @@ void reservoir_outflow_obs(const OrcReservoir& r, double precipitation, double e
     }
 }
 
-// reservoir.jl:583-628
-void update_reservoir(OrcReservoir& r, double inflow, double dt) {
+// reservoir.jl:583-628, reservoir i of the member's reservoirs `res`
+void update_reservoir(OrcReservoir* res, int64_t i, double inflow, double dt) {
+    OrcReservoir& r = res[i];
     double precipitation = r.precipitation * r.area;
     double available_storage = r.storage + (inflow + precipitation) * dt;
     double potential_evaporation = r.evaporation * r.area;
     double evaporation = jmin(available_storage / dt, potential_evaporation);
     double outflow = 0.0, storage = r.storage;
     if (!std::isnan(r.outflow_obs)) reservoir_outflow_obs(r, precipitation, evaporation, inflow, dt, outflow, storage);
-    else if (r.outflow_type == 2) reservoir_free_weir(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else if (r.outflow_type == 1) reservoir_hq(r, precipitation, evaporation, inflow, dt, outflow, storage);
+    else if (r.outflow_type == 2) reservoir_free_weir(res, i, precipitation, evaporation, inflow, dt, outflow, storage);
     else if (r.outflow_type == 3) reservoir_modified_puls(r, precipitation, evaporation, inflow, dt, outflow, storage);
     else reservoir_simple(r, precipitation, evaporation, inflow, dt, outflow, storage);
-    double waterlevel = r.waterlevel + (storage - r.storage) / r.area;  // linear profile
+    double waterlevel = r.storage_curve_type == 2 ? interpolate_linear(storage, r.sh_s, r.sh_h, r.sh_n)
+                                                  : r.waterlevel + (storage - r.storage) / r.area;
     r.storage = storage;
     r.waterlevel = waterlevel;
     r.outflow = outflow;
@@ -963,8 +1055,9 @@ void update_reservoir(OrcReservoir& r, double inflow, double dt) {
     r.actevap_cumulative += evaporation / r.area * dt;
 }
 
-// surface_kinwave.jl:441-489: net inflow of the reservoir at a river node whose discharge is q
-void update_reservoir_at_node(OrcReservoir& r, double q, double dt) {
+// surface_kinwave.jl:441-489: net inflow of reservoir i at a river node whose discharge is q
+void update_reservoir_at_node(OrcReservoir* res, int64_t i, double q, double dt) {
+    OrcReservoir& r = res[i];
     double inflow;
     if (r.external_inflow < 0.0) {
         double abstraction = jmin(-r.external_inflow, (r.storage / dt) * 0.98);
@@ -974,7 +1067,7 @@ void update_reservoir_at_node(OrcReservoir& r, double q, double dt) {
         inflow = r.external_inflow;
     }
     double net_inflow = q + r.inflow_overland + r.inflow_subsurface + inflow;
-    update_reservoir(r, net_inflow, dt);
+    update_reservoir(res, i, net_inflow, dt);
 }
 
 }  // namespace
@@ -1045,6 +1138,8 @@ struct OrcModel {
     // reservoirs (member-major [mbr * nres + k])
     int64_t nres = 0;
     std::vector<OrcReservoir> res;
+    std::vector<double> res_tables;          // the reservoirs' S-H and H-Q tables (OrcReservoir points here)
+    std::vector<int64_t> res_sh_at, res_hq_at;  // [nres] start of each reservoir's tables
     std::vector<int32_t> res_of_river;  // [nr] reservoir at a river cell, or -1
     std::vector<int32_t> res_land;      // [nres] land cell of the reservoir outlet
     std::vector<double> res_out_avg, res_in_avg, res_evap_avg, res_abs_avg, res_prev, res_err, res_rel;
@@ -1521,6 +1616,15 @@ int32_t orc_topo_order_dfs(int64_t n, const int32_t* ds, int64_t* order) {
 // utils.jl:61-71); the topological orders stay those of the full graphs, which remain valid.
 int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p,
                                          const WfReservoirs* rs, OrcModel** out) {
+    return orc_model_create_with_reservoir_tables(c, d, p, rs, nullptr, out);
+}
+
+// The same with the reservoirs' S-H and H-Q tables and links (ReservoirParameters,
+// reservoir.jl:5-44, 152-192): the tables are copied into the model; a linked lower reservoir
+// is stored 1-based (lower_reservoir_ind).
+int32_t orc_model_create_with_reservoir_tables(const WfConfig* c, const WfDomain* d, const WfParams* p,
+                                               const WfReservoirs* rs, const WfReservoirTables* tb,
+                                               OrcModel** out) {
     int32_t st = orc_model_create(c, d, p, out);
     if (st != WF_OK || !rs || rs->n == 0) return st;
     OrcModel* m = *out;
@@ -1544,7 +1648,7 @@ int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, c
         if (m->r_ds[v] < 0) return fail("a reservoir without a downstream river node is not supported");
         if (fed[m->r_ds[v]] >= 0) return fail("two reservoirs drain into one river cell");
         const int32_t t = rs->outflow_curve_type[k];
-        if (t != 2 && t != 3 && t != 4) return fail("unsupported reservoir outflow type");
+        if (t < 1 || t > 4) return fail("unsupported reservoir outflow type");
         if (!(rs->area[k] > 0.0)) return fail("reservoir area must be positive");
         fed[m->r_ds[v]] = (int32_t)k;
         m->res_of_river[v] = (int32_t)k;
@@ -1560,6 +1664,49 @@ int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, c
     build_ups(nr, rds_cut.data(), m->r_ups);
     const double NaN = std::numeric_limits<double>::quiet_NaN();
     auto par = [&](const double* a, int64_t k) { return a ? a[k] : NaN; };
+    // tables: per reservoir the S-H table (H then S) and the H-Q table (H then Q), copied
+    m->res_sh_at.assign(nres, 0);
+    m->res_hq_at.assign(nres, 0);
+    m->res_tables.clear();
+    if (tb) {
+        auto increasing = [](const double* v, int64_t a, int64_t b) {
+            for (int64_t i = a + 1; i < b; ++i)
+                if (!(v[i] > v[i - 1])) return false;
+            for (int64_t i = a; i < b; ++i)
+                if (!std::isfinite(v[i])) return false;
+            return true;
+        };
+        for (int64_t k = 0; k < nres; ++k) {
+            const int32_t prof = tb->storage_curve_type ? tb->storage_curve_type[k] : 1;
+            if (prof != 1 && prof != 2) return fail("unknown reservoir storage curve type");
+            if (prof == 2) {
+                if (!tb->sh_offset || !tb->sh_h || !tb->sh_s) return fail("reservoir S-H tables missing");
+                const int64_t a = tb->sh_offset[k], b = tb->sh_offset[k + 1];
+                if (a < 0 || b <= a) return fail("empty reservoir S-H table");
+                if (!increasing(tb->sh_h, a, b) || !increasing(tb->sh_s, a, b))
+                    return fail("reservoir S-H table not strictly increasing");
+                m->res_sh_at[k] = (int64_t)m->res_tables.size();
+                m->res_tables.insert(m->res_tables.end(), tb->sh_h + a, tb->sh_h + b);
+                m->res_tables.insert(m->res_tables.end(), tb->sh_s + a, tb->sh_s + b);
+            }
+            if (rs->outflow_curve_type[k] == 1) {
+                if (!tb->hq_offset || !tb->hq_h || !tb->hq_q) return fail("reservoir H-Q tables missing");
+                const int64_t a = tb->hq_offset[k], b = tb->hq_offset[k + 1];
+                if (a < 0 || b <= a) return fail("empty reservoir H-Q table");
+                if (!increasing(tb->hq_h, a, b)) return fail("reservoir H-Q table not strictly increasing");
+                m->res_hq_at[k] = (int64_t)m->res_tables.size();
+                m->res_tables.insert(m->res_tables.end(), tb->hq_h + a, tb->hq_h + b);
+                m->res_tables.insert(m->res_tables.end(), tb->hq_q + a * 365, tb->hq_q + b * 365);
+            }
+            if (tb->lower_reservoir) {
+                const int32_t lo = tb->lower_reservoir[k];
+                if (lo < -1 || lo >= nres || lo == k) return fail("linked lower reservoir out of range");
+            }
+        }
+    } else {
+        for (int64_t k = 0; k < nres; ++k)
+            if (rs->outflow_curve_type[k] == 1) return fail("reservoir H-Q tables missing");
+    }
     m->res.resize((size_t)M * nres);
     for (int mbr = 0; mbr < M; ++mbr)
         for (int64_t k = 0; k < nres; ++k) {
@@ -1582,7 +1729,25 @@ int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, c
             r.inflow_subsurface = 0.0;
             r.outflow_obs = NaN;
             r.waterlevel = rs->waterlevel[k];
-            r.storage = r.area * r.waterlevel;  // initialize_storage, linear profile (reservoir.jl:343-360)
+            r.storage_curve_type = 1;
+            r.hq_day = 1;
+            if (tb) {
+                if (tb->storage_curve_type) r.storage_curve_type = tb->storage_curve_type[k];
+                if (tb->lower_reservoir) r.lower = tb->lower_reservoir[k] + 1;
+                if (r.storage_curve_type == 2) {
+                    const int64_t a = tb->sh_offset[k], b = tb->sh_offset[k + 1];
+                    r.sh_n = b - a;
+                    r.sh_h = m->res_tables.data() + m->res_sh_at[k];
+                    r.sh_s = r.sh_h + r.sh_n;
+                }
+                if (r.outflow_type == 1) {
+                    r.hq_n = tb->hq_offset[k + 1] - tb->hq_offset[k];
+                    r.hq_h = m->res_tables.data() + m->res_hq_at[k];
+                    r.hq_q = r.hq_h + r.hq_n;
+                    r.maximum_storage = rating_curve_maximum_storage(r);
+                }
+            }
+            r.storage = initial_storage(r);
             r.outflow = NaN;
         }
     for (auto* v : {&m->res_out_avg, &m->res_in_avg, &m->res_evap_avg, &m->res_abs_avg, &m->res_prev, &m->res_err,
@@ -1977,9 +2142,9 @@ void member_step(OrcModel* m, int mbr, int n_threads) {
                 if (m->nres && m->res_of_river[v] >= 0) {
                     // update_reservoir_model! (surface_kinwave.jl:441-489): the reservoir outflow
                     // is the inflow of the downstream river cell
-                    OrcReservoir& r = res[m->res_of_river[v]];
-                    update_reservoir_at_node(r, m->rv_q[j], dt_s);
-                    m->rv_qin[orr + m->r_ds[v]] = r.outflow;
+                    const int32_t k = m->res_of_river[v];
+                    update_reservoir_at_node(res, k, m->rv_q[j], dt_s);
+                    m->rv_qin[orr + m->r_ds[v]] = res[k].outflow;
                 }
                 m->rv_h[j] = kw[1] / m->r_width[v];
                 m->rv_storage[j] = m->r_length[v] * kw[1];
@@ -2525,8 +2690,22 @@ double orc_li_domain_stable_timestep(const WfLiLandGrid* L, const WfLiRiverNetwo
 
 extern "C" {
 // Reservoir at a river node with discharge q after the node's kinematic-wave update.
-void orc_reservoir_update(OrcReservoir* r, double q, double dt) { update_reservoir_at_node(*r, q, dt); }
+void orc_reservoir_update(OrcReservoir* r, double q, double dt) { update_reservoir_at_node(r, 0, q, dt); }
+// update_reservoir_model!(reservoir_model, i, inflow, dt) (reservoir.jl:583-628) on reservoir i
+// (0-based) of `res`, which holds every reservoir a linked one refers to
+void orc_reservoir_update_model(OrcReservoir* res, int64_t i, double inflow, double dt) {
+    update_reservoir(res, i, inflow, dt);
+}
+double orc_interpolate_linear(double x, const double* xp, const double* fp, int64_t n) {
+    return interpolate_linear(x, xp, fp, n);
+}
 int32_t orc_reservoir_size() { return (int32_t)sizeof(OrcReservoir); }
+// col_index_hq of every reservoir (update_index_hq!, reservoir.jl:376-382)
+int32_t orc_model_set_rating_curve_day(OrcModel* m, int32_t day) {
+    if (day < 1 || day > 365) return WF_ERR_INVALID;
+    for (OrcReservoir& r : m->res) r.hq_day = day;
+    return WF_OK;
+}
 int64_t orc_model_reservoirs(const OrcModel* m) { return m->nres; }
 }  // extern "C"
 

@@ -220,6 +220,12 @@ int32_t orc_model_substep_signature(OrcModel* m, int32_t kind, double* out);
 int32_t orc_model_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p,
                                          const WfReservoirs* rs, OrcModel** out);
 int64_t orc_model_reservoirs(const OrcModel* m);
+/* the same with the reservoirs' S-H and H-Q tables and links (tables may be NULL) */
+int32_t orc_model_create_with_reservoir_tables(const WfConfig* c, const WfDomain* d, const WfParams* p,
+                                               const WfReservoirs* rs, const WfReservoirTables* tables,
+                                               OrcModel** out);
+/* the H-Q tables' column (day of year 1..365, col_index_hq) of the next steps */
+int32_t orc_model_set_rating_curve_day(OrcModel* m, int32_t day);
 /* Route the land grid with its river by the local-inertial scheme inside the step, in place of
  * the kinematic waves (surface_routing.jl:62-89): one member, no reservoirs, fixed sub-steps;
  * the grid's land and active river cells are the model's. Warm state h_land [n], h_river [river n]. */

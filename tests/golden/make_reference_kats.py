@@ -1,6 +1,7 @@
 """Extract the known-answer tests (KATs) of Wflow.jl's unit tests into reference_kats.json.
 
-Wflow.jl's unit tests (Wflow/test/land_process.jl, soil.jl, routing_process.jl, utils.jl)
+Wflow.jl's unit tests (Wflow/test/land_process.jl, soil.jl, routing_process.jl, reservoir.jl,
+utils.jl)
 hold input/output literals for every process function on the SBM + kinematic-wave path.
 Julia is not available to run them, so this script reads the test files as text and
 copies each literal from the cited line. Each case records the function, its inputs, the
@@ -41,9 +42,10 @@ _TOK = re.compile(r"[A-Za-z_][A-Za-z_0-9]*|-?\d+(?:\.\d*)?(?:[eE][-+]?\d+)?")
 
 
 def nums(fname, line, count=None):
-    """Numeric literals (NaN included) on a (1-based) line of a reference test file."""
+    """Numeric literals (NaN included) on a (1-based) line of a reference test file (Julia's
+    digit separators, as in 25_000_000.0, are dropped first)."""
     vals = []
-    for tok in _TOK.findall(_lines(fname)[line - 1]):
+    for tok in _TOK.findall(re.sub(r"(?<=\d)_(?=\d)", "", _lines(fname)[line - 1])):
         if tok == "NaN":
             vals.append(float("nan"))
         elif tok[0].isdigit() or tok[0] == "-":
@@ -365,6 +367,51 @@ def build():
                   dict(mean_abs_error=num(R, 1317)),
                   note="bed levels integrate the analytical slope (the test's quadgk, rtol 1e-12); "
                        "the analytical depth profile is MacDonald's (1997), restated from lines 1199-1211"))
+    # -------------------------------------------------------------------- reservoir.jl
+    # update_reservoir_model!(res, i, inflow, dt) of one reservoir after set_reservoir_vars!
+    # (reservoir.jl:583-628), and the river-side wrapper that limits the abstraction and hands
+    # the outflow to the downstream cell (surface_kinwave.jl:441-489). The linked-reservoir and
+    # rating-curve tests read CSV tables that the checkout does not hold.
+    V = "reservoir.jl"
+    simple = dict(outflow_type=4, precipitation=num(V, 9), evaporation=num(V, 10), demand=num(V, 14),
+                  maximum_release=num(V, 15), maximum_storage=num(V, 16), area=num(V, 17),
+                  target_full_fraction=num(V, 18), target_minimum_fraction=num(V, 19), storage=num(V, 25),
+                  waterlevel=num(V, 26))
+    K.append(case("reservoir_simple", "update_reservoir_model", f"{V}:1-44",
+                  dict(reservoir=simple, inflow=num(V, 36), dt=num(V, 4)),
+                  dict(outflow=num(V, 38), storage=num(V, 40), actevap_cumulative=num(V, 43))))
+    K.append(case("reservoir_simple_observed_outflow", "update_reservoir_model", f"{V}:46-57",
+                  dict(reservoir=dict(simple, outflow_obs=num(V, 47), storage=num(V, 48), waterlevel=num(V, 49)),
+                       inflow=num(V, 52), dt=num(V, 4)),
+                  dict(outflow=num(V, 54), storage=num(V, 56))))
+    K.append(case("reservoir_modified_puls", "update_reservoir_model", f"{V}:60-115",
+                  dict(reservoir=dict(outflow_type=3, precipitation=num(V, 68), evaporation=num(V, 69),
+                                      area=num(V, 73), threshold=num(V, 74), rating_curve_coefficient=num(V, 77),
+                                      rating_curve_exponent=num(V, 78), waterlevel=num(V, 80),
+                                      storage=num(V, 73) * num(V, 80)),
+                       inflow=num(V, 100), dt=num(V, 65)),
+                  dict(waterlevel=num(V, 107), outflow=num(V, 108), storage=num(V, 110),
+                       actevap_cumulative=num(V, 114)),
+                  note="initialize_storage of the linear profile: storage = area * waterlevel"))
+    K.append(case("reservoir_observed_outflow_at_node", "update_reservoir_at_node", f"{V}:117-167",
+                  dict(reservoir=dict(outflow_type=4, external_inflow=num(V, 127), inflow_overland=num(V, 128),
+                                      inflow_subsurface=num(V, 129), precipitation=num(V, 130),
+                                      evaporation=num(V, 131), area=num(V, 137), threshold=num(V, 138),
+                                      rating_curve_coefficient=num(V, 139), rating_curve_exponent=num(V, 140),
+                                      waterlevel=num(V, 143), storage=num(V, 144), outflow_obs=num(V, 147)),
+                       q=nums(V, 152)[-2], dt=num(V, 159)),
+                  dict(qin_downstream=num(V, 162), abstraction_cumulative=num(V, 163), storage=num(V, 164),
+                       waterlevel=num(V, 165), outflow=num(V, 166))))
+    K.append(case("reservoir_simple_at_node", "update_reservoir_at_node", f"{V}:169-221",
+                  dict(reservoir=dict(outflow_type=4, external_inflow=num(V, 178), inflow_overland=num(V, 179),
+                                      inflow_subsurface=num(V, 180), precipitation=num(V, 181),
+                                      evaporation=num(V, 182), area=num(V, 188), maximum_release=num(V, 189),
+                                      demand=num(V, 190), target_minimum_fraction=num(V, 191),
+                                      target_full_fraction=num(V, 192), maximum_storage=num(V, 193),
+                                      waterlevel=num(V, 196), storage=num(V, 197)),
+                       q=nums(V, 204)[0], dt=num(V, 212)),
+                  dict(qin_downstream=num(V, 215), abstraction_cumulative=num(V, 217), storage=num(V, 218),
+                       waterlevel=num(V, 219), outflow=num(V, 220))))
     # ------------------------------------------------------------------------ utils.jl
     # units (the file helpers' conversions) and the affine transform of [input] entries
     K.append(case("units_absolute_degrees", "to_si", f"{U}:40-45", dict(value=0.0, unit="degC"),

@@ -4,9 +4,10 @@ A model created with wf_create_with_reservoirs cuts the land and river upstream 
 reservoir outlets (domain.jl:95-121), feeds each reservoir from its outlet cell's overland and
 subsurface discharge (surface_kinwave.jl:771-802), updates it inside the river sweep after its
 cell's kinematic wave and hands its outflow to the downstream river cell
-(surface_kinwave.jl:441-489, reservoir.jl:583-628). The reservoirs here cover the three outflow
-functions (simple, modified Puls, free weir), a negative and a positive external inflow and an
-observed outflow on alternate steps.
+(surface_kinwave.jl:441-489, reservoir.jl:583-628). The reservoirs here cover the four outflow
+functions (simple, modified Puls, free weir, rating curve), both storage profiles, a free weir
+linked to a lower reservoir (water flowing back when the lower one is higher), a negative and a
+positive external inflow and an observed outflow on alternate steps.
 
 FP64 form: every land, river and reservoir field within relative 1e-9 of the oracle (the
 drop-in bar; the arithmetic is the oracle's, operation for operation). Split form: the outlet
@@ -51,7 +52,12 @@ def step_inputs(dom, res, s, dt, M, pfac, precip_scale):
     return (P, PET, T), inputs
 
 
-def run_res_pair(dom, res, cfg, steps, params=None, pfac=None, precip_scale=3.0, check_every=1):
+def rating_day(s):
+    """The H-Q tables' column of step s: a different day of the year every step."""
+    return 1 + (40 + 37 * s) % 365
+
+
+def run_res_pair(dom, res, cfg, steps, params=None, pfac=None, precip_scale=3.0, check_every=1, trace=None):
     gpu = Model(cfg, dom, params=params, reservoirs=res)
     orc = O.OracleModel(cfg, dom, params=params, reservoirs=res)
     M = max(1, cfg.n_members)
@@ -63,6 +69,8 @@ def run_res_pair(dom, res, cfg, steps, params=None, pfac=None, precip_scale=3.0,
         for name, v in inputs.items():
             gpu.set_value(name, v)
             orc.set(F[name], v)
+        gpu.set_rating_curve_day(rating_day(s))
+        orc.set_rating_curve_day(rating_day(s))
         gpu.run_timestep(P, PET, T)
         orc.set_forcing(P, PET, T)
         orc.step()
@@ -70,6 +78,9 @@ def run_res_pair(dom, res, cfg, steps, params=None, pfac=None, precip_scale=3.0,
         counts.append(((now["substeps_land"] - prev["substeps_land"], now["substeps_river"] - prev["substeps_river"]),
                        orc.substeps()[:2]))
         prev = now
+        if trace is not None:
+            trace.append({f: gpu.get_value(f) for f in ("RESERVOIR_OUTFLOW", "RESERVOIR_OUTFLOW_AVERAGE",
+                                                         "RESERVOIR_WATERLEVEL")})
         if (s + 1) % check_every == 0 or s == steps - 1:
             results.append(compare(gpu, orc, LAND + ["LAND_QIN_AVERAGE", "UNSATURATED_LAYER_DEPTH"] + RIVER + RES,
                                    layers=gpu.N))
@@ -140,6 +151,37 @@ def test_reservoir_state_roundtrip(gpu_lib):
         assert np.array_equal(x, y)
 
 
+# Reservoir tables and links (synthetic.make_linked_reservoirs): an upper free weir linked to a
+# lower reservoir four river cells downstream (interpolated S-H profiles; the lower one released
+# by a rating curve read in a different day's column every step), a modified Puls reservoir with
+# the linear profile and a simple reservoir with an interpolated profile. The lower reservoir
+# starts above the upper one, so water first runs back (a negative outflow of the upper one).
+def test_linked_reservoirs_and_tables_fp64_daily(gpu_lib):
+    dom = synthetic.make_domain(48, 1000.0, seed=12)
+    res = synthetic.make_linked_reservoirs(dom, seed=3)
+    cfg = synthetic.make_config(86400.0)
+    trace = []
+    gpu, orc, results, _ = run_res_pair(dom, res, cfg, 12, check_every=4, trace=trace)
+    assert_parity(results)
+    assert np.array_equal(gpu.outlets(0), orc.outlets(0))
+    assert reservoir_closure(gpu) <= 1e-9
+    upper = np.array([t["RESERVOIR_OUTFLOW"][0] for t in trace])
+    assert upper.min() < 0.0 < upper.max(), upper  # back flow and forward flow both happened
+
+
+def test_linked_reservoirs_fp64_hourly_ensemble(gpu_lib):
+    # four river sub-steps per step, each its own launch (linked reservoirs); members differ
+    dom = synthetic.make_domain(32, 250.0, seed=13)
+    res = synthetic.make_linked_reservoirs(dom, seed=5)
+    M = 4
+    kv0, f, pfac = synthetic.perturb_members(dom.params, M, seed=13)
+    params = dict(dom.params, kv_0=kv0, f=f)
+    cfg = synthetic.make_config(3600.0, n_members=M, per_member_soil=True)
+    gpu, orc, results, _ = run_res_pair(dom, res, cfg, 8, params=params, pfac=pfac * 3.0, check_every=4)
+    assert_parity(results)
+    assert reservoir_closure(gpu) <= 1e-9
+
+
 def split_res_errors(dom, res, cfg, steps, precip_scale=3.0):
     import copy
     cfg64 = copy.copy(cfg)
@@ -152,6 +194,8 @@ def split_res_errors(dom, res, cfg, steps, precip_scale=3.0):
         for name, v in inputs.items():
             gpu.set_value(name, v)
             orc.set(F[name], v)
+        gpu.set_rating_curve_day(rating_day(s))
+        orc.set_rating_curve_day(rating_day(s))
         gpu.run_timestep(P, PET, T)
         orc.set_forcing(P, PET, T)
         orc.step()
@@ -184,4 +228,16 @@ def test_reservoirs_split_accuracy(gpu_lib, adaptive):
     assert w["storage"] <= 1e-5, w
     assert w["outflow"] <= 1e-4, w
     assert w["closure"] <= 1e-6, w
+    assert w["res_closure"] <= 1e-9, w
+
+
+def test_linked_reservoirs_split_accuracy(gpu_lib):
+    dom = synthetic.make_domain(48, 1000.0, seed=12)
+    res = synthetic.make_linked_reservoirs(dom, seed=3)
+    cfg = synthetic.make_config(86400.0, form=abi.WF_FORM_SPLIT)
+    w = split_res_errors(dom, res, cfg, 12)
+    print("split linked reservoirs with tables, errors", w)
+    assert w["outlet_q"] <= 1e-4, w
+    assert w["storage"] <= 1e-5, w
+    assert w["outflow"] <= 1e-4, w
     assert w["res_closure"] <= 1e-9, w

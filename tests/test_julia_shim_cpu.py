@@ -30,3 +30,8 @@ def test_struct_field_counts_match_the_headers():
         fields = [ln for ln in m.group(1).splitlines() if "::" in ln]
         from wflow_gb300 import li_river
         assert len(fields) == len(getattr(li_river, jl_name)._fields_), jl_name
+    for jl_name in ("WfReservoirs", "WfReservoirTables"):
+        m = re.search(r"struct %s\n(.*?)\nend" % jl_name, text, re.S)
+        assert m, jl_name
+        fields = [ln.split("::")[0].strip() for ln in m.group(1).splitlines() if "::" in ln]
+        assert fields == [f for f, _ in getattr(abi, jl_name)._fields_], jl_name

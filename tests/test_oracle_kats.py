@@ -240,6 +240,18 @@ def run_case(c, prev):
         from wflow_gb300 import staticmaps
         return dict(out=list(staticmaps.apply_affine_transform(np.asarray(a["v"]), a.get("scale", [1.0]),
                                                                a.get("offset", [0.0]))))
+    if fn == "update_reservoir_model":
+        # set_reservoir_vars! (the cumulatives start at zero), then update_reservoir_model!
+        res = (O.Reservoir * 1)(O.Reservoir(**a["reservoir"]))
+        O.reservoir_update_model(res, 0, a["inflow"], a["dt"])
+        r = res[0]
+        return dict(outflow=r.outflow, storage=r.storage, waterlevel=r.waterlevel,
+                    actevap_cumulative=r.actevap_cumulative)
+    if fn == "update_reservoir_at_node":
+        r = O.Reservoir(**a["reservoir"])
+        O.reservoir_update(r, a["q"], a["dt"])
+        return dict(qin_downstream=r.outflow, abstraction_cumulative=r.abstraction_cumulative, storage=r.storage,
+                    waterlevel=r.waterlevel, outflow=r.outflow)
     if fn == "local_inertial_macdonald":
         return dict(mean_abs_error=macdonald(a))
     if fn == "kinwave_river_update":

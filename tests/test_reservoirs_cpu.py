@@ -156,7 +156,8 @@ def _create_status(dom, res):
     return st, (msg.decode() if msg else "")
 
 
-@pytest.mark.parametrize("case", ["pit", "two_into_one", "bad_type", "bad_area", "missing_param", "out_of_range"])
+@pytest.mark.parametrize("case", ["pit", "two_into_one", "bad_type", "rating_curve_without_table", "bad_area",
+                                  "missing_param", "out_of_range"])
 def test_abi_rejects_invalid_reservoirs(domain, case):
     build.build_all()
     dom, res = domain
@@ -173,8 +174,11 @@ def test_abi_rejects_invalid_reservoirs(domain, case):
         res["river_index"][1] = sib[0]
         expect = (abi.WF_ERR_UNSUPPORTED, "drain into one")
     elif case == "bad_type":
-        res["outflow_curve_type"][0] = 1
+        res["outflow_curve_type"][0] = 5
         expect = (abi.WF_ERR_UNSUPPORTED, "outflow type")
+    elif case == "rating_curve_without_table":
+        res["outflow_curve_type"][0] = abi.WF_RES_RATING_CURVE
+        expect = (abi.WF_ERR_INVALID, "H-Q tables missing")
     elif case == "bad_area":
         res["area"][0] = 0.0
         expect = (abi.WF_ERR_INVALID, "area")
@@ -187,6 +191,6 @@ def test_abi_rejects_invalid_reservoirs(domain, case):
     st, msg = _create_status(dom, res)
     assert st == expect[0] and expect[1] in msg, (st, msg)
     # the oracle refuses the same sets (the sibling case included)
-    if case in ("pit", "two_into_one", "bad_type", "bad_area", "out_of_range"):
+    if case in ("pit", "two_into_one", "bad_type", "rating_curve_without_table", "bad_area", "out_of_range"):
         with pytest.raises(RuntimeError):
             O.OracleModel(synthetic.make_config(86400.0), dom, reservoirs=res)

@@ -182,3 +182,36 @@ def test_reservoir_maps_round_trip(tmp_path):
     m.set_forcing(P, PET, T)
     m.step()
     assert np.all(np.isfinite(m.get(F["RESERVOIR_STORAGE"])))
+
+
+def test_reservoir_tables_and_links_round_trip(tmp_path):
+    # storage profiles, rating curves and a link in the maps, the tables in reservoir_sh_<id>.csv
+    # and reservoir_hq_<id>.csv beside them (reservoir.jl:152-192; read_sh_csv / read_hq_csv,
+    # io.jl:1129-1147): the oracle fed the loaded set follows the one fed the original set
+    dom = synthetic.make_domain(48, 1000.0, seed=3)
+    res = synthetic.make_linked_reservoirs(dom, seed=3)
+    p = tmp_path / "r.nc"
+    staticmaps.write_staticmaps(dom, p, reservoirs=res)
+    assert (tmp_path / "reservoir_hq_2.csv").exists() and (tmp_path / "reservoir_sh_1.csv").exists()
+    got, _, gres = staticmaps.load_staticmaps(p, reservoirs=True)
+    order = np.argsort(res["river_index"])
+    np.testing.assert_array_equal(gres["river_index"], res["river_index"][order])
+    np.testing.assert_array_equal(gres["storage_curve_type"], res["storage_curve_type"][order])
+    inv = np.argsort(order)
+    lo = res["lower_reservoir"][order]
+    np.testing.assert_array_equal(gres["lower_reservoir"], np.where(lo >= 0, inv[np.maximum(lo, 0)], -1))
+    cfg = synthetic.make_config(86400.0)
+    a = O.OracleModel(cfg, dom, reservoirs=res)
+    b = O.OracleModel(cfg, got, reservoirs=gres)
+    for s in range(6):
+        P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=3)
+        for m, r in ((a, res), (b, gres)):
+            m.set_forcing(P * 3.0, PET, T)
+            rp, re = synthetic.reservoir_forcing(dom, r, P * 3.0, PET)
+            m.set(F["RESERVOIR_PRECIPITATION"], rp)
+            m.set(F["RESERVOIR_EVAPORATION"], re)
+            m.set_rating_curve_day(100 + s)
+            m.step()
+    for f in ("RESERVOIR_STORAGE", "RESERVOIR_WATERLEVEL", "RESERVOIR_OUTFLOW_AVERAGE"):
+        np.testing.assert_allclose(b.get(F[f]), a.get(F[f])[order], rtol=1e-12, err_msg=f)
+    np.testing.assert_allclose(b.outlets(0), a.outlets(0), rtol=1e-12)

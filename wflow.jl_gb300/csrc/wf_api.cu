@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -196,9 +197,10 @@ int upload_slots_ff(WfHandle* h, float** hi, float** lo, const std::vector<doubl
     return rc ? rc : upload(h, lo, vl);
 }
 
-int plan_graph(WfHandle* h, DevGraphAlloc& G, int64_t n, const int32_t* ds, int M, int32_t s_cap) {
+int plan_graph(WfHandle* h, DevGraphAlloc& G, int64_t n, const int32_t* ds, int M, int32_t s_cap,
+               const int64_t* heavy_hint = nullptr) {
     std::string err;
-    int rc = wf_build_plan(n, ds, M, G.plan, err);
+    int rc = wf_build_plan(n, ds, M, G.plan, err, heavy_hint);
     if (rc) return set_err(h, rc == WF_ERR_CYCLE ? WF_ERR_CYCLE : WF_ERR_INVALID, err);
     const WfRoutingPlan& P = G.plan;
     if ((rc = upload(h, &G.chunk_base, P.chunk_base))) return rc;
@@ -681,6 +683,127 @@ struct StateHeader {
 
 int run_step(WfHandle* h);
 
+__global__ void set_day_kernel(int32_t* day, int32_t v) { *day = v; }
+
+// reservoir.jl:363-375 on n rows at xp[i] and fp[i * fs], xp strictly increasing (the host copy of
+// wfr::interpolate_linear, for the initial and maximum storages)
+double interpolate_linear_host(double x, const double* xp, const double* fp, int64_t fs, int64_t n) {
+    double fmin = fp[0], fmax = fp[0];
+    for (int64_t i = 1; i < n; ++i) {
+        fmin = wfm::jmin(fmin, fp[i * fs]);
+        fmax = wfm::jmax(fmax, fp[i * fs]);
+    }
+    if (x <= xp[0]) return fmin;
+    if (x >= xp[n - 1]) return fmax;
+    int64_t i1 = 0;
+    while (i1 + 1 < n && xp[i1 + 1] <= x) ++i1;
+    const int64_t i2 = i1 + 1;
+    const double f1 = fp[i1 * fs], f2 = fp[i2 * fs];
+    return f1 * (1.0 - (x - xp[i1]) / (xp[i2] - xp[i1])) + f2 * (x - xp[i1]) / (xp[i2] - xp[i1]);
+}
+
+// The reservoirs' tables and links, checked and laid out for the device (ReservoirParameters,
+// reservoir.jl:5-44, 152-192), with each reservoir's initial storage (initialize_storage,
+// :343-360), a rating curve's maximum storage (get_maximum_storage, :322-340) and, for linked
+// reservoirs, the river planner's hints that keep each upper-to-lower path on one chain.
+struct ResTables {
+    bool any = false, linked = false;
+    std::vector<int32_t> profile, lower;
+    std::vector<int64_t> meta;  // [4 n]: S-H start, rows, H-Q start, rows (into tab)
+    std::vector<double> tab, initial_storage, maximum_storage;
+    std::vector<int64_t> heavy_hint;  // [n_river]
+};
+
+int res_tables(const WfReservoirs* rs, const WfReservoirTables* tb, int64_t nr, const int32_t* rds, ResTables& rt) {
+    const int64_t n = rs->n;
+    const double NaN = wfm::from_bits(0x7ff8000000000000ULL);
+    rt.profile.assign(n, WF_RES_PROFILE_LINEAR);
+    rt.lower.assign(n, -1);
+    rt.meta.assign(4 * n, 0);
+    rt.initial_storage.assign(n, 0.0);
+    rt.maximum_storage.assign(n, NaN);
+    auto bad = [](int rc, const char* msg) { return set_err(nullptr, rc, msg); };
+    auto increasing = [](const double* v, int64_t a, int64_t b) {
+        for (int64_t i = a; i < b; ++i)
+            if (!std::isfinite(v[i]) || (i > a && !(v[i] > v[i - 1]))) return false;
+        return true;
+    };
+    for (int64_t k = 0; k < n; ++k) {
+        const int32_t prof = tb && tb->storage_curve_type ? tb->storage_curve_type[k] : WF_RES_PROFILE_LINEAR;
+        if (prof != WF_RES_PROFILE_LINEAR && prof != WF_RES_PROFILE_INTERPOLATION)
+            return bad(WF_ERR_INVALID, "unknown reservoir storage curve type");
+        rt.profile[k] = prof;
+        if (prof == WF_RES_PROFILE_INTERPOLATION) {
+            if (!tb->sh_offset || !tb->sh_h || !tb->sh_s) return bad(WF_ERR_INVALID, "reservoir S-H tables missing");
+            const int64_t a = tb->sh_offset[k], b = tb->sh_offset[k + 1];
+            if (a < 0 || b <= a) return bad(WF_ERR_INVALID, "empty reservoir S-H table");
+            if (!increasing(tb->sh_h, a, b) || !increasing(tb->sh_s, a, b))
+                return bad(WF_ERR_INVALID, "reservoir S-H table not strictly increasing");
+            rt.meta[4 * k] = (int64_t)rt.tab.size();
+            rt.meta[4 * k + 1] = b - a;
+            rt.tab.insert(rt.tab.end(), tb->sh_h + a, tb->sh_h + b);
+            rt.tab.insert(rt.tab.end(), tb->sh_s + a, tb->sh_s + b);
+            rt.any = true;
+        }
+        if (rs->outflow_curve_type[k] == WF_RES_RATING_CURVE) {
+            if (!tb || !tb->hq_offset || !tb->hq_h || !tb->hq_q)
+                return bad(WF_ERR_INVALID, "reservoir H-Q tables missing for a rating curve");
+            const int64_t a = tb->hq_offset[k], b = tb->hq_offset[k + 1];
+            if (a < 0 || b <= a) return bad(WF_ERR_INVALID, "empty reservoir H-Q table");
+            if (!increasing(tb->hq_h, a, b)) return bad(WF_ERR_INVALID, "reservoir H-Q table not strictly increasing");
+            for (int64_t i = a * 365; i < b * 365; ++i)
+                if (!std::isfinite(tb->hq_q[i])) return bad(WF_ERR_INVALID, "reservoir H-Q table not finite");
+            rt.meta[4 * k + 2] = (int64_t)rt.tab.size();
+            rt.meta[4 * k + 3] = b - a;
+            rt.tab.insert(rt.tab.end(), tb->hq_h + a, tb->hq_h + b);
+            rt.tab.insert(rt.tab.end(), tb->hq_q + a * 365, tb->hq_q + b * 365);
+            rt.any = true;
+        }
+        if (tb && tb->lower_reservoir) {
+            const int32_t lo = tb->lower_reservoir[k];
+            if (lo < -1 || lo >= n || lo == k) return bad(WF_ERR_INVALID, "linked lower reservoir out of range");
+            rt.lower[k] = lo;
+            if (lo >= 0) rt.any = rt.linked = true;
+        }
+    }
+    for (int64_t k = 0; k < n; ++k) {
+        const double* sh = rt.tab.data() + rt.meta[4 * k];
+        const int64_t nsh = rt.meta[4 * k + 1];
+        const double wl = rs->waterlevel[k];
+        rt.initial_storage[k] = rt.profile[k] == WF_RES_PROFILE_INTERPOLATION
+                                    ? interpolate_linear_host(wl, sh, sh + nsh, 1, nsh)
+                                    : rs->area[k] * wl;
+        if (rs->outflow_curve_type[k] == WF_RES_RATING_CURVE) {
+            const double* hq = rt.tab.data() + rt.meta[4 * k + 2];
+            double hmax = hq[0];
+            for (int64_t i = 1; i < rt.meta[4 * k + 3]; ++i) hmax = wfm::jmax(hmax, hq[i]);
+            rt.maximum_storage[k] = rt.profile[k] == WF_RES_PROFILE_INTERPOLATION
+                                        ? interpolate_linear_host(hmax, sh, sh + nsh, 1, nsh)
+                                        : rs->area[k] * hmax;
+        }
+    }
+    if (rt.linked) {
+        rt.heavy_hint.assign(nr, -1);
+        for (int64_t k = 0; k < n; ++k) {
+            if (rt.lower[k] < 0) continue;
+            const int64_t target = rs->river_index[rt.lower[k]];
+            int64_t prev = rs->river_index[k], x = rds[prev], steps = 0;
+            while (x >= 0 && steps++ <= nr) {
+                if (rt.heavy_hint[x] >= 0 && rt.heavy_hint[x] != prev)
+                    return bad(WF_ERR_UNSUPPORTED, "the river paths of two linked reservoir pairs join");
+                rt.heavy_hint[x] = prev;
+                if (x == target) break;
+                prev = x;
+                x = rds[x];
+            }
+            if (x != target)
+                return bad(WF_ERR_UNSUPPORTED,
+                           "a linked lower reservoir must lie downstream of its upper reservoir on the river");
+        }
+    }
+    return WF_OK;
+}
+
 }  // namespace
 
 // ============================================================================ C ABI =======
@@ -696,6 +819,7 @@ int32_t wf_struct_size(int32_t which) {
         case 3: return (int32_t)sizeof(WfMetrics);
         case 4: return (int32_t)sizeof(WfTuning);
         case 5: return (int32_t)sizeof(WfReservoirs);
+        case 6: return (int32_t)sizeof(WfReservoirTables);
         default: return -1;
     }
 }
@@ -708,6 +832,12 @@ int32_t wf_create(const WfConfig* c, const WfDomain* d, const WfParams* p, int32
 
 int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const WfParams* p, const WfReservoirs* rs,
                                   int32_t device, WfHandle** out) {
+    return wf_create_with_reservoir_tables(c, d, p, rs, nullptr, device, out);
+}
+
+int32_t wf_create_with_reservoir_tables(const WfConfig* c, const WfDomain* d, const WfParams* p,
+                                        const WfReservoirs* rs, const WfReservoirTables* tb, int32_t device,
+                                        WfHandle** out) {
     WfHandle* h = nullptr;
     if (!out) return set_err(nullptr, WF_ERR_INVALID, "null output handle");
     *out = nullptr;
@@ -764,14 +894,14 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
                 return set_err(nullptr, WF_ERR_INVALID, "a reservoir without a downstream river node is not supported");
             if (fed[dv]) return set_err(nullptr, WF_ERR_UNSUPPORTED, "two reservoirs drain into one river cell");
             const int32_t t = rs->outflow_curve_type[k];
-            if (t != WF_RES_FREE_WEIR && t != WF_RES_MODIFIED_PULS && t != WF_RES_SIMPLE)
-                return set_err(nullptr, WF_ERR_UNSUPPORTED, "reservoir outflow type must be 2, 3 or 4");
+            if (t != WF_RES_RATING_CURVE && t != WF_RES_FREE_WEIR && t != WF_RES_MODIFIED_PULS && t != WF_RES_SIMPLE)
+                return set_err(nullptr, WF_ERR_UNSUPPORTED, "reservoir outflow type must be 1, 2, 3 or 4");
             if (!(rs->area[k] > 0.0)) return set_err(nullptr, WF_ERR_INVALID, "reservoir area must be positive");
             const bool simple_ok = rs->maximum_storage && rs->maximum_release && rs->demand &&
                                    rs->target_minimum_fraction && rs->target_full_fraction;
             const bool weir_ok = rs->threshold && rs->rating_curve_coefficient &&
                                  (t != WF_RES_FREE_WEIR || rs->rating_curve_exponent);
-            if (t == WF_RES_SIMPLE ? !simple_ok : !weir_ok)
+            if (t == WF_RES_SIMPLE ? !simple_ok : t != WF_RES_RATING_CURVE && !weir_ok)
                 return set_err(nullptr, WF_ERR_INVALID, "reservoir parameter array missing for its outflow type");
             fed[dv] = 1;
             res_of_river[v] = (int32_t)k;
@@ -779,6 +909,11 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
             if (li < 0 || li >= d->n_land) return set_err(nullptr, WF_ERR_INVALID, "river_land_index out of range");
             land_ds[li] = -1;  // the outlet cell is a pit of the land upstream lists (domain.jl:95-121)
         }
+    }
+    ResTables rt;
+    if (nres > 0) {
+        const int rc = res_tables(rs, tb, d->n_river, d->river_downstream, rt);
+        if (rc) return rc;
     }
 
     h = new WfHandle();
@@ -854,9 +989,18 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
     // the largest domains)
     const size_t cap = c->form == WF_FORM_SPLIT ? (size_t)wfv::MAX_GROUP : (size_t)32;
     const int cap_land = (int)std::min<size_t>(std::max(h->h_dts_land.size(), h->h_dts_ssf.size()), cap);
-    const int cap_river = (int)std::min<size_t>(h->h_dts_river.size(), cap);
+    // linked reservoirs: the river runs one sub-step per launch and keeps every upper-to-lower
+    // path on one chain (wf_reservoir.cuh)
+    const int cap_river = rt.linked ? 1 : (int)std::min<size_t>(h->h_dts_river.size(), cap);
     CKR(plan_graph(h, h->land, n, land_ds.data(), M, cap_land));
-    CKR(plan_graph(h, h->river, nr, d->river_downstream ? d->river_downstream : nullptr, M, cap_river));
+    CKR(plan_graph(h, h->river, nr, d->river_downstream ? d->river_downstream : nullptr, M, cap_river,
+                   rt.linked ? rt.heavy_hint.data() : nullptr));
+    for (int64_t k = 0; k < nres && rt.linked; ++k)
+        if (rt.lower[k] >= 0 && h->river.plan.chain_of_node[rs->river_index[k]] !=
+                                    h->river.plan.chain_of_node[rs->river_index[rt.lower[k]]]) {
+            set_err(h, WF_ERR_INVALID, "linked reservoirs not on one routing chain");
+            return fail(WF_ERR_INVALID);
+        }
     const WfRoutingPlan& PL = h->land.plan;
     const WfRoutingPlan& PR = h->river.plan;
 
@@ -1271,6 +1415,9 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
         for (int f = 0; f < RP_COUNT; ++f) {
             std::vector<double> v(nres, NaN);
             if (src[f]) v.assign(src[f], src[f] + nres);
+            if (f == RP_MAXSTOR)  // a rating curve's maximum storage follows from its tables
+                for (int64_t k = 0; k < nres; ++k)
+                    if (rs->outflow_curve_type[k] == WF_RES_RATING_CURVE) v[k] = rt.maximum_storage[k];
             CKR(upload(h, &F.RP[f], v));
         }
         for (int f = 0; f < RS_COUNT; ++f) {
@@ -1279,11 +1426,26 @@ int32_t wf_create_with_reservoirs(const WfConfig* c, const WfDomain* d, const Wf
                 for (int m = 0; m < M; ++m) {
                     double x = 0.0;
                     if (f == RS_WATERLEVEL) x = rs->waterlevel[k];
-                    if (f == RS_STORAGE) x = rs->area[k] * rs->waterlevel[k];  // linear profile (reservoir.jl:343-360)
+                    if (f == RS_STORAGE) x = rt.initial_storage[k];  // initialize_storage (reservoir.jl:343-360)
                     if (f == RS_OUTFLOW || f == RS_OBS) x = NaN;
                     v[(size_t)k * M + m] = x;
                 }
             CKR(upload(h, &F.RS[f], v));
+        }
+        if (rt.any) {
+            int32_t *prof, *lower, *day;
+            int64_t* meta;
+            double* tab;
+            CKR(upload(h, &prof, rt.profile));
+            CKR(upload(h, &lower, rt.lower));
+            CKR(upload(h, &meta, rt.meta));
+            CKR(upload(h, &tab, rt.tab.empty() ? std::vector<double>{0.0} : rt.tab));
+            CKR(upload(h, &day, std::vector<int32_t>{1}));
+            F.res_profile = prof;
+            F.res_lower = lower;
+            F.res_tab_meta = meta;
+            F.res_tab = tab;
+            F.res_hq_day = day;
         }
     }
     F.land_slots = PL.n_slots;
@@ -1773,6 +1935,15 @@ int32_t wf_get_substep_signature(WfHandle* h, int32_t kind, double* sig, int32_t
     if (!h->adaptive) return set_err(h, WF_ERR_INVALID, "the model takes fixed sub-steps");
     CK(cudaMemcpyAsync(sig, h->ad[kind].sig, (size_t)h->M * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    return WF_OK;
+}
+
+int32_t wf_set_rating_curve_day(WfHandle* h, int32_t day_of_year) {
+    if (!h) return WF_ERR_INVALID;
+    if (day_of_year < 1 || day_of_year > 365) return set_err(h, WF_ERR_INVALID, "day of the year must be 1..365");
+    if (!h->F.res_hq_day) return WF_OK;  // no reservoir tables: nothing reads the day
+    set_day_kernel<<<1, 1, 0, h->stream>>>(const_cast<int32_t*>(h->F.res_hq_day), day_of_year);
+    if (cudaGetLastError() != cudaSuccess) return set_err(h, WF_ERR_CUDA, "setting the rating-curve day failed");
     return WF_OK;
 }
 

@@ -155,6 +155,14 @@ struct WfDevFields {
     const int32_t* res_type;       // [n_res] WfReservoirOutflow
     const int64_t* res_land_slot;  // [n_res] land slot of the reservoir outlet cell
     const int32_t* res_of_rslot;   // [river slots] reservoir at a river slot, or -1
+    // reservoir tables and links (null without them): storage profile (1 S = A H, 2 S-H table),
+    // linked lower reservoir (-1 none), per reservoir {S-H start, rows, H-Q start, rows} into
+    // res_tab, and the day of the year (1..365) whose H-Q column the rating curves read
+    const int32_t* res_profile;    // [n_res]
+    const int32_t* res_lower;      // [n_res]
+    const int64_t* res_tab_meta;   // [4 n_res]
+    const double* res_tab;
+    const int32_t* res_hq_day;     // [1]
     // gravitational snow transport and glacier (off: flags 0 and null pointers)
     int32_t snow_transport;
     int32_t glacier;

@@ -6,7 +6,8 @@
 
 #include "wflow_gb300.h"
 
-int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& P, std::string& err) {
+int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& P, std::string& err,
+                  const int64_t* heavy_hint) {
     P = WfRoutingPlan();
     P.n = n;
     P.M = members < 1 ? 1 : members;
@@ -64,13 +65,21 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
         err = "cycle in drainage graph";
         return WF_ERR_CYCLE;
     }
-    // heavy child: highest child, ties to the lowest node index
+    // heavy child: the hinted child, else the highest child (ties to the lowest node index)
     std::vector<int64_t> heavy(n, -1);
     for (int64_t v = 0; v < n; ++v) {
         int64_t best = -1;
         for (int64_t k = cptr[v]; k < cptr[v + 1]; ++k) {
             int64_t u = child[k];
             if (best < 0 || height[u] > height[best]) best = u;
+        }
+        if (heavy_hint && heavy_hint[v] >= 0) {
+            const int64_t u = heavy_hint[v];
+            if (u >= n || ds[u] != v) {
+                err = "heavy-child hint is not a child of its node";
+                return -1;
+            }
+            best = u;
         }
         heavy[v] = best;
     }

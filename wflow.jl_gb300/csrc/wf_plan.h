@@ -49,7 +49,10 @@ struct WfRoutingPlan {
 };
 
 // Build the plan; returns 0 or -3 (cycle) / -1 (bad input); err receives a message.
-int wf_build_plan(int64_t n, const int32_t* downstream, int32_t members, WfRoutingPlan& plan, std::string& err);
+// heavy_hint (optional, [n]): a child of node v that must continue v's chain (-1: the planner's
+// choice, the highest child); it keeps a given river path on one chain.
+int wf_build_plan(int64_t n, const int32_t* downstream, int32_t members, WfRoutingPlan& plan, std::string& err,
+                  const int64_t* heavy_hint = nullptr);
 
 // Host check of the schedule invariants (tests): every light upstream chain precedes the
 // chain that consumes it, and positions equal heights.

@@ -104,6 +104,19 @@ struct WfReservoirs
     target_full_fraction::Ptr{Float64}
 end
 
+# tables and links of reservoirs (WfReservoirTables): S-H and H-Q tables concatenated over the
+# reservoirs (offsets [n + 1]), H-Q discharges row-major with 365 columns, lower reservoir 0-based
+struct WfReservoirTables
+    storage_curve_type::Ptr{Int32}
+    sh_offset::Ptr{Int64}
+    sh_h::Ptr{Float64}
+    sh_s::Ptr{Float64}
+    hq_offset::Ptr{Int64}
+    hq_h::Ptr{Float64}
+    hq_q::Ptr{Float64}
+    lower_reservoir::Ptr{Int32}
+end
+
 # WfField ids (enum WfField)
 const F_LAND = (:canopy_storage, :snow_storage, :snow_water, :soil_surface_temperature,
     :saturated_water_depth, :unsaturated_layer_depth, :ssf_q, :land_q, :land_h, :water_table_depth)
@@ -154,9 +167,10 @@ Throw when the model uses a component outside the GPU step (the caller then keep
 reference's own `update_model!`): model type other than `sbm`, water demand, floodplains,
 drains, staggered Manning routing, local-inertial routing of the river alone or of the land alone,
 local-inertial routing with reservoirs or adaptive kinematic-wave steps, Kv profiles other than
-exponential / exponential_constant, reservoirs with tabulated curves, gravitational snow transport
-together with reservoirs. Glaciers, gravitational snow transport and local-inertial routing of the
-land with its river run on the GPU.
+exponential / exponential_constant, gravitational snow transport together with reservoirs.
+Glaciers, gravitational snow transport, reservoirs of every outflow type and storage profile
+(linked reservoirs whose river paths join excepted: `wf_create_with_reservoir_tables` refuses
+them) and local-inertial routing of the land with its river run on the GPU.
 """
 "Land and river both routed by the local-inertial scheme (surface_routing.jl:62-89)."
 local_inertial_both(config) = config.model.land_routing == Wflow.RoutingType.local_inertial &&
@@ -256,27 +270,26 @@ function GpuStep(model)
     end
     params = WfParams(ntuple(i -> haskey(src, PARAM_NAMES[i]) ? k(src[PARAM_NAMES[i]]) : Ptr{Float64}(0), 39))
     # reservoirs at their outlet river cells, in the reservoir model's order
-    # (NetworkReservoir.river_indices, network.jl:333-350); the storage profile must be linear
+    # (NetworkReservoir.river_indices, network.jl:333-350), with their S-H / H-Q tables and links
     nres = 0
     res = WfReservoirs(0, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL,
         C_NULL, C_NULL)
+    tables = WfReservoirTables(C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL)
     if config.model.reservoir__flag
         rv = routing.river_flow.boundary_conditions.reservoir
         p = rv.parameters
-        all(==(Wflow.ReservoirProfileType.linear), p.storage_curve_type) ||
-            error("the GPU step supports the linear reservoir storage profile only")
-        all(iszero, p.lower_reservoir_ind) || error("the GPU step does not support linked reservoirs")
         nres = length(p.area)
         res = WfReservoirs(nres, k(Int32.(domain.reservoir.network.river_indices .- 1)),
             k(Int32.(Integer.(p.outflow_curve_type))), k(p.area), k(rv.variables.waterlevel),
             k(p.maximum_storage), k(p.threshold), k(p.rating_curve_coefficient), k(p.rating_curve_exponent),
             k(p.maximum_release), k(p.demand), k(p.target_minimum_fraction), k(p.target_full_fraction))
+        tables = reservoir_tables(p, k)
     end
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    st = ccall((:wf_create_with_reservoirs, LIB), Int32,
-        (Ref{WfConfig}, Ref{WfDomain}, Ref{WfParams}, Ref{WfReservoirs}, Int32, Ref{Ptr{Cvoid}}),
-        cfg, dom, params, res, Int32(0), h)
-    check(st, C_NULL, "wf_create_with_reservoirs")
+    st = ccall((:wf_create_with_reservoir_tables, LIB), Int32,
+        (Ref{WfConfig}, Ref{WfDomain}, Ref{WfParams}, Ref{WfReservoirs}, Ref{WfReservoirTables}, Int32,
+         Ref{Ptr{Cvoid}}), cfg, dom, params, res, tables, Int32(0), h)
+    check(st, C_NULL, "wf_create_with_reservoir_tables")
     n = length(ds_land)
     gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)), nres, nothing)
     finalizer(g -> ccall((:wf_destroy, LIB), Cvoid, (Ptr{Cvoid},), g.handle), gpu)
@@ -288,6 +301,37 @@ function GpuStep(model)
             gpu.handle, "wf_attach_local_inertial")
     end
     return gpu
+end
+
+"""
+    reservoir_tables(p, k)
+
+The S-H and H-Q tables (`storage_waterlevel_curve`, `waterlevel_discharge_curve`, read from
+reservoir_sh_<id>.csv / reservoir_hq_<id>.csv by read_sh_csv / read_hq_csv, io.jl:1129-1147) and
+the links (`lower_reservoir_ind`, 1-based, 0 none) of ReservoirParameters `p` as a
+WfReservoirTables; `k` keeps the arrays alive.
+"""
+function reservoir_tables(p, k)
+    n = length(p.area)
+    sh_off, hq_off = zeros(Int64, n + 1), zeros(Int64, n + 1)
+    sh_h, sh_s, hq_h, hq_q = Float64[], Float64[], Float64[], Float64[]
+    for i in 1:n
+        sh = p.storage_waterlevel_curve[i]
+        if p.storage_curve_type[i] == Wflow.ReservoirProfileType.interpolation
+            append!(sh_h, sh.H)
+            append!(sh_s, sh.S)
+        end
+        sh_off[i + 1] = length(sh_h)
+        hq = p.waterlevel_discharge_curve[i]
+        if p.outflow_curve_type[i] == Wflow.ReservoirOutflowType.rating_curve
+            append!(hq_h, hq.H)
+            append!(hq_q, vec(permutedims(hq.Q)))  # row-major: the 365 days of each level
+        end
+        hq_off[i + 1] = length(hq_h)
+    end
+    ptr(v) = isempty(v) ? Ptr{Float64}(0) : k(v)
+    return WfReservoirTables(k(Int32.(Integer.(p.storage_curve_type))), k(sh_off), ptr(sh_h), ptr(sh_s),
+        k(hq_off), ptr(hq_h), ptr(hq_q), k(Int32.(p.lower_reservoir_ind .- 1)))
 end
 
 """
@@ -308,6 +352,13 @@ function gpu_update_model!(gpu::GpuStep, model)
         set_field!(gpu, F_RESERVOIR_EVAPORATION, rv.boundary_conditions.evaporation)
         set_field!(gpu, F_RESERVOIR_EXTERNAL_INFLOW, rv.boundary_conditions.external_inflow)
         set_field!(gpu, F_RESERVOIR_OUTFLOW_OBS, rv.variables.outflow_obs)
+        # update_index_hq! (reservoir.jl:379-385): the H-Q column of the step's first day
+        if Wflow.ReservoirOutflowType.rating_curve in rv.parameters.outflow_curve_type
+            day = Wflow.julian_day(model.clock.time - model.clock.dt)
+            rv.parameters.col_index_hq[1] = day
+            check(ccall((:wf_set_rating_curve_day, LIB), Int32, (Ptr{Cvoid}, Int32), gpu.handle, Int32(day)),
+                gpu.handle, "wf_set_rating_curve_day")
+        end
     end
     check(ccall((:wf_step, LIB), Int32, (Ptr{Cvoid},), gpu.handle), gpu.handle, "wf_step")
     sync_mirrors!(gpu, model)

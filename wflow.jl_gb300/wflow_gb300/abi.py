@@ -106,6 +106,7 @@ class WfMetrics(C.Structure):
 
 
 # WfReservoirOutflow
+WF_RES_RATING_CURVE = 1
 WF_RES_FREE_WEIR = 2
 WF_RES_MODIFIED_PULS = 3
 WF_RES_SIMPLE = 4
@@ -117,6 +118,16 @@ RESERVOIR_PARAMS = ["area", "waterlevel", "maximum_storage", "threshold", "ratin
 class WfReservoirs(C.Structure):
     _fields_ = ([("n", _i64), ("river_index", _pi32), ("outflow_curve_type", _pi32)]
                 + [(k, _pd) for k in RESERVOIR_PARAMS])
+
+
+WF_RES_PROFILE_LINEAR = 1
+WF_RES_PROFILE_INTERPOLATION = 2
+
+
+class WfReservoirTables(C.Structure):
+    """The reservoirs' S-H and H-Q tables and links (include/wflow_gb300.h)."""
+    _fields_ = [("storage_curve_type", _pi32), ("sh_offset", C.POINTER(_i64)), ("sh_h", _pd), ("sh_s", _pd),
+                ("hq_offset", C.POINTER(_i64)), ("hq_h", _pd), ("hq_q", _pd), ("lower_reservoir", _pi32)]
 
 
 class WfTuning(C.Structure):
@@ -243,6 +254,10 @@ def _declare(lib):
         "wf_plan_routing": (_i32, [_i64, _pi32, _i32, C.POINTER(_i64), C.POINTER(_i64), _pi32, _pi32]),
         "wf_create_with_reservoirs": (_i32, [C.POINTER(WfConfig), C.POINTER(WfDomain), C.POINTER(WfParams),
                                              C.POINTER(WfReservoirs), _i32, C.POINTER(H)]),
+        "wf_create_with_reservoir_tables": (_i32, [C.POINTER(WfConfig), C.POINTER(WfDomain), C.POINTER(WfParams),
+                                                   C.POINTER(WfReservoirs), C.POINTER(WfReservoirTables), _i32,
+                                                   C.POINTER(H)]),
+        "wf_set_rating_curve_day": (_i32, [H, _i32]),
         "wf_get_reservoir_count": (_i32, [H, C.POINTER(_i64)]),
         "wf_get_substep_signature": (_i32, [H, _i32, _pd, _i32]),
     }

@@ -28,10 +28,13 @@ class Model:
         h = C.c_void_p()
         if reservoirs is not None:
             # ReservoirModel (reservoir.jl:290-300) at the reservoirs' river cells
+            # (with the S-H / H-Q tables and links of the dict's table keys, when it has them)
             self._reservoirs = reservoirs
             self._r = synthetic.c_reservoirs(reservoirs)
-            st = self.lib.wf_create_with_reservoirs(C.byref(config), C.byref(self._d), C.byref(self._p),
-                                                    C.byref(self._r), int(device), C.byref(h))
+            self._rt = synthetic.c_reservoir_tables(reservoirs)
+            st = self.lib.wf_create_with_reservoir_tables(
+                C.byref(config), C.byref(self._d), C.byref(self._p), C.byref(self._r),
+                C.byref(self._rt) if self._rt is not None else None, int(device), C.byref(h))
         else:
             st = self.lib.wf_create(C.byref(config), C.byref(self._d), C.byref(self._p), int(device), C.byref(h))
         if st != abi.WF_OK:
@@ -104,6 +107,11 @@ class Model:
         """The step without any allocation (wf_step_static): scratch from a fixed 16 MiB device
         array shared by all models on the device; calls must not overlap on the GPU."""
         self._check(self.lib.wf_step_static(self.h), "wf_step_static")
+
+    def set_rating_curve_day(self, day_of_year):
+        """wf_set_rating_curve_day: the H-Q tables' column the next steps read (col_index_hq =
+        julian_day(time - dt), update_index_hq!, reservoir.jl:376-382)."""
+        self._check(self.lib.wf_set_rating_curve_day(self.h, int(day_of_year)), "wf_set_rating_curve_day")
 
     def step_async(self):
         self._check(self.lib.wf_step_async(self.h), "wf_step_async")

@@ -19,6 +19,8 @@ Axes are standardised as read_standardized does (io.jl:1346-1384): x and y incre
 land cells are numbered x fastest, then y. Reservoir maps are read when asked for.
 """
 
+from pathlib import Path
+
 import numpy as np
 
 from . import ncio
@@ -285,7 +287,7 @@ def load_staticmaps(path, mapping=None, cell_length_in_meter=True, n_layers=4, r
                  upstream_cells=ups)
     dom.outlets = [int(r) for r in np.flatnonzero(rds < 0)]
     grid = Grid(nx, ny, col, row, xc=S.xc, yc=S.yc, cell_length_in_meter=cell_length_in_meter)
-    res = _reservoirs(S, cells, river_land) if reservoirs else None
+    res = _reservoirs(S, cells, river_land, Path(path).parent) if reservoirs else None
     S.nc.close()
     return dom, grid, res
 
@@ -318,9 +320,38 @@ def _upstream_cells(ds, order):
     return ups
 
 
-def _reservoirs(S, cells, river_land):
+def read_sh_csv(path):
+    """An S-H table (read_sh_csv, io.jl:1129-1140): the columns headed H and S (any case) of a
+    comma-separated file with one header line."""
+    with open(path) as f:
+        names = [c.strip().strip('"').upper() for c in f.readline().split(",")]
+        data = np.loadtxt(f, delimiter=",", ndmin=2)
+    if "H" not in names or "S" not in names:
+        raise ValueError(f"{path} needs to provide H and S columns, got {names}")
+    return data[:, names.index("H")].copy(), data[:, names.index("S")].copy()
+
+
+def read_hq_csv(path):
+    """An H-Q table (read_hq_csv, io.jl:1143-1147): after one header line, the level in the first
+    column and the discharge of each of the 365 days of the year in the next 365."""
+    data = np.loadtxt(path, delimiter=",", skiprows=1, ndmin=2)
+    return data[:, 0].copy(), np.ascontiguousarray(data[:, 1:366])
+
+
+def write_sh_csv(path, h, s):
+    np.savetxt(path, np.column_stack([h, s]), delimiter=",", header="H,S", comments="", fmt="%.17g")
+
+
+def write_hq_csv(path, h, q):
+    header = "H," + ",".join(str(d) for d in range(1, 366))
+    np.savetxt(path, np.column_stack([h, q]), delimiter=",", header=header, comments="", fmt="%.17g")
+
+
+def _reservoirs(S, cells, river_land, folder):
     """Reservoirs at the river cells where reservoir_location__count > 0, in river order
-    (network.jl:314-350), with their parameters (reservoir.jl:40-200) and initial water level."""
+    (network.jl:314-350), with their parameters (reservoir.jl:40-200), initial water level, storage
+    profile, link to a lower reservoir and the S-H / H-Q tables of the CSV files
+    reservoir_sh_<id>.csv and reservoir_hq_<id>.csv beside the static maps (reservoir.jl:152-192)."""
     if not S.has("reservoir_location__count"):
         return None
     loc = S.read("reservoir_location__count", default=0.0).reshape(-1)[cells][river_land]
@@ -343,10 +374,40 @@ def _reservoirs(S, cells, river_land):
                     ("target_minimum_fraction", "reservoir_water__target_min_volume_fraction"),
                     ("target_full_fraction", "reservoir_water__target_full_volume_fraction")]:
         res[key] = at(sn, nan)
+    ids_r = ids[ri]
+    k = len(ri)
+    prof = at("reservoir_water__storage_curve_type_count", 1.0)
+    prof = np.where(np.isnan(prof), 1.0, prof).astype(np.int32)
+    linked = at("reservoir_lower_location__count", 0.0)
+    linked = np.where(np.isnan(linked), 0.0, linked)
+    lower = np.full(k, -1, np.int32)
+    for i in range(k):
+        if linked[i] > 0:
+            match = np.flatnonzero(ids_r == linked[i])
+            if len(match) != 1:
+                raise ValueError(f"reservoir {ids_r[i]:g}: lower reservoir {linked[i]:g} not found once")
+            lower[i] = match[0]
+    tables = any(prof == 2) or any(res["outflow_curve_type"] == 1) or any(lower >= 0)
+    if tables:
+        sh_h, sh_s, hq_h, hq_q, sh_off, hq_off = [], [], [], [], [0], [0]
+        for i in range(k):
+            rid = int(ids_r[i])
+            if prof[i] == 2:
+                h, sv = read_sh_csv(Path(folder) / f"reservoir_sh_{rid}.csv")
+                sh_h.append(h)
+                sh_s.append(sv)
+            sh_off.append(sh_off[-1] + (len(sh_h[-1]) if prof[i] == 2 else 0))
+            if res["outflow_curve_type"][i] == 1:
+                h, q = read_hq_csv(Path(folder) / f"reservoir_hq_{rid}.csv")
+                hq_h.append(h)
+                hq_q.append(q.reshape(-1))
+            hq_off.append(hq_off[-1] + (len(hq_h[-1]) if res["outflow_curve_type"][i] == 1 else 0))
+        cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0)  # noqa: E731
+        res.update(storage_curve_type=prof, sh_offset=np.array(sh_off, np.int64), sh_h=cat(sh_h), sh_s=cat(sh_s),
+                   hq_offset=np.array(hq_off, np.int64), hq_h=cat(hq_h), hq_q=cat(hq_q), lower_reservoir=lower)
     out = {k: np.ascontiguousarray(v) for k, v in res.items()}
     # the reservoirs' areas: grid cells (flat y * nx + x, active or not) of each reservoir id
     # (network.jl:325-347), for averaging the forcing over them
-    ids_r = ids[ri]
     if S.has("reservoir_area__count"):
         area_map = S.read("reservoir_area__count").reshape(-1)
         out["coverage_cells"] = [np.flatnonzero(area_map == v) for v in ids_r]
@@ -412,7 +473,21 @@ def write_staticmaps(dom, path, grid=None, reservoirs=None, format=2, names=None
         maps["reservoir_area__count"] = (ncio.NC_INT, grid_of(np.arange(1, k + 1), cells, 0.0), -999.0)
         maps["reservoir_water__rating_curve_type_count"] = (ncio.NC_INT, grid_of(reservoirs["outflow_curve_type"],
                                                                                  cells), -999.0)
-        maps["reservoir_water__storage_curve_type_count"] = (ncio.NC_INT, grid_of(np.ones(k), cells), -999.0)
+        prof = reservoirs.get("storage_curve_type", np.ones(k))
+        maps["reservoir_water__storage_curve_type_count"] = (ncio.NC_INT, grid_of(prof, cells), -999.0)
+        if "lower_reservoir" in reservoirs:  # ids are 1..k in reservoir order
+            lo = np.asarray(reservoirs["lower_reservoir"])
+            maps["reservoir_lower_location__count"] = (ncio.NC_INT, grid_of(np.where(lo >= 0, lo + 1, 0), cells, 0.0),
+                                                       -999.0)
+        folder = Path(path).parent
+        for i in range(k):  # the CSV tables beside the static maps (reservoir.jl:152-192)
+            if "sh_offset" in reservoirs and prof[i] == 2:
+                a, b = reservoirs["sh_offset"][i], reservoirs["sh_offset"][i + 1]
+                write_sh_csv(folder / f"reservoir_sh_{i + 1}.csv", reservoirs["sh_h"][a:b], reservoirs["sh_s"][a:b])
+            if "hq_offset" in reservoirs and reservoirs["outflow_curve_type"][i] == 1:
+                a, b = reservoirs["hq_offset"][i], reservoirs["hq_offset"][i + 1]
+                write_hq_csv(folder / f"reservoir_hq_{i + 1}.csv", reservoirs["hq_h"][a:b],
+                             reservoirs["hq_q"][a * 365:b * 365].reshape(-1, 365))
         for key, sn in [("area", "reservoir_surface__area"), ("waterlevel", "reservoir_water_surface__initial_elevation"),
                         ("maximum_storage", "reservoir_water__max_volume"),
                         ("threshold", "reservoir_water_flow_threshold_level__elevation"),

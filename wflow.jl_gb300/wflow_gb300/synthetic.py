@@ -315,6 +315,121 @@ def make_reservoirs(dom, n, seed=1, types=(abi.WF_RES_SIMPLE, abi.WF_RES_MODIFIE
     return {key: np.ascontiguousarray(v) for key, v in res.items()}
 
 
+TABLE_KEYS = ("storage_curve_type", "sh_offset", "sh_h", "sh_s", "hq_offset", "hq_h", "hq_q", "lower_reservoir")
+
+
+def _sh_table(area, wl, rng, rows=9):
+    """An S-H table around water level `wl`: storage grows a little faster than linearly with
+    the level (a basin widening upward), zero at the lowest level."""
+    h = wl + np.linspace(-3.0, 4.0, rows)
+    s = area * (h - h[0]) ** rng.uniform(1.05, 1.3) + np.arange(rows) * 1e-3 * area
+    return h, s
+
+
+def _hq_table(wl, threshold, rng, rows=7):
+    """An H-Q table: no outflow up to `threshold`, then a weir-like rise; the discharge of each
+    day of the year varies seasonally by +-30 %."""
+    h = np.sort(np.concatenate([[threshold], wl + np.linspace(-2.5, 4.5, rows - 1)]))
+    h = np.unique(h)
+    base = np.where(h > threshold, rng.uniform(0.5, 2.0) * np.maximum(h - threshold, 0.0) ** 1.5, 0.0)
+    season = 1.0 + 0.3 * np.sin(2.0 * np.pi * (np.arange(365) + rng.uniform(0, 365)) / 365.0)
+    return h, np.ascontiguousarray(np.outer(base, season))
+
+
+def make_linked_reservoirs(dom, seed=1, extra=2):
+    """Reservoirs with tables and a link (ReservoirParameters, reservoir.jl:5-44): an upper free
+    weir linked to a lower reservoir a few river cells downstream on the main stem (both with
+    interpolated S-H profiles, the lower one released by a rating curve), the lower reservoir's
+    level above the upper one's at the start so that water first flows back; plus `extra`
+    reservoirs elsewhere (a modified Puls with the linear profile and a simple reservoir with an
+    interpolated profile, cycling)."""
+    rng = np.random.default_rng([int(seed), 91])
+    rds = dom.river["river_downstream"]
+    nr = rds.size
+    rland = dom.river["river_land_index"]
+    up = np.asarray(dom.upstream_cells)[rland]
+    # main stem: from the outlet upward, always into the upstream neighbour of largest area
+    children = [[] for _ in range(nr)]
+    for v in range(nr):
+        if rds[v] >= 0:
+            children[rds[v]].append(v)
+    outlet = int(np.argmax(np.where(rds < 0, up, -1)))
+    stem = [outlet]
+    while children[stem[-1]]:
+        stem.append(max(children[stem[-1]], key=lambda c: up[c]))
+    lo_v, up_v = stem[len(stem) // 3], stem[len(stem) // 3 + 4]  # four river cells apart
+    others = [int(v) for v in np.argsort(-up, kind="stable")
+              if rds[v] >= 0 and v not in stem and rds[v] not in stem][: 8 * extra]
+    rng.shuffle(others)
+    chosen, fed = [up_v, lo_v], {int(rds[up_v]), int(rds[lo_v])}
+    for v in others:
+        if len(chosen) == 2 + extra:
+            break
+        if int(rds[v]) in fed or v in chosen:
+            continue
+        chosen.append(v)
+        fed.add(int(rds[v]))
+    k = len(chosen)
+    t = np.array([abi.WF_RES_FREE_WEIR, abi.WF_RES_RATING_CURVE]
+                 + [(abi.WF_RES_MODIFIED_PULS, abi.WF_RES_SIMPLE)[i % 2] for i in range(k - 2)], np.int32)
+    area = rng.uniform(5.0e4, 2.0e5, k)
+    wl = np.concatenate([[5.0, 5.3], rng.uniform(2.0, 8.0, k - 2)])
+    prof = np.array([2, 2] + [(1, 2)[i % 2] for i in range(k - 2)], np.int32)
+    nan = np.full(k, np.nan)
+    simple = t == abi.WF_RES_SIMPLE
+    weir = (t == abi.WF_RES_FREE_WEIR) | (t == abi.WF_RES_MODIFIED_PULS)
+    thr = np.where(weir | (t == abi.WF_RES_RATING_CURVE), wl - rng.uniform(0.2, 0.8, k), nan)
+    sh_h, sh_s, sh_off, hq_h, hq_q, hq_off = [], [], [0], [], [], [0]
+    s0 = area * wl
+    for i in range(k):
+        if prof[i] == 2:
+            h, sv = _sh_table(area[i], wl[i], rng)
+            sh_h.append(h)
+            sh_s.append(sv)
+            s0[i] = np.interp(wl[i], h, sv)
+        sh_off.append(sh_off[-1] + (len(sh_h[-1]) if prof[i] == 2 else 0))
+        if t[i] == abi.WF_RES_RATING_CURVE:
+            h, q = _hq_table(wl[i], thr[i], rng)
+            hq_h.append(h)
+            hq_q.append(q)
+        hq_off.append(hq_off[-1] + (len(hq_h[-1]) if t[i] == abi.WF_RES_RATING_CURVE else 0))
+    lower = np.full(k, -1, np.int32)
+    lower[0] = 1
+    res = dict(
+        river_index=np.array(chosen, np.int32), outflow_curve_type=t, area=area, waterlevel=wl,
+        maximum_storage=np.where(simple, s0 * rng.uniform(1.05, 1.4, k), nan),
+        threshold=np.where(weir, thr, nan),
+        rating_curve_coefficient=np.where(weir, rng.uniform(0.5, 5.0, k), nan),
+        rating_curve_exponent=np.where(t == abi.WF_RES_FREE_WEIR, rng.uniform(1.2, 2.0, k), nan),
+        maximum_release=np.where(simple, rng.uniform(0.5, 5.0, k), nan),
+        demand=np.where(simple, rng.uniform(0.01, 0.3, k), nan),
+        target_minimum_fraction=np.where(simple, rng.uniform(0.05, 0.2, k), nan),
+        target_full_fraction=np.where(simple, rng.uniform(0.6, 0.9, k), nan),
+        storage_curve_type=prof, sh_offset=np.array(sh_off, np.int64),
+        sh_h=np.concatenate(sh_h) if sh_h else np.zeros(0), sh_s=np.concatenate(sh_s) if sh_s else np.zeros(0),
+        hq_offset=np.array(hq_off, np.int64), hq_h=np.concatenate(hq_h) if hq_h else np.zeros(0),
+        hq_q=np.concatenate(hq_q).reshape(-1) if hq_q else np.zeros(0), lower_reservoir=lower,
+    )
+    return {key: np.ascontiguousarray(v) for key, v in res.items()}
+
+
+def c_reservoir_tables(res):
+    """WfReservoirTables struct pointing into a reservoir dict's table arrays (keep `res` alive),
+    or None when the dict has no tables or links."""
+    import ctypes as C
+    if res is None or not any(k in res for k in TABLE_KEYS):
+        return None
+    t = abi.WfReservoirTables()
+    for k in TABLE_KEYS:
+        a = res.get(k)
+        if a is None:
+            continue
+        ct = C.c_int32 if k in ("storage_curve_type", "lower_reservoir") else C.c_int64 if k.endswith("offset") \
+            else C.c_double
+        setattr(t, k, abi.as_ptr(a, ct))
+    return t
+
+
 def reservoir_forcing(dom, res, P, PET, M=1):
     """Reservoir precipitation and evaporation of a step [m s-1], member-major, taken from the
     land forcing at each reservoir's outlet cell (a one-cell reservoir area; Wflow averages the
