@@ -248,7 +248,8 @@ typedef enum WfReservoirOutflow {
 } WfReservoirOutflow;
 
 /* Reservoirs at river cells (reservoir__flag; reservoir.jl:1-300, network.jl:296-357), with the
- * linear storage profile S = A H (storage_curve_type 1). The reservoir's outlet cell becomes a pit
+ * linear storage profile S = A H (storage_curve_type 1) unless WfReservoirTables gives an S-H
+ * table (wf_create_with_reservoir_tables). The reservoir's outlet cell becomes a pit
  * of the land and river upstream lists (domain.jl:95-121): the outlet cell's overland and
  * subsurface discharge feed the reservoir (surface_kinwave.jl:771-802), its river discharge
  * enters the reservoir within the river sweep and the reservoir outflow is the inflow of the
