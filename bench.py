@@ -686,7 +686,8 @@ def run_profile(args):
     side, cell, dt, members, _ = WORKLOADS[args.workload]
     model = Model(cfg, dom, params=params)
     model.set_tuning(vertical_block=128, routing_warps=2, routing_blocks_per_sm=0, use_graph=0, kernel_timing=1,
-                     substep_lanes=args.sub_lanes, sweep_inputs=args.sweep_inputs)
+                     substep_lanes=args.sub_lanes, sweep_inputs=args.sweep_inputs,
+                     separate_overland_river=args.separate_overland_river)
     for s in range(args.steps):
         P, PET, T = member_forcing(s, dt, dom.n_land, members, pfac, seed=args.seed)
         model.run_timestep(P, PET, T)
@@ -769,6 +770,8 @@ def main():
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64 plain comparison leg")
     ap.add_argument("--sub-lanes", type=int, default=0,
                     help="profiler driver: cap of the routing sweeps' sub-step lanes (0: the library default)")
+    ap.add_argument("--separate-overland-river", type=int, default=0, choices=[0, 1],
+                    help="--profile: 1 runs the split form's overland and river sweeps in separate launches")
     ap.add_argument("--sweep-inputs", type=int, default=0,
                     help="profiler driver: bit k keeps the inputs of node-major sweep k (0 subsurface, 1 "
                          "overland, 2 river) in registers instead of staging them in shared memory")

@@ -182,14 +182,15 @@ def test_graph_and_eager_paths_agree(gpu_lib):
 
 def test_launch_tuning_leaves_split_results_unchanged(gpu_lib):
     # the launch shapes the autotuner picks (resident warps, sub-step lanes, staged or register
-    # sweep inputs, the vertical kernel's block and grid) change no arithmetic of the split form
+    # sweep inputs, the vertical kernel's block and grid, the overland and river sweeps in one
+    # launch or two) change no arithmetic of the split form
     dom = synthetic.make_domain(48, 1000.0, seed=12)
     M = 32
     cfg = synthetic.make_config(3600.0, n_members=M, form=abi.WF_FORM_SPLIT)
     a = Model(cfg, dom)
     b = Model(cfg, dom)
     b.set_tuning(routing_warps=2, routing_blocks_per_sm=3, substep_lanes=4, sweep_inputs=5,
-                 vertical_block=128, vertical_blocks_per_sm=1)
+                 vertical_block=128, vertical_blocks_per_sm=1, separate_overland_river=1)
     for s in range(4):
         P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=12)
         P, PET, T = (np.tile(x, M) for x in (P, PET, T))
@@ -197,9 +198,31 @@ def test_launch_tuning_leaves_split_results_unchanged(gpu_lib):
         b.run_timestep(P, PET, T)
     for f in ["SATURATED_WATER_DEPTH", "SSF_Q", "LAND_Q", "RIVER_Q", "TOTAL_STORAGE"]:
         assert np.array_equal(a.get_value(f), b.get_value(f)), f
-    for bad in (dict(vertical_blocks_per_sm=-1), dict(vertical_blocks_per_sm=65), dict(sweep_inputs=8)):
+    for bad in (dict(vertical_blocks_per_sm=-1), dict(vertical_blocks_per_sm=65), dict(sweep_inputs=8),
+                dict(separate_overland_river=2)):
         with pytest.raises(RuntimeError):
             b.set_tuning(**bad)
+
+
+@pytest.mark.parametrize("M,lanes", [(1, 0), (1, 1), (64, 0), (64, 1)])
+def test_shared_overland_river_launch_matches_separate_launches(gpu_lib, M, lanes):
+    # hourly steps: one overland sub-step and four river sub-steps, all in the shared launch
+    # (lanes 0: the river's first-dispatched chains on the diagonal schedule, 1: all node-major);
+    # a stale lateral inflow (a river node not waiting for the overland walker) would show here
+    dom = synthetic.make_domain(64, 250.0, seed=15)
+    cfg = synthetic.make_config(3600.0, n_members=M, form=abi.WF_FORM_SPLIT)
+    a = Model(cfg, dom)
+    a.set_tuning(substep_lanes=lanes)
+    b = Model(cfg, dom)
+    b.set_tuning(separate_overland_river=1)
+    for s in range(6):
+        P, PET, T = synthetic.forcing(s, cfg.dt, dom.n_land, seed=15, precip_scale=2.0 + s)
+        P, PET, T = (np.tile(x, M) for x in (P, PET, T))
+        a.run_timestep(P, PET, T)
+        b.run_timestep(P, PET, T)
+        for f in ["RIVER_Q", "RIVER_INWATER", "LAND_Q", "BALANCE_RIVER_ERROR"]:
+            assert np.array_equal(a.get_value(f), b.get_value(f)), (s, f)
+    assert np.abs(a.get_value("RIVER_INWATER")).max() > 0.0
 
 
 def test_bounded_wait_reports_error_and_recovers(gpu_lib):

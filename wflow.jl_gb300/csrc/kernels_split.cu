@@ -1573,10 +1573,38 @@ struct SsfWave {
     }
 };
 
+// The lateral inflow of river cell rs (element re) from the land cell of element le, with trsum
+// the step's sum of the overland flow to the river (update_lateral_inflow!,
+// surface_kinwave.jl:710-734): stores the river cell's inflow, lateral inflow and the lateral
+// inflow with the external inflow, and returns the latter. One function for the overland
+// wavefront and the per-cell completion kernel, so both give the same words.
+__device__ __forceinline__ wff::ff river_lateral(const WfDevFields& F, int64_t le, int64_t rs, int64_t re,
+                                                 wff::ff trsum) {
+    using wff::ff;
+    const ff tr_avg = wff::mul(trsum, ff{F.inv_dt_hi, F.inv_dt_lo});
+    const ff inv_len = ldrs(F, R_INV_LENGTH, rs);
+    const ff inw = wff::add(wff::add(ldm(F, SSF_TR_AVG, le), tr_avg),
+                            wff::mul(ldm(F, NET_RUNOFF_RIVER, le), ldrs(F, R_AREA, rs)));
+    str(F, RV_INWATER, re, inw);
+    const ff qlat = wff::mul(inw, inv_len);
+    str(F, RV_QLAT, re, qlat);
+    const float ext = F.Rf[R_EXT_INFLOW][rs];
+    const ff qlt = ext < 0.0f ? qlat : wff::add(qlat, wff::mul(inv_len, ext));
+    F.RMh[RV_QLATTH][re] = qlt.hi;
+    F.RMh[RV_QLATTL][re] = qlt.lo;
+    return qlt;
+}
+
 // Overland flow (surface_process.jl:24-70 per node, routing/surface_kinwave.jl sub-steps) in
 // double-FP32: discharge, u = Q^0.2 and the lateral inflow are pairs of FP32 arrays. ADAPT: one
 // sub-step per launch of each member's own (adaptive) size.
-template <bool ADAPT>
+// At the land cell of a river cell the walker also sums the upstream discharge that goes to the
+// river (q of each upstream cell times its flow fraction to the river, times the sub-step;
+// to_river_cumulative, surface_kinwave.jl:310-318), the only cells where it is not zero
+// (get_flow_fraction_to_river, utils.jl:485-505). FUSE: a river wavefront shares the launch;
+// after the step's last sub-step the walker publishes the river cell's lateral inflow for it
+// (F.rv_lat_pub).
+template <bool ADAPT, bool FUSE = false>
 struct OlWave {
     static constexpr int kDepth = 2;
     WfDevFields F;
@@ -1586,8 +1614,20 @@ struct OlWave {
         wff::ff u, q, qlat, invdx;
         float alpha;
         bool sfw_pos;
+        int32_t rs;           // river slot of the cell, or -1
+        float fr_hv, fr0, fr1;  // fractions to the river of the heavy child and light children 0, 1
         wfv::UpRec up;
     };
+    __device__ __forceinline__ void load_river(int64_t slot, In& x) const {
+        if (x.rs >= 0) {
+            const float4 f = g.up_frec[slot];
+            x.fr_hv = f.x;
+            x.fr0 = f.y;
+            x.fr1 = f.z;
+        } else {
+            x.fr_hv = x.fr0 = x.fr1 = 0.0f;
+        }
+    }
     __device__ __forceinline__ void load(int64_t slot, int64_t e, int m, In& x) const {
         float* const* Mh = F.Mh;
         x.u = {Mh[OL_UH][e], Mh[OL_UL][e]};
@@ -1596,11 +1636,13 @@ struct OlWave {
         x.invdx = {F.Lf[INV_FLOW_LENGTH][slot], F.Lf[INV_DX_LO][slot]};
         x.alpha = F.Lf[OL_ALPHA][slot];
         x.sfw_pos = F.Lf[SFW][slot] > 0.0f;
+        x.rs = (int32_t)F.land_river_slot[slot];
+        load_river(slot, x);
         wfv::load_rec<true>(g, slot, x.up);
     }
     // the same inputs staged in shared memory (wfv::walk_ring)
     static constexpr int kSweep = 1;
-    static constexpr int kWords = 10;
+    static constexpr int kWords = 14;
     static constexpr bool kWeighted = true;
     __device__ __forceinline__ void sources(int64_t slot, int64_t e, const void** src) const {
         src[0] = &F.Mh[OL_UH][e];
@@ -1613,6 +1655,10 @@ struct OlWave {
         src[7] = &F.Lf[INV_DX_LO][slot];
         src[8] = &F.Lf[OL_ALPHA][slot];
         src[9] = &F.Lf[SFW][slot];
+        src[10] = &F.land_river_slot[slot];  // the low word (slots < 2^31; -1 stays -1)
+        src[11] = &g.up_frec[slot].x;
+        src[12] = &g.up_frec[slot].y;
+        src[13] = &g.up_frec[slot].z;
     }
     __device__ __forceinline__ void from_words(const uint32_t* w, int st, In& x) const {
         auto f = [&](int i) { return __uint_as_float(w[i * st]); };
@@ -1622,14 +1668,72 @@ struct OlWave {
         x.invdx = {f(6), f(7)};
         x.alpha = f(8);
         x.sfw_pos = f(9) > 0.0f;
+        x.rs = (int32_t)w[10 * st];
+        x.fr_hv = f(11);
+        x.fr0 = f(12);
+        x.fr1 = f(13);
     }
     struct St {
-        wff::ff u, qp, qsum;
+        wff::ff u, qp, qsum, trsum;
+        int32_t rs;
     };
     __device__ __forceinline__ void start(const In& x, St& st) const {
         st.u = x.u;
         st.qp = x.q;
         st.qsum = {0.0f, 0.0f};
+        st.trsum = {0.0f, 0.0f};
+        st.rs = x.rs;
+    }
+    // entry hook of the diagonal schedule (nothing to wait for)
+    __device__ __forceinline__ bool enter(St&, int64_t) const { return true; }
+    // gather_w<true> with, at the land cell of a river cell, the upstream flow to the river
+    __device__ __forceinline__ bool gather_tr(const In& x, unsigned long long w0, unsigned long long w1, int64_t slot,
+                                              int m, int s, bool heavy, unsigned long long qh, wff::ff& qin,
+                                              wff::ff& tr) const {
+        const wfv::UpRec& r = x.up;
+        const bool riv = x.rs >= 0;
+        wff::ff acc = {0.0f, 0.0f}, t = {0.0f, 0.0f};
+        if (heavy) {
+            const wff::ff q = wff::unpack(qh);
+            acc = wff::mul(q, r.w_hv);
+            if (riv) t = wff::mul(q, x.fr_hv);
+        }
+        if (r.lt0 >= 0) {
+            const int64_t idx = wfv::end_index(g, r.lt0, m, s);
+            unsigned long long first = w0;
+            if (first == wfv::SENTINEL) first = wfv::ld_relaxed(&g.end_q[idx]);
+            unsigned long long w;
+            if (!wfv::await_end(g, sw, idx, first, F.status, w)) return false;
+            const wff::ff q = wff::unpack(w);
+            acc = wff::add(acc, wff::mul(q, r.w_lt0));
+            if (riv) t = wff::add(t, wff::mul(q, x.fr0));
+        }
+        if (r.lt1 >= 0) {
+            const int64_t idx = wfv::end_index(g, r.lt1, m, s);
+            unsigned long long first = w1;
+            if (first == wfv::SENTINEL) first = wfv::ld_relaxed(&g.end_q[idx]);
+            unsigned long long w;
+            if (!wfv::await_end(g, sw, idx, first, F.status, w)) return false;
+            const wff::ff q = wff::unpack(w);
+            acc = wff::add(acc, wff::mul(q, r.w_lt1));
+            if (riv) t = wff::add(t, wff::mul(q, x.fr1));
+        }
+        if (r.n_lt > 2) {  // further light children, in up-list order after the first two
+            int seen = 0;
+            for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
+                const int32_t uc = g.up_chain[o];
+                if (uc < 0 || ++seen <= 2) continue;
+                const int64_t idx = wfv::end_index(g, uc, m, s);
+                unsigned long long w;
+                if (!wfv::await_end(g, sw, idx, wfv::ld_relaxed(&g.end_q[idx]), F.status, w)) return false;
+                const wff::ff q = wff::unpack(w);
+                acc = wff::add(acc, wff::mul(q, g.up_wf[o]));
+                if (riv) t = wff::add(t, wff::mul(q, g.up_frf[o]));
+            }
+        }
+        qin = acc;
+        tr = t;
+        return true;
     }
     // sub-step s of the node
     __device__ __forceinline__ bool sub(const In& x, St& st, unsigned long long w0, unsigned long long w1,
@@ -1639,8 +1743,8 @@ struct OlWave {
         DT dt_s;
         if constexpr (ADAPT) dt_s = wff::ff{sw.adt_hi[m], sw.adt_lo[m]};
         else dt_s = sw.dts_f[s];
-        wff::ff qin;
-        if (!wfv::gather_w<true>(g, sw, x.up, w0, w1, slot, m, s, heavy, qh_in, F.status, qin)) return false;
+        wff::ff qin, tr;
+        if (!gather_tr(x, w0, w1, slot, m, s, heavy, qh_in, qin, tr)) return false;
         if (!x.sfw_pos) qin = {0.0f, 0.0f};
         wff::ff un, qn;
         kw_node_ff<ADAPT>(qin, st.qp, x.qlat, st.u, x.invdx, dt_s, x.alpha, un, qn);
@@ -1649,10 +1753,13 @@ struct OlWave {
         qh_out = wff::pack(qn);
         if (is_end) wfv::publish(g, chain, m, s, qn);
         st.qsum = wff::add(st.qsum, mul_dt(qn, dt_s));
+        if (x.rs >= 0) st.trsum = wff::add(st.trsum, mul_dt(tr, dt_s));
         return true;
     }
     // the node's state after the last sub-step of the launch (or of a round of the diagonal
-    // schedule); add_stored: the step's cumulative discharge so far is added
+    // schedule); add_stored: the step's cumulative discharge so far is added. At the land cell of
+    // a river cell, the flow to the river goes to the river cell's element; with FUSE, after the
+    // step's last sub-step, the river cell's lateral inflow is published.
     __device__ __forceinline__ void finish(const St& st, int64_t e, bool add_stored) const {
         float* const* Mh = F.Mh;
         Mh[OL_UH][e] = st.u.hi;
@@ -1662,6 +1769,16 @@ struct OlWave {
         if (add_stored) qsum = wff::add(qsum, wff::ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]});
         Mh[OL_QSUMH][e] = qsum.hi;
         Mh[OL_QSUML][e] = qsum.lo;
+        if (st.rs >= 0) {
+            const int m = (int)(e % F.M);
+            const int64_t re = (int64_t)st.rs * F.M + m;
+            wff::ff trsum = st.trsum;
+            if (add_stored) trsum = wff::add(trsum, wff::ff{F.RMh[RV_TRSUMH][re], F.RMh[RV_TRSUML][re]});
+            F.RMh[RV_TRSUMH][re] = trsum.hi;
+            F.RMh[RV_TRSUML][re] = trsum.lo;
+            if (FUSE && sw.last_of_step)
+                wfv::st_relaxed(&F.rv_lat_pub[re], wff::pack(river_lateral(F, e, st.rs, re, trsum)));
+        }
     }
     __device__ __forceinline__ bool node(const In& x, const wfv::Ends& ends, int64_t slot, int64_t e, int m,
                                          int64_t chain, bool is_end, bool heavy, unsigned long long* qh) {
@@ -1692,7 +1809,10 @@ struct OlWave {
 // RES: the model has reservoirs. At a reservoir cell the reservoir update follows the cell's
 // kinematic wave in every sub-step (FP64, wf_reservoir.cuh) and the reservoir's outflow, not the
 // cell's discharge, is handed downstream (heavy hand-off row and published chain end alike).
-template <bool ADAPT, bool RES>
+// FUSE: the overland wavefront shares the launch (its tickets first); a node takes its lateral
+// inflow from the word the overland walker publishes at the river cell's land cell
+// (F.rv_lat_pub), waiting for it like for a light child.
+template <bool ADAPT, bool RES, bool FUSE = false>
 struct RvWave {
     static constexpr int kDepth = 2;
     WfDevFields F;
@@ -1747,13 +1867,23 @@ struct RvWave {
         x.res = RES ? (int32_t)w[11 * st] : -1;
     }
     struct St {
-        wff::ff u, qp, qsum, asum;
+        wff::ff u, qp, qsum, asum, qlatt;
     };
     __device__ __forceinline__ void start(const In& x, St& st) const {
         st.u = x.u;
         st.qp = x.q;
         st.qsum = {0.0f, 0.0f};
         st.asum = {0.0f, 0.0f};
+        st.qlatt = x.qlatt;
+    }
+    // FUSE: the lateral inflow the overland walker publishes for element e (entry hook of both
+    // schedules); false when the wait ran out
+    __device__ __forceinline__ bool enter(St& st, int64_t e) const {
+        if (!FUSE) return true;
+        unsigned long long w;
+        if (!wfv::await_word(sw, &F.rv_lat_pub[e], F.status, w)) return false;
+        st.qlatt = wff::unpack(w);
+        return true;
     }
     // sub-step s of the node
     __device__ __forceinline__ bool sub(const In& x, St& st, unsigned long long w0, unsigned long long w1,
@@ -1771,7 +1901,7 @@ struct RvWave {
         }
         wff::ff qin;
         if (!wfv::gather_w<false>(g, sw, x.up, w0, w1, slot, m, s, heavy, qh_in, F.status, qin)) return false;
-        wff::ff ql = x.qlatt;
+        wff::ff ql = st.qlatt;
         if (x.ext < 0.0f) {  // abstraction: qlatt holds the lateral inflow alone
             const float storage = x.len * (x.alpha * (st.u.hi * st.u.hi * st.u.hi));
             const float absd = fminf(-x.ext, (storage / dt_f) * 0.80f);
@@ -1820,6 +1950,7 @@ struct RvWave {
         }
         St st;
         start(x, st);
+        if (!enter(st, e)) return false;
         for (int s = 0; s < sw.S; ++s) {
             unsigned long long out;
             if (!sub(x, st, wfv::end_word0(ends, s), s == 0 ? ends.lq1 : wfv::SENTINEL, slot, e, m, s, chain, is_end,
@@ -2072,32 +2203,26 @@ __global__ void __launch_bounds__(256) ol_post_kernel(WfDevFields F, WfDevGraph 
             stm(F, OL_H, e, wff::mul(a, inv_sfw));
             stm(F, OL_STORAGE, e, wff::mul(a, lds(F, FLOW_LENGTH, slot)));
         }
-        ff qin = {0.0f, 0.0f}, tr = {0.0f, 0.0f};
+        ff qin = {0.0f, 0.0f};
         for (int32_t o = g.up_ptr[slot]; o < g.up_ptr[slot + 1]; ++o) {
             const int64_t ue = g.up_slot[o] * M + m;
             const ff qs = {Mh[OL_QSUMH][ue], Mh[OL_QSUML][ue]};
             qin = wff::add(qin, wff::mul(qs, g.up_wf[o]));
-            tr = wff::add(tr, wff::mul(qs, g.up_frf[o]));
         }
         if (!(inv_sfw.hi > 0.0f)) qin = {0.0f, 0.0f};
         stm(F, OL_Q_AVG, e, wff::mul(ff{Mh[OL_QSUMH][e], Mh[OL_QSUML][e]}, inv_dt));
-        const ff tr_avg = wff::mul(tr, inv_dt);
-        stm(F, OL_TR_AVG, e, tr_avg);
         stm(F, OL_QIN_AVG, e, wff::mul(qin, inv_dt));
+        // the flow to the river, summed by the wavefront at the land cells of river cells (zero
+        // elsewhere), and the river cell's lateral inflow
         const int64_t rs = F.land_river_slot[slot];
+        ff tr_avg = {0.0f, 0.0f};
         if (rs >= 0) {
             const int64_t re = rs * M + m;
-            const ff inv_len = ldrs(F, R_INV_LENGTH, rs);
-            const ff inw = wff::add(wff::add(ldm(F, SSF_TR_AVG, e), tr_avg),
-                                    wff::mul(ldm(F, NET_RUNOFF_RIVER, e), ldrs(F, R_AREA, rs)));
-            str(F, RV_INWATER, re, inw);
-            const ff qlat = wff::mul(inw, inv_len);
-            str(F, RV_QLAT, re, qlat);
-            const float ext = F.Rf[R_EXT_INFLOW][rs];
-            const ff qlt = ext < 0.0f ? qlat : wff::add(qlat, wff::mul(inv_len, ext));
-            F.RMh[RV_QLATTH][re] = qlt.hi;
-            F.RMh[RV_QLATTL][re] = qlt.lo;
+            const ff trsum = {F.RMh[RV_TRSUMH][re], F.RMh[RV_TRSUML][re]};
+            tr_avg = wff::mul(trsum, inv_dt);
+            river_lateral(F, e, rs, re, trsum);
         }
+        stm(F, OL_TR_AVG, e, tr_avg);
     }
 }
 
@@ -2346,6 +2471,67 @@ cudaError_t wf_split_river_wave(const WfDevFields& F, const WfDevGraph& g, const
     }
     if (sw.aflag) return launch_wave(RvWave<true, false>{F, g, sw}, c);
     return launch_wave_sub(RvWave<false, false>{F, g, sw}, c);
+}
+
+namespace {
+template <class PA, class PB>
+__global__ void __launch_bounds__(128) wave_pair_kernel(PA pa, PB pb, int S_alloc) {
+    wfv::walk_pair(pa, pb, S_alloc, pa.F.status);
+}
+template <class PA, class PB>
+__global__ void __launch_bounds__(128) wave_pair_diag_kernel(PA pa, PB pb, int S_alloc, int64_t p_chunks, int SL) {
+    wfv::walk_pair_diag(pa, pb, S_alloc, p_chunks, SL, pa.F.status);
+}
+}  // namespace
+
+// The river's first-dispatched chunks run on the diagonal schedule when the river launch has
+// several sub-steps and the tuning's sub-step lanes (wave_sub_lanes) give more than one lane per
+// chain-member pair; the rest of both sweeps node-major.
+cudaError_t wf_split_overland_river_wave(const WfDevFields& F, const WfDevGraph& gl, const WfSweep& swl,
+                                         const WfDevGraph& gr, const WfSweep& swr, const WfLaunchCfg& c) {
+    using PA = OlWave<false, true>;
+    using PB = RvWave<false, false, true>;
+    PA pa{F, gl, swl};
+    PB pb{F, gr, swr};
+    pa.sw.SL = 1;
+    pb.sw.SL = 1;
+    const int threads = 32 * (c.walk_warps > 0 ? c.walk_warps : 4);
+    const int S_alloc = swl.S > swr.S ? swl.S : swr.S;
+    const int SL = wave_sub_lanes(swr.S, c);
+    int blocks_l, blocks_r;
+    if (SL <= 1) {
+        const size_t smem = wfv::walk_smem(threads, S_alloc);
+        auto kernel = wave_pair_kernel<PA, PB>;
+        cudaError_t err = wave_grid(kernel, threads, smem, c, gl, blocks_l, pa.sw.prio_items);
+        if (err != cudaSuccess) return err;
+        err = wave_grid(kernel, threads, smem, c, gr, blocks_r, pb.sw.prio_items);
+        if (err != cudaSuccess) return err;
+        kernel<<<blocks_l > blocks_r ? blocks_l : blocks_r, threads, smem, c.stream>>>(pa, pb, S_alloc);
+        return cudaGetLastError();
+    }
+    const size_t smem = wfv::pair_diag_smem(threads, S_alloc);
+    auto kernel = wave_pair_diag_kernel<PA, PB>;
+    int64_t prio_r;
+    cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    err = wave_grid(kernel, threads, smem, c, gl, blocks_l, pa.sw.prio_items);
+    if (err != cudaSuccess) return err;
+    err = wave_grid(kernel, threads, smem, c, gr, blocks_r, prio_r);
+    if (err != cudaSuccess) return err;
+    const int blocks = blocks_l > blocks_r ? blocks_l : blocks_r;
+    // at most half of the resident warps hold first-dispatched river tickets (diagonal items and
+    // node-major long chunks together), as in wave_grid
+    int per_sm = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    if (err != cudaSuccess) return err;
+    const int64_t resident = (int64_t)std::min(blocks, c.num_sms * std::max(per_sm, 1)) * (threads / 32);
+    const int64_t ipc_d = wf_items_per_chunk(gr.G, gr.M, SL);
+    const int64_t gpc = gr.M > 32 ? gr.M / 32 : 1;
+    const int64_t p_chunks = std::min<int64_t>(gr.n_long_chunks, (resident / 2) / ipc_d);
+    pb.sw.prio_items = std::max<int64_t>(0, std::min<int64_t>((gr.n_long_chunks - p_chunks) * gpc,
+                                                              resident / 2 - p_chunks * ipc_d));
+    kernel<<<blocks, threads, smem, c.stream>>>(pa, pb, S_alloc, p_chunks, SL);
+    return cudaGetLastError();
 }
 
 cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c) {

@@ -41,6 +41,7 @@ struct DevGraphAlloc {
     int4* up_rec = nullptr;
     float* up_whv = nullptr;
     uint8_t* up_nlt = nullptr;
+    float4* up_frec = nullptr;
     uint32_t* flags = nullptr;
     double* end_q = nullptr;
     unsigned long long* ticket = nullptr;
@@ -249,6 +250,7 @@ WfDevGraph dev_graph(const DevGraphAlloc& G, int M) {
     g.up_rec = G.up_rec;
     g.up_whv = G.up_whv;
     g.up_nlt = G.up_nlt;
+    g.up_frec = G.up_frec;
     g.flags = G.flags;
     g.end_q = G.end_q;
     g.ticket = G.ticket;
@@ -1298,11 +1300,13 @@ int32_t wf_create_with_reservoir_tables(const WfConfig* c, const WfDomain* d, co
         std::vector<int4> rec(std::max<int64_t>(P.n_slots, 1), int4{-1, -1, 0, 0});
         std::vector<float> whv(rec.size(), 0.0f);
         std::vector<uint8_t> nlt(rec.size(), 0);
+        std::vector<float4> frec(rec.size(), float4{0.0f, 0.0f, 0.0f, 0.0f});
         for (int64_t sl = 0; sl < P.n_slots; ++sl) {
             int lights = 0;
             for (int32_t o = P.up_ptr[sl]; o < P.up_ptr[sl + 1]; ++o) {
                 if (P.up_chain[o] < 0) {
                     whv[sl] = wf[o];
+                    frec[sl].x = frf[o];
                     continue;
                 }
                 float wo = wf[o];
@@ -1311,9 +1315,11 @@ int32_t wf_create_with_reservoir_tables(const WfConfig* c, const WfDomain* d, co
                 if (lights == 0) {
                     rec[sl].x = P.up_chain[o];
                     rec[sl].z = bits;
+                    frec[sl].y = frf[o];
                 } else if (lights == 1) {
                     rec[sl].y = P.up_chain[o];
                     rec[sl].w = bits;
+                    frec[sl].z = frf[o];
                 }
                 ++lights;
             }
@@ -1322,6 +1328,7 @@ int32_t wf_create_with_reservoir_tables(const WfConfig* c, const WfDomain* d, co
         CKR(upload(h, &G.up_rec, rec));
         CKR(upload(h, &G.up_whv, whv));
         CKR(upload(h, &G.up_nlt, nlt));
+        CKR(upload(h, &G.up_frec, frec));
     }
     // ---- split form: FP32 copies of the static fields and FP32 member fields
     if (F.split) {
@@ -1463,6 +1470,7 @@ int32_t wf_create_with_reservoir_tables(const WfConfig* c, const WfDomain* d, co
     // adaptive sub-steps that sub-step is the whole model step (used when every member's first
     // Courant sub-step reaches the end of the step, the usual case)
     F.ssf_single = F.split && h->h_dts_ssf.size() == 1;
+    if (F.split && PR.n_slots > 0) CKR(dalloc(h, &F.rv_lat_pub, (size_t)PR.n_slots * M));
     F.dt_ssf = h->h_dts_ssf[0];
     F.inv_dt_ssf = 1.0 / h->h_dts_ssf[0];
     F.inv_dt_hi = (float)F.inv_dt;
@@ -1880,15 +1888,17 @@ int32_t wf_set_tuning(WfHandle* h, const WfTuning* t) {
     if (t->reserved[4] < 0 || t->reserved[4] > 7) return set_err(h, WF_ERR_INVALID, "sweep input mask out of range");
     if (t->reserved[5] < 0 || t->reserved[5] > 64)
         return set_err(h, WF_ERR_INVALID, "vertical blocks per SM out of range");
-    for (int k = 6; k < 8; ++k)
-        if (t->reserved[k] != 0) return set_err(h, WF_ERR_INVALID, "reserved tuning fields must be 0");
+    if (t->reserved[6] < 0 || t->reserved[6] > 1)
+        return set_err(h, WF_ERR_INVALID, "overland-river launch switch must be 0 or 1");
+    if (t->reserved[7] != 0) return set_err(h, WF_ERR_INVALID, "reserved tuning fields must be 0");
     h->tuning = *t;
     h->graph_valid = false;
     // reserved[]: [0] = wait budget in microseconds, [1] = awaited-epoch offset (test hooks),
     // [2] = per-kernel event timing, [3] = cap of the routing sweeps' sub-step lanes (0 = default),
     // [4] = bit k: node-major sweep k (0 subsurface, 1 overland, 2 river) keeps its inputs in
     // registers instead of staging them in shared memory, [5] = blocks per SM of the split
-    // vertical kernel's grid-stride loop (0 = 16)
+    // vertical kernel's grid-stride loop (0 = 16), [6] = 1: the split form's overland and river
+    // sweeps in separate launches (0: one launch where the model allows it)
     if (t->reserved[0] > 0) h->wait_ns = (uint64_t)t->reserved[0] * 1000ull;
     h->wait_offset = (uint32_t)t->reserved[1];
     h->kernel_timing = t->reserved[2] != 0;
@@ -2061,22 +2071,28 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
     };
     // split form: slim wavefronts (end_q sentinel hand-off, node-major sub-step groups)
     // followed by their per-cell completion kernels
-    auto wave = [&](DevGraphAlloc& G, const WfDevGraph& g, const std::vector<double>& dts, double* d_dts,
-                    int which) -> int {
+    auto wave_sw = [&](const DevGraphAlloc& G, const std::vector<double>& dts, double* d_dts, int first) {
         const int total = (int)dts.size();
         const int group = std::min<int>(G.s_cap, wfv::MAX_GROUP);
-        for (int first = 0; first < total; first += group) {
-            WfSweep sw{};
-            sw.S = std::min(group, total - first);
-            sw.first = first;
-            sw.last_of_step = (first + sw.S == total);
-            sw.total = total;
-            sw.epoch0 = 1;
-            sw.dt = h->cfg.dt;
-            sw.dts = d_dts + first;
-            for (int j = 0; j < sw.S && j < 16; ++j) sw.dts_f[j] = (float)dts[first + j];
-            sw.wait_ns = h->wait_ns;
-            sw.wait_offset = h->wait_offset;
+        WfSweep sw{};
+        sw.S = std::min(group, total - first);
+        sw.first = first;
+        sw.last_of_step = (first + sw.S == total);
+        sw.total = total;
+        sw.epoch0 = 1;
+        sw.dt = h->cfg.dt;
+        sw.dts = d_dts + first;
+        for (int j = 0; j < sw.S && j < 16; ++j) sw.dts_f[j] = (float)dts[first + j];
+        sw.wait_ns = h->wait_ns;
+        sw.wait_offset = h->wait_offset;
+        return sw;
+    };
+    auto wave = [&](DevGraphAlloc& G, const WfDevGraph& g, const std::vector<double>& dts, double* d_dts, int which,
+                    int first0 = 0) -> int {
+        const int total = (int)dts.size();
+        const int group = std::min<int>(G.s_cap, wfv::MAX_GROUP);
+        for (int first = first0; first < total; first += group) {
+            const WfSweep sw = wave_sw(G, dts, d_dts, first);
             CK(cudaMemsetAsync(G.end_q, 0xFF, (size_t)G.plan.n_chains * h->M * G.s_cap * sizeof(double), h->stream));
             CK(cudaMemsetAsync(G.ticket, 0, sizeof(unsigned long long), h->stream));
             cudaError_t e;
@@ -2182,12 +2198,37 @@ int enqueue_step(WfHandle* h, int64_t* launches) {
         else rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0);
         if (rc) return rc;
         mark(2);
-        if ((rc = wave(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
-        mark(3);
-        if ((rc = res_prep())) return rc;
-        if (h->nr > 0 && (rc = wave(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
-        if ((rc = res_post())) return rc;
-        mark(4);
+        // the overland sweep and the river's first sub-step group in one launch (the river cells
+        // take their lateral inflow from the overland walker as it passes them), unless the
+        // tuning asks for separate launches; models with reservoirs (whose inflow is the
+        // overland step average) and steps of more overland sub-steps than one launch holds
+        // keep them apart
+        const bool fuse = h->tuning.reserved[6] == 0 && h->nres == 0 && h->nr > 0 &&
+                          (int)h->h_dts_land.size() <= std::min<int>(h->land.s_cap, wfv::MAX_GROUP);
+        if (fuse) {
+            const WfSweep swl = wave_sw(h->land, h->h_dts_land, h->dts_land, 0);
+            const WfSweep swr = wave_sw(h->river, h->h_dts_river, h->dts_river, 0);
+            CK(cudaMemsetAsync(h->land.end_q, 0xFF,
+                               (size_t)h->land.plan.n_chains * h->M * h->land.s_cap * sizeof(double), h->stream));
+            CK(cudaMemsetAsync(h->river.end_q, 0xFF,
+                               (size_t)h->river.plan.n_chains * h->M * h->river.s_cap * sizeof(double), h->stream));
+            CK(cudaMemsetAsync(h->F.rv_lat_pub, 0xFF, (size_t)h->river.plan.n_slots * h->M * sizeof(double),
+                               h->stream));
+            CK(cudaMemsetAsync(h->land.ticket, 0, sizeof(unsigned long long), h->stream));
+            CK(wf_split_overland_river_wave(h->F, gl, swl, gr, swr, lc));
+            CK(wf_split_overland_post(h->F, gl, lc));
+            nl += 2;
+            mark(3);
+            if ((rc = wave(h->river, gr, h->h_dts_river, h->dts_river, 2, swr.S))) return rc;
+            mark(4);
+        } else {
+            if ((rc = wave(h->land, gl, h->h_dts_land, h->dts_land, 1))) return rc;
+            mark(3);
+            if ((rc = res_prep())) return rc;
+            if (h->nr > 0 && (rc = wave(h->river, gr, h->h_dts_river, h->dts_river, 2))) return rc;
+            if ((rc = res_post())) return rc;
+            mark(4);
+        }
     } else if (h->li) {
         // local-inertial land and river routing (surface_routing.jl:62-89) after the subsurface
         if ((rc = sweep(h->land, gl, h->h_dts_ssf, h->dts_ssf, 0))) return rc;

@@ -40,7 +40,8 @@
 #define WF_RM_FIELDS(X)                                                                            \
     X(RV_Q) X(RV_H) X(RV_STORAGE) X(RV_Q_AVG) X(RV_QIN_AVG) X(RV_INWATER) X(RV_QLAT) X(RV_ABS_AVG)    \
     X(RV_Q_CUM) X(RV_QIN_CUM) X(RV_ABS_CUM) X(BR_PREV) X(BR_ERR) X(BR_REL)                         \
-    X(RV_UH) X(RV_UL) X(RV_QSUMH) X(RV_QSUML) X(RV_ABSH) X(RV_ABSL) X(RV_QLATTH) X(RV_QLATTL)
+    X(RV_UH) X(RV_UL) X(RV_QSUMH) X(RV_QSUML) X(RV_ABSH) X(RV_ABSL) X(RV_QLATTH) X(RV_QLATTL)      \
+    X(RV_TRSUMH) X(RV_TRSUML)
 
 // Reservoirs, per reservoir and member (element r * M + m), FP64 in both forms. The first
 // fifteen follow the order of the WF_F_RESERVOIR_* field ids (WF_F_RESERVOIR_STORAGE + i).
@@ -172,6 +173,10 @@ struct WfDevFields {
     // local-inertial land and river routing in place of the kinematic waves (wf_li_couple.cuh):
     // the overland and river balances are the scheme's
     int32_t li_coupled;
+    // split form: the lateral inflow of each river cell and member as a packed double-FP32
+    // word, published by the overland wavefront for a river wavefront sharing its launch
+    // (filled with the sentinel pattern before such a launch)
+    unsigned long long* rv_lat_pub;  // [river slots * M]
 };
 
 // Routing graph on the device (one per land / river graph).
@@ -202,6 +207,9 @@ struct WfDevGraph {
     const int4* up_rec;
     const float* up_whv;
     const uint8_t* up_nlt;
+    // land graph: per slot, the fractions to the river of the heavy child and of light children
+    // 0 and 1 (up_frf of those entries; 0 where absent)
+    const float4* up_frec;
     uint32_t* flags;      // [n_chains * M] epoch of the last published sub-step
     double* end_q;        // [n_chains * M * s_cap] q of each chain end per sub-step
     unsigned long long* ticket;  // work counter of the current launch

@@ -52,6 +52,10 @@ cudaError_t wf_split_ssf_wave(const WfDevFields& F, const WfDevGraph& g, const W
 cudaError_t wf_split_overland_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw,
                                    const WfLaunchCfg& c);
 cudaError_t wf_split_river_wave(const WfDevFields& F, const WfDevGraph& g, const WfSweep& sw, const WfLaunchCfg& c);
+// The overland sweep (all its sub-steps, swl) and the river's first sub-step group (swr) in one
+// persistent launch; the land graph's ticket counter serves both (overland tickets first).
+cudaError_t wf_split_overland_river_wave(const WfDevFields& F, const WfDevGraph& gl, const WfSweep& swl,
+                                         const WfDevGraph& gr, const WfSweep& swr, const WfLaunchCfg& c);
 cudaError_t wf_split_ssf_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
 cudaError_t wf_split_overland_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);
 cudaError_t wf_split_river_post(const WfDevFields& F, const WfDevGraph& g, const WfLaunchCfg& c);

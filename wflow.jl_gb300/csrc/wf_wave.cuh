@@ -90,6 +90,30 @@ __device__ __forceinline__ bool await_end(const WfDevGraph& g, const WfSweep& sw
     }
 }
 
+// A published word at `p` other than an end_q slot (same sentinel and budget as await_end).
+__device__ __forceinline__ bool await_word(const WfSweep& sw, const unsigned long long* p, int32_t* status,
+                                           unsigned long long& out) {
+    unsigned long long b = ld_relaxed(p);
+    if (b != SENTINEL && sw.wait_offset == 0) {
+        out = b;
+        return true;
+    }
+    const uint64_t t0 = now_ns();
+    while (true) {
+        __nanosleep(32);
+        b = ld_relaxed(p);
+        if (b != SENTINEL && sw.wait_offset == 0) {
+            out = b;
+            return true;
+        }
+        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return false;
+        if (now_ns() - t0 > sw.wait_ns) {
+            atomicOr(status, WF_DEV_SPIN_TIMEOUT);
+            return false;
+        }
+    }
+}
+
 __device__ __forceinline__ void publish(const WfDevGraph& g, int64_t chain, int m, int s, wff::ff q) {
     st_relaxed(&g.end_q[end_index(g, chain, m, s)], wff::pack(q));
 }
@@ -246,13 +270,24 @@ __host__ __device__ constexpr size_t walk_smem(int threads, int substeps) {
 //             bool heavy, unsigned long long* qh)
 //     advances the node through sw.S sub-steps; qh[s * stride] holds the heavy child's packed
 //     discharge of sub-step s on entry and this node's on exit. Returns false to abort.
+// Tickets of a node-major sweep: the first prio_items take the longest items, longest first; the
+// rest take the others in dependency order, short ones in batches of BATCH.
+__device__ __forceinline__ uint64_t walk_tickets(const WfDevGraph& g, const WfSweep& sw) {
+    const int gpc = g.M > 32 ? g.M / 32 : 1;
+    const int64_t n_items = g.n_chunks * gpc;
+    const int64_t n_norm = n_items - sw.prio_items;
+    const int64_t n_short = min(g.n_short_chunks * gpc, n_norm);
+    const int64_t n_sb = (n_short + BATCH - 1) / BATCH;
+    return (uint64_t)(sw.prio_items + n_sb + (n_norm - n_short));
+}
+
+// One ticket t of a node-major sweep (walk_tickets). `wb` is the warp's batch descriptor, qh the
+// thread's hand-off row (qh[s * blockDim.x]). False when the sweep aborts (a wait ran out).
 template <class Phys>
-__device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
-    extern __shared__ unsigned long long wave_smem[];
+__device__ __forceinline__ bool walk_ticket(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status,
+                                            uint64_t t, WarpBatch* wb, unsigned long long* qh) {
     constexpr int DEPTH = Phys::kDepth;
     const unsigned lane = threadIdx.x & 31u;
-    unsigned long long* qh = wave_smem + threadIdx.x;  // row of this thread: qh[s * blockDim.x]
-    WarpBatch* wb = reinterpret_cast<WarpBatch*>(wave_smem + (size_t)blockDim.x * sw.S) + (threadIdx.x >> 5);
     const int M = g.M;
     const int gpc = M > 32 ? M / 32 : 1;
     const int gi = M <= 32 ? (int)lane / M : 0;
@@ -261,107 +296,138 @@ __device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phy
     const int64_t n_norm = n_items - prio;
     const int64_t n_short = min(g.n_short_chunks * gpc, n_norm);
     const int64_t n_sb = (n_short + BATCH - 1) / BATCH;
-    const uint64_t n_tickets = (uint64_t)(prio + n_sb + (n_norm - n_short));
+    int64_t first;
+    int count = 1;
+    if ((int64_t)t < prio) {
+        first = n_items - 1 - (int64_t)t;
+    } else {
+        const int64_t u = (int64_t)t - prio;
+        if (u < n_sb) {
+            first = u * BATCH;
+            count = (int)min((int64_t)BATCH, n_short - first);
+        } else {
+            first = n_short + (u - n_sb);
+        }
+    }
+    if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return false;
+    if ((int)lane < count) {
+        const int64_t item = first + lane;
+        const int64_t chunk = item / gpc;
+        wb->base[lane] = g.chunk_base[chunk];
+        wb->chain0[lane] = g.chunk_chain0[chunk];
+        wb->L[lane] = g.chunk_len[chunk];
+        wb->Gc[lane] = g.chunk_g[chunk];
+        wb->mbase[lane] = (int)(item % gpc) * 32;
+    }
+    __syncwarp();
+    for (int j = 0; j < count; ++j) {
+        const int Gc = wb->Gc[j];
+        wb->len[j][lane] = gi < Gc ? g.chain_len[wb->chain0[j] + gi] : 0;
+    }
+    __syncwarp();
+    const int m_fixed = (int)lane % (M <= 32 ? M : 32);
+    // the walk over the positions (item it, chain position k) of the batch
+    auto valid = [&](int it, int k) { return it < count && k < wb->len[it][lane]; };
+    auto slot_of = [&](int it, int k) { return wb->base[it] + (int64_t)k * wb->Gc[it] + gi; };
+    auto member = [&](int it) { return M > 32 ? wb->mbase[it] + (int)lane : m_fixed; };
+    auto advance = [&](int& it, int& k) {
+        if (k + 1 < wb->L[it]) {
+            ++k;
+        } else {
+            ++it;
+            k = 0;
+        }
+    };
+    typename Phys::In cur, nxt;
+    Ends ecur, enxt;
+    int cit = 0, ck = 0;
+    if (valid(cit, ck)) {
+        const int64_t sl = slot_of(cit, ck);
+        const int mm = member(cit);
+        phys.load(sl, sl * M + mm, mm, cur);
+        load_ends(g, sw, mm, cur.up, ecur);
+    }
+    int nit = cit, nk = ck;
+    advance(nit, nk);
+    if (DEPTH > 1 && valid(nit, nk)) {
+        const int64_t sl = slot_of(nit, nk);
+        const int mm = member(nit);
+        phys.load(sl, sl * M + mm, mm, nxt);
+    }
+    while (cit < count) {
+        int nnit = nit, nnk = nk;
+        if (nnit < count) advance(nnit, nnk);
+        typename Phys::In nn;
+        if (DEPTH > 1) {
+            if (valid(nit, nk)) load_ends(g, sw, member(nit), nxt.up, enxt);
+            if (valid(nnit, nnk)) {
+                const int64_t sl = slot_of(nnit, nnk);
+                const int mm = member(nnit);
+                phys.load(sl, sl * M + mm, mm, nn);
+            }
+        } else if (valid(nit, nk)) {
+            const int64_t sl = slot_of(nit, nk);
+            const int mm = member(nit);
+            phys.load(sl, sl * M + mm, mm, nxt);
+            load_ends(g, sw, mm, nxt.up, enxt);
+        }
+        bool ok = true;
+        if (valid(cit, ck)) {
+            const int64_t sl = slot_of(cit, ck);
+            const int mm = member(cit);
+            ok = phys.node(cur, ecur, sl, sl * M + mm, mm, wb->chain0[cit] + gi, ck == wb->len[cit][lane] - 1, ck > 0,
+                           qh);
+        }
+        if (__any_sync(0xffffffffu, !ok)) return false;
+        __syncwarp();
+        cur = nxt;
+        ecur = enxt;
+        if (DEPTH > 1) nxt = nn;
+        cit = nit;
+        ck = nk;
+        nit = nnit;
+        nk = nnk;
+    }
+    __syncwarp();
+    return true;
+}
+
+template <class Phys>
+__device__ __forceinline__ void walk(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
+    extern __shared__ unsigned long long wave_smem[];
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long* qh = wave_smem + threadIdx.x;  // row of this thread: qh[s * blockDim.x]
+    WarpBatch* wb = reinterpret_cast<WarpBatch*>(wave_smem + (size_t)blockDim.x * sw.S) + (threadIdx.x >> 5);
+    const uint64_t n_tickets = walk_tickets(g, sw);
     while (true) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(g.ticket, 1ULL);
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= n_tickets) return;
-        // the first prio_items tickets take the longest items, longest first; the rest take the
-        // others in dependency order, short ones in batches
-        int64_t first;
-        int count = 1;
-        if ((int64_t)t < prio) {
-            first = n_items - 1 - (int64_t)t;
-        } else {
-            const int64_t u = (int64_t)t - prio;
-            if (u < n_sb) {
-                first = u * BATCH;
-                count = (int)min((int64_t)BATCH, n_short - first);
-            } else {
-                first = n_short + (u - n_sb);
-            }
-        }
-        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
-        if ((int)lane < count) {
-            const int64_t item = first + lane;
-            const int64_t chunk = item / gpc;
-            wb->base[lane] = g.chunk_base[chunk];
-            wb->chain0[lane] = g.chunk_chain0[chunk];
-            wb->L[lane] = g.chunk_len[chunk];
-            wb->Gc[lane] = g.chunk_g[chunk];
-            wb->mbase[lane] = (int)(item % gpc) * 32;
-        }
-        __syncwarp();
-        for (int j = 0; j < count; ++j) {
-            const int Gc = wb->Gc[j];
-            wb->len[j][lane] = gi < Gc ? g.chain_len[wb->chain0[j] + gi] : 0;
-        }
-        __syncwarp();
-        const int m_fixed = (int)lane % (M <= 32 ? M : 32);
-        // the walk over the positions (item it, chain position k) of the batch
-        auto valid = [&](int it, int k) { return it < count && k < wb->len[it][lane]; };
-        auto slot_of = [&](int it, int k) { return wb->base[it] + (int64_t)k * wb->Gc[it] + gi; };
-        auto member = [&](int it) { return M > 32 ? wb->mbase[it] + (int)lane : m_fixed; };
-        auto advance = [&](int& it, int& k) {
-            if (k + 1 < wb->L[it]) {
-                ++k;
-            } else {
-                ++it;
-                k = 0;
-            }
-        };
-        typename Phys::In cur, nxt;
-        Ends ecur, enxt;
-        int cit = 0, ck = 0;
-        if (valid(cit, ck)) {
-            const int64_t sl = slot_of(cit, ck);
-            const int mm = member(cit);
-            phys.load(sl, sl * M + mm, mm, cur);
-            load_ends(g, sw, mm, cur.up, ecur);
-        }
-        int nit = cit, nk = ck;
-        advance(nit, nk);
-        if (DEPTH > 1 && valid(nit, nk)) {
-            const int64_t sl = slot_of(nit, nk);
-            const int mm = member(nit);
-            phys.load(sl, sl * M + mm, mm, nxt);
-        }
-        while (cit < count) {
-            int nnit = nit, nnk = nk;
-            if (nnit < count) advance(nnit, nnk);
-            typename Phys::In nn;
-            if (DEPTH > 1) {
-                if (valid(nit, nk)) load_ends(g, sw, member(nit), nxt.up, enxt);
-                if (valid(nnit, nnk)) {
-                    const int64_t sl = slot_of(nnit, nnk);
-                    const int mm = member(nnit);
-                    phys.load(sl, sl * M + mm, mm, nn);
-                }
-            } else if (valid(nit, nk)) {
-                const int64_t sl = slot_of(nit, nk);
-                const int mm = member(nit);
-                phys.load(sl, sl * M + mm, mm, nxt);
-                load_ends(g, sw, mm, nxt.up, enxt);
-            }
-            bool ok = true;
-            if (valid(cit, ck)) {
-                const int64_t sl = slot_of(cit, ck);
-                const int mm = member(cit);
-                ok = phys.node(cur, ecur, sl, sl * M + mm, mm, wb->chain0[cit] + gi, ck == wb->len[cit][lane] - 1,
-                               ck > 0, qh);
-            }
-            if (__any_sync(0xffffffffu, !ok)) return;
-            __syncwarp();
-            cur = nxt;
-            ecur = enxt;
-            if (DEPTH > 1) nxt = nn;
-            cit = nit;
-            ck = nk;
-            nit = nnit;
-            nk = nnk;
-        }
-        __syncwarp();
+        if (!walk_ticket(g, sw, phys, status, t, wb, qh)) return;
+    }
+}
+
+// Two node-major sweeps in one persistent launch: the tickets of sweep A (ga's counter) come
+// first, then those of sweep B, so every wait of a B node is on A work or on earlier B tickets,
+// all of them already dispatched to resident warps (A never waits on B). The hand-off rows are
+// sized for the larger sub-step count S_alloc of the two.
+template <class PhysA, class PhysB>
+__device__ __forceinline__ void walk_pair(PhysA& pa, PhysB& pb, int S_alloc, int32_t* status) {
+    extern __shared__ unsigned long long wave_smem[];
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long* qh = wave_smem + threadIdx.x;
+    WarpBatch* wb = reinterpret_cast<WarpBatch*>(wave_smem + (size_t)blockDim.x * S_alloc) + (threadIdx.x >> 5);
+    const uint64_t na = walk_tickets(pa.g, pa.sw), nb = walk_tickets(pb.g, pb.sw);
+    while (true) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(pa.g.ticket, 1ULL);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        bool ok;
+        if (t < na) ok = walk_ticket(pa.g, pa.sw, pa, status, t, wb, qh);
+        else if (t < na + nb) ok = walk_ticket(pb.g, pb.sw, pb, status, t - na, wb, qh);
+        else return;
+        if (!ok) return;
     }
 }
 
@@ -615,28 +681,168 @@ struct DiagBatch {  // per-warp shared descriptors of the items of the current t
 
 __host__ __device__ constexpr size_t diag_smem(int threads) { return (size_t)(threads / 32) * sizeof(DiagBatch); }
 
+// One ticket of a diagonal-schedule sweep: `count` consecutive items from `first` (wb: the warp's
+// descriptors). False when the sweep aborts.
 template <class Phys>
-__device__ __forceinline__ void walk_diag(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
-    extern __shared__ unsigned long long wave_smem[];
+__device__ __forceinline__ bool diag_ticket(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status,
+                                            int64_t first, int count, DiagBatch* wb) {
     constexpr int DEPTH = Phys::kDepth;
     using In = typename Phys::In;
     using St = typename Phys::St;
     const unsigned lane = threadIdx.x & 31u;
-    DiagBatch* wb = reinterpret_cast<DiagBatch*>(wave_smem) + (threadIdx.x >> 5);
     const int M = g.M;
     const int SL = sw.SL;
     const int J = 32 / SL;
     const int sl = (int)lane % SL;
     const int j = (int)lane / SL;
     const int64_t ipc = wf_items_per_chunk(g.G, M, SL);
+    const int rounds = (sw.S + SL - 1) / SL;
+    const bool launch_first = sw.first == 0;
+    if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return false;
+    if ((int)lane < count) {
+        const int64_t item = first + lane;
+        const int64_t chunk = item / ipc;
+        wb->base[lane] = g.chunk_base[chunk];
+        wb->chain0[lane] = g.chunk_chain0[chunk];
+        wb->L[lane] = g.chunk_len[chunk];
+        wb->Gc[lane] = g.chunk_g[chunk];
+        wb->p0[lane] = (int)(item % ipc) * J;
+    }
+    __syncwarp();
+    int npos = 0, work = 0;
+    for (int it = 0; it < count; ++it) {
+        const int p = wb->p0[it] + j;
+        const int gi = M <= 32 ? p / M : 0;
+        const bool ok = M <= 32 ? gi < wb->Gc[it] : p < M;
+        const int len = ok ? g.chain_len[wb->chain0[it] + gi] : 0;
+        wb->len[it][lane] = len;
+        work |= len;
+        npos += wb->L[it];
+    }
+    __syncwarp();
+    if (!__any_sync(0xffffffffu, work > 0)) return true;  // items past their chunks' pairs
+    auto gi_of = [&](int it) { return M <= 32 ? (wb->p0[it] + j) / M : 0; };
+    auto m_of = [&](int it) { return M <= 32 ? (wb->p0[it] + j) % M : wb->p0[it] + j; };
+    auto slot_of = [&](int it, int k) { return wb->base[it] + (int64_t)k * wb->Gc[it] + gi_of(it); };
+    auto valid = [&](int it, int k) { return it < count && k < wb->len[it][lane]; };
+    auto advance = [&](int& it, int& k) {
+        if (k + 1 < wb->L[it]) {
+            ++k;
+        } else {
+            ++it;
+            k = 0;
+        }
+    };
+    for (int r = 0; r < rounds; ++r) {
+        const int s = r * SL + sl;
+        const int s0 = r * SL;  // lane 0's sub-step
+        const bool last_lane = (s == sw.S - 1) || (sl == SL - 1);
+        // lane 0's pipeline over the sequence positions: cur (this time step), nxt, nn
+        In cur, nxt;
+        unsigned long long c0 = SENTINEL, c1 = SENTINEL, n0 = SENTINEL, n1 = SENTINEL;
+        int cit = 0, ck = 0;
+        if (sl == 0 && valid(cit, ck)) {
+            const int64_t sl0 = slot_of(cit, ck);
+            const int mm = m_of(cit);
+            phys.load(sl0, sl0 * M + mm, mm, cur);
+            load_words(g, mm, cur.up, s0, c0, c1);
+        }
+        int nit = cit, nk = ck;
+        advance(nit, nk);
+        if (DEPTH > 1 && sl == 0 && valid(nit, nk)) {
+            const int64_t sl1 = slot_of(nit, nk);
+            const int mm = m_of(nit);
+            phys.load(sl1, sl1 * M + mm, mm, nxt);
+        }
+        // what this lane works on at the current time step
+        In x;
+        St st;
+        unsigned long long w0 = SENTINEL, w1 = SENTINEL;
+        int pit = count, pk = 0;
+        unsigned long long hq = 0ull;
+        bool entered = true;  // lane 0: the node's entry hook succeeded (Phys::enter)
+        for (int tt = 0; tt < npos + SL - 1; ++tt) {
+            if (sl == 0) {
+                x = cur;
+                w0 = c0;
+                w1 = c1;
+                pit = cit;
+                pk = ck;
+                phys.start(x, st);
+                entered = !valid(pit, pk) || phys.enter(st, slot_of(pit, pk) * M + m_of(pit));
+                // advance the pipeline: the words of nxt, the inputs of the position after it
+                int nnit = nit, nnk = nk;
+                if (nnit < count) advance(nnit, nnk);
+                In nn;
+                if (DEPTH > 1) {
+                    if (valid(nit, nk)) load_words(g, m_of(nit), nxt.up, s0, n0, n1);
+                    if (valid(nnit, nnk)) {
+                        const int64_t sl2 = slot_of(nnit, nnk);
+                        const int mm = m_of(nnit);
+                        phys.load(sl2, sl2 * M + mm, mm, nn);
+                    }
+                } else if (valid(nit, nk)) {
+                    const int64_t sl1 = slot_of(nit, nk);
+                    const int mm = m_of(nit);
+                    phys.load(sl1, sl1 * M + mm, mm, nxt);
+                    load_words(g, mm, nxt.up, s0, n0, n1);
+                }
+                cur = nxt;
+                c0 = n0;
+                c1 = n1;
+                n0 = n1 = SENTINEL;
+                if (DEPTH > 1) nxt = nn;
+                cit = nit;
+                ck = nk;
+                nit = nnit;
+                nk = nnk;
+            }
+            bool ok = entered;
+            unsigned long long v0 = SENTINEL, v1 = SENTINEL;  // words of sub-step s + 1 for the next lane
+            if (pit < count && pk < wb->len[pit][lane] && s < sw.S) {
+                const int64_t slot = slot_of(pit, pk);
+                const int mm = m_of(pit);
+                const int64_t e = slot * M + mm;
+                if (sl + 1 < SL && s + 1 < sw.S) load_words(g, mm, x.up, s + 1, v0, v1);
+                unsigned long long out = 0ull;
+                ok = phys.sub(x, st, w0, w1, slot, e, mm, s, wb->chain0[pit] + gi_of(pit),
+                              pk == wb->len[pit][lane] - 1, pk > 0, hq, out);
+                hq = out;
+                if (ok && last_lane) phys.finish(st, e, r > 0 || !launch_first);
+            }
+            if (__any_sync(0xffffffffu, !ok)) return false;
+            // hand the node to the next lane
+            shfl_up_pod(x, SL);
+            shfl_up_pod(st, SL);
+            const int pit_up = __shfl_up_sync(0xffffffffu, pit, 1, SL);
+            const int pk_up = __shfl_up_sync(0xffffffffu, pk, 1, SL);
+            const unsigned long long v0_up = __shfl_up_sync(0xffffffffu, v0, 1, SL);
+            const unsigned long long v1_up = __shfl_up_sync(0xffffffffu, v1, 1, SL);
+            if (sl > 0) {
+                pit = pit_up;
+                pk = pk_up;
+                w0 = v0_up;
+                w1 = v1_up;
+            }
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+    return true;
+}
+
+template <class Phys>
+__device__ __forceinline__ void walk_diag(const WfDevGraph& g, const WfSweep& sw, Phys& phys, int32_t* status) {
+    extern __shared__ unsigned long long wave_smem[];
+    const unsigned lane = threadIdx.x & 31u;
+    DiagBatch* wb = reinterpret_cast<DiagBatch*>(wave_smem) + (threadIdx.x >> 5);
+    const int64_t ipc = wf_items_per_chunk(g.G, g.M, sw.SL);
     const int64_t n_items = g.n_chunks * ipc;
     const int64_t prio = sw.prio_items;
     const int64_t n_norm = n_items - prio;
     const int64_t n_short = min(g.n_short_chunks * ipc, n_norm);
     const int64_t n_sb = (n_short + BATCH - 1) / BATCH;
     const uint64_t n_tickets = (uint64_t)(prio + n_sb + (n_norm - n_short));
-    const int rounds = (sw.S + SL - 1) / SL;
-    const bool launch_first = sw.first == 0;
     while (true) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(g.ticket, 1ULL);
@@ -655,135 +861,56 @@ __device__ __forceinline__ void walk_diag(const WfDevGraph& g, const WfSweep& sw
                 first = n_short + (u - n_sb);
             }
         }
-        if (status_ld(status) & WF_DEV_SPIN_TIMEOUT) return;
-        if ((int)lane < count) {
-            const int64_t item = first + lane;
-            const int64_t chunk = item / ipc;
-            wb->base[lane] = g.chunk_base[chunk];
-            wb->chain0[lane] = g.chunk_chain0[chunk];
-            wb->L[lane] = g.chunk_len[chunk];
-            wb->Gc[lane] = g.chunk_g[chunk];
-            wb->p0[lane] = (int)(item % ipc) * J;
-        }
-        __syncwarp();
-        int npos = 0, work = 0;
-        for (int it = 0; it < count; ++it) {
-            const int p = wb->p0[it] + j;
-            const int gi = M <= 32 ? p / M : 0;
-            const bool ok = M <= 32 ? gi < wb->Gc[it] : p < M;
-            const int len = ok ? g.chain_len[wb->chain0[it] + gi] : 0;
-            wb->len[it][lane] = len;
-            work |= len;
-            npos += wb->L[it];
-        }
-        __syncwarp();
-        if (!__any_sync(0xffffffffu, work > 0)) continue;  // items past their chunks' pairs
-        auto gi_of = [&](int it) { return M <= 32 ? (wb->p0[it] + j) / M : 0; };
-        auto m_of = [&](int it) { return M <= 32 ? (wb->p0[it] + j) % M : wb->p0[it] + j; };
-        auto slot_of = [&](int it, int k) { return wb->base[it] + (int64_t)k * wb->Gc[it] + gi_of(it); };
-        auto valid = [&](int it, int k) { return it < count && k < wb->len[it][lane]; };
-        auto advance = [&](int& it, int& k) {
-            if (k + 1 < wb->L[it]) {
-                ++k;
-            } else {
-                ++it;
-                k = 0;
-            }
-        };
-        for (int r = 0; r < rounds; ++r) {
-            const int s = r * SL + sl;
-            const int s0 = r * SL;  // lane 0's sub-step
-            const bool last_lane = (s == sw.S - 1) || (sl == SL - 1);
-            // lane 0's pipeline over the sequence positions: cur (this time step), nxt, nn
-            In cur, nxt;
-            unsigned long long c0 = SENTINEL, c1 = SENTINEL, n0 = SENTINEL, n1 = SENTINEL;
-            int cit = 0, ck = 0;
-            if (sl == 0 && valid(cit, ck)) {
-                const int64_t sl0 = slot_of(cit, ck);
-                const int mm = m_of(cit);
-                phys.load(sl0, sl0 * M + mm, mm, cur);
-                load_words(g, mm, cur.up, s0, c0, c1);
-            }
-            int nit = cit, nk = ck;
-            advance(nit, nk);
-            if (DEPTH > 1 && sl == 0 && valid(nit, nk)) {
-                const int64_t sl1 = slot_of(nit, nk);
-                const int mm = m_of(nit);
-                phys.load(sl1, sl1 * M + mm, mm, nxt);
-            }
-            // what this lane works on at the current time step
-            In x;
-            St st;
-            unsigned long long w0 = SENTINEL, w1 = SENTINEL;
-            int pit = count, pk = 0;
-            unsigned long long hq = 0ull;
-            for (int tt = 0; tt < npos + SL - 1; ++tt) {
-                if (sl == 0) {
-                    x = cur;
-                    w0 = c0;
-                    w1 = c1;
-                    pit = cit;
-                    pk = ck;
-                    phys.start(x, st);
-                    // advance the pipeline: the words of nxt, the inputs of the position after it
-                    int nnit = nit, nnk = nk;
-                    if (nnit < count) advance(nnit, nnk);
-                    In nn;
-                    if (DEPTH > 1) {
-                        if (valid(nit, nk)) load_words(g, m_of(nit), nxt.up, s0, n0, n1);
-                        if (valid(nnit, nnk)) {
-                            const int64_t sl2 = slot_of(nnit, nnk);
-                            const int mm = m_of(nnit);
-                            phys.load(sl2, sl2 * M + mm, mm, nn);
-                        }
-                    } else if (valid(nit, nk)) {
-                        const int64_t sl1 = slot_of(nit, nk);
-                        const int mm = m_of(nit);
-                        phys.load(sl1, sl1 * M + mm, mm, nxt);
-                        load_words(g, mm, nxt.up, s0, n0, n1);
-                    }
-                    cur = nxt;
-                    c0 = n0;
-                    c1 = n1;
-                    n0 = n1 = SENTINEL;
-                    if (DEPTH > 1) nxt = nn;
-                    cit = nit;
-                    ck = nk;
-                    nit = nnit;
-                    nk = nnk;
-                }
-                bool ok = true;
-                unsigned long long v0 = SENTINEL, v1 = SENTINEL;  // words of sub-step s + 1 for the next lane
-                if (pit < count && pk < wb->len[pit][lane] && s < sw.S) {
-                    const int64_t slot = slot_of(pit, pk);
-                    const int mm = m_of(pit);
-                    const int64_t e = slot * M + mm;
-                    if (sl + 1 < SL && s + 1 < sw.S) load_words(g, mm, x.up, s + 1, v0, v1);
-                    unsigned long long out = 0ull;
-                    ok = phys.sub(x, st, w0, w1, slot, e, mm, s, wb->chain0[pit] + gi_of(pit),
-                                  pk == wb->len[pit][lane] - 1, pk > 0, hq, out);
-                    hq = out;
-                    if (ok && last_lane) phys.finish(st, e, r > 0 || !launch_first);
-                }
-                if (__any_sync(0xffffffffu, !ok)) return;
-                // hand the node to the next lane
-                shfl_up_pod(x, SL);
-                shfl_up_pod(st, SL);
-                const int pit_up = __shfl_up_sync(0xffffffffu, pit, 1, SL);
-                const int pk_up = __shfl_up_sync(0xffffffffu, pk, 1, SL);
-                const unsigned long long v0_up = __shfl_up_sync(0xffffffffu, v0, 1, SL);
-                const unsigned long long v1_up = __shfl_up_sync(0xffffffffu, v1, 1, SL);
-                if (sl > 0) {
-                    pit = pit_up;
-                    pk = pk_up;
-                    w0 = v0_up;
-                    w1 = v1_up;
-                }
-                __syncwarp();
-            }
-        }
-        __syncwarp();
+        if (!diag_ticket(g, sw, phys, status, first, count, wb)) return;
     }
+}
+
+// The overland sweep A (node-major) and the river sweep B in one launch, B's first-dispatched
+// chunks on the diagonal schedule (their long chains are the critical path; sw.SL lanes per
+// chain-member pair) and its other chunks node-major. Tickets: A's, then B's p_chunks last chunks
+// as diagonal items (longest first), then B's remaining chunks node-major (pb.sw.prio_items of
+// them dispatched first). Each warp has a node-major batch descriptor after the hand-off rows
+// and a diagonal one after those.
+template <class PhysA, class PhysB>
+__device__ __forceinline__ void walk_pair_diag(PhysA& pa, PhysB& pb, int S_alloc, int64_t p_chunks, int SL,
+                                               int32_t* status) {
+    extern __shared__ unsigned long long wave_smem[];
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long* qh = wave_smem + threadIdx.x;
+    const int warps = blockDim.x >> 5;
+    WarpBatch* wbn = reinterpret_cast<WarpBatch*>(wave_smem + (size_t)blockDim.x * S_alloc) + (threadIdx.x >> 5);
+    DiagBatch* wbd = reinterpret_cast<DiagBatch*>(reinterpret_cast<WarpBatch*>(wave_smem + (size_t)blockDim.x * S_alloc) +
+                                                  warps) + (threadIdx.x >> 5);
+    WfSweep swd = pb.sw;
+    swd.SL = SL;
+    WfDevGraph gn = pb.g;  // the node-major part: every chunk but the last p_chunks
+    gn.n_chunks = pb.g.n_chunks - p_chunks;
+    const int64_t ipc = wf_items_per_chunk(pb.g.G, pb.g.M, SL);
+    const uint64_t na = walk_tickets(pa.g, pa.sw);
+    const uint64_t nd = (uint64_t)(p_chunks * ipc);
+    const uint64_t nn = walk_tickets(gn, pb.sw);
+    const int64_t n_items_d = pb.g.n_chunks * ipc;
+    while (true) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(pa.g.ticket, 1ULL);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        bool ok;
+        if (t < na) {
+            ok = walk_ticket(pa.g, pa.sw, pa, status, t, wbn, qh);
+        } else if (t < na + nd) {
+            swd.SL = SL;
+            ok = diag_ticket(pb.g, swd, pb, status, n_items_d - 1 - (int64_t)(t - na), 1, wbd);
+        } else if (t < na + nd + nn) {
+            ok = walk_ticket(gn, pb.sw, pb, status, t - na - nd, wbn, qh);
+        } else {
+            return;
+        }
+        if (!ok) return;
+    }
+}
+
+__host__ __device__ constexpr size_t pair_diag_smem(int threads, int substeps) {
+    return walk_smem(threads, substeps) + (size_t)(threads / 32) * sizeof(DiagBatch);
 }
 
 }  // namespace wfv

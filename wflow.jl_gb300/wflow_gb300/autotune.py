@@ -5,8 +5,9 @@ share an SM's FP64 pipe while the short chains drain, so the best number of resi
 depends on the graph (chain-length distribution) and the form; a sweep of several sub-steps also
 depends on how many lanes share a chain-member pair on the diagonal schedule (more lanes: a
 shorter critical path, fewer pairs per warp), and each node-major sweep on whether its inputs are
-staged in shared memory or held in registers; the per-cell kernel depends on its block size and
-on its grid, which sets how many elements each thread walks. The
+staged in shared memory or held in registers; the overland and river sweeps may share one launch
+(the river walking behind the overland front) or run one after the other; the per-cell kernel
+depends on its block size and on its grid, which sets how many elements each thread walks. The
 tuner times a few steps of each candidate with per-kernel CUDA events and keeps the fastest for
 each kernel family. Candidates only change the schedule, never the result: the wavefront
 produces the same values for any dispatch order and any lane count.
@@ -31,12 +32,16 @@ def _time_steps(model: Model, forcing, steps):
 def tune(model: Model, forcing, steps=1, verbose=False):
     """Pick routing warps/blocks per SM and the per-cell block size; returns the choice and the
     measured milliseconds per step of each candidate."""
-    model._tune_state = dict(vertical_block=0, routing_warps=0, routing_blocks_per_sm=0, substep_lanes=0)
+    # the launch shapes of the separate sweeps first; whether the overland and river sweeps share a
+    # launch is decided last
+    model._tune_state = dict(vertical_block=0, routing_warps=0, routing_blocks_per_sm=0, substep_lanes=0,
+                             separate_overland_river=1)
     _time_steps(model, forcing, 1)  # warm-up
     results = []
     best_route, best_route_t = None, float("inf")
     for warps, bps in itertools.product([2, 4], [1, 2, 4, 0]):
-        model._tune_state = dict(vertical_block=0, routing_warps=warps, routing_blocks_per_sm=bps, substep_lanes=0)
+        model._tune_state = dict(vertical_block=0, routing_warps=warps, routing_blocks_per_sm=bps, substep_lanes=0,
+                                 separate_overland_river=1)
         t = _time_steps(model, forcing, steps)
         route = t["subsurface"] + t["overland"] + t["river"]
         results.append(("routing", warps, bps, route))
@@ -52,7 +57,8 @@ def tune(model: Model, forcing, steps=1, verbose=False):
         best_lanes_t = best_route_t
         for lanes in [1, 2, 4, 16]:  # 0 (the default, 8) was measured above
             model._tune_state = dict(vertical_block=0, routing_warps=best_route[0],
-                                     routing_blocks_per_sm=best_route[1], substep_lanes=lanes)
+                                     routing_blocks_per_sm=best_route[1], substep_lanes=lanes,
+                                     separate_overland_river=1)
             t = _time_steps(model, forcing, steps)
             route = t["subsurface"] + t["overland"] + t["river"]
             results.append(("lanes", lanes, 0, route))
@@ -63,7 +69,7 @@ def tune(model: Model, forcing, steps=1, verbose=False):
     # inputs of the node-major sweeps: staged in shared memory or held in registers, per sweep
     # (both runs time every sweep; each keeps its faster mode)
     base = dict(vertical_block=0, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1],
-                substep_lanes=best_lanes)
+                substep_lanes=best_lanes, separate_overland_river=1)
     model._tune_state = dict(base, sweep_inputs=0)
     staged = _time_steps(model, forcing, steps)
     model._tune_state = dict(base, sweep_inputs=7)
@@ -73,13 +79,32 @@ def tune(model: Model, forcing, steps=1, verbose=False):
     results.append(("inputs", best_inputs, 0, 0.0))
     if verbose:
         print(f"sweep inputs held in registers (bit mask): {best_inputs}")
+    # the overland sweep and the river's first sub-steps in one launch (the river walks behind
+    # the overland front), against separate launches; both phases together, since the shared
+    # launch is timed as the overland phase
+    # (the shared launch runs the river's first-dispatched chains on the diagonal schedule when
+    # the sub-step lanes allow it, so it is tried with the lanes chosen above and with none)
+    best_sep = 1
+    model._tune_state = dict(base, sweep_inputs=best_inputs)
+    t = _time_steps(model, forcing, steps + 1)
+    best_pair_t = t["overland"] + t["river"]
+    for lanes in dict.fromkeys([best_lanes, 1]):
+        model._tune_state = dict(base, sweep_inputs=best_inputs, substep_lanes=lanes, separate_overland_river=0)
+        t = _time_steps(model, forcing, steps + 1)
+        results.append(("overland_river_shared_launch", lanes, 0, t["overland"] + t["river"]))
+        if verbose:
+            print(f"overland and river in one launch (lanes={lanes}): {t['overland'] + t['river']:.3f} ms, "
+                  f"separate {best_pair_t:.3f} ms")
+        if t["overland"] + t["river"] < best_pair_t:
+            best_sep, best_lanes, best_pair_t = 0, lanes, t["overland"] + t["river"]
     # the per-cell kernel: block size and grid (the elements each thread walks in its grid-stride
     # loop: one wave of resident blocks, a few waves, or the default 16 blocks per SM)
     best_block, best_bps, best_block_t = 0, 0, float("inf")
     for block, vbps in itertools.product([128, 256], [0, 4, 8]):
         model._tune_state = dict(vertical_block=block, routing_warps=best_route[0],
                                  routing_blocks_per_sm=best_route[1], substep_lanes=best_lanes,
-                                 sweep_inputs=best_inputs, vertical_blocks_per_sm=vbps)
+                                 sweep_inputs=best_inputs, vertical_blocks_per_sm=vbps,
+                                 separate_overland_river=best_sep)
         t = _time_steps(model, forcing, steps)
         results.append(("vertical", block, vbps, t["vertical"]))
         if verbose:
@@ -87,7 +112,8 @@ def tune(model: Model, forcing, steps=1, verbose=False):
         if t["vertical"] < best_block_t:
             best_block, best_bps, best_block_t = block, vbps, t["vertical"]
     choice = dict(vertical_block=best_block, routing_warps=best_route[0], routing_blocks_per_sm=best_route[1],
-                  substep_lanes=best_lanes, sweep_inputs=best_inputs, vertical_blocks_per_sm=best_bps)
+                  substep_lanes=best_lanes, sweep_inputs=best_inputs, vertical_blocks_per_sm=best_bps,
+                  separate_overland_river=best_sep)
     model._tune_state = choice
     model.set_tuning(**choice, use_graph=1)
     return choice, results

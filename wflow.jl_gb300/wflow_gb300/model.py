@@ -172,7 +172,7 @@ class Model:
 
     def set_tuning(self, vertical_block=0, routing_warps=0, routing_blocks_per_sm=0, use_graph=1,
                    wait_budget_us=0, wait_offset=0, kernel_timing=0, substep_lanes=0, sweep_inputs=0,
-                   vertical_blocks_per_sm=0):
+                   vertical_blocks_per_sm=0, separate_overland_river=0):
         """Launch shape of the step's kernels (results do not depend on it): threads per block of
         the per-cell kernels, warps per block and blocks per SM of the routing sweeps, the cap of
         the sub-step lanes of their diagonal schedule (0: default), the CUDA graph, and test hooks."""
@@ -185,6 +185,7 @@ class Model:
         t.reserved[3] = substep_lanes
         t.reserved[4] = sweep_inputs  # bit k: sweep k (subsurface, overland, river) keeps its inputs in registers
         t.reserved[5] = vertical_blocks_per_sm  # grid of the split vertical kernel (elements per thread)
+        t.reserved[6] = separate_overland_river  # 1: split overland and river sweeps in separate launches
         self._check(self.lib.wf_set_tuning(self.h, C.byref(t)), "wf_set_tuning")
 
     def stream(self):
