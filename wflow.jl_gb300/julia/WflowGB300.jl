@@ -16,7 +16,9 @@ seam, `Wflow.run_timestep!(model; update_func = ...)` (Wflow/src/Wflow.jl:311-32
 `gpu_update_model!` replaces `update_model!` (Wflow/src/sbm_model.jl:60-92) and
 `compute_mass_balance!` (Wflow/src/mass_balance.jl:541-545): it uploads the step's
 `AtmosphericForcing`, runs one step on the GPU and refreshes the host mirrors that BMI
-`get_value_ptr` hands out (Wflow/src/bmi.jl:208-228). Errors come back as a negative status
+`get_value_ptr` hands out (Wflow/src/bmi.jl:208-228): after every step (`mirrors = :eager`, the
+default, for Wflow's output writers), or on demand (`GpuStep(model; mirrors = :lazy)`, then
+`refresh_mirrors!` before reading and `set_value!` to write through). Errors come back as a negative status
 and are rethrown as Julia exceptions with the library's message, like Wflow's own
 throw-and-log path (Wflow/src/Wflow.jl:285-299).
 """
@@ -144,6 +146,8 @@ mutable struct GpuStep
     forcing::NTuple{3, Vector{Float64}}
     n_reservoirs::Int
     li::Any                        # GpuLocalInertial routing the land and river in the step, or nothing
+    mirrors::Symbol                # :eager (refresh the host mirrors after every step) or :lazy
+    stale::Bool                    # :lazy: the host mirrors predate the last GPU step
 end
 
 check(st, h, what) = st == 0 || error("$what failed ($st): " *
@@ -199,12 +203,14 @@ function check_supported(config)
 end
 
 """
-    GpuStep(model::Wflow.Model)
+    GpuStep(model::Wflow.Model; mirrors = :eager)
 
 Copy the model's domain, parameters (as read from the static maps, in SI) and current state
-to a new library handle (`wf_create`, then `wf_set_field` for a warm state).
+to a new library handle (`wf_create`, then `wf_set_field` for a warm state). `mirrors`: when
+the host copies of the GPU state are refreshed (`gpu_update_model!`, `refresh_mirrors!`).
 """
-function GpuStep(model)
+function GpuStep(model; mirrors::Symbol = :eager)
+    mirrors in (:eager, :lazy) || error("mirrors must be :eager or :lazy")
     (; domain, land, routing, config) = model
     check_supported(config)
     lp = domain.land.parameters
@@ -291,7 +297,7 @@ function GpuStep(model)
          Ref{Ptr{Cvoid}}), cfg, dom, params, res, tables, Int32(0), h)
     check(st, C_NULL, "wf_create_with_reservoir_tables")
     n = length(ds_land)
-    gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)), nres, nothing)
+    gpu = GpuStep(h[], keep, n, length(ds_river), (zeros(n), zeros(n), zeros(n)), nres, nothing, mirrors, false)
     finalizer(g -> ccall((:wf_destroy, LIB), Cvoid, (Ptr{Cvoid},), g.handle), gpu)
     if local_inertial_both(config)
         # the land grid with its river routes inside wf_step (wf_attach_local_inertial); the
@@ -361,7 +367,11 @@ function gpu_update_model!(gpu::GpuStep, model)
         end
     end
     check(ccall((:wf_step, LIB), Int32, (Ptr{Cvoid},), gpu.handle), gpu.handle, "wf_step")
-    sync_mirrors!(gpu, model)
+    if gpu.mirrors === :eager
+        sync_mirrors!(gpu, model)
+    else
+        gpu.stale = true
+    end
     gpu.li === nothing || li_copy_back!(gpu.li, model, tosecond(model.clock.dt))
     return nothing
 end
@@ -379,6 +389,35 @@ function set_field!(gpu::GpuStep, field::Integer, src::Vector{Float64}; layer::I
     st = ccall((:wf_set_field, LIB), Int32, (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}, Int64, Int64),
         gpu.handle, Int32(field), Int32(layer), src, 0, length(src))
     check(st, gpu.handle, "wf_set_field")
+end
+
+"""
+    refresh_mirrors!(gpu::GpuStep, model)
+
+With `mirrors = :lazy`, copy the GPU state into the host vectors if a step ran since the last
+refresh (a dirty flag); call it before BMI `get_value` / `get_value_ptr` (Wflow/src/bmi.jl:208-228)
+or before writing output. With `:eager` the mirrors are always current.
+"""
+function refresh_mirrors!(gpu::GpuStep, model)
+    if gpu.stale
+        sync_mirrors!(gpu, model)
+        gpu.stale = false
+    end
+    return nothing
+end
+
+"""
+    set_value!(gpu::GpuStep, model, host::Vector{Float64}, field::Integer, values)
+
+BMI `set_value` for a field the GPU step owns (Wflow/src/bmi.jl:241-262): the host vector is
+brought up to date first (a lazy mirror), then `values` is written through to both the host
+vector and the GPU field `field` (a WfField id), so the next step and the next read see it.
+"""
+function set_value!(gpu::GpuStep, model, host::Vector{Float64}, field::Integer, values)
+    refresh_mirrors!(gpu, model)
+    copyto!(host, values)
+    set_field!(gpu, field, host)
+    return nothing
 end
 
 "Refresh the host vectors Wflow's BMI and writers read after a GPU step."
