@@ -335,14 +335,16 @@ def run_gpu(args):
             raise RuntimeError(f"wf_get_outlets failed {st}")
     model.synchronize()
     loop_resident_ms = (time.perf_counter() - t1) / K * 1e3
-    # ---- per-kernel times (eager launches with events between kernels) for the roofline
+    # ---- per-kernel times (eager launches with events between kernels) for the roofline; the
+    # handle's counters also hold the autotuner's timed steps, so only this pass's share counts
     model.set_tuning(**(tuning or {}), use_graph=0, kernel_timing=1)
+    kt0, calls0 = model.kernel_times()
     for s in range(min(K, 5)):
         b = resident[W + s]
         model.set_forcing_device_slots(b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr())
         model.update_model()
     kt, calls = model.kernel_times()
-    kt = {k: v / max(calls, 1) for k, v in kt.items()}
+    kt = {k: (v - kt0[k]) / max(calls - calls0, 1) for k, v in kt.items()}
     mt = model.metrics()
     result = {
         "metric": "cell-timesteps/s",
@@ -685,8 +687,8 @@ def run_profile(args):
     dom, params, cfg, pfac = build_workload(args.workload, form, seed=args.seed)
     side, cell, dt, members, _ = WORKLOADS[args.workload]
     model = Model(cfg, dom, params=params)
-    model.set_tuning(vertical_block=128, routing_warps=2, routing_blocks_per_sm=0, use_graph=0, kernel_timing=1,
-                     substep_lanes=args.sub_lanes, sweep_inputs=args.sweep_inputs,
+    model.set_tuning(vertical_block=128, routing_warps=args.routing_warps, routing_blocks_per_sm=args.routing_bps,
+                     use_graph=0, kernel_timing=1, substep_lanes=args.sub_lanes, sweep_inputs=args.sweep_inputs,
                      separate_overland_river=args.separate_overland_river)
     for s in range(args.steps):
         P, PET, T = member_forcing(s, dt, dom.n_land, members, pfac, seed=args.seed)
@@ -770,6 +772,8 @@ def main():
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64 plain comparison leg")
     ap.add_argument("--sub-lanes", type=int, default=0,
                     help="profiler driver: cap of the routing sweeps' sub-step lanes (0: the library default)")
+    ap.add_argument("--routing-warps", type=int, default=2, help="--profile: warps per block of the sweeps")
+    ap.add_argument("--routing-bps", type=int, default=0, help="--profile: sweep blocks per SM (0: all resident)")
     ap.add_argument("--separate-overland-river", type=int, default=0, choices=[0, 1],
                     help="--profile: 1 runs the split form's overland and river sweeps in separate launches")
     ap.add_argument("--sweep-inputs", type=int, default=0,

@@ -2499,12 +2499,20 @@ cudaError_t wf_split_overland_river_wave(const WfDevFields& F, const WfDevGraph&
     const int S_alloc = swl.S > swr.S ? swl.S : swr.S;
     const int SL = wave_sub_lanes(swr.S, c);
     int blocks_l, blocks_r;
+    // a persistent launch gains nothing from blocks beyond those resident at once (the shared
+    // launch holds more registers per thread than the separate sweeps the tuning was made for)
+    WfLaunchCfg cp = c;
+    cp.walk_blocks = 0;
     if (SL <= 1) {
         const size_t smem = wfv::walk_smem(threads, S_alloc);
         auto kernel = wave_pair_kernel<PA, PB>;
-        cudaError_t err = wave_grid(kernel, threads, smem, c, gl, blocks_l, pa.sw.prio_items);
+        int per_sm = 0;
+        cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
         if (err != cudaSuccess) return err;
-        err = wave_grid(kernel, threads, smem, c, gr, blocks_r, pb.sw.prio_items);
+        if (c.walk_blocks > 0) cp.walk_blocks = std::min(c.walk_blocks, c.num_sms * std::max(per_sm, 1));
+        err = wave_grid(kernel, threads, smem, cp, gl, blocks_l, pa.sw.prio_items);
+        if (err != cudaSuccess) return err;
+        err = wave_grid(kernel, threads, smem, cp, gr, blocks_r, pb.sw.prio_items);
         if (err != cudaSuccess) return err;
         kernel<<<blocks_l > blocks_r ? blocks_l : blocks_r, threads, smem, c.stream>>>(pa, pb, S_alloc);
         return cudaGetLastError();
@@ -2514,16 +2522,17 @@ cudaError_t wf_split_overland_river_wave(const WfDevFields& F, const WfDevGraph&
     int64_t prio_r;
     cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    err = wave_grid(kernel, threads, smem, c, gl, blocks_l, pa.sw.prio_items);
+    int per_sm = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     if (err != cudaSuccess) return err;
-    err = wave_grid(kernel, threads, smem, c, gr, blocks_r, prio_r);
+    if (c.walk_blocks > 0) cp.walk_blocks = std::min(c.walk_blocks, c.num_sms * std::max(per_sm, 1));
+    err = wave_grid(kernel, threads, smem, cp, gl, blocks_l, pa.sw.prio_items);
+    if (err != cudaSuccess) return err;
+    err = wave_grid(kernel, threads, smem, cp, gr, blocks_r, prio_r);
     if (err != cudaSuccess) return err;
     const int blocks = blocks_l > blocks_r ? blocks_l : blocks_r;
     // at most half of the resident warps hold first-dispatched river tickets (diagonal items and
     // node-major long chunks together), as in wave_grid
-    int per_sm = 0;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-    if (err != cudaSuccess) return err;
     const int64_t resident = (int64_t)std::min(blocks, c.num_sms * std::max(per_sm, 1)) * (threads / 32);
     const int64_t ipc_d = wf_items_per_chunk(gr.G, gr.M, SL);
     const int64_t gpc = gr.M > 32 ? gr.M / 32 : 1;
