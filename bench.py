@@ -409,9 +409,9 @@ def run_gpu(args):
                   "algorithmic_bytes": phase_bytes(k)} for k in kt}
     # the split form's overland sweep and the river's first sub-steps share one launch (timed as
     # the overland phase; the river phase is then its completion kernel alone): one phase for both
-    shared = (form == abi.WF_FORM_SPLIT and not cfg.adaptive_timestep and dom.n_river > 0
-              and (tuning or {}).get("separate_overland_river", 0) == 0 and substeps["land"] <= 16)
-    if shared:
+    shared_launch = (form == abi.WF_FORM_SPLIT and not cfg.adaptive_timestep and dom.n_river > 0
+                     and (tuning or {}).get("separate_overland_river", 0) == 0 and substeps["land"] <= 16)
+    if shared_launch:
         b = phase_bytes("overland") + phase_bytes("river")
         ms = kt["overland"] + kt["river"]
         a = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
