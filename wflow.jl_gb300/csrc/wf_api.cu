@@ -791,6 +791,7 @@ int res_tables(const WfReservoirs* rs, const WfReservoirTables* tb, int64_t nr, 
             const int64_t target = rs->river_index[rt.lower[k]];
             int64_t prev = rs->river_index[k], x = rds[prev], steps = 0;
             while (x >= 0 && steps++ <= nr) {
+                if (x >= nr) return bad(WF_ERR_INVALID, "river_downstream out of range");
                 if (rt.heavy_hint[x] >= 0 && rt.heavy_hint[x] != prev)
                     return bad(WF_ERR_UNSUPPORTED, "the river paths of two linked reservoir pairs join");
                 rt.heavy_hint[x] = prev;
