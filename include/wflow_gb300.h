@@ -485,6 +485,11 @@ int32_t wf_struct_size(int32_t which);
  * ok = 1 when the schedule invariants hold; g_out = chains per chunk. */
 int32_t wf_plan_routing(int64_t n, const int32_t* downstream, int32_t members, int64_t* out_counts,
                         int64_t* slot_of_node, int32_t* ok, int32_t* g_out);
+/* The same with heavy-child hints (heavy_hint[v]: a child of v that must continue v's chain, -1
+ * none; the hints wf_create_with_reservoir_tables gives for linked reservoirs); chain_of_node
+ * optional [n]. */
+int32_t wf_plan_routing_hinted(int64_t n, const int32_t* downstream, int32_t members, const int64_t* heavy_hint,
+                               int64_t* out_counts, int64_t* chain_of_node, int32_t* ok, int32_t* g_out);
 
 #ifdef __cplusplus
 }

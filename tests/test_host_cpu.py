@@ -36,7 +36,7 @@ def test_synth_header_symbols_exported():
 
 def test_struct_sizes_match(lib):
     for i, cls in enumerate([abi.WfConfig, abi.WfDomain, abi.WfParams, abi.WfMetrics, abi.WfTuning,
-                             abi.WfReservoirs]):
+                             abi.WfReservoirs, abi.WfReservoirTables]):
         assert lib.wf_struct_size(i) == C.sizeof(cls), cls.__name__
 
 
@@ -140,3 +140,39 @@ def test_forcing_distribution():
     mm_day = P * 86400.0 * 1000.0
     assert abs(mm_day[mm_day > 0].mean() - 4.0) < 0.3   # gamma(0.4, 10) mean
     assert np.all(T > 250) and np.all(PET >= 0)
+
+
+@pytest.mark.parametrize("members", [1, 64])
+def test_heavy_hints_keep_a_path_on_one_chain(lib, members):
+    # the planner's hints for linked reservoirs: the river path from an upper node to a lower one
+    # lies on one chain (one lane walks both in order), and the plan's invariants still hold
+    rng = np.random.default_rng(7)
+    for trial in range(20):
+        n = int(rng.integers(20, 400))
+        ds = _random_forest(n, rng, n_roots=int(rng.integers(1, 4)))
+        # a path: start at a leaf-ish node, go down a few links
+        u = int(rng.integers(0, n))
+        path = [u]
+        while ds[path[-1]] >= 0 and len(path) < 12:
+            path.append(int(ds[path[-1]]))
+        hint = np.full(n, -1, np.int64)
+        for a, b in zip(path[:-1], path[1:]):
+            hint[b] = a
+        counts = np.zeros(4, np.int64)
+        chain = np.zeros(n, np.int64)
+        ok, g = C.c_int32(), C.c_int32()
+        st = lib.wf_plan_routing_hinted(n, ds.ctypes.data_as(C.POINTER(C.c_int32)), members,
+                                        hint.ctypes.data_as(C.POINTER(C.c_int64)),
+                                        counts.ctypes.data_as(C.POINTER(C.c_int64)),
+                                        chain.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(ok), C.byref(g))
+        assert st == 0 and ok.value == 1, (trial, st, ok.value)
+        assert len(set(chain[path].tolist())) == 1, (trial, path, chain[path])
+    # a hint that is not a child of its node is refused
+    ds = np.array([1, 2, -1, 2], np.int32)
+    bad = np.array([-1, -1, 0, -1], np.int64)  # node 0 drains into 1, not into 2
+    counts = np.zeros(4, np.int64)
+    ok, g = C.c_int32(), C.c_int32()
+    st = lib.wf_plan_routing_hinted(4, ds.ctypes.data_as(C.POINTER(C.c_int32)), members,
+                                    bad.ctypes.data_as(C.POINTER(C.c_int64)),
+                                    counts.ctypes.data_as(C.POINTER(C.c_int64)), None, C.byref(ok), C.byref(g))
+    assert st != 0

@@ -83,11 +83,15 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
         }
         heavy[v] = best;
     }
-    // chains from every leaf
+    // chains from every leaf; key = height of the chain's end + 1, which equals the length when
+    // every heavy child is the highest one, and which grows strictly from a chain to the chain
+    // it flows into whatever the heavy children are (heights grow strictly downstream), so that
+    // ordering by key is a dependency order with heavy-child hints too
     struct Chain {
         int64_t start;
         int32_t len;
         int64_t end;
+        int32_t key;
     };
     std::vector<Chain> chains;
     for (int64_t v = 0; v < n; ++v) {
@@ -98,17 +102,19 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
             u = ds[u];
             ++len;
         }
-        chains.push_back({v, len, u});
+        chains.push_back({v, len, u, height[u] + 1});
     }
     std::stable_sort(chains.begin(), chains.end(), [](const Chain& a, const Chain& b) {
-        return a.len != b.len ? a.len < b.len : a.end < b.end;
+        return a.key != b.key ? a.key < b.key : a.end < b.end;
     });
+    P.hinted = heavy_hint != nullptr;
     const int G = P.G;
     const int64_t nc_real = (int64_t)chains.size();
     // Dispatch order. The sweeps first dispatch, all at once, the chains at the end of the order
     // (one chain per chunk; wave_grid caps them at half the resident warps), then the others in
-    // length order, which is a dependency order (a light child is strictly shorter than its
-    // consumer), short chains batched. The first group holds up to kFirst chains: the longest
+    // key order (the length, without heavy-child hints), which is a dependency order (a light
+    // child is strictly shorter than its consumer, and its end strictly lower), short chains
+    // batched. The first group holds up to kFirst chains: the longest
     // ones (at least max(64, longest / 8) nodes), which carry the critical path, and then the
     // most urgent of the rest: with one time unit per position, a chain ending at position k of
     // its consumer must start by LS(c) = LS(consumer) + k - len(c) (a chain ending at a pit by
@@ -121,7 +127,8 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
     constexpr int64_t kFirst = 256;
     int64_t n_solo = 0;
     if (nc_real > 0) {
-        const int32_t longest = chains.back().len;
+        int32_t longest = 0;
+        for (const Chain& c : chains) longest = std::max(longest, c.len);
         std::vector<int64_t> chain_of(n, -1), pos_of(n, -1);
         for (int64_t c = 0; c < nc_real; ++c) {
             int64_t u = chains[c].start;
@@ -138,7 +145,7 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
         }
         std::vector<char> first(nc_real, 0);
         const int32_t thr = std::max<int32_t>(64, longest / 8);
-        for (int64_t c = nc_real - 1; c >= 0 && n_solo < kFirst && chains[c].len >= thr; --c) {
+        for (int64_t c = nc_real - 1; c >= 0 && n_solo < kFirst && chains[c].key >= thr; --c) {
             first[c] = 1;
             ++n_solo;
         }
@@ -249,10 +256,11 @@ int wf_build_plan(int64_t n, const int32_t* ds, int32_t members, WfRoutingPlan& 
 }
 
 bool wf_check_plan(const WfRoutingPlan& P, const int32_t* ds, std::string& err) {
-    // chain lengths sorted before the first-dispatched group (padding chains have length 0);
-    // every chain waits only for chains of smaller index (checked per node below)
+    // chain lengths sorted before the first-dispatched group (padding chains have length 0;
+    // with heavy-child hints the order is by end height, checked through the per-node condition
+    // below); every chain waits only for chains of smaller index (checked per node below)
     int32_t prev = 0;
-    for (int64_t c = 0; c < P.n_chains - P.n_long_chunks; ++c) {
+    for (int64_t c = 0; c < P.n_chains - P.n_long_chunks && !P.hinted; ++c) {
         if (P.chain_len[c] == 0) continue;
         if (P.chain_len[c] < prev) {
             err = "chains not sorted by length";
@@ -282,7 +290,7 @@ bool wf_check_plan(const WfRoutingPlan& P, const int32_t* ds, std::string& err) 
                 }
             } else {
                 int64_t uc = P.up_chain[o];
-                if (!P.is_chain_end[us] || uc >= my_chain || P.chain_len[uc] > k) {
+                if (!P.is_chain_end[us] || uc >= my_chain || (!P.hinted && P.chain_len[uc] > k)) {
                     err = "light child chain does not precede its consumer";
                     return false;
                 }
@@ -309,6 +317,25 @@ int32_t wf_plan_routing(int64_t n, const int32_t* downstream, int32_t members, i
     out_counts[3] = P.max_len;
     if (slot_of_node)
         for (int64_t i = 0; i < n; ++i) slot_of_node[i] = P.slot_of_node[i];
+    *ok = wf_check_plan(P, downstream, err) ? 1 : 0;
+    *g_out = P.G;
+    return 0;
+}
+
+// The same with heavy-child hints (heavy_hint [n], -1: none): chain_of_node [n] (optional)
+// receives each node's chain.
+int32_t wf_plan_routing_hinted(int64_t n, const int32_t* downstream, int32_t members, const int64_t* heavy_hint,
+                               int64_t* out_counts, int64_t* chain_of_node, int32_t* ok, int32_t* g_out) {
+    WfRoutingPlan P;
+    std::string err;
+    int rc = wf_build_plan(n, downstream, members, P, err, heavy_hint);
+    if (rc != 0) return rc;
+    out_counts[0] = P.n_chains;
+    out_counts[1] = P.n_chunks;
+    out_counts[2] = P.n_slots;
+    out_counts[3] = P.max_len;
+    if (chain_of_node)
+        for (int64_t i = 0; i < n; ++i) chain_of_node[i] = P.chain_of_node[i];
     *ok = wf_check_plan(P, downstream, err) ? 1 : 0;
     *g_out = P.G;
     return 0;

@@ -33,6 +33,7 @@ struct WfRoutingPlan {
     int64_t n_slots = 0;    // node slots including padding
     int32_t max_len = 0;    // longest chain = graph height + 1
     int64_t n_long_chunks = 0;  // trailing chunks of the first-dispatched group (one chain each)
+    bool hinted = false;        // built with heavy-child hints (chains ordered by end height, not length)
     std::vector<int64_t> chunk_base;    // [n_chunks + 1]
     std::vector<int32_t> chunk_len;     // [n_chunks]
     std::vector<int32_t> chunk_g;       // [n_chunks] chains in the chunk (G, or 1 for a long chain)

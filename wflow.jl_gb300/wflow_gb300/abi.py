@@ -252,6 +252,8 @@ def _declare(lib):
         "wf_get_kernel_times": (_i32, [H, _pd, C.POINTER(_i64)]),
         "wf_struct_size": (_i32, [_i32]),
         "wf_plan_routing": (_i32, [_i64, _pi32, _i32, C.POINTER(_i64), C.POINTER(_i64), _pi32, _pi32]),
+        "wf_plan_routing_hinted": (_i32, [_i64, _pi32, _i32, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64),
+                                          _pi32, _pi32]),
         "wf_create_with_reservoirs": (_i32, [C.POINTER(WfConfig), C.POINTER(WfDomain), C.POINTER(WfParams),
                                              C.POINTER(WfReservoirs), _i32, C.POINTER(H)]),
         "wf_create_with_reservoir_tables": (_i32, [C.POINTER(WfConfig), C.POINTER(WfDomain), C.POINTER(WfParams),
