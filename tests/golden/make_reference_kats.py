@@ -425,6 +425,11 @@ def build():
     K.append(case("affine_scale_offset", "affine", f"{U}:291-305", dict(v=v, scale=[6.0], offset=[7.0] * 3),
                   dict(out=[6.0 * x + 7.0 for x in v]), cmp="exact",
                   note="scale = [6.0], offset = fill(7.0, 3) (utils.jl:301-304)"))
+    # julian_day (leap days not counted): the standard-calendar cases
+    for ln in range(19, 28):
+        y, mo, d, day = nums(U, ln)[:4]
+        K.append(case(f"julian_day_{int(y)}_{int(mo):02d}_{int(d):02d}", "julian_day", f"{U}:{ln}",
+                      dict(year=int(y), month=int(mo), day=int(d)), dict(julian_day=int(day)), cmp="exact"))
     K.append(case("scurve", "scurve", f"{U}:66-77",
                   dict(x=num(U, 71), a=num(U, 67), b=num(U, 68), c=num(U, 69)), dict(s=num(U, 73))))
     K.append(case("mass_balance_zero", "compute_mass_balance_error", f"{U}:105-112",

@@ -240,6 +240,11 @@ def run_case(c, prev):
         from wflow_gb300 import staticmaps
         return dict(out=list(staticmaps.apply_affine_transform(np.asarray(a["v"]), a.get("scale", [1.0]),
                                                                a.get("offset", [0.0]))))
+    if fn == "julian_day":
+        # host logic of the rating-curve day (the file-driven run computes it, as Wflow's clock does)
+        import datetime
+        from wflow_gb300.config import julian_day
+        return dict(julian_day=julian_day(datetime.datetime(a["year"], a["month"], a["day"])))
     if fn == "update_reservoir_model":
         # set_reservoir_vars! (the cumulatives start at zero), then update_reservoir_model!
         res = (O.Reservoir * 1)(O.Reservoir(**a["reservoir"]))

@@ -157,6 +157,20 @@ class WflowConfig:
         return out
 
 
+def julian_day(t):
+    """Day of the year with leap days not counted (Wflow's julian_day, utils.jl:674-678):
+    February 28 is day 59 and March 1 day 60 in every year."""
+    doy = t.timetuple().tm_yday
+    leap = t.year % 4 == 0 and (t.year % 100 != 0 or t.year % 400 == 0)
+    return doy - (1 if leap and doy > 60 else 0)
+
+
+def rating_curve_day(time, dt):
+    """The H-Q tables' column of the step that ends at `time` (update_index_hq!,
+    routing/surface/reservoir.jl:379-385: julian_day(clock.time - clock.dt))."""
+    return julian_day(time - _dt.timedelta(seconds=float(dt)))
+
+
 def _as_datetime(v):
     if v is None:
         return None
