@@ -35,10 +35,17 @@ FIELDS = ["RIVER_Q", "RIVER_Q_AVERAGE", "LAND_Q", "SSF_Q", "SATURATED_WATER_DEPT
           "SNOW_STORAGE", "TOTAL_STORAGE", "BALANCE_LAND_ERROR", "BALANCE_RIVER_ERROR"]
 
 
-@pytest.mark.parametrize("with_reservoirs", [False, True])
+@pytest.mark.parametrize("with_reservoirs", [False, True, "tables"])
 def test_warm_start_continues_the_run(tmp_path, with_reservoirs):
+    # "tables": interpolated S-H profiles, a rating curve and a linked pair; the storage read
+    # back is the S-H table at the stored level (initialize_storage), which inverts the level the
+    # run reached from its storage to within rounding
     dom = synthetic.make_domain(24, 1000.0, seed=5)
-    res = synthetic.make_reservoirs(dom, 2, seed=2) if with_reservoirs else None
+    if with_reservoirs == "tables":
+        dom = synthetic.make_domain(48, 1000.0, seed=3)
+        res = synthetic.make_linked_reservoirs(dom, seed=3)
+    else:
+        res = synthetic.make_reservoirs(dom, 2, seed=2) if with_reservoirs else None
     cfg = synthetic.make_config(86400.0)
     a = O.OracleModel(cfg, dom, reservoirs=res)
     for s in range(6):

@@ -155,6 +155,34 @@ def write_states(model, dom, path, grid=None, names=None, ncnames=None, member=0
     nc.close()
 
 
+def interpolate_linear(x, xp, fp):
+    """interpolate_linear (routing/surface/reservoir.jl:363-375): the bounds are the columns'
+    extremes, between them the last row at or below x and the next."""
+    if x <= min(xp):
+        return min(fp)
+    if x >= max(xp):
+        return max(fp)
+    i1 = max(i for i in range(len(xp)) if xp[i] <= x)
+    i2 = i1 + 1
+    return fp[i1] * (1.0 - (x - xp[i1]) / (xp[i2] - xp[i1])) + fp[i2] * (x - xp[i1]) / (xp[i2] - xp[i1])
+
+
+def reservoir_storage(reservoirs, waterlevel):
+    """initialize_storage (reservoir.jl:343-360) of every reservoir at `waterlevel` ([members,
+    reservoirs]): A H for the linear profile, the S-H table interpolated at H otherwise."""
+    wl = np.asarray(waterlevel, float)
+    out = reservoirs["area"] * wl
+    prof = reservoirs.get("storage_curve_type")
+    if prof is not None:
+        for k in np.flatnonzero(np.asarray(prof) == 2):
+            a, b = reservoirs["sh_offset"][k], reservoirs["sh_offset"][k + 1]
+            h = [float(v) for v in reservoirs["sh_h"][a:b]]
+            sv = [float(v) for v in reservoirs["sh_s"][a:b]]
+            for m in range(wl.shape[0]):
+                out[m, k] = interpolate_linear(float(wl[m, k]), h, sv)
+    return out
+
+
 def read_states(model, dom, path, grid=None, names=None, ncnames=None, reservoirs=None, time_index=0):
     """Set a model's states from a Wflow state file (every member gets the file's states) and
     derive what set_states! derives from them (sbm_model.jl:120-190): q and h zero on land cells
@@ -216,5 +244,6 @@ def read_states(model, dom, path, grid=None, names=None, ncnames=None, reservoir
             ust = ust + acc.get("UNSATURATED_LAYER_DEPTH", layer=k)
         acc.set("TOTAL_SOIL_WATER_STORAGE", sat + ust)
     if reservoirs is not None and "reservoir_water_surface__elevation" in got:
+        # the storage is re-initialised from the water level (sbm_model.jl:181-190)
         wl = acc.get("RESERVOIR_WATERLEVEL").reshape(M, -1)
-        acc.set("RESERVOIR_STORAGE", (reservoirs["area"] * wl).reshape(-1))
+        acc.set("RESERVOIR_STORAGE", reservoir_storage(reservoirs, wl).reshape(-1))
