@@ -3,16 +3,19 @@
 // GB300 runs FP32 at about 64 times its FP64 rate, so this form evaluates every rate that
 // needs a transcendental (Brooks-Corey powers, exponential Kv profile, Feddes heads, s-curves,
 // the Gash log, soil-column drainage iterations) in FP32 with CUDA's accurate expf/logf, reads
-// parameters and forcing as FP32, and keeps in FP64 only:
-//   * every storage state (canopy, snow, unsaturated layers, saturated store / water table,
-//     subsurface, overland and river discharge and storage) and every update applied to it,
-//     so the water balance stays closed to FP64 rounding;
+// parameters and forcing as FP32, and keeps at higher precision:
+//   * every storage state (canopy, snow, unsaturated layers, subsurface, overland and river
+//     discharge and storage) and every update applied to it as a double-FP32 pair (wf_ff.cuh,
+//     a 48-bit significand), and the large stores that a step changes by as little as 1e-15 of
+//     their size (saturated depth, water-table depths, total soil water, the land balance's
+//     previous storage) in FP64, so the water balance stays closed;
 //   * the flux partitions and sums that enter the balance (throughfall/stemflow/canopy,
-//     rain/snow, infiltration and excess water, actual evapotranspiration, runoff);
-//   * the kinematic-wave Newton-Raphson solves for discharge (surface_process.jl:24-70,
-//     subsurface_process.jl:57-78), with FP32 only for the initial guess, the q^0.2 seed
-//     (refined by one FP64 Newton step) and the reciprocal of the Newton derivative;
-//   * the cumulative sub-step fluxes and the balance terms.
+//     rain/snow, infiltration and excess water, actual evapotranspiration, runoff) as pairs;
+//   * the kinematic-wave solves for discharge (surface_process.jl:24-70,
+//     subsurface_process.jl:57-78): Newton iterations in FP32 from an FP32 initial guess, then
+//     one Newton correction evaluated in double-FP32 (kw_node_ff), so the discharge carries the
+//     pair's precision although the iterations are FP32;
+//   * the cumulative sub-step fluxes and the balance terms as pairs; reservoirs in FP64.
 // The process structure, limiters and branch order are those of the FP64 form (see
 // kernels_fp64.cu for the reference line citations of each function).
 #include <cuda_runtime.h>
