@@ -11,10 +11,11 @@
 //     previous storage) in FP64, so the water balance stays closed;
 //   * the flux partitions and sums that enter the balance (throughfall/stemflow/canopy,
 //     rain/snow, infiltration and excess water, actual evapotranspiration, runoff) as pairs;
-//   * the kinematic-wave solves for discharge (surface_process.jl:24-70,
-//     subsurface_process.jl:57-78): Newton iterations in FP32 from an FP32 initial guess, then
-//     one Newton correction evaluated in double-FP32 (kw_node_ff), so the discharge carries the
-//     pair's precision although the iterations are FP32;
+//   * the kinematic-wave solves for discharge: overland and river (surface_process.jl:24-70)
+//     iterate Newton in FP32 from an FP32 initial guess and finish with one Newton correction
+//     evaluated in double-FP32 (kw_node_ff), so the discharge carries the pair's precision
+//     although the iterations are FP32; the subsurface solve (subsurface_process.jl:57-78) runs
+//     in FP64 (kw_ssf_newton_s);
 //   * the cumulative sub-step fluxes and the balance terms as pairs; reservoirs in FP64.
 // The process structure, limiters and branch order are those of the FP64 form (see
 // kernels_fp64.cu for the reference line citations of each function).
