@@ -8,8 +8,9 @@
 // the upstream discharges and the solve.
 //
 // A warp owns one chunk (G chains x M members, or one chain x 32 members) taken from a global
-// ticket counter (a bounded number of the longest chains first, then the others in chain-length
-// order; wave_grid in wf_launch.cuh) and walks it leaf -> chain end. Each node is advanced
+// ticket counter (a bounded number of the longest chains first, then the others in the plan's
+// dependency order, chain length for plans without heavy-child hints; wave_grid in
+// wf_launch.cuh) and walks it leaf -> chain end. Two sweeps can share one launch (walk_pair). Each node is advanced
 // through all sub-steps of the launch before the walker moves downstream (node-major order):
 // the node's own state stays in registers across sub-steps and the heavy child's discharge
 // of every sub-step is handed over in a per-thread shared-memory row. Chain ends publish the
