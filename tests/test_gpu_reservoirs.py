@@ -182,7 +182,7 @@ def test_linked_reservoirs_fp64_hourly_ensemble(gpu_lib):
     assert reservoir_closure(gpu) <= 1e-9
 
 
-def split_res_errors(dom, res, cfg, steps, precip_scale=3.0):
+def split_res_errors(dom, res, cfg, steps, precip_scale=3.0, models=None):
     import copy
     cfg64 = copy.copy(cfg)
     cfg64.form = abi.WF_FORM_FP64
@@ -207,6 +207,8 @@ def split_res_errors(dom, res, cfg, steps, precip_scale=3.0):
         w["outflow"] = max(w["outflow"], float(np.max(np.abs(og - oo)) / max(float(np.max(np.abs(oo))), 1e-12)))
         w["closure"] = max(w["closure"], float(np.abs(gpu.get_value("BALANCE_LAND_RELATIVE_ERROR")).max()))
         w["res_closure"] = max(w["res_closure"], reservoir_closure(gpu))
+    if models is not None:
+        models.extend([gpu, orc])
     return w
 
 
@@ -235,9 +237,19 @@ def test_linked_reservoirs_split_accuracy(gpu_lib):
     dom = synthetic.make_domain(48, 1000.0, seed=12)
     res = synthetic.make_linked_reservoirs(dom, seed=3)
     cfg = synthetic.make_config(86400.0, form=abi.WF_FORM_SPLIT)
-    w = split_res_errors(dom, res, cfg, 12)
+    models = []
+    w = split_res_errors(dom, res, cfg, 12, models=models)
     print("split linked reservoirs with tables, errors", w)
     assert w["outlet_q"] <= 1e-4, w
     assert w["storage"] <= 1e-5, w
     assert w["outflow"] <= 1e-4, w
     assert w["res_closure"] <= 1e-9, w
+    # the river cells below the reservoirs receive each reservoir's own outflow: the water the
+    # upper reservoir draws back from the lower one leaves the lower reservoir but does not flow
+    # down the river (reservoir.jl:482-521, surface_kinwave.jl:441-489)
+    gpu, orc = models
+    below = dom.river["river_downstream"][res["river_index"]]
+    qo = orc.get(F["RIVER_QIN_AVERAGE"])[below]
+    qg = gpu.get_value("RIVER_QIN_AVERAGE")[below]
+    scale = max(float(np.max(np.abs(qo))), 1e-12)
+    assert float(np.max(np.abs(qg - qo))) <= 1e-4 * scale, (qg, qo)

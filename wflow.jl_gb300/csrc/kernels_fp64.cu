@@ -1327,6 +1327,7 @@ __global__ void __launch_bounds__(256) reservoir_prep_kernel(WfDevFields F) {
         RS[RS_IN_SSF][e] = land_member_d(F, SSF_Q_AVG, le);
         RS[RS_IN_CUM][e] = 0.0;
         RS[RS_OUT_CUM][e] = 0.0;
+        RS[RS_DOWN_CUM][e] = 0.0;
         RS[RS_EVAP_CUM][e] = 0.0;
         RS[RS_ABS_CUM][e] = 0.0;
     }

@@ -2251,7 +2251,7 @@ __global__ void __launch_bounds__(256) rv_post_kernel(WfDevFields F, WfDevGraph 
             const int64_t ue = us * M + m;
             const int32_t ru = F.n_res > 0 ? F.res_of_rslot[us] : -1;
             // a reservoir cell contributes its reservoir's outflow (sum of outflow x sub-step)
-            qin = wff::add(qin, ru >= 0 ? wff::from_d(F.RS[RS_OUT_CUM][(int64_t)ru * M + m])
+            qin = wff::add(qin, ru >= 0 ? wff::from_d(F.RS[RS_DOWN_CUM][(int64_t)ru * M + m])
                                         : ff{RMh[RV_QSUMH][ue], RMh[RV_QSUML][ue]});
         }
         str(F, RV_Q_AVG, e, wff::mul(ff{RMh[RV_QSUMH][e], RMh[RV_QSUML][e]}, inv_dt));

@@ -48,7 +48,7 @@
 #define WF_RS_FIELDS(X)                                                                            \
     X(RS_STORAGE) X(RS_WATERLEVEL) X(RS_OUTFLOW) X(RS_OUT_AVG) X(RS_IN_AVG) X(RS_EVAP_AVG)          \
     X(RS_ABS_AVG) X(RS_IN_OL) X(RS_IN_SSF) X(RS_PRECIP) X(RS_EVAP) X(RS_EXT) X(RS_OBS) X(RS_ERR)     \
-    X(RS_REL) X(RS_OUT_CUM) X(RS_IN_CUM) X(RS_EVAP_CUM) X(RS_ABS_CUM) X(RS_PREV)
+    X(RS_REL) X(RS_OUT_CUM) X(RS_IN_CUM) X(RS_EVAP_CUM) X(RS_ABS_CUM) X(RS_PREV) X(RS_DOWN_CUM)
 
 // Reservoir parameters, per reservoir.
 #define WF_RP_FIELDS(X)                                                                            \

@@ -167,6 +167,9 @@ __device__ inline double reservoir_node(const WfDevFields& F, int32_t r, int m, 
     RS[RS_OUTFLOW][e] = outflow;
     RS[RS_IN_CUM][e] += net * dt;
     RS[RS_OUT_CUM][e] += outflow * dt;
+    // what went to the downstream river cell: the reservoir's own outflows only (RS_OUT_CUM of a
+    // linked lower reservoir also counts the water its upper reservoir drew back)
+    RS[RS_DOWN_CUM][e] += outflow * dt;
     RS[RS_EVAP_CUM][e] += evaporation / area * dt;
     return outflow;
 }
